@@ -1,0 +1,339 @@
+/*
+ * kgr.h -- C ABI of the GB300-native ray-tracing hot path for Kobra.
+ *
+ * This header is the drop-in boundary.  It replaces, for the path-tracer and
+ * ReSTIR attachments, the C++ surface of the reference's Armada plugin layer:
+ *
+ *   class AttachmentRTX          include/amadeus/armada.cuh:107-139
+ *   struct ArmadaLaunchInfo      include/amadeus/armada.cuh:43-83
+ *   extern "C" load_attachment   source/amadeus/naive_path_tracer.cu:280-348
+ *   Accelerator GAS/IAS build    include/amadeus/accelerator.cuh:46-277
+ *   software BVH build/layout    source/bvh.cpp:102-260
+ *   GLSL trace()/any-hit         shaders/rt/modules/bvh.glsl:52-127,
+ *                                source/optix/amadeus_common.cuh:190-212
+ *
+ * Conventions.  Every function returns a kgr_status and never throws across
+ * the ABI (the reference throws from CUDA_CHECK/OPTIX_CHECK,
+ * include/cuda/error.cuh:40-123).  The message of the last failure on the
+ * calling thread is returned by kgr_last_error().  Pointers documented as
+ * "device" are CUDA device pointers on the device the object was created on;
+ * streams are cudaStream_t passed as void* (NULL = the legacy default stream,
+ * which is what the reference launches on).  No function allocates on the
+ * caller's behalf except the *_create functions, which own what they
+ * allocate until the matching *_destroy.
+ */
+#ifndef KGR_H_
+#define KGR_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KGR_ABI_VERSION 1
+
+typedef enum kgr_status {
+	KGR_OK = 0,
+	KGR_ERR_INVALID_ARGUMENT = 1,
+	KGR_ERR_OUT_OF_MEMORY = 2,
+	KGR_ERR_CUDA = 3,
+	KGR_ERR_UNSUPPORTED = 4,
+	KGR_ERR_NOT_ATTACHED = 5,
+	KGR_ERR_NOT_LOADED = 6,
+	KGR_ERR_BVH_FORMAT = 7,
+	KGR_ERR_BUDGET = 8,
+	KGR_ERR_TIMEOUT = 9,
+	KGR_ERR_UNKNOWN_OPTION = 10,
+	KGR_ERR_TYPE = 11,
+	KGR_ERR_INTERNAL = 12,
+	KGR_ERR_NO_DEVICE = 13
+} kgr_status;
+
+/* Human-readable name of a status, and the last error message on this thread. */
+const char *kgr_status_string(kgr_status status);
+const char *kgr_last_error(void);
+int kgr_abi_version(void);
+
+/* ------------------------------------------------------------------ data -- */
+
+/* Shading flags, same values as the reference's `enum Shading`
+ * (include/types.hpp:17-25). */
+enum {
+	KGR_SHADING_NONE = 0,
+	KGR_SHADING_REFLECTION = 1 << 0,
+	KGR_SHADING_TRANSMISSION = 1 << 1,
+	KGR_SHADING_DIFFUSE = 1 << 2,
+	KGR_SHADING_GLOSSY = 1 << 3,
+	KGR_SHADING_SPECULAR = 1 << 4,
+	KGR_SHADING_EMISSIVE = 1 << 5
+};
+
+/* Material, field for field the reference's cuda::Material
+ * (include/cuda/material.cuh:13-23) without the unused light_index; the
+ * texture slots of cuda::_material (:26-49) are not supported. 64 bytes. */
+typedef struct kgr_material {
+	float diffuse[3];
+	float specular[3];
+	float emission[3];
+	float ambient[3];
+	float shininess;
+	float roughness;
+	float refraction;
+	int32_t type;
+} kgr_material;
+
+/* Triangle area light {a, ab, ac, intensity}: optix::TriangleLight
+ * (include/optix/lighting.cuh:96-120).  48 bytes. */
+typedef struct kgr_triangle_light {
+	float a[3];
+	float ab[3];
+	float ac[3];
+	float intensity[3];
+} kgr_triangle_light;
+
+/* One mesh of a scene.  Positions and normals are xyz triples; normals may be
+ * NULL (the face normal is used).  `model` is an optional column-major 4x4
+ * world transform (glm layout, the Hit::model of include/optix/sbt.cuh:14-21);
+ * NULL means identity.  Triangles index this mesh's vertices. */
+typedef struct kgr_mesh {
+	const float *positions;
+	const float *normals;
+	uint32_t vertex_count;
+	const uint32_t *indices;
+	const uint32_t *material_indices; /* one per triangle, or NULL = 0 */
+	uint32_t triangle_count;
+	const float *model;
+} kgr_mesh;
+
+/* BVH builders. */
+enum {
+	/* binned SAH (32 bins) with leaves of at most max_leaf_size triangles,
+	 * written as chains of one-triangle leaf records in the bvh.cpp layout */
+	KGR_BUILDER_SAH = 0,
+	/* the reference builder: partition() of source/bvh.cpp:102-210 (SAH over
+	 * 10 bins of the largest primitive's extent, one triangle per leaf) */
+	KGR_BUILDER_KOBRA = 1
+};
+
+typedef struct kgr_scene_options {
+	int32_t builder;       /* KGR_BUILDER_* */
+	int32_t max_leaf_size; /* SAH builder only, 1..8; 0 = 4 */
+	int32_t device;        /* CUDA ordinal; -1 = current device */
+	int32_t reserved;
+} kgr_scene_options;
+
+typedef struct kgr_scene kgr_scene;
+
+typedef struct kgr_scene_info {
+	uint32_t vertex_count;
+	uint32_t triangle_count;
+	uint32_t light_count;
+	uint32_t material_count;
+	uint32_t bvh_vec4_count;  /* threaded bvh.cpp layout, 3 vec4 per node */
+	uint32_t fast_node_count; /* 64-byte child-pair nodes */
+	uint64_t device_bytes;
+	double build_ms;
+	float bounds_min[3];
+	float bounds_max[3];
+} kgr_scene_info;
+
+/* Build the BVH on the host and upload the scene to the device.  Emissive
+ * triangles (any emission component > 0) become triangle lights in triangle
+ * order, as ArmadaRTX::update_triangle_light_buffers does
+ * (source/amadeus/armada.cu:98-212).  Triangle i of the concatenated mesh
+ * list has primitive id i. */
+kgr_status kgr_scene_create(const kgr_mesh *meshes, uint32_t mesh_count,
+		const kgr_material *materials, uint32_t material_count,
+		const kgr_scene_options *options, kgr_scene **out);
+
+/* Same, but with a caller-serialised BVH in the bvh.cpp layout
+ * (source/bvh.cpp:213-260: 3 vec4 per node, header {leaf ? 1.0f : 0.0f,
+ * bits(object), bits(hit), bits(miss)}, then bbox min, then bbox max; links
+ * count vec4 units).  Leaf objects are primitive ids of the concatenated
+ * triangle list.  Both layouts on the device are derived from it. */
+kgr_status kgr_scene_create_from_bvh(const kgr_mesh *meshes, uint32_t mesh_count,
+		const kgr_material *materials, uint32_t material_count,
+		const float *bvh_vec4, uint32_t bvh_vec4_count,
+		int32_t device, kgr_scene **out);
+
+kgr_status kgr_scene_info_get(const kgr_scene *scene, kgr_scene_info *info);
+
+/* Host copy of the threaded bvh.cpp-layout buffer (capacity in vec4 units). */
+kgr_status kgr_scene_copy_bvh(const kgr_scene *scene, float *out_vec4,
+		uint32_t capacity, uint32_t *count);
+
+/* Host copy of the triangle lights. */
+kgr_status kgr_scene_copy_lights(const kgr_scene *scene, kgr_triangle_light *out,
+		uint32_t capacity, uint32_t *count);
+
+kgr_status kgr_scene_destroy(kgr_scene *scene);
+
+/* ------------------------------------------------------------- traversal -- */
+
+/* Hit record: primitive id (-1 = miss), distance and the barycentrics
+ * (b1, b2) of the Moller-Trumbore test of include/optix/lighting.cuh:34-55. */
+typedef struct kgr_hit {
+	int32_t prim;
+	float t;
+	float b1;
+	float b2;
+} kgr_hit;
+
+/* Which device layout a traversal walks. */
+enum {
+	/* child-pair BVH2 with ordered descent and a short stack (default) */
+	KGR_LAYOUT_FAST = 0,
+	/* the threaded bvh.cpp layout, walked exactly as bvh.glsl:52-99 does */
+	KGR_LAYOUT_THREADED = 1
+};
+
+/* Closest hit for n rays.  `rays` (device) holds 8 floats per ray:
+ * {ox, oy, oz, unused, dx, dy, dz, tmax}; a primitive is accepted when
+ * 0 < t < best with best starting at tmax (pass INFINITY for the GLSL
+ * trace(), 1e16 for the OptiX launches of amadeus_common.cuh:467-478).
+ * Equal distances resolve to the primitive the threaded walk meets first.
+ * `hits` (device) receives n records.  Asynchronous on `stream`. */
+kgr_status kgr_trace_closest(const kgr_scene *scene, const float *rays,
+		uint32_t n, kgr_hit *hits, int32_t layout, void *stream);
+
+/* Any hit: occluded[i] = 1 if some primitive has 0 < t < tmax, else 0
+ * (is_occluded, source/optix/amadeus_common.cuh:190-212). */
+kgr_status kgr_trace_any(const kgr_scene *scene, const float *rays,
+		uint32_t n, uint32_t *occluded, int32_t layout, void *stream);
+
+/* Same two calls on HOST buffers: the rays are copied in, the results out,
+ * synchronously.  For callers that hold no device memory. */
+kgr_status kgr_trace_closest_host(const kgr_scene *scene, const float *rays,
+		uint32_t n, kgr_hit *hits, int32_t layout);
+kgr_status kgr_trace_any_host(const kgr_scene *scene, const float *rays,
+		uint32_t n, uint32_t *occluded, int32_t layout);
+
+/* ----------------------------------------------------------- attachments -- */
+
+typedef struct kgr_attachment kgr_attachment;
+
+/* Option values: std::variant<int, float, bool, std::string> of
+ * AttachmentRTX::OptionValue (armada.cuh:120). */
+enum { KGR_VALUE_NONE = 0, KGR_VALUE_INT = 1, KGR_VALUE_FLOAT = 2, KGR_VALUE_BOOL = 3, KGR_VALUE_STRING = 4 };
+
+typedef struct kgr_value {
+	int32_t tag;
+	int32_t i;
+	float f;
+	int32_t b;
+	const char *s; /* borrowed for set_option; owned by the attachment for get_option */
+} kgr_value;
+
+/* What attach() learns from ArmadaRTX: extent() and the device. */
+typedef struct kgr_context {
+	uint32_t width;
+	uint32_t height;
+	int32_t device;
+	int32_t reserved;
+} kgr_context;
+
+/* ArmadaLaunchInfo (armada.cuh:43-83) with POD types: glm::vec2/vec3 become
+ * float[2]/float[3], glm::mat4 becomes float[16] column-major.  Buffers are
+ * device float4 arrays of width * height owned by the caller. */
+typedef struct kgr_launch_info {
+	float resolution[2];
+	struct {
+		float center[3];
+		float ax_u[3];
+		float ax_v[3];
+		float ax_w[3];
+		float projection[16];
+		float view[16];
+	} camera;
+	struct {
+		const kgr_triangle_light *tri_lights; /* device; NULL = the scene's */
+		int32_t tri_count;
+		int32_t quad_count; /* quad lights are not supported: must be 0 */
+	} lights;
+	struct {
+		float *color;
+		float *normal;
+		float *albedo;
+		float *position;
+	} buffers;
+	const kgr_material *materials; /* device; NULL = the scene's */
+	int32_t has_environment_map;   /* must be 0 */
+	int32_t accumulate;
+	float time;
+	int32_t max_depth;
+	int32_t samples;
+	uint32_t frame; /* RNG stream index of this frame */
+} kgr_launch_info;
+
+/* kind: "path_tracer", "restir_di" or "restir_gi". */
+kgr_status kgr_create(const char *kind, kgr_attachment **out);
+kgr_status kgr_attach(kgr_attachment *att, const kgr_context *ctx);
+kgr_status kgr_load(kgr_attachment *att);
+kgr_status kgr_unload(kgr_attachment *att);
+kgr_status kgr_set_option(kgr_attachment *att, const char *name, const kgr_value *value);
+kgr_status kgr_get_option(const kgr_attachment *att, const char *name, kgr_value *value);
+kgr_status kgr_render(kgr_attachment *att, const kgr_launch_info *info,
+		const kgr_scene *scene, void *stream);
+kgr_status kgr_destroy(kgr_attachment *att);
+
+/* Counters of the last render: rays traced by kind and kernel launches. */
+typedef struct kgr_render_stats {
+	uint64_t camera_rays;
+	uint64_t bounce_rays;
+	uint64_t shadow_rays;
+	uint32_t kernel_launches;
+	uint32_t reserved;
+} kgr_render_stats;
+kgr_status kgr_get_render_stats(const kgr_attachment *att, kgr_render_stats *stats);
+
+/* The .rtxa plugin export (source/amadeus/naive_path_tracer.cu:280-348),
+ * returning a C handle instead of an AttachmentRTX*.  NULL name and ptr on
+ * failure, as the reference does. */
+typedef struct kgr_plugin_ret {
+	const char *name;
+	kgr_attachment *ptr;
+} kgr_plugin_ret;
+kgr_plugin_ret kgr_load_attachment(const char *kind);
+
+/* ------------------------------------------------------ procedural scenes -- */
+
+/* Seeded procedural scenes used by the tests and the benchmark.  The
+ * generator uses integer hashing and IEEE + - * / sqrt only, so a given
+ * (name, seed) gives the same bits on every host.
+ *   "box4k"    box [-2,2]^3 (12 tris) + 4096 random tris + 64 ceiling quads
+ *   "terrain"  512x512 value-noise height field + 2000 icospheres (320 tris)
+ *              + 512 emissive quads (1024 tris)
+ *   "terrain_s","terrain_m","terrain_l": 0.25M / 1M / 4M triangle variants
+ *   "tiny"     a few triangles, for unit tests                               */
+typedef struct kgr_generated kgr_generated;
+
+typedef struct kgr_generated_view {
+	const float *positions;   /* 3 * vertex_count */
+	const float *normals;     /* 3 * vertex_count */
+	uint32_t vertex_count;
+	const uint32_t *indices;  /* 3 * triangle_count */
+	const uint32_t *material_indices;
+	uint32_t triangle_count;
+	const kgr_material *materials;
+	uint32_t material_count;
+	float camera_eye[3];
+	float camera_target[3];
+	float camera_fov_deg;
+} kgr_generated_view;
+
+kgr_status kgr_generate_scene(const char *name, uint64_t seed, kgr_generated **out);
+kgr_status kgr_generated_get(const kgr_generated *g, kgr_generated_view *view);
+kgr_status kgr_generated_destroy(kgr_generated *g);
+
+/* Camera helper: uvw_frame of include/camera.hpp:45-63 plus the glm
+ * perspective/lookAt matrices of camera.hpp:20-34 (near 0.1, far 1000). */
+kgr_status kgr_camera_setup(const float eye[3], const float target[3], const float up[3],
+		float fov_deg, float aspect, kgr_launch_info *info);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,1473 @@
+/*
+ * oracle.cpp -- CPU restatement of the reference's ray-tracing hot path.
+ *
+ * TEST INFRASTRUCTURE: the checker the CUDA kernels are compared against.
+ * Nothing in the product links or calls this file.  Built by oracle/Makefile
+ * with g++ -O2 -ffp-contract=off -fopenmp into oracle/liboracle.so.
+ *
+ * Floating-point expressions keep the reference's evaluation order; the
+ * vector helpers and the transcendentals come from kgr_math.h, whose
+ * definitions follow include/cuda/math.cuh and are identical on CPU and GPU.
+ */
+#include "oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <memory>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../artemis_gb300/csrc/kgr_math.h"
+
+using namespace kgr;
+
+namespace {
+
+/* ============================================================ BVH build == */
+
+/* BoundingBox (include/bbox.hpp:9-30) */
+struct Box {
+	f3 min, max;
+	float surface_area() const
+	{
+		float dx = max.x - min.x;
+		float dy = max.y - min.y;
+		float dz = max.z - min.z;
+		float xy = dx * dy;
+		float yz = dy * dz;
+		float xz = dx * dz;
+		return 2.0f * (xy + yz + xz);
+	}
+};
+
+/* glm::min / glm::max: (y < x) ? y : x, componentwise */
+inline f3 gmin(const f3 &a, const f3 &b)
+{
+	return mk(b.x < a.x ? b.x : a.x, b.y < a.y ? b.y : a.y, b.z < a.z ? b.z : a.z);
+}
+inline f3 gmax(const f3 &a, const f3 &b)
+{
+	return mk(a.x < b.x ? b.x : a.x, a.y < b.y ? b.y : a.y, a.z < b.z ? b.z : a.z);
+}
+
+/* BVHNode (include/bvh.hpp:24-38), index-based instead of shared_ptr */
+struct Node {
+	Box bbox;
+	int object = -1;
+	int left = -1, right = -1;
+};
+
+struct Builder {
+	std::vector<Node> nodes;
+
+	/* union_of (source/bvh.cpp:32-43) */
+	Box union_of(const std::vector<int> &ids) const
+	{
+		f3 mn = nodes[ids[0]].bbox.min, mx = nodes[ids[0]].bbox.max;
+		for (size_t i = 1; i < ids.size(); i++) {
+			mn = gmin(mn, nodes[ids[i]].bbox.min);
+			mx = gmax(mx, nodes[ids[i]].bbox.max);
+		}
+		return Box{mn, mx};
+	}
+
+	/* sah_cost (source/bvh.cpp:46-98) */
+	float sah_cost(const std::vector<int> &ids, int axis, float split) const
+	{
+		f3 min_left = mk(FLT_MAX), max_left = mk(-FLT_MAX);
+		f3 min_right = mk(FLT_MAX), max_right = mk(-FLT_MAX);
+		f3 tmin = nodes[ids[0]].bbox.min, tmax = nodes[ids[0]].bbox.max;
+		int prims_left = 0, prims_right = 0;
+		for (int id : ids) {
+			f3 mn = nodes[id].bbox.min, mx = nodes[id].bbox.max;
+			tmin = gmin(tmin, mn);
+			tmax = gmax(tmax, mx);
+			float value = (comp(mn, axis) + comp(mx, axis)) / 2.0f;
+			if (value < split) {
+				prims_left++;
+				min_left = gmin(min_left, mn);
+				max_left = gmax(max_left, mx);
+			} else {
+				prims_right++;
+				min_right = gmin(min_right, mn);
+				max_right = gmax(max_right, mx);
+			}
+		}
+		if (prims_left == 0 || prims_right == 0)
+			return FLT_MAX;
+		float sa_left = Box{min_left, max_left}.surface_area();
+		float sa_right = Box{min_right, max_right}.surface_area();
+		float sa_total = Box{tmin, tmax}.surface_area();
+		return 1 + (prims_left * sa_left + prims_right * sa_right) / sa_total;
+	}
+
+	/* partition (source/bvh.cpp:102-195) */
+	int partition(const std::vector<int> &ids)
+	{
+		if (ids.size() == 0)
+			return -1;
+		if (ids.size() == 1)
+			return ids[0];
+		if (ids.size() == 2) {
+			Node node;
+			node.bbox = union_of(ids);
+			node.left = ids[0];
+			node.right = ids[1];
+			nodes.push_back(node);
+			return (int)nodes.size() - 1;
+		}
+
+		int axis = 0;
+		float max_extent = 0.0f;
+		float min_value = FLT_MAX;
+		float max_value = -FLT_MAX;
+		for (size_t n = 0; n < ids.size(); n++) {
+			for (int i = 0; i < 3; i++) {
+				f3 mn = nodes[ids[n]].bbox.min, mx = nodes[ids[n]].bbox.max;
+				float extent = fabsf(comp(mx, i) - comp(mn, i));
+				if (extent > max_extent) {
+					max_extent = extent;
+					min_value = comp(mn, i);
+					max_value = comp(mx, i);
+					axis = i;
+				}
+			}
+		}
+
+		float min_cost = FLT_MAX;
+		float min_split = 0.0f;
+		int bins = 10;
+		for (int i = 0; i < bins; i++) {
+			float split = (max_value - min_value) / bins * i + min_value;
+			float cost = sah_cost(ids, axis, split);
+			if (cost < min_cost) {
+				min_cost = cost;
+				min_split = split;
+			}
+		}
+
+		std::vector<int> left, right;
+		if (min_cost == FLT_MAX) {
+			for (size_t i = 0; i < ids.size(); i++) {
+				if (i % 2 == 0)
+					left.push_back(ids[i]);
+				else
+					right.push_back(ids[i]);
+			}
+		} else {
+			for (int id : ids) {
+				f3 mn = nodes[id].bbox.min, mx = nodes[id].bbox.max;
+				float value = (comp(mn, axis) + comp(mx, axis)) / 2.0f;
+				if (value < min_split)
+					left.push_back(id);
+				else
+					right.push_back(id);
+			}
+		}
+
+		Box bbox = union_of(ids);
+		int l = partition(left);
+		int r = partition(right);
+		Node node;
+		node.bbox = bbox;
+		node.left = l;
+		node.right = r;
+		nodes.push_back(node);
+		return (int)nodes.size() - 1;
+	}
+
+	/* BVHNode::node_count (source/bvh.cpp:18-22) */
+	size_t node_count(int i) const
+	{
+		if (i < 0)
+			return 0;
+		return 1 + node_count(nodes[i].left) + node_count(nodes[i].right);
+	}
+
+	/* serialize (source/bvh.cpp:213-260) */
+	void serialize(std::vector<float> &buf, int bvh, int miss) const
+	{
+		if (bvh < 0)
+			return;
+		int size = (int)(buf.size() / 4);
+		int after = size + 3;
+		int left = nodes[bvh].left, right = nodes[bvh].right;
+		int32_t left_index = left >= 0 ? after : -1;
+		int32_t left_size = left >= 0 ? 3 * (int32_t)node_count(left) : 0;
+		int32_t right_index = right >= 0 ? after + left_size : -1;
+		int32_t hit = left_index;
+		if (left < 0 && right < 0)
+			hit = miss;
+		int32_t miss_left = right_index;
+		if (right < 0)
+			miss_left = miss;
+		int32_t object = nodes[bvh].object;
+		float leaf = object != -1 ? 1.0f : 0.0f;
+		const Box &b = nodes[bvh].bbox;
+		float v[12] = {leaf, u2f((uint32_t)object), u2f((uint32_t)hit), u2f((uint32_t)miss),
+			b.min.x, b.min.y, b.min.z, 0.0f, b.max.x, b.max.y, b.max.z, 0.0f};
+		buf.insert(buf.end(), v, v + 12);
+		if (left >= 0)
+			serialize(buf, left, miss_left);
+		if (right >= 0)
+			serialize(buf, right, miss);
+	}
+};
+
+/* ========================================================== intersection == */
+
+inline f3 ld3(const float *p, uint32_t i) { return mk(p[3 * i + 0], p[3 * i + 1], p[3 * i + 2]); }
+
+/* intersects_triangle (include/optix/lighting.cuh:34-55) == _intersect_t
+ * (shaders/rt/modules/intersect.glsl:14-33).  1.0 / divisor is a double
+ * division rounded to float; for binary32 operands that equals the float
+ * division (double rounding of a quotient is innocuous at 53 >= 2*24+2). */
+inline float intersect_triangle(const f3 &v1, const f3 &v2, const f3 &v3,
+		const f3 &origin, const f3 &dir, float &b1, float &b2)
+{
+	f3 e1 = v2 - v1;
+	f3 e2 = v3 - v1;
+	f3 s1 = cross(dir, e2);
+	float divisor = dot(s1, e1);
+	if (divisor == 0.0f)
+		return -1;
+	f3 s = origin - v1;
+	float inv_divisor = (float)(1.0 / (double)divisor);
+	b1 = dot(s, s1) * inv_divisor;
+	if (b1 < 0.0f || b1 > 1.0f)
+		return -1;
+	f3 s2 = cross(s, e1);
+	b2 = dot(dir, s2) * inv_divisor;
+	if (b2 < 0.0f || b1 + b2 > 1.0f)
+		return -1;
+	return dot(e2, s2) * inv_divisor;
+}
+
+/* intersect_box (shaders/rt/modules/bbox.glsl:8-58) */
+inline float intersect_box(const f3 &o, const f3 &d, const f3 &pmin, const f3 &pmax)
+{
+	float tmin = (pmin.x - o.x) / d.x;
+	float tmax = (pmax.x - o.x) / d.x;
+	if (tmin > tmax) { float t = tmin; tmin = tmax; tmax = t; }
+	float tymin = (pmin.y - o.y) / d.y;
+	float tymax = (pmax.y - o.y) / d.y;
+	if (tymin > tymax) { float t = tymin; tymin = tymax; tymax = t; }
+	if ((tmin > tymax) || (tymin > tmax))
+		return -1.0f;
+	if (tymin > tmin)
+		tmin = tymin;
+	if (tymax < tmax)
+		tmax = tymax;
+	float tzmin = (pmin.z - o.z) / d.z;
+	float tzmax = (pmax.z - o.z) / d.z;
+	if (tzmin > tzmax) { float t = tzmin; tzmin = tzmax; tzmax = t; }
+	if ((tmin > tzmax) || (tzmin > tmax))
+		return -1.0f;
+	if (tzmin > tmin)
+		tmin = tzmin;
+	if (tzmax < tmax)
+		tmax = tzmax;
+	return tmin;
+}
+
+/* in_box (bbox.glsl:61-67) */
+inline bool in_box(const f3 &p, const f3 &pmin, const f3 &pmax)
+{
+	bool lt = p.x < pmin.x || p.y < pmin.y || p.z < pmin.z;
+	bool gt = p.x > pmax.x || p.y > pmax.y || p.z > pmax.z;
+	return !(lt || gt);
+}
+
+inline int32_t bits_i(float f) { return (int32_t)f2u(f); }
+
+struct Tri {
+	f3 a, b, c;
+};
+
+inline Tri load_tri(const oracle_scene *s, int prim)
+{
+	const uint32_t *t = s->tris + 4 * (size_t)prim;
+	return Tri{ld3(s->positions, t[0]), ld3(s->positions, t[1]), ld3(s->positions, t[2])};
+}
+
+/* trace (shaders/rt/modules/bvh.glsl:52-99): threaded walk, a primitive
+ * replaces the best hit when 0 < t < best; a box is entered when its entry
+ * distance is in (0, best) or the origin lies inside it. */
+kgr_hit trace_closest(const oracle_scene *s, const f3 &o, const f3 &d, float tmax,
+		uint64_t *internal, uint64_t *leaves)
+{
+	kgr_hit best = {-1, tmax, 0.0f, 0.0f};
+	const float *bvh = s->bvh;
+	int node = 0;
+	if (s->bvh_vec4_count == 0)
+		node = -1;
+	while (node != -1) {
+		const float *h = bvh + 4 * (size_t)node;
+		int object = bits_i(h[1]);
+		if (object != -1) {
+			(*leaves)++;
+			Tri tri = load_tri(s, object);
+			float b1 = 0, b2 = 0;
+			float t = intersect_triangle(tri.a, tri.b, tri.c, o, d, b1, b2);
+			if (t > 0.0f && t < best.t) {
+				best.prim = object;
+				best.t = t;
+				best.b1 = b1;
+				best.b2 = b2;
+			}
+			node = bits_i(h[3]);
+		} else {
+			(*internal)++;
+			f3 pmin = mk(h[4], h[5], h[6]), pmax = mk(h[8], h[9], h[10]);
+			float t = intersect_box(o, d, pmin, pmax);
+			bool inside = in_box(o, pmin, pmax);
+			if ((t > 0.0f && t < best.t) || inside)
+				node = bits_i(h[2]);
+			else
+				node = bits_i(h[3]);
+		}
+	}
+	if (best.prim < 0)
+		best.t = tmax;
+	return best;
+}
+
+/* Occlusion over (0, tmax): the walk of trace() with best = tmax that stops
+ * at the first accepted primitive (OPTIX_RAY_FLAG_TERMINATE_ON_FIRST_HIT in
+ * is_occluded, source/optix/amadeus_common.cuh:190-212). */
+bool trace_any(const oracle_scene *s, const f3 &o, const f3 &d, float tmax,
+		uint64_t *internal, uint64_t *leaves)
+{
+	const float *bvh = s->bvh;
+	int node = s->bvh_vec4_count ? 0 : -1;
+	while (node != -1) {
+		const float *h = bvh + 4 * (size_t)node;
+		int object = bits_i(h[1]);
+		if (object != -1) {
+			(*leaves)++;
+			Tri tri = load_tri(s, object);
+			float b1 = 0, b2 = 0;
+			float t = intersect_triangle(tri.a, tri.b, tri.c, o, d, b1, b2);
+			if (t > 0.0f && t < tmax)
+				return true;
+			node = bits_i(h[3]);
+		} else {
+			(*internal)++;
+			f3 pmin = mk(h[4], h[5], h[6]), pmax = mk(h[8], h[9], h[10]);
+			float t = intersect_box(o, d, pmin, pmax);
+			bool inside = in_box(o, pmin, pmax);
+			if ((t > 0.0f && t < tmax) || inside)
+				node = bits_i(h[2]);
+			else
+				node = bits_i(h[3]);
+		}
+	}
+	return false;
+}
+
+/* ================================================================ BSDF == */
+
+struct Material {
+	f3 diffuse, specular, emission, ambient;
+	float shininess, roughness, refraction;
+	int type;
+};
+
+inline Material load_material(const kgr_material &m)
+{
+	Material r;
+	r.diffuse = mk(m.diffuse[0], m.diffuse[1], m.diffuse[2]);
+	r.specular = mk(m.specular[0], m.specular[1], m.specular[2]);
+	r.emission = mk(m.emission[0], m.emission[1], m.emission[2]);
+	r.ambient = mk(m.ambient[0], m.ambient[1], m.ambient[2]);
+	r.shininess = m.shininess;
+	r.roughness = m.roughness;
+	r.refraction = m.refraction;
+	r.type = m.type;
+	return r;
+}
+
+/* SurfaceHit (include/cuda/brdf.cuh:67-74) */
+struct SurfaceHit {
+	Material mat;
+	bool entering;
+	f3 n, wo, x;
+};
+
+const float PI_F = 3.14159265358979323846f; /* brdf.cuh:64 */
+
+/* G1 (brdf.cuh:179-192) */
+float G1(f3 n, f3 v, const Material &mat)
+{
+	if (dot(v, n) <= 0.0f)
+		return 0.0f;
+	float alpha = mat.roughness;
+	float theta = kacos(clampf(dot(n, v), 0.0f, 0.999f));
+	float tan_theta = ktan(theta);
+	float denom = 1 + ksqrt(1 + alpha * alpha * tan_theta * tan_theta);
+	return 2.0f / denom;
+}
+
+/* G (brdf.cuh:195-199) */
+float G(f3 n, f3 wi, f3 wo, const Material &mat) { return G1(n, wo, mat) * G1(n, wi, mat); }
+
+/* shlick_F (brdf.cuh:202-207) */
+f3 shlick_F(f3 wi, f3 h, const Material &mat)
+{
+	float k = kpow5(1 - dot(wi, h));
+	return mat.specular + (1.0f - mat.specular) * k;
+}
+
+/* Microfacets::GGX (brdf.cuh:210-220) */
+float ggx_D(f3 n, f3 h, const Material &mat)
+{
+	float alpha = mat.roughness;
+	float theta = kacos(clampf(dot(n, h), 0.0f, 1.0f));
+	float c, sn;
+	ksincos(theta, sn, c);
+	float tn = sn / c;
+	return (alpha * alpha) / (PI_F * kpow4(c) * kpow2(alpha * alpha + tn * tn));
+}
+
+/* GGX::brdf (brdf.cuh:337-353) */
+f3 ggx_brdf(const Material &mat, f3 n, f3 wi, f3 wo)
+{
+	if (dot(wo, n) <= 0.0f)
+		n = -n;
+	f3 h = normalize(wi + wo);
+	f3 f = shlick_F(wi, h, mat);
+	float g = G(n, wi, wo, mat);
+	float d = ggx_D(n, h, mat);
+	f3 num = f * g * d;
+	float denom = 4 * dot(wi, n) * dot(wo, n);
+	return num / (denom + 1e-6f);
+}
+
+/* GGX::pdf (brdf.cuh:356-382) */
+float ggx_pdf(const Material &mat, f3 n, f3 wi, f3 wo)
+{
+	if (dot(wo, n) <= 0.0f)
+		n = -n;
+	if (dot(wi, n) <= 0.0f)
+		return 0.0f;
+	f3 h = normalize(wi + wo);
+	float avg_Kd = (mat.diffuse.x + mat.diffuse.y + mat.diffuse.z) / 3.0f;
+	float avg_Ks = (mat.specular.x + mat.specular.y + mat.specular.z) / 3.0f;
+	float t = 1.0f;
+	if (avg_Kd + avg_Ks > 0.0f)
+		t = kmax(avg_Ks / (avg_Kd + avg_Ks), 0.25f);
+	float term1 = dot(n, wi) / PI_F;
+	float term2 = ggx_D(n, h, mat) * dot(n, h) / (4.0f * dot(wi, h));
+	return (1 - t) * term1 + t * term2;
+}
+
+/* GGX::sample (brdf.cuh:385-433) */
+f3 ggx_sample(const Material &mat, f3 n, f3 wo, f3 &seed)
+{
+	if (dot(wo, n) <= 0.0f)
+		n = -n;
+	float avg_Kd = (mat.diffuse.x + mat.diffuse.y + mat.diffuse.z) / 3.0f;
+	float avg_Ks = (mat.specular.x + mat.specular.y + mat.specular.z) / 3.0f;
+	float t = 1.0f;
+	if (avg_Kd + avg_Ks > 0.0f)
+		t = avg_Ks / (avg_Kd + avg_Ks);
+	f3 eta = rand_uniform_3f(seed);
+	if (eta.x < t) {
+		float k = ksqrt(eta.y / (1 - eta.y));
+		float theta = katan(k * mat.roughness);
+		float phi = 2.0f * PI_F * eta.z;
+		float st, ct, sp, cp;
+		ksincos(theta, st, ct);
+		ksincos(phi, sp, cp);
+		f3 h = mk(st * cp, st * sp, ct);
+		h = rotate(h, n);
+		return reflect(-wo, h);
+	}
+	float theta = kacos(ksqrt(eta.y));
+	float phi = 2.0f * PI_F * eta.z;
+	float st, ct, sp, cp;
+	ksincos(theta, st, ct);
+	ksincos(phi, sp, cp);
+	f3 s = mk(st * cp, st * sp, ct);
+	return rotate(s, n);
+}
+
+/* brdf() (brdf.cuh:437-449) for out = eDiffuse, the only lobe the path uses */
+f3 brdf(const SurfaceHit &sh, f3 wi)
+{
+	return sh.mat.diffuse / PI_F + ggx_brdf(sh.mat, sh.n, wi, sh.wo);
+}
+
+/* Glass::sample (brdf.cuh:154-175) */
+f3 glass_refract(f3 v, f3 n, float ni_over_nt)
+{
+	float cos_theta = dot(-v, n);
+	f3 r_out_parallel = ni_over_nt * (v + cos_theta * n);
+	float r_out_length = length(r_out_parallel);
+	float r_out_length_squared = r_out_length * r_out_length;
+	f3 r_out_perp = -ksqrt(fabsf(1.0f - r_out_length_squared)) * n;
+	return r_out_parallel + r_out_perp;
+}
+
+/* eval() (brdf.cuh:573-589 -> eval<GGX> :477-492, Glass :576-583).  pdf is
+ * set to 0 when the sampled direction is degenerate (the reference leaves
+ * it unset there). */
+f3 eval(const SurfaceHit &sh, f3 &wi, float &pdf, f3 &seed)
+{
+	if (sh.mat.type & KGR_SHADING_TRANSMISSION) {
+		float eta = sh.mat.refraction;
+		float cos_theta = kmin(dot(-sh.wo, sh.n), 1.0f);
+		float sin_theta = ksqrt(1.0f - cos_theta * cos_theta);
+		bool reflect_ray = (eta * sin_theta > 1.0f);
+		float ni_over_nt = (float)(1.0 / (double)eta);
+		if (!sh.entering)
+			ni_over_nt = eta;
+		wi = reflect_ray ? reflect(sh.wo, sh.n) : glass_refract(sh.wo, sh.n, ni_over_nt);
+		pdf = 1.0f;
+		return sh.mat.specular;
+	}
+	wi = ggx_sample(sh.mat, sh.n, sh.wo, seed);
+	if (length(wi) < 1e-6f) {
+		pdf = 0.0f;
+		return mk(0.0f);
+	}
+	pdf = ggx_pdf(sh.mat, sh.n, wi, sh.wo);
+	return brdf(sh, wi);
+}
+
+/* ============================================================== lights == */
+
+struct TriLight {
+	f3 a, ab, ac, intensity;
+	/* TriangleLight::area (lighting.cuh:103-105): length * 0.5 in double */
+	float area() const { return (float)((double)length(cross(ab, ac)) * 0.5); }
+	f3 normal() const { return normalize(cross(ab, ac)); }
+};
+
+inline TriLight load_light(const kgr_triangle_light &l)
+{
+	return TriLight{mk(l.a[0], l.a[1], l.a[2]), mk(l.ab[0], l.ab[1], l.ab[2]),
+		mk(l.ac[0], l.ac[1], l.ac[2]), mk(l.intensity[0], l.intensity[1], l.intensity[2])};
+}
+
+/* sample_area_light(TriangleLight) (lighting.cuh:133-146) */
+f3 sample_area_light(const TriLight &light, f3 &seed)
+{
+	f3 r = pcg3f(seed);
+	float u = fract(r.x);
+	float v = fract(r.y);
+	if (u + v > 1.0f) {
+		u = 1.0f - u;
+		v = 1.0f - v;
+	}
+	return light.a + u * light.ab + v * light.ac;
+}
+
+const float SHADOW_EPS = 0.05f; /* is_occluded, amadeus_common.cuh:193 */
+const float OFFSET_EPS = 1e-3f; /* amadeus_common.cuh:22 */
+
+struct Ctx {
+	const oracle_scene *s;
+	std::vector<TriLight> lights;
+	oracle_render_stats stats;
+	uint64_t internal = 0, leaves = 0;
+	float tmax_closest = 1e16f;
+
+	bool occluded(const f3 &o, const f3 &d, float R)
+	{
+		stats.shadow_rays++;
+		return trace_any(s, o, d, R - SHADOW_EPS, &internal, &leaves);
+	}
+
+	/* Ld_light (lighting.cuh:149-174) + Ld (amadeus_common.cuh:256-286),
+	 * triangle lights only (no quads, no environment map). */
+	f3 Ld(const SurfaceHit &sh, f3 &seed)
+	{
+		int total_count = (int)lights.size();
+		if (total_count == 0)
+			return mk(0.0f);
+		unsigned int i = (unsigned int)(rand_uniform(seed) * total_count);
+		f3 contr = mk(0.0f);
+		float pdf = 1.0f / total_count;
+		float light_pdf = 0.0f;
+		if (i < (unsigned int)total_count) {
+			const TriLight &light = lights[i];
+			light_pdf = 1.0f / light.area();
+			f3 lpos = sample_area_light(light, seed);
+			f3 wi = normalize(lpos - sh.x);
+			float R = length(lpos - sh.x);
+			if (!occluded(sh.x, wi, R)) {
+				f3 f = brdf(sh, wi);
+				float ldot = fabsf(dot(light.normal(), wi));
+				float geometric = ldot * fabsf(dot(sh.n, wi)) / (R * R);
+				contr = f * light.intensity * geometric;
+			}
+		}
+		pdf *= light_pdf;
+		return contr / pdf;
+	}
+
+	/* sample_direct (amadeus_common.cuh:301-377), triangle branch */
+	void sample_direct(const SurfaceHit &sh, f3 &seed, int &index, f3 &point, float &pdf)
+	{
+		(void)sh;
+		unsigned int total_lights = (unsigned int)lights.size();
+		unsigned int light_index = (unsigned int)(rand_uniform(seed) * total_lights);
+		if (light_index < total_lights) {
+			const TriLight &light = lights[light_index];
+			point = sample_area_light(light, seed);
+			pdf = 1.0f / (light.area() * total_lights);
+			index = (int)light_index;
+		} else {
+			index = -1;
+			point = mk(0.0f);
+			pdf = 0.0f;
+		}
+	}
+
+	/* direct_unoccluded (amadeus_common.cuh:380-397) */
+	f3 direct_unoccluded(const SurfaceHit &sh, const f3 &Le, const f3 &normal, f3 D, float d)
+	{
+		f3 rho = brdf(sh, D);
+		float geometric = fabsf(dot(sh.n, D));
+		float ldot = fabsf(dot(normal, D));
+		geometric *= ldot / (d * d);
+		return rho * Le * geometric;
+	}
+
+	/* direct_occluded (amadeus_common.cuh:399-421) */
+	f3 direct_occluded(const SurfaceHit &sh, const f3 &Le, const f3 &normal, f3 D, float d)
+	{
+		f3 Li = mk(0.0f);
+		if (!occluded(sh.x, D, d)) {
+			f3 rho = brdf(sh, D);
+			float geometric = fabsf(dot(sh.n, D));
+			float ldot = fabsf(dot(normal, D));
+			geometric *= ldot / (d * d);
+			Li = rho * Le * geometric;
+		}
+		return Li;
+	}
+};
+
+/* ============================================================ hit data == */
+
+/* LOAD_INTERSECTION_DATA (amadeus_common.cuh:490-515) with
+ * calculate_normal (:74-150), calculate_intersection (:62-71) and
+ * calculate_material (:153-187); world-space vertices (identity model).
+ * Returns false when the normal is NaN (the path then contributes 0). */
+bool surface(const oracle_scene *s, const kgr_hit &h, const f3 &dir, SurfaceHit &sh)
+{
+	const uint32_t *t = s->tris + 4 * (size_t)h.prim;
+	f3 a = ld3(s->positions, t[0]), b = ld3(s->positions, t[1]), c = ld3(s->positions, t[2]);
+	f3 e1 = b - a;
+	f3 e2 = c - a;
+	f3 ng = normalize(cross(e1, e2));
+	bool entering;
+	if (dot(ng, dir) > 0.0f) {
+		ng = -ng;
+		entering = false;
+	} else {
+		entering = true;
+	}
+	ng = normalize(ng);
+	f3 na = ld3(s->normals, t[0]), nb = ld3(s->normals, t[1]), nc = ld3(s->normals, t[2]);
+	float w0 = 1.0f - h.b1 - h.b2;
+	f3 normal = w0 * na + h.b1 * nb + h.b2 * nc;
+	if (dot(normal, ng) < 0.0f)
+		normal = -normal;
+	normal = normalize(normal);
+	f3 x = w0 * a + h.b1 * b + h.b2 * c;
+	sh.mat = load_material(s->materials[t[3]]);
+	sh.entering = entering;
+	sh.n = normal;
+	sh.wo = -dir;
+	sh.x = x;
+	return !anynan(normal);
+}
+
+/* make_ray (amadeus_path_tracer.cu:25-56; amadeus_restir.cu:30-65 uses a
+ * fixed -0.5 offset but still draws once) */
+void make_ray(const oracle_render_params *p, uint32_t ix, uint32_t iy, bool jitter,
+		f3 &seed, f3 &origin, f3 &direction)
+{
+	f3 U = mk(p->ax_u[0], p->ax_u[1], p->ax_u[2]);
+	f3 V = mk(p->ax_v[0], p->ax_v[1], p->ax_v[2]);
+	f3 W = mk(p->ax_w[0], p->ax_w[1], p->ax_w[2]);
+	pcg3f(seed);
+	float xoffset = jitter ? (fract(seed.x) - 0.5f) : -0.5f;
+	float yoffset = jitter ? (fract(seed.y) - 0.5f) : -0.5f;
+	float ax = ((float)ix + xoffset) / (float)p->width;
+	float ay = ((float)iy + yoffset) / (float)p->height;
+	float dx = 2.0f * ax - 1.0f;
+	float dy = 2.0f * ay - 1.0f;
+	origin = mk(p->center[0], p->center[1], p->center[2]);
+	direction = normalize(dx * U + dy * V + W);
+}
+
+struct PathResult {
+	f3 L;
+	f3 normal, albedo, position;
+	bool hit;
+};
+
+/* One path of the recursive __closesthit__ (amadeus_path_tracer.cu:133-201)
+ * written as a loop: L = sum_k beta_k * (Le_k + Ld_k), beta_{k+1} = beta_k *
+ * f |wi.n| / pdf.  Hits at depth > max_depth contribute nothing
+ * (LOAD_RAYPACKET, amadeus_common.cuh:480-488), so no ray is cast there.
+ * Russian roulette follows naive_path_tracer.cu:294-303.  restir_primary
+ * turns the depth-0 vertex into the ReSTIR initial vertex
+ * (amadeus_restir.cu:473-526), which adds no direct term; `on_primary` is
+ * then called to run RIS. */
+template <class OnPrimary>
+PathResult trace_path(Ctx &ctx, const oracle_render_params *p, f3 o, f3 d, f3 &seed,
+		bool restir_primary, OnPrimary on_primary)
+{
+	PathResult r;
+	r.L = mk(0.0f);
+	r.normal = r.albedo = r.position = mk(0.0f);
+	r.hit = false;
+	f3 beta = mk(1.0f);
+	for (int depth = 0;; depth++) {
+		if (depth > p->max_depth)
+			break;
+		if (depth == 0)
+			ctx.stats.camera_rays++;
+		else
+			ctx.stats.bounce_rays++;
+		kgr_hit h = trace_closest(ctx.s, o, d, ctx.tmax_closest, &ctx.internal, &ctx.leaves);
+		if (h.prim < 0)
+			break;
+		SurfaceHit sh;
+		if (!surface(ctx.s, h, d, sh))
+			break;
+		f3 n = sh.n;
+		float sgn = sh.mat.type == KGR_SHADING_TRANSMISSION ? -1.0f : 1.0f;
+		sh.x = sh.x + sgn * n * OFFSET_EPS;
+		if (depth == 0) {
+			r.hit = true;
+			r.normal = n;
+			r.albedo = sh.mat.diffuse;
+			r.position = sh.x;
+		}
+		if (restir_primary && depth == 0) {
+			on_primary(sh, seed);
+		} else {
+			f3 direct = sh.mat.emission + ctx.Ld(sh, seed);
+			r.L = r.L + beta * direct;
+		}
+		f3 wi;
+		float pdf = 0.0f;
+		f3 f = eval(sh, wi, pdf, seed);
+		if (!(pdf > 0))
+			break;
+		f3 T = f * fabsf(dot(wi, n)) / pdf;
+		beta = beta * T;
+		if (p->russian_roulette && depth >= p->rr_start_depth) {
+			float q = 1.0f - kmin(kmax(0.05f, beta.y), 1.0f);
+			float rr = fract(seed.x);
+			if (rr < q)
+				break;
+			beta = beta / (1.0f - q);
+		}
+		o = sh.x;
+		d = wi;
+	}
+	return r;
+}
+
+struct NoPrimary {
+	void operator()(const SurfaceHit &, f3 &) const {}
+};
+
+inline void store4(float *buf, size_t i, const f3 &v, float w)
+{
+	buf[4 * i + 0] = v.x;
+	buf[4 * i + 1] = v.y;
+	buf[4 * i + 2] = v.z;
+	buf[4 * i + 3] = w;
+}
+
+inline f3 load4(const float *buf, size_t i) { return mk(buf[4 * i], buf[4 * i + 1], buf[4 * i + 2]); }
+
+/* accumulate (amadeus_path_tracer.cu:59-70): glm::vec4 divided by a scalar
+ * divides each component. */
+inline void accumulate4(float *buf, size_t i, const f3 &v, float w, bool acc, float count)
+{
+	if (acc) {
+		float *d = buf + 4 * i;
+		float s[4] = {v.x, v.y, v.z, w};
+		for (int c = 0; c < 4; c++)
+			d[c] = (d[c] * count + s[c]) / (count + 1);
+	} else {
+		store4(buf, i, v, w);
+	}
+}
+
+std::vector<TriLight> load_lights(const oracle_scene *s)
+{
+	std::vector<TriLight> v(s->light_count);
+	for (uint32_t i = 0; i < s->light_count; i++)
+		v[i] = load_light(s->lights[i]);
+	return v;
+}
+
+void merge_stats(oracle_render_stats *dst, const oracle_render_stats &src)
+{
+	dst->camera_rays += src.camera_rays;
+	dst->bounce_rays += src.bounce_rays;
+	dst->shadow_rays += src.shadow_rays;
+}
+
+int nthreads(int t)
+{
+#ifdef _OPENMP
+	return t > 0 ? t : omp_get_max_threads();
+#else
+	(void)t;
+	return 1;
+#endif
+}
+
+/* ============================================================== ReSTIR == */
+
+struct Sample {
+	int light;
+	f3 point;
+};
+
+/* Reservoir<T> (include/amadeus/reservoir.cuh:19-75) */
+struct Reservoir {
+	Sample data = {-1, {0.0f, 0.0f, 0.0f}};
+	float w = 0.0f, W = 0.0f;
+	int M = 0;
+	f3 seed;
+
+	bool update(const Sample &sample, float weight)
+	{
+		w += weight;
+		float eta = rand_uniform(seed);
+		bool selected = (eta * w) < weight;
+		if (selected)
+			data = sample;
+		M++;
+		return selected;
+	}
+	void resample(float target)
+	{
+		float d = target * M;
+		W = (d > 0) ? w / d : 0.0f;
+	}
+	void reset()
+	{
+		w = 0.0f;
+		M = 0;
+		W = 0.0f;
+	}
+};
+
+/* Salt of the RIS reservoir's own stream.  The reference seeds reservoirs
+ * from std::random_device on the host (reservoir.cuh:29-36); here the seed
+ * is a fixed function of pixel and frame so runs are reproducible. */
+const uint32_t RIS_SALT = 0x9E3779B9u;
+
+struct RestirBufs {
+	int32_t *light; float *point; float *w; float *W; int32_t *M;
+	Reservoir get(size_t i) const
+	{
+		Reservoir r;
+		r.data.light = light[i];
+		r.data.point = mk(point[3 * i], point[3 * i + 1], point[3 * i + 2]);
+		r.w = w[i];
+		r.W = W[i];
+		r.M = M[i];
+		return r;
+	}
+	void set(size_t i, const Reservoir &r) const
+	{
+		light[i] = r.data.light;
+		point[3 * i] = r.data.point.x;
+		point[3 * i + 1] = r.data.point.y;
+		point[3 * i + 2] = r.data.point.z;
+		w[i] = r.w;
+		W[i] = r.W;
+		M[i] = r.M;
+	}
+	void reset(size_t i) const
+	{
+		w[i] = 0.0f;
+		M[i] = 0;
+		W[i] = 0.0f;
+	}
+};
+
+/* target (amadeus_restir.cu:147-161) */
+float target(Ctx &ctx, const Sample &smp, const SurfaceHit &hit)
+{
+	if (smp.light < 0)
+		return 0.0f;
+	const TriLight &l = ctx.lights[smp.light];
+	f3 D = smp.point - hit.x;
+	float d = length(D);
+	f3 Li = ctx.direct_unoccluded(hit, l.intensity, l.normal(), D / d, d);
+	return Li.x + Li.y + Li.z;
+}
+
+/* occluded_target (amadeus_restir.cu:163-178) */
+float occluded_target(Ctx &ctx, const Sample &smp, const SurfaceHit &hit)
+{
+	if (smp.light < 0)
+		return 0.0f;
+	const TriLight &l = ctx.lights[smp.light];
+	f3 D = smp.point - hit.x;
+	float d = length(D);
+	f3 Li = ctx.direct_occluded(hit, l.intensity, l.normal(), D / d, d);
+	return Li.x + Li.y + Li.z;
+}
+
+/* glm::mat4 * glm::mat4 and mat4 * vec4, column-major, columns summed in
+ * order (glm/detail/type_mat4x4.inl). */
+void mat4_mul(const float *a, const float *b, float *out)
+{
+	for (int j = 0; j < 4; j++) {
+		for (int i = 0; i < 4; i++) {
+			float v = a[0 * 4 + i] * b[j * 4 + 0] + a[1 * 4 + i] * b[j * 4 + 1]
+				+ a[2 * 4 + i] * b[j * 4 + 2] + a[3 * 4 + i] * b[j * 4 + 3];
+			out[j * 4 + i] = v;
+		}
+	}
+}
+
+/* reproject (amadeus_restir.cu:181-210); indices past the image edge are
+ * rejected instead of read out of bounds. */
+int reproject(const oracle_render_params *p, int index, const f3 &position)
+{
+	if (p->samples > 0)
+		return index;
+	float pv[16];
+	mat4_mul(p->prev_projection, p->prev_view, pv);
+	float q[4];
+	for (int i = 0; i < 4; i++)
+		q[i] = pv[0 * 4 + i] * position.x + pv[1 * 4 + i] * position.y
+			+ pv[2 * 4 + i] * position.z + pv[3 * 4 + i] * 1.0f;
+	float u = q[0] / q[3];
+	float v = q[1] / q[3];
+	bool in_u = (u >= -1.0f && u <= 1.0f);
+	bool in_v = (v >= -1.0f && v <= 1.0f);
+	if (!(in_u && in_v))
+		return -1;
+	u = (u + 1.0f) * 0.5f;
+	v = (v + 1.0f) * 0.5f;
+	int ix = (int)((double)(u * (float)p->width) + 0.5);
+	int iy = (int)((double)(v * (float)p->height) + 0.5);
+	if (ix < 0 || iy < 0 || ix >= (int)p->width || iy >= (int)p->height)
+		return -1;
+	return iy * (int)p->width + ix;
+}
+
+/* sample_spatial_neighborhood (amadeus_restir.cu:294-314); 2 * M_PI is the
+ * double constant of <math.h>, so theta is computed in double and rounded. */
+int spatial_neighbor(const oracle_render_params *p, int index, f3 &seed, int radius)
+{
+	int width = (int)p->width, height = (int)p->height;
+	int x = index % width;
+	int y = index / width;
+	f3 offset = rand_uniform_3f(seed);
+	float theta = (float)(2.0 * 3.14159265358979323846 * (double)offset.x);
+	float r = (float)radius * ksqrt(offset.y);
+	float st, ct;
+	ksincos(theta, st, ct);
+	int x0 = (int)((float)x + r * ct);
+	int y0 = (int)((float)y + r * st);
+	x0 = x0 < 0 ? 0 : (x0 > width - 1 ? width - 1 : x0);
+	y0 = y0 < 0 ? 0 : (y0 > height - 1 ? height - 1 : y0);
+	return x0 + y0 * width;
+}
+
+/* glm::normalize(center - position) for the reuse passes' wo */
+inline f3 view_wo(const oracle_render_params *p, const f3 &position)
+{
+	f3 c = mk(p->center[0], p->center[1], p->center[2]);
+	return normalize(c - position);
+}
+
+} /* namespace */
+
+/* ================================================================= API == */
+
+extern "C" {
+
+int64_t oracle_build_kobra(const float *boxes, uint32_t n, float *out_vec4, uint64_t capacity)
+{
+	Builder b;
+	b.nodes.reserve(2 * (size_t)n);
+	std::vector<int> ids(n);
+	for (uint32_t i = 0; i < n; i++) {
+		Node node;
+		node.bbox.min = mk(boxes[6 * i + 0], boxes[6 * i + 1], boxes[6 * i + 2]);
+		node.bbox.max = mk(boxes[6 * i + 3], boxes[6 * i + 4], boxes[6 * i + 5]);
+		node.object = (int)i;
+		b.nodes.push_back(node);
+		ids[i] = (int)i;
+	}
+	int root = b.partition(ids);
+	std::vector<float> buf;
+	b.serialize(buf, root, -1);
+	uint64_t count = buf.size() / 4;
+	if (count > capacity)
+		return -1;
+	memcpy(out_vec4, buf.data(), buf.size() * sizeof(float));
+	return (int64_t)count;
+}
+
+void oracle_triangle_boxes(const oracle_scene *s, float *boxes)
+{
+	for (uint32_t i = 0; i < s->triangle_count; i++) {
+		Tri t = load_tri(s, (int)i);
+		f3 mn = gmin(t.a, gmin(t.b, t.c));
+		f3 mx = gmax(t.a, gmax(t.b, t.c));
+		float *o = boxes + 6 * (size_t)i;
+		o[0] = mn.x; o[1] = mn.y; o[2] = mn.z;
+		o[3] = mx.x; o[4] = mx.y; o[5] = mx.z;
+	}
+}
+
+void oracle_trace_closest(const oracle_scene *s, const float *rays, uint32_t n,
+		kgr_hit *hits, oracle_trace_stats *stats, int threads)
+{
+	uint64_t internal = 0, leaves = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(+:internal, leaves) num_threads(nthreads(threads))
+	for (int64_t i = 0; i < (int64_t)n; i++) {
+		const float *r = rays + 8 * i;
+		hits[i] = trace_closest(s, mk(r[0], r[1], r[2]), mk(r[4], r[5], r[6]), r[7], &internal, &leaves);
+	}
+	if (stats) {
+		stats->internal_visits += internal;
+		stats->leaf_visits += leaves;
+		stats->rays += n;
+	}
+}
+
+void oracle_trace_any(const oracle_scene *s, const float *rays, uint32_t n,
+		uint32_t *occluded, oracle_trace_stats *stats, int threads)
+{
+	uint64_t internal = 0, leaves = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(+:internal, leaves) num_threads(nthreads(threads))
+	for (int64_t i = 0; i < (int64_t)n; i++) {
+		const float *r = rays + 8 * i;
+		occluded[i] = trace_any(s, mk(r[0], r[1], r[2]), mk(r[4], r[5], r[6]), r[7], &internal, &leaves) ? 1u : 0u;
+	}
+	if (stats) {
+		stats->internal_visits += internal;
+		stats->leaf_visits += leaves;
+		stats->rays += n;
+	}
+}
+
+void oracle_trace_closest_brute(const oracle_scene *s, const float *rays, uint32_t n, kgr_hit *hits)
+{
+	/* rank = order of the leaf records in the threaded buffer */
+	std::vector<int> order;
+	for (uint32_t v = 0; v < s->bvh_vec4_count; v += 3) {
+		int object = bits_i(s->bvh[4 * (size_t)v + 1]);
+		if (object != -1)
+			order.push_back(object);
+	}
+#pragma omp parallel for schedule(dynamic, 64)
+	for (int64_t i = 0; i < (int64_t)n; i++) {
+		const float *r = rays + 8 * i;
+		f3 o = mk(r[0], r[1], r[2]), d = mk(r[4], r[5], r[6]);
+		kgr_hit best = {-1, r[7], 0, 0};
+		for (int prim : order) {
+			Tri t = load_tri(s, prim);
+			float b1 = 0, b2 = 0;
+			float tt = intersect_triangle(t.a, t.b, t.c, o, d, b1, b2);
+			if (tt > 0.0f && tt < best.t) {
+				best.prim = prim;
+				best.t = tt;
+				best.b1 = b1;
+				best.b2 = b2;
+			}
+		}
+		hits[i] = best;
+	}
+}
+
+static void render_pt_rows(const oracle_scene *s, const oracle_render_params *p,
+		float *color, float *normal, float *albedo, float *position,
+		double *out64, oracle_render_stats *stats)
+{
+	std::vector<TriLight> lights = load_lights(s);
+	uint32_t row_end = p->row_end ? p->row_end : p->height;
+	int64_t npix = (int64_t)(row_end - p->row_begin) * p->width;
+	oracle_render_stats total = {0, 0, 0};
+#pragma omp parallel num_threads(nthreads(p->threads))
+	{
+		Ctx ctx;
+		ctx.s = s;
+		ctx.lights = lights;
+		ctx.stats = {0, 0, 0};
+#pragma omp for schedule(dynamic, 64)
+		for (int64_t k = 0; k < npix; k++) {
+			uint32_t iy = p->row_begin + (uint32_t)(k / p->width);
+			uint32_t ix = (uint32_t)(k % p->width);
+			uint32_t pix = ix + iy * p->width;
+			double acc[3] = {0, 0, 0};
+			for (int sidx = 0; sidx < p->spp; sidx++) {
+				uint32_t stream = p->frame * (uint32_t)p->spp + (uint32_t)sidx;
+				f3 seed = pixel_seed(pix, stream, 0);
+				f3 o, d;
+				make_ray(p, ix, iy, true, seed, o, d);
+				PathResult r = trace_path(ctx, p, o, d, seed, false, NoPrimary());
+				f3 L = r.L;
+				if (anynan(L))
+					L = mk(1.0f, 0.0f, 1.0f);
+				if (out64) {
+					acc[0] += L.x;
+					acc[1] += L.y;
+					acc[2] += L.z;
+					continue;
+				}
+				bool acc_on = p->accumulate || sidx > 0;
+				float count = (float)(p->accumulate ? p->samples + sidx : sidx);
+				accumulate4(color, pix, L, 1.0f, acc_on, count);
+				accumulate4(normal, pix, r.normal, 0.0f, acc_on, count);
+				accumulate4(albedo, pix, r.albedo, 0.0f, acc_on, count);
+				store4(position, pix, r.position, 0.0f);
+			}
+			if (out64) {
+				for (int c = 0; c < 3; c++)
+					out64[3 * (size_t)pix + c] = acc[c] / p->spp;
+			}
+		}
+#pragma omp critical
+		merge_stats(&total, ctx.stats);
+	}
+	if (stats)
+		merge_stats(stats, total);
+}
+
+void oracle_render_pt(const oracle_scene *s, const oracle_render_params *p,
+		float *color, float *normal, float *albedo, float *position,
+		oracle_render_stats *stats)
+{
+	render_pt_rows(s, p, color, normal, albedo, position, nullptr, stats);
+}
+
+void oracle_render_pt_f64(const oracle_scene *s, const oracle_render_params *p,
+		double *out_rgb, oracle_render_stats *stats)
+{
+	render_pt_rows(s, p, nullptr, nullptr, nullptr, nullptr, out_rgb, stats);
+}
+
+void oracle_render_restir(const oracle_scene *s, const oracle_render_params *p,
+		oracle_restir_state *st, float *color, float *normal, float *albedo,
+		float *position, oracle_render_stats *stats)
+{
+	std::vector<TriLight> lights = load_lights(s);
+	int64_t npix = (int64_t)p->width * p->height;
+	RestirBufs A = {st->cur_light, st->cur_point, st->cur_w, st->cur_W, st->cur_M};
+	RestirBufs B = {st->prev_light, st->prev_point, st->prev_w, st->prev_W, st->prev_M};
+	oracle_render_stats total = {0, 0, 0};
+	float count = (float)p->samples;
+	bool acc = p->accumulate != 0;
+
+	/* ---- initial pass (amadeus_restir.cu:82-144, 437-559) ---- */
+#pragma omp parallel num_threads(nthreads(p->threads))
+	{
+		Ctx ctx;
+		ctx.s = s;
+		ctx.lights = lights;
+		ctx.stats = {0, 0, 0};
+#pragma omp for schedule(dynamic, 64)
+		for (int64_t k = 0; k < npix; k++) {
+			uint32_t ix = (uint32_t)(k % p->width), iy = (uint32_t)(k / p->width);
+			uint32_t pix = (uint32_t)k;
+			A.reset(pix);
+			f3 seed = pixel_seed(pix, p->frame, 0);
+			f3 o, d;
+			make_ray(p, ix, iy, false, seed, o, d);
+			auto ris = [&](const SurfaceHit &sh, f3 &pseed) {
+				Reservoir res;
+				res.seed = pixel_seed(pix, p->frame, RIS_SALT);
+				res.data.light = -1;
+				res.data.point = mk(0.0f);
+				for (int i = 0; i < p->candidates; i++) {
+					Sample smp;
+					float pdf;
+					ctx.sample_direct(sh, pseed, smp.light, smp.point, pdf);
+					float tgt = 0.0f;
+					if (smp.light >= 0) {
+						const TriLight &l = ctx.lights[smp.light];
+						f3 D = smp.point - sh.x;
+						float dd = length(D);
+						f3 Li = ctx.direct_unoccluded(sh, l.intensity, l.normal(), D / dd, dd);
+						tgt = Li.x + Li.y + Li.z;
+					}
+					res.update(smp, (pdf > 0) ? tgt / pdf : 0);
+				}
+				float tgt = 0.0f;
+				f3 D = mk(0.0f);
+				float dd = 0.0f;
+				if (res.data.light >= 0) {
+					const TriLight &l = ctx.lights[res.data.light];
+					D = res.data.point - sh.x;
+					dd = length(D);
+					f3 Li = ctx.direct_occluded(sh, l.intensity, l.normal(), D / dd, dd);
+					tgt = Li.x + Li.y + Li.z;
+				}
+				res.resample(tgt);
+				bool occ = ctx.occluded(sh.x, D / dd, dd);
+				res.W *= 1.0f - (occ ? 1.0f : 0.0f);
+				A.set(pix, res);
+				kgr_material m;
+				memcpy(m.diffuse, &sh.mat.diffuse, 12);
+				memcpy(m.specular, &sh.mat.specular, 12);
+				memcpy(m.emission, &sh.mat.emission, 12);
+				memcpy(m.ambient, &sh.mat.ambient, 12);
+				m.shininess = sh.mat.shininess;
+				m.roughness = sh.mat.roughness;
+				m.refraction = sh.mat.refraction;
+				m.type = sh.mat.type;
+				st->materials[pix] = m;
+			};
+			PathResult r = trace_path(ctx, p, o, d, seed, true, ris);
+			f3 L = r.L;
+			if (anynan(L))
+				L = mk(1.0f, 0.0f, 1.0f);
+			store4(st->intermediate, pix, L, 1.0f);
+			store4(st->auxiliary, pix, seed, 1.0f);
+			accumulate4(normal, pix, r.normal, 0.0f, acc, count);
+			accumulate4(albedo, pix, r.albedo, 0.0f, acc, count);
+			store4(position, pix, r.position, 0.0f);
+		}
+#pragma omp critical
+		merge_stats(&total, ctx.stats);
+	}
+
+	/* ---- temporal pass (amadeus_restir.cu:213-291): current = A, previous = B ---- */
+	if (p->temporal) {
+#pragma omp parallel num_threads(nthreads(p->threads))
+		{
+			Ctx ctx;
+			ctx.s = s;
+			ctx.lights = lights;
+			ctx.stats = {0, 0, 0};
+#pragma omp for schedule(dynamic, 64)
+			for (int64_t k = 0; k < npix; k++) {
+				int pix = (int)k;
+				Reservoir cur = A.get(pix);
+				if (cur.M <= 0)
+					continue;
+				f3 xpos = load4(position, pix);
+				SurfaceHit hit;
+				hit.mat = load_material(st->materials[pix]);
+				hit.entering = false;
+				hit.n = load4(normal, pix);
+				hit.wo = view_wo(p, xpos);
+				hit.x = xpos;
+				int pindex = reproject(p, pix, xpos);
+				Reservoir merged;
+				merged.seed = load4(st->auxiliary, pix);
+				float t_current = occluded_target(ctx, cur.data, hit);
+				merged.update(cur.data, t_current * cur.W * cur.M);
+				int N = cur.M;
+				if (pindex >= 0) {
+					Reservoir prev = B.get(pindex);
+					if (prev.M > 0) {
+						prev.M = prev.M < p->temporal_mcap ? prev.M : p->temporal_mcap;
+						float t_previous = occluded_target(ctx, prev.data, hit);
+						merged.update(prev.data, t_previous * prev.W * prev.M);
+						N += (t_previous > 0) * prev.M;
+					}
+				}
+				merged.M = N;
+				float t_merged = target(ctx, merged.data, hit);
+				merged.resample(t_merged);
+				A.set(pix, merged);
+			}
+#pragma omp critical
+			merge_stats(&total, ctx.stats);
+		}
+	}
+
+	/* ---- spatial passes (amadeus_restir.cu:317-434), ping-pong of
+	 * restir.cuh:280-300: read `in`, write `out`, then swap ---- */
+	RestirBufs in = A, out = B;
+	for (int pass = 0; pass < p->spatial_passes; pass++) {
+#pragma omp parallel num_threads(nthreads(p->threads))
+		{
+			Ctx ctx;
+			ctx.s = s;
+			ctx.lights = lights;
+			ctx.stats = {0, 0, 0};
+			const int K = p->spatial_neighbors;
+			std::vector<SurfaceHit> hits(K);
+			std::vector<int> sizes(K);
+#pragma omp for schedule(dynamic, 64)
+			for (int64_t k = 0; k < npix; k++) {
+				int pix = (int)k;
+				f3 xpos = load4(position, pix);
+				SurfaceHit hit;
+				hit.mat = load_material(st->materials[pix]);
+				hit.entering = false;
+				hit.n = load4(normal, pix);
+				hit.wo = view_wo(p, xpos);
+				hit.x = xpos;
+				Reservoir current = in.get(pix);
+				f3 direct = mk(0.0f);
+				if (current.M > 0) {
+					Reservoir merged;
+					merged.seed = load4(st->auxiliary, pix);
+					float t_current = target(ctx, current.data, hit);
+					merged.update(current.data, t_current * current.W * current.M);
+					int cnt = 0;
+					for (int i = 0; i < K; i++) {
+						int index0 = spatial_neighbor(p, pix, merged.seed, p->spatial_radius);
+						Reservoir nb = in.get(index0);
+						if (nb.M > 0) {
+							float t_neighbor = occluded_target(ctx, nb.data, hit);
+							merged.update(nb.data, t_neighbor * nb.W * nb.M);
+						}
+						SurfaceHit h0;
+						h0.mat = load_material(st->materials[index0]);
+						h0.entering = nb.M > 0;
+						h0.n = load4(normal, index0);
+						h0.wo = hit.wo;
+						h0.x = load4(position, index0);
+						hits[i] = h0;
+						sizes[i] = nb.M;
+						cnt += nb.M;
+					}
+					merged.M = current.M + cnt;
+					int Z = current.M;
+					for (int i = 0; i < K; i++) {
+						float t_neighbor = hits[i].entering ? occluded_target(ctx, merged.data, hits[i]) : 0.0f;
+						if (t_neighbor > 0.0f)
+							Z += sizes[i];
+					}
+					float t_merged = target(ctx, merged.data, hit);
+					float denominator = t_merged * Z;
+					merged.W = (denominator > 0.0f) ? merged.w / denominator : 0.0f;
+					f3 lighting = mk(0.0f);
+					if (merged.data.light >= 0) {
+						const TriLight &l = ctx.lights[merged.data.light];
+						f3 D = merged.data.point - hit.x;
+						float dd = length(D);
+						lighting = ctx.direct_occluded(hit, l.intensity, l.normal(), D / dd, dd);
+					}
+					direct = hit.mat.emission + lighting * merged.W;
+					out.set(pix, merged);
+				} else {
+					out.reset(pix);
+				}
+				f3 c = direct + load4(st->intermediate, pix);
+				float cw = 1.0f + st->intermediate[4 * (size_t)pix + 3];
+				if (anynan(c) || kisnan(cw)) {
+					c = mk(1.0f, 0.0f, 1.0f);
+					cw = 1.0f;
+				}
+				accumulate4(color, pix, c, cw, acc, count);
+			}
+#pragma omp critical
+			merge_stats(&total, ctx.stats);
+		}
+		std::swap(in, out);
+	}
+	/* restir.cuh:300: the final swap makes `previous` the last spatial
+	 * output.  With the pass loop's swaps, that output is now `in`; copy it
+	 * into the caller's prev buffers if it lives in the cur buffers. */
+	if (p->spatial_passes > 0 && in.light == A.light) {
+		for (int64_t k = 0; k < npix; k++)
+			B.set(k, A.get(k));
+	}
+	if (stats)
+		merge_stats(stats, total);
+}
+
+/* --------------------------------------------------------- known answers */
+
+void oracle_kat_rng(float sx, float sy, float sz, int draws, float *out)
+{
+	f3 seed = mk(sx, sy, sz);
+	for (int i = 0; i < draws; i++) {
+		float u = rand_uniform(seed);
+		out[4 * i + 0] = u;
+		out[4 * i + 1] = seed.x;
+		out[4 * i + 2] = seed.y;
+		out[4 * i + 3] = seed.z;
+	}
+}
+
+float oracle_kat_intersect(const float *v1, const float *v2, const float *v3,
+		const float *o, const float *d, float *b1b2)
+{
+	float b1 = 0, b2 = 0;
+	float t = intersect_triangle(mk(v1[0], v1[1], v1[2]), mk(v2[0], v2[1], v2[2]),
+		mk(v3[0], v3[1], v3[2]), mk(o[0], o[1], o[2]), mk(d[0], d[1], d[2]), b1, b2);
+	b1b2[0] = b1;
+	b1b2[1] = b2;
+	return t;
+}
+
+void oracle_kat_sample_light(const kgr_triangle_light *l, const float *seed, float *point, float *area_normal)
+{
+	TriLight L = load_light(*l);
+	f3 sd = mk(seed[0], seed[1], seed[2]);
+	f3 pt = sample_area_light(L, sd);
+	point[0] = pt.x; point[1] = pt.y; point[2] = pt.z;
+	f3 n = L.normal();
+	area_normal[0] = L.area();
+	area_normal[1] = n.x; area_normal[2] = n.y; area_normal[3] = n.z;
+}
+
+void oracle_kat_brdf_eval(const kgr_material *m, const float *n, const float *wo,
+		const float *seed_in, float *out)
+{
+	SurfaceHit sh;
+	sh.mat = load_material(*m);
+	sh.entering = true;
+	sh.n = mk(n[0], n[1], n[2]);
+	sh.wo = mk(wo[0], wo[1], wo[2]);
+	sh.x = mk(0.0f);
+	f3 seed = mk(seed_in[0], seed_in[1], seed_in[2]);
+	f3 wi;
+	float pdf = 0;
+	f3 f = eval(sh, wi, pdf, seed);
+	float v[10] = {f.x, f.y, f.z, wi.x, wi.y, wi.z, pdf, seed.x, seed.y, seed.z};
+	memcpy(out, v, sizeof(v));
+}
+
+void oracle_kat_brdf(const kgr_material *m, const float *n, const float *wo, const float *wi, float *out)
+{
+	SurfaceHit sh;
+	sh.mat = load_material(*m);
+	sh.entering = true;
+	sh.n = mk(n[0], n[1], n[2]);
+	sh.wo = mk(wo[0], wo[1], wo[2]);
+	sh.x = mk(0.0f);
+	f3 w = mk(wi[0], wi[1], wi[2]);
+	f3 f = brdf(sh, w);
+	out[0] = f.x; out[1] = f.y; out[2] = f.z;
+	out[3] = ggx_pdf(sh.mat, sh.n, w, sh.wo);
+}
+
+void oracle_kat_math(const float *x, int n, float *out)
+{
+	for (int i = 0; i < n; i++) {
+		out[5 * i + 0] = ksin(x[i]);
+		out[5 * i + 1] = kcos(x[i]);
+		out[5 * i + 2] = ktan(x[i]);
+		out[5 * i + 3] = katan(x[i]);
+		out[5 * i + 4] = kacos(x[i]);
+	}
+}
+
+} /* extern "C" */

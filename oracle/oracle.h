@@ -1,0 +1,141 @@
+/*
+ * oracle.h -- CPU oracle for the ray-tracing hot path (TEST INFRASTRUCTURE).
+ *
+ * This library is the checker, not the product: only tests/, the smoke test
+ * of __graft_entry__.py and the cpu_baseline / --impl reference legs of
+ * bench.py load it.  It restates, function by function, the reference's
+ * algorithms (each definition in oracle.cpp cites the reference file:line it
+ * follows) in plain C++ compiled with -O2 -ffp-contract=off, so that its
+ * float results can be compared bit for bit with the CUDA kernels.
+ *
+ * Parity pin: the reference has no tests or golden vectors.  The RNG, the
+ * triangle test, the area-light sampler and the GGX BRDF are pinned against
+ * known-answer vectors produced by compiling the reference's own headers
+ * (include/cuda/random.cuh, include/cuda/math.cuh, include/cuda/brdf.cuh,
+ * include/optix/lighting.cuh) on the host (oracle/_ref, tests/golden/).  The
+ * BVH builder, the GLSL traversal and the OptiX programs cannot be compiled
+ * here (glm, OptiX runtime and Vulkan are absent), so those restatements are
+ * unpinned beyond structural invariants.
+ */
+#ifndef KGR_ORACLE_H_
+#define KGR_ORACLE_H_
+
+#include <stdint.h>
+#include "../include/kgr.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct oracle_scene {
+	const float *positions;        /* 3 * vertex_count */
+	const float *normals;          /* 3 * vertex_count */
+	const uint32_t *tris;          /* 4 * triangle_count: i0, i1, i2, material */
+	const kgr_material *materials;
+	const kgr_triangle_light *lights;
+	const float *bvh;              /* threaded bvh.cpp layout */
+	uint32_t vertex_count;
+	uint32_t triangle_count;
+	uint32_t material_count;
+	uint32_t light_count;
+	uint32_t bvh_vec4_count;
+	uint32_t pad;
+} oracle_scene;
+
+typedef struct oracle_trace_stats {
+	uint64_t internal_visits; /* 48 B each: header, min, max */
+	uint64_t leaf_visits;     /* 16 B header + 64 B triangle (index + 3 positions) */
+	uint64_t rays;
+} oracle_trace_stats;
+
+/* Reference builder: partition() + serialize() of source/bvh.cpp.
+ * boxes: 6 floats per primitive {min xyz, max xyz}.  Returns the number of
+ * vec4 written (3 per node) or -1 if capacity is too small. */
+int64_t oracle_build_kobra(const float *boxes, uint32_t n, float *out_vec4, uint64_t capacity);
+
+/* Per-triangle AABBs as Submesh::bvh computes them (include/mesh.hpp:48-78). */
+void oracle_triangle_boxes(const oracle_scene *s, float *boxes);
+
+/* GLSL trace() (bvh.glsl:52-99) over the threaded layout; rays are 8 floats
+ * {o, unused, d, tmax}.  Multithreaded over rays when threads > 1. */
+void oracle_trace_closest(const oracle_scene *s, const float *rays, uint32_t n,
+		kgr_hit *hits, oracle_trace_stats *stats, int threads);
+void oracle_trace_any(const oracle_scene *s, const float *rays, uint32_t n,
+		uint32_t *occluded, oracle_trace_stats *stats, int threads);
+
+/* Brute force closest hit over all triangles: same triangle test, ties to
+ * the lower rank (position in the threaded walk), for cross-checking. */
+void oracle_trace_closest_brute(const oracle_scene *s, const float *rays, uint32_t n, kgr_hit *hits);
+
+typedef struct oracle_render_params {
+	uint32_t width, height;
+	float center[3], ax_u[3], ax_v[3], ax_w[3];
+	float projection[16], view[16];
+	float prev_projection[16], prev_view[16];
+	int32_t max_depth;
+	int32_t spp;
+	int32_t samples;        /* previously accumulated samples (count) */
+	int32_t accumulate;
+	uint32_t frame;
+	int32_t russian_roulette;
+	int32_t rr_start_depth;
+	int32_t candidates;     /* ReSTIR RIS candidates (32) */
+	int32_t temporal;       /* run the temporal pass */
+	int32_t temporal_mcap;  /* 200 in the reference */
+	int32_t spatial_passes; /* 2 in the reference */
+	int32_t spatial_neighbors; /* 5 */
+	int32_t spatial_radius;    /* 30 */
+	uint32_t row_begin, row_end; /* PT only: rows to render (crop) */
+	int32_t threads;
+} oracle_render_params;
+
+typedef struct oracle_render_stats {
+	uint64_t camera_rays, bounce_rays, shadow_rays;
+} oracle_render_stats;
+
+/* Path tracer: amadeus_path_tracer.cu + naive_path_tracer.cu Russian
+ * roulette.  Buffers are float4 width*height (color, normal, albedo,
+ * position); only rows [row_begin, row_end) are written. */
+void oracle_render_pt(const oracle_scene *s, const oracle_render_params *p,
+		float *color, float *normal, float *albedo, float *position,
+		oracle_render_stats *stats);
+
+/* Same path tracer with double-precision accumulation of the per-pixel
+ * sample mean (the "FP64 oracle" image): out is 3 doubles per pixel. */
+void oracle_render_pt_f64(const oracle_scene *s, const oracle_render_params *p,
+		double *out_rgb, oracle_render_stats *stats);
+
+/* ReSTIR DI state, all width*height: reservoirs in the 32-byte SoA layout
+ * (light index, point xyz, w, W, M), the per-pixel material, the indirect
+ * "intermediate" colour and the auxiliary seed. */
+typedef struct oracle_restir_state {
+	int32_t *cur_light; float *cur_point; float *cur_w; float *cur_W; int32_t *cur_M;
+	int32_t *prev_light; float *prev_point; float *prev_w; float *prev_W; int32_t *prev_M;
+	kgr_material *materials;
+	float *intermediate; /* float4 */
+	float *auxiliary;    /* float4 */
+} oracle_restir_state;
+
+/* One ReSTIR DI frame: initial (amadeus_restir.cu:82-144,437-559), temporal
+ * (:213-291), spatial passes (:294-434) and the buffer swaps of
+ * include/amadeus/restir.cuh:258-303.  After the call prev_* holds the
+ * reservoirs the next frame's temporal pass reuses. */
+void oracle_render_restir(const oracle_scene *s, const oracle_render_params *p,
+		oracle_restir_state *st, float *color, float *normal, float *albedo,
+		float *position, oracle_render_stats *stats);
+
+/* Known-answer helpers exposed for the golden-vector tests. */
+void oracle_kat_rng(float seed_x, float seed_y, float seed_z, int draws, float *out);
+float oracle_kat_intersect(const float *v1, const float *v2, const float *v3,
+		const float *o, const float *d, float *b1b2);
+void oracle_kat_sample_light(const kgr_triangle_light *l, const float *seed, float *point, float *area_normal);
+void oracle_kat_brdf_eval(const kgr_material *m, const float *n, const float *wo,
+		const float *seed_in, float *f_wi_pdf_seed);
+void oracle_kat_brdf(const kgr_material *m, const float *n, const float *wo, const float *wi, float *f_pdf);
+void oracle_kat_math(const float *x, int n, float *sin_cos_tan_atan_acos);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,225 @@
+"""ctypes binding of the CPU oracle (oracle/liboracle.so).
+
+TEST INFRASTRUCTURE: imported only by tests/, __graft_entry__.smoke() and the
+CPU legs of bench.py.  The product path never loads this module.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+u32p = ctypes.POINTER(ctypes.c_uint32)
+f32p = ctypes.POINTER(ctypes.c_float)
+
+
+class OracleScene(ctypes.Structure):
+    _fields_ = [("positions", ctypes.c_void_p), ("normals", ctypes.c_void_p),
+                ("tris", ctypes.c_void_p), ("materials", ctypes.c_void_p),
+                ("lights", ctypes.c_void_p), ("bvh", ctypes.c_void_p),
+                ("vertex_count", ctypes.c_uint32), ("triangle_count", ctypes.c_uint32),
+                ("material_count", ctypes.c_uint32), ("light_count", ctypes.c_uint32),
+                ("bvh_vec4_count", ctypes.c_uint32), ("pad", ctypes.c_uint32)]
+
+
+class TraceStats(ctypes.Structure):
+    _fields_ = [("internal_visits", ctypes.c_uint64), ("leaf_visits", ctypes.c_uint64),
+                ("rays", ctypes.c_uint64)]
+
+
+class RenderParams(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("center", ctypes.c_float * 3), ("ax_u", ctypes.c_float * 3),
+                ("ax_v", ctypes.c_float * 3), ("ax_w", ctypes.c_float * 3),
+                ("projection", ctypes.c_float * 16), ("view", ctypes.c_float * 16),
+                ("prev_projection", ctypes.c_float * 16), ("prev_view", ctypes.c_float * 16),
+                ("max_depth", ctypes.c_int32), ("spp", ctypes.c_int32),
+                ("samples", ctypes.c_int32), ("accumulate", ctypes.c_int32),
+                ("frame", ctypes.c_uint32), ("russian_roulette", ctypes.c_int32),
+                ("rr_start_depth", ctypes.c_int32), ("candidates", ctypes.c_int32),
+                ("temporal", ctypes.c_int32), ("temporal_mcap", ctypes.c_int32),
+                ("spatial_passes", ctypes.c_int32), ("spatial_neighbors", ctypes.c_int32),
+                ("spatial_radius", ctypes.c_int32), ("row_begin", ctypes.c_uint32),
+                ("row_end", ctypes.c_uint32), ("threads", ctypes.c_int32)]
+
+
+class RenderStats(ctypes.Structure):
+    _fields_ = [("camera_rays", ctypes.c_uint64), ("bounce_rays", ctypes.c_uint64),
+                ("shadow_rays", ctypes.c_uint64)]
+
+
+class RestirState(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in (
+        "cur_light", "cur_point", "cur_w", "cur_W", "cur_M",
+        "prev_light", "prev_point", "prev_w", "prev_W", "prev_M",
+        "materials", "intermediate", "auxiliary")]
+
+
+def build():
+    """Compile liboracle.so with the committed Makefile (g++, -ffp-contract=off)."""
+    subprocess.check_call(["make", "-s", "-C", HERE, "liboracle.so"])
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(HERE, "liboracle.so")
+        if not os.path.exists(path):
+            build()
+        L = ctypes.CDLL(path)
+        vp = ctypes.c_void_p
+        L.oracle_build_kobra.restype = ctypes.c_int64
+        L.oracle_build_kobra.argtypes = [vp, ctypes.c_uint32, vp, ctypes.c_uint64]
+        L.oracle_triangle_boxes.argtypes = [ctypes.POINTER(OracleScene), vp]
+        for fn in (L.oracle_trace_closest, L.oracle_trace_any):
+            fn.argtypes = [ctypes.POINTER(OracleScene), vp, ctypes.c_uint32, vp,
+                           ctypes.POINTER(TraceStats), ctypes.c_int]
+        L.oracle_trace_closest_brute.argtypes = [ctypes.POINTER(OracleScene), vp, ctypes.c_uint32, vp]
+        L.oracle_render_pt.argtypes = [ctypes.POINTER(OracleScene), ctypes.POINTER(RenderParams),
+                                       vp, vp, vp, vp, ctypes.POINTER(RenderStats)]
+        L.oracle_render_pt_f64.argtypes = [ctypes.POINTER(OracleScene), ctypes.POINTER(RenderParams),
+                                           vp, ctypes.POINTER(RenderStats)]
+        L.oracle_render_restir.argtypes = [ctypes.POINTER(OracleScene), ctypes.POINTER(RenderParams),
+                                           ctypes.POINTER(RestirState), vp, vp, vp, vp,
+                                           ctypes.POINTER(RenderStats)]
+        L.oracle_kat_rng.argtypes = [ctypes.c_float] * 3 + [ctypes.c_int, vp]
+        L.oracle_kat_intersect.restype = ctypes.c_float
+        L.oracle_kat_intersect.argtypes = [vp] * 6
+        L.oracle_kat_sample_light.argtypes = [vp] * 4
+        L.oracle_kat_brdf_eval.argtypes = [vp] * 5
+        L.oracle_kat_brdf.argtypes = [vp] * 5
+        L.oracle_kat_math.argtypes = [vp, ctypes.c_int, vp]
+        _LIB = L
+    return _LIB
+
+
+def ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+class Scene:
+    """Host arrays of one scene, as the oracle reads them.
+
+    positions/normals: (V,3) float32; tris: (T,4) uint32 (i0,i1,i2,material);
+    materials: structured kgr_material array as raw float32 (M,16);
+    lights: (L,12) float32; bvh: (K,4) float32 threaded layout."""
+
+    def __init__(self, positions, normals, tris, materials, lights, bvh):
+        self.positions = np.ascontiguousarray(positions, dtype=np.float32)
+        self.normals = np.ascontiguousarray(normals, dtype=np.float32)
+        self.tris = np.ascontiguousarray(tris, dtype=np.uint32)
+        self.materials = np.ascontiguousarray(materials, dtype=np.float32)
+        self.lights = np.ascontiguousarray(lights, dtype=np.float32)
+        self.bvh = np.ascontiguousarray(bvh, dtype=np.float32)
+        self.c = OracleScene(ptr(self.positions), ptr(self.normals), ptr(self.tris),
+                             ptr(self.materials), ptr(self.lights), ptr(self.bvh),
+                             len(self.positions), len(self.tris), len(self.materials),
+                             len(self.lights), len(self.bvh), 0)
+
+    def triangle_boxes(self):
+        boxes = np.zeros((len(self.tris), 6), np.float32)
+        lib().oracle_triangle_boxes(ctypes.byref(self.c), ptr(boxes))
+        return boxes
+
+    def trace_closest(self, rays, threads=0):
+        rays = np.ascontiguousarray(rays, dtype=np.float32)
+        hits = np.zeros((len(rays), 4), np.float32)
+        st = TraceStats()
+        lib().oracle_trace_closest(ctypes.byref(self.c), ptr(rays), len(rays), ptr(hits),
+                                   ctypes.byref(st), threads)
+        return hits_view(hits), st
+
+    def trace_any(self, rays, threads=0):
+        rays = np.ascontiguousarray(rays, dtype=np.float32)
+        occ = np.zeros(len(rays), np.uint32)
+        st = TraceStats()
+        lib().oracle_trace_any(ctypes.byref(self.c), ptr(rays), len(rays), ptr(occ),
+                               ctypes.byref(st), threads)
+        return occ, st
+
+    def trace_brute(self, rays):
+        rays = np.ascontiguousarray(rays, dtype=np.float32)
+        hits = np.zeros((len(rays), 4), np.float32)
+        lib().oracle_trace_closest_brute(ctypes.byref(self.c), ptr(rays), len(rays), ptr(hits))
+        return hits_view(hits)
+
+
+def hits_view(raw):
+    """(N,4) float32 hit records -> dict of prim (int32), t, b1, b2."""
+    raw = np.ascontiguousarray(raw, dtype=np.float32)
+    return {"prim": raw[:, 0].view(np.int32).copy(), "t": raw[:, 1].copy(),
+            "b1": raw[:, 2].copy(), "b2": raw[:, 3].copy(), "raw": raw}
+
+
+def build_kobra_bvh(boxes):
+    boxes = np.ascontiguousarray(boxes, dtype=np.float32)
+    n = len(boxes)
+    cap = max(3 * (2 * n), 3)
+    out = np.zeros((cap, 4), np.float32)
+    cnt = lib().oracle_build_kobra(ptr(boxes), n, ptr(out), cap)
+    assert cnt >= 0
+    return out[:cnt].copy()
+
+
+def render_params(width, height, cam, **kw):
+    p = RenderParams()
+    p.width, p.height = width, height
+    for k in ("center", "ax_u", "ax_v", "ax_w"):
+        getattr(p, k)[:] = [float(x) for x in cam[k]]
+    for k in ("projection", "view"):
+        getattr(p, k)[:] = [float(x) for x in cam[k]]
+        getattr(p, "prev_" + k)[:] = [float(x) for x in cam.get("prev_" + k, cam[k])]
+    defaults = dict(max_depth=2, spp=1, samples=0, accumulate=0, frame=0, russian_roulette=0,
+                    rr_start_depth=3, candidates=32, temporal=1, temporal_mcap=200,
+                    spatial_passes=2, spatial_neighbors=5, spatial_radius=30,
+                    row_begin=0, row_end=0, threads=0)
+    defaults.update(kw)
+    for k, v in defaults.items():
+        setattr(p, k, v)
+    return p
+
+
+def render_pt(scene, params):
+    n = params.width * params.height
+    bufs = [np.zeros((n, 4), np.float32) for _ in range(4)]
+    st = RenderStats()
+    lib().oracle_render_pt(ctypes.byref(scene.c), ctypes.byref(params), *[ptr(b) for b in bufs],
+                           ctypes.byref(st))
+    return bufs, st
+
+
+def render_pt_f64(scene, params):
+    out = np.zeros((params.width * params.height, 3), np.float64)
+    st = RenderStats()
+    lib().oracle_render_pt_f64(ctypes.byref(scene.c), ctypes.byref(params), ptr(out), ctypes.byref(st))
+    return out, st
+
+
+class RestirBuffers:
+    """Oracle-side ReSTIR DI state (32-byte SoA reservoirs + per-pixel data)."""
+
+    def __init__(self, n):
+        self.arrays = {
+            "cur_light": np.full(n, -1, np.int32), "cur_point": np.zeros((n, 3), np.float32),
+            "cur_w": np.zeros(n, np.float32), "cur_W": np.zeros(n, np.float32),
+            "cur_M": np.zeros(n, np.int32),
+            "prev_light": np.full(n, -1, np.int32), "prev_point": np.zeros((n, 3), np.float32),
+            "prev_w": np.zeros(n, np.float32), "prev_W": np.zeros(n, np.float32),
+            "prev_M": np.zeros(n, np.int32),
+            "materials": np.zeros((n, 16), np.float32),
+            "intermediate": np.zeros((n, 4), np.float32), "auxiliary": np.zeros((n, 4), np.float32),
+        }
+        self.c = RestirState(*[ptr(self.arrays[f[0]]) for f in RestirState._fields_])
+
+
+def render_restir(scene, params, state, bufs=None):
+    n = params.width * params.height
+    if bufs is None:
+        bufs = [np.zeros((n, 4), np.float32) for _ in range(4)]
+    st = RenderStats()
+    lib().oracle_render_restir(ctypes.byref(scene.c), ctypes.byref(params), ctypes.byref(state.c),
+                               *[ptr(b) for b in bufs], ctypes.byref(st))
+    return bufs, st

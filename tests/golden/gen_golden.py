@@ -1,0 +1,38 @@
+"""Regenerate tests/golden/reference_kat.json from the reference's own headers.
+
+Builds oracle/_ref/ref_kat (oracle/Makefile, target `ref`), which compiles
+include/cuda/random.cuh, include/cuda/math.cuh, include/cuda/brdf.cuh and
+include/optix/lighting.cuh of the reference checkout unmodified on the host,
+runs it and stores its JSON output.  Needs the reference checkout
+(REFERENCE=..., default /root/reference); the committed JSON is what the
+tests read, so this script only runs when the vectors are regenerated.
+
+    python tests/golden/gen_golden.py [--reference PATH]
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default=os.environ.get("REFERENCE", "/root/reference"))
+    args = ap.parse_args()
+    subprocess.check_call(["make", "-C", os.path.join(ROOT, "oracle"), "ref",
+                           "REFERENCE=" + args.reference])
+    out = subprocess.check_output([os.path.join(ROOT, "oracle", "_ref", "ref_kat")])
+    data = json.loads(out)
+    data["_generated_by"] = "tests/golden/gen_golden.py from the reference headers " \
+        "include/cuda/{random,math,brdf}.cuh and include/optix/lighting.cuh"
+    with open(os.path.join(HERE, "reference_kat.json"), "w") as f:
+        json.dump(data, f, indent=0)
+    print("wrote", os.path.join(HERE, "reference_kat.json"), file=sys.stderr)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,142 @@
+"""The CPU oracle against known-answer vectors compiled from the reference's
+own headers (tests/golden/reference_kat.json, made by gen_golden.py from
+include/cuda/random.cuh, math.cuh, brdf.cuh and include/optix/lighting.cuh).
+
+RNG and triangle-test values are exact integer/IEEE arithmetic and must match
+bit for bit.  The BRDF golden values come from the reference code with the C
+library's tanf/cosf/sinf/powf in place of the GPU fast intrinsics, while the
+oracle uses the project's own transcendentals, so they agree to a relative
+1e-5 (both are within a few ulp of the exact function)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "reference_kat.json")
+
+
+@pytest.fixture(scope="module")
+def kat():
+    with open(GOLDEN) as f:
+        return json.load(f)
+
+
+def f32(x):
+    return np.array(x, dtype=np.float32)
+
+
+def test_rng_streams_bit_exact(kat):
+    L = pyoracle.lib()
+    for case in kat["rng"]:
+        out = np.zeros((16, 4), np.float32)
+        s = case["seed"]
+        L.oracle_kat_rng(s[0], s[1], s[2], 16, pyoracle.ptr(out))
+        np.testing.assert_array_equal(out, f32(case["draws"]))
+
+
+def test_rng_integer_seeded_streams(kat):
+    """Seeds {pixel ^ stream, pixel, stream} bit-cast to float3 (the per-pixel
+    PCG stream this project uses) through the reference's rand_uniform_3f."""
+    for case in kat["rng_bits"]:
+        p, s = case["pixel"], case["stream"]
+        bits = np.array([p ^ s, p, s], np.uint32).view(np.float32)
+        # rand_uniform_3f == pcg3f followed by fract (a no-op on [0,1))
+        out = np.zeros((8, 4), np.float32)
+        pyoracle.lib().oracle_kat_rng(float(bits[0]), float(bits[1]), float(bits[2]), 8,
+                                      pyoracle.ptr(out))
+        np.testing.assert_array_equal(out[:, 1:4], f32(case["draws"]))
+
+
+def test_known_answer_from_survey():
+    out = np.zeros((1, 4), np.float32)
+    pyoracle.lib().oracle_kat_rng(1.0, 2.0, 3.0, 1, pyoracle.ptr(out))
+    assert out[0, 0] == np.float32(0.486618757)
+    np.testing.assert_array_equal(out[0, 1:], f32([0.486618757, 0.19627893, 0.857907772]))
+
+
+def test_triangle_intersection_bit_exact(kat):
+    L = pyoracle.lib()
+    hits = 0
+    for case in kat["intersect"]:
+        v = f32(case["v"])
+        o, d = f32(case["o"]), f32(case["d"])
+        b = np.zeros(2, np.float32)
+        t = L.oracle_kat_intersect(pyoracle.ptr(v[0]), pyoracle.ptr(v[1]), pyoracle.ptr(v[2]),
+                                   pyoracle.ptr(o), pyoracle.ptr(d), pyoracle.ptr(b))
+        assert np.float32(t) == np.float32(case["t"])
+        hits += case["t"] > 0
+    assert hits > 50  # the vector set exercises both hits and misses
+
+
+def test_area_light_sampling(kat):
+    L = pyoracle.lib()
+    for case in kat["lights"]:
+        light = np.zeros(12, np.float32)
+        light[0:3], light[3:6], light[6:9] = case["a"], case["ab"], case["ac"]
+        light[9:12] = [1, 2, 3]
+        seed = f32(case["seed"])
+        point = np.zeros(3, np.float32)
+        an = np.zeros(4, np.float32)
+        L.oracle_kat_sample_light(pyoracle.ptr(light), pyoracle.ptr(seed), pyoracle.ptr(point),
+                                  pyoracle.ptr(an))
+        np.testing.assert_array_equal(point, f32(case["point"]))
+        assert an[0] == np.float32(case["area"])
+        np.testing.assert_array_equal(an[1:], f32(case["normal"]))
+
+
+def _material(case):
+    m = np.zeros(16, np.float32)
+    m[0:3] = case["diffuse"]
+    m[3:6] = case["specular"]
+    m[13] = case["roughness"]
+    m[14] = 1.0
+    m[15:16] = np.array([4], np.int32).view(np.float32)  # eDiffuse
+    return m
+
+
+def test_brdf_and_pdf(kat):
+    L = pyoracle.lib()
+    for case in kat["brdf"]:
+        m = _material(case)
+        n, wo, wi = f32(case["n"]), f32(case["wo"]), f32(case["wi_fixed"])
+        out = np.zeros(4, np.float32)
+        L.oracle_kat_brdf(pyoracle.ptr(m), pyoracle.ptr(n), pyoracle.ptr(wo), pyoracle.ptr(wi),
+                          pyoracle.ptr(out))
+        np.testing.assert_allclose(out[:3], f32(case["f_fixed"]), rtol=1e-5, atol=1e-7)
+        np.testing.assert_allclose(out[3], np.float32(case["pdf_fixed"]), rtol=1e-5, atol=1e-7)
+
+
+def test_brdf_sampling_eval(kat):
+    L = pyoracle.lib()
+    for case in kat["brdf"]:
+        m = _material(case)
+        n, wo, seed = f32(case["n"]), f32(case["wo"]), f32(case["seed"])
+        out = np.zeros(10, np.float32)
+        L.oracle_kat_brdf_eval(pyoracle.ptr(m), pyoracle.ptr(n), pyoracle.ptr(wo),
+                               pyoracle.ptr(seed), pyoracle.ptr(out))
+        # the RNG advance is exact
+        np.testing.assert_array_equal(out[7:10], f32(case["seed_after"]))
+        np.testing.assert_allclose(out[3:6], f32(case["wi"]), rtol=1e-5, atol=2e-6)
+        np.testing.assert_allclose(out[0:3], f32(case["f"]), rtol=2e-5, atol=1e-6)
+        np.testing.assert_allclose(out[6], np.float32(case["pdf"]), rtol=2e-5, atol=1e-6)
+
+
+def test_transcendentals_against_float64():
+    xs = np.concatenate([np.linspace(-7, 7, 20001), np.linspace(0, np.pi / 2, 5001)]).astype(np.float32)
+    out = np.zeros((len(xs), 5), np.float32)
+    pyoracle.lib().oracle_kat_math(pyoracle.ptr(xs), len(xs), pyoracle.ptr(out))
+    x = xs.astype(np.float64)
+    for col, ref in ((0, np.sin(x)), (1, np.cos(x)), (3, np.arctan(x))):
+        err = np.abs(out[:, col] - ref)
+        assert np.all(err <= 2.5e-7 * np.maximum(np.abs(ref), 1e-2)), col
+    inside = np.abs(x) <= 1
+    ref = np.arccos(x[inside])
+    err = np.abs(out[inside, 4] - ref)
+    assert np.all(err <= 4e-7 * np.maximum(ref, 1e-3))
+    assert np.all(np.isnan(out[~inside, 4]))
+    safe = np.abs(np.cos(x)) > 1e-2
+    ref = np.tan(x[safe])
+    assert np.all(np.abs(out[safe, 2] - ref) <= 1e-6 * np.maximum(np.abs(ref), 1.0) * 10)

@@ -1,0 +1,1285 @@
+/*
+ * capi.cpp -- the C ABI of include/kgr.h: scenes, traversal entry points,
+ * the path-tracer / ReSTIR attachments and the procedural scene generator.
+ *
+ * The attachment keeps the life cycle of the reference's AttachmentRTX
+ * (include/amadeus/armada.cuh:107-139): attach() learns the extent,
+ * load() allocates the per-pixel state (restir.cuh:203-211), unload() frees
+ * it, render() launches one frame.  Unlike the reference no render call
+ * synchronises the device: every launch is asynchronous on the caller's
+ * stream, and the launch sequence has no host round trip, so a frame can be
+ * captured into a CUDA graph.
+ */
+#include <math.h>
+#include <string.h>
+
+#include <chrono>
+#include <cstdio>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <string>
+#include <variant>
+
+#include "kgr_internal.h"
+#include "kgr_wavefront.h"
+
+namespace kgr {
+void generate_scene(const std::string &name, uint64_t seed, kgr_generated *g);
+}
+
+namespace kgr {
+
+static thread_local std::string g_last_error;
+
+void set_last_error(const std::string &msg) { g_last_error = msg; }
+
+DeviceGuard::DeviceGuard(int device)
+{
+	if (device < 0)
+		return;
+	cudaGetDevice(&prev);
+	if (prev != device)
+		KGR_CUDA(cudaSetDevice(device));
+	else
+		prev = -1;
+}
+
+DeviceGuard::~DeviceGuard()
+{
+	if (prev >= 0)
+		cudaSetDevice(prev);
+}
+
+template <class F>
+static kgr_status guarded(F &&f)
+{
+	try {
+		f();
+		return KGR_OK;
+	} catch (const Error &e) {
+		set_last_error(e.what());
+		return e.status;
+	} catch (const std::bad_alloc &) {
+		set_last_error("host allocation failed");
+		return KGR_ERR_OUT_OF_MEMORY;
+	} catch (const std::exception &e) {
+		set_last_error(e.what());
+		return KGR_ERR_INTERNAL;
+	}
+}
+
+static int resolve_device(int device)
+{
+	int count = 0;
+	cudaError_t e = cudaGetDeviceCount(&count);
+	if (e != cudaSuccess || count == 0) {
+		cudaGetLastError();
+		throw Error(KGR_ERR_NO_DEVICE, "no CUDA device available");
+	}
+	if (device < 0)
+		KGR_CUDA(cudaGetDevice(&device));
+	KGR_REQUIRE(device < count, KGR_ERR_INVALID_ARGUMENT, "device ordinal out of range");
+	return device;
+}
+
+static bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
+} /* namespace kgr */
+
+using namespace kgr;
+
+/* ================================================================ scene == */
+
+kgr::DeviceScene kgr_scene::view() const
+{
+	DeviceScene s;
+	s.positions = d_positions.ptr;
+	s.normals = d_normals.ptr;
+	s.tris = d_tris.ptr;
+	s.bvh = d_bvh.ptr;
+	s.fast_nodes = d_fast_nodes.ptr;
+	s.fast_tris = d_fast_tris.ptr;
+	s.materials = d_materials.ptr;
+	s.lights = d_lights.ptr;
+	s.triangle_count = (uint32_t)(tris4.size() / 4);
+	s.light_count = (uint32_t)lights.size();
+	s.bvh_vec4_count = (uint32_t)(bvh.size() / 4);
+	s.fast_node_count = fast_node_count;
+	return s;
+}
+
+uint64_t kgr_scene::device_bytes() const
+{
+	return d_positions.bytes() + d_normals.bytes() + d_tris.bytes() + d_bvh.bytes() + d_fast_tris.bytes()
+		+ d_fast_nodes.bytes() + d_materials.bytes() + d_lights.bytes();
+}
+
+namespace {
+
+/* glm::mat4 * vec4(p, w), columns summed in order */
+void transform_point(const float *m, const float *p, float w, float *out)
+{
+	for (int i = 0; i < 3; i++)
+		out[i] = m[0 * 4 + i] * p[0] + m[1 * 4 + i] * p[1] + m[2 * 4 + i] * p[2] + m[3 * 4 + i] * w;
+}
+
+void gather_meshes(kgr_scene *sc, const kgr_mesh *meshes, uint32_t mesh_count, const kgr_material *materials,
+		uint32_t material_count)
+{
+	KGR_REQUIRE(mesh_count == 0 || meshes, KGR_ERR_INVALID_ARGUMENT, "meshes is NULL");
+	KGR_REQUIRE(material_count > 0 && materials, KGR_ERR_INVALID_ARGUMENT, "at least one material is required");
+	sc->materials.assign(materials, materials + material_count);
+	uint64_t vtotal = 0, ttotal = 0;
+	for (uint32_t m = 0; m < mesh_count; m++) {
+		vtotal += meshes[m].vertex_count;
+		ttotal += meshes[m].triangle_count;
+	}
+	KGR_REQUIRE(ttotal < (1ull << 27), KGR_ERR_UNSUPPORTED, "more than 2^27 triangles");
+	sc->positions.resize(3 * vtotal);
+	sc->normals.resize(3 * vtotal);
+	sc->tris4.resize(4 * ttotal);
+	uint64_t vb = 0, tb = 0;
+	for (uint32_t m = 0; m < mesh_count; m++) {
+		const kgr_mesh &me = meshes[m];
+		KGR_REQUIRE(me.vertex_count == 0 || me.positions, KGR_ERR_INVALID_ARGUMENT, "mesh positions are NULL");
+		KGR_REQUIRE(me.triangle_count == 0 || me.indices, KGR_ERR_INVALID_ARGUMENT, "mesh indices are NULL");
+		for (uint32_t v = 0; v < me.vertex_count; v++) {
+			float *pp = &sc->positions[3 * (vb + v)];
+			float *nn = &sc->normals[3 * (vb + v)];
+			if (me.model) {
+				transform_point(me.model, me.positions + 3 * (size_t)v, 1.0f, pp);
+				if (me.normals)
+					transform_point(me.model, me.normals + 3 * (size_t)v, 0.0f, nn);
+			} else {
+				memcpy(pp, me.positions + 3 * (size_t)v, 12);
+				if (me.normals)
+					memcpy(nn, me.normals + 3 * (size_t)v, 12);
+			}
+		}
+		for (uint32_t t = 0; t < me.triangle_count; t++) {
+			uint32_t *o = &sc->tris4[4 * (tb + t)];
+			for (int k = 0; k < 3; k++) {
+				uint32_t idx = me.indices[3 * (size_t)t + k];
+				KGR_REQUIRE(idx < me.vertex_count, KGR_ERR_INVALID_ARGUMENT,
+					"triangle index out of range in mesh " + std::to_string(m));
+				o[k] = (uint32_t)(vb + idx);
+			}
+			uint32_t mat = me.material_indices ? me.material_indices[t] : 0;
+			KGR_REQUIRE(mat < material_count, KGR_ERR_INVALID_ARGUMENT, "material index out of range");
+			o[3] = mat;
+			if (!me.normals) {
+				/* face normal for every vertex of a mesh without normals */
+				const float *a = &sc->positions[3 * o[0]], *b = &sc->positions[3 * o[1]],
+					    *c = &sc->positions[3 * o[2]];
+				float e1[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+				float e2[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+				float n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
+					e1[0] * e2[1] - e1[1] * e2[0]};
+				for (int k = 0; k < 3; k++)
+					memcpy(&sc->normals[3 * o[k]], n, 12);
+			}
+		}
+		vb += me.vertex_count;
+		tb += me.triangle_count;
+	}
+	/* triangle lights in triangle order (armada.cu:98-212) */
+	sc->lights.clear();
+	for (uint64_t t = 0; t < ttotal; t++) {
+		const uint32_t *o = &sc->tris4[4 * t];
+		const kgr_material &m = sc->materials[o[3]];
+		if (!(m.emission[0] > 0 || m.emission[1] > 0 || m.emission[2] > 0))
+			continue;
+		const float *a = &sc->positions[3 * o[0]], *b = &sc->positions[3 * o[1]], *c = &sc->positions[3 * o[2]];
+		kgr_triangle_light l;
+		for (int k = 0; k < 3; k++) {
+			l.a[k] = a[k];
+			l.ab[k] = b[k] - a[k];
+			l.ac[k] = c[k] - a[k];
+			l.intensity[k] = m.emission[k];
+		}
+		sc->lights.push_back(l);
+	}
+	for (int k = 0; k < 3; k++) {
+		sc->bounds_min[k] = INFINITY;
+		sc->bounds_max[k] = -INFINITY;
+	}
+	for (uint64_t v = 0; v < vtotal; v++)
+		for (int k = 0; k < 3; k++) {
+			sc->bounds_min[k] = fminf(sc->bounds_min[k], sc->positions[3 * v + k]);
+			sc->bounds_max[k] = fmaxf(sc->bounds_max[k], sc->positions[3 * v + k]);
+		}
+}
+
+/* Submesh::bvh boxes (include/mesh.hpp:48-78): min(p1, min(p2, p3)) */
+std::vector<PrimBox> prim_boxes(const kgr_scene *sc)
+{
+	size_t n = sc->tris4.size() / 4;
+	std::vector<PrimBox> boxes(n);
+	auto gmin = [](float a, float b) { return b < a ? b : a; };
+	auto gmax = [](float a, float b) { return a < b ? b : a; };
+	for (size_t i = 0; i < n; i++) {
+		const float *a = &sc->positions[3 * sc->tris4[4 * i]];
+		const float *b = &sc->positions[3 * sc->tris4[4 * i + 1]];
+		const float *c = &sc->positions[3 * sc->tris4[4 * i + 2]];
+		for (int k = 0; k < 3; k++) {
+			boxes[i].bmin[k] = gmin(a[k], gmin(b[k], c[k]));
+			boxes[i].bmax[k] = gmax(a[k], gmax(b[k], c[k]));
+		}
+	}
+	return boxes;
+}
+
+uint32_t tree_depth(const Tree &t)
+{
+	if (t.nodes.empty())
+		return 0;
+	uint32_t best = 0;
+	std::vector<std::pair<int32_t, uint32_t>> st = {{0, 1}};
+	while (!st.empty()) {
+		auto [i, d] = st.back();
+		st.pop_back();
+		best = d > best ? d : best;
+		if (!t.nodes[i].count) {
+			st.push_back({t.nodes[i].left, d + 1});
+			st.push_back({t.nodes[i].right, d + 1});
+		}
+	}
+	return best;
+}
+
+void finish_scene(kgr_scene *sc, const Tree &tree, const std::vector<PrimBox> &boxes)
+{
+	KGR_REQUIRE(tree_depth(tree) < KGR_STACK_DEPTH_HOST, KGR_ERR_UNSUPPORTED,
+		"BVH deeper than the traversal stack (" + std::to_string(tree_depth(tree)) + " levels)");
+	std::vector<FastNode> nodes;
+	std::vector<float4> tri_records;
+	build_fast(tree, boxes, sc->positions.data(), sc->tris4.data(), nodes, tri_records);
+	sc->fast_node_count = (uint32_t)nodes.size();
+	size_t nv = sc->positions.size() / 3, nt = sc->tris4.size() / 4;
+	std::vector<float4> p4(nv), n4(nv);
+	for (size_t v = 0; v < nv; v++) {
+		p4[v] = make_float4(sc->positions[3 * v], sc->positions[3 * v + 1], sc->positions[3 * v + 2], 0.0f);
+		n4[v] = make_float4(sc->normals[3 * v], sc->normals[3 * v + 1], sc->normals[3 * v + 2], 0.0f);
+	}
+	sc->d_positions.upload(p4);
+	sc->d_normals.upload(n4);
+	sc->d_tris.upload(reinterpret_cast<const uint4 *>(sc->tris4.data()), nt);
+	sc->d_bvh.upload(reinterpret_cast<const float4 *>(sc->bvh.data()), sc->bvh.size() / 4);
+	sc->d_fast_nodes.upload(nodes);
+	sc->d_fast_tris.upload(tri_records);
+	sc->d_materials.upload(sc->materials);
+	sc->d_lights.upload(sc->lights);
+}
+
+} /* namespace */
+
+extern "C" {
+
+const char *kgr_status_string(kgr_status s)
+{
+	switch (s) {
+	case KGR_OK: return "ok";
+	case KGR_ERR_INVALID_ARGUMENT: return "invalid argument";
+	case KGR_ERR_OUT_OF_MEMORY: return "out of memory";
+	case KGR_ERR_CUDA: return "CUDA error";
+	case KGR_ERR_UNSUPPORTED: return "unsupported";
+	case KGR_ERR_NOT_ATTACHED: return "attachment not attached";
+	case KGR_ERR_NOT_LOADED: return "attachment not loaded";
+	case KGR_ERR_BVH_FORMAT: return "malformed BVH";
+	case KGR_ERR_BUDGET: return "over memory budget";
+	case KGR_ERR_TIMEOUT: return "timed out";
+	case KGR_ERR_UNKNOWN_OPTION: return "unknown option";
+	case KGR_ERR_TYPE: return "wrong option type";
+	case KGR_ERR_INTERNAL: return "internal error";
+	case KGR_ERR_NO_DEVICE: return "no CUDA device";
+	}
+	return "unknown status";
+}
+
+const char *kgr_last_error(void) { return g_last_error.c_str(); }
+
+int kgr_abi_version(void) { return KGR_ABI_VERSION; }
+
+kgr_status kgr_scene_create(const kgr_mesh *meshes, uint32_t mesh_count, const kgr_material *materials,
+		uint32_t material_count, const kgr_scene_options *options, kgr_scene **out)
+{
+	return guarded([&] {
+		KGR_REQUIRE(out, KGR_ERR_INVALID_ARGUMENT, "out is NULL");
+		*out = nullptr;
+		kgr_scene_options opt = {KGR_BUILDER_SAH, 4, -1, 0};
+		if (options)
+			opt = *options;
+		int max_leaf = opt.max_leaf_size ? opt.max_leaf_size : 4;
+		KGR_REQUIRE(max_leaf >= 1 && max_leaf <= 8, KGR_ERR_INVALID_ARGUMENT, "max_leaf_size must be 1..8");
+		KGR_REQUIRE(opt.builder == KGR_BUILDER_SAH || opt.builder == KGR_BUILDER_KOBRA,
+			KGR_ERR_INVALID_ARGUMENT, "unknown builder");
+		int device = resolve_device(opt.device);
+		DeviceGuard guard(device);
+		std::unique_ptr<kgr_scene> sc(new kgr_scene());
+		sc->device = device;
+		gather_meshes(sc.get(), meshes, mesh_count, materials, material_count);
+		auto t0 = std::chrono::steady_clock::now();
+		std::vector<PrimBox> boxes = prim_boxes(sc.get());
+		Tree tree;
+		if (opt.builder == KGR_BUILDER_KOBRA)
+			build_kobra(boxes, tree);
+		else
+			build_sah(boxes, max_leaf, tree);
+		serialize_threaded(tree, boxes, sc->bvh);
+		sc->build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+		finish_scene(sc.get(), tree, boxes);
+		*out = sc.release();
+	});
+}
+
+kgr_status kgr_scene_create_from_bvh(const kgr_mesh *meshes, uint32_t mesh_count, const kgr_material *materials,
+		uint32_t material_count, const float *bvh_vec4, uint32_t bvh_vec4_count, int32_t device,
+		kgr_scene **out)
+{
+	return guarded([&] {
+		KGR_REQUIRE(out, KGR_ERR_INVALID_ARGUMENT, "out is NULL");
+		*out = nullptr;
+		KGR_REQUIRE(bvh_vec4 || bvh_vec4_count == 0, KGR_ERR_INVALID_ARGUMENT, "bvh is NULL");
+		int dev = resolve_device(device);
+		DeviceGuard guard(dev);
+		std::unique_ptr<kgr_scene> sc(new kgr_scene());
+		sc->device = dev;
+		gather_meshes(sc.get(), meshes, mesh_count, materials, material_count);
+		auto t0 = std::chrono::steady_clock::now();
+		std::vector<PrimBox> boxes = prim_boxes(sc.get());
+		Tree tree;
+		parse_threaded(bvh_vec4, bvh_vec4_count, (uint32_t)boxes.size(), boxes, tree);
+		sc->bvh.assign(bvh_vec4, bvh_vec4 + 4 * (size_t)bvh_vec4_count);
+		sc->build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+		finish_scene(sc.get(), tree, boxes);
+		*out = sc.release();
+	});
+}
+
+kgr_status kgr_bvh_build_host(const float *positions, uint32_t vertex_count, const uint32_t *indices,
+		uint32_t triangle_count, int32_t builder, int32_t max_leaf_size, float *out_vec4, uint32_t capacity,
+		uint32_t *count)
+{
+	return guarded([&] {
+		KGR_REQUIRE(count && (positions || vertex_count == 0) && (indices || triangle_count == 0),
+			KGR_ERR_INVALID_ARGUMENT, "NULL argument");
+		int max_leaf = max_leaf_size ? max_leaf_size : 4;
+		KGR_REQUIRE(max_leaf >= 1 && max_leaf <= 8, KGR_ERR_INVALID_ARGUMENT, "max_leaf_size must be 1..8");
+		kgr_scene sc;
+		kgr_material m;
+		memset(&m, 0, sizeof(m));
+		kgr_mesh mesh = {positions, nullptr, vertex_count, indices, nullptr, triangle_count, nullptr};
+		gather_meshes(&sc, &mesh, 1, &m, 1);
+		std::vector<PrimBox> boxes = prim_boxes(&sc);
+		Tree tree;
+		if (builder == KGR_BUILDER_KOBRA)
+			build_kobra(boxes, tree);
+		else
+			build_sah(boxes, max_leaf, tree);
+		std::vector<float> buf;
+		serialize_threaded(tree, boxes, buf);
+		*count = (uint32_t)(buf.size() / 4);
+		if (out_vec4) {
+			KGR_REQUIRE(capacity >= *count, KGR_ERR_INVALID_ARGUMENT, "capacity too small");
+			memcpy(out_vec4, buf.data(), buf.size() * sizeof(float));
+		}
+	});
+}
+
+kgr_status kgr_scene_info_get(const kgr_scene *sc, kgr_scene_info *info)
+{
+	return guarded([&] {
+		KGR_REQUIRE(sc && info, KGR_ERR_INVALID_ARGUMENT, "NULL argument");
+		info->vertex_count = (uint32_t)(sc->positions.size() / 3);
+		info->triangle_count = (uint32_t)(sc->tris4.size() / 4);
+		info->light_count = (uint32_t)sc->lights.size();
+		info->material_count = (uint32_t)sc->materials.size();
+		info->bvh_vec4_count = (uint32_t)(sc->bvh.size() / 4);
+		info->fast_node_count = sc->fast_node_count;
+		info->device_bytes = sc->device_bytes();
+		info->build_ms = sc->build_ms;
+		memcpy(info->bounds_min, sc->bounds_min, 12);
+		memcpy(info->bounds_max, sc->bounds_max, 12);
+	});
+}
+
+kgr_status kgr_scene_copy_bvh(const kgr_scene *sc, float *out_vec4, uint32_t capacity, uint32_t *count)
+{
+	return guarded([&] {
+		KGR_REQUIRE(sc && count, KGR_ERR_INVALID_ARGUMENT, "NULL argument");
+		uint32_t n = (uint32_t)(sc->bvh.size() / 4);
+		*count = n;
+		if (out_vec4) {
+			KGR_REQUIRE(capacity >= n, KGR_ERR_INVALID_ARGUMENT, "capacity too small");
+			memcpy(out_vec4, sc->bvh.data(), sc->bvh.size() * sizeof(float));
+		}
+	});
+}
+
+kgr_status kgr_scene_copy_lights(const kgr_scene *sc, kgr_triangle_light *out, uint32_t capacity, uint32_t *count)
+{
+	return guarded([&] {
+		KGR_REQUIRE(sc && count, KGR_ERR_INVALID_ARGUMENT, "NULL argument");
+		*count = (uint32_t)sc->lights.size();
+		if (out) {
+			KGR_REQUIRE(capacity >= sc->lights.size(), KGR_ERR_INVALID_ARGUMENT, "capacity too small");
+			memcpy(out, sc->lights.data(), sc->lights.size() * sizeof(kgr_triangle_light));
+		}
+	});
+}
+
+kgr_status kgr_scene_destroy(kgr_scene *sc)
+{
+	return guarded([&] {
+		if (!sc)
+			return;
+		DeviceGuard guard(sc->device);
+		delete sc;
+	});
+}
+
+/* ============================================================ traversal == */
+
+kgr_status kgr_trace_closest(const kgr_scene *sc, const float *rays, uint32_t n, kgr_hit *hits, int32_t layout,
+		void *stream)
+{
+	return guarded([&] {
+		KGR_REQUIRE(sc, KGR_ERR_INVALID_ARGUMENT, "scene is NULL");
+		KGR_REQUIRE(n == 0 || (rays && hits), KGR_ERR_INVALID_ARGUMENT, "NULL buffer");
+		KGR_REQUIRE(aligned16(rays) && aligned16(hits), KGR_ERR_INVALID_ARGUMENT, "buffers must be 16-byte aligned");
+		KGR_REQUIRE(layout == KGR_LAYOUT_FAST || layout == KGR_LAYOUT_THREADED, KGR_ERR_INVALID_ARGUMENT, "unknown layout");
+		DeviceGuard guard(sc->device);
+		launch_trace_closest(sc->view(), reinterpret_cast<const float4 *>(rays), n, hits, layout,
+			(cudaStream_t)stream);
+	});
+}
+
+kgr_status kgr_trace_any(const kgr_scene *sc, const float *rays, uint32_t n, uint32_t *occluded, int32_t layout,
+		void *stream)
+{
+	return guarded([&] {
+		KGR_REQUIRE(sc, KGR_ERR_INVALID_ARGUMENT, "scene is NULL");
+		KGR_REQUIRE(n == 0 || (rays && occluded), KGR_ERR_INVALID_ARGUMENT, "NULL buffer");
+		KGR_REQUIRE(aligned16(rays), KGR_ERR_INVALID_ARGUMENT, "rays must be 16-byte aligned");
+		KGR_REQUIRE(layout == KGR_LAYOUT_FAST || layout == KGR_LAYOUT_THREADED, KGR_ERR_INVALID_ARGUMENT, "unknown layout");
+		DeviceGuard guard(sc->device);
+		launch_trace_any(sc->view(), reinterpret_cast<const float4 *>(rays), n, occluded, layout,
+			(cudaStream_t)stream);
+	});
+}
+
+kgr_status kgr_trace_closest_host(const kgr_scene *sc, const float *rays, uint32_t n, kgr_hit *hits, int32_t layout)
+{
+	return guarded([&] {
+		KGR_REQUIRE(sc, KGR_ERR_INVALID_ARGUMENT, "scene is NULL");
+		KGR_REQUIRE(n == 0 || (rays && hits), KGR_ERR_INVALID_ARGUMENT, "NULL buffer");
+		KGR_REQUIRE(layout == KGR_LAYOUT_FAST || layout == KGR_LAYOUT_THREADED, KGR_ERR_INVALID_ARGUMENT, "unknown layout");
+		if (n == 0)
+			return;
+		DeviceGuard guard(sc->device);
+		DevBuf<float4> dr;
+		DevBuf<kgr_hit> dh;
+		dr.upload(reinterpret_cast<const float4 *>(rays), 2 * (size_t)n);
+		dh.alloc(n);
+		launch_trace_closest(sc->view(), dr.ptr, n, dh.ptr, layout, 0);
+		KGR_CUDA(cudaMemcpy(hits, dh.ptr, n * sizeof(kgr_hit), cudaMemcpyDeviceToHost));
+	});
+}
+
+kgr_status kgr_trace_any_host(const kgr_scene *sc, const float *rays, uint32_t n, uint32_t *occluded, int32_t layout)
+{
+	return guarded([&] {
+		KGR_REQUIRE(sc, KGR_ERR_INVALID_ARGUMENT, "scene is NULL");
+		KGR_REQUIRE(n == 0 || (rays && occluded), KGR_ERR_INVALID_ARGUMENT, "NULL buffer");
+		KGR_REQUIRE(layout == KGR_LAYOUT_FAST || layout == KGR_LAYOUT_THREADED, KGR_ERR_INVALID_ARGUMENT, "unknown layout");
+		if (n == 0)
+			return;
+		DeviceGuard guard(sc->device);
+		DevBuf<float4> dr;
+		DevBuf<uint32_t> dout;
+		dr.upload(reinterpret_cast<const float4 *>(rays), 2 * (size_t)n);
+		dout.alloc(n);
+		launch_trace_any(sc->view(), dr.ptr, n, dout.ptr, layout, 0);
+		KGR_CUDA(cudaMemcpy(occluded, dout.ptr, n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+	});
+}
+
+kgr_status kgr_trace_counts(const kgr_scene *sc, const float *rays, uint32_t n, int32_t any, uint64_t *counts)
+{
+	return guarded([&] {
+		KGR_REQUIRE(sc && counts, KGR_ERR_INVALID_ARGUMENT, "NULL argument");
+		KGR_REQUIRE(n == 0 || rays, KGR_ERR_INVALID_ARGUMENT, "rays is NULL");
+		DeviceGuard guard(sc->device);
+		DevBuf<unsigned long long> dc;
+		dc.alloc(4);
+		KGR_CUDA(cudaMemset(dc.ptr, 0, 4 * sizeof(unsigned long long)));
+		launch_trace_stats(sc->view(), reinterpret_cast<const float4 *>(rays), n, any, dc.ptr, 0);
+		KGR_CUDA(cudaMemcpy(counts, dc.ptr, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+	});
+}
+
+} /* extern "C" */
+
+/* ========================================================== attachments == */
+
+namespace {
+
+enum Kind { KIND_PT = 0, KIND_RESTIR_DI = 1, KIND_RESTIR_GI = 2 };
+
+using OptionValue = std::variant<int, float, bool, std::string>;
+
+struct Timing {
+	cudaEvent_t ev[2] = {nullptr, nullptr};
+};
+
+} /* namespace */
+
+struct kgr_attachment {
+	Kind kind;
+	std::string name;
+	bool attached = false, loaded = false;
+	uint32_t width = 0, height = 0;
+	int device = 0;
+	std::map<std::string, OptionValue> options;
+	std::string option_string; /* storage for get_option strings */
+
+	/* path state */
+	DevBuf<float4> f4[14];
+	DevBuf<uint32_t> queues[3];
+	DevBuf<uint32_t> counters;
+	uint32_t capacity = 0;
+
+	/* ReSTIR state */
+	DevBuf<float4> res_a[2], res_b[2], intermediate, auxiliary;
+	DevBuf<kgr_material> pixel_materials;
+	int prev_index = 1;
+	bool have_prev_camera = false;
+	float prev_projection[16], prev_view[16];
+
+	kgr_render_stats stats = {0, 0, 0, 0, 0};
+	uint32_t last_paths = 0;
+	cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+
+	/* per-launch timing: one event after every launch, tagged by stage */
+	std::vector<cudaEvent_t> event_pool;
+	std::vector<int> event_kinds; /* kind of the launch that ends at event i; -1 = start */
+	double stage_ms[STAGE_COUNT] = {0};
+	uint32_t stage_launches[STAGE_COUNT] = {0};
+	DevBuf<unsigned long long> visits;
+
+	bool profiling() const { return opt_int("profile", 0) != 0; }
+	void mark(int kind, cudaStream_t st)
+	{
+		if (!profiling())
+			return;
+		size_t i = event_kinds.size();
+		if (i == event_pool.size()) {
+			cudaEvent_t e;
+			KGR_CUDA(cudaEventCreate(&e));
+			event_pool.push_back(e);
+		}
+		KGR_CUDA(cudaEventRecord(event_pool[i], st));
+		event_kinds.push_back(kind);
+	}
+	/* fold recorded events into per-stage totals (synchronises on the last event) */
+	void collect_times()
+	{
+		if (event_kinds.empty())
+			return;
+		KGR_CUDA(cudaEventSynchronize(event_pool[event_kinds.size() - 1]));
+		for (size_t i = 1; i < event_kinds.size(); i++) {
+			int k = event_kinds[i];
+			if (k < 0)
+				continue;
+			float ms = 0.0f;
+			KGR_CUDA(cudaEventElapsedTime(&ms, event_pool[i - 1], event_pool[i]));
+			stage_ms[k] += ms;
+			stage_launches[k]++;
+		}
+		event_kinds.clear();
+	}
+
+	int opt_int(const char *k, int def) const
+	{
+		auto it = options.find(k);
+		if (it == options.end())
+			return def;
+		if (auto p = std::get_if<int>(&it->second))
+			return *p;
+		if (auto b = std::get_if<bool>(&it->second))
+			return *b ? 1 : 0;
+		return def;
+	}
+	std::string opt_str(const char *k, const std::string &def) const
+	{
+		auto it = options.find(k);
+		if (it == options.end())
+			return def;
+		if (auto p = std::get_if<std::string>(&it->second))
+			return *p;
+		return def;
+	}
+	int layout() const { return opt_str("layout", "fast") == "threaded" ? KGR_LAYOUT_THREADED : KGR_LAYOUT_FAST; }
+
+	PathBuffers path_buffers()
+	{
+		PathBuffers pb;
+		float4 **fields[14] = {&pb.ray_o, &pb.ray_d, &pb.beta, &pb.L, &pb.seed, &pb.hit, &pb.sh_o, &pb.sh_d,
+			&pb.pend_c, &pb.pend_e, &pb.pend_b, &pb.aov_n, &pb.aov_a, &pb.aov_p};
+		for (int k = 0; k < 14; k++)
+			*fields[k] = f4[k].ptr;
+		pb.queue[0] = queues[0].ptr;
+		pb.queue[1] = queues[1].ptr;
+		pb.shadow_queue = queues[2].ptr;
+		pb.counters = counters.ptr;
+		if (opt_int("count_visits", 0) && !visits.ptr)
+			visits.alloc(4);
+		pb.visits = opt_int("count_visits", 0) ? visits.ptr : nullptr;
+		pb.capacity = capacity;
+		return pb;
+	}
+
+	void ensure_paths(uint32_t paths)
+	{
+		if (paths <= capacity)
+			return;
+		for (auto &b : f4)
+			b.alloc(paths);
+		for (auto &q : queues)
+			q.alloc(paths);
+		capacity = paths;
+	}
+
+	void release_all()
+	{
+		for (auto &b : f4)
+			b.release();
+		for (auto &q : queues)
+			q.release();
+		counters.release();
+		for (int k = 0; k < 2; k++) {
+			res_a[k].release();
+			res_b[k].release();
+		}
+		intermediate.release();
+		auxiliary.release();
+		pixel_materials.release();
+		capacity = 0;
+	}
+
+	~kgr_attachment()
+	{
+		release_all();
+		visits.release();
+		if (ev_start)
+			cudaEventDestroy(ev_start);
+		if (ev_stop)
+			cudaEventDestroy(ev_stop);
+		for (cudaEvent_t e : event_pool)
+			cudaEventDestroy(e);
+	}
+};
+
+namespace {
+
+void mat4_mul(const float *a, const float *b, float *out)
+{
+	for (int j = 0; j < 4; j++)
+		for (int i = 0; i < 4; i++)
+			out[j * 4 + i] = a[0 * 4 + i] * b[j * 4 + 0] + a[1 * 4 + i] * b[j * 4 + 1]
+				+ a[2 * 4 + i] * b[j * 4 + 2] + a[3 * 4 + i] * b[j * 4 + 3];
+}
+
+void check_launch(const kgr_attachment *att, const kgr_launch_info *info, const kgr_scene *sc)
+{
+	KGR_REQUIRE(att, KGR_ERR_INVALID_ARGUMENT, "attachment is NULL");
+	KGR_REQUIRE(att->attached, KGR_ERR_NOT_ATTACHED, "attach() was not called");
+	KGR_REQUIRE(att->loaded, KGR_ERR_NOT_LOADED, "load() was not called");
+	KGR_REQUIRE(info && sc, KGR_ERR_INVALID_ARGUMENT, "NULL launch info or scene");
+	KGR_REQUIRE(sc->device == att->device, KGR_ERR_INVALID_ARGUMENT, "scene and attachment are on different devices");
+	KGR_REQUIRE((uint32_t)info->resolution[0] == att->width && (uint32_t)info->resolution[1] == att->height,
+		KGR_ERR_INVALID_ARGUMENT, "resolution differs from the attached extent");
+	KGR_REQUIRE(!info->has_environment_map, KGR_ERR_UNSUPPORTED, "environment maps are not supported");
+	KGR_REQUIRE(info->lights.quad_count == 0, KGR_ERR_UNSUPPORTED, "quad lights are not supported");
+	KGR_REQUIRE(info->buffers.color, KGR_ERR_INVALID_ARGUMENT, "color buffer is NULL");
+	const void *bufs[4] = {info->buffers.color, info->buffers.normal, info->buffers.albedo, info->buffers.position};
+	for (const void *b : bufs)
+		KGR_REQUIRE(aligned16(b), KGR_ERR_INVALID_ARGUMENT, "output buffers must be 16-byte aligned");
+	KGR_REQUIRE(info->max_depth >= 0 && info->max_depth <= 64, KGR_ERR_INVALID_ARGUMENT, "max_depth out of range");
+}
+
+FrameParams frame_params(const kgr_attachment *att, const kgr_launch_info *info)
+{
+	FrameParams fp;
+	memset(&fp, 0, sizeof(fp));
+	fp.width = att->width;
+	fp.height = att->height;
+	fp.npix = att->width * att->height;
+	memcpy(fp.center, info->camera.center, 12);
+	memcpy(fp.U, info->camera.ax_u, 12);
+	memcpy(fp.V, info->camera.ax_v, 12);
+	memcpy(fp.W, info->camera.ax_w, 12);
+	int md = att->opt_int("max_depth", -1);
+	fp.max_depth = md >= 0 ? md : info->max_depth;
+	fp.russian_roulette = att->opt_int("russian_roulette", 0);
+	fp.rr_start_depth = att->opt_int("rr_start_depth", 3);
+	fp.frame = info->frame;
+	fp.accumulate = info->accumulate ? 1 : 0;
+	fp.samples = info->samples;
+	fp.layout = att->layout();
+	fp.candidates = att->opt_int("candidates", 32);
+	fp.temporal = att->opt_int("temporal", 1);
+	fp.temporal_mcap = att->opt_int("temporal_mcap", 200);
+	fp.spatial_neighbors = att->opt_int("spatial_neighbors", 5);
+	fp.spatial_radius = att->opt_int("spatial_radius", 30);
+	return fp;
+}
+
+DeviceScene scene_for_launch(const kgr_scene *sc, const kgr_launch_info *info)
+{
+	DeviceScene s = sc->view();
+	if (info->lights.tri_lights) {
+		s.lights = info->lights.tri_lights;
+		s.light_count = (uint32_t)info->lights.tri_count;
+	}
+	if (info->materials)
+		s.materials = info->materials;
+	return s;
+}
+
+/* Zero the visit counters at the start of a frame when counting is on. */
+void prepare_visits(kgr_attachment *att, cudaStream_t st)
+{
+	if (!att->opt_int("count_visits", 0))
+		return;
+	if (!att->visits.ptr)
+		att->visits.alloc(4);
+	KGR_CUDA(cudaMemsetAsync(att->visits.ptr, 0, 4 * sizeof(unsigned long long), st));
+}
+
+void render_pt(kgr_attachment *att, const kgr_launch_info *info, const kgr_scene *sc, cudaStream_t st)
+{
+	FrameParams fp = frame_params(att, info);
+	int spp = att->opt_int("spp", 1);
+	KGR_REQUIRE(spp >= 1 && spp <= 4096, KGR_ERR_INVALID_ARGUMENT, "spp out of range");
+	uint64_t paths = (uint64_t)fp.npix * (uint64_t)spp;
+	KGR_REQUIRE(paths < (1ull << 31), KGR_ERR_UNSUPPORTED, "too many paths per frame");
+	fp.spp = (uint32_t)spp;
+	fp.paths = (uint32_t)paths;
+	fp.jitter = 1;
+	att->ensure_paths(fp.paths);
+	PathBuffers pb = att->path_buffers();
+	DeviceScene s = scene_for_launch(sc, info);
+	OutputBuffers out = {reinterpret_cast<float4 *>(info->buffers.color),
+		reinterpret_cast<float4 *>(info->buffers.normal), reinterpret_cast<float4 *>(info->buffers.albedo),
+		reinterpret_cast<float4 *>(info->buffers.position)};
+	uint32_t launches = 0;
+	prepare_visits(att, st);
+	att->mark(-1, st);
+	pt_generate(pb, fp, st);
+	att->mark(STAGE_GENERATE, st);
+	launches++;
+	for (int d = 0; d <= fp.max_depth; d++) {
+		int q = d & 1;
+		if (d > 0) {
+			reset_counters(pb, (1 << (q ^ 1)) | (1 << CNT_SHADOW), st);
+			att->mark(-1, st);
+		}
+		pt_trace_closest(s, pb, q, fp.layout, st);
+		att->mark(STAGE_TRACE_CLOSEST, st);
+		pt_shade(s, pb, fp, d, q, st);
+		att->mark(STAGE_SHADE, st);
+		pt_shadow_resolve(s, pb, fp.layout, st);
+		att->mark(STAGE_SHADOW, st);
+		launches += 3;
+	}
+	pt_accumulate(pb, fp, out, st);
+	att->mark(STAGE_ACCUMULATE, st);
+	launches++;
+	att->stats.kernel_launches = launches;
+	att->stats.camera_rays = fp.paths;
+	att->last_paths = fp.paths;
+}
+
+void render_restir_di(kgr_attachment *att, const kgr_launch_info *info, const kgr_scene *sc, cudaStream_t st)
+{
+	FrameParams fp = frame_params(att, info);
+	fp.spp = 1;
+	fp.paths = fp.npix;
+	fp.jitter = 0;
+	KGR_REQUIRE(fp.spatial_neighbors >= 0 && fp.spatial_neighbors <= 16, KGR_ERR_INVALID_ARGUMENT,
+		"spatial_neighbors must be 0..16");
+	KGR_REQUIRE(fp.candidates >= 1 && fp.candidates <= 1024, KGR_ERR_INVALID_ARGUMENT, "candidates must be 1..1024");
+	KGR_REQUIRE(info->buffers.normal && info->buffers.albedo && info->buffers.position, KGR_ERR_INVALID_ARGUMENT,
+		"ReSTIR needs the normal, albedo and position buffers");
+	if (!att->have_prev_camera) {
+		memcpy(att->prev_projection, info->camera.projection, 64);
+		memcpy(att->prev_view, info->camera.view, 64);
+		att->have_prev_camera = true;
+	}
+	mat4_mul(att->prev_projection, att->prev_view, fp.prev_proj_view);
+	att->ensure_paths(fp.paths);
+	PathBuffers pb = att->path_buffers();
+	DeviceScene s = scene_for_launch(sc, info);
+	OutputBuffers out = {reinterpret_cast<float4 *>(info->buffers.color),
+		reinterpret_cast<float4 *>(info->buffers.normal), reinterpret_cast<float4 *>(info->buffers.albedo),
+		reinterpret_cast<float4 *>(info->buffers.position)};
+	RestirFrameBuffers rb;
+	for (int k = 0; k < 2; k++) {
+		rb.res[k].a = att->res_a[k].ptr;
+		rb.res[k].b = att->res_b[k].ptr;
+	}
+	rb.materials = att->pixel_materials.ptr;
+	rb.intermediate = att->intermediate.ptr;
+	rb.auxiliary = att->auxiliary.ptr;
+	int prev = att->prev_index, cur = 1 - prev;
+	uint32_t launches = 0;
+
+	/* initial pass */
+	prepare_visits(att, st);
+	KGR_CUDA(cudaMemsetAsync(rb.res[cur].b, 0, sizeof(float4) * fp.npix, st));
+	att->mark(-1, st);
+	pt_generate(pb, fp, st);
+	att->mark(STAGE_GENERATE, st);
+	pt_trace_closest(s, pb, 0, fp.layout, st);
+	att->mark(STAGE_TRACE_CLOSEST, st);
+	restir_primary(s, pb, fp, rb, cur, st);
+	att->mark(STAGE_RESTIR_PRIMARY, st);
+	launches += 3;
+	for (int d = 1; d <= fp.max_depth; d++) {
+		int q = d & 1;
+		reset_counters(pb, (1 << (q ^ 1)) | (1 << CNT_SHADOW), st);
+		att->mark(-1, st);
+		pt_trace_closest(s, pb, q, fp.layout, st);
+		att->mark(STAGE_TRACE_CLOSEST, st);
+		pt_shade_final_seed(s, pb, fp, d, q, st);
+		att->mark(STAGE_SHADE, st);
+		pt_shadow_resolve(s, pb, fp.layout, st);
+		att->mark(STAGE_SHADOW, st);
+		launches += 3;
+	}
+	restir_finalize(pb, fp, rb, out, st);
+	att->mark(STAGE_RESTIR_FINALIZE, st);
+	launches++;
+	/* temporal pass */
+	if (fp.temporal) {
+		restir_temporal(s, fp, rb, out, cur, prev, st);
+		att->mark(STAGE_RESTIR_TEMPORAL, st);
+		launches++;
+	}
+	/* spatial passes with the ping-pong of restir.cuh:280-300 */
+	int passes = att->opt_int("spatial_passes", 2);
+	KGR_REQUIRE(passes >= 0 && passes <= 16, KGR_ERR_INVALID_ARGUMENT, "spatial_passes must be 0..16");
+	int in = cur, outb = prev;
+	for (int k = 0; k < passes; k++) {
+		restir_spatial(s, fp, rb, out, in, outb, st);
+		att->mark(STAGE_RESTIR_SPATIAL, st);
+		std::swap(in, outb);
+		launches++;
+	}
+	att->prev_index = in;
+	memcpy(att->prev_projection, info->camera.projection, 64);
+	memcpy(att->prev_view, info->camera.view, 64);
+	att->stats.kernel_launches = launches;
+	att->stats.camera_rays = fp.paths;
+	att->last_paths = fp.paths;
+}
+
+} /* namespace */
+
+extern "C" {
+
+kgr_status kgr_create(const char *kind, kgr_attachment **out)
+{
+	return guarded([&] {
+		KGR_REQUIRE(kind && out, KGR_ERR_INVALID_ARGUMENT, "NULL argument");
+		*out = nullptr;
+		std::string k(kind);
+		Kind kd;
+		std::string name;
+		if (k == "path_tracer") {
+			kd = KIND_PT;
+			name = "Path Tracer";
+		} else if (k == "restir_di" || k == "restir") {
+			kd = KIND_RESTIR_DI;
+			name = "ReSTIR";
+		} else if (k == "restir_gi") {
+			throw Error(KGR_ERR_UNSUPPORTED, "restir_gi is not built yet");
+		} else {
+			throw Error(KGR_ERR_INVALID_ARGUMENT, "unknown attachment kind: " + k);
+		}
+		kgr_attachment *a = new kgr_attachment();
+		a->kind = kd;
+		a->name = name;
+		*out = a;
+	});
+}
+
+kgr_status kgr_attach(kgr_attachment *att, const kgr_context *ctx)
+{
+	return guarded([&] {
+		KGR_REQUIRE(att && ctx, KGR_ERR_INVALID_ARGUMENT, "NULL argument");
+		KGR_REQUIRE(ctx->width > 0 && ctx->height > 0, KGR_ERR_INVALID_ARGUMENT, "empty extent");
+		KGR_REQUIRE((uint64_t)ctx->width * ctx->height < (1ull << 30), KGR_ERR_UNSUPPORTED, "extent too large");
+		int dev = resolve_device(ctx->device);
+		if (att->loaded) {
+			DeviceGuard g(att->device);
+			att->release_all();
+			att->loaded = false;
+		}
+		att->device = dev;
+		att->width = ctx->width;
+		att->height = ctx->height;
+		att->attached = true;
+		att->have_prev_camera = false;
+	});
+}
+
+kgr_status kgr_load(kgr_attachment *att)
+{
+	return guarded([&] {
+		KGR_REQUIRE(att, KGR_ERR_INVALID_ARGUMENT, "attachment is NULL");
+		KGR_REQUIRE(att->attached, KGR_ERR_NOT_ATTACHED, "attach() was not called");
+		DeviceGuard g(att->device);
+		size_t npix = (size_t)att->width * att->height;
+		try {
+			att->counters.alloc(CNT_COUNT);
+			KGR_CUDA(cudaMemset(att->counters.ptr, 0, CNT_COUNT * sizeof(uint32_t)));
+			if (att->kind == KIND_RESTIR_DI) {
+				for (int k = 0; k < 2; k++) {
+					att->res_a[k].alloc(npix);
+					att->res_b[k].alloc(npix);
+					KGR_CUDA(cudaMemset(att->res_a[k].ptr, 0xff, npix * sizeof(float4)));
+					KGR_CUDA(cudaMemset(att->res_b[k].ptr, 0, npix * sizeof(float4)));
+				}
+				att->intermediate.alloc(npix);
+				att->auxiliary.alloc(npix);
+				att->pixel_materials.alloc(npix);
+				KGR_CUDA(cudaMemset(att->pixel_materials.ptr, 0, npix * sizeof(kgr_material)));
+				att->prev_index = 1;
+				att->ensure_paths((uint32_t)npix);
+			}
+			if (!att->ev_start) {
+				KGR_CUDA(cudaEventCreate(&att->ev_start));
+				KGR_CUDA(cudaEventCreate(&att->ev_stop));
+			}
+		} catch (...) {
+			att->release_all();
+			throw;
+		}
+		att->loaded = true;
+	});
+}
+
+kgr_status kgr_unload(kgr_attachment *att)
+{
+	return guarded([&] {
+		KGR_REQUIRE(att, KGR_ERR_INVALID_ARGUMENT, "attachment is NULL");
+		if (!att->loaded)
+			return;
+		DeviceGuard g(att->device);
+		att->release_all();
+		att->loaded = false;
+	});
+}
+
+kgr_status kgr_destroy(kgr_attachment *att)
+{
+	return guarded([&] {
+		if (!att)
+			return;
+		DeviceGuard g(att->attached ? att->device : -1);
+		delete att;
+	});
+}
+
+/* Known options, their types and defaults.  Unknown names are ignored, as
+ * the reference's attachments ignore them (naive_path_tracer.cu:215-225);
+ * a known name with the wrong type is rejected with KGR_ERR_TYPE (the
+ * reference logs a warning and keeps the old value). */
+static const std::map<std::string, OptionValue> &option_defaults()
+{
+	static const std::map<std::string, OptionValue> d = {
+		{"max_depth", -1}, {"russian_roulette", false}, {"rr_start_depth", 3}, {"spp", 1},
+		{"layout", std::string("fast")}, {"candidates", 32}, {"temporal", true}, {"temporal_mcap", 200},
+		{"spatial_passes", 2}, {"spatial_neighbors", 5}, {"spatial_radius", 30},
+		{"profile", false}, {"count_visits", false}};
+	return d;
+}
+
+kgr_status kgr_set_option(kgr_attachment *att, const char *name, const kgr_value *value)
+{
+	return guarded([&] {
+		KGR_REQUIRE(att && name && value, KGR_ERR_INVALID_ARGUMENT, "NULL argument");
+		auto it = option_defaults().find(name);
+		if (it == option_defaults().end())
+			return;
+		OptionValue v;
+		switch (value->tag) {
+		case KGR_VALUE_INT: v = (int)value->i; break;
+		case KGR_VALUE_FLOAT: v = value->f; break;
+		case KGR_VALUE_BOOL: v = value->b != 0; break;
+		case KGR_VALUE_STRING:
+			KGR_REQUIRE(value->s, KGR_ERR_INVALID_ARGUMENT, "NULL string value");
+			v = std::string(value->s);
+			break;
+		default: throw Error(KGR_ERR_TYPE, "option value has no type");
+		}
+		KGR_REQUIRE(v.index() == it->second.index(), KGR_ERR_TYPE, std::string("wrong type for option ") + name);
+		if (std::string(name) == "layout") {
+			const std::string &s = std::get<std::string>(v);
+			KGR_REQUIRE(s == "fast" || s == "threaded", KGR_ERR_INVALID_ARGUMENT, "layout is fast or threaded");
+		}
+		att->options[name] = v;
+	});
+}
+
+kgr_status kgr_get_option(const kgr_attachment *att, const char *name, kgr_value *value)
+{
+	return guarded([&] {
+		KGR_REQUIRE(att && name && value, KGR_ERR_INVALID_ARGUMENT, "NULL argument");
+		memset(value, 0, sizeof(*value));
+		auto d = option_defaults().find(name);
+		if (d == option_defaults().end()) {
+			/* AttachmentRTX::get_option returns {} -- a variant holding int 0 */
+			value->tag = KGR_VALUE_INT;
+			return;
+		}
+		auto it = att->options.find(name);
+		const OptionValue &v = it == att->options.end() ? d->second : it->second;
+		if (auto p = std::get_if<int>(&v)) {
+			value->tag = KGR_VALUE_INT;
+			value->i = *p;
+		} else if (auto f = std::get_if<float>(&v)) {
+			value->tag = KGR_VALUE_FLOAT;
+			value->f = *f;
+		} else if (auto b = std::get_if<bool>(&v)) {
+			value->tag = KGR_VALUE_BOOL;
+			value->b = *b;
+		} else {
+			const_cast<kgr_attachment *>(att)->option_string = std::get<std::string>(v);
+			value->tag = KGR_VALUE_STRING;
+			value->s = att->option_string.c_str();
+		}
+	});
+}
+
+kgr_status kgr_render(kgr_attachment *att, const kgr_launch_info *info, const kgr_scene *sc, void *stream)
+{
+	return guarded([&] {
+		check_launch(att, info, sc);
+		DeviceGuard g(att->device);
+		cudaStream_t st = (cudaStream_t)stream;
+		switch (att->kind) {
+		case KIND_PT: render_pt(att, info, sc, st); break;
+		case KIND_RESTIR_DI: render_restir_di(att, info, sc, st); break;
+		default: throw Error(KGR_ERR_UNSUPPORTED, "attachment kind not built");
+		}
+	});
+}
+
+kgr_status kgr_get_render_stats(const kgr_attachment *att, kgr_render_stats *stats)
+{
+	return guarded([&] {
+		KGR_REQUIRE(att && stats, KGR_ERR_INVALID_ARGUMENT, "NULL argument");
+		*stats = att->stats;
+		if (att->loaded && att->counters.ptr) {
+			DeviceGuard g(att->device);
+			uint32_t c[CNT_COUNT];
+			KGR_CUDA(cudaMemcpy(c, att->counters.ptr, sizeof(c), cudaMemcpyDeviceToHost));
+			stats->bounce_rays = c[CNT_BOUNCE_TOTAL];
+			stats->shadow_rays = c[CNT_SHADOW_TOTAL];
+		}
+	});
+}
+
+kgr_status kgr_get_stage_times(kgr_attachment *att, double *ms, uint32_t *launches, uint32_t count)
+{
+	return guarded([&] {
+		KGR_REQUIRE(att && ms && launches, KGR_ERR_INVALID_ARGUMENT, "NULL argument");
+		DeviceGuard g(att->device);
+		att->collect_times();
+		for (uint32_t k = 0; k < count; k++) {
+			ms[k] = k < STAGE_COUNT ? att->stage_ms[k] : 0.0;
+			launches[k] = k < STAGE_COUNT ? att->stage_launches[k] : 0;
+		}
+		for (int k = 0; k < STAGE_COUNT; k++) {
+			att->stage_ms[k] = 0.0;
+			att->stage_launches[k] = 0;
+		}
+	});
+}
+
+kgr_status kgr_get_visit_counts(const kgr_attachment *att, uint64_t counts[4])
+{
+	return guarded([&] {
+		KGR_REQUIRE(att && counts, KGR_ERR_INVALID_ARGUMENT, "NULL argument");
+		memset(counts, 0, 4 * sizeof(uint64_t));
+		if (!att->visits.ptr)
+			return;
+		DeviceGuard g(att->device);
+		KGR_CUDA(cudaMemcpy(counts, att->visits.ptr, 4 * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+	});
+}
+
+kgr_status kgr_measure_read_bandwidth(int32_t device, uint64_t bytes, int32_t iters, double *gbps)
+{
+	return guarded([&] {
+		KGR_REQUIRE(gbps && bytes >= 16 && iters >= 1, KGR_ERR_INVALID_ARGUMENT, "bad argument");
+		int dev = resolve_device(device);
+		DeviceGuard g(dev);
+		size_t n = (size_t)(bytes / 16);
+		DevBuf<float4> buf, sink;
+		buf.alloc(n);
+		sink.alloc(1);
+		KGR_CUDA(cudaMemset(buf.ptr, 0, n * sizeof(float4)));
+		launch_read_probe(buf.ptr, n, sink.ptr, 1, 0);
+		cudaEvent_t a, b;
+		KGR_CUDA(cudaEventCreate(&a));
+		KGR_CUDA(cudaEventCreate(&b));
+		float best = 1e30f;
+		for (int rep = 0; rep < 5; rep++) {
+			KGR_CUDA(cudaEventRecord(a, 0));
+			launch_read_probe(buf.ptr, n, sink.ptr, iters, 0);
+			KGR_CUDA(cudaEventRecord(b, 0));
+			KGR_CUDA(cudaEventSynchronize(b));
+			float ms = 0.0f;
+			KGR_CUDA(cudaEventElapsedTime(&ms, a, b));
+			best = ms < best ? ms : best;
+		}
+		cudaEventDestroy(a);
+		cudaEventDestroy(b);
+		*gbps = (double)n * 16.0 * iters / (best * 1e-3) / 1e9;
+	});
+}
+
+kgr_status kgr_debug_copy(const kgr_attachment *att, const char *what, void *host, uint64_t bytes)
+{
+	return guarded([&] {
+		KGR_REQUIRE(att && what && host, KGR_ERR_INVALID_ARGUMENT, "NULL argument");
+		KGR_REQUIRE(att->loaded, KGR_ERR_NOT_LOADED, "not loaded");
+		DeviceGuard g(att->device);
+		std::string w(what);
+		const void *src = nullptr;
+		size_t n = 0;
+		int prev = att->prev_index;
+		if (w == "reservoir_prev_a") { src = att->res_a[prev].ptr; n = att->res_a[prev].bytes(); }
+		else if (w == "reservoir_prev_b") { src = att->res_b[prev].ptr; n = att->res_b[prev].bytes(); }
+		else if (w == "intermediate") { src = att->intermediate.ptr; n = att->intermediate.bytes(); }
+		else if (w == "auxiliary") { src = att->auxiliary.ptr; n = att->auxiliary.bytes(); }
+		else if (w == "materials") { src = att->pixel_materials.ptr; n = att->pixel_materials.bytes(); }
+		else throw Error(KGR_ERR_INVALID_ARGUMENT, "unknown buffer " + w);
+		KGR_REQUIRE(src && bytes <= n, KGR_ERR_INVALID_ARGUMENT, "buffer missing or too small");
+		KGR_CUDA(cudaMemcpy(host, src, bytes, cudaMemcpyDeviceToHost));
+	});
+}
+
+kgr_plugin_ret kgr_load_attachment(const char *kind)
+{
+	kgr_attachment *a = nullptr;
+	if (kgr_create(kind ? kind : "path_tracer", &a) != KGR_OK)
+		return {nullptr, nullptr};
+	return {a->name.c_str(), a};
+}
+
+/* ====================================================== procedural scenes == */
+
+kgr_status kgr_generate_scene(const char *name, uint64_t seed, kgr_generated **out)
+{
+	return guarded([&] {
+		KGR_REQUIRE(name && out, KGR_ERR_INVALID_ARGUMENT, "NULL argument");
+		std::unique_ptr<kgr_generated> g(new kgr_generated());
+		generate_scene(name, seed, g.get());
+		*out = g.release();
+	});
+}
+
+kgr_status kgr_generated_get(const kgr_generated *g, kgr_generated_view *v)
+{
+	return guarded([&] {
+		KGR_REQUIRE(g && v, KGR_ERR_INVALID_ARGUMENT, "NULL argument");
+		v->positions = g->positions.data();
+		v->normals = g->normals.data();
+		v->vertex_count = (uint32_t)(g->positions.size() / 3);
+		v->indices = g->indices.data();
+		v->material_indices = g->material_indices.data();
+		v->triangle_count = (uint32_t)(g->indices.size() / 3);
+		v->materials = g->materials.data();
+		v->material_count = (uint32_t)g->materials.size();
+		memcpy(v->camera_eye, g->eye, 12);
+		memcpy(v->camera_target, g->target, 12);
+		v->camera_fov_deg = g->fov;
+	});
+}
+
+kgr_status kgr_generated_destroy(kgr_generated *g)
+{
+	delete g;
+	return KGR_OK;
+}
+
+/* uvw_frame (include/camera.hpp:45-63), glm::perspective and glm::lookAt
+ * (camera.hpp:20-34) with near 0.1 and far 1000. */
+kgr_status kgr_camera_setup(const float eye[3], const float target[3], const float up[3], float fov_deg,
+		float aspect, kgr_launch_info *info)
+{
+	return guarded([&] {
+		KGR_REQUIRE(eye && target && up && info, KGR_ERR_INVALID_ARGUMENT, "NULL argument");
+		auto sub = [](const float *a, const float *b, float *o) { for (int k = 0; k < 3; k++) o[k] = a[k] - b[k]; };
+		auto crs = [](const float *a, const float *b, float *o) {
+			o[0] = a[1] * b[2] - b[1] * a[2];
+			o[1] = a[2] * b[0] - b[2] * a[0];
+			o[2] = a[0] * b[1] - b[0] * a[1];
+		};
+		auto dotp = [](const float *a, const float *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
+		auto nrm = [&](float *v) { float inv = 1.0f / sqrtf(dotp(v, v)); for (int k = 0; k < 3; k++) v[k] *= inv; };
+		float w[3], u[3], v[3];
+		sub(target, eye, w);
+		float wlen = sqrtf(dotp(w, w));
+		crs(w, up, u);
+		nrm(u);
+		crs(u, w, v);
+		nrm(v);
+		float half = (float)(fov_deg * 0.01745329251994329576923690768489) / 2.0f;
+		float vlen = wlen * tanf(half);
+		for (int k = 0; k < 3; k++)
+			v[k] *= vlen;
+		float ulen = vlen * aspect;
+		for (int k = 0; k < 3; k++)
+			u[k] *= ulen;
+		memcpy(info->camera.center, eye, 12);
+		memcpy(info->camera.ax_u, u, 12);
+		memcpy(info->camera.ax_v, v, 12);
+		memcpy(info->camera.ax_w, w, 12);
+		/* glm::perspective (right-handed, depth -1..1) */
+		float *P = info->camera.projection;
+		memset(P, 0, 64);
+		float tan_half = tanf(half);
+		P[0] = 1.0f / (aspect * tan_half);
+		P[5] = 1.0f / tan_half;
+		float zn = 0.1f, zf = 1000.0f;
+		P[10] = -(zf + zn) / (zf - zn);
+		P[11] = -1.0f;
+		P[14] = -(2.0f * zf * zn) / (zf - zn);
+		/* glm::lookAt (right-handed) */
+		float f[3], s[3], uu[3];
+		sub(target, eye, f);
+		nrm(f);
+		crs(f, up, s);
+		nrm(s);
+		crs(s, f, uu);
+		float *V = info->camera.view;
+		memset(V, 0, 64);
+		V[0] = s[0]; V[4] = s[1]; V[8] = s[2];
+		V[1] = uu[0]; V[5] = uu[1]; V[9] = uu[2];
+		V[2] = -f[0]; V[6] = -f[1]; V[10] = -f[2];
+		V[12] = -dotp(s, eye);
+		V[13] = -dotp(uu, eye);
+		V[14] = dotp(f, eye);
+		V[15] = 1.0f;
+	});
+}
+
+} /* extern "C" */

@@ -1,0 +1,512 @@
+/*
+ * kgr_device.cuh -- device functions of the hot path: BVH traversal of both
+ * layouts, hit reconstruction, light sampling, the GGX BSDF and reservoirs.
+ *
+ * Compiled with -fmad=false, -prec-div=true, -prec-sqrt=true and without
+ * flush-to-zero, so every expression rounds exactly as written.  The
+ * evaluation order of each expression is the reference's (cited per
+ * function); that keeps hit ids, bounce directions, Russian-roulette
+ * decisions and reservoir selections identical to the CPU restatement.
+ * The fast-layout slab test is the one place that uses explicit FMA
+ * (__fmaf_rn): its boxes are padded at build time so that culling stays
+ * conservative, and it only decides which triangles get tested.
+ */
+#ifndef KGR_DEVICE_CUH_
+#define KGR_DEVICE_CUH_
+
+#include "kgr_internal.h"
+#include "kgr_math.h"
+
+namespace kgr {
+
+#define KGR_STACK_DEPTH KGR_STACK_DEPTH_HOST
+
+__device__ __forceinline__ f3 f3_of(float4 v) { return mk(v.x, v.y, v.z); }
+__device__ __forceinline__ float4 f4_of(f3 v, float w) { return make_float4(v.x, v.y, v.z, w); }
+__device__ __forceinline__ int32_t ibits(float f) { return __float_as_int(f); }
+__device__ __forceinline__ float fbits(int32_t i) { return __int_as_float(i); }
+
+/* ----------------------------------------------------------- triangles -- */
+
+/* intersects_triangle (include/optix/lighting.cuh:34-55) with the edges
+ * e1 = v2 - v1, e2 = v3 - v1 given (computed by the same float
+ * subtraction on the host). 1.0/divisor as a float IEEE division equals the
+ * reference's double division rounded to float. */
+__device__ __forceinline__ float mt_test(const f3 &v1, const f3 &e1, const f3 &e2,
+		const f3 &origin, const f3 &dir, float &b1, float &b2)
+{
+	f3 s1 = cross(dir, e2);
+	float divisor = dot(s1, e1);
+	if (divisor == 0.0f)
+		return -1.0f;
+	f3 s = origin - v1;
+	float inv_divisor = 1.0f / divisor;
+	b1 = dot(s, s1) * inv_divisor;
+	if (b1 < 0.0f || b1 > 1.0f)
+		return -1.0f;
+	f3 s2 = cross(s, e1);
+	b2 = dot(dir, s2) * inv_divisor;
+	if (b2 < 0.0f || b1 + b2 > 1.0f)
+		return -1.0f;
+	return dot(e2, s2) * inv_divisor;
+}
+
+/* ---------------------------------------------------- threaded layout -- */
+
+/* intersect_box (shaders/rt/modules/bbox.glsl:8-58), IEEE divisions */
+__device__ __forceinline__ float slab_box(const f3 &o, const f3 &d, const f3 &pmin, const f3 &pmax)
+{
+	float tmin = (pmin.x - o.x) / d.x;
+	float tmax = (pmax.x - o.x) / d.x;
+	if (tmin > tmax) { float t = tmin; tmin = tmax; tmax = t; }
+	float tymin = (pmin.y - o.y) / d.y;
+	float tymax = (pmax.y - o.y) / d.y;
+	if (tymin > tymax) { float t = tymin; tymin = tymax; tymax = t; }
+	if ((tmin > tymax) || (tymin > tmax))
+		return -1.0f;
+	if (tymin > tmin)
+		tmin = tymin;
+	if (tymax < tmax)
+		tmax = tymax;
+	float tzmin = (pmin.z - o.z) / d.z;
+	float tzmax = (pmax.z - o.z) / d.z;
+	if (tzmin > tzmax) { float t = tzmin; tzmin = tzmax; tzmax = t; }
+	if ((tmin > tzmax) || (tzmin > tmax))
+		return -1.0f;
+	if (tzmin > tmin)
+		tmin = tzmin;
+	if (tzmax < tmax)
+		tmax = tzmax;
+	return tmin;
+}
+
+/* in_box (bbox.glsl:61-67) */
+__device__ __forceinline__ bool origin_in_box(const f3 &p, const f3 &pmin, const f3 &pmax)
+{
+	bool lt = p.x < pmin.x || p.y < pmin.y || p.z < pmin.z;
+	bool gt = p.x > pmax.x || p.y > pmax.y || p.z > pmax.z;
+	return !(lt || gt);
+}
+
+struct TraceCounters {
+	uint32_t nodes, tris;
+};
+
+/* trace() (shaders/rt/modules/bvh.glsl:52-99): the stackless threaded walk
+ * over 3-vec4 records.  ANY: stop at the first primitive with 0 < t < tmax
+ * (is_occluded, amadeus_common.cuh:190-212). */
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ bool trace_threaded(const DeviceScene &s, const f3 &o, const f3 &d,
+		float tmax, kgr_hit &best, TraceCounters *cnt = nullptr)
+{
+	best.prim = -1;
+	best.t = tmax;
+	best.b1 = 0.0f;
+	best.b2 = 0.0f;
+	int32_t node = s.bvh_vec4_count ? 0 : -1;
+	while (node != -1) {
+		float4 h = __ldg(&s.bvh[node]);
+		int32_t object = ibits(h.y);
+		if (object != -1) {
+			if (COUNT)
+				cnt->tris++;
+			uint4 t = __ldg(&s.tris[object]);
+			f3 v1 = f3_of(__ldg(&s.positions[t.x]));
+			f3 v2 = f3_of(__ldg(&s.positions[t.y]));
+			f3 v3 = f3_of(__ldg(&s.positions[t.z]));
+			float b1 = 0.0f, b2 = 0.0f;
+			float tt = mt_test(v1, v2 - v1, v3 - v1, o, d, b1, b2);
+			if (tt > 0.0f && tt < best.t) {
+				if (ANY)
+					return true;
+				best.prim = object;
+				best.t = tt;
+				best.b1 = b1;
+				best.b2 = b2;
+			}
+			node = ibits(h.w);
+		} else {
+			if (COUNT)
+				cnt->nodes++;
+			f3 pmin = f3_of(__ldg(&s.bvh[node + 1]));
+			f3 pmax = f3_of(__ldg(&s.bvh[node + 2]));
+			float tb = slab_box(o, d, pmin, pmax);
+			bool inside = origin_in_box(o, pmin, pmax);
+			node = ((tb > 0.0f && tb < best.t) || inside) ? ibits(h.z) : ibits(h.w);
+		}
+	}
+	return best.prim >= 0;
+}
+
+/* -------------------------------------------------------- fast layout -- */
+
+/* Ordered descent over 64-byte child-pair nodes with a per-thread stack.
+ * Closest hit: a triangle replaces the best when 0 < t < best, or t == best
+ * and its rank (position in the threaded walk) is lower -- the primitive the
+ * reference's strict `t < best` walk would keep.  Box culling keeps every
+ * child whose padded slab interval reaches [0, best]. */
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ bool trace_fast(const DeviceScene &s, const f3 &o, const f3 &d,
+		float tmax, kgr_hit &best, TraceCounters *cnt = nullptr)
+{
+	best.prim = -1;
+	best.t = tmax;
+	best.b1 = 0.0f;
+	best.b2 = 0.0f;
+	int32_t best_rank = 0x7fffffff;
+	const float ix = 1.0f / d.x, iy = 1.0f / d.y, iz = 1.0f / d.z;
+	const float ox = o.x * ix, oy = o.y * iy, oz = o.z * iz;
+	int32_t stack[KGR_STACK_DEPTH];
+	int sp = 0;
+	int32_t ref = 0;
+	for (;;) {
+		while (ref >= 0) {
+			if (COUNT)
+				cnt->nodes++;
+			const float4 *np = reinterpret_cast<const float4 *>(s.fast_nodes + ref);
+			float4 lxy = __ldg(np + 0);
+			float4 rxy = __ldg(np + 1);
+			float4 lrz = __ldg(np + 2);
+			int4 refs = __ldg(reinterpret_cast<const int4 *>(np + 3));
+			float l0x = __fmaf_rn(lxy.x, ix, -ox), l1x = __fmaf_rn(lxy.y, ix, -ox);
+			float l0y = __fmaf_rn(lxy.z, iy, -oy), l1y = __fmaf_rn(lxy.w, iy, -oy);
+			float l0z = __fmaf_rn(lrz.x, iz, -oz), l1z = __fmaf_rn(lrz.y, iz, -oz);
+			float r0x = __fmaf_rn(rxy.x, ix, -ox), r1x = __fmaf_rn(rxy.y, ix, -ox);
+			float r0y = __fmaf_rn(rxy.z, iy, -oy), r1y = __fmaf_rn(rxy.w, iy, -oy);
+			float r0z = __fmaf_rn(lrz.z, iz, -oz), r1z = __fmaf_rn(lrz.w, iz, -oz);
+			float ln = fmaxf(fmaxf(fminf(l0x, l1x), fminf(l0y, l1y)), fmaxf(fminf(l0z, l1z), 0.0f));
+			float lf = fminf(fminf(fmaxf(l0x, l1x), fmaxf(l0y, l1y)), fmaxf(l0z, l1z));
+			float rn = fmaxf(fmaxf(fminf(r0x, r1x), fminf(r0y, r1y)), fmaxf(fminf(r0z, r1z), 0.0f));
+			float rf = fminf(fminf(fmaxf(r0x, r1x), fmaxf(r0y, r1y)), fmaxf(r0z, r1z));
+			bool hl = ln <= lf && ln <= best.t;
+			bool hr = rn <= rf && rn <= best.t;
+			if (hl && hr) {
+				int32_t near_ref = refs.x, far_ref = refs.y;
+				if (rn < ln) {
+					near_ref = refs.y;
+					far_ref = refs.x;
+				}
+				stack[sp++] = far_ref;
+				ref = near_ref;
+			} else if (hl) {
+				ref = refs.x;
+			} else if (hr) {
+				ref = refs.y;
+			} else {
+				if (sp == 0)
+					return best.prim >= 0;
+				ref = stack[--sp];
+			}
+		}
+		/* leaf */
+		uint32_t code = ~(uint32_t)ref;
+		uint32_t start = code >> 3, n = (code & 7u) + 1u;
+		const float4 *tp = s.fast_tris + 3 * (size_t)start;
+		for (uint32_t k = 0; k < n; k++) {
+			if (COUNT)
+				cnt->tris++;
+			float4 a = __ldg(tp + 3 * k + 0);
+			float4 e1 = __ldg(tp + 3 * k + 1);
+			float4 e2 = __ldg(tp + 3 * k + 2);
+			float b1 = 0.0f, b2 = 0.0f;
+			float tt = mt_test(f3_of(a), f3_of(e1), f3_of(e2), o, d, b1, b2);
+			if (ANY) {
+				if (tt > 0.0f && tt < best.t) {
+					best.prim = ibits(a.w);
+					best.t = tt;
+					return true;
+				}
+				continue;
+			}
+			int32_t rank = (int32_t)(start + k);
+			if (tt > 0.0f && (tt < best.t || (tt == best.t && rank < best_rank))) {
+				best.prim = ibits(a.w);
+				best.t = tt;
+				best.b1 = b1;
+				best.b2 = b2;
+				best_rank = rank;
+			}
+		}
+		if (sp == 0)
+			return best.prim >= 0;
+		ref = stack[--sp];
+	}
+}
+
+template <bool ANY>
+__device__ __forceinline__ bool trace(const DeviceScene &s, int layout, const f3 &o, const f3 &d,
+		float tmax, kgr_hit &best)
+{
+	if (layout == KGR_LAYOUT_THREADED)
+		return trace_threaded<ANY, false>(s, o, d, tmax, best);
+	return trace_fast<ANY, false>(s, o, d, tmax, best);
+}
+
+/* -------------------------------------------------------------- shading -- */
+
+struct Material {
+	f3 diffuse, specular, emission;
+	float roughness, refraction;
+	int type;
+};
+
+__device__ __forceinline__ Material load_material(const kgr_material *mats, uint32_t i)
+{
+	const float4 *p = reinterpret_cast<const float4 *>(mats + i);
+	float4 a = __ldg(p + 0), b = __ldg(p + 1), c = __ldg(p + 2), e = __ldg(p + 3);
+	Material m;
+	m.diffuse = mk(a.x, a.y, a.z);
+	m.specular = mk(a.w, b.x, b.y);
+	m.emission = mk(b.z, b.w, c.x);
+	/* c.y..c.w = ambient, e.x = shininess */
+	m.roughness = e.y;
+	m.refraction = e.z;
+	m.type = __float_as_int(e.w);
+	return m;
+}
+
+/* SurfaceHit (include/cuda/brdf.cuh:67-74) */
+struct SurfaceHit {
+	Material mat;
+	bool entering;
+	f3 n, wo, x;
+};
+
+#define KGR_PI_DEV 3.14159265358979323846f /* brdf.cuh:64 */
+
+/* G1 (brdf.cuh:179-192) */
+__device__ __forceinline__ float G1(const f3 &n, const f3 &v, const Material &mat)
+{
+	if (dot(v, n) <= 0.0f)
+		return 0.0f;
+	float alpha = mat.roughness;
+	float theta = kacos(clampf(dot(n, v), 0.0f, 0.999f));
+	float tan_theta = ktan(theta);
+	float denom = 1 + ksqrt(1 + alpha * alpha * tan_theta * tan_theta);
+	return 2.0f / denom;
+}
+
+/* Microfacets::GGX (brdf.cuh:210-220) */
+__device__ __forceinline__ float ggx_D(const f3 &n, const f3 &h, const Material &mat)
+{
+	float alpha = mat.roughness;
+	float theta = kacos(clampf(dot(n, h), 0.0f, 1.0f));
+	float sn, c;
+	ksincos(theta, sn, c);
+	float tn = sn / c;
+	return (alpha * alpha) / (KGR_PI_DEV * kpow4(c) * kpow2(alpha * alpha + tn * tn));
+}
+
+/* GGX::brdf (brdf.cuh:337-353) with shlick_F (:202-207) and G (:195-199) */
+__device__ __forceinline__ f3 ggx_brdf(const Material &mat, f3 n, const f3 &wi, const f3 &wo)
+{
+	if (dot(wo, n) <= 0.0f)
+		n = -n;
+	f3 h = normalize(wi + wo);
+	float k = kpow5(1 - dot(wi, h));
+	f3 f = mat.specular + (1.0f - mat.specular) * k;
+	float g = G1(n, wo, mat) * G1(n, wi, mat);
+	float d = ggx_D(n, h, mat);
+	f3 num = f * g * d;
+	float denom = 4 * dot(wi, n) * dot(wo, n);
+	return num / (denom + 1e-6f);
+}
+
+/* GGX::pdf (brdf.cuh:356-382) */
+__device__ __forceinline__ float ggx_pdf(const Material &mat, f3 n, const f3 &wi, const f3 &wo)
+{
+	if (dot(wo, n) <= 0.0f)
+		n = -n;
+	if (dot(wi, n) <= 0.0f)
+		return 0.0f;
+	f3 h = normalize(wi + wo);
+	float avg_Kd = (mat.diffuse.x + mat.diffuse.y + mat.diffuse.z) / 3.0f;
+	float avg_Ks = (mat.specular.x + mat.specular.y + mat.specular.z) / 3.0f;
+	float t = 1.0f;
+	if (avg_Kd + avg_Ks > 0.0f)
+		t = kmax(avg_Ks / (avg_Kd + avg_Ks), 0.25f);
+	float term1 = dot(n, wi) / KGR_PI_DEV;
+	float term2 = ggx_D(n, h, mat) * dot(n, h) / (4.0f * dot(wi, h));
+	return (1 - t) * term1 + t * term2;
+}
+
+/* GGX::sample (brdf.cuh:385-433) */
+__device__ __forceinline__ f3 ggx_sample(const Material &mat, f3 n, const f3 &wo, f3 &seed)
+{
+	if (dot(wo, n) <= 0.0f)
+		n = -n;
+	float avg_Kd = (mat.diffuse.x + mat.diffuse.y + mat.diffuse.z) / 3.0f;
+	float avg_Ks = (mat.specular.x + mat.specular.y + mat.specular.z) / 3.0f;
+	float t = 1.0f;
+	if (avg_Kd + avg_Ks > 0.0f)
+		t = avg_Ks / (avg_Kd + avg_Ks);
+	f3 eta = rand_uniform_3f(seed);
+	float theta;
+	if (eta.x < t) {
+		float k = ksqrt(eta.y / (1 - eta.y));
+		theta = katan(k * mat.roughness);
+	} else {
+		theta = kacos(ksqrt(eta.y));
+	}
+	float phi = 2.0f * KGR_PI_DEV * eta.z;
+	float st, ct, sp, cp;
+	ksincos(theta, st, ct);
+	ksincos(phi, sp, cp);
+	f3 v = mk(st * cp, st * sp, ct);
+	if (eta.x < t) {
+		f3 h = rotate(v, n);
+		return reflect(-wo, h);
+	}
+	return rotate(v, n);
+}
+
+/* brdf() (brdf.cuh:437-449), out = eDiffuse */
+__device__ __forceinline__ f3 brdf(const SurfaceHit &sh, const f3 &wi)
+{
+	return sh.mat.diffuse / KGR_PI_DEV + ggx_brdf(sh.mat, sh.n, wi, sh.wo);
+}
+
+/* eval() (brdf.cuh:573-589): GGX, or Glass::sample (:154-175) for
+ * transmissive materials; pdf = 0 for a degenerate direction. */
+__device__ __forceinline__ f3 eval(const SurfaceHit &sh, f3 &wi, float &pdf, f3 &seed)
+{
+	if (sh.mat.type & KGR_SHADING_TRANSMISSION) {
+		float eta = sh.mat.refraction;
+		float cos_theta = kmin(dot(-sh.wo, sh.n), 1.0f);
+		float sin_theta = ksqrt(1.0f - cos_theta * cos_theta);
+		bool reflect_ray = (eta * sin_theta > 1.0f);
+		float ni_over_nt = 1.0f / eta;
+		if (!sh.entering)
+			ni_over_nt = eta;
+		if (reflect_ray) {
+			wi = reflect(sh.wo, sh.n);
+		} else {
+			float c2 = dot(-sh.wo, sh.n);
+			f3 par = ni_over_nt * (sh.wo + c2 * sh.n);
+			float pl = length(par);
+			float pl2 = pl * pl;
+			f3 perp = -ksqrt(fabsf(1.0f - pl2)) * sh.n;
+			wi = par + perp;
+		}
+		pdf = 1.0f;
+		return sh.mat.specular;
+	}
+	wi = ggx_sample(sh.mat, sh.n, sh.wo, seed);
+	if (length(wi) < 1e-6f) {
+		pdf = 0.0f;
+		return mk(0.0f);
+	}
+	pdf = ggx_pdf(sh.mat, sh.n, wi, sh.wo);
+	return brdf(sh, wi);
+}
+
+/* --------------------------------------------------------------- lights -- */
+
+struct TriLight {
+	f3 a, ab, ac, intensity;
+	/* TriangleLight::area (lighting.cuh:103-105): `length * 0.5` is a double
+	 * product; halving is exact, so the float product is the same value. */
+	__device__ __forceinline__ float area() const { return length(cross(ab, ac)) * 0.5f; }
+	__device__ __forceinline__ f3 normal() const { return normalize(cross(ab, ac)); }
+};
+
+__device__ __forceinline__ TriLight load_light(const kgr_triangle_light *lights, uint32_t i)
+{
+	const float4 *p = reinterpret_cast<const float4 *>(lights + i);
+	float4 a = __ldg(p + 0), b = __ldg(p + 1), c = __ldg(p + 2);
+	TriLight l;
+	l.a = mk(a.x, a.y, a.z);
+	l.ab = mk(a.w, b.x, b.y);
+	l.ac = mk(b.z, b.w, c.x);
+	l.intensity = mk(c.y, c.z, c.w);
+	return l;
+}
+
+/* sample_area_light(TriangleLight) (lighting.cuh:133-146) */
+__device__ __forceinline__ f3 sample_area_light(const TriLight &light, f3 &seed)
+{
+	f3 r = pcg3f(seed);
+	float u = fract(r.x);
+	float v = fract(r.y);
+	if (u + v > 1.0f) {
+		u = 1.0f - u;
+		v = 1.0f - v;
+	}
+	return light.a + u * light.ab + v * light.ac;
+}
+
+#define KGR_SHADOW_EPS 0.05f /* is_occluded, amadeus_common.cuh:193 */
+#define KGR_OFFSET_EPS 1e-3f /* amadeus_common.cuh:22 */
+
+/* direct_unoccluded (amadeus_common.cuh:380-397) for a triangle light */
+__device__ __forceinline__ f3 direct_unoccluded(const SurfaceHit &sh, const f3 &Le, const f3 &normal,
+		const f3 &D, float d)
+{
+	f3 rho = brdf(sh, D);
+	float geometric = fabsf(dot(sh.n, D));
+	float ldot = fabsf(dot(normal, D));
+	geometric *= ldot / (d * d);
+	return rho * Le * geometric;
+}
+
+/* ------------------------------------------------------------ hit data -- */
+
+/* LOAD_INTERSECTION_DATA (amadeus_common.cuh:490-515): geometric normal
+ * flipped against the ray (entering), interpolated shading normal made
+ * consistent with it, interpolated position; world-space vertices. */
+__device__ __forceinline__ bool surface(const DeviceScene &s, const kgr_hit &h, const f3 &dir,
+		SurfaceHit &sh)
+{
+	uint4 t = __ldg(&s.tris[h.prim]);
+	f3 a = f3_of(__ldg(&s.positions[t.x])), b = f3_of(__ldg(&s.positions[t.y])),
+	   c = f3_of(__ldg(&s.positions[t.z]));
+	f3 ng = normalize(cross(b - a, c - a));
+	bool entering;
+	if (dot(ng, dir) > 0.0f) {
+		ng = -ng;
+		entering = false;
+	} else {
+		entering = true;
+	}
+	ng = normalize(ng);
+	f3 na = f3_of(__ldg(&s.normals[t.x])), nb = f3_of(__ldg(&s.normals[t.y])),
+	   nc = f3_of(__ldg(&s.normals[t.z]));
+	float w0 = 1.0f - h.b1 - h.b2;
+	f3 normal = w0 * na + h.b1 * nb + h.b2 * nc;
+	if (dot(normal, ng) < 0.0f)
+		normal = -normal;
+	normal = normalize(normal);
+	sh.x = w0 * a + h.b1 * b + h.b2 * c;
+	sh.mat = load_material(s.materials, t.w);
+	sh.entering = entering;
+	sh.n = normal;
+	sh.wo = -dir;
+	return !anynan(normal);
+}
+
+/* ------------------------------------------------------------- queues -- */
+
+/* Warp-aggregated append: one atomic per warp, lanes write in lane order. */
+__device__ __forceinline__ void queue_append(uint32_t *queue, uint32_t *counter, uint32_t value, bool pred,
+		uint32_t *total = nullptr)
+{
+	unsigned mask = __activemask();
+	unsigned ballot = __ballot_sync(mask, pred);
+	if (!ballot)
+		return;
+	int lane = threadIdx.x & 31;
+	int leader = __ffs(ballot) - 1;
+	uint32_t base = 0;
+	if (lane == leader) {
+		base = atomicAdd(counter, (uint32_t)__popc(ballot));
+		if (total)
+			atomicAdd(total, (uint32_t)__popc(ballot));
+	}
+	base = __shfl_sync(mask, base, leader);
+	if (pred)
+		queue[base + __popc(ballot & ((1u << lane) - 1u))] = value;
+}
+
+} /* namespace kgr */
+
+#endif

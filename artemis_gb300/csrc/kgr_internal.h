@@ -1,0 +1,199 @@
+/*
+ * kgr_internal.h -- internal structures of libkgr shared by the host C++
+ * translation units and the CUDA kernels.
+ */
+#ifndef KGR_INTERNAL_H_
+#define KGR_INTERNAL_H_
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/kgr.h"
+
+namespace kgr {
+
+/* ---------------------------------------------------------------- errors -- */
+
+struct Error : std::runtime_error {
+	kgr_status status;
+	Error(kgr_status s, const std::string &msg) : std::runtime_error(msg), status(s) {}
+};
+
+void set_last_error(const std::string &msg);
+
+#define KGR_CUDA(call)                                                                 \
+	do {                                                                           \
+		cudaError_t err_ = (call);                                             \
+		if (err_ != cudaSuccess)                                               \
+			throw ::kgr::Error(err_ == cudaErrorMemoryAllocation ?          \
+				KGR_ERR_OUT_OF_MEMORY : KGR_ERR_CUDA,                  \
+				std::string(#call) + ": " + cudaGetErrorString(err_)); \
+	} while (0)
+
+#define KGR_REQUIRE(cond, status, msg)                                                 \
+	do {                                                                           \
+		if (!(cond))                                                           \
+			throw ::kgr::Error((status), (msg));                            \
+	} while (0)
+
+/* Sets the device for the lifetime of the guard and restores the caller's. */
+struct DeviceGuard {
+	int prev = -1;
+	explicit DeviceGuard(int device);
+	~DeviceGuard();
+};
+
+/* ------------------------------------------------------- device buffers -- */
+
+template <class T>
+struct DevBuf {
+	T *ptr = nullptr;
+	size_t count = 0;
+	DevBuf() = default;
+	DevBuf(const DevBuf &) = delete;
+	DevBuf &operator=(const DevBuf &) = delete;
+	~DevBuf() { release(); }
+	void release()
+	{
+		if (ptr)
+			cudaFree(ptr);
+		ptr = nullptr;
+		count = 0;
+	}
+	void alloc(size_t n)
+	{
+		if (n == count && ptr)
+			return;
+		release();
+		if (n == 0)
+			return;
+		KGR_CUDA(cudaMalloc((void **)&ptr, n * sizeof(T)));
+		count = n;
+	}
+	void upload(const T *host, size_t n)
+	{
+		alloc(n);
+		if (n)
+			KGR_CUDA(cudaMemcpy(ptr, host, n * sizeof(T), cudaMemcpyHostToDevice));
+	}
+	void upload(const std::vector<T> &v) { upload(v.data(), v.size()); }
+	size_t bytes() const { return count * sizeof(T); }
+};
+
+/* ---------------------------------------------------------- BVH layouts -- */
+
+/* Binary tree produced by the host builders.  Leaves hold a contiguous range
+ * of the builder's primitive order. */
+struct TreeNode {
+	float bmin[3], bmax[3];
+	int32_t left = -1, right = -1; /* internal: child node indices */
+	int32_t first = 0, count = 0;  /* leaf: range in prim_order */
+};
+
+struct Tree {
+	std::vector<TreeNode> nodes; /* nodes[0] is the root (if any) */
+	std::vector<uint32_t> prim_order;
+};
+
+/* 64-byte child-pair node of the fast layout: boxes of both children
+ * (x/y of left, x/y of right, z of both) and two child references.  A
+ * reference >= 0 is an internal node; < 0 is a leaf ~((start << 3) | (n-1))
+ * over the leaf-ordered triangle array. */
+struct FastNode {
+	float4 lxy;  /* l.min.x, l.max.x, l.min.y, l.max.y */
+	float4 rxy;  /* r.min.x, r.max.x, r.min.y, r.max.y */
+	float4 lrz;  /* l.min.z, l.max.z, r.min.z, r.max.z */
+	int4 refs;   /* left ref, right ref, unused, unused */
+};
+
+/* Host builders (bvh_build.cpp). */
+struct PrimBox {
+	float bmin[3], bmax[3];
+};
+
+void build_sah(const std::vector<PrimBox> &boxes, int max_leaf, Tree &tree);
+void build_kobra(const std::vector<PrimBox> &boxes, Tree &tree);
+/* Threaded bvh.cpp layout, leaves as chains of one-primitive records. */
+void serialize_threaded(const Tree &tree, const std::vector<PrimBox> &boxes,
+		std::vector<float> &out_vec4);
+/* Parse a threaded buffer back into a tree (for caller-supplied buffers). */
+void parse_threaded(const float *vec4, uint32_t count, uint32_t prim_count,
+		const std::vector<PrimBox> &boxes, Tree &tree);
+/* Fast layout from a tree: nodes + leaf-ordered triangle records
+ * {v0.xyz, prim}, {e1}, {e2}.  Boxes are padded outward so that culling is
+ * conservative with respect to the exact triangle test. */
+void build_fast(const Tree &tree, const std::vector<PrimBox> &boxes,
+		const float *positions, const uint32_t *tris4, std::vector<FastNode> &nodes,
+		std::vector<float4> &tri_records);
+
+/* ---------------------------------------------------------------- scene -- */
+
+struct DeviceScene {
+	const float4 *positions;  /* xyz */
+	const float4 *normals;    /* xyz */
+	const uint4 *tris;        /* i0, i1, i2, material */
+	const float4 *bvh;        /* threaded layout, 3 per node */
+	const FastNode *fast_nodes;
+	const float4 *fast_tris;  /* 3 per triangle, leaf order */
+	const kgr_material *materials;
+	const kgr_triangle_light *lights;
+	uint32_t triangle_count;
+	uint32_t light_count;
+	uint32_t bvh_vec4_count;
+	uint32_t fast_node_count;
+};
+
+} /* namespace kgr */
+
+/* Host arrays of a procedural scene (kgr_generate_scene). */
+struct kgr_generated {
+	std::vector<float> positions, normals;
+	std::vector<uint32_t> indices, material_indices;
+	std::vector<kgr_material> materials;
+	float eye[3], target[3], fov;
+};
+
+#define KGR_STACK_DEPTH_HOST 64
+
+struct kgr_scene {
+	int device = 0;
+	std::vector<float> positions, normals; /* 3 per vertex */
+	std::vector<uint32_t> tris4;           /* 4 per triangle */
+	std::vector<kgr_material> materials;
+	std::vector<kgr_triangle_light> lights;
+	std::vector<float> bvh;                /* threaded, 4 floats per vec4 */
+	uint32_t fast_node_count = 0;
+	float bounds_min[3] = {0, 0, 0}, bounds_max[3] = {0, 0, 0};
+	double build_ms = 0.0;
+
+	kgr::DevBuf<float4> d_positions, d_normals, d_bvh, d_fast_tris;
+	kgr::DevBuf<uint4> d_tris;
+	kgr::DevBuf<kgr::FastNode> d_fast_nodes;
+	kgr::DevBuf<kgr_material> d_materials;
+	kgr::DevBuf<kgr_triangle_light> d_lights;
+
+	kgr::DeviceScene view() const;
+	uint64_t device_bytes() const;
+};
+
+namespace kgr {
+
+/* ------------------------------------------------------ kernel launchers -- */
+
+/* Traversal of a ray buffer (8 floats per ray) into hits or occlusion flags. */
+void launch_trace_closest(const DeviceScene &s, const float4 *rays, uint32_t n,
+		kgr_hit *hits, int layout, cudaStream_t stream);
+void launch_trace_any(const DeviceScene &s, const float4 *rays, uint32_t n,
+		uint32_t *occluded, int layout, cudaStream_t stream);
+
+/* Per-ray node/triangle visit counts of the fast layout (diagnostics). */
+void launch_trace_stats(const DeviceScene &s, const float4 *rays, uint32_t n, int any,
+		unsigned long long *counters, cudaStream_t stream);
+
+} /* namespace kgr */
+
+#endif

@@ -1,0 +1,125 @@
+/*
+ * kgr_wavefront.h -- device state of the wavefront integrators (path tracer
+ * and ReSTIR DI/GI) and the launchers the attachments call.
+ *
+ * Paths live in structure-of-arrays buffers of 16-byte records indexed by
+ * path id p; stages exchange work through queues of path ids compacted with
+ * warp ballots.  Path id p = sample * pixels + pixel, so consecutive threads
+ * of the first bounce trace neighbouring pixels.
+ */
+#ifndef KGR_WAVEFRONT_H_
+#define KGR_WAVEFRONT_H_
+
+#include "kgr_internal.h"
+
+namespace kgr {
+
+enum Counter {
+	CNT_Q0 = 0,        /* live paths in queue 0 */
+	CNT_Q1 = 1,        /* live paths in queue 1 */
+	CNT_SHADOW = 2,    /* shadow rays of this bounce */
+	CNT_BOUNCE_TOTAL = 3,
+	CNT_SHADOW_TOTAL = 4,
+	CNT_COUNT = 8
+};
+
+struct PathBuffers {
+	float4 *ray_o;  /* origin xyz */
+	float4 *ray_d;  /* direction xyz, tmax */
+	float4 *beta;   /* throughput */
+	float4 *L;      /* radiance */
+	float4 *seed;   /* seed bits xyz */
+	float4 *hit;    /* prim bits, t, b1, b2 */
+	float4 *sh_o;   /* shadow ray origin */
+	float4 *sh_d;   /* shadow ray direction, tmax */
+	float4 *pend_c; /* unoccluded NEE contribution xyz, pdf */
+	float4 *pend_e; /* emission xyz */
+	float4 *pend_b; /* throughput before the bounce */
+	float4 *aov_n, *aov_a, *aov_p;
+	uint32_t *queue[2];
+	uint32_t *shadow_queue;
+	uint32_t *counters;
+	/* traversal visit counters (nodes, triangles) of the closest and the
+	 * any-hit stage; NULL unless visit counting is on */
+	unsigned long long *visits;
+	uint32_t capacity;
+};
+
+/* Stage kinds for the per-launch CUDA-event timing of an attachment. */
+enum StageKind {
+	STAGE_GENERATE = 0,
+	STAGE_TRACE_CLOSEST = 1,
+	STAGE_SHADE = 2,
+	STAGE_SHADOW = 3,
+	STAGE_ACCUMULATE = 4,
+	STAGE_RESTIR_PRIMARY = 5,
+	STAGE_RESTIR_TEMPORAL = 6,
+	STAGE_RESTIR_SPATIAL = 7,
+	STAGE_RESTIR_FINALIZE = 8,
+	STAGE_COUNT = 9
+};
+
+/* Streaming read of a buffer with 16-byte loads (bandwidth probe). */
+void launch_read_probe(const float4 *buf, size_t n, float4 *sink, int iters, cudaStream_t st);
+
+struct FrameParams {
+	uint32_t width, height, npix, spp, paths;
+	float center[3], U[3], V[3], W[3];
+	float prev_proj_view[16]; /* previous camera projection * view */
+	int32_t max_depth;
+	int32_t russian_roulette, rr_start_depth;
+	uint32_t frame;
+	int32_t accumulate, samples;
+	int32_t layout;
+	int32_t jitter;
+	/* ReSTIR */
+	int32_t candidates, temporal, temporal_mcap, spatial_neighbors, spatial_radius;
+};
+
+/* 32-byte reservoir in two 16-byte SoA arrays:
+ *   a[i] = {sample point xyz, light index bits}
+ *   b[i] = {w, W, M bits, unused} */
+struct ReservoirBuffers {
+	float4 *a;
+	float4 *b;
+};
+
+struct RestirFrameBuffers {
+	ReservoirBuffers res[2];
+	kgr_material *materials; /* per pixel */
+	float4 *intermediate;
+	float4 *auxiliary;
+};
+
+struct OutputBuffers {
+	float4 *color, *normal, *albedo, *position;
+};
+
+/* --- path tracer (pt.cu) --- */
+void pt_generate(const PathBuffers &pb, const FrameParams &fp, cudaStream_t st);
+void pt_trace_closest(const DeviceScene &s, const PathBuffers &pb, int q, int layout, cudaStream_t st);
+void pt_shade(const DeviceScene &s, const PathBuffers &pb, const FrameParams &fp, int depth, int q,
+		cudaStream_t st);
+/* shade that also advances the RNG at the last depth (ReSTIR keeps the
+ * path's final seed as its auxiliary seed) */
+void pt_shade_final_seed(const DeviceScene &s, const PathBuffers &pb, const FrameParams &fp, int depth,
+		int q, cudaStream_t st);
+void pt_shadow_resolve(const DeviceScene &s, const PathBuffers &pb, int layout, cudaStream_t st);
+void pt_accumulate(const PathBuffers &pb, const FrameParams &fp, const OutputBuffers &out, cudaStream_t st);
+void reset_counters(const PathBuffers &pb, int which_mask, cudaStream_t st);
+
+/* --- ReSTIR DI (restir.cu) --- */
+void restir_primary(const DeviceScene &s, const PathBuffers &pb, const FrameParams &fp,
+		const RestirFrameBuffers &rb, int cur, cudaStream_t st);
+void restir_finalize(const PathBuffers &pb, const FrameParams &fp, const RestirFrameBuffers &rb,
+		const OutputBuffers &out, cudaStream_t st);
+void restir_temporal(const DeviceScene &s, const FrameParams &fp, const RestirFrameBuffers &rb,
+		const OutputBuffers &out, int cur, int prev, cudaStream_t st);
+void restir_spatial(const DeviceScene &s, const FrameParams &fp, const RestirFrameBuffers &rb,
+		const OutputBuffers &out, int in, int outbuf, cudaStream_t st);
+
+int device_sm_count();
+
+} /* namespace kgr */
+
+#endif

@@ -1,0 +1,349 @@
+/*
+ * pt.cu -- wavefront path tracer: generate -> traverse (closest) -> shade
+ * (NEE sample + BSDF sample, emits shadow rays and continuation rays into
+ * compacted queues) -> traverse (any) + resolve -> ... -> accumulate.
+ *
+ * The integrator is the recursion of source/optix/amadeus_path_tracer.cu:
+ * 133-201 (emission plus one-light NEE at every vertex, GGX continuation)
+ * unrolled forward as L = sum_k beta_k (Le_k + Ld_k), with the Russian
+ * roulette of source/optix/naive_path_tracer.cu:294-303 as an option.
+ */
+#include "kgr_device.cuh"
+#include "kgr_wavefront.h"
+
+namespace kgr {
+
+int device_sm_count()
+{
+	int dev = 0, sms = 152;
+	cudaGetDevice(&dev);
+	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+	return sms;
+}
+
+namespace {
+
+inline int grid_for(uint32_t n, int block, int per_sm = 16)
+{
+	long long blocks = ((long long)n + block - 1) / block;
+	long long cap = (long long)device_sm_count() * per_sm;
+	if (blocks < 1)
+		blocks = 1;
+	return (int)(blocks < cap ? blocks : cap);
+}
+
+__device__ __forceinline__ f3 v3(const float *p) { return mk(p[0], p[1], p[2]); }
+
+/* make_ray (amadeus_path_tracer.cu:25-56): one pcg3f draw for the jitter;
+ * the ReSTIR variant (amadeus_restir.cu:30-65) draws it but uses -0.5. */
+__device__ __forceinline__ void make_ray(const FrameParams &fp, uint32_t ix, uint32_t iy, f3 &seed,
+		f3 &origin, f3 &direction)
+{
+	f3 U = v3(fp.U), V = v3(fp.V), W = v3(fp.W);
+	pcg3f(seed);
+	float xoffset = fp.jitter ? (fract(seed.x) - 0.5f) : -0.5f;
+	float yoffset = fp.jitter ? (fract(seed.y) - 0.5f) : -0.5f;
+	float ax = ((float)ix + xoffset) / (float)fp.width;
+	float ay = ((float)iy + yoffset) / (float)fp.height;
+	float dx = 2.0f * ax - 1.0f;
+	float dy = 2.0f * ay - 1.0f;
+	origin = v3(fp.center);
+	direction = normalize(dx * U + dy * V + W);
+}
+
+__global__ void generate_kernel(PathBuffers pb, FrameParams fp)
+{
+	uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+	if (p == 0) {
+		pb.counters[CNT_Q0] = fp.paths;
+		pb.counters[CNT_Q1] = 0;
+		pb.counters[CNT_SHADOW] = 0;
+		pb.counters[CNT_BOUNCE_TOTAL] = 0;
+		pb.counters[CNT_SHADOW_TOTAL] = 0;
+	}
+	if (p >= fp.paths)
+		return;
+	uint32_t s = p / fp.npix, pix = p - s * fp.npix;
+	uint32_t ix = pix % fp.width, iy = pix / fp.width;
+	uint32_t stream = fp.frame * fp.spp + s;
+	f3 seed = pixel_seed(pix, stream, 0);
+	f3 o, d;
+	make_ray(fp, ix, iy, seed, o, d);
+	pb.ray_o[p] = f4_of(o, 0.0f);
+	pb.ray_d[p] = f4_of(d, 1e16f);
+	pb.beta[p] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+	pb.L[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+	pb.seed[p] = f4_of(seed, 0.0f);
+	pb.aov_n[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+	pb.aov_a[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+	pb.aov_p[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+	pb.queue[0][p] = p;
+}
+
+/* Sum per-thread visit counts into two 64-bit counters, one atomic per warp. */
+__device__ __forceinline__ void add_visits(unsigned long long *dst, const TraceCounters &c)
+{
+	unsigned long long a = c.nodes, b = c.tris;
+	for (int off = 16; off > 0; off >>= 1) {
+		a += __shfl_down_sync(0xffffffffu, a, off);
+		b += __shfl_down_sync(0xffffffffu, b, off);
+	}
+	if ((threadIdx.x & 31) == 0) {
+		atomicAdd(dst, a);
+		atomicAdd(dst + 1, b);
+	}
+}
+
+template <int LAYOUT, bool COUNT>
+__global__ void __launch_bounds__(128) trace_closest_kernel(DeviceScene s, PathBuffers pb, int q)
+{
+	const uint32_t n = pb.counters[q == 0 ? CNT_Q0 : CNT_Q1];
+	const uint32_t *queue = pb.queue[q];
+	uint32_t stride = gridDim.x * blockDim.x;
+	TraceCounters cnt = {0, 0};
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+		uint32_t p = queue[i];
+		float4 a = pb.ray_o[p], b = pb.ray_d[p];
+		kgr_hit h;
+		if (LAYOUT == KGR_LAYOUT_THREADED)
+			trace_threaded<false, COUNT>(s, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), b.w, h, &cnt);
+		else
+			trace_fast<false, COUNT>(s, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), b.w, h, &cnt);
+		pb.hit[p] = make_float4(__int_as_float(h.prim), h.t, h.b1, h.b2);
+	}
+	if (COUNT)
+		add_visits(pb.visits, cnt);
+}
+
+/* One vertex of amadeus_path_tracer.cu:133-201 for every queued path. */
+__global__ void __launch_bounds__(128) shade_kernel(DeviceScene s, PathBuffers pb, FrameParams fp,
+		int depth, int q, int final_seed)
+{
+	const int qn = q ^ 1;
+	const uint32_t n = pb.counters[q == 0 ? CNT_Q0 : CNT_Q1];
+	uint32_t *out_counter = pb.counters + (qn == 0 ? CNT_Q0 : CNT_Q1);
+	const uint32_t *queue = pb.queue[q];
+	uint32_t stride = gridDim.x * blockDim.x;
+	uint32_t iters = (n + stride - 1) / stride;
+	for (uint32_t it = 0; it < iters; it++) {
+		uint32_t i = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
+		bool active = i < n;
+		uint32_t p = active ? queue[i] : 0;
+		bool shadow = false, cont = false;
+		if (active) {
+			float4 hv = pb.hit[p];
+			kgr_hit h;
+			h.prim = __float_as_int(hv.x);
+			h.t = hv.y;
+			h.b1 = hv.z;
+			h.b2 = hv.w;
+			float4 dv = pb.ray_d[p];
+			f3 dir = mk(dv.x, dv.y, dv.z);
+			SurfaceHit sh;
+			if (h.prim >= 0 && surface(s, h, dir, sh)) {
+				f3 n3 = sh.n;
+				float sgn = sh.mat.type == KGR_SHADING_TRANSMISSION ? -1.0f : 1.0f;
+				sh.x = sh.x + sgn * n3 * KGR_OFFSET_EPS;
+				if (depth == 0) {
+					pb.aov_n[p] = f4_of(n3, 0.0f);
+					pb.aov_a[p] = f4_of(sh.mat.diffuse, 0.0f);
+					pb.aov_p[p] = f4_of(sh.x, 0.0f);
+				}
+				float4 sv = pb.seed[p];
+				f3 seed = mk(sv.x, sv.y, sv.z);
+				float4 bv = pb.beta[p];
+				f3 beta = mk(bv.x, bv.y, bv.z);
+				/* Ld (amadeus_common.cuh:256-286) with Ld_light (lighting.cuh:
+				 * 149-174); visibility is resolved by the shadow stage */
+				if (s.light_count == 0) {
+					f3 direct = sh.mat.emission + mk(0.0f);
+					float4 Lv = pb.L[p];
+					pb.L[p] = f4_of(mk(Lv.x, Lv.y, Lv.z) + beta * direct, 0.0f);
+				} else {
+					int total_count = (int)s.light_count;
+					unsigned int li = (unsigned int)(rand_uniform(seed) * total_count);
+					float pdf = 1.0f / total_count;
+					TriLight light = load_light(s.lights, li < s.light_count ? li : s.light_count - 1);
+					float light_pdf = 1.0f / light.area();
+					f3 lpos = sample_area_light(light, seed);
+					f3 wi = normalize(lpos - sh.x);
+					float R = length(lpos - sh.x);
+					f3 f = brdf(sh, wi);
+					float ldot = fabsf(dot(light.normal(), wi));
+					float geometric = ldot * fabsf(dot(sh.n, wi)) / (R * R);
+					f3 contr = f * light.intensity * geometric;
+					pdf *= light_pdf;
+					pb.pend_c[p] = f4_of(contr, pdf);
+					pb.pend_e[p] = f4_of(sh.mat.emission, 0.0f);
+					pb.pend_b[p] = f4_of(beta, 0.0f);
+					pb.sh_o[p] = f4_of(sh.x, 0.0f);
+					pb.sh_d[p] = f4_of(wi, R - KGR_SHADOW_EPS);
+					shadow = true;
+				}
+				/* continuation (eval, brdf.cuh:573-589) */
+				if (depth < fp.max_depth || final_seed) {
+					f3 wi;
+					float pdf = 0.0f;
+					f3 f = eval(sh, wi, pdf, seed);
+					if (pdf > 0) {
+						f3 T = f * fabsf(dot(wi, n3)) / pdf;
+						beta = beta * T;
+						bool alive = true;
+						if (fp.russian_roulette && depth >= fp.rr_start_depth) {
+							float qq = 1.0f - kmin(kmax(0.05f, beta.y), 1.0f);
+							float r = fract(seed.x);
+							if (r < qq)
+								alive = false;
+							else
+								beta = beta / (1.0f - qq);
+						}
+						if (alive && depth < fp.max_depth) {
+							pb.ray_o[p] = f4_of(sh.x, 0.0f);
+							pb.ray_d[p] = f4_of(wi, 1e16f);
+							pb.beta[p] = f4_of(beta, 0.0f);
+							cont = true;
+						}
+					}
+				}
+				pb.seed[p] = f4_of(seed, 0.0f);
+			}
+		}
+		queue_append(pb.queue[qn], out_counter, p, cont, pb.counters + CNT_BOUNCE_TOTAL);
+		queue_append(pb.shadow_queue, pb.counters + CNT_SHADOW, p, shadow, pb.counters + CNT_SHADOW_TOTAL);
+	}
+}
+
+/* is_occluded for every queued shadow ray, then Ld = contr / pdf and
+ * L += beta * (Le + Ld) in the order of the recursion. */
+template <int LAYOUT, bool COUNT>
+__global__ void __launch_bounds__(128) shadow_resolve_kernel(DeviceScene s, PathBuffers pb)
+{
+	const uint32_t n = pb.counters[CNT_SHADOW];
+	uint32_t stride = gridDim.x * blockDim.x;
+	TraceCounters cnt = {0, 0};
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+		uint32_t p = pb.shadow_queue[i];
+		float4 a = pb.sh_o[p], b = pb.sh_d[p];
+		kgr_hit h;
+		bool occ;
+		if (LAYOUT == KGR_LAYOUT_THREADED)
+			occ = trace_threaded<true, COUNT>(s, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), b.w, h, &cnt);
+		else
+			occ = trace_fast<true, COUNT>(s, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), b.w, h, &cnt);
+		float4 c = pb.pend_c[p], e = pb.pend_e[p], be = pb.pend_b[p];
+		f3 contr = occ ? mk(0.0f) : mk(c.x, c.y, c.z);
+		f3 direct = mk(e.x, e.y, e.z) + contr / c.w;
+		float4 Lv = pb.L[p];
+		pb.L[p] = f4_of(mk(Lv.x, Lv.y, Lv.z) + mk(be.x, be.y, be.z) * direct, 0.0f);
+	}
+	if (COUNT)
+		add_visits(pb.visits + 2, cnt);
+}
+
+__device__ __forceinline__ void accumulate4(float4 *buf, uint32_t i, float4 v, bool acc, float count)
+{
+	if (acc) {
+		float4 d = buf[i];
+		d.x = (d.x * count + v.x) / (count + 1);
+		d.y = (d.y * count + v.y) / (count + 1);
+		d.z = (d.z * count + v.z) / (count + 1);
+		d.w = (d.w * count + v.w) / (count + 1);
+		buf[i] = d;
+	} else {
+		buf[i] = v;
+	}
+}
+
+/* accumulate (amadeus_path_tracer.cu:59-70), the frame's samples in order */
+__global__ void accumulate_kernel(PathBuffers pb, FrameParams fp, OutputBuffers out)
+{
+	uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+	if (pix >= fp.npix)
+		return;
+	for (uint32_t sidx = 0; sidx < fp.spp; sidx++) {
+		uint32_t p = sidx * fp.npix + pix;
+		float4 L = pb.L[p];
+		f3 c = mk(L.x, L.y, L.z);
+		if (anynan(c))
+			c = mk(1.0f, 0.0f, 1.0f);
+		bool acc = fp.accumulate || sidx > 0;
+		float count = (float)(fp.accumulate ? fp.samples + (int)sidx : (int)sidx);
+		if (out.color)
+			accumulate4(out.color, pix, f4_of(c, 1.0f), acc, count);
+		if (out.normal)
+			accumulate4(out.normal, pix, pb.aov_n[p], acc, count);
+		if (out.albedo)
+			accumulate4(out.albedo, pix, pb.aov_a[p], acc, count);
+		if (out.position)
+			out.position[pix] = pb.aov_p[p];
+	}
+}
+
+} /* namespace */
+
+void reset_counters(const PathBuffers &pb, int which_mask, cudaStream_t st)
+{
+	for (int k = 0; k < CNT_COUNT; k++)
+		if (which_mask & (1 << k))
+			KGR_CUDA(cudaMemsetAsync(pb.counters + k, 0, sizeof(uint32_t), st));
+}
+
+void pt_generate(const PathBuffers &pb, const FrameParams &fp, cudaStream_t st)
+{
+	generate_kernel<<<(fp.paths + 255) / 256, 256, 0, st>>>(pb, fp);
+	KGR_CUDA(cudaGetLastError());
+}
+
+void pt_trace_closest(const DeviceScene &s, const PathBuffers &pb, int q, int layout, cudaStream_t st)
+{
+	int grid = grid_for(pb.capacity, 128);
+	bool c = pb.visits != nullptr;
+	if (layout == KGR_LAYOUT_THREADED && c)
+		trace_closest_kernel<KGR_LAYOUT_THREADED, true><<<grid, 128, 0, st>>>(s, pb, q);
+	else if (layout == KGR_LAYOUT_THREADED)
+		trace_closest_kernel<KGR_LAYOUT_THREADED, false><<<grid, 128, 0, st>>>(s, pb, q);
+	else if (c)
+		trace_closest_kernel<KGR_LAYOUT_FAST, true><<<grid, 128, 0, st>>>(s, pb, q);
+	else
+		trace_closest_kernel<KGR_LAYOUT_FAST, false><<<grid, 128, 0, st>>>(s, pb, q);
+	KGR_CUDA(cudaGetLastError());
+}
+
+void pt_shade(const DeviceScene &s, const PathBuffers &pb, const FrameParams &fp, int depth, int q,
+		cudaStream_t st)
+{
+	int grid = grid_for(pb.capacity, 128);
+	shade_kernel<<<grid, 128, 0, st>>>(s, pb, fp, depth, q, 0);
+	KGR_CUDA(cudaGetLastError());
+}
+
+void pt_shade_final_seed(const DeviceScene &s, const PathBuffers &pb, const FrameParams &fp, int depth,
+		int q, cudaStream_t st)
+{
+	int grid = grid_for(pb.capacity, 128);
+	shade_kernel<<<grid, 128, 0, st>>>(s, pb, fp, depth, q, 1);
+	KGR_CUDA(cudaGetLastError());
+}
+
+void pt_shadow_resolve(const DeviceScene &s, const PathBuffers &pb, int layout, cudaStream_t st)
+{
+	int grid = grid_for(pb.capacity, 128);
+	bool c = pb.visits != nullptr;
+	if (layout == KGR_LAYOUT_THREADED && c)
+		shadow_resolve_kernel<KGR_LAYOUT_THREADED, true><<<grid, 128, 0, st>>>(s, pb);
+	else if (layout == KGR_LAYOUT_THREADED)
+		shadow_resolve_kernel<KGR_LAYOUT_THREADED, false><<<grid, 128, 0, st>>>(s, pb);
+	else if (c)
+		shadow_resolve_kernel<KGR_LAYOUT_FAST, true><<<grid, 128, 0, st>>>(s, pb);
+	else
+		shadow_resolve_kernel<KGR_LAYOUT_FAST, false><<<grid, 128, 0, st>>>(s, pb);
+	KGR_CUDA(cudaGetLastError());
+}
+
+void pt_accumulate(const PathBuffers &pb, const FrameParams &fp, const OutputBuffers &out, cudaStream_t st)
+{
+	accumulate_kernel<<<(fp.npix + 255) / 256, 256, 0, st>>>(pb, fp, out);
+	KGR_CUDA(cudaGetLastError());
+}
+
+} /* namespace kgr */

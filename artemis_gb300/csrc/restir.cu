@@ -1,0 +1,472 @@
+/*
+ * restir.cu -- ReSTIR DI kernels: RIS at the primary vertex, the per-pixel
+ * finalisation of the initial pass, temporal reuse and spatial reuse.
+ *
+ * Follows source/optix/amadeus_restir.cu: __closesthit__initial (:437-559)
+ * for RIS with 32 candidates, __raygen__temporal (:213-291) and
+ * __raygen__spatial (:317-434) with the bias-corrected normalisation of
+ * :387-399.  Reservoirs are 32 bytes in two 16-byte SoA arrays; a sample is
+ * a light index plus the point on it (Le and the light normal are looked up
+ * from the light, which gives the same values the reference stores).
+ */
+#include "kgr_device.cuh"
+#include "kgr_wavefront.h"
+
+namespace kgr {
+
+namespace {
+
+/* Salt of the RIS reservoir's own stream (the reference seeds it from
+ * std::random_device on the host, reservoir.cuh:29-36). */
+#define KGR_RIS_SALT 0x9E3779B9u
+
+struct Sample {
+	int32_t light;
+	f3 point;
+};
+
+/* Reservoir<T>::update/resample (include/amadeus/reservoir.cuh:43-62) */
+struct Reservoir {
+	Sample data;
+	float w, W;
+	int32_t M;
+	f3 seed;
+	__device__ __forceinline__ void init(const f3 &s)
+	{
+		data.light = -1;
+		data.point = mk(0.0f);
+		w = 0.0f;
+		W = 0.0f;
+		M = 0;
+		seed = s;
+	}
+	__device__ __forceinline__ bool update(const Sample &sample, float weight)
+	{
+		w += weight;
+		float eta = rand_uniform(seed);
+		bool selected = (eta * w) < weight;
+		if (selected)
+			data = sample;
+		M++;
+		return selected;
+	}
+	__device__ __forceinline__ void resample(float target)
+	{
+		float d = target * M;
+		W = (d > 0) ? w / d : 0.0f;
+	}
+};
+
+__device__ __forceinline__ void load_res(const ReservoirBuffers &rb, uint32_t i, Sample &smp, float &w,
+		float &W, int32_t &M)
+{
+	float4 a = rb.a[i], b = rb.b[i];
+	smp.light = __float_as_int(a.w);
+	smp.point = mk(a.x, a.y, a.z);
+	w = b.x;
+	W = b.y;
+	M = __float_as_int(b.z);
+}
+
+__device__ __forceinline__ void store_res(const ReservoirBuffers &rb, uint32_t i, const Sample &smp,
+		float w, float W, int32_t M)
+{
+	rb.a[i] = make_float4(smp.point.x, smp.point.y, smp.point.z, __int_as_float(smp.light));
+	rb.b[i] = make_float4(w, W, __int_as_float(M), 0.0f);
+}
+
+__device__ __forceinline__ bool occluded(const DeviceScene &s, int layout, const f3 &o, const f3 &d, float R)
+{
+	kgr_hit h;
+	return trace<true>(s, layout, o, d, R - KGR_SHADOW_EPS, h);
+}
+
+/* target (amadeus_restir.cu:147-161) */
+__device__ __forceinline__ float target(const DeviceScene &s, const Sample &smp, const SurfaceHit &hit)
+{
+	if (smp.light < 0)
+		return 0.0f;
+	TriLight l = load_light(s.lights, (uint32_t)smp.light);
+	f3 D = smp.point - hit.x;
+	float d = length(D);
+	f3 Li = direct_unoccluded(hit, l.intensity, l.normal(), D / d, d);
+	return Li.x + Li.y + Li.z;
+}
+
+/* occluded_target (amadeus_restir.cu:163-178) via direct_occluded
+ * (amadeus_common.cuh:399-421) */
+__device__ __forceinline__ float occluded_target(const DeviceScene &s, int layout, const Sample &smp,
+		const SurfaceHit &hit)
+{
+	if (smp.light < 0)
+		return 0.0f;
+	TriLight l = load_light(s.lights, (uint32_t)smp.light);
+	f3 D = smp.point - hit.x;
+	float d = length(D);
+	f3 Dn = D / d;
+	if (occluded(s, layout, hit.x, Dn, d))
+		return 0.0f;
+	f3 Li = direct_unoccluded(hit, l.intensity, l.normal(), Dn, d);
+	return Li.x + Li.y + Li.z;
+}
+
+__device__ __forceinline__ f3 v3(const float *p) { return mk(p[0], p[1], p[2]); }
+
+/* The reuse passes rebuild the surface from the per-pixel material, the
+ * normal and position AOVs and wo = normalize(center - position)
+ * (amadeus_restir.cu:226-240, 326-336). */
+__device__ __forceinline__ SurfaceHit gbuffer_hit(const FrameParams &fp, const RestirFrameBuffers &rb,
+		const OutputBuffers &out, uint32_t pix)
+{
+	SurfaceHit h;
+	float4 pv = out.position[pix];
+	float4 nv = out.normal[pix];
+	f3 x = mk(pv.x, pv.y, pv.z);
+	h.mat = load_material(rb.materials, pix);
+	h.entering = false;
+	h.n = mk(nv.x, nv.y, nv.z);
+	h.wo = normalize(v3(fp.center) - x);
+	h.x = x;
+	return h;
+}
+
+/* RIS at the primary vertex, then the continuation ray. */
+__global__ void __launch_bounds__(128) primary_kernel(DeviceScene s, PathBuffers pb, FrameParams fp,
+		RestirFrameBuffers rb, int cur)
+{
+	const uint32_t n = pb.counters[CNT_Q0];
+	uint32_t *out_counter = pb.counters + CNT_Q1;
+	uint32_t stride = gridDim.x * blockDim.x;
+	uint32_t iters = (n + stride - 1) / stride;
+	ReservoirBuffers R = rb.res[cur];
+	for (uint32_t it = 0; it < iters; it++) {
+		uint32_t i = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
+		bool active = i < n;
+		uint32_t p = active ? pb.queue[0][i] : 0;
+		bool cont = false;
+		if (active) {
+			float4 hv = pb.hit[p];
+			kgr_hit h;
+			h.prim = __float_as_int(hv.x);
+			h.t = hv.y;
+			h.b1 = hv.z;
+			h.b2 = hv.w;
+			float4 dv = pb.ray_d[p];
+			SurfaceHit sh;
+			if (h.prim >= 0 && surface(s, h, mk(dv.x, dv.y, dv.z), sh)) {
+				f3 n3 = sh.n;
+				float sgn = sh.mat.type == KGR_SHADING_TRANSMISSION ? -1.0f : 1.0f;
+				sh.x = sh.x + sgn * n3 * KGR_OFFSET_EPS;
+				pb.aov_n[p] = f4_of(n3, 0.0f);
+				pb.aov_a[p] = f4_of(sh.mat.diffuse, 0.0f);
+				pb.aov_p[p] = f4_of(sh.x, 0.0f);
+				float4 sv = pb.seed[p];
+				f3 seed = mk(sv.x, sv.y, sv.z);
+				Reservoir res;
+				res.init(pixel_seed(p, fp.frame, KGR_RIS_SALT));
+				unsigned int total = s.light_count;
+				for (int c = 0; c < fp.candidates; c++) {
+					/* sample_direct (amadeus_common.cuh:301-377), triangle branch */
+					unsigned int li = (unsigned int)(rand_uniform(seed) * total);
+					Sample smp;
+					float pdf = 0.0f, tgt = 0.0f;
+					if (li < total) {
+						TriLight l = load_light(s.lights, li);
+						smp.point = sample_area_light(l, seed);
+						pdf = 1.0f / (l.area() * total);
+						smp.light = (int32_t)li;
+						f3 D = smp.point - sh.x;
+						float d = length(D);
+						f3 Li = direct_unoccluded(sh, l.intensity, l.normal(), D / d, d);
+						tgt = Li.x + Li.y + Li.z;
+					} else {
+						smp.light = -1;
+						smp.point = mk(0.0f);
+					}
+					res.update(smp, (pdf > 0) ? tgt / pdf : 0);
+				}
+				/* direct_occluded of the selection, resample, and the second
+				 * visibility test of :522-523 (the same ray, so the same answer) */
+				float tgt = 0.0f;
+				bool occ = false;
+				if (res.data.light >= 0) {
+					TriLight l = load_light(s.lights, (uint32_t)res.data.light);
+					f3 D = res.data.point - sh.x;
+					float d = length(D);
+					f3 Dn = D / d;
+					occ = occluded(s, fp.layout, sh.x, Dn, d);
+					if (!occ) {
+						f3 Li = direct_unoccluded(sh, l.intensity, l.normal(), Dn, d);
+						tgt = Li.x + Li.y + Li.z;
+					}
+				}
+				res.resample(tgt);
+				res.W *= 1.0f - (occ ? 1.0f : 0.0f);
+				store_res(R, p, res.data, res.w, res.W, res.M);
+				/* per-pixel material (:526) */
+				uint4 tr = __ldg(&s.tris[h.prim]);
+				const float4 *src = reinterpret_cast<const float4 *>(s.materials + tr.w);
+				float4 *dst = reinterpret_cast<float4 *>(rb.materials + p);
+				for (int k = 0; k < 4; k++)
+					dst[k] = __ldg(src + k);
+				/* continuation (:531-558) */
+				f3 wi;
+				float pdf = 0.0f;
+				f3 f = eval(sh, wi, pdf, seed);
+				if (pdf > 0) {
+					f3 T = f * fabsf(dot(wi, n3)) / pdf;
+					float4 bv = pb.beta[p];
+					f3 beta = mk(bv.x, bv.y, bv.z) * T;
+					bool alive = true;
+					if (fp.russian_roulette && 0 >= fp.rr_start_depth) {
+						float qq = 1.0f - kmin(kmax(0.05f, beta.y), 1.0f);
+						if (fract(seed.x) < qq)
+							alive = false;
+						else
+							beta = beta / (1.0f - qq);
+					}
+					if (alive && 0 < fp.max_depth) {
+						pb.ray_o[p] = f4_of(sh.x, 0.0f);
+						pb.ray_d[p] = f4_of(wi, 1e16f);
+						pb.beta[p] = f4_of(beta, 0.0f);
+						cont = true;
+					}
+				}
+				pb.seed[p] = f4_of(seed, 0.0f);
+			}
+		}
+		queue_append(pb.queue[1], out_counter, p, cont, pb.counters + CNT_BOUNCE_TOTAL);
+	}
+}
+
+__device__ __forceinline__ void accumulate4(float4 *buf, uint32_t i, float4 v, bool acc, float count)
+{
+	if (acc) {
+		float4 d = buf[i];
+		d.x = (d.x * count + v.x) / (count + 1);
+		d.y = (d.y * count + v.y) / (count + 1);
+		d.z = (d.z * count + v.z) / (count + 1);
+		d.w = (d.w * count + v.w) / (count + 1);
+		buf[i] = d;
+	} else {
+		buf[i] = v;
+	}
+}
+
+/* End of __raygen__initial (amadeus_restir.cu:126-143): indirect colour,
+ * auxiliary seed, normal/albedo AOVs accumulated, position stored. */
+__global__ void finalize_kernel(PathBuffers pb, FrameParams fp, RestirFrameBuffers rb, OutputBuffers out)
+{
+	uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+	if (pix >= fp.npix)
+		return;
+	float4 L = pb.L[pix];
+	f3 c = mk(L.x, L.y, L.z);
+	if (anynan(c))
+		c = mk(1.0f, 0.0f, 1.0f);
+	rb.intermediate[pix] = f4_of(c, 1.0f);
+	float4 sv = pb.seed[pix];
+	rb.auxiliary[pix] = make_float4(sv.x, sv.y, sv.z, 1.0f);
+	bool acc = fp.accumulate != 0;
+	float count = (float)fp.samples;
+	accumulate4(out.normal, pix, pb.aov_n[pix], acc, count);
+	accumulate4(out.albedo, pix, pb.aov_a[pix], acc, count);
+	out.position[pix] = pb.aov_p[pix];
+}
+
+/* reproject (amadeus_restir.cu:181-210); out-of-image indices rejected */
+__device__ __forceinline__ int reproject(const FrameParams &fp, int index, const f3 &x)
+{
+	if (fp.samples > 0)
+		return index;
+	const float *m = fp.prev_proj_view;
+	float q[4];
+	for (int i = 0; i < 4; i++)
+		q[i] = m[0 * 4 + i] * x.x + m[1 * 4 + i] * x.y + m[2 * 4 + i] * x.z + m[3 * 4 + i] * 1.0f;
+	float u = q[0] / q[3];
+	float v = q[1] / q[3];
+	bool in_u = (u >= -1.0f && u <= 1.0f);
+	bool in_v = (v >= -1.0f && v <= 1.0f);
+	if (!(in_u && in_v))
+		return -1;
+	u = (u + 1.0f) * 0.5f;
+	v = (v + 1.0f) * 0.5f;
+	int ix = (int)((double)(u * (float)fp.width) + 0.5);
+	int iy = (int)((double)(v * (float)fp.height) + 0.5);
+	if (ix < 0 || iy < 0 || ix >= (int)fp.width || iy >= (int)fp.height)
+		return -1;
+	return iy * (int)fp.width + ix;
+}
+
+__global__ void __launch_bounds__(128) temporal_kernel(DeviceScene s, FrameParams fp, RestirFrameBuffers rb,
+		OutputBuffers out, int cur, int prev)
+{
+	uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+	if (pix >= fp.npix)
+		return;
+	ReservoirBuffers C = rb.res[cur], P = rb.res[prev];
+	Sample cs;
+	float cw, cW;
+	int32_t cM;
+	load_res(C, pix, cs, cw, cW, cM);
+	if (cM <= 0)
+		return;
+	SurfaceHit hit = gbuffer_hit(fp, rb, out, pix);
+	int pindex = reproject(fp, (int)pix, hit.x);
+	float4 av = rb.auxiliary[pix];
+	Reservoir merged;
+	merged.init(mk(av.x, av.y, av.z));
+	float t_current = occluded_target(s, fp.layout, cs, hit);
+	merged.update(cs, t_current * cW * cM);
+	int32_t N = cM;
+	if (pindex >= 0) {
+		Sample ps;
+		float pw, pW;
+		int32_t pM;
+		load_res(P, (uint32_t)pindex, ps, pw, pW, pM);
+		if (pM > 0) {
+			pM = pM < fp.temporal_mcap ? pM : fp.temporal_mcap;
+			float t_previous = occluded_target(s, fp.layout, ps, hit);
+			merged.update(ps, t_previous * pW * pM);
+			N += (t_previous > 0) * pM;
+		}
+	}
+	merged.M = N;
+	float t_merged = target(s, merged.data, hit);
+	merged.resample(t_merged);
+	store_res(C, pix, merged.data, merged.w, merged.W, merged.M);
+}
+
+/* sample_spatial_neighborhood (amadeus_restir.cu:294-314); 2 * M_PI is the
+ * double constant of <math.h>, so theta is a double product rounded. */
+__device__ __forceinline__ int spatial_neighbor(const FrameParams &fp, int index, f3 &seed)
+{
+	int width = (int)fp.width, height = (int)fp.height;
+	int x = index % width;
+	int y = index / width;
+	f3 offset = rand_uniform_3f(seed);
+	float theta = (float)(2.0 * 3.14159265358979323846 * (double)offset.x);
+	float r = (float)fp.spatial_radius * ksqrt(offset.y);
+	float st, ct;
+	ksincos(theta, st, ct);
+	int x0 = (int)((float)x + r * ct);
+	int y0 = (int)((float)y + r * st);
+	x0 = x0 < 0 ? 0 : (x0 > width - 1 ? width - 1 : x0);
+	y0 = y0 < 0 ? 0 : (y0 > height - 1 ? height - 1 : y0);
+	return x0 + y0 * width;
+}
+
+#define KGR_MAX_NEIGHBORS 16
+
+__global__ void __launch_bounds__(128) spatial_kernel(DeviceScene s, FrameParams fp, RestirFrameBuffers rb,
+		OutputBuffers out, int inb, int outb)
+{
+	uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+	if (pix >= fp.npix)
+		return;
+	ReservoirBuffers IN = rb.res[inb], OUT = rb.res[outb];
+	SurfaceHit hit = gbuffer_hit(fp, rb, out, pix);
+	Sample cs;
+	float cw, cW;
+	int32_t cM;
+	load_res(IN, pix, cs, cw, cW, cM);
+	f3 direct = mk(0.0f);
+	if (cM > 0) {
+		float4 av = rb.auxiliary[pix];
+		Reservoir merged;
+		merged.init(mk(av.x, av.y, av.z));
+		float t_current = target(s, cs, hit);
+		merged.update(cs, t_current * cW * cM);
+		int K = fp.spatial_neighbors;
+		int32_t nidx[KGR_MAX_NEIGHBORS];
+		int32_t sizes[KGR_MAX_NEIGHBORS];
+		int32_t count = 0;
+		for (int i = 0; i < K; i++) {
+			int index0 = spatial_neighbor(fp, (int)pix, merged.seed);
+			Sample ns;
+			float nw, nW;
+			int32_t nM;
+			load_res(IN, (uint32_t)index0, ns, nw, nW, nM);
+			if (nM > 0) {
+				float t_neighbor = occluded_target(s, fp.layout, ns, hit);
+				merged.update(ns, t_neighbor * nW * nM);
+			}
+			nidx[i] = index0;
+			sizes[i] = nM;
+			count += nM;
+		}
+		merged.M = cM + count;
+		/* bias correction (:387-393): neighbours whose surface sees the
+		 * selected sample count towards Z */
+		int32_t Z = cM;
+		for (int i = 0; i < K; i++) {
+			if (sizes[i] <= 0)
+				continue;
+			SurfaceHit h0 = gbuffer_hit(fp, rb, out, (uint32_t)nidx[i]);
+			h0.wo = hit.wo;
+			h0.entering = true;
+			float t_neighbor = occluded_target(s, fp.layout, merged.data, h0);
+			if (t_neighbor > 0.0f)
+				Z += sizes[i];
+		}
+		float t_merged = target(s, merged.data, hit);
+		float denominator = t_merged * Z;
+		merged.W = (denominator > 0.0f) ? merged.w / denominator : 0.0f;
+		f3 lighting = mk(0.0f);
+		if (merged.data.light >= 0) {
+			TriLight l = load_light(s.lights, (uint32_t)merged.data.light);
+			f3 D = merged.data.point - hit.x;
+			float d = length(D);
+			f3 Dn = D / d;
+			if (!occluded(s, fp.layout, hit.x, Dn, d))
+				lighting = direct_unoccluded(hit, l.intensity, l.normal(), Dn, d);
+		}
+		direct = hit.mat.emission + lighting * merged.W;
+		store_res(OUT, pix, merged.data, merged.w, merged.W, merged.M);
+	} else {
+		float4 b = OUT.b[pix];
+		OUT.b[pix] = make_float4(0.0f, 0.0f, __int_as_float(0), b.w);
+	}
+	float4 iv = rb.intermediate[pix];
+	f3 c = direct + mk(iv.x, iv.y, iv.z);
+	float cwt = 1.0f + iv.w;
+	if (anynan(c) || kisnan(cwt)) {
+		c = mk(1.0f, 0.0f, 1.0f);
+		cwt = 1.0f;
+	}
+	accumulate4(out.color, pix, f4_of(c, cwt), fp.accumulate != 0, (float)fp.samples);
+}
+
+} /* namespace */
+
+void restir_primary(const DeviceScene &s, const PathBuffers &pb, const FrameParams &fp,
+		const RestirFrameBuffers &rb, int cur, cudaStream_t st)
+{
+	int grid = (int)((pb.capacity + 127) / 128);
+	int cap = device_sm_count() * 16;
+	primary_kernel<<<grid < cap ? grid : cap, 128, 0, st>>>(s, pb, fp, rb, cur);
+	KGR_CUDA(cudaGetLastError());
+}
+
+void restir_finalize(const PathBuffers &pb, const FrameParams &fp, const RestirFrameBuffers &rb,
+		const OutputBuffers &out, cudaStream_t st)
+{
+	finalize_kernel<<<(fp.npix + 255) / 256, 256, 0, st>>>(pb, fp, rb, out);
+	KGR_CUDA(cudaGetLastError());
+}
+
+void restir_temporal(const DeviceScene &s, const FrameParams &fp, const RestirFrameBuffers &rb,
+		const OutputBuffers &out, int cur, int prev, cudaStream_t st)
+{
+	temporal_kernel<<<(fp.npix + 127) / 128, 128, 0, st>>>(s, fp, rb, out, cur, prev);
+	KGR_CUDA(cudaGetLastError());
+}
+
+void restir_spatial(const DeviceScene &s, const FrameParams &fp, const RestirFrameBuffers &rb,
+		const OutputBuffers &out, int in, int outbuf, cudaStream_t st)
+{
+	spatial_kernel<<<(fp.npix + 127) / 128, 128, 0, st>>>(s, fp, rb, out, in, outbuf);
+	KGR_CUDA(cudaGetLastError());
+}
+
+} /* namespace kgr */

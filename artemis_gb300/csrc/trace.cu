@@ -1,0 +1,133 @@
+/*
+ * trace.cu -- ray-buffer traversal kernels behind kgr_trace_closest and
+ * kgr_trace_any: one thread per ray, rays read as two 16-byte loads
+ * {o, unused} {d, tmax}, hits written as one 16-byte store.
+ */
+#include "kgr_device.cuh"
+#include "kgr_wavefront.h"
+
+namespace kgr {
+
+namespace {
+
+template <bool ANY, int LAYOUT>
+__global__ void __launch_bounds__(128) trace_rays_kernel(DeviceScene s, const float4 *__restrict__ rays,
+		uint32_t n, kgr_hit *__restrict__ hits, uint32_t *__restrict__ occluded)
+{
+	uint32_t stride = gridDim.x * blockDim.x;
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+		float4 a = __ldg(&rays[2 * (size_t)i]);
+		float4 b = __ldg(&rays[2 * (size_t)i + 1]);
+		f3 o = mk(a.x, a.y, a.z), d = mk(b.x, b.y, b.z);
+		kgr_hit h;
+		bool r;
+		if (LAYOUT == KGR_LAYOUT_THREADED)
+			r = trace_threaded<ANY, false>(s, o, d, b.w, h);
+		else
+			r = trace_fast<ANY, false>(s, o, d, b.w, h);
+		if (ANY) {
+			occluded[i] = r ? 1u : 0u;
+		} else {
+			reinterpret_cast<float4 *>(hits)[i] = make_float4(__int_as_float(h.prim), h.t, h.b1, h.b2);
+		}
+	}
+}
+
+template <bool ANY>
+__global__ void __launch_bounds__(128) trace_stats_kernel(DeviceScene s, const float4 *__restrict__ rays,
+		uint32_t n, unsigned long long *counters)
+{
+	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	TraceCounters tf = {0, 0}, tt = {0, 0};
+	if (i < n) {
+		float4 a = __ldg(&rays[2 * (size_t)i]);
+		float4 b = __ldg(&rays[2 * (size_t)i + 1]);
+		f3 o = mk(a.x, a.y, a.z), d = mk(b.x, b.y, b.z);
+		kgr_hit h;
+		trace_fast<ANY, true>(s, o, d, b.w, h, &tf);
+		trace_threaded<ANY, true>(s, o, d, b.w, h, &tt);
+	}
+	unsigned long long v[4] = {tf.nodes, tf.tris, tt.nodes, tt.tris};
+	for (int k = 0; k < 4; k++) {
+		unsigned long long x = v[k];
+		for (int off = 16; off > 0; off >>= 1)
+			x += __shfl_down_sync(0xffffffffu, x, off);
+		if ((threadIdx.x & 31) == 0)
+			atomicAdd(&counters[k], x);
+	}
+}
+
+int grid_for(uint32_t n, int block)
+{
+	int dev = 0, sms = 152;
+	cudaGetDevice(&dev);
+	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+	long long blocks = ((long long)n + block - 1) / block;
+	long long cap = (long long)sms * 16;
+	return (int)(blocks < cap ? (blocks > 0 ? blocks : 1) : cap);
+}
+
+__global__ void read_probe_kernel(const float4 *__restrict__ buf, size_t n, float4 *sink, int iters)
+{
+	float acc = 0.0f;
+	size_t stride = (size_t)gridDim.x * blockDim.x;
+	for (int it = 0; it < iters; it++)
+		for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+			float4 v = __ldcg(&buf[i]);
+			acc += (v.x + v.y) + (v.z + v.w);
+		}
+	if (acc == 1234.5678f)
+		sink[0] = make_float4(acc, 0.0f, 0.0f, 0.0f);
+}
+
+} /* namespace */
+
+void launch_read_probe(const float4 *buf, size_t n, float4 *sink, int iters, cudaStream_t st)
+{
+	int dev = 0, sms = 152;
+	cudaGetDevice(&dev);
+	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+	read_probe_kernel<<<sms * 8, 256, 0, st>>>(buf, n, sink, iters);
+	KGR_CUDA(cudaGetLastError());
+}
+
+void launch_trace_closest(const DeviceScene &s, const float4 *rays, uint32_t n, kgr_hit *hits,
+		int layout, cudaStream_t stream)
+{
+	if (n == 0)
+		return;
+	int grid = grid_for(n, 128);
+	if (layout == KGR_LAYOUT_THREADED)
+		trace_rays_kernel<false, KGR_LAYOUT_THREADED><<<grid, 128, 0, stream>>>(s, rays, n, hits, nullptr);
+	else
+		trace_rays_kernel<false, KGR_LAYOUT_FAST><<<grid, 128, 0, stream>>>(s, rays, n, hits, nullptr);
+	KGR_CUDA(cudaGetLastError());
+}
+
+void launch_trace_any(const DeviceScene &s, const float4 *rays, uint32_t n, uint32_t *occluded,
+		int layout, cudaStream_t stream)
+{
+	if (n == 0)
+		return;
+	int grid = grid_for(n, 128);
+	if (layout == KGR_LAYOUT_THREADED)
+		trace_rays_kernel<true, KGR_LAYOUT_THREADED><<<grid, 128, 0, stream>>>(s, rays, n, nullptr, occluded);
+	else
+		trace_rays_kernel<true, KGR_LAYOUT_FAST><<<grid, 128, 0, stream>>>(s, rays, n, nullptr, occluded);
+	KGR_CUDA(cudaGetLastError());
+}
+
+void launch_trace_stats(const DeviceScene &s, const float4 *rays, uint32_t n, int any,
+		unsigned long long *counters, cudaStream_t stream)
+{
+	if (n == 0)
+		return;
+	int grid = (int)((n + 127) / 128);
+	if (any)
+		trace_stats_kernel<true><<<grid, 128, 0, stream>>>(s, rays, n, counters);
+	else
+		trace_stats_kernel<false><<<grid, 128, 0, stream>>>(s, rays, n, counters);
+	KGR_CUDA(cudaGetLastError());
+}
+
+} /* namespace kgr */

@@ -1,0 +1,402 @@
+"""ctypes binding of libkgr (include/kgr.h).
+
+The Python side is a thin mirror of the C ABI used by the tests and the
+benchmark: scenes, traversal calls and the attachment life cycle of the
+reference's AttachmentRTX (attach, load, set_option/get_option, render,
+unload).  All compute goes through libkgr's CUDA kernels; there is no
+Python or CPU fallback.  Device buffers are passed as raw pointers (for
+example torch CUDA tensors' data_ptr()).
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+c_u32, c_i32, c_u64, c_f = ctypes.c_uint32, ctypes.c_int32, ctypes.c_uint64, ctypes.c_float
+vp = ctypes.c_void_p
+
+LAYOUT_FAST, LAYOUT_THREADED = 0, 1
+BUILDER_SAH, BUILDER_KOBRA = 0, 1
+VALUE_NONE, VALUE_INT, VALUE_FLOAT, VALUE_BOOL, VALUE_STRING = range(5)
+
+
+class KgrError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"kgr status {status}: {msg}")
+        self.status = status
+
+
+class Mesh(ctypes.Structure):
+    _fields_ = [("positions", vp), ("normals", vp), ("vertex_count", c_u32), ("indices", vp),
+                ("material_indices", vp), ("triangle_count", c_u32), ("model", vp)]
+
+
+class SceneOptions(ctypes.Structure):
+    _fields_ = [("builder", c_i32), ("max_leaf_size", c_i32), ("device", c_i32), ("reserved", c_i32)]
+
+
+class SceneInfo(ctypes.Structure):
+    _fields_ = [("vertex_count", c_u32), ("triangle_count", c_u32), ("light_count", c_u32),
+                ("material_count", c_u32), ("bvh_vec4_count", c_u32), ("fast_node_count", c_u32),
+                ("device_bytes", c_u64), ("build_ms", ctypes.c_double),
+                ("bounds_min", c_f * 3), ("bounds_max", c_f * 3)]
+
+
+class Value(ctypes.Structure):
+    _fields_ = [("tag", c_i32), ("i", c_i32), ("f", c_f), ("b", c_i32), ("s", ctypes.c_char_p)]
+
+
+class Context(ctypes.Structure):
+    _fields_ = [("width", c_u32), ("height", c_u32), ("device", c_i32), ("reserved", c_i32)]
+
+
+class _Camera(ctypes.Structure):
+    _fields_ = [("center", c_f * 3), ("ax_u", c_f * 3), ("ax_v", c_f * 3), ("ax_w", c_f * 3),
+                ("projection", c_f * 16), ("view", c_f * 16)]
+
+
+class _Lights(ctypes.Structure):
+    _fields_ = [("tri_lights", vp), ("tri_count", c_i32), ("quad_count", c_i32)]
+
+
+class _Buffers(ctypes.Structure):
+    _fields_ = [("color", vp), ("normal", vp), ("albedo", vp), ("position", vp)]
+
+
+class LaunchInfo(ctypes.Structure):
+    _fields_ = [("resolution", c_f * 2), ("camera", _Camera), ("lights", _Lights), ("buffers", _Buffers),
+                ("materials", vp), ("has_environment_map", c_i32), ("accumulate", c_i32), ("time", c_f),
+                ("max_depth", c_i32), ("samples", c_i32), ("frame", c_u32)]
+
+
+class RenderStats(ctypes.Structure):
+    _fields_ = [("camera_rays", c_u64), ("bounce_rays", c_u64), ("shadow_rays", c_u64),
+                ("kernel_launches", c_u32), ("reserved", c_u32)]
+
+
+class GeneratedView(ctypes.Structure):
+    _fields_ = [("positions", vp), ("normals", vp), ("vertex_count", c_u32), ("indices", vp),
+                ("material_indices", vp), ("triangle_count", c_u32), ("materials", vp),
+                ("material_count", c_u32), ("camera_eye", c_f * 3), ("camera_target", c_f * 3),
+                ("camera_fov_deg", c_f)]
+
+
+class PluginRet(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char_p), ("ptr", vp)]
+
+
+_LIB = None
+
+
+def lib():
+    """Load libkgr.so, building it first if it is missing."""
+    global _LIB
+    if _LIB is None:
+        path = _build.LIB
+        if not os.path.exists(path):
+            _build.build()
+        L = ctypes.CDLL(path)
+        sigs = {
+            "kgr_status_string": (ctypes.c_char_p, [c_i32]),
+            "kgr_last_error": (ctypes.c_char_p, []),
+            "kgr_abi_version": (ctypes.c_int, []),
+            "kgr_scene_create": (c_i32, [vp, c_u32, vp, c_u32, vp, vp]),
+            "kgr_scene_create_from_bvh": (c_i32, [vp, c_u32, vp, c_u32, vp, c_u32, c_i32, vp]),
+            "kgr_scene_info_get": (c_i32, [vp, vp]),
+            "kgr_bvh_build_host": (c_i32, [vp, c_u32, vp, c_u32, c_i32, c_i32, vp, c_u32, vp]),
+            "kgr_scene_copy_bvh": (c_i32, [vp, vp, c_u32, vp]),
+            "kgr_scene_copy_lights": (c_i32, [vp, vp, c_u32, vp]),
+            "kgr_scene_destroy": (c_i32, [vp]),
+            "kgr_trace_closest": (c_i32, [vp, vp, c_u32, vp, c_i32, vp]),
+            "kgr_trace_any": (c_i32, [vp, vp, c_u32, vp, c_i32, vp]),
+            "kgr_trace_closest_host": (c_i32, [vp, vp, c_u32, vp, c_i32]),
+            "kgr_trace_any_host": (c_i32, [vp, vp, c_u32, vp, c_i32]),
+            "kgr_trace_counts": (c_i32, [vp, vp, c_u32, c_i32, vp]),
+            "kgr_create": (c_i32, [ctypes.c_char_p, vp]),
+            "kgr_attach": (c_i32, [vp, vp]),
+            "kgr_load": (c_i32, [vp]),
+            "kgr_unload": (c_i32, [vp]),
+            "kgr_set_option": (c_i32, [vp, ctypes.c_char_p, vp]),
+            "kgr_get_option": (c_i32, [vp, ctypes.c_char_p, vp]),
+            "kgr_render": (c_i32, [vp, vp, vp, vp]),
+            "kgr_destroy": (c_i32, [vp]),
+            "kgr_get_render_stats": (c_i32, [vp, vp]),
+            "kgr_debug_copy": (c_i32, [vp, ctypes.c_char_p, vp, c_u64]),
+            "kgr_get_stage_times": (c_i32, [vp, vp, vp, c_u32]),
+            "kgr_get_visit_counts": (c_i32, [vp, vp]),
+            "kgr_measure_read_bandwidth": (c_i32, [c_i32, c_u64, c_i32, vp]),
+            "kgr_load_attachment": (PluginRet, [ctypes.c_char_p]),
+            "kgr_generate_scene": (c_i32, [ctypes.c_char_p, c_u64, vp]),
+            "kgr_generated_get": (c_i32, [vp, vp]),
+            "kgr_generated_destroy": (c_i32, [vp]),
+            "kgr_camera_setup": (c_i32, [vp, vp, vp, c_f, c_f, vp]),
+        }
+        for name, (res, args) in sigs.items():
+            fn = getattr(L, name)
+            fn.restype, fn.argtypes = res, args
+        _LIB = L
+    return _LIB
+
+
+def check(status):
+    if status != 0:
+        msg = lib().kgr_last_error().decode(errors="replace")
+        raise KgrError(status, msg)
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(vp)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _u32(a):
+    return np.ascontiguousarray(a, dtype=np.uint32)
+
+
+MATERIAL_DTYPE = np.dtype([("diffuse", "<f4", 3), ("specular", "<f4", 3), ("emission", "<f4", 3),
+                           ("ambient", "<f4", 3), ("shininess", "<f4"), ("roughness", "<f4"),
+                           ("refraction", "<f4"), ("type", "<i4")])
+
+
+def bvh_build_host(positions, indices, builder=BUILDER_SAH, max_leaf=4):
+    """Threaded bvh.cpp-layout buffer built on the host (no device needed)."""
+    pos, idx = _f32(positions), _u32(indices)
+    n = c_u32()
+    check(lib().kgr_bvh_build_host(_ptr(pos), len(pos), _ptr(idx), len(idx), builder, max_leaf, None, 0,
+                                   ctypes.byref(n)))
+    out = np.zeros((n.value, 4), np.float32)
+    check(lib().kgr_bvh_build_host(_ptr(pos), len(pos), _ptr(idx), len(idx), builder, max_leaf, _ptr(out),
+                                   n.value, ctypes.byref(n)))
+    return out
+
+
+class Generated:
+    """Host arrays of a procedural scene (copied out of the library)."""
+
+    def __init__(self, name, seed=0):
+        h = vp()
+        check(lib().kgr_generate_scene(name.encode(), seed, ctypes.byref(h)))
+        try:
+            v = GeneratedView()
+            check(lib().kgr_generated_get(h, ctypes.byref(v)))
+            V, T, M = v.vertex_count, v.triangle_count, v.material_count
+            self.positions = np.ctypeslib.as_array((c_f * (3 * V)).from_address(v.positions)).reshape(V, 3).copy()
+            self.normals = np.ctypeslib.as_array((c_f * (3 * V)).from_address(v.normals)).reshape(V, 3).copy()
+            self.indices = np.ctypeslib.as_array((c_u32 * (3 * T)).from_address(v.indices)).reshape(T, 3).copy()
+            self.material_indices = np.ctypeslib.as_array((c_u32 * T).from_address(v.material_indices)).copy()
+            raw = np.ctypeslib.as_array((c_f * (16 * M)).from_address(v.materials)).copy()
+            self.materials = raw.view(MATERIAL_DTYPE)
+            self.materials_raw = raw.reshape(M, 16)
+            self.eye = np.array(v.camera_eye[:], np.float32)
+            self.target = np.array(v.camera_target[:], np.float32)
+            self.fov = float(v.camera_fov_deg)
+        finally:
+            lib().kgr_generated_destroy(h)
+
+    def tris4(self):
+        return np.concatenate([self.indices, self.material_indices[:, None]], axis=1).astype(np.uint32)
+
+
+class Scene:
+    """A device-resident scene: triangles, materials, lights and both BVH layouts."""
+
+    def __init__(self, positions, indices, materials_raw, normals=None, material_indices=None,
+                 builder=BUILDER_SAH, max_leaf=4, device=-1, bvh=None):
+        self._keep = [_f32(positions), None if normals is None else _f32(normals), _u32(indices),
+                      None if material_indices is None else _u32(material_indices),
+                      _f32(materials_raw)]
+        pos, nrm, idx, mid, mats = self._keep
+        mesh = Mesh(_ptr(pos), _ptr(nrm), len(pos), _ptr(idx), _ptr(mid), len(idx), None)
+        h = vp()
+        if bvh is None:
+            opt = SceneOptions(builder, max_leaf, device, 0)
+            check(lib().kgr_scene_create(ctypes.byref(mesh), 1, _ptr(mats), len(mats), ctypes.byref(opt),
+                                         ctypes.byref(h)))
+        else:
+            b = _f32(bvh)
+            check(lib().kgr_scene_create_from_bvh(ctypes.byref(mesh), 1, _ptr(mats), len(mats), _ptr(b),
+                                                  len(b), device, ctypes.byref(h)))
+        self.handle = h
+
+    @classmethod
+    def from_generated(cls, g, **kw):
+        return cls(g.positions, g.indices, g.materials_raw, normals=g.normals,
+                   material_indices=g.material_indices, **kw)
+
+    def info(self):
+        i = SceneInfo()
+        check(lib().kgr_scene_info_get(self.handle, ctypes.byref(i)))
+        return i
+
+    def bvh(self):
+        n = c_u32()
+        check(lib().kgr_scene_copy_bvh(self.handle, None, 0, ctypes.byref(n)))
+        out = np.zeros((n.value, 4), np.float32)
+        check(lib().kgr_scene_copy_bvh(self.handle, _ptr(out), n.value, ctypes.byref(n)))
+        return out
+
+    def lights(self):
+        n = c_u32()
+        check(lib().kgr_scene_copy_lights(self.handle, None, 0, ctypes.byref(n)))
+        out = np.zeros((n.value, 12), np.float32)
+        check(lib().kgr_scene_copy_lights(self.handle, _ptr(out), n.value, ctypes.byref(n)))
+        return out
+
+    def trace_closest(self, rays_ptr, n, hits_ptr, layout=LAYOUT_FAST, stream=None):
+        check(lib().kgr_trace_closest(self.handle, rays_ptr, n, hits_ptr, layout, stream))
+
+    def trace_any(self, rays_ptr, n, occ_ptr, layout=LAYOUT_FAST, stream=None):
+        check(lib().kgr_trace_any(self.handle, rays_ptr, n, occ_ptr, layout, stream))
+
+    def trace_closest_host(self, rays, layout=LAYOUT_FAST):
+        rays = _f32(rays)
+        hits = np.zeros((len(rays), 4), np.float32)
+        check(lib().kgr_trace_closest_host(self.handle, _ptr(rays), len(rays), _ptr(hits), layout))
+        return hits
+
+    def trace_any_host(self, rays, layout=LAYOUT_FAST):
+        rays = _f32(rays)
+        occ = np.zeros(len(rays), np.uint32)
+        check(lib().kgr_trace_any_host(self.handle, _ptr(rays), len(rays), _ptr(occ), layout))
+        return occ
+
+    def trace_counts(self, rays_ptr, n, any_hit=False):
+        out = (c_u64 * 4)()
+        check(lib().kgr_trace_counts(self.handle, rays_ptr, n, 1 if any_hit else 0, out))
+        return list(out)
+
+    def close(self):
+        if self.handle:
+            lib().kgr_scene_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def read_bandwidth(nbytes, iters, device=-1):
+    """GB/s of a streaming read of nbytes, repeated iters times (best of 5)."""
+    out = ctypes.c_double()
+    check(lib().kgr_measure_read_bandwidth(device, nbytes, iters, ctypes.byref(out)))
+    return out.value
+
+
+def camera(eye, target, fov, aspect, up=(0.0, 1.0, 0.0)):
+    """uvw_frame + projection/view matrices filled into a fresh LaunchInfo."""
+    info = LaunchInfo()
+    e, t, u = _f32(eye), _f32(target), _f32(up)
+    check(lib().kgr_camera_setup(_ptr(e), _ptr(t), _ptr(u), fov, aspect, ctypes.byref(info)))
+    return info
+
+
+def camera_dict(info):
+    c = info.camera
+    return {"center": list(c.center), "ax_u": list(c.ax_u), "ax_v": list(c.ax_v), "ax_w": list(c.ax_w),
+            "projection": list(c.projection), "view": list(c.view)}
+
+
+class Attachment:
+    """kgr_attachment: the AttachmentRTX life cycle over the C ABI."""
+
+    def __init__(self, kind="path_tracer"):
+        h = vp()
+        check(lib().kgr_create(kind.encode(), ctypes.byref(h)))
+        self.handle = h
+        self.kind = kind
+
+    def attach(self, width, height, device=-1):
+        ctx = Context(width, height, device, 0)
+        check(lib().kgr_attach(self.handle, ctypes.byref(ctx)))
+
+    def load(self):
+        check(lib().kgr_load(self.handle))
+
+    def unload(self):
+        check(lib().kgr_unload(self.handle))
+
+    def set_option(self, name, value):
+        v = Value()
+        if isinstance(value, bool):
+            v.tag, v.b = VALUE_BOOL, int(value)
+        elif isinstance(value, int):
+            v.tag, v.i = VALUE_INT, value
+        elif isinstance(value, float):
+            v.tag, v.f = VALUE_FLOAT, value
+        elif isinstance(value, str):
+            v.tag, v.s = VALUE_STRING, value.encode()
+        else:
+            raise TypeError(type(value))
+        check(lib().kgr_set_option(self.handle, name.encode(), ctypes.byref(v)))
+
+    def get_option(self, name):
+        v = Value()
+        check(lib().kgr_get_option(self.handle, name.encode(), ctypes.byref(v)))
+        if v.tag == VALUE_INT:
+            return v.i
+        if v.tag == VALUE_FLOAT:
+            return v.f
+        if v.tag == VALUE_BOOL:
+            return bool(v.b)
+        if v.tag == VALUE_STRING:
+            return v.s.decode()
+        return None
+
+    def render(self, info, scene, stream=None):
+        check(lib().kgr_render(self.handle, ctypes.byref(info), scene.handle, stream))
+
+    def stats(self):
+        s = RenderStats()
+        check(lib().kgr_get_render_stats(self.handle, ctypes.byref(s)))
+        return s
+
+    STAGES = ("generate", "trace_closest", "shade", "shadow", "accumulate", "restir_primary",
+              "restir_temporal", "restir_spatial", "restir_finalize")
+
+    def stage_times(self):
+        """{stage: (total ms, launches)} since the last call ("profile" option)."""
+        n = len(self.STAGES)
+        ms = (ctypes.c_double * n)()
+        la = (c_u32 * n)()
+        check(lib().kgr_get_stage_times(self.handle, ms, la, n))
+        return {s: (ms[i], la[i]) for i, s in enumerate(self.STAGES)}
+
+    def visit_counts(self):
+        out = (c_u64 * 4)()
+        check(lib().kgr_get_visit_counts(self.handle, out))
+        return list(out)
+
+    def debug_copy(self, what, out):
+        check(lib().kgr_debug_copy(self.handle, what.encode(), _ptr(out), out.nbytes))
+        return out
+
+    def close(self):
+        if self.handle:
+            lib().kgr_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def launch_info(cam_info, width, height, buffers, max_depth=2, samples=0, accumulate=False, frame=0):
+    """Fill a LaunchInfo from a camera LaunchInfo and four device pointers."""
+    info = LaunchInfo()
+    ctypes.pointer(info)[0] = cam_info
+    info.resolution[0], info.resolution[1] = float(width), float(height)
+    info.buffers.color, info.buffers.normal, info.buffers.albedo, info.buffers.position = buffers
+    info.max_depth = max_depth
+    info.samples = samples
+    info.accumulate = 1 if accumulate else 0
+    info.frame = frame
+    return info

@@ -1,0 +1,370 @@
+#!/usr/bin/env python
+"""Headline benchmark: the plain unidirectional path tracer at 1920x1080,
+4 spp, max depth 8, Russian roulette from depth 3, next-event estimation
+against 1024 emissive triangles, on a seeded procedural scene of 1.16M
+triangles (512x512 value-noise height field + 2000 icospheres of 320
+triangles + 512 emissive quads), SAH BVH with leaves of at most 4.
+
+One step renders one frame through the attachment API (kgr_render).  `value`
+is Mrays/s (camera + bounce + shadow rays) with the scene resident on the
+device; `e2e` is the same metric through the C ABI with the frame read back
+to pinned host memory every step.  The roofline entry is computed live from
+CUDA events the library records after every launch on the render stream and
+from the traversal visit counts of one counting frame.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Under torchrun each rank renders its own frame (replicas: the path does not
+shard across GPUs); `value` is the sum over ranks divided by the slowest
+rank's time.  `--impl reference` times the reference's per-pixel CPU path
+(the oracle restatement) on all host cores on a bounded crop of the same
+frame.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "1080p ms/frame & Mrays/s at equal relMSE vs plain GPU PT; serve p50/p99 latency"
+WORKLOAD = ("plain PT 1920x1080 4spp, max depth 8, RR from depth 3, NEE over 1024 emissive tris; "
+            "procedural terrain 1.16M tris (512^2 height field + 2000 icospheres), SAH leaves<=4")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--spp", type=int, default=4)
+    ap.add_argument("--max-depth", type=int, default=8)
+    ap.add_argument("--scene", default="terrain")
+    ap.add_argument("--layout", default="fast", choices=["fast", "threaded"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU sample time per measurement")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_scene(name):
+    from artemis_gb300 import kgr
+    g = kgr.Generated(name, 1)
+    sc = kgr.Scene.from_generated(g, builder=kgr.BUILDER_SAH, max_leaf=4)
+    return g, sc
+
+
+def cpu_sample(g, sc, args, target_s):
+    """Oracle PT (reference per-pixel path, all host cores) on a crop of rows
+    of the same frame, sized to about target_s seconds.  Returns
+    (Mrays/s, cores, description, ms per full frame)."""
+    from artemis_gb300 import kgr
+    from oracle import pyoracle
+    osc = pyoracle.Scene(g.positions, g.normals, g.tris4(), g.materials_raw, sc.lights(), sc.bvh())
+    cam = kgr.camera(g.eye, g.target, g.fov, args.width / args.height)
+    cores = os.cpu_count() or 1
+    mid = args.height // 2
+
+    def run(rows, frame=0):
+        r0 = max(0, mid - rows // 2)
+        p = pyoracle.render_params(args.width, args.height, kgr.camera_dict(cam), max_depth=args.max_depth,
+                                   spp=args.spp, russian_roulette=1, rr_start_depth=3, frame=frame,
+                                   row_begin=r0, row_end=min(args.height, r0 + rows), threads=cores)
+        bufs = [np.zeros((args.width * args.height, 4), np.float32) for _ in range(4)]
+        t = time.perf_counter()
+        _, st = pyoracle.render_pt(osc, p, bufs)
+        dt = time.perf_counter() - t
+        return dt, st.camera_rays + st.bounce_rays + st.shadow_rays, min(args.height, r0 + rows) - r0
+
+    dt, rays, rows = run(4)
+    want = int(max(4, min(args.height, 4 * target_s / max(dt, 1e-3))))
+    return run, want, cores
+
+
+def bench_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    g, sc = make_scene_cpu(args.scene)
+    run, rows, cores = cpu_sample(g, sc, args, args.cpu_seconds)
+    for _ in range(args.warmup):
+        run(max(4, rows // 8))
+    times, rays_total, rows_done = [], 0, 0
+    for s in range(args.steps):
+        dt, rays, r = run(rows, frame=s)
+        times.append(dt)
+        rays_total += rays
+        rows_done += r
+    mrays = rays_total / sum(times) / 1e6
+    ms_frame = sum(times) / rows_done * args.height * 1e3
+    sample = f"{rows} centre rows x {args.width} px x {args.spp} spp per step ({rows / args.height:.3f} of the frame)"
+    line = {"metric": METRIC, "value": round(mrays, 4), "unit": "Mrays/s", "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms_frame, 2), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+            "config": {"workload": WORKLOAD, "crop": sample, "l2_flush": False},
+            "cpu_baseline": {"value": round(mrays, 4), "unit": "Mrays/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(mrays, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def make_scene_cpu(name):
+    """Scene arrays and BVH without a device (the reference arm runs on CPU)."""
+    from artemis_gb300 import kgr
+
+    class CpuScene:
+        def __init__(self, g):
+            self._bvh = kgr.bvh_build_host(g.positions, g.indices, kgr.BUILDER_SAH, 4)
+            em = g.materials["emission"][g.material_indices]
+            lit = np.nonzero(em.max(axis=1) > 0)[0]
+            p = g.positions[g.indices[lit]]
+            self._lights = np.concatenate([p[:, 0], p[:, 1] - p[:, 0], p[:, 2] - p[:, 0], em[lit]],
+                                          axis=1).astype(np.float32)
+
+        def bvh(self):
+            return self._bvh
+
+        def lights(self):
+            return self._lights
+
+    g = kgr.Generated(name, 1)
+    return g, CpuScene(g)
+
+
+def bench_ours(args):
+    import torch
+
+    from artemis_gb300 import kgr
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.cuda.current_device()
+    W, H = args.width, args.height
+    g, sc = make_scene(args.scene)
+    info_s = sc.info()
+    cam = kgr.camera(g.eye, g.target, g.fov, W / H)
+    bufs = [torch.zeros((W * H, 4), dtype=torch.float32, device="cuda") for _ in range(4)]
+    att = kgr.Attachment("path_tracer")
+    att.attach(W, H, dev)
+    att.load()
+    att.set_option("spp", args.spp)
+    att.set_option("russian_roulette", True)
+    att.set_option("rr_start_depth", 3)
+    att.set_option("layout", args.layout)
+    stream = torch.cuda.current_stream()
+    sptr = ctypes.c_void_p(stream.cuda_stream)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def info_for(step, samples=0):
+        return kgr.launch_info(cam, W, H, [b.data_ptr() for b in bufs], max_depth=args.max_depth,
+                               samples=samples, accumulate=False, frame=step)
+
+    for s in range(args.warmup):
+        att.render(info_for(s), sc, sptr)
+    torch.cuda.synchronize()
+
+    # traversal visit counts of one frame (untimed): algorithmic bytes
+    att.set_option("count_visits", True)
+    att.render(info_for(0), sc, sptr)
+    torch.cuda.synchronize()
+    visits = att.visit_counts()
+    att.set_option("count_visits", False)
+    att.stats()
+
+    # timed region
+    att.set_option("profile", True)
+    att.stage_times()
+    clocks = ClockSampler(dev)
+    clocks.start()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    step_ms, rays = [], 0
+    for s in range(args.steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        att.render(info_for(args.warmup + s), sc, sptr)
+        e1.record(stream)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        st = att.stats()
+        rays += st.camera_rays + st.bounce_rays + st.shadow_rays
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    stages = att.stage_times()
+    att.set_option("profile", False)
+    launches_per_frame = st.kernel_launches
+    total_ms = float(sum(step_ms))
+    if ws > 1:
+        t = torch.tensor([total_ms, float(rays)], dtype=torch.float64, device="cuda")
+        tmax = t.clone()
+        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
+        total_ms, rays = float(tmax[0]), float(t[1])
+    value = rays / (total_ms * 1e-3) / 1e6
+
+    # end to end through the C ABI with the frame read back to pinned host memory
+    host = torch.empty((W * H, 4), dtype=torch.float32, pin_memory=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_rays = 0
+    for s in range(args.steps):
+        att.render(info_for(1000 + s), sc, sptr)
+        host.copy_(bufs[0], non_blocking=True)
+        stream.synchronize()
+        st = att.stats()
+        e2e_rays += st.camera_rays + st.bounce_rays + st.shadow_rays
+    e2e_s = time.perf_counter() - t0
+    e2e_value = e2e_rays / e2e_s / 1e6
+
+    peaks, peak_kind = measured_peaks()
+    l2_gbs = kgr.read_bandwidth(64 << 20, 50, dev)
+    # dominant kernel and its algorithmic bytes per launch (fast layout: 64 B
+    # child-pair node, 48 B triangle record)
+    node_b, tri_b = (64, 48) if args.layout == "fast" else (48, 80)
+    per_stage_bytes = {"trace_closest": visits[0] * node_b + visits[1] * tri_b,
+                       "shadow": visits[2] * node_b + visits[3] * tri_b}
+    dom = max(("trace_closest", "shadow"), key=lambda k: stages[k][0])
+    ms_dom, n_dom = stages[dom]
+    launches_frame = n_dom / max(1, args.steps)
+    bytes_per_launch = per_stage_bytes[dom] / max(1, launches_frame)
+    achieved = bytes_per_launch / (ms_dom / max(1, n_dom) * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                "frac": round(achieved / peaks.get("hbm_gbs"), 4), "traffic": None,
+                "kernel": dom + "_kernel", "peak_source": peak_kind,
+                "l2": {"peak_measured_read_gbs": round(l2_gbs, 1), "frac": round(achieved / l2_gbs, 4)}}
+
+    cpu_base = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            run, rows, cores = cpu_sample(g, sc, args, args.cpu_seconds)
+            dt, crays, r = run(rows)
+            cpu_base = {"value": round(crays / dt / 1e6, 4), "unit": "Mrays/s", "cores": cores, "kind": "port",
+                        "sample": f"{r} centre rows x {W} px x {args.spp} spp ({dt:.1f} s)"}
+        except Exception as exc:  # the baseline is reported, not required
+            cpu_base = {"value": None, "unit": "Mrays/s", "cores": os.cpu_count(), "kind": "port",
+                        "sample": f"failed: {exc}"}
+
+    if rank == 0:
+        stage_ms = {k: round(v[0] / max(1, args.steps), 3) for k, v in stages.items() if v[1]}
+        line = {"metric": METRIC, "value": round(value, 2), "unit": "Mrays/s", "n_gpus": ws,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded procedural scene, random-free camera)",
+                "config": {"workload": WORKLOAD, "scene": args.scene, "triangles": info_s.triangle_count,
+                           "lights": info_s.light_count, "resolution": [W, H], "spp": args.spp,
+                           "max_depth": args.max_depth, "layout": args.layout,
+                           "l2_flush": "256 MB buffer written between timed steps",
+                           "parallelism": "replicas" if ws > 1 else "1 GPU"},
+                "ms_per_frame": round(total_ms / args.steps, 3),
+                "rays_per_frame": int(rays / args.steps / max(1, ws)),
+                "stage_ms_per_frame": stage_ms,
+                "roofline": roofline,
+                "cpu_baseline": cpu_base,
+                "e2e": {"value": round(e2e_value, 2), "unit": "Mrays/s",
+                        "h2d_bytes_per_step": ctypes.sizeof(kgr.LaunchInfo),
+                        "d2h_bytes_per_step": W * H * 16},
+                "gpu_launches": int(launches_per_frame * args.steps),
+                "clocks": clk,
+                "scene_build_ms": round(info_s.build_ms, 1)}
+        print(json.dumps(line))
+    att.close()
+    sc.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        bench_reference(args)
+    else:
+        bench_ours(args)
+
+
+if __name__ == "__main__":
+    main()

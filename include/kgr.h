@@ -160,6 +160,13 @@ kgr_status kgr_scene_create_from_bvh(const kgr_mesh *meshes, uint32_t mesh_count
 
 kgr_status kgr_scene_info_get(const kgr_scene *scene, kgr_scene_info *info);
 
+/* Host-only BVH build (no device needed): the threaded bvh.cpp-layout
+ * buffer kgr_scene_create would build for one mesh.  Call with out_vec4 =
+ * NULL to learn the size. */
+kgr_status kgr_bvh_build_host(const float *positions, uint32_t vertex_count,
+		const uint32_t *indices, uint32_t triangle_count, int32_t builder,
+		int32_t max_leaf_size, float *out_vec4, uint32_t capacity, uint32_t *count);
+
 /* Host copy of the threaded bvh.cpp-layout buffer (capacity in vec4 units). */
 kgr_status kgr_scene_copy_bvh(const kgr_scene *scene, float *out_vec4,
 		uint32_t capacity, uint32_t *count);
@@ -209,6 +216,12 @@ kgr_status kgr_trace_closest_host(const kgr_scene *scene, const float *rays,
 		uint32_t n, kgr_hit *hits, int32_t layout);
 kgr_status kgr_trace_any_host(const kgr_scene *scene, const float *rays,
 		uint32_t n, uint32_t *occluded, int32_t layout);
+
+/* Visit counts for n device rays (synchronous, diagnostics and roofline
+ * accounting): counts[0..1] = internal nodes and triangles visited on the
+ * fast layout, counts[2..3] = the same on the threaded layout. */
+kgr_status kgr_trace_counts(const kgr_scene *scene, const float *rays, uint32_t n,
+		int32_t any, uint64_t counts[4]);
 
 /* ----------------------------------------------------------- attachments -- */
 
@@ -287,6 +300,32 @@ typedef struct kgr_render_stats {
 	uint32_t reserved;
 } kgr_render_stats;
 kgr_status kgr_get_render_stats(const kgr_attachment *att, kgr_render_stats *stats);
+
+/* Per-stage device time of the frames rendered since the last call, when
+ * the "profile" option is on: a CUDA event is recorded on the render stream
+ * after every launch, and the time between consecutive events is charged to
+ * the stage that launched.  Stages: 0 generate, 1 closest-hit traversal,
+ * 2 shade, 3 shadow rays (any-hit traversal + resolve), 4 accumulate,
+ * 5 ReSTIR RIS, 6 temporal, 7 spatial, 8 ReSTIR finalise.  Synchronises on
+ * the last event, then resets the totals. */
+kgr_status kgr_get_stage_times(kgr_attachment *att, double *ms, uint32_t *launches, uint32_t count);
+
+/* Traversal visit counts of the last frame rendered with the
+ * "count_visits" option: {closest nodes, closest triangles, shadow nodes,
+ * shadow triangles} on the layout the frame used. */
+kgr_status kgr_get_visit_counts(const kgr_attachment *att, uint64_t counts[4]);
+
+/* Streaming-read bandwidth probe (GB/s, best of 5): a buffer of `bytes`
+ * read `iters` times with 16-byte L2-cached loads.  A buffer well below the
+ * L2 size measures L2 bandwidth, one well above measures HBM. */
+kgr_status kgr_measure_read_bandwidth(int32_t device, uint64_t bytes, int32_t iters, double *gbps);
+
+/* Copy an internal per-pixel buffer of a ReSTIR attachment to the host
+ * (synchronous; for inspection and tests): "reservoir_prev_a",
+ * "reservoir_prev_b" (the 32-byte reservoirs kept for the next frame, as
+ * {point xyz, light index bits} and {w, W, M bits, 0}), "intermediate",
+ * "auxiliary" (float4 per pixel) or "materials" (kgr_material per pixel). */
+kgr_status kgr_debug_copy(const kgr_attachment *att, const char *what, void *host, uint64_t bytes);
 
 /* The .rtxa plugin export (source/amadeus/naive_path_tracer.cu:280-348),
  * returning a C handle instead of an AttachmentRTX*.  NULL name and ptr on

@@ -182,9 +182,10 @@ def render_params(width, height, cam, **kw):
     return p
 
 
-def render_pt(scene, params):
+def render_pt(scene, params, bufs=None):
     n = params.width * params.height
-    bufs = [np.zeros((n, 4), np.float32) for _ in range(4)]
+    if bufs is None:
+        bufs = [np.zeros((n, 4), np.float32) for _ in range(4)]
     st = RenderStats()
     lib().oracle_render_pt(ctypes.byref(scene.c), ctypes.byref(params), *[ptr(b) for b in bufs],
                            ctypes.byref(st))

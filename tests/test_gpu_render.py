@@ -1,0 +1,131 @@
+"""GPU path tracer and ReSTIR DI parity against the oracle on the same
+per-pixel PCG streams: colour, AOVs and reservoirs.
+
+Tolerance: the spec bar is per-pixel FP32 radiance within 1e-4
+relative and >= 99.9% equal ReSTIR selections; because kernels and oracle
+share the float evaluation order and the transcendental implementations,
+the tests also report (and expect) exact equality for nearly every pixel."""
+import numpy as np
+import pytest
+
+from artemis_gb300 import kgr
+from oracle import pyoracle
+from tests import helpers
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-4
+
+
+def rel_ok(a, b, rtol=RTOL, atol=1e-6):
+    return np.abs(a - b) <= rtol * np.maximum(np.abs(a), np.abs(b)) + atol
+
+
+@pytest.fixture(scope="module")
+def box4k():
+    return helpers.both("box4k", 1)
+
+
+def render_pt_gpu(g, sc, W, H, opts, frames=1, layout="fast", **kw):
+    cam = kgr.camera(g.eye, g.target, g.fov, W / H)
+    bufs = helpers.device_buffers(torch, W * H)
+    att = kgr.Attachment("path_tracer")
+    att.attach(W, H)
+    att.load()
+    for k, v in opts.items():
+        att.set_option(k, v)
+    att.set_option("layout", layout)
+    for f in range(frames):
+        info = helpers.launch(cam, W, H, bufs, frame=f, samples=f * opts.get("spp", 1), accumulate=f > 0, **kw)
+        att.render(info, sc)
+    torch.cuda.synchronize()
+    st = att.stats()
+    att.close()
+    return cam, [b.cpu().numpy() for b in bufs], st
+
+
+@pytest.mark.parametrize("layout", ["fast", "threaded"])
+def test_path_tracer_matches_oracle(box4k, layout):
+    g, sc, osc = box4k
+    W, H = 96, 96
+    opts = {"spp": 2, "russian_roulette": True, "rr_start_depth": 1}
+    cam, out, st = render_pt_gpu(g, sc, W, H, opts, frames=2, layout=layout, max_depth=5)
+    ref = [np.zeros((W * H, 4), np.float32) for _ in range(4)]
+    for f in range(2):
+        p = helpers.oracle_params(cam, W, H, max_depth=5, spp=2, frame=f, samples=2 * f, accumulate=int(f > 0),
+                                  russian_roulette=1, rr_start_depth=1)
+        pyoracle.render_pt(osc, p, ref)
+    color, ocolor = out[0], ref[0]
+    exact = np.all(color.view(np.uint32) == ocolor.view(np.uint32), axis=1).mean()
+    close = np.all(rel_ok(color, ocolor), axis=1).mean()
+    print(f"PT {layout}: exact {exact:.6f}, within 1e-4 {close:.6f}")
+    assert close >= 0.999
+    assert exact >= 0.99
+    for k in (1, 2, 3):
+        assert np.all(rel_ok(out[k], ref[k]), axis=1).mean() >= 0.999
+    assert color[:, :3].mean() > 0.01
+    assert st.camera_rays == W * H * 2 and st.shadow_rays > 0 and st.bounce_rays > 0
+
+
+def test_path_tracer_no_nan_and_converges(box4k):
+    g, sc, _ = box4k
+    W, H = 64, 64
+    _, out, _ = render_pt_gpu(g, sc, W, H, {"spp": 16}, max_depth=3)
+    c = out[0]
+    assert np.isfinite(c).all()
+    magenta = np.all(c[:, :3] == [1, 0, 1], axis=1).mean()
+    assert magenta < 1e-3
+
+
+def restir_gpu(g, sc, W, H, frames, opts, max_depth=2):
+    cam = kgr.camera(g.eye, g.target, g.fov, W / H)
+    bufs = helpers.device_buffers(torch, W * H)
+    att = kgr.Attachment("restir_di")
+    att.attach(W, H)
+    att.load()
+    for k, v in opts.items():
+        att.set_option(k, v)
+    for f in range(frames):
+        info = helpers.launch(cam, W, H, bufs, frame=f, samples=0, accumulate=False, max_depth=max_depth)
+        att.render(info, sc)
+    torch.cuda.synchronize()
+    n = W * H
+    res_a = att.debug_copy("reservoir_prev_a", np.zeros((n, 4), np.float32))
+    res_b = att.debug_copy("reservoir_prev_b", np.zeros((n, 4), np.float32))
+    inter = att.debug_copy("intermediate", np.zeros((n, 4), np.float32))
+    st = att.stats()
+    att.close()
+    return cam, [b.cpu().numpy() for b in bufs], res_a, res_b, inter, st
+
+
+@pytest.mark.parametrize("passes,layout", [(1, "fast"), (2, "threaded")])
+def test_restir_di_matches_oracle(box4k, passes, layout):
+    g, sc, osc = box4k
+    W, H = 96, 96
+    opts = {"candidates": 32, "temporal": True, "temporal_mcap": 20, "spatial_passes": passes,
+            "spatial_neighbors": 5, "spatial_radius": 30, "layout": layout}
+    cam, out, res_a, res_b, inter, st = restir_gpu(g, sc, W, H, 2, opts)
+    n = W * H
+    state = pyoracle.RestirBuffers(n)
+    ref = [np.zeros((n, 4), np.float32) for _ in range(4)]
+    for f in range(2):
+        p = helpers.oracle_params(cam, W, H, max_depth=2, spp=1, frame=f, samples=0, accumulate=0,
+                                  candidates=32, temporal=1, temporal_mcap=20, spatial_passes=passes,
+                                  spatial_neighbors=5, spatial_radius=30)
+        pyoracle.render_restir(osc, p, state, ref)
+    A = state.arrays
+    light_gpu = res_a[:, 3].view(np.int32)
+    M_gpu = res_b[:, 2].view(np.int32)
+    valid = A["prev_M"] > 0
+    same_sel = ((light_gpu == A["prev_light"]) & np.all(res_a[:, :3] == A["prev_point"], axis=1))[valid].mean()
+    print(f"ReSTIR passes={passes}: selected-sample agreement {same_sel:.6f} over {valid.sum()} pixels")
+    assert valid.mean() > 0.95
+    assert same_sel >= 0.999
+    np.testing.assert_array_equal(M_gpu, A["prev_M"])
+    assert np.all(rel_ok(res_b[:, 1], A["prev_W"]))
+    assert np.all(rel_ok(inter, A["intermediate"]), axis=1).mean() >= 0.999
+    close = np.all(rel_ok(out[0], ref[0]), axis=1).mean()
+    print(f"ReSTIR colour within 1e-4: {close:.6f}")
+    assert close >= 0.999
+    assert st.shadow_rays > 0

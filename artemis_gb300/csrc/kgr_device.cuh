@@ -154,7 +154,13 @@ __device__ __forceinline__ bool trace_fast(const DeviceScene &s, const f3 &o, co
 	best.b1 = 0.0f;
 	best.b2 = 0.0f;
 	int32_t best_rank = 0x7fffffff;
-	const float ix = 1.0f / d.x, iy = 1.0f / d.y, iz = 1.0f / d.z;
+	/* A zero direction component would give an infinite reciprocal, and
+	 * lo * inf - o * inf turns into NaN for the far plane; a tiny stand-in
+	 * keeps every slab finite and the interval of a parallel ray unbounded
+	 * (inside the slab) or out of reach (outside it). */
+	const float ix = 1.0f / (fabsf(d.x) > 1e-20f ? d.x : copysignf(1e-20f, d.x));
+	const float iy = 1.0f / (fabsf(d.y) > 1e-20f ? d.y : copysignf(1e-20f, d.y));
+	const float iz = 1.0f / (fabsf(d.z) > 1e-20f ? d.z : copysignf(1e-20f, d.z));
 	const float ox = o.x * ix, oy = o.y * iy, oz = o.z * iz;
 	int32_t stack[KGR_STACK_DEPTH];
 	int sp = 0;

@@ -163,7 +163,9 @@ def bench_reference(args):
     if rank != 0:
         return
     g, sc = make_scene_cpu(args.scene)
-    run, rows, cores = cpu_sample(g, sc, args, args.cpu_seconds)
+    # bound the whole run to about 150 s of CPU work however many steps are asked
+    per_step = min(args.cpu_seconds, 150.0 / max(1, args.steps + args.warmup))
+    run, rows, cores = cpu_sample(g, sc, args, per_step)
     for _ in range(args.warmup):
         run(max(4, rows // 8))
     times, rays_total, rows_done = [], 0, 0

@@ -125,6 +125,7 @@ def lib():
             "kgr_get_render_stats": (c_i32, [vp, vp]),
             "kgr_debug_copy": (c_i32, [vp, ctypes.c_char_p, vp, c_u64]),
             "kgr_get_stage_times": (c_i32, [vp, vp, vp, c_u32]),
+            "kgr_render_pt_noalloc": (c_i32, [vp, vp, c_i32, c_i32, c_i32, vp]),
             "kgr_get_visit_counts": (c_i32, [vp, vp]),
             "kgr_measure_read_bandwidth": (c_i32, [c_i32, c_u64, c_i32, vp]),
             "kgr_load_attachment": (PluginRet, [ctypes.c_char_p]),

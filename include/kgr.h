@@ -291,6 +291,20 @@ kgr_status kgr_render(kgr_attachment *att, const kgr_launch_info *info,
 		const kgr_scene *scene, void *stream);
 kgr_status kgr_destroy(kgr_attachment *att);
 
+/* One path-traced frame that allocates no device memory.  No counterpart in
+ * the reference: it exists for callers that cannot call cudaMalloc when they
+ * render -- a host that fixes its device memory at start-up, or a renderer
+ * running while its stream is captured into a CUDA graph.  The same kernels
+ * as the "path_tracer" attachment (fast layout) write one frame into the
+ * caller's buffers of info->buffers; the per-path scratch is a fixed array of
+ * about 14.8 MiB inside the library, so width * height * spp must be at most
+ * 65536 (KGR_ERR_INVALID_ARGUMENT otherwise).  All calls on a device share
+ * that array: calls that overlap on the GPU race, so order them on one
+ * stream.  The first call on a device looks up the array's address
+ * (cudaGetSymbolAddress); make it before any stream capture. */
+kgr_status kgr_render_pt_noalloc(const kgr_scene *scene, const kgr_launch_info *info,
+		int32_t spp, int32_t russian_roulette, int32_t rr_start_depth, void *stream);
+
 /* Counters of the last render: rays traced by kind and kernel launches. */
 typedef struct kgr_render_stats {
 	uint64_t camera_rays;

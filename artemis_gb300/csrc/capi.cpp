@@ -23,6 +23,7 @@
 #include <variant>
 
 #include "kgr_internal.h"
+#include "kgr_gi.h"
 #include "kgr_wavefront.h"
 
 namespace kgr {
@@ -556,7 +557,11 @@ struct kgr_attachment {
 	DevBuf<kgr_material> pixel_materials;
 	int prev_index = 1;
 	bool have_prev_camera = false;
-	float prev_projection[16], prev_view[16];
+	float prev_projection[16], prev_view[16], prev_center[3];
+
+	/* ReSTIR GI state */
+	DevBuf<float4> gi_a[3], gi_b[3], g_pos, g_nrm, g_ppos, g_pnrm, g_direct, g_dir;
+	int gi_prev = 0;
 
 	kgr_render_stats stats = {0, 0, 0, 0, 0};
 	uint32_t last_paths = 0;
@@ -666,6 +671,12 @@ struct kgr_attachment {
 		intermediate.release();
 		auxiliary.release();
 		pixel_materials.release();
+		for (int k = 0; k < 3; k++) {
+			gi_a[k].release();
+			gi_b[k].release();
+		}
+		for (DevBuf<float4> *b : {&g_pos, &g_nrm, &g_ppos, &g_pnrm, &g_direct, &g_dir})
+			b->release();
 		capacity = 0;
 	}
 
@@ -887,6 +898,102 @@ void render_restir_di(kgr_attachment *att, const kgr_launch_info *info, const kg
 	att->last_paths = fp.paths;
 }
 
+/* One ReSTIR GI frame: primary vertex (G-buffer, DI candidates, GI
+ * direction), the GI path from the secondary vertex, initial reservoirs,
+ * temporal reuse, spatial iterations (ping-pong), final shading. */
+void render_restir_gi(kgr_attachment *att, const kgr_launch_info *info, const kgr_scene *sc, cudaStream_t st)
+{
+	FrameParams fp = frame_params(att, info);
+	fp.spp = 1;
+	fp.paths = fp.npix;
+	fp.jitter = 1;
+	fp.gi_capture = 1;
+	fp.gi_mcap = att->opt_int("gi_mcap", 30);
+	fp.gi_neighbors = att->opt_int("gi_neighbors", 8);
+	fp.gi_radius = att->opt_int("gi_radius", 30);
+	KGR_REQUIRE(fp.gi_neighbors >= 0 && fp.gi_neighbors <= 16, KGR_ERR_INVALID_ARGUMENT, "gi_neighbors must be 0..16");
+	KGR_REQUIRE(fp.candidates >= 1 && fp.candidates <= 1024, KGR_ERR_INVALID_ARGUMENT, "candidates must be 1..1024");
+	KGR_REQUIRE(fp.max_depth >= 1, KGR_ERR_INVALID_ARGUMENT, "ReSTIR GI needs max_depth >= 1");
+	if (!att->have_prev_camera) {
+		memcpy(att->prev_projection, info->camera.projection, 64);
+		memcpy(att->prev_view, info->camera.view, 64);
+		memcpy(att->prev_center, info->camera.center, 12);
+		att->have_prev_camera = true;
+	}
+	mat4_mul(att->prev_projection, att->prev_view, fp.prev_proj_view);
+	memcpy(fp.prev_center, att->prev_center, 12);
+	att->ensure_paths(fp.paths);
+	PathBuffers pb = att->path_buffers();
+	DeviceScene s = scene_for_launch(sc, info);
+	OutputBuffers out = {reinterpret_cast<float4 *>(info->buffers.color),
+		reinterpret_cast<float4 *>(info->buffers.normal), reinterpret_cast<float4 *>(info->buffers.albedo),
+		reinterpret_cast<float4 *>(info->buffers.position)};
+	GiFrameBuffers gb;
+	for (int k = 0; k < 3; k++) {
+		gb.res[k].a = att->gi_a[k].ptr;
+		gb.res[k].b = att->gi_b[k].ptr;
+	}
+	gb.materials = att->pixel_materials.ptr;
+	gb.position = att->g_pos.ptr;
+	gb.normal = att->g_nrm.ptr;
+	gb.prev_position = att->g_ppos.ptr;
+	gb.prev_normal = att->g_pnrm.ptr;
+	gb.direct = att->g_direct.ptr;
+	gb.gi_dir = att->g_dir.ptr;
+	gb.auxiliary = att->auxiliary.ptr;
+	int prev = att->gi_prev, cur = (prev + 1) % 3, tmp = (prev + 2) % 3;
+	uint32_t launches = 0;
+
+	prepare_visits(att, st);
+	att->mark(-1, st);
+	pt_generate(pb, fp, st);
+	att->mark(STAGE_GENERATE, st);
+	pt_trace_closest(s, pb, 0, fp.layout, st);
+	att->mark(STAGE_TRACE_CLOSEST, st);
+	gi_primary(s, pb, fp, gb, st);
+	att->mark(STAGE_RESTIR_PRIMARY, st);
+	launches += 3;
+	for (int d = 1; d <= fp.max_depth; d++) {
+		int q = d & 1;
+		reset_counters(pb, (1 << (q ^ 1)) | (1 << CNT_SHADOW), st);
+		att->mark(-1, st);
+		pt_trace_closest(s, pb, q, fp.layout, st);
+		att->mark(STAGE_TRACE_CLOSEST, st);
+		pt_shade_final_seed(s, pb, fp, d, q, st);
+		att->mark(STAGE_SHADE, st);
+		pt_shadow_resolve(s, pb, fp.layout, st);
+		att->mark(STAGE_SHADOW, st);
+		launches += 3;
+	}
+	gi_initial(pb, fp, gb, cur, st);
+	att->mark(STAGE_RESTIR_FINALIZE, st);
+	launches++;
+	if (att->opt_int("gi_temporal", 1)) {
+		gi_temporal(s, fp, gb, cur, prev, st);
+		att->mark(STAGE_RESTIR_TEMPORAL, st);
+		launches++;
+	}
+	int iters = att->opt_int("gi_spatial_iterations", 3);
+	KGR_REQUIRE(iters >= 0 && iters <= 16, KGR_ERR_INVALID_ARGUMENT, "gi_spatial_iterations must be 0..16");
+	int in = cur, outb = tmp;
+	for (int k = 0; k < iters; k++) {
+		gi_spatial(s, fp, gb, in, outb, st);
+		att->mark(STAGE_RESTIR_SPATIAL, st);
+		std::swap(in, outb);
+		launches++;
+	}
+	gi_final(s, fp, gb, out, in, st);
+	att->mark(STAGE_ACCUMULATE, st);
+	launches++;
+	att->gi_prev = in;
+	memcpy(att->prev_projection, info->camera.projection, 64);
+	memcpy(att->prev_view, info->camera.view, 64);
+	memcpy(att->prev_center, info->camera.center, 12);
+	att->stats.kernel_launches = launches;
+	att->stats.camera_rays = fp.paths;
+	att->last_paths = fp.paths;
+}
+
 } /* namespace */
 
 extern "C" {
@@ -906,7 +1013,8 @@ kgr_status kgr_create(const char *kind, kgr_attachment **out)
 			kd = KIND_RESTIR_DI;
 			name = "ReSTIR";
 		} else if (k == "restir_gi") {
-			throw Error(KGR_ERR_UNSUPPORTED, "restir_gi is not built yet");
+			kd = KIND_RESTIR_GI;
+			name = "ReSTIR GI";
 		} else {
 			throw Error(KGR_ERR_INVALID_ARGUMENT, "unknown attachment kind: " + k);
 		}
@@ -961,6 +1069,23 @@ kgr_status kgr_load(kgr_attachment *att)
 				att->prev_index = 1;
 				att->ensure_paths((uint32_t)npix);
 			}
+			if (att->kind == KIND_RESTIR_GI) {
+				for (int k = 0; k < 3; k++) {
+					att->gi_a[k].alloc(npix);
+					att->gi_b[k].alloc(npix);
+					KGR_CUDA(cudaMemset(att->gi_a[k].ptr, 0, npix * sizeof(float4)));
+					KGR_CUDA(cudaMemset(att->gi_b[k].ptr, 0, npix * sizeof(float4)));
+				}
+				for (DevBuf<float4> *b : {&att->g_pos, &att->g_nrm, &att->g_ppos, &att->g_pnrm, &att->g_direct,
+					     &att->g_dir, &att->auxiliary}) {
+					b->alloc(npix);
+					KGR_CUDA(cudaMemset(b->ptr, 0, npix * sizeof(float4)));
+				}
+				att->pixel_materials.alloc(npix);
+				KGR_CUDA(cudaMemset(att->pixel_materials.ptr, 0, npix * sizeof(kgr_material)));
+				att->gi_prev = 0;
+				att->ensure_paths((uint32_t)npix);
+			}
 			if (!att->ev_start) {
 				KGR_CUDA(cudaEventCreate(&att->ev_start));
 				KGR_CUDA(cudaEventCreate(&att->ev_stop));
@@ -1005,7 +1130,9 @@ static const std::map<std::string, OptionValue> &option_defaults()
 		{"max_depth", -1}, {"russian_roulette", false}, {"rr_start_depth", 3}, {"spp", 1},
 		{"layout", std::string("fast")}, {"candidates", 32}, {"temporal", true}, {"temporal_mcap", 200},
 		{"spatial_passes", 2}, {"spatial_neighbors", 5}, {"spatial_radius", 30},
-		{"profile", false}, {"count_visits", false}};
+		{"profile", false}, {"count_visits", false},
+		{"gi_temporal", true}, {"gi_mcap", 30}, {"gi_spatial_iterations", 3}, {"gi_neighbors", 8},
+		{"gi_radius", 30}};
 	return d;
 }
 
@@ -1075,6 +1202,7 @@ kgr_status kgr_render(kgr_attachment *att, const kgr_launch_info *info, const kg
 		switch (att->kind) {
 		case KIND_PT: render_pt(att, info, sc, st); break;
 		case KIND_RESTIR_DI: render_restir_di(att, info, sc, st); break;
+		case KIND_RESTIR_GI: render_restir_gi(att, info, sc, st); break;
 		default: throw Error(KGR_ERR_UNSUPPORTED, "attachment kind not built");
 		}
 	});
@@ -1170,6 +1298,9 @@ kgr_status kgr_debug_copy(const kgr_attachment *att, const char *what, void *hos
 		else if (w == "intermediate") { src = att->intermediate.ptr; n = att->intermediate.bytes(); }
 		else if (w == "auxiliary") { src = att->auxiliary.ptr; n = att->auxiliary.bytes(); }
 		else if (w == "materials") { src = att->pixel_materials.ptr; n = att->pixel_materials.bytes(); }
+		else if (w == "gi_reservoir_a") { src = att->gi_a[att->gi_prev].ptr; n = att->gi_a[att->gi_prev].bytes(); }
+		else if (w == "gi_reservoir_b") { src = att->gi_b[att->gi_prev].ptr; n = att->gi_b[att->gi_prev].bytes(); }
+		else if (w == "gi_direct") { src = att->g_direct.ptr; n = att->g_direct.bytes(); }
 		else throw Error(KGR_ERR_INVALID_ARGUMENT, "unknown buffer " + w);
 		KGR_REQUIRE(src && bytes <= n, KGR_ERR_INVALID_ARGUMENT, "buffer missing or too small");
 		KGR_CUDA(cudaMemcpy(host, src, bytes, cudaMemcpyDeviceToHost));

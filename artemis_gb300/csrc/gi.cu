@@ -1,0 +1,510 @@
+/*
+ * gi.cu -- ReSTIR GI: reservoir resampling of one-bounce path samples.
+ *
+ * The reference has no working ReSTIR GI (its PathSample reservoirs in
+ * include/optix/parameters.cuh:34-60 are never read by compiled code; a
+ * dormant sketch lies in source/layers/optix_rt.cu:670-856).  This follows
+ * that sketch where it is specific -- target function = the largest
+ * component of the sample radiance, neighbours rejected when their normals
+ * differ by more than 10 degrees or their depth by more than 10% -- and
+ * otherwise the reconnection-shift formulation of ReSTIR GI:
+ *
+ *  sample     x_s, n_s: the secondary vertex; L_o: radiance leaving x_s
+ *             toward the primary vertex x_v (emission + NEE + the rest of
+ *             the path, max depth as configured)
+ *  initial    BSDF-sampled direction at x_v, source pdf p;
+ *             w = p^(L_o) / p, M = 1
+ *  shift      reusing a sample created at receiver x_r for receiver x_q
+ *             multiplies its weight by the Jacobian
+ *             |J| = (|cos phi_q| / |cos phi_r|) (|x_r - x_s|^2 / |x_q - x_s|^2),
+ *             phi the angle at x_s between n_s and the receiver
+ *  temporal   previous frame's reservoir at the reprojected pixel, M capped
+ *  spatial    k neighbours in a disk, shadow ray to each reused sample,
+ *             bias correction over the neighbours that can see the result
+ *  weights    W = w_sum / (Z p^(sample)) evaluated in FP64
+ *  shading    f(x_v, w) L_o |n_v . w| W with a visibility ray, plus the
+ *             primary vertex's emission and its ReSTIR DI direct light
+ *
+ * Reservoirs are 32 bytes in two 16-byte SoA arrays:
+ *   a = {x_s.xyz, bits(n_s octahedral 12+12, M 8)},  b = {L_o.rgb, W}.
+ */
+#include "kgr_device.cuh"
+#include "kgr_gi.h"
+
+namespace kgr {
+
+namespace {
+
+#define KGR_GI_RIS_SALT 0x9E3779B9u
+#define KGR_GI_COS_10DEG 0.984807753f
+
+__device__ __forceinline__ f3 v3(const float *p) { return mk(p[0], p[1], p[2]); }
+
+struct GiSample {
+	f3 xs, ns, Lo;
+	bool valid;
+};
+
+struct GiRes {
+	GiSample s;
+	float W;
+	int32_t M;
+};
+
+__device__ __forceinline__ GiRes load_gi(const GiReservoirs &r, uint32_t i)
+{
+	float4 a = r.a[i], b = r.b[i];
+	uint32_t w = __float_as_uint(a.w);
+	GiRes g;
+	g.s.xs = mk(a.x, a.y, a.z);
+	g.s.ns = unpack_normal(w);
+	g.s.Lo = mk(b.x, b.y, b.z);
+	g.s.valid = true;
+	g.W = b.w;
+	g.M = unpack_m(w);
+	return g;
+}
+
+__device__ __forceinline__ void store_gi(const GiReservoirs &r, uint32_t i, const GiSample &s, float W, int32_t M)
+{
+	r.a[i] = make_float4(s.xs.x, s.xs.y, s.xs.z, __uint_as_float(pack_normal_m(s.ns, M)));
+	r.b[i] = make_float4(s.Lo.x, s.Lo.y, s.Lo.z, W);
+}
+
+/* Weighted reservoir over GI samples (reservoir.cuh:43-56 update rule). */
+struct GiMerge {
+	GiSample sel;
+	float w;
+	f3 seed;
+	__device__ __forceinline__ void init(const f3 &s)
+	{
+		sel.xs = sel.ns = sel.Lo = mk(0.0f);
+		sel.valid = false;
+		w = 0.0f;
+		seed = s;
+	}
+	__device__ __forceinline__ void update(const GiSample &s, float weight)
+	{
+		w += weight;
+		float eta = rand_uniform(seed);
+		if ((eta * w) < weight)
+			sel = s;
+	}
+};
+
+/* W = w_sum / (Z p^) in double precision */
+__device__ __forceinline__ float gi_normalise(float w_sum, int32_t Z, float target)
+{
+	if (!(target > 0.0f) || Z <= 0)
+		return 0.0f;
+	return (float)((double)w_sum / ((double)Z * (double)target));
+}
+
+/* Solid-angle Jacobian of moving a sample's receiver from xr to xq. */
+__device__ __forceinline__ float gi_jacobian(const f3 &xq, const f3 &xr, const GiSample &s)
+{
+	f3 dq = xq - s.xs, dr = xr - s.xs;
+	float lq2 = dot(dq, dq), lr2 = dot(dr, dr);
+	float cq = fabsf(dot(s.ns, dq)) / ksqrt(lq2);
+	float cr = fabsf(dot(s.ns, dr)) / ksqrt(lr2);
+	float j = (cq / cr) * (lr2 / lq2);
+	return (j > 0.0f && j < 1e30f) ? j : 0.0f;
+}
+
+__device__ __forceinline__ bool visible(const DeviceScene &s, int layout, const f3 &from, const f3 &to)
+{
+	f3 D = to - from;
+	float d = length(D);
+	kgr_hit h;
+	return !trace<true>(s, layout, from, D / d, d - KGR_SHADOW_EPS, h);
+}
+
+struct GBuf {
+	f3 x, n;
+	bool hit;
+};
+
+__device__ __forceinline__ GBuf gbuf(const float4 *pos, const float4 *nrm, uint32_t i)
+{
+	float4 p = pos[i], n = nrm[i];
+	GBuf g;
+	g.x = mk(p.x, p.y, p.z);
+	g.n = mk(n.x, n.y, n.z);
+	g.hit = p.w > 0.0f;
+	return g;
+}
+
+/* the reference sketch's geometric test: normals within 10 degrees, view
+ * depth within 10% (optix_rt.cu:745-752) */
+__device__ __forceinline__ bool similar(const GBuf &a, float depth_a, const GBuf &b, float depth_b)
+{
+	if (!a.hit || !b.hit)
+		return false;
+	if (dot(a.n, b.n) < KGR_GI_COS_10DEG)
+		return false;
+	return fabsf(depth_b - depth_a) / depth_a <= 0.1f;
+}
+
+__device__ __forceinline__ SurfaceHit receiver(const FrameParams &fp, const GiFrameBuffers &gb, uint32_t pix,
+		const GBuf &g)
+{
+	SurfaceHit h;
+	h.mat = load_material(gb.materials, pix);
+	h.entering = false;
+	h.n = g.n;
+	h.wo = normalize(v3(fp.center) - g.x);
+	h.x = g.x;
+	return h;
+}
+
+/* Primary vertex: G-buffer, ReSTIR DI candidates for direct light, and the
+ * BSDF-sampled direction of the GI sample, after which the path continues
+ * with throughput 1 so that it accumulates L_o at the secondary vertex. */
+__global__ void __launch_bounds__(128) gi_primary_kernel(DeviceScene s, PathBuffers pb, FrameParams fp,
+		GiFrameBuffers gb)
+{
+	const uint32_t n = pb.counters[CNT_Q0];
+	uint32_t *out_counter = pb.counters + CNT_Q1;
+	uint32_t stride = gridDim.x * blockDim.x;
+	uint32_t iters = (n + stride - 1) / stride;
+	for (uint32_t it = 0; it < iters; it++) {
+		uint32_t i = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
+		bool active = i < n;
+		uint32_t p = active ? pb.queue[0][i] : 0;
+		bool cont = false;
+		if (active) {
+			float4 hv = pb.hit[p];
+			kgr_hit h;
+			h.prim = __float_as_int(hv.x);
+			h.t = hv.y;
+			h.b1 = hv.z;
+			h.b2 = hv.w;
+			float4 dv = pb.ray_d[p];
+			SurfaceHit sh;
+			gb.position[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+			gb.gi_dir[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+			gb.direct[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+			if (h.prim >= 0 && surface(s, h, mk(dv.x, dv.y, dv.z), sh)) {
+				f3 n3 = sh.n;
+				float sgn = sh.mat.type == KGR_SHADING_TRANSMISSION ? -1.0f : 1.0f;
+				sh.x = sh.x + sgn * n3 * KGR_OFFSET_EPS;
+				gb.position[p] = f4_of(sh.x, 1.0f);
+				gb.normal[p] = f4_of(n3, 0.0f);
+				uint4 tr = __ldg(&s.tris[h.prim]);
+				const float4 *src = reinterpret_cast<const float4 *>(s.materials + tr.w);
+				float4 *dst = reinterpret_cast<float4 *>(gb.materials + p);
+				for (int k = 0; k < 4; k++)
+					dst[k] = __ldg(src + k);
+				float4 sv = pb.seed[p];
+				f3 seed = mk(sv.x, sv.y, sv.z);
+				/* ReSTIR DI candidates (amadeus_restir.cu:478-523), shaded directly */
+				f3 risseed = pixel_seed(p, fp.frame, KGR_GI_RIS_SALT);
+				float wsum = 0.0f;
+				int32_t M = 0, sel = -1;
+				f3 selp = mk(0.0f);
+				unsigned int total = s.light_count;
+				for (int c = 0; c < fp.candidates; c++) {
+					unsigned int li = (unsigned int)(rand_uniform(seed) * total);
+					float weight = 0.0f;
+					f3 pt = mk(0.0f);
+					if (li < total) {
+						TriLight l = load_light(s.lights, li);
+						pt = sample_area_light(l, seed);
+						float pdf = 1.0f / (l.area() * total);
+						f3 D = pt - sh.x;
+						float d = length(D);
+						f3 Li = direct_unoccluded(sh, l.intensity, l.normal(), D / d, d);
+						float tgt = Li.x + Li.y + Li.z;
+						weight = (pdf > 0) ? tgt / pdf : 0;
+					}
+					wsum += weight;
+					float eta = rand_uniform(risseed);
+					if ((eta * wsum) < weight) {
+						sel = (int32_t)li;
+						selp = pt;
+					}
+					M++;
+				}
+				f3 direct = mk(0.0f);
+				if (sel >= 0) {
+					TriLight l = load_light(s.lights, (uint32_t)sel);
+					f3 D = selp - sh.x;
+					float d = length(D);
+					f3 Dn = D / d;
+					kgr_hit hh;
+					if (!trace<true>(s, fp.layout, sh.x, Dn, d - KGR_SHADOW_EPS, hh)) {
+						f3 Li = direct_unoccluded(sh, l.intensity, l.normal(), Dn, d);
+						float tgt = Li.x + Li.y + Li.z;
+						float dd = tgt * M;
+						float W = (dd > 0) ? wsum / dd : 0.0f;
+						direct = Li * W;
+					}
+				}
+				gb.direct[p] = f4_of(direct, 0.0f);
+				/* GI direction (eval, brdf.cuh:573-589) */
+				f3 wi;
+				float pdf = 0.0f;
+				eval(sh, wi, pdf, seed);
+				if (pdf > 0 && 0 < fp.max_depth) {
+					gb.gi_dir[p] = f4_of(wi, pdf);
+					pb.ray_o[p] = f4_of(sh.x, 0.0f);
+					pb.ray_d[p] = f4_of(wi, 1e16f);
+					pb.beta[p] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+					pb.aov_p[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+					cont = true;
+				}
+				pb.seed[p] = f4_of(seed, 0.0f);
+			}
+		}
+		queue_append(pb.queue[1], out_counter, p, cont, pb.counters + CNT_BOUNCE_TOTAL);
+	}
+}
+
+/* Initial reservoir from the finished path: one candidate, W in FP64. */
+__global__ void gi_initial_kernel(PathBuffers pb, FrameParams fp, GiFrameBuffers gb, int cur)
+{
+	uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+	if (pix >= fp.npix)
+		return;
+	float4 dir = gb.gi_dir[pix];
+	float4 xs = pb.aov_p[pix];
+	float4 ns = pb.aov_n[pix];
+	float4 L = pb.L[pix];
+	GiSample smp;
+	smp.xs = mk(xs.x, xs.y, xs.z);
+	smp.ns = mk(ns.x, ns.y, ns.z);
+	smp.Lo = mk(L.x, L.y, L.z);
+	bool valid = dir.w > 0.0f && xs.w > 0.0f && !anynan(smp.Lo);
+	float W = 0.0f;
+	if (valid) {
+		float target = max3(smp.Lo);
+		float w = target / dir.w;
+		W = gi_normalise(w, 1, target);
+	} else {
+		smp.xs = smp.Lo = mk(0.0f);
+		smp.ns = mk(0.0f, 0.0f, 1.0f);
+	}
+	store_gi(gb.res[cur], pix, smp, W, 1);
+	float4 sv = pb.seed[pix];
+	gb.auxiliary[pix] = make_float4(sv.x, sv.y, sv.z, 1.0f);
+}
+
+__device__ __forceinline__ int reproject_gi(const FrameParams &fp, const f3 &x)
+{
+	const float *m = fp.prev_proj_view;
+	float q[4];
+	for (int i = 0; i < 4; i++)
+		q[i] = m[0 * 4 + i] * x.x + m[1 * 4 + i] * x.y + m[2 * 4 + i] * x.z + m[3 * 4 + i] * 1.0f;
+	float u = q[0] / q[3];
+	float v = q[1] / q[3];
+	if (!(u >= -1.0f && u <= 1.0f && v >= -1.0f && v <= 1.0f))
+		return -1;
+	u = (u + 1.0f) * 0.5f;
+	v = (v + 1.0f) * 0.5f;
+	int ix = (int)((double)(u * (float)fp.width) + 0.5);
+	int iy = (int)((double)(v * (float)fp.height) + 0.5);
+	if (ix < 0 || iy < 0 || ix >= (int)fp.width || iy >= (int)fp.height)
+		return -1;
+	return iy * (int)fp.width + ix;
+}
+
+__global__ void __launch_bounds__(128) gi_temporal_kernel(DeviceScene s, FrameParams fp, GiFrameBuffers gb,
+		int cur, int prev)
+{
+	uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+	if (pix >= fp.npix)
+		return;
+	GBuf g = gbuf(gb.position, gb.normal, pix);
+	if (!g.hit)
+		return;
+	int pindex = reproject_gi(fp, g.x);
+	if (pindex < 0)
+		return;
+	GBuf gp = gbuf(gb.prev_position, gb.prev_normal, (uint32_t)pindex);
+	float depth = length(g.x - v3(fp.center));
+	float pdepth = length(gp.x - v3(fp.prev_center));
+	if (!similar(g, depth, gp, pdepth))
+		return;
+	GiRes P = load_gi(gb.res[prev], (uint32_t)pindex);
+	if (P.M <= 0)
+		return;
+	GiRes C = load_gi(gb.res[cur], pix);
+	int32_t pM = P.M < fp.gi_mcap ? P.M : fp.gi_mcap;
+	float4 av = gb.auxiliary[pix];
+	GiMerge r;
+	r.init(mk(av.x, av.y, av.z));
+	r.update(C.s, max3(C.s.Lo) * C.W * C.M);
+	float J = gi_jacobian(g.x, gp.x, P.s);
+	float wp = max3(P.s.Lo) * J * P.W * pM;
+	r.update(P.s, wp);
+	int32_t M = C.M + (wp > 0.0f ? pM : 0);
+	float W = gi_normalise(r.w, M, max3(r.sel.Lo));
+	store_gi(gb.res[cur], pix, r.sel, W, M);
+}
+
+/* sample_spatial_neighborhood (amadeus_restir.cu:294-314) */
+__device__ __forceinline__ int gi_neighbor(const FrameParams &fp, int index, f3 &seed)
+{
+	int width = (int)fp.width, height = (int)fp.height;
+	int x = index % width;
+	int y = index / width;
+	f3 offset = rand_uniform_3f(seed);
+	float theta = (float)(2.0 * 3.14159265358979323846 * (double)offset.x);
+	float r = (float)fp.gi_radius * ksqrt(offset.y);
+	float st, ct;
+	ksincos(theta, st, ct);
+	int x0 = (int)((float)x + r * ct);
+	int y0 = (int)((float)y + r * st);
+	x0 = x0 < 0 ? 0 : (x0 > width - 1 ? width - 1 : x0);
+	y0 = y0 < 0 ? 0 : (y0 > height - 1 ? height - 1 : y0);
+	return x0 + y0 * width;
+}
+
+#define KGR_GI_MAX_NEIGHBORS 16
+
+__global__ void __launch_bounds__(128) gi_spatial_kernel(DeviceScene s, FrameParams fp, GiFrameBuffers gb,
+		int in, int out)
+{
+	uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+	if (pix >= fp.npix)
+		return;
+	GiRes C = load_gi(gb.res[in], pix);
+	GBuf g = gbuf(gb.position, gb.normal, pix);
+	if (!g.hit) {
+		store_gi(gb.res[out], pix, C.s, C.W, C.M);
+		return;
+	}
+	float depth = length(g.x - v3(fp.center));
+	float4 av = gb.auxiliary[pix];
+	GiMerge r;
+	r.init(mk(av.x, av.y, av.z));
+	r.update(C.s, max3(C.s.Lo) * C.W * C.M);
+	int32_t nidx[KGR_GI_MAX_NEIGHBORS];
+	int32_t nM[KGR_GI_MAX_NEIGHBORS];
+	int32_t Msum = C.M;
+	for (int k = 0; k < fp.gi_neighbors; k++) {
+		int index0 = gi_neighbor(fp, (int)pix, r.seed);
+		nidx[k] = -1;
+		nM[k] = 0;
+		GBuf gn = gbuf(gb.position, gb.normal, (uint32_t)index0);
+		if (!similar(g, depth, gn, length(gn.x - v3(fp.center))))
+			continue;
+		GiRes N = load_gi(gb.res[in], (uint32_t)index0);
+		if (N.M <= 0)
+			continue;
+		nidx[k] = index0;
+		nM[k] = N.M;
+		Msum += N.M;
+		float J = gi_jacobian(g.x, gn.x, N.s);
+		float wn = max3(N.s.Lo) * J * N.W * N.M;
+		if (wn > 0.0f && !visible(s, fp.layout, g.x, N.s.xs))
+			wn = 0.0f;
+		r.update(N.s, wn);
+	}
+	/* bias correction: the centre and every neighbour whose receiver sees
+	 * the selected sample through a valid shift */
+	int32_t Z = C.M;
+	float target = max3(r.sel.Lo);
+	if (target > 0.0f) {
+		for (int k = 0; k < fp.gi_neighbors; k++) {
+			if (nidx[k] < 0)
+				continue;
+			GBuf gn = gbuf(gb.position, gb.normal, (uint32_t)nidx[k]);
+			if (gi_jacobian(gn.x, g.x, r.sel) > 0.0f && visible(s, fp.layout, gn.x, r.sel.xs))
+				Z += nM[k];
+		}
+	}
+	float W = gi_normalise(r.w, Z, target);
+	store_gi(gb.res[out], pix, r.sel, W, Msum);
+}
+
+__device__ __forceinline__ void accumulate4(float4 *buf, uint32_t i, float4 v, bool acc, float count)
+{
+	if (acc) {
+		float4 d = buf[i];
+		d.x = (d.x * count + v.x) / (count + 1);
+		d.y = (d.y * count + v.y) / (count + 1);
+		d.z = (d.z * count + v.z) / (count + 1);
+		d.w = (d.w * count + v.w) / (count + 1);
+		buf[i] = d;
+	} else {
+		buf[i] = v;
+	}
+}
+
+/* Final shading: emission + direct + f L_o |n.w| W through a visibility ray;
+ * the G-buffer becomes the history of the next frame. */
+__global__ void __launch_bounds__(128) gi_final_kernel(DeviceScene s, FrameParams fp, GiFrameBuffers gb,
+		OutputBuffers out, int fin)
+{
+	uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+	if (pix >= fp.npix)
+		return;
+	GBuf g = gbuf(gb.position, gb.normal, pix);
+	f3 c = mk(0.0f);
+	if (g.hit) {
+		SurfaceHit h = receiver(fp, gb, pix, g);
+		float4 dv = gb.direct[pix];
+		f3 gi = mk(0.0f);
+		GiRes R = load_gi(gb.res[fin], pix);
+		if (R.W > 0.0f) {
+			f3 D = R.s.xs - g.x;
+			float d = length(D);
+			f3 w = D / d;
+			kgr_hit hh;
+			if (!trace<true>(s, fp.layout, g.x, w, d - KGR_SHADOW_EPS, hh))
+				gi = brdf(h, w) * R.s.Lo * (fabsf(dot(h.n, w)) * R.W);
+		}
+		c = h.mat.emission + mk(dv.x, dv.y, dv.z) + gi;
+	}
+	if (anynan(c))
+		c = mk(1.0f, 0.0f, 1.0f);
+	accumulate4(out.color, pix, f4_of(c, 1.0f), fp.accumulate != 0, (float)fp.samples);
+	float4 pv = gb.position[pix];
+	if (out.position)
+		out.position[pix] = make_float4(pv.x, pv.y, pv.z, 0.0f);
+	if (out.normal)
+		out.normal[pix] = gb.normal[pix];
+	gb.prev_position[pix] = pv;
+	gb.prev_normal[pix] = gb.normal[pix];
+}
+
+} /* namespace */
+
+void gi_primary(const DeviceScene &s, const PathBuffers &pb, const FrameParams &fp, const GiFrameBuffers &gb,
+		cudaStream_t st)
+{
+	int grid = (int)((pb.capacity + 127) / 128);
+	int cap = device_sm_count() * 16;
+	gi_primary_kernel<<<grid < cap ? grid : cap, 128, 0, st>>>(s, pb, fp, gb);
+	KGR_CUDA(cudaGetLastError());
+}
+
+void gi_initial(const PathBuffers &pb, const FrameParams &fp, const GiFrameBuffers &gb, int cur, cudaStream_t st)
+{
+	gi_initial_kernel<<<(fp.npix + 255) / 256, 256, 0, st>>>(pb, fp, gb, cur);
+	KGR_CUDA(cudaGetLastError());
+}
+
+void gi_temporal(const DeviceScene &s, const FrameParams &fp, const GiFrameBuffers &gb, int cur, int prev,
+		cudaStream_t st)
+{
+	gi_temporal_kernel<<<(fp.npix + 127) / 128, 128, 0, st>>>(s, fp, gb, cur, prev);
+	KGR_CUDA(cudaGetLastError());
+}
+
+void gi_spatial(const DeviceScene &s, const FrameParams &fp, const GiFrameBuffers &gb, int in, int out,
+		cudaStream_t st)
+{
+	gi_spatial_kernel<<<(fp.npix + 127) / 128, 128, 0, st>>>(s, fp, gb, in, out);
+	KGR_CUDA(cudaGetLastError());
+}
+
+void gi_final(const DeviceScene &s, const FrameParams &fp, const GiFrameBuffers &gb, const OutputBuffers &out,
+		int fin, cudaStream_t st)
+{
+	gi_final_kernel<<<(fp.npix + 127) / 128, 128, 0, st>>>(s, fp, gb, out, fin);
+	KGR_CUDA(cudaGetLastError());
+}
+
+} /* namespace kgr */

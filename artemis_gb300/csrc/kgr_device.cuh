@@ -40,8 +40,22 @@ __device__ __forceinline__ float mt_test(const f3 &v1, const f3 &e1, const f3 &e
 	if (divisor == 0.0f)
 		return -1.0f;
 	f3 s = origin - v1;
+	float d1 = dot(s, s1);
+	/* Early reject without the division, only where b1 = d1 * (1/divisor)
+	 * must fail the reference's test: for a finite divisor, opposite signs
+	 * and |d1| >= 2^-60 |divisor| make b1 a normal negative number, and equal
+	 * signs with |d1| > (1 + 2^-10) |divisor| make it greater than 1 after
+	 * both roundings. */
+	{
+		float ad = fabsf(divisor), a1 = fabsf(d1);
+		if (ad < INFINITY) {
+			bool opposite = (d1 < 0.0f) != (divisor < 0.0f);
+			if (opposite ? (d1 != 0.0f && a1 >= ad * 8.67361738e-19f) : (a1 > ad * 1.0009765625f))
+				return -1.0f;
+		}
+	}
 	float inv_divisor = 1.0f / divisor;
-	b1 = dot(s, s1) * inv_divisor;
+	b1 = d1 * inv_divisor;
 	if (b1 < 0.0f || b1 > 1.0f)
 		return -1.0f;
 	f3 s2 = cross(s, e1);
@@ -140,11 +154,105 @@ __device__ __forceinline__ bool trace_threaded(const DeviceScene &s, const f3 &o
 
 /* -------------------------------------------------------- fast layout -- */
 
+/* A ray prepared for the slab tests of the fast layout.  A zero direction
+ * component would give an infinite reciprocal, and lo * inf - o * inf turns
+ * into NaN for the far plane; a tiny stand-in keeps every slab finite and the
+ * interval of a parallel ray unbounded (inside the slab) or out of reach
+ * (outside it). */
+struct FastRay {
+	f3 o, d;
+	float ix, iy, iz, ox, oy, oz;
+};
+
+__device__ __forceinline__ FastRay fast_ray(const f3 &o, const f3 &d)
+{
+	FastRay r;
+	r.o = o;
+	r.d = d;
+	r.ix = 1.0f / (fabsf(d.x) > 1e-20f ? d.x : copysignf(1e-20f, d.x));
+	r.iy = 1.0f / (fabsf(d.y) > 1e-20f ? d.y : copysignf(1e-20f, d.y));
+	r.iz = 1.0f / (fabsf(d.z) > 1e-20f ? d.z : copysignf(1e-20f, d.z));
+	r.ox = o.x * r.ix;
+	r.oy = o.y * r.iy;
+	r.oz = o.z * r.iz;
+	return r;
+}
+
+/* One child-pair node: which children the ray reaches within [0, best_t],
+ * nearer one first.  Returns the number of children hit (0, 1 or 2). */
+__device__ __forceinline__ int fast_node(const DeviceScene &s, const FastRay &r, int32_t ref, float best_t,
+		int32_t &first, int32_t &second)
+{
+	const float4 *np = reinterpret_cast<const float4 *>(s.fast_nodes + ref);
+	float4 lxy = __ldg(np + 0);
+	float4 rxy = __ldg(np + 1);
+	float4 lrz = __ldg(np + 2);
+	int4 refs = __ldg(reinterpret_cast<const int4 *>(np + 3));
+	float l0x = __fmaf_rn(lxy.x, r.ix, -r.ox), l1x = __fmaf_rn(lxy.y, r.ix, -r.ox);
+	float l0y = __fmaf_rn(lxy.z, r.iy, -r.oy), l1y = __fmaf_rn(lxy.w, r.iy, -r.oy);
+	float l0z = __fmaf_rn(lrz.x, r.iz, -r.oz), l1z = __fmaf_rn(lrz.y, r.iz, -r.oz);
+	float r0x = __fmaf_rn(rxy.x, r.ix, -r.ox), r1x = __fmaf_rn(rxy.y, r.ix, -r.ox);
+	float r0y = __fmaf_rn(rxy.z, r.iy, -r.oy), r1y = __fmaf_rn(rxy.w, r.iy, -r.oy);
+	float r0z = __fmaf_rn(lrz.z, r.iz, -r.oz), r1z = __fmaf_rn(lrz.w, r.iz, -r.oz);
+	float ln = fmaxf(fmaxf(fminf(l0x, l1x), fminf(l0y, l1y)), fmaxf(fminf(l0z, l1z), 0.0f));
+	float lf = fminf(fminf(fmaxf(l0x, l1x), fmaxf(l0y, l1y)), fmaxf(l0z, l1z));
+	float rn = fmaxf(fmaxf(fminf(r0x, r1x), fminf(r0y, r1y)), fmaxf(fminf(r0z, r1z), 0.0f));
+	float rf = fminf(fminf(fmaxf(r0x, r1x), fmaxf(r0y, r1y)), fmaxf(r0z, r1z));
+	bool hl = ln <= lf && ln <= best_t;
+	bool hr = rn <= rf && rn <= best_t;
+	if (hl && hr) {
+		bool swap = rn < ln;
+		first = swap ? refs.y : refs.x;
+		second = swap ? refs.x : refs.y;
+		return 2;
+	}
+	first = hl ? refs.x : refs.y;
+	return (hl || hr) ? 1 : 0;
+}
+
+/* The triangles of one leaf.  Closest hit: a triangle replaces the best when
+ * 0 < t < best, or t == best and its rank (position in the threaded walk)
+ * is lower -- the primitive the reference's strict `t < best` walk keeps.
+ * Any hit: returns true at the first triangle with 0 < t < tmax. */
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ bool fast_leaf(const DeviceScene &s, const FastRay &r, int32_t ref, kgr_hit &best,
+		int32_t &best_rank, TraceCounters *cnt)
+{
+	uint32_t code = ~(uint32_t)ref;
+	uint32_t start = code >> 3, n = (code & 7u) + 1u;
+	const float4 *tp = s.fast_tris + 3 * (size_t)start;
+	for (uint32_t k = 0; k < n; k++) {
+		if (COUNT)
+			cnt->tris++;
+		float4 a = __ldg(tp + 3 * k + 0);
+		float4 e1 = __ldg(tp + 3 * k + 1);
+		float4 e2 = __ldg(tp + 3 * k + 2);
+		float b1 = 0.0f, b2 = 0.0f;
+		float tt = mt_test(f3_of(a), f3_of(e1), f3_of(e2), r.o, r.d, b1, b2);
+		if (ANY) {
+			if (tt > 0.0f && tt < best.t) {
+				best.prim = ibits(a.w);
+				best.t = tt;
+				return true;
+			}
+			continue;
+		}
+		int32_t rank = (int32_t)(start + k);
+		if (tt > 0.0f && (tt < best.t || (tt == best.t && rank < best_rank))) {
+			best.prim = ibits(a.w);
+			best.t = tt;
+			best.b1 = b1;
+			best.b2 = b2;
+			best_rank = rank;
+		}
+	}
+	return false;
+}
+
 /* Ordered descent over 64-byte child-pair nodes with a per-thread stack.
- * Closest hit: a triangle replaces the best when 0 < t < best, or t == best
- * and its rank (position in the threaded walk) is lower -- the primitive the
- * reference's strict `t < best` walk would keep.  Box culling keeps every
- * child whose padded slab interval reaches [0, best]. */
+ * Box culling keeps every child whose padded slab interval reaches
+ * [0, best]; the build pads boxes so that no triangle the exact test accepts
+ * is culled. */
 template <bool ANY, bool COUNT>
 __device__ __forceinline__ bool trace_fast(const DeviceScene &s, const f3 &o, const f3 &d,
 		float tmax, kgr_hit &best, TraceCounters *cnt = nullptr)
@@ -154,14 +262,7 @@ __device__ __forceinline__ bool trace_fast(const DeviceScene &s, const f3 &o, co
 	best.b1 = 0.0f;
 	best.b2 = 0.0f;
 	int32_t best_rank = 0x7fffffff;
-	/* A zero direction component would give an infinite reciprocal, and
-	 * lo * inf - o * inf turns into NaN for the far plane; a tiny stand-in
-	 * keeps every slab finite and the interval of a parallel ray unbounded
-	 * (inside the slab) or out of reach (outside it). */
-	const float ix = 1.0f / (fabsf(d.x) > 1e-20f ? d.x : copysignf(1e-20f, d.x));
-	const float iy = 1.0f / (fabsf(d.y) > 1e-20f ? d.y : copysignf(1e-20f, d.y));
-	const float iz = 1.0f / (fabsf(d.z) > 1e-20f ? d.z : copysignf(1e-20f, d.z));
-	const float ox = o.x * ix, oy = o.y * iy, oz = o.z * iz;
+	FastRay r = fast_ray(o, d);
 	int32_t stack[KGR_STACK_DEPTH];
 	int sp = 0;
 	int32_t ref = 0;
@@ -169,70 +270,21 @@ __device__ __forceinline__ bool trace_fast(const DeviceScene &s, const f3 &o, co
 		while (ref >= 0) {
 			if (COUNT)
 				cnt->nodes++;
-			const float4 *np = reinterpret_cast<const float4 *>(s.fast_nodes + ref);
-			float4 lxy = __ldg(np + 0);
-			float4 rxy = __ldg(np + 1);
-			float4 lrz = __ldg(np + 2);
-			int4 refs = __ldg(reinterpret_cast<const int4 *>(np + 3));
-			float l0x = __fmaf_rn(lxy.x, ix, -ox), l1x = __fmaf_rn(lxy.y, ix, -ox);
-			float l0y = __fmaf_rn(lxy.z, iy, -oy), l1y = __fmaf_rn(lxy.w, iy, -oy);
-			float l0z = __fmaf_rn(lrz.x, iz, -oz), l1z = __fmaf_rn(lrz.y, iz, -oz);
-			float r0x = __fmaf_rn(rxy.x, ix, -ox), r1x = __fmaf_rn(rxy.y, ix, -ox);
-			float r0y = __fmaf_rn(rxy.z, iy, -oy), r1y = __fmaf_rn(rxy.w, iy, -oy);
-			float r0z = __fmaf_rn(lrz.z, iz, -oz), r1z = __fmaf_rn(lrz.w, iz, -oz);
-			float ln = fmaxf(fmaxf(fminf(l0x, l1x), fminf(l0y, l1y)), fmaxf(fminf(l0z, l1z), 0.0f));
-			float lf = fminf(fminf(fmaxf(l0x, l1x), fmaxf(l0y, l1y)), fmaxf(l0z, l1z));
-			float rn = fmaxf(fmaxf(fminf(r0x, r1x), fminf(r0y, r1y)), fmaxf(fminf(r0z, r1z), 0.0f));
-			float rf = fminf(fminf(fmaxf(r0x, r1x), fmaxf(r0y, r1y)), fmaxf(r0z, r1z));
-			bool hl = ln <= lf && ln <= best.t;
-			bool hr = rn <= rf && rn <= best.t;
-			if (hl && hr) {
-				int32_t near_ref = refs.x, far_ref = refs.y;
-				if (rn < ln) {
-					near_ref = refs.y;
-					far_ref = refs.x;
-				}
-				stack[sp++] = far_ref;
-				ref = near_ref;
-			} else if (hl) {
-				ref = refs.x;
-			} else if (hr) {
-				ref = refs.y;
+			int32_t first, second;
+			int hits = fast_node(s, r, ref, best.t, first, second);
+			if (hits == 2) {
+				stack[sp++] = second;
+				ref = first;
+			} else if (hits == 1) {
+				ref = first;
 			} else {
 				if (sp == 0)
 					return best.prim >= 0;
 				ref = stack[--sp];
 			}
 		}
-		/* leaf */
-		uint32_t code = ~(uint32_t)ref;
-		uint32_t start = code >> 3, n = (code & 7u) + 1u;
-		const float4 *tp = s.fast_tris + 3 * (size_t)start;
-		for (uint32_t k = 0; k < n; k++) {
-			if (COUNT)
-				cnt->tris++;
-			float4 a = __ldg(tp + 3 * k + 0);
-			float4 e1 = __ldg(tp + 3 * k + 1);
-			float4 e2 = __ldg(tp + 3 * k + 2);
-			float b1 = 0.0f, b2 = 0.0f;
-			float tt = mt_test(f3_of(a), f3_of(e1), f3_of(e2), o, d, b1, b2);
-			if (ANY) {
-				if (tt > 0.0f && tt < best.t) {
-					best.prim = ibits(a.w);
-					best.t = tt;
-					return true;
-				}
-				continue;
-			}
-			int32_t rank = (int32_t)(start + k);
-			if (tt > 0.0f && (tt < best.t || (tt == best.t && rank < best_rank))) {
-				best.prim = ibits(a.w);
-				best.t = tt;
-				best.b1 = b1;
-				best.b2 = b2;
-				best_rank = rank;
-			}
-		}
+		if (fast_leaf<ANY, COUNT>(s, r, ref, best, best_rank, cnt))
+			return true;
 		if (sp == 0)
 			return best.prim >= 0;
 		ref = stack[--sp];

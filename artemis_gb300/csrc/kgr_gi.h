@@ -1,0 +1,43 @@
+/*
+ * kgr_gi.h -- per-pixel state and launchers of ReSTIR GI (gi.cu).
+ */
+#ifndef KGR_GI_H_
+#define KGR_GI_H_
+
+#include "kgr_wavefront.h"
+
+namespace kgr {
+
+/* 32-byte GI reservoirs in two SoA arrays:
+ *   a[i] = {x_s.xyz, bits(n_s octahedral 12+12 | M 8)}
+ *   b[i] = {L_o.rgb, W} */
+struct GiReservoirs {
+	float4 *a;
+	float4 *b;
+};
+
+struct GiFrameBuffers {
+	GiReservoirs res[3];    /* previous frame, current, spatial ping-pong */
+	kgr_material *materials; /* per pixel */
+	float4 *position;       /* primary vertex, w = 1 when there is one */
+	float4 *normal;
+	float4 *prev_position;  /* last frame's primary vertices (temporal reuse) */
+	float4 *prev_normal;
+	float4 *direct;         /* ReSTIR DI direct light of the primary vertex */
+	float4 *gi_dir;         /* GI direction xyz, source pdf */
+	float4 *auxiliary;      /* final path seed (reuse RNG) */
+};
+
+void gi_primary(const DeviceScene &s, const PathBuffers &pb, const FrameParams &fp, const GiFrameBuffers &gb,
+		cudaStream_t st);
+void gi_initial(const PathBuffers &pb, const FrameParams &fp, const GiFrameBuffers &gb, int cur, cudaStream_t st);
+void gi_temporal(const DeviceScene &s, const FrameParams &fp, const GiFrameBuffers &gb, int cur, int prev,
+		cudaStream_t st);
+void gi_spatial(const DeviceScene &s, const FrameParams &fp, const GiFrameBuffers &gb, int in, int out,
+		cudaStream_t st);
+void gi_final(const DeviceScene &s, const FrameParams &fp, const GiFrameBuffers &gb, const OutputBuffers &out,
+		int fin, cudaStream_t st);
+
+} /* namespace kgr */
+
+#endif

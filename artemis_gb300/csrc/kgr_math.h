@@ -289,6 +289,47 @@ KGR_HD f3 pixel_seed(uint32_t pixel, uint32_t stream, uint32_t salt)
 	return mk(u2f(pixel ^ stream), u2f(pixel ^ salt), u2f(stream));
 }
 
+/* ------------------------------------------------- GI reservoir packing -- */
+
+/* A unit normal in octahedral form, 12 bits per coordinate, and a sample
+ * count M clamped to 255, in one 32-bit word: bits 0-11 u, 12-23 v, 24-31 M.
+ * Only exact operations, so both sides pack and unpack identically. */
+KGR_HD uint32_t pack_normal_m(const f3 &n, int32_t m)
+{
+	float s = kabs(n.x) + kabs(n.y) + kabs(n.z);
+	float px = n.x / s, py = n.y / s;
+	if (n.z < 0.0f) {
+		float qx = (1.0f - kabs(py)) * (px >= 0.0f ? 1.0f : -1.0f);
+		float qy = (1.0f - kabs(px)) * (py >= 0.0f ? 1.0f : -1.0f);
+		px = qx;
+		py = qy;
+	}
+	px = clampf(px, -1.0f, 1.0f);
+	py = clampf(py, -1.0f, 1.0f);
+	uint32_t u = (uint32_t)(int32_t)kfloor(px * 2047.0f + 2047.5f);
+	uint32_t v = (uint32_t)(int32_t)kfloor(py * 2047.0f + 2047.5f);
+	uint32_t mm = (uint32_t)(m < 0 ? 0 : (m > 255 ? 255 : m));
+	return (u & 0xfffu) | ((v & 0xfffu) << 12) | (mm << 24);
+}
+
+KGR_HD f3 unpack_normal(uint32_t w)
+{
+	float px = ((float)(int32_t)(w & 0xfffu) - 2047.0f) / 2047.0f;
+	float py = ((float)(int32_t)((w >> 12) & 0xfffu) - 2047.0f) / 2047.0f;
+	float pz = 1.0f - kabs(px) - kabs(py);
+	if (pz < 0.0f) {
+		float qx = (1.0f - kabs(py)) * (px >= 0.0f ? 1.0f : -1.0f);
+		float qy = (1.0f - kabs(px)) * (py >= 0.0f ? 1.0f : -1.0f);
+		px = qx;
+		py = qy;
+	}
+	return normalize(mk(px, py, pz));
+}
+
+KGR_HD int32_t unpack_m(uint32_t w) { return (int32_t)(w >> 24); }
+
+KGR_HD float max3(const f3 &v) { return kmax(v.x, kmax(v.y, v.z)); }
+
 /* rotate (math.cuh:2653-2668): express s in a frame around n. */
 KGR_HD f3 rotate(const f3 &s, const f3 &n)
 {

@@ -20,6 +20,8 @@ enum Counter {
 	CNT_SHADOW = 2,    /* shadow rays of this bounce */
 	CNT_BOUNCE_TOTAL = 3,
 	CNT_SHADOW_TOTAL = 4,
+	CNT_FETCH_CLOSEST = 5, /* next queue entry of the persistent closest-hit kernel */
+	CNT_FETCH_SHADOW = 6,  /* next queue entry of the persistent shadow kernel */
 	CNT_COUNT = 8
 };
 
@@ -74,6 +76,10 @@ struct FrameParams {
 	int32_t jitter;
 	/* ReSTIR */
 	int32_t candidates, temporal, temporal_mcap, spatial_neighbors, spatial_radius;
+	/* ReSTIR GI */
+	int32_t gi_capture; /* shade records the depth-1 vertex in aov_p/aov_n */
+	int32_t gi_mcap, gi_neighbors, gi_radius;
+	float prev_center[3];
 };
 
 /* 32-byte reservoir in two 16-byte SoA arrays:

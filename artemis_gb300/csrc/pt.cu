@@ -11,6 +11,12 @@
 #include "kgr_device.cuh"
 #include "kgr_wavefront.h"
 
+/* Resident 128-thread blocks per SM the traversal kernels are compiled for
+ * (bounds their registers). */
+#ifndef KGR_TRACE_MIN_BLOCKS
+#define KGR_TRACE_MIN_BLOCKS 1
+#endif
+
 namespace kgr {
 
 int device_sm_count()
@@ -148,6 +154,10 @@ __global__ void __launch_bounds__(128) shade_kernel(DeviceScene s, PathBuffers p
 					pb.aov_n[p] = f4_of(n3, 0.0f);
 					pb.aov_a[p] = f4_of(sh.mat.diffuse, 0.0f);
 					pb.aov_p[p] = f4_of(sh.x, 0.0f);
+				} else if (depth == 1 && fp.gi_capture) {
+					/* the secondary vertex of a ReSTIR GI sample */
+					pb.aov_n[p] = f4_of(n3, 0.0f);
+					pb.aov_p[p] = f4_of(sh.x, 1.0f);
 				}
 				float4 sv = pb.seed[p];
 				f3 seed = mk(sv.x, sv.y, sv.z);
@@ -216,7 +226,7 @@ __global__ void __launch_bounds__(128) shade_kernel(DeviceScene s, PathBuffers p
 /* is_occluded for every queued shadow ray, then Ld = contr / pdf and
  * L += beta * (Le + Ld) in the order of the recursion. */
 template <int LAYOUT, bool COUNT>
-__global__ void __launch_bounds__(128) shadow_resolve_kernel(DeviceScene s, PathBuffers pb)
+__global__ void __launch_bounds__(128, KGR_TRACE_MIN_BLOCKS) shadow_resolve_kernel(DeviceScene s, PathBuffers pb)
 {
 	const uint32_t n = pb.counters[CNT_SHADOW];
 	uint32_t stride = gridDim.x * blockDim.x;
@@ -238,6 +248,118 @@ __global__ void __launch_bounds__(128) shadow_resolve_kernel(DeviceScene s, Path
 	}
 	if (COUNT)
 		add_visits(pb.visits + 2, cnt);
+}
+
+/* Shadow-ray resolve: Ld = contr / pdf (zero contribution when occluded),
+ * L += beta * (Le + Ld) in the order of the recursion. */
+__device__ __forceinline__ void resolve_shadow(const PathBuffers &pb, uint32_t p, bool occ)
+{
+	float4 c = pb.pend_c[p], e = pb.pend_e[p], be = pb.pend_b[p];
+	f3 contr = occ ? mk(0.0f) : mk(c.x, c.y, c.z);
+	f3 direct = mk(e.x, e.y, e.z) + contr / c.w;
+	float4 Lv = pb.L[p];
+	pb.L[p] = f4_of(mk(Lv.x, Lv.y, Lv.z) + mk(be.x, be.y, be.z) * direct, 0.0f);
+}
+
+/* Persistent traversal of the fast layout: each lane takes a new ray from the
+ * queue (one atomic per warp) as soon as its current ray is finished, so a
+ * lane whose ray ends early does not idle until the longest ray of its warp
+ * is done.  One loop iteration descends to a leaf and tests it.  ANY: shadow
+ * rays, resolved into the path radiance.  The grid is sized to the resident
+ * capacity of the GPU. */
+template <bool ANY, bool COUNT>
+__global__ void __launch_bounds__(128, KGR_TRACE_MIN_BLOCKS) fast_persistent_kernel(DeviceScene s, PathBuffers pb, int q)
+{
+	const uint32_t n = ANY ? pb.counters[CNT_SHADOW] : pb.counters[q == 0 ? CNT_Q0 : CNT_Q1];
+	const uint32_t *queue = ANY ? pb.shadow_queue : pb.queue[q];
+	uint32_t *fetch = pb.counters + (ANY ? CNT_FETCH_SHADOW : CNT_FETCH_CLOSEST);
+	const int lane = threadIdx.x & 31;
+	TraceCounters cnt = {0, 0};
+	uint32_t p = 0;
+	bool have = false, exhausted = false;
+	FastRay r;
+	kgr_hit best;
+	int32_t best_rank = 0x7fffffff;
+	int32_t stack[KGR_STACK_DEPTH];
+	int sp = 0;
+	int32_t ref = 0;
+	for (;;) {
+		bool need = !have && !exhausted;
+		unsigned m = __ballot_sync(0xffffffffu, need);
+		if (m) {
+			int leader = __ffs(m) - 1;
+			uint32_t base = 0;
+			if (lane == leader)
+				base = atomicAdd(fetch, (uint32_t)__popc(m));
+			base = __shfl_sync(0xffffffffu, base, leader);
+			if (need) {
+				uint32_t i = base + __popc(m & ((1u << lane) - 1u));
+				if (i < n) {
+					p = queue[i];
+					float4 a = ANY ? pb.sh_o[p] : pb.ray_o[p];
+					float4 b = ANY ? pb.sh_d[p] : pb.ray_d[p];
+					r = fast_ray(mk(a.x, a.y, a.z), mk(b.x, b.y, b.z));
+					best.prim = -1;
+					best.t = b.w;
+					best.b1 = 0.0f;
+					best.b2 = 0.0f;
+					best_rank = 0x7fffffff;
+					sp = 0;
+					ref = 0;
+					have = true;
+				} else {
+					exhausted = true;
+				}
+			}
+		}
+		if (!__any_sync(0xffffffffu, have))
+			break;
+		if (!have)
+			continue;
+		bool done = false, occ = false;
+		while (ref >= 0) {
+			if (COUNT)
+				cnt.nodes++;
+			int32_t first, second;
+			int hits = fast_node(s, r, ref, best.t, first, second);
+			if (hits == 2) {
+				stack[sp++] = second;
+				ref = first;
+			} else if (hits == 1) {
+				ref = first;
+			} else if (sp == 0) {
+				done = true;
+				break;
+			} else {
+				ref = stack[--sp];
+			}
+		}
+		if (!done) {
+			occ = fast_leaf<ANY, COUNT>(s, r, ref, best, best_rank, &cnt);
+			if (occ || sp == 0)
+				done = true;
+			else
+				ref = stack[--sp];
+		}
+		if (done) {
+			if (ANY)
+				resolve_shadow(pb, p, occ);
+			else
+				pb.hit[p] = make_float4(__int_as_float(best.prim), best.t, best.b1, best.b2);
+			have = false;
+		}
+	}
+	if (COUNT)
+		add_visits(pb.visits + (ANY ? 2 : 0), cnt);
+}
+
+template <class K>
+int resident_grid(K kernel, int block)
+{
+	int per_sm = 0;
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0) != cudaSuccess || per_sm < 1)
+		per_sm = 1;
+	return per_sm * device_sm_count();
 }
 
 __device__ __forceinline__ void accumulate4(float4 *buf, uint32_t i, float4 v, bool acc, float count)
@@ -302,10 +424,16 @@ void pt_trace_closest(const DeviceScene &s, const PathBuffers &pb, int q, int la
 		trace_closest_kernel<KGR_LAYOUT_THREADED, true><<<grid, 128, 0, st>>>(s, pb, q);
 	else if (layout == KGR_LAYOUT_THREADED)
 		trace_closest_kernel<KGR_LAYOUT_THREADED, false><<<grid, 128, 0, st>>>(s, pb, q);
-	else if (c)
-		trace_closest_kernel<KGR_LAYOUT_FAST, true><<<grid, 128, 0, st>>>(s, pb, q);
-	else
-		trace_closest_kernel<KGR_LAYOUT_FAST, false><<<grid, 128, 0, st>>>(s, pb, q);
+	else {
+		KGR_CUDA(cudaMemsetAsync(pb.counters + CNT_FETCH_CLOSEST, 0, sizeof(uint32_t), st));
+		if (c) {
+			static const int g = resident_grid(fast_persistent_kernel<false, true>, 128);
+			fast_persistent_kernel<false, true><<<g, 128, 0, st>>>(s, pb, q);
+		} else {
+			static const int g = resident_grid(fast_persistent_kernel<false, false>, 128);
+			fast_persistent_kernel<false, false><<<g, 128, 0, st>>>(s, pb, q);
+		}
+	}
 	KGR_CUDA(cudaGetLastError());
 }
 
@@ -333,10 +461,15 @@ void pt_shadow_resolve(const DeviceScene &s, const PathBuffers &pb, int layout, 
 		shadow_resolve_kernel<KGR_LAYOUT_THREADED, true><<<grid, 128, 0, st>>>(s, pb);
 	else if (layout == KGR_LAYOUT_THREADED)
 		shadow_resolve_kernel<KGR_LAYOUT_THREADED, false><<<grid, 128, 0, st>>>(s, pb);
-	else if (c)
-		shadow_resolve_kernel<KGR_LAYOUT_FAST, true><<<grid, 128, 0, st>>>(s, pb);
-	else
-		shadow_resolve_kernel<KGR_LAYOUT_FAST, false><<<grid, 128, 0, st>>>(s, pb);
+	else if (c) {
+		/* shadow rays are short: a grid-stride loop over a resident grid
+		 * beats per-lane refill, whose bookkeeping costs more than it saves */
+		static const int g = resident_grid(shadow_resolve_kernel<KGR_LAYOUT_FAST, true>, 128);
+		shadow_resolve_kernel<KGR_LAYOUT_FAST, true><<<g, 128, 0, st>>>(s, pb);
+	} else {
+		static const int g = resident_grid(shadow_resolve_kernel<KGR_LAYOUT_FAST, false>, 128);
+		shadow_resolve_kernel<KGR_LAYOUT_FAST, false><<<g, 128, 0, st>>>(s, pb);
+	}
 	KGR_CUDA(cudaGetLastError());
 }
 

@@ -1392,6 +1392,424 @@ void oracle_render_restir(const oracle_scene *s, const oracle_render_params *p,
 		merge_stats(stats, total);
 }
 
+/* ================================================================== GI == */
+
+namespace {
+
+const float GI_COS_10DEG = 0.984807753f;
+
+struct GiS {
+	f3 xs, ns, Lo;
+};
+
+inline void gi_load(const float *a, const float *b, size_t i, GiS &s, float &W, int &M)
+{
+	uint32_t w = f2u(a[4 * i + 3]);
+	s.xs = mk(a[4 * i], a[4 * i + 1], a[4 * i + 2]);
+	s.ns = unpack_normal(w);
+	s.Lo = mk(b[4 * i], b[4 * i + 1], b[4 * i + 2]);
+	W = b[4 * i + 3];
+	M = unpack_m(w);
+}
+
+inline void gi_store(float *a, float *b, size_t i, const GiS &s, float W, int M)
+{
+	a[4 * i] = s.xs.x; a[4 * i + 1] = s.xs.y; a[4 * i + 2] = s.xs.z;
+	a[4 * i + 3] = u2f(pack_normal_m(s.ns, M));
+	b[4 * i] = s.Lo.x; b[4 * i + 1] = s.Lo.y; b[4 * i + 2] = s.Lo.z; b[4 * i + 3] = W;
+}
+
+inline float gi_norm(float w_sum, int Z, float target)
+{
+	if (!(target > 0.0f) || Z <= 0)
+		return 0.0f;
+	return (float)((double)w_sum / ((double)Z * (double)target));
+}
+
+inline float gi_jac(const f3 &xq, const f3 &xr, const GiS &s)
+{
+	f3 dq = xq - s.xs, dr = xr - s.xs;
+	float lq2 = dot(dq, dq), lr2 = dot(dr, dr);
+	float cq = fabsf(dot(s.ns, dq)) / ksqrt(lq2);
+	float cr = fabsf(dot(s.ns, dr)) / ksqrt(lr2);
+	float j = (cq / cr) * (lr2 / lq2);
+	return (j > 0.0f && j < 1e30f) ? j : 0.0f;
+}
+
+struct GiMergeO {
+	GiS sel;
+	float w = 0.0f;
+	f3 seed;
+	void update(const GiS &s, float weight)
+	{
+		w += weight;
+		float eta = rand_uniform(seed);
+		if ((eta * w) < weight)
+			sel = s;
+	}
+};
+
+struct GB {
+	f3 x, n;
+	bool hit;
+};
+
+inline GB gb_at(const float *pos, const float *nrm, size_t i)
+{
+	GB g;
+	g.x = mk(pos[4 * i], pos[4 * i + 1], pos[4 * i + 2]);
+	g.n = mk(nrm[4 * i], nrm[4 * i + 1], nrm[4 * i + 2]);
+	g.hit = pos[4 * i + 3] > 0.0f;
+	return g;
+}
+
+inline bool gi_similar(const GB &a, float da, const GB &b, float db)
+{
+	if (!a.hit || !b.hit)
+		return false;
+	if (dot(a.n, b.n) < GI_COS_10DEG)
+		return false;
+	return fabsf(db - da) / da <= 0.1f;
+}
+
+inline bool gi_visible(Ctx &ctx, const f3 &from, const f3 &to)
+{
+	f3 D = to - from;
+	float d = length(D);
+	return !ctx.occluded(from, D / d, d);
+}
+
+int gi_neighbor(const oracle_render_params *p, int index, f3 &seed, int radius)
+{
+	return spatial_neighbor(p, index, seed, radius);
+}
+
+} /* namespace */
+
+extern "C" void oracle_render_gi(const oracle_scene *s, const oracle_render_params *p, oracle_gi_state *st,
+		float *color, float *direct_out, oracle_render_stats *stats)
+{
+	std::vector<TriLight> lights = load_lights(s);
+	size_t npix = (size_t)p->width * p->height;
+	std::vector<float> pos(4 * npix, 0.0f), nrm(4 * npix, 0.0f), dir(4 * npix, 0.0f), direct(4 * npix, 0.0f);
+	std::vector<float> aux(4 * npix, 0.0f);
+	std::vector<kgr_material> mats(npix);
+	std::vector<float> cur_a(4 * npix), cur_b(4 * npix), tmp_a(4 * npix), tmp_b(4 * npix);
+	oracle_render_stats total = {0, 0, 0};
+	f3 center = mk(p->center[0], p->center[1], p->center[2]);
+	f3 pcenter = mk(st->prev_center[0], st->prev_center[1], st->prev_center[2]);
+
+	/* primary vertex, DI candidates, GI path, initial reservoir */
+#pragma omp parallel num_threads(nthreads(p->threads))
+	{
+		Ctx ctx;
+		ctx.s = s;
+		ctx.lights = lights;
+		ctx.stats = {0, 0, 0};
+#pragma omp for schedule(dynamic, 64)
+		for (int64_t k = 0; k < (int64_t)npix; k++) {
+			uint32_t pix = (uint32_t)k;
+			uint32_t ix = pix % p->width, iy = pix / p->width;
+			f3 seed = pixel_seed(pix, p->frame, 0);
+			f3 o, d;
+			make_ray(p, ix, iy, true, seed, o, d);
+			ctx.stats.camera_rays++;
+			kgr_hit h = trace_closest(s, o, d, 1e16f, &ctx.internal, &ctx.leaves);
+			SurfaceHit sh;
+			GiS smp = {mk(0.0f), mk(0.0f, 0.0f, 1.0f), mk(0.0f)};
+			bool valid = false;
+			float gpdf = 0.0f;
+			if (h.prim >= 0 && surface(s, h, d, sh)) {
+				f3 n3 = sh.n;
+				float sgn = sh.mat.type == KGR_SHADING_TRANSMISSION ? -1.0f : 1.0f;
+				sh.x = sh.x + sgn * n3 * OFFSET_EPS;
+				store4(pos.data(), pix, sh.x, 1.0f);
+				store4(nrm.data(), pix, n3, 0.0f);
+				mats[pix] = s->materials[s->tris[4 * (size_t)h.prim + 3]];
+				/* DI candidates */
+				f3 risseed = pixel_seed(pix, p->frame, RIS_SALT);
+				float wsum = 0.0f;
+				int M = 0, sel = -1;
+				f3 selp = mk(0.0f);
+				unsigned int tot = (unsigned int)lights.size();
+				for (int c = 0; c < p->candidates; c++) {
+					unsigned int li = (unsigned int)(rand_uniform(seed) * tot);
+					float weight = 0.0f;
+					f3 pt = mk(0.0f);
+					if (li < tot) {
+						const TriLight &l = lights[li];
+						pt = sample_area_light(l, seed);
+						float pdf = 1.0f / (l.area() * tot);
+						f3 D = pt - sh.x;
+						float dd = length(D);
+						f3 Li = ctx.direct_unoccluded(sh, l.intensity, l.normal(), D / dd, dd);
+						float tgt = Li.x + Li.y + Li.z;
+						weight = (pdf > 0) ? tgt / pdf : 0;
+					}
+					wsum += weight;
+					float eta = rand_uniform(risseed);
+					if ((eta * wsum) < weight) {
+						sel = (int)li;
+						selp = pt;
+					}
+					M++;
+				}
+				f3 dl = mk(0.0f);
+				if (sel >= 0) {
+					const TriLight &l = lights[sel];
+					f3 D = selp - sh.x;
+					float dd = length(D);
+					f3 Dn = D / dd;
+					if (!ctx.occluded(sh.x, Dn, dd)) {
+						f3 Li = ctx.direct_unoccluded(sh, l.intensity, l.normal(), Dn, dd);
+						float tgt = Li.x + Li.y + Li.z;
+						float den = tgt * M;
+						float W = (den > 0) ? wsum / den : 0.0f;
+						dl = Li * W;
+					}
+				}
+				store4(direct.data(), pix, dl, 0.0f);
+				/* GI path from the BSDF-sampled direction, throughput 1 */
+				f3 wi;
+				float pdf = 0.0f;
+				eval(sh, wi, pdf, seed);
+				if (pdf > 0 && p->max_depth >= 1) {
+					gpdf = pdf;
+					store4(dir.data(), pix, wi, pdf);
+					f3 L = mk(0.0f), beta = mk(1.0f);
+					f3 oo = sh.x, dd3 = wi;
+					bool captured = false;
+					for (int depth = 1; depth <= p->max_depth; depth++) {
+						ctx.stats.bounce_rays++;
+						kgr_hit hh = trace_closest(s, oo, dd3, 1e16f, &ctx.internal, &ctx.leaves);
+						if (hh.prim < 0)
+							break;
+						SurfaceHit s2;
+						if (!surface(s, hh, dd3, s2))
+							break;
+						f3 n2 = s2.n;
+						float sg = s2.mat.type == KGR_SHADING_TRANSMISSION ? -1.0f : 1.0f;
+						s2.x = s2.x + sg * n2 * OFFSET_EPS;
+						if (depth == 1) {
+							smp.xs = s2.x;
+							smp.ns = n2;
+							captured = true;
+						}
+						f3 dir2 = s2.mat.emission + ctx.Ld(s2, seed);
+						L = L + beta * dir2;
+						f3 w2;
+						float pdf2 = 0.0f;
+						f3 f2 = eval(s2, w2, pdf2, seed);
+						if (!(pdf2 > 0))
+							break;
+						beta = beta * (f2 * fabsf(dot(w2, n2)) / pdf2);
+						if (p->russian_roulette && depth >= p->rr_start_depth) {
+							float q = 1.0f - kmin(kmax(0.05f, beta.y), 1.0f);
+							if (fract(seed.x) < q)
+								break;
+							beta = beta / (1.0f - q);
+						}
+						oo = s2.x;
+						dd3 = w2;
+					}
+					smp.Lo = L;
+					valid = captured && !anynan(L);
+				}
+			}
+			store4(aux.data(), pix, seed, 1.0f);
+			float W = 0.0f;
+			if (valid) {
+				float target = max3(smp.Lo);
+				W = gi_norm(target / gpdf, 1, target);
+			} else {
+				smp.xs = smp.Lo = mk(0.0f);
+				smp.ns = mk(0.0f, 0.0f, 1.0f);
+			}
+			gi_store(cur_a.data(), cur_b.data(), pix, smp, W, 1);
+		}
+#pragma omp critical
+		merge_stats(&total, ctx.stats);
+	}
+
+	/* temporal */
+	if (st->gi_temporal) {
+		float pv[16];
+		mat4_mul(p->prev_projection, p->prev_view, pv);
+#pragma omp parallel num_threads(nthreads(p->threads))
+		{
+			Ctx ctx;
+			ctx.s = s;
+			ctx.lights = lights;
+			ctx.stats = {0, 0, 0};
+#pragma omp for schedule(dynamic, 64)
+			for (int64_t k = 0; k < (int64_t)npix; k++) {
+				size_t pix = (size_t)k;
+				GB g = gb_at(pos.data(), nrm.data(), pix);
+				if (!g.hit)
+					continue;
+				/* reprojection as reproject() without the samples > 0 shortcut */
+				float qv[4];
+				for (int i = 0; i < 4; i++)
+					qv[i] = pv[0 * 4 + i] * g.x.x + pv[1 * 4 + i] * g.x.y + pv[2 * 4 + i] * g.x.z
+						+ pv[3 * 4 + i] * 1.0f;
+				float u = qv[0] / qv[3], v = qv[1] / qv[3];
+				if (!(u >= -1.0f && u <= 1.0f && v >= -1.0f && v <= 1.0f))
+					continue;
+				u = (u + 1.0f) * 0.5f;
+				v = (v + 1.0f) * 0.5f;
+				int ixp = (int)((double)(u * (float)p->width) + 0.5);
+				int iyp = (int)((double)(v * (float)p->height) + 0.5);
+				if (ixp < 0 || iyp < 0 || ixp >= (int)p->width || iyp >= (int)p->height)
+					continue;
+				size_t pi = (size_t)iyp * p->width + ixp;
+				GB gp = gb_at(st->prev_position, st->prev_normal, pi);
+				if (!gi_similar(g, length(g.x - center), gp, length(gp.x - pcenter)))
+					continue;
+				GiS ps, cs;
+				float pW, cW;
+				int pM, cM;
+				gi_load(st->res_a, st->res_b, pi, ps, pW, pM);
+				if (pM <= 0)
+					continue;
+				gi_load(cur_a.data(), cur_b.data(), pix, cs, cW, cM);
+				int pMc = pM < st->gi_mcap ? pM : st->gi_mcap;
+				GiMergeO r;
+				r.sel = {mk(0.0f), mk(0.0f), mk(0.0f)};
+				r.seed = load4(aux.data(), pix);
+				r.update(cs, max3(cs.Lo) * cW * cM);
+				float J = gi_jac(g.x, gp.x, ps);
+				float wp = max3(ps.Lo) * J * pW * pMc;
+				r.update(ps, wp);
+				int Mt = cM + (wp > 0.0f ? pMc : 0);
+				float W = gi_norm(r.w, Mt, max3(r.sel.Lo));
+				gi_store(cur_a.data(), cur_b.data(), pix, r.sel, W, Mt);
+			}
+#pragma omp critical
+			merge_stats(&total, ctx.stats);
+		}
+	}
+
+	/* spatial iterations, ping-pong */
+	float *in_a = cur_a.data(), *in_b = cur_b.data(), *out_a = tmp_a.data(), *out_b = tmp_b.data();
+	for (int it = 0; it < st->gi_spatial_iterations; it++) {
+#pragma omp parallel num_threads(nthreads(p->threads))
+		{
+			Ctx ctx;
+			ctx.s = s;
+			ctx.lights = lights;
+			ctx.stats = {0, 0, 0};
+			std::vector<int> nidx(st->gi_neighbors), nM(st->gi_neighbors);
+#pragma omp for schedule(dynamic, 64)
+			for (int64_t k = 0; k < (int64_t)npix; k++) {
+				size_t pix = (size_t)k;
+				GiS cs;
+				float cW;
+				int cM;
+				gi_load(in_a, in_b, pix, cs, cW, cM);
+				GB g = gb_at(pos.data(), nrm.data(), pix);
+				if (!g.hit) {
+					gi_store(out_a, out_b, pix, cs, cW, cM);
+					continue;
+				}
+				float depth = length(g.x - center);
+				GiMergeO r;
+				r.sel = {mk(0.0f), mk(0.0f), mk(0.0f)};
+				r.seed = load4(aux.data(), pix);
+				r.update(cs, max3(cs.Lo) * cW * cM);
+				int Msum = cM;
+				for (int i = 0; i < st->gi_neighbors; i++) {
+					int index0 = gi_neighbor(p, (int)pix, r.seed, st->gi_radius);
+					nidx[i] = -1;
+					nM[i] = 0;
+					GB gn = gb_at(pos.data(), nrm.data(), (size_t)index0);
+					if (!gi_similar(g, depth, gn, length(gn.x - center)))
+						continue;
+					GiS ns;
+					float nW;
+					int nMi;
+					gi_load(in_a, in_b, (size_t)index0, ns, nW, nMi);
+					if (nMi <= 0)
+						continue;
+					nidx[i] = index0;
+					nM[i] = nMi;
+					Msum += nMi;
+					float J = gi_jac(g.x, gn.x, ns);
+					float wn = max3(ns.Lo) * J * nW * nMi;
+					if (wn > 0.0f && !gi_visible(ctx, g.x, ns.xs))
+						wn = 0.0f;
+					r.update(ns, wn);
+				}
+				int Z = cM;
+				float target = max3(r.sel.Lo);
+				if (target > 0.0f) {
+					for (int i = 0; i < st->gi_neighbors; i++) {
+						if (nidx[i] < 0)
+							continue;
+						GB gn = gb_at(pos.data(), nrm.data(), (size_t)nidx[i]);
+						if (gi_jac(gn.x, g.x, r.sel) > 0.0f && gi_visible(ctx, gn.x, r.sel.xs))
+							Z += nM[i];
+					}
+				}
+				gi_store(out_a, out_b, pix, r.sel, gi_norm(r.w, Z, target), Msum);
+			}
+#pragma omp critical
+			merge_stats(&total, ctx.stats);
+		}
+		std::swap(in_a, out_a);
+		std::swap(in_b, out_b);
+	}
+
+	/* final shading and history */
+#pragma omp parallel num_threads(nthreads(p->threads))
+	{
+		Ctx ctx;
+		ctx.s = s;
+		ctx.lights = lights;
+		ctx.stats = {0, 0, 0};
+#pragma omp for schedule(dynamic, 64)
+		for (int64_t k = 0; k < (int64_t)npix; k++) {
+			size_t pix = (size_t)k;
+			GB g = gb_at(pos.data(), nrm.data(), pix);
+			f3 c = mk(0.0f);
+			if (g.hit) {
+				SurfaceHit h;
+				h.mat = load_material(mats[pix]);
+				h.entering = false;
+				h.n = g.n;
+				h.wo = normalize(center - g.x);
+				h.x = g.x;
+				GiS rs;
+				float W;
+				int M;
+				gi_load(in_a, in_b, pix, rs, W, M);
+				f3 gi = mk(0.0f);
+				if (W > 0.0f) {
+					f3 D = rs.xs - g.x;
+					float d = length(D);
+					f3 w = D / d;
+					if (!ctx.occluded(g.x, w, d))
+						gi = brdf(h, w) * rs.Lo * (fabsf(dot(h.n, w)) * W);
+				}
+				c = h.mat.emission + load4(direct.data(), pix) + gi;
+			}
+			if (anynan(c))
+				c = mk(1.0f, 0.0f, 1.0f);
+			accumulate4(color, pix, c, 1.0f, p->accumulate != 0, (float)p->samples);
+			if (direct_out)
+				memcpy(direct_out + 4 * pix, direct.data() + 4 * pix, 16);
+		}
+#pragma omp critical
+		merge_stats(&total, ctx.stats);
+	}
+	memcpy(st->res_a, in_a, 16 * npix);
+	memcpy(st->res_b, in_b, 16 * npix);
+	memcpy(st->prev_position, pos.data(), 16 * npix);
+	memcpy(st->prev_normal, nrm.data(), 16 * npix);
+	memcpy(st->prev_center, p->center, 12);
+	if (stats)
+		merge_stats(stats, total);
+}
+
 /* --------------------------------------------------------- known answers */
 
 void oracle_kat_rng(float sx, float sy, float sz, int draws, float *out)

@@ -124,6 +124,26 @@ void oracle_render_restir(const oracle_scene *s, const oracle_render_params *p,
 		oracle_restir_state *st, float *color, float *normal, float *albedo,
 		float *position, oracle_render_stats *stats);
 
+/* ReSTIR GI (no working reference; the project's specification restated):
+ * state carried between frames -- last frame's GI reservoirs in the 32-byte
+ * two-array layout ({x_s, bits(n_s oct | M)}, {L_o, W}) and its G-buffer --
+ * plus the previous camera. */
+typedef struct oracle_gi_state {
+	float *res_a;         /* float4 per pixel */
+	float *res_b;         /* float4 per pixel */
+	float *prev_position; /* float4 per pixel, w = 1 on a hit */
+	float *prev_normal;   /* float4 per pixel */
+	float prev_center[3];
+	int32_t gi_temporal, gi_mcap, gi_spatial_iterations, gi_neighbors, gi_radius;
+} oracle_gi_state;
+
+/* One ReSTIR GI frame (DI candidates + GI reservoir reuse), see gi.cu's
+ * header for the algorithm.  color accumulates with p->accumulate; the
+ * state is updated for the next frame.  direct (float4 per pixel, may be
+ * NULL) receives the DI term. */
+void oracle_render_gi(const oracle_scene *s, const oracle_render_params *p, oracle_gi_state *st,
+		float *color, float *direct, oracle_render_stats *stats);
+
 /* Known-answer helpers exposed for the golden-vector tests. */
 void oracle_kat_rng(float seed_x, float seed_y, float seed_z, int draws, float *out);
 float oracle_kat_intersect(const float *v1, const float *v2, const float *v3,

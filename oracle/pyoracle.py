@@ -58,6 +58,39 @@ class RestirState(ctypes.Structure):
         "materials", "intermediate", "auxiliary")]
 
 
+class GiStateC(ctypes.Structure):
+    _fields_ = [("res_a", ctypes.c_void_p), ("res_b", ctypes.c_void_p), ("prev_position", ctypes.c_void_p),
+                ("prev_normal", ctypes.c_void_p), ("prev_center", ctypes.c_float * 3),
+                ("gi_temporal", ctypes.c_int32), ("gi_mcap", ctypes.c_int32),
+                ("gi_spatial_iterations", ctypes.c_int32), ("gi_neighbors", ctypes.c_int32),
+                ("gi_radius", ctypes.c_int32)]
+
+
+class GiState:
+    """Oracle-side ReSTIR GI state carried between frames."""
+
+    def __init__(self, n, temporal=True, mcap=30, iterations=3, neighbors=8, radius=30):
+        self.arrays = {k: np.zeros((n, 4), np.float32)
+                       for k in ("res_a", "res_b", "prev_position", "prev_normal")}
+        self.c = GiStateC(*[ptr(self.arrays[k]) for k in ("res_a", "res_b", "prev_position", "prev_normal")],
+                          (ctypes.c_float * 3)(0, 0, 0), int(temporal), mcap, iterations, neighbors, radius)
+        self.started = False
+
+
+def render_gi(scene, params, state, color=None):
+    n = params.width * params.height
+    if color is None:
+        color = np.zeros((n, 4), np.float32)
+    direct = np.zeros((n, 4), np.float32)
+    if not state.started:
+        state.c.prev_center[:] = params.center[:]
+        state.started = True
+    st = RenderStats()
+    lib().oracle_render_gi(ctypes.byref(scene.c), ctypes.byref(params), ctypes.byref(state.c), ptr(color),
+                           ptr(direct), ctypes.byref(st))
+    return color, direct, st
+
+
 def build():
     """Compile liboracle.so with the committed Makefile (g++, -ffp-contract=off)."""
     subprocess.check_call(["make", "-s", "-C", HERE, "liboracle.so"])
@@ -85,6 +118,8 @@ def lib():
         L.oracle_render_restir.argtypes = [ctypes.POINTER(OracleScene), ctypes.POINTER(RenderParams),
                                            ctypes.POINTER(RestirState), vp, vp, vp, vp,
                                            ctypes.POINTER(RenderStats)]
+        L.oracle_render_gi.argtypes = [ctypes.POINTER(OracleScene), ctypes.POINTER(RenderParams),
+                                       ctypes.POINTER(GiStateC), vp, vp, ctypes.POINTER(RenderStats)]
         L.oracle_kat_rng.argtypes = [ctypes.c_float] * 3 + [ctypes.c_int, vp]
         L.oracle_kat_intersect.restype = ctypes.c_float
         L.oracle_kat_intersect.argtypes = [vp] * 6

@@ -23,6 +23,7 @@
 #include <variant>
 
 #include "kgr_internal.h"
+#include "kgr_cache.h"
 #include "kgr_gi.h"
 #include "kgr_wavefront.h"
 
@@ -563,6 +564,16 @@ struct kgr_attachment {
 	DevBuf<float4> gi_a[3], gi_b[3], g_pos, g_nrm, g_ppos, g_pnrm, g_direct, g_dir;
 	int gi_prev = 0;
 
+	/* radiance cache: network, query rows, training paths, records, batch */
+	kgr_mlp *cache_mlp = nullptr;
+	DevBuf<uint16_t> q_feat, r_feat, b_x;
+	DevBuf<float4> q_le, q_out, r_beta, r_lb, r_le, b_t;
+	DevBuf<uint32_t> b_count;
+	DevBuf<float4> t_f4[14];
+	DevBuf<uint32_t> t_queues[3], t_counters;
+	uint32_t t_capacity = 0;
+	int record_depths = 0;
+
 	kgr_render_stats stats = {0, 0, 0, 0, 0};
 	uint32_t last_paths = 0;
 	cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
@@ -677,12 +688,50 @@ struct kgr_attachment {
 		}
 		for (DevBuf<float4> *b : {&g_pos, &g_nrm, &g_ppos, &g_pnrm, &g_direct, &g_dir})
 			b->release();
+		for (DevBuf<uint16_t> *b : {&q_feat, &r_feat, &b_x})
+			b->release();
+		for (DevBuf<float4> *b : {&q_le, &q_out, &r_beta, &r_lb, &r_le, &b_t})
+			b->release();
+		b_count.release();
+		for (auto &b : t_f4)
+			b.release();
+		for (auto &q : t_queues)
+			q.release();
+		t_counters.release();
+		t_capacity = 0;
 		capacity = 0;
+	}
+
+	/* path buffers of the cache's training paths */
+	PathBuffers train_buffers(uint32_t paths)
+	{
+		if (paths > t_capacity) {
+			for (auto &b : t_f4)
+				b.alloc(paths);
+			for (auto &q : t_queues)
+				q.alloc(paths);
+			t_counters.alloc(CNT_COUNT);
+			t_capacity = paths;
+		}
+		PathBuffers pb;
+		float4 **fields[14] = {&pb.ray_o, &pb.ray_d, &pb.beta, &pb.L, &pb.seed, &pb.hit, &pb.sh_o, &pb.sh_d,
+			&pb.pend_c, &pb.pend_e, &pb.pend_b, &pb.aov_n, &pb.aov_a, &pb.aov_p};
+		for (int k = 0; k < 14; k++)
+			*fields[k] = t_f4[k].ptr;
+		pb.queue[0] = t_queues[0].ptr;
+		pb.queue[1] = t_queues[1].ptr;
+		pb.shadow_queue = t_queues[2].ptr;
+		pb.counters = t_counters.ptr;
+		pb.visits = nullptr;
+		pb.capacity = t_capacity;
+		return pb;
 	}
 
 	~kgr_attachment()
 	{
 		release_all();
+		if (cache_mlp)
+			kgr_mlp_destroy(cache_mlp);
 		visits.release();
 		if (ev_start)
 			cudaEventDestroy(ev_start);
@@ -893,6 +942,118 @@ void render_restir_di(kgr_attachment *att, const kgr_launch_info *info, const kg
 	att->prev_index = in;
 	memcpy(att->prev_projection, info->camera.projection, 64);
 	memcpy(att->prev_view, info->camera.view, 64);
+	att->stats.kernel_launches = launches;
+	att->stats.camera_rays = fp.paths;
+	att->last_paths = fp.paths;
+}
+
+/* Path tracer with the radiance cache: render paths end at the first bounce
+ * with a network query; training paths (plain, full depth) train it. */
+void render_pt_cached(kgr_attachment *att, const kgr_launch_info *info, const kgr_scene *sc, cudaStream_t st)
+{
+	FrameParams fp = frame_params(att, info);
+	int spp = att->opt_int("spp", 1);
+	KGR_REQUIRE(spp >= 1 && spp <= 4096, KGR_ERR_INVALID_ARGUMENT, "spp out of range");
+	KGR_REQUIRE(fp.max_depth >= 1, KGR_ERR_INVALID_ARGUMENT, "the cached tracer needs max_depth >= 1");
+	uint64_t paths = (uint64_t)fp.npix * (uint64_t)spp;
+	KGR_REQUIRE(paths < (1ull << 31), KGR_ERR_UNSUPPORTED, "too many paths per frame");
+	fp.spp = (uint32_t)spp;
+	fp.paths = (uint32_t)paths;
+	fp.jitter = 1;
+	att->ensure_paths(fp.paths);
+	PathBuffers pb = att->path_buffers();
+	DeviceScene s = scene_for_launch(sc, info);
+	OutputBuffers out = {reinterpret_cast<float4 *>(info->buffers.color),
+		reinterpret_cast<float4 *>(info->buffers.normal), reinterpret_cast<float4 *>(info->buffers.albedo),
+		reinterpret_cast<float4 *>(info->buffers.position)};
+	int dtype = att->opt_str("cache_dtype", "bf16") == "fp16" ? KGR_MLP_FP16 : KGR_MLP_BF16;
+	if (!att->cache_mlp || att->cache_mlp->dtype != dtype) {
+		if (att->cache_mlp)
+			kgr_mlp_destroy(att->cache_mlp);
+		att->cache_mlp = nullptr;
+		KGR_REQUIRE(kgr_mlp_create(dtype, 1, att->device, &att->cache_mlp) == KGR_OK, KGR_ERR_CUDA,
+			std::string("radiance cache: ") + kgr_last_error());
+	}
+	MlpParams mp = att->cache_mlp->params();
+	CacheParams cp;
+	cp.dtype = dtype;
+	for (int k = 0; k < 3; k++) {
+		cp.bmin[k] = sc->bounds_min[k];
+		float ext = sc->bounds_max[k] - sc->bounds_min[k];
+		cp.binv[k] = ext > 0.0f ? 1.0f / ext : 1.0f;
+	}
+	att->q_feat.alloc((size_t)att->capacity * 64);
+	att->q_le.alloc(att->capacity);
+	att->q_out.alloc(att->capacity);
+	uint32_t launches = 0;
+
+	/* render: primary vertex, first bounce, cache */
+	att->mark(-1, st);
+	pt_generate(pb, fp, st);
+	att->mark(STAGE_GENERATE, st);
+	pt_trace_closest(s, pb, 0, fp.layout, st);
+	att->mark(STAGE_TRACE_CLOSEST, st);
+	pt_shade(s, pb, fp, 0, 0, st);
+	att->mark(STAGE_SHADE, st);
+	pt_shadow_resolve(s, pb, fp.layout, st);
+	att->mark(STAGE_SHADOW, st);
+	reset_counters(pb, (1 << CNT_Q0) | (1 << CNT_SHADOW), st);
+	att->mark(-1, st);
+	pt_trace_closest(s, pb, 1, fp.layout, st);
+	att->mark(STAGE_TRACE_CLOSEST, st);
+	cache_query(s, pb, 1, cp, att->q_feat.ptr, att->q_le.ptr, st);
+	mlp_infer(mp, att->q_feat.ptr, att->capacity, att->q_out.ptr, st, pb.counters + CNT_Q1);
+	cache_apply(pb, 1, att->q_out.ptr, att->q_le.ptr, st);
+	att->mark(STAGE_CACHE_INFER, st);
+	pt_accumulate(pb, fp, out, st);
+	att->mark(STAGE_ACCUMULATE, st);
+	launches += 10;
+
+	/* training paths */
+	if (att->opt_int("cache_train", 1)) {
+		uint32_t tpaths = (uint32_t)att->opt_int("cache_train_paths", 16384);
+		KGR_REQUIRE(tpaths >= 128 && tpaths <= (1u << 22), KGR_ERR_INVALID_ARGUMENT, "cache_train_paths out of range");
+		const uint32_t cap = 1u << 16;
+		PathBuffers tb = att->train_buffers(tpaths);
+		int depths = fp.max_depth + 1;
+		size_t slots = (size_t)tpaths * depths;
+		att->r_feat.alloc(slots * 64);
+		att->r_beta.alloc(slots);
+		att->r_lb.alloc(slots);
+		att->r_le.alloc(slots);
+		att->b_x.alloc((size_t)cap * 64);
+		att->b_t.alloc(cap);
+		att->b_count.alloc(1);
+		KGR_CUDA(cudaMemsetAsync(att->r_le.ptr, 0, slots * sizeof(float4), st));
+		CacheRecords rec = {att->r_feat.ptr, att->r_beta.ptr, att->r_lb.ptr, att->r_le.ptr, depths};
+		FrameParams tf = fp;
+		tf.spp = 1;
+		tf.paths = tpaths;
+		cache_train_generate(tb, tf, tpaths, st);
+		for (int d = 0; d <= fp.max_depth; d++) {
+			int q = d & 1;
+			if (d > 0)
+				reset_counters(tb, (1 << (q ^ 1)) | (1 << CNT_SHADOW), st);
+			pt_trace_closest(s, tb, q, fp.layout, st);
+			if (d >= 1)
+				cache_record(s, tb, q, d, cp, rec, st);
+			pt_shade(s, tb, tf, d, q, st);
+			pt_shadow_resolve(s, tb, fp.layout, st);
+			launches += d >= 1 ? 4 : 3;
+		}
+		cache_targets(tb, tpaths, rec, dtype, att->b_x.ptr, att->b_t.ptr, att->b_count.ptr, cap, st);
+		mlp_gradients(mp, att->b_x.ptr, att->b_t.ptr, cap, att->cache_mlp->grad.ptr, att->cache_mlp->loss.ptr, st,
+			att->b_count.ptr);
+		att->cache_mlp->step++;
+		float lr = 1e-3f;
+		auto it = att->options.find("cache_lr");
+		if (it != att->options.end())
+			if (auto f = std::get_if<float>(&it->second))
+				lr = *f;
+		mlp_adam(mp, att->cache_mlp->grad.ptr, lr, att->cache_mlp->step, st);
+		att->mark(STAGE_CACHE_TRAIN, st);
+		launches += 4;
+	}
 	att->stats.kernel_launches = launches;
 	att->stats.camera_rays = fp.paths;
 	att->last_paths = fp.paths;
@@ -1132,7 +1293,9 @@ static const std::map<std::string, OptionValue> &option_defaults()
 		{"spatial_passes", 2}, {"spatial_neighbors", 5}, {"spatial_radius", 30},
 		{"profile", false}, {"count_visits", false},
 		{"gi_temporal", true}, {"gi_mcap", 30}, {"gi_spatial_iterations", 3}, {"gi_neighbors", 8},
-		{"gi_radius", 30}};
+		{"gi_radius", 30},
+		{"cache", false}, {"cache_train", true}, {"cache_train_paths", 16384}, {"cache_lr", 1e-3f},
+		{"cache_dtype", std::string("bf16")}};
 	return d;
 }
 
@@ -1200,7 +1363,12 @@ kgr_status kgr_render(kgr_attachment *att, const kgr_launch_info *info, const kg
 		DeviceGuard g(att->device);
 		cudaStream_t st = (cudaStream_t)stream;
 		switch (att->kind) {
-		case KIND_PT: render_pt(att, info, sc, st); break;
+		case KIND_PT:
+			if (att->opt_int("cache", 0))
+				render_pt_cached(att, info, sc, st);
+			else
+				render_pt(att, info, sc, st);
+			break;
 		case KIND_RESTIR_DI: render_restir_di(att, info, sc, st); break;
 		case KIND_RESTIR_GI: render_restir_gi(att, info, sc, st); break;
 		default: throw Error(KGR_ERR_UNSUPPORTED, "attachment kind not built");

@@ -1,0 +1,51 @@
+/*
+ * kgr_mlp.h -- the radiance-cache MLP (mlp.cu) and the device buffers of one
+ * network: FP32 master weights W[6][64][64] ([in][out]; the last layer's
+ * outputs 3..63 unused), Adam moments, and half-precision copies
+ * wn[l] = [in][cols] and wt[l] = [cols][in] (cols = 64, or 16 for the last).
+ */
+#ifndef KGR_MLP_H_
+#define KGR_MLP_H_
+
+#include "kgr_internal.h"
+
+namespace kgr {
+
+#define KGR_MLP_PARAMS (6 * 64 * 64)
+#define KGR_MLP_INPUTS 64
+
+struct MlpParams {
+	int dtype; /* KGR_MLP_BF16 or KGR_MLP_FP16 */
+	float *master, *m, *v;
+	void *wn, *wt;
+};
+
+/* out[i] = {r, g, b, 0} for the n rows of x ([n][64] half precision); with
+ * n_dev, the row count is min(n, *n_dev) read on the device. */
+void mlp_infer(const MlpParams &mp, const void *x, uint32_t n, float4 *out, cudaStream_t st,
+		const uint32_t *n_dev = nullptr);
+/* grad (FP32, [6][64][64]) = d loss / d W over n rows; loss = sum of the
+ * relative L2 terms (not divided by n). */
+void mlp_gradients(const MlpParams &mp, const void *x, const float4 *target, uint32_t n, float *grad, float *loss,
+		cudaStream_t st, const uint32_t *n_dev = nullptr);
+/* One Adam step (lr, bias correction for `step`); step <= 0 only refreshes
+ * the half-precision copies from the master weights. */
+void mlp_adam(const MlpParams &mp, const float *grad, float lr, int step, cudaStream_t st);
+
+int device_sm_count();
+
+} /* namespace kgr */
+
+struct kgr_mlp {
+	int device = 0;
+	int dtype = 0;
+	int step = 0;
+	kgr::DevBuf<float> master, m, v, grad, loss;
+	kgr::DevBuf<uint16_t> wn, wt;
+	kgr::MlpParams params()
+	{
+		return kgr::MlpParams{dtype, master.ptr, m.ptr, v.ptr, wn.ptr, wt.ptr};
+	}
+};
+
+#endif

@@ -58,7 +58,9 @@ enum StageKind {
 	STAGE_RESTIR_TEMPORAL = 6,
 	STAGE_RESTIR_SPATIAL = 7,
 	STAGE_RESTIR_FINALIZE = 8,
-	STAGE_COUNT = 9
+	STAGE_CACHE_INFER = 9,  /* radiance-cache query + network + apply */
+	STAGE_CACHE_TRAIN = 10, /* training paths + targets + gradient + Adam */
+	STAGE_COUNT = 11
 };
 
 /* Streaming read of a buffer with 16-byte loads (bandwidth probe). */

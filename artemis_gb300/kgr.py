@@ -126,6 +126,13 @@ def lib():
             "kgr_debug_copy": (c_i32, [vp, ctypes.c_char_p, vp, c_u64]),
             "kgr_get_stage_times": (c_i32, [vp, vp, vp, c_u32]),
             "kgr_render_pt_noalloc": (c_i32, [vp, vp, c_i32, c_i32, c_i32, vp]),
+            "kgr_mlp_create": (c_i32, [c_i32, c_u64, c_i32, vp]),
+            "kgr_mlp_get_weights": (c_i32, [vp, vp]),
+            "kgr_mlp_set_weights": (c_i32, [vp, vp]),
+            "kgr_mlp_forward": (c_i32, [vp, vp, c_u32, vp, vp]),
+            "kgr_mlp_gradients": (c_i32, [vp, vp, vp, c_u32, vp, vp]),
+            "kgr_mlp_train_step": (c_i32, [vp, vp, vp, c_u32, c_f, vp]),
+            "kgr_mlp_destroy": (c_i32, [vp]),
             "kgr_get_visit_counts": (c_i32, [vp, vp]),
             "kgr_measure_read_bandwidth": (c_i32, [c_i32, c_u64, c_i32, vp]),
             "kgr_load_attachment": (PluginRet, [ctypes.c_char_p]),
@@ -304,6 +311,47 @@ def camera_dict(info):
             "projection": list(c.projection), "view": list(c.view)}
 
 
+class Mlp:
+    """kgr_mlp: the radiance-cache network (device pointers for x/out/targets)."""
+
+    def __init__(self, dtype="bf16", seed=0, device=-1):
+        h = vp()
+        check(lib().kgr_mlp_create(0 if dtype == "bf16" else 1, seed, device, ctypes.byref(h)))
+        self.handle, self.dtype = h, dtype
+
+    def weights(self):
+        w = np.zeros((6, 64, 64), np.float32)
+        check(lib().kgr_mlp_get_weights(self.handle, _ptr(w)))
+        return w
+
+    def set_weights(self, w):
+        w = np.ascontiguousarray(w, np.float32)
+        check(lib().kgr_mlp_set_weights(self.handle, _ptr(w)))
+
+    def forward(self, x_ptr, n, out_ptr, stream=None):
+        check(lib().kgr_mlp_forward(self.handle, x_ptr, n, out_ptr, stream))
+
+    def gradients(self, x_ptr, t_ptr, n):
+        g = np.zeros((6, 64, 64), np.float32)
+        loss = ctypes.c_float()
+        check(lib().kgr_mlp_gradients(self.handle, x_ptr, t_ptr, n, _ptr(g), ctypes.byref(loss)))
+        return loss.value, g
+
+    def train_step(self, x_ptr, t_ptr, n, lr=1e-3, stream=None):
+        check(lib().kgr_mlp_train_step(self.handle, x_ptr, t_ptr, n, lr, stream))
+
+    def close(self):
+        if self.handle:
+            lib().kgr_mlp_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Attachment:
     """kgr_attachment: the AttachmentRTX life cycle over the C ABI."""
 
@@ -359,7 +407,7 @@ class Attachment:
         return s
 
     STAGES = ("generate", "trace_closest", "shade", "shadow", "accumulate", "restir_primary",
-              "restir_temporal", "restir_spatial", "restir_finalize")
+              "restir_temporal", "restir_spatial", "restir_finalize", "cache_infer", "cache_train")
 
     def stage_times(self):
         """{stage: (total ms, launches)} since the last call ("profile" option)."""

@@ -350,6 +350,33 @@ typedef struct kgr_plugin_ret {
 } kgr_plugin_ret;
 kgr_plugin_ret kgr_load_attachment(const char *kind);
 
+/* --------------------------------------------------------- radiance cache -- */
+
+/* The radiance-cache network: 64 inputs -> 5 hidden layers of 64 (ReLU) ->
+ * RGB, half-precision weights and activations with FP32 accumulation on the
+ * tensor cores, trained with Adam on a relative L2 loss.  The reference's
+ * only network is an unused FP32 forward pass (editor/mlp.cuh:48-154). */
+enum { KGR_MLP_BF16 = 0, KGR_MLP_FP16 = 1 };
+typedef struct kgr_mlp kgr_mlp;
+
+/* Uniform(+-sqrt(6/fan_in)) initialisation from `seed`. */
+kgr_status kgr_mlp_create(int32_t dtype, uint64_t seed, int32_t device, kgr_mlp **out);
+/* FP32 master weights W[6][64][64] as [layer][in][out] (last layer: out < 3). */
+kgr_status kgr_mlp_get_weights(const kgr_mlp *mlp, float *host);
+kgr_status kgr_mlp_set_weights(kgr_mlp *mlp, const float *host);
+/* out (device, n x 4 floats) = network(x) for x (device, n x 64 halves of the
+ * network's type).  Asynchronous on `stream`. */
+kgr_status kgr_mlp_forward(kgr_mlp *mlp, const void *x, uint32_t n, float *out, void *stream);
+/* Gradient of the loss sum_rows sum_c (y-t)^2/(y^2+0.01) / n over n rows
+ * (targets device n x 4) into host memory (6*64*64 floats, may be NULL) and
+ * the loss into *loss (may be NULL).  Synchronous. */
+kgr_status kgr_mlp_gradients(kgr_mlp *mlp, const void *x, const float *targets, uint32_t n,
+		float *grad_host, float *loss);
+/* One Adam step (beta 0.9/0.99, eps 1e-8) at learning rate lr on n rows. */
+kgr_status kgr_mlp_train_step(kgr_mlp *mlp, const void *x, const float *targets, uint32_t n,
+		float lr, void *stream);
+kgr_status kgr_mlp_destroy(kgr_mlp *mlp);
+
 /* ------------------------------------------------------ procedural scenes -- */
 
 /* Seeded procedural scenes used by the tests and the benchmark.  The

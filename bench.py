@@ -38,6 +38,16 @@ METRIC = "1080p ms/frame & Mrays/s at equal relMSE vs plain GPU PT; serve p50/p9
 WORKLOAD = ("plain PT 1920x1080 4spp, max depth 8, RR from depth 3, NEE over 1024 emissive tris; "
             "procedural terrain 1.16M tris (512^2 height field + 2000 icospheres), SAH leaves<=4")
 
+# Kernel behind each traversal stage, per layout.
+KERNELS = {("trace_closest", "fast"): "fast_persistent_kernel<false>",
+           ("shadow", "fast"): "shadow_resolve_kernel<fast>",
+           ("trace_closest", "threaded"): "trace_closest_kernel<threaded>",
+           ("shadow", "threaded"): "shadow_resolve_kernel<threaded>"}
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
+# traversal kernels at this workload, from one ncu capture of a smaller frame
+# of the same scene scaled by the rays it traced; None where not captured.
+TRAFFIC = {}
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -246,12 +256,18 @@ def bench_ours(args):
         att.render(info_for(s), sc, sptr)
     torch.cuda.synchronize()
 
-    # traversal visit counts of one frame (untimed): algorithmic bytes
-    att.set_option("count_visits", True)
-    att.render(info_for(0), sc, sptr)
-    torch.cuda.synchronize()
-    visits = att.visit_counts()
+    # traversal visit counts of one frame (untimed), on the timed layout and on
+    # the reference's threaded layout: both layouts give bit-identical paths,
+    # so the second count is the reference walk over the same rays
+    visits = {}
+    for lay in dict.fromkeys((args.layout, "threaded")):
+        att.set_option("layout", lay)
+        att.set_option("count_visits", True)
+        att.render(info_for(0), sc, sptr)
+        torch.cuda.synchronize()
+        visits[lay] = att.visit_counts()
     att.set_option("count_visits", False)
+    att.set_option("layout", args.layout)
     att.stats()
 
     # timed region
@@ -305,20 +321,32 @@ def bench_ours(args):
 
     peaks, peak_kind = measured_peaks()
     l2_gbs = kgr.read_bandwidth(64 << 20, 50, dev)
-    # dominant kernel and its algorithmic bytes per launch (fast layout: 64 B
-    # child-pair node, 48 B triangle record)
-    node_b, tri_b = (64, 48) if args.layout == "fast" else (48, 80)
-    per_stage_bytes = {"trace_closest": visits[0] * node_b + visits[1] * tri_b,
-                       "shadow": visits[2] * node_b + visits[3] * tri_b}
+    # dominant traversal stage and its algorithmic bytes per launch: the
+    # reference walk's reads for the same rays (threaded bvh.cpp layout: 48 B
+    # per interior record; 16 B leaf header + 64 B triangle = index vec4 and
+    # three position vec4s per leaf record), divided by the timed kernel's
+    # per-launch CUDA-event time.  `own_layout` gives the bytes the timed
+    # layout itself reads (fast: 64 B child-pair node, 48 B triangle record).
+    def stage_bytes(v, node_b, tri_b):
+        return {"trace_closest": v[0] * node_b + v[1] * tri_b, "shadow": v[2] * node_b + v[3] * tri_b}
+
+    ref_bytes = stage_bytes(visits["threaded"], 48, 80)
+    own_bytes = stage_bytes(visits[args.layout], *((64, 48) if args.layout == "fast" else (48, 80)))
     dom = max(("trace_closest", "shadow"), key=lambda k: stages[k][0])
     ms_dom, n_dom = stages[dom]
     launches_frame = n_dom / max(1, args.steps)
-    bytes_per_launch = per_stage_bytes[dom] / max(1, launches_frame)
-    achieved = bytes_per_launch / (ms_dom / max(1, n_dom) * 1e-3) / 1e9
-    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
-                "frac": round(achieved / peaks.get("hbm_gbs"), 4), "traffic": None,
-                "kernel": dom + "_kernel", "peak_source": peak_kind,
-                "l2": {"peak_measured_read_gbs": round(l2_gbs, 1), "frac": round(achieved / l2_gbs, 4)}}
+    launch_s = ms_dom / max(1, n_dom) * 1e-3
+    achieved = ref_bytes[dom] / max(1, launches_frame) / launch_s / 1e9
+    own = own_bytes[dom] / max(1, launches_frame) / launch_s / 1e9
+    hbm = peaks.get("hbm_gbs")
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                "frac": round(achieved / hbm, 4), "traffic": TRAFFIC.get((dom, args.layout)),
+                "kernel": KERNELS.get((dom, args.layout), dom), "peak_source": peak_kind,
+                "work_unit": "reference threaded walk: 48 B per interior record, 80 B per leaf record",
+                "l2": {"peak_measured_read_gbs": round(l2_gbs, 1), "frac": round(achieved / l2_gbs, 4)},
+                "own_layout": {"achieved": round(own, 1), "l2_frac": round(own / l2_gbs, 4),
+                               "hbm_frac": round(own / hbm, 4)},
+                "visits_per_frame": {"reference": list(visits["threaded"]), args.layout: list(visits[args.layout])}}
 
     cpu_base = None
     if rank == 0 and not args.no_cpu_baseline:

@@ -569,10 +569,12 @@ struct kgr_attachment {
 	DevBuf<uint16_t> q_feat, r_feat, b_x;
 	DevBuf<float4> q_le, q_out, r_beta, r_lb, r_le, b_t;
 	DevBuf<uint32_t> b_count;
-	DevBuf<float4> t_f4[14];
-	DevBuf<uint32_t> t_queues[3], t_counters;
-	uint32_t t_capacity = 0;
-	int record_depths = 0;
+	DevBuf<float4> t_L; /* final radiance of each training path */
+	/* training runs on a side stream, overlapped with the frame:
+	 * fork -> (side) training paths, targets, gradient -> wait for the
+	 * frame's inference -> Adam -> join */
+	cudaStream_t side = nullptr;
+	cudaEvent_t ev_fork = nullptr, ev_infer = nullptr, ev_train = nullptr;
 
 	kgr_render_stats stats = {0, 0, 0, 0, 0};
 	uint32_t last_paths = 0;
@@ -581,15 +583,19 @@ struct kgr_attachment {
 	/* per-launch timing: one event after every launch, tagged by stage */
 	std::vector<cudaEvent_t> event_pool;
 	std::vector<int> event_kinds; /* kind of the launch that ends at event i; -1 = start */
+	std::vector<int> event_prev;  /* the event a span ends after: i - 1 unless given */
 	double stage_ms[STAGE_COUNT] = {0};
 	uint32_t stage_launches[STAGE_COUNT] = {0};
 	DevBuf<unsigned long long> visits;
 
 	bool profiling() const { return opt_int("profile", 0) != 0; }
-	void mark(int kind, cudaStream_t st)
+	/* Record an event on `st` ending a span of stage `kind` (-1: a start)
+	 * that began at event `prev` (default: the previous event, which must
+	 * then be on the same stream).  Returns the event's index. */
+	int mark(int kind, cudaStream_t st, int prev = -1)
 	{
 		if (!profiling())
-			return;
+			return -1;
 		size_t i = event_kinds.size();
 		if (i == event_pool.size()) {
 			cudaEvent_t e;
@@ -598,23 +604,28 @@ struct kgr_attachment {
 		}
 		KGR_CUDA(cudaEventRecord(event_pool[i], st));
 		event_kinds.push_back(kind);
+		event_prev.push_back(prev);
+		return (int)i;
 	}
-	/* fold recorded events into per-stage totals (synchronises on the last event) */
+	/* fold recorded events into per-stage totals (waits for every event) */
 	void collect_times()
 	{
 		if (event_kinds.empty())
 			return;
-		KGR_CUDA(cudaEventSynchronize(event_pool[event_kinds.size() - 1]));
+		for (size_t i = 0; i < event_kinds.size(); i++)
+			KGR_CUDA(cudaEventSynchronize(event_pool[i]));
 		for (size_t i = 1; i < event_kinds.size(); i++) {
 			int k = event_kinds[i];
 			if (k < 0)
 				continue;
+			int j = event_prev[i] >= 0 ? event_prev[i] : (int)i - 1;
 			float ms = 0.0f;
-			KGR_CUDA(cudaEventElapsedTime(&ms, event_pool[i - 1], event_pool[i]));
+			KGR_CUDA(cudaEventElapsedTime(&ms, event_pool[j], event_pool[i]));
 			stage_ms[k] += ms;
 			stage_launches[k]++;
 		}
 		event_kinds.clear();
+		event_prev.clear();
 	}
 
 	int opt_int(const char *k, int def) const
@@ -670,6 +681,8 @@ struct kgr_attachment {
 
 	void release_all()
 	{
+		if (side)
+			cudaStreamSynchronize(side);
 		for (auto &b : f4)
 			b.release();
 		for (auto &q : queues)
@@ -693,38 +706,19 @@ struct kgr_attachment {
 		for (DevBuf<float4> *b : {&q_le, &q_out, &r_beta, &r_lb, &r_le, &b_t})
 			b->release();
 		b_count.release();
-		for (auto &b : t_f4)
-			b.release();
-		for (auto &q : t_queues)
-			q.release();
-		t_counters.release();
-		t_capacity = 0;
+		t_L.release();
 		capacity = 0;
 	}
 
 	/* path buffers of the cache's training paths */
-	PathBuffers train_buffers(uint32_t paths)
+	void ensure_side_stream()
 	{
-		if (paths > t_capacity) {
-			for (auto &b : t_f4)
-				b.alloc(paths);
-			for (auto &q : t_queues)
-				q.alloc(paths);
-			t_counters.alloc(CNT_COUNT);
-			t_capacity = paths;
-		}
-		PathBuffers pb;
-		float4 **fields[14] = {&pb.ray_o, &pb.ray_d, &pb.beta, &pb.L, &pb.seed, &pb.hit, &pb.sh_o, &pb.sh_d,
-			&pb.pend_c, &pb.pend_e, &pb.pend_b, &pb.aov_n, &pb.aov_a, &pb.aov_p};
-		for (int k = 0; k < 14; k++)
-			*fields[k] = t_f4[k].ptr;
-		pb.queue[0] = t_queues[0].ptr;
-		pb.queue[1] = t_queues[1].ptr;
-		pb.shadow_queue = t_queues[2].ptr;
-		pb.counters = t_counters.ptr;
-		pb.visits = nullptr;
-		pb.capacity = t_capacity;
-		return pb;
+		if (side)
+			return;
+		KGR_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+		KGR_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+		KGR_CUDA(cudaEventCreateWithFlags(&ev_infer, cudaEventDisableTiming));
+		KGR_CUDA(cudaEventCreateWithFlags(&ev_train, cudaEventDisableTiming));
 	}
 
 	~kgr_attachment()
@@ -732,6 +726,11 @@ struct kgr_attachment {
 		release_all();
 		if (cache_mlp)
 			kgr_mlp_destroy(cache_mlp);
+		for (cudaEvent_t e : {ev_fork, ev_infer, ev_train})
+			if (e)
+				cudaEventDestroy(e);
+		if (side)
+			cudaStreamDestroy(side);
 		visits.release();
 		if (ev_start)
 			cudaEventDestroy(ev_start);
@@ -986,6 +985,51 @@ void render_pt_cached(kgr_attachment *att, const kgr_launch_info *info, const kg
 	att->q_le.alloc(att->capacity);
 	att->q_out.alloc(att->capacity);
 	uint32_t launches = 0;
+	const bool train = att->opt_int("cache_train", 1) != 0;
+	float lr = 1e-3f;
+	{
+		auto it = att->options.find("cache_lr");
+		if (it != att->options.end())
+			if (auto f = std::get_if<float>(&it->second))
+				lr = *f;
+	}
+
+	/* training, forked onto the side stream: paths, targets, gradient with
+	 * the weights this frame's inference also reads */
+	int train_start = -1;
+	if (train) {
+		uint32_t tpaths = (uint32_t)att->opt_int("cache_train_paths", 16384);
+		KGR_REQUIRE(tpaths >= 128 && tpaths <= (1u << 22), KGR_ERR_INVALID_ARGUMENT, "cache_train_paths out of range");
+		const uint32_t cap = 1u << 16;
+		int depths = fp.max_depth + 1;
+		size_t slots = (size_t)tpaths * depths;
+		att->ensure_side_stream();
+		att->t_L.alloc(tpaths);
+		att->r_feat.alloc(slots * 64);
+		att->r_beta.alloc(slots);
+		att->r_lb.alloc(slots);
+		att->r_le.alloc(slots);
+		att->b_x.alloc((size_t)cap * 64);
+		att->b_t.alloc(cap);
+		att->b_count.alloc(1);
+		cudaStream_t side = att->side;
+		KGR_CUDA(cudaEventRecord(att->ev_fork, st));
+		KGR_CUDA(cudaStreamWaitEvent(side, att->ev_fork, 0));
+		train_start = att->mark(-1, side);
+		KGR_CUDA(cudaMemsetAsync(att->r_le.ptr, 0, slots * sizeof(float4), side));
+		CacheRecords rec = {att->r_feat.ptr, att->r_beta.ptr, att->r_lb.ptr, att->r_le.ptr, depths};
+		PathBuffers tb = {};
+		tb.L = att->t_L.ptr;
+		tb.capacity = tpaths;
+		FrameParams tf = fp;
+		tf.spp = 1;
+		tf.paths = tpaths;
+		cache_train_paths(s, tb, tf, tpaths, cp, rec, side);
+		cache_targets(tb, tpaths, rec, dtype, att->b_x.ptr, att->b_t.ptr, att->b_count.ptr, cap, side);
+		mlp_gradients(mp, att->b_x.ptr, att->b_t.ptr, cap, att->cache_mlp->grad.ptr, att->cache_mlp->loss.ptr, side,
+			att->b_count.ptr);
+		launches += 4;
+	}
 
 	/* render: primary vertex, first bounce, cache */
 	att->mark(-1, st);
@@ -1003,56 +1047,24 @@ void render_pt_cached(kgr_attachment *att, const kgr_launch_info *info, const kg
 	att->mark(STAGE_TRACE_CLOSEST, st);
 	cache_query(s, pb, 1, cp, att->q_feat.ptr, att->q_le.ptr, st);
 	mlp_infer(mp, att->q_feat.ptr, att->capacity, att->q_out.ptr, st, pb.counters + CNT_Q1);
+	if (train)
+		KGR_CUDA(cudaEventRecord(att->ev_infer, st));
 	cache_apply(pb, 1, att->q_out.ptr, att->q_le.ptr, st);
 	att->mark(STAGE_CACHE_INFER, st);
 	pt_accumulate(pb, fp, out, st);
 	att->mark(STAGE_ACCUMULATE, st);
 	launches += 10;
 
-	/* training paths */
-	if (att->opt_int("cache_train", 1)) {
-		uint32_t tpaths = (uint32_t)att->opt_int("cache_train_paths", 16384);
-		KGR_REQUIRE(tpaths >= 128 && tpaths <= (1u << 22), KGR_ERR_INVALID_ARGUMENT, "cache_train_paths out of range");
-		const uint32_t cap = 1u << 16;
-		PathBuffers tb = att->train_buffers(tpaths);
-		int depths = fp.max_depth + 1;
-		size_t slots = (size_t)tpaths * depths;
-		att->r_feat.alloc(slots * 64);
-		att->r_beta.alloc(slots);
-		att->r_lb.alloc(slots);
-		att->r_le.alloc(slots);
-		att->b_x.alloc((size_t)cap * 64);
-		att->b_t.alloc(cap);
-		att->b_count.alloc(1);
-		KGR_CUDA(cudaMemsetAsync(att->r_le.ptr, 0, slots * sizeof(float4), st));
-		CacheRecords rec = {att->r_feat.ptr, att->r_beta.ptr, att->r_lb.ptr, att->r_le.ptr, depths};
-		FrameParams tf = fp;
-		tf.spp = 1;
-		tf.paths = tpaths;
-		cache_train_generate(tb, tf, tpaths, st);
-		for (int d = 0; d <= fp.max_depth; d++) {
-			int q = d & 1;
-			if (d > 0)
-				reset_counters(tb, (1 << (q ^ 1)) | (1 << CNT_SHADOW), st);
-			pt_trace_closest(s, tb, q, fp.layout, st);
-			if (d >= 1)
-				cache_record(s, tb, q, d, cp, rec, st);
-			pt_shade(s, tb, tf, d, q, st);
-			pt_shadow_resolve(s, tb, fp.layout, st);
-			launches += d >= 1 ? 4 : 3;
-		}
-		cache_targets(tb, tpaths, rec, dtype, att->b_x.ptr, att->b_t.ptr, att->b_count.ptr, cap, st);
-		mlp_gradients(mp, att->b_x.ptr, att->b_t.ptr, cap, att->cache_mlp->grad.ptr, att->cache_mlp->loss.ptr, st,
-			att->b_count.ptr);
+	/* Adam once this frame's inference is done, then join */
+	if (train) {
+		cudaStream_t side = att->side;
+		KGR_CUDA(cudaStreamWaitEvent(side, att->ev_infer, 0));
 		att->cache_mlp->step++;
-		float lr = 1e-3f;
-		auto it = att->options.find("cache_lr");
-		if (it != att->options.end())
-			if (auto f = std::get_if<float>(&it->second))
-				lr = *f;
-		mlp_adam(mp, att->cache_mlp->grad.ptr, lr, att->cache_mlp->step, st);
-		att->mark(STAGE_CACHE_TRAIN, st);
-		launches += 4;
+		mlp_adam(mp, att->cache_mlp->grad.ptr, lr, att->cache_mlp->step, side);
+		att->mark(STAGE_CACHE_TRAIN, side, train_start);
+		KGR_CUDA(cudaEventRecord(att->ev_train, side));
+		KGR_CUDA(cudaStreamWaitEvent(st, att->ev_train, 0));
+		launches += 1;
 	}
 	att->stats.kernel_launches = launches;
 	att->stats.camera_rays = fp.paths;

@@ -26,9 +26,10 @@ struct CacheRecords {
 void cache_query(const DeviceScene &s, const PathBuffers &pb, int q, const CacheParams &cp, void *feat,
 		float4 *le, cudaStream_t st);
 void cache_apply(const PathBuffers &pb, int q, const float4 *out, const float4 *le, cudaStream_t st);
-void cache_train_generate(const PathBuffers &pb, const FrameParams &fp, uint32_t paths, cudaStream_t st);
-void cache_record(const DeviceScene &s, const PathBuffers &pb, int q, int depth, const CacheParams &cp,
-		const CacheRecords &rec, cudaStream_t st);
+/* Trace `paths` training paths to the full depth (one thread each), filling
+ * `rec` and tb.L (final radiance); rec.le must be zero on entry. */
+void cache_train_paths(const DeviceScene &s, const PathBuffers &tb, const FrameParams &fp, uint32_t paths,
+		const CacheParams &cp, const CacheRecords &rec, cudaStream_t st);
 void cache_targets(const PathBuffers &pb, uint32_t paths, const CacheRecords &rec, int dtype, void *xb, float4 *tb,
 		uint32_t *count, uint32_t cap, cudaStream_t st);
 

@@ -18,6 +18,8 @@ struct MlpParams {
 	int dtype; /* KGR_MLP_BF16 or KGR_MLP_FP16 */
 	float *master, *m, *v;
 	void *wn, *wt;
+	float *partial;     /* per-block gradient slices [partial_blocks][6][64][64] */
+	int partial_blocks;
 };
 
 /* out[i] = {r, g, b, 0} for the n rows of x ([n][64] half precision); with
@@ -25,7 +27,8 @@ struct MlpParams {
 void mlp_infer(const MlpParams &mp, const void *x, uint32_t n, float4 *out, cudaStream_t st,
 		const uint32_t *n_dev = nullptr);
 /* grad (FP32, [6][64][64]) = d loss / d W over n rows; loss = sum of the
- * relative L2 terms (not divided by n). */
+ * relative L2 terms (not divided by n).  Uses mp.partial as scratch; the
+ * result does not depend on block scheduling. */
 void mlp_gradients(const MlpParams &mp, const void *x, const float4 *target, uint32_t n, float *grad, float *loss,
 		cudaStream_t st, const uint32_t *n_dev = nullptr);
 /* One Adam step (lr, bias correction for `step`); step <= 0 only refreshes
@@ -40,11 +43,12 @@ struct kgr_mlp {
 	int device = 0;
 	int dtype = 0;
 	int step = 0;
-	kgr::DevBuf<float> master, m, v, grad, loss;
+	int partial_blocks = 0;
+	kgr::DevBuf<float> master, m, v, grad, loss, partial;
 	kgr::DevBuf<uint16_t> wn, wt;
 	kgr::MlpParams params()
 	{
-		return kgr::MlpParams{dtype, master.ptr, m.ptr, v.ptr, wn.ptr, wt.ptr};
+		return kgr::MlpParams{dtype, master.ptr, m.ptr, v.ptr, wn.ptr, wt.ptr, partial.ptr, partial_blocks};
 	}
 };
 

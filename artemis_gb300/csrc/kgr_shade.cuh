@@ -1,0 +1,87 @@
+/*
+ * kgr_shade.cuh -- one path vertex of the path tracer: next-event estimation
+ * against the triangle lights and the BSDF continuation with Russian
+ * roulette.  The wavefront shade kernel (pt.cu) and the per-thread training
+ * paths of the radiance cache (cache.cu) share this code, so both estimate
+ * the same radiance with the same operations in the same order.
+ */
+#ifndef KGR_SHADE_CUH_
+#define KGR_SHADE_CUH_
+
+#include "kgr_device.cuh"
+#include "kgr_wavefront.h"
+
+namespace kgr {
+
+/* Ld (amadeus_common.cuh:256-286) with Ld_light (lighting.cuh:149-174) and
+ * the continuation (eval, brdf.cuh:573-589; Russian roulette as in
+ * naive_path_tracer.cu:294-303).  `seed` advances in place.  At the last
+ * depth the continuation is sampled only when final_seed is set (ReSTIR
+ * keeps that seed).  Results go to `out` as they are produced:
+ *   out.vertex(x, n)      offset hit point and shading normal
+ *   out.emit(add)         beta * emission (scene without lights)
+ *   out.nee(c, e, b, o, d) NEE record {contribution, pdf}, emission, beta,
+ *                         shadow ray origin and {direction, tmax}
+ *   out.next(x, wi, beta) the path continues from x along wi */
+template <class Sink>
+__device__ __forceinline__ void shade_surface(const DeviceScene &s, const FrameParams &fp, int depth, int final_seed,
+		SurfaceHit sh, f3 beta, f3 &seed, Sink &out)
+{
+	f3 n3 = sh.n;
+	float sgn = sh.mat.type == KGR_SHADING_TRANSMISSION ? -1.0f : 1.0f;
+	sh.x = sh.x + sgn * n3 * KGR_OFFSET_EPS;
+	out.vertex(sh.x, n3);
+	if (s.light_count == 0) {
+		f3 direct = sh.mat.emission + mk(0.0f);
+		out.emit(beta * direct);
+	} else {
+		int total_count = (int)s.light_count;
+		unsigned int li = (unsigned int)(rand_uniform(seed) * total_count);
+		float pdf = 1.0f / total_count;
+		TriLight light = load_light(s.lights, li < s.light_count ? li : s.light_count - 1);
+		float light_pdf = 1.0f / light.area();
+		f3 lpos = sample_area_light(light, seed);
+		f3 wi = normalize(lpos - sh.x);
+		float R = length(lpos - sh.x);
+		f3 f = brdf(sh, wi);
+		float ldot = fabsf(dot(light.normal(), wi));
+		float geometric = ldot * fabsf(dot(sh.n, wi)) / (R * R);
+		f3 contr = f * light.intensity * geometric;
+		pdf *= light_pdf;
+		out.nee(f4_of(contr, pdf), f4_of(sh.mat.emission, 0.0f), f4_of(beta, 0.0f), f4_of(sh.x, 0.0f),
+			f4_of(wi, R - KGR_SHADOW_EPS));
+	}
+	if (depth < fp.max_depth || final_seed) {
+		f3 wi;
+		float pdf = 0.0f;
+		f3 f = eval(sh, wi, pdf, seed);
+		if (pdf > 0) {
+			f3 T = f * fabsf(dot(wi, n3)) / pdf;
+			beta = beta * T;
+			bool alive = true;
+			if (fp.russian_roulette && depth >= fp.rr_start_depth) {
+				float qq = 1.0f - kmin(kmax(0.05f, beta.y), 1.0f);
+				float r = fract(seed.x);
+				if (r < qq)
+					alive = false;
+				else
+					beta = beta / (1.0f - qq);
+			}
+			if (alive && depth < fp.max_depth)
+				out.next(sh.x, wi, beta);
+		}
+	}
+}
+
+/* L += beta * (Le + Ld) once the shadow ray is resolved, in the order of
+ * the recursion (Ld = contribution / pdf, zero when occluded). */
+__device__ __forceinline__ float4 nee_add(float4 L, float4 c, float4 e, float4 be, bool occ)
+{
+	f3 contr = occ ? mk(0.0f) : mk(c.x, c.y, c.z);
+	f3 direct = mk(e.x, e.y, e.z) + contr / c.w;
+	return f4_of(mk(L.x, L.y, L.z) + mk(be.x, be.y, be.z) * direct, 0.0f);
+}
+
+} /* namespace kgr */
+
+#endif

@@ -20,10 +20,11 @@
  * fragments of the next layer's m16n8k16, so activations never leave the
  * registers.
  *
- * Training: one kernel runs forward and backward for tiles of 128 rows with
- * the activations of all layers in shared memory (184 KB per block); each
- * warp's weight-gradient contribution (an m16n8k16 over its 32 rows) is
- * added to the FP32 global gradient with atomics.  Loss: relative L2,
+ * Training: one kernel runs forward and backward for tiles of 64 rows with
+ * the activations of all layers in shared memory and the block's FP32
+ * weight gradient accumulated there too (213 KB per block, one block per
+ * SM); per-block gradients are summed in a fixed order by a second kernel,
+ * so training is deterministic.  Loss: relative L2,
  * sum_rows sum_c (y_c - t_c)^2 / (y_c^2 + 0.01) / rows, with y_c^2 in the
  * denominator treated as a constant (as in neural radiance caching).
  */
@@ -241,11 +242,40 @@ __device__ __forceinline__ uint32_t gather2(const T *p0, const T *p1)
 	return *reinterpret_cast<uint32_t *>(v);
 }
 
-#define TRAIN_ROWS 128
+#define TRAIN_ROWS 64 /* rows per tile: 4 warps x 16 */
 
+/* A fragments of one m16 tile: rows [r0, r0 + 16) of a row-major [rows][64]
+ * half array; rows at or past n read as zero. */
+template <class T>
+__device__ __forceinline__ void load_a_tile(const T *x, size_t r0, uint32_t n, int lane, uint32_t a[4][4])
+{
+	int g = lane >> 2, t = lane & 3;
+	size_t ra = r0 + g, rb = ra + 8;
+#pragma unroll
+	for (int kk = 0; kk < 4; kk++) {
+		int k = 16 * kk + 2 * t;
+		a[kk][0] = ra < n ? __ldg(reinterpret_cast<const uint32_t *>(x + ra * MLP_W + k)) : 0u;
+		a[kk][1] = rb < n ? __ldg(reinterpret_cast<const uint32_t *>(x + rb * MLP_W + k)) : 0u;
+		a[kk][2] = ra < n ? __ldg(reinterpret_cast<const uint32_t *>(x + ra * MLP_W + k + 8)) : 0u;
+		a[kk][3] = rb < n ? __ldg(reinterpret_cast<const uint32_t *>(x + rb * MLP_W + k + 8)) : 0u;
+	}
+}
+
+/* Forward and backward over tiles of 64 rows; the grid is persistent (at
+ * most one block per SM) and each block accumulates its weight gradient in
+ * shared memory (FP32, every element owned by one lane, so no atomics),
+ * then writes it to its own slice of `partial` ([gridDim.x][6][64][64]).
+ * reduce_partials sums the slices in block order, so the gradient does not
+ * depend on scheduling.
+ *
+ * Per tile: warp w runs the forward of rows [16w, 16w + 16) with the layer
+ * inputs kept in shared memory, writes the output delta of its rows, and in
+ * the backward computes for each layer the 16-row block [16w, 16w + 16) of
+ * dW = A^T delta over all 64 rows of the tile (an m16n8k16 chain with K =
+ * rows), then the delta of its own rows' layer input. */
 template <class T>
 __global__ void __launch_bounds__(128) mlp_train_kernel(const T *__restrict__ wt_g, const T *__restrict__ x,
-		const float4 *__restrict__ target, uint32_t n, float *__restrict__ grad, float *__restrict__ loss_sum,
+		const float4 *__restrict__ target, uint32_t n, float *__restrict__ partial, float *__restrict__ loss_sum,
 		const uint32_t *__restrict__ n_dev)
 {
 	if (n_dev) {
@@ -254,195 +284,198 @@ __global__ void __launch_bounds__(128) mlp_train_kernel(const T *__restrict__ wt
 	}
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	T *wt_s = reinterpret_cast<T *>(smem_raw);
-	T *act = wt_s + (size_t)MLP_LAYERS * MLP_W * MLP_STRIDE;             /* 6 x [128][72] */
-	T *dlt = act + (size_t)MLP_LAYERS * TRAIN_ROWS * MLP_STRIDE;          /* [128][72] */
+	T *act = wt_s + (size_t)MLP_LAYERS * MLP_W * MLP_STRIDE;             /* 6 x [64][72] */
+	T *dlt = act + (size_t)MLP_LAYERS * TRAIN_ROWS * MLP_STRIDE;          /* [64][72] */
+	float *gacc = reinterpret_cast<float *>(dlt + (size_t)TRAIN_ROWS * MLP_STRIDE); /* [6][64][64] */
 	stage_weights<T>(wt_g, wt_s, nullptr, nullptr);
+	for (int i = threadIdx.x; i < MLP_LAYERS * MLP_W * MLP_W / 4; i += blockDim.x)
+		reinterpret_cast<float4 *>(gacc)[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 	__syncthreads();
 	int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	int g = lane >> 2, t = lane & 3;
+	const int lr0 = 16 * warp; /* this warp's rows within the tile */
 	float lsum = 0.0f;
 	for (size_t base = (size_t)blockIdx.x * TRAIN_ROWS; base < n; base += (size_t)gridDim.x * TRAIN_ROWS) {
 		/* ---- forward, keeping every layer's input in shared memory ---- */
-		size_t r0 = base + 32 * warp;
-		int lr0 = 32 * warp; /* this warp's rows within the tile */
-		uint32_t a[2][4][4];
-		load_a_rows<T>(x, r0, n, lane, a);
+		uint32_t a[4][4];
+		load_a_tile<T>(x, base + lr0, n, lane, a);
 		for (int l = 0; l < MLP_LAYERS; l++) {
 			T *A = act + (size_t)l * TRAIN_ROWS * MLP_STRIDE;
 #pragma unroll
-			for (int mt = 0; mt < 2; mt++)
-#pragma unroll
-				for (int kk = 0; kk < 4; kk++) {
-					int ra = lr0 + 16 * mt + g, k = 16 * kk + 2 * t;
-					*reinterpret_cast<uint32_t *>(A + ra * MLP_STRIDE + k) = a[mt][kk][0];
-					*reinterpret_cast<uint32_t *>(A + (ra + 8) * MLP_STRIDE + k) = a[mt][kk][1];
-					*reinterpret_cast<uint32_t *>(A + ra * MLP_STRIDE + k + 8) = a[mt][kk][2];
-					*reinterpret_cast<uint32_t *>(A + (ra + 8) * MLP_STRIDE + k + 8) = a[mt][kk][3];
-				}
+			for (int kk = 0; kk < 4; kk++) {
+				int ra = lr0 + g, k = 16 * kk + 2 * t;
+				*reinterpret_cast<uint32_t *>(A + ra * MLP_STRIDE + k) = a[kk][0];
+				*reinterpret_cast<uint32_t *>(A + (ra + 8) * MLP_STRIDE + k) = a[kk][1];
+				*reinterpret_cast<uint32_t *>(A + ra * MLP_STRIDE + k + 8) = a[kk][2];
+				*reinterpret_cast<uint32_t *>(A + (ra + 8) * MLP_STRIDE + k + 8) = a[kk][3];
+			}
 			if (l == MLP_LAYERS - 1)
 				break;
 			const T *w = wt_s + (size_t)l * MLP_W * MLP_STRIDE;
-			float acc[2][8][4];
+			float acc[8][4];
 #pragma unroll
-			for (int mt = 0; mt < 2; mt++)
+			for (int j = 0; j < 8; j++)
 #pragma unroll
-				for (int j = 0; j < 8; j++)
-#pragma unroll
-					for (int r = 0; r < 4; r++)
-						acc[mt][j][r] = 0.0f;
+				for (int r = 0; r < 4; r++)
+					acc[j][r] = 0.0f;
 #pragma unroll
 			for (int kk = 0; kk < 4; kk++)
 #pragma unroll
 				for (int j = 0; j < 8; j++) {
 					uint32_t b[2];
 					load_b(w, 8 * j, 16 * kk, lane, b);
-					HalfOps<T>::mma(acc[0][j], a[0][kk], b);
-					HalfOps<T>::mma(acc[1][j], a[1][kk], b);
+					HalfOps<T>::mma(acc[j], a[kk], b);
 				}
 #pragma unroll
-			for (int mt = 0; mt < 2; mt++)
-#pragma unroll
-				for (int kk = 0; kk < 4; kk++) {
-					float *c0 = acc[mt][2 * kk], *c1 = acc[mt][2 * kk + 1];
-					a[mt][kk][0] = HalfOps<T>::pack(fmaxf(c0[0], 0.0f), fmaxf(c0[1], 0.0f));
-					a[mt][kk][1] = HalfOps<T>::pack(fmaxf(c0[2], 0.0f), fmaxf(c0[3], 0.0f));
-					a[mt][kk][2] = HalfOps<T>::pack(fmaxf(c1[0], 0.0f), fmaxf(c1[1], 0.0f));
-					a[mt][kk][3] = HalfOps<T>::pack(fmaxf(c1[2], 0.0f), fmaxf(c1[3], 0.0f));
-				}
+			for (int kk = 0; kk < 4; kk++) {
+				float *c0 = acc[2 * kk], *c1 = acc[2 * kk + 1];
+				a[kk][0] = HalfOps<T>::pack(fmaxf(c0[0], 0.0f), fmaxf(c0[1], 0.0f));
+				a[kk][1] = HalfOps<T>::pack(fmaxf(c0[2], 0.0f), fmaxf(c0[3], 0.0f));
+				a[kk][2] = HalfOps<T>::pack(fmaxf(c1[0], 0.0f), fmaxf(c1[1], 0.0f));
+				a[kk][3] = HalfOps<T>::pack(fmaxf(c1[2], 0.0f), fmaxf(c1[3], 0.0f));
+			}
 		}
 		/* output layer */
-		float o[2][2][4];
+		float o[2][4];
 		{
 			const T *w = wt_s + (size_t)(MLP_LAYERS - 1) * MLP_W * MLP_STRIDE;
 #pragma unroll
-			for (int mt = 0; mt < 2; mt++)
+			for (int j = 0; j < 2; j++)
 #pragma unroll
-				for (int j = 0; j < 2; j++)
-#pragma unroll
-					for (int r = 0; r < 4; r++)
-						o[mt][j][r] = 0.0f;
+				for (int r = 0; r < 4; r++)
+					o[j][r] = 0.0f;
 #pragma unroll
 			for (int kk = 0; kk < 4; kk++)
 #pragma unroll
 				for (int j = 0; j < 2; j++) {
 					uint32_t b[2];
 					load_b(w, 8 * j, 16 * kk, lane, b);
-					HalfOps<T>::mma(o[0][j], a[0][kk], b);
-					HalfOps<T>::mma(o[1][j], a[1][kk], b);
+					HalfOps<T>::mma(o[j], a[kk], b);
 				}
 		}
 		/* loss and output delta (columns 0..15, only 0..2 non-zero) */
 #pragma unroll
-		for (int mt = 0; mt < 2; mt++)
+		for (int half = 0; half < 2; half++) {
+			int lr = lr0 + g + 8 * half;
+			size_t gr = base + lr;
+			float4 tg = gr < n ? target[gr] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+			float tv[3] = {tg.x, tg.y, tg.z};
 #pragma unroll
-			for (int half = 0; half < 2; half++) {
-				int lr = lr0 + 16 * mt + g + 8 * half;
-				size_t gr = base + lr;
-				float4 tg = gr < n ? target[gr] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-				float tv[3] = {tg.x, tg.y, tg.z};
+			for (int j = 0; j < 2; j++)
 #pragma unroll
-				for (int j = 0; j < 2; j++)
-#pragma unroll
-					for (int e = 0; e < 2; e++) {
-						int col = 8 * j + 2 * t + e;
-						float y = o[mt][j][2 * half + e];
-						float d = 0.0f;
-						if (col < 3 && gr < n) {
-							float diff = y - tv[col];
-							float den = y * y + 0.01f;
-							lsum += diff * diff / den;
-							d = 2.0f * diff / den / (float)n;
-						}
-						dlt[lr * MLP_STRIDE + col] = HalfOps<T>::from_float(d);
+				for (int e = 0; e < 2; e++) {
+					int col = 8 * j + 2 * t + e;
+					float y = o[j][2 * half + e];
+					float d = 0.0f;
+					if (col < 3 && gr < n) {
+						float diff = y - tv[col];
+						float den = y * y + 0.01f;
+						lsum += diff * diff / den;
+						d = 2.0f * diff / den / (float)n;
 					}
-			}
-		__syncwarp();
+					dlt[lr * MLP_STRIDE + col] = HalfOps<T>::from_float(d);
+				}
+		}
+		__syncthreads();
 		/* ---- backward ---- */
 		int ncols = MLP_OUT_PAD;
 		for (int l = MLP_LAYERS - 1; l >= 0; l--) {
 			const T *A = act + (size_t)l * TRAIN_ROWS * MLP_STRIDE; /* layer input [rows][64] */
-			/* dW[i][j] += sum over this warp's 32 rows of A[r][i] dlt[r][j]:
-			 * an MMA with M = 64 (i), N = ncols (j), K = 32 (rows) */
-			float *gl = grad + (size_t)l * MLP_W * MLP_W;
-			for (int mi = 0; mi < 4; mi++) {
-				for (int nj = 0; nj < ncols / 8; nj++) {
-					float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+			/* dW[i][j] += sum over the tile's rows r of A[r][i] dlt[r][j]
+			 * for i in this warp's block: M = 16 (i), N = ncols, K = 64 */
+			float *gl = gacc + (size_t)l * MLP_W * MLP_W;
+			const int i0 = lr0 + g; /* weight row (layer input index) */
+			for (int nj = 0; nj < ncols / 8; nj++) {
+				float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+				const int jn = 8 * nj + g;
 #pragma unroll
-					for (int kk = 0; kk < 2; kk++) {
-						int rr = lr0 + 16 * kk + 2 * t;
-						int i0 = 16 * mi + g, jn = 8 * nj + g;
-						uint32_t af[4], bf[2];
-						af[0] = gather2(A + rr * MLP_STRIDE + i0, A + (rr + 1) * MLP_STRIDE + i0);
-						af[1] = gather2(A + rr * MLP_STRIDE + i0 + 8, A + (rr + 1) * MLP_STRIDE + i0 + 8);
-						af[2] = gather2(A + (rr + 8) * MLP_STRIDE + i0, A + (rr + 9) * MLP_STRIDE + i0);
-						af[3] = gather2(A + (rr + 8) * MLP_STRIDE + i0 + 8, A + (rr + 9) * MLP_STRIDE + i0 + 8);
-						bf[0] = gather2(dlt + rr * MLP_STRIDE + jn, dlt + (rr + 1) * MLP_STRIDE + jn);
-						bf[1] = gather2(dlt + (rr + 8) * MLP_STRIDE + jn, dlt + (rr + 9) * MLP_STRIDE + jn);
-						HalfOps<T>::mma(c, af, bf);
-					}
-					int i = 16 * mi + g, j = 8 * nj + 2 * t;
-					atomicAdd(&gl[i * MLP_W + j], c[0]);
-					atomicAdd(&gl[i * MLP_W + j + 1], c[1]);
-					atomicAdd(&gl[(i + 8) * MLP_W + j], c[2]);
-					atomicAdd(&gl[(i + 8) * MLP_W + j + 1], c[3]);
+				for (int kk = 0; kk < TRAIN_ROWS / 16; kk++) {
+					int rr = 16 * kk + 2 * t;
+					uint32_t af[4], bf[2];
+					af[0] = gather2(A + rr * MLP_STRIDE + i0, A + (rr + 1) * MLP_STRIDE + i0);
+					af[1] = gather2(A + rr * MLP_STRIDE + i0 + 8, A + (rr + 1) * MLP_STRIDE + i0 + 8);
+					af[2] = gather2(A + (rr + 8) * MLP_STRIDE + i0, A + (rr + 9) * MLP_STRIDE + i0);
+					af[3] = gather2(A + (rr + 8) * MLP_STRIDE + i0 + 8, A + (rr + 9) * MLP_STRIDE + i0 + 8);
+					bf[0] = gather2(dlt + rr * MLP_STRIDE + jn, dlt + (rr + 1) * MLP_STRIDE + jn);
+					bf[1] = gather2(dlt + (rr + 8) * MLP_STRIDE + jn, dlt + (rr + 9) * MLP_STRIDE + jn);
+					HalfOps<T>::mma(c, af, bf);
 				}
+				int j = 8 * nj + 2 * t;
+				float2 *p0 = reinterpret_cast<float2 *>(gl + i0 * MLP_W + j);
+				float2 *p1 = reinterpret_cast<float2 *>(gl + (i0 + 8) * MLP_W + j);
+				float2 v0 = *p0, v1 = *p1;
+				v0.x += c[0];
+				v0.y += c[1];
+				v1.x += c[2];
+				v1.y += c[3];
+				*p0 = v0;
+				*p1 = v1;
 			}
 			if (l == 0)
 				break;
-			/* delta of the layer input: (dlt W^T) * relu'(A), K = ncols.
-			 * B[k = out][n = in] = W[in][out] = wt[out][in], gathered. */
+			/* delta of this warp's rows of the layer input: (dlt W^T) *
+			 * relu'(A), K = ncols; B[k = out][n = in] = wt[out][in] */
 			const T *w = wt_s + (size_t)l * MLP_W * MLP_STRIDE;
-			float acc[2][8][4];
+			float acc[8][4];
 #pragma unroll
-			for (int mt = 0; mt < 2; mt++)
+			for (int j = 0; j < 8; j++)
 #pragma unroll
-				for (int j = 0; j < 8; j++)
-#pragma unroll
-					for (int r = 0; r < 4; r++)
-						acc[mt][j][r] = 0.0f;
+				for (int r = 0; r < 4; r++)
+					acc[j][r] = 0.0f;
 			for (int kk = 0; kk < ncols / 16; kk++) {
-				uint32_t af[2][4];
-#pragma unroll
-				for (int mt = 0; mt < 2; mt++) {
-					int ra = lr0 + 16 * mt + g, k = 16 * kk + 2 * t;
-					af[mt][0] = *reinterpret_cast<const uint32_t *>(dlt + ra * MLP_STRIDE + k);
-					af[mt][1] = *reinterpret_cast<const uint32_t *>(dlt + (ra + 8) * MLP_STRIDE + k);
-					af[mt][2] = *reinterpret_cast<const uint32_t *>(dlt + ra * MLP_STRIDE + k + 8);
-					af[mt][3] = *reinterpret_cast<const uint32_t *>(dlt + (ra + 8) * MLP_STRIDE + k + 8);
-				}
+				uint32_t af[4];
+				int ra = lr0 + g, k = 16 * kk + 2 * t;
+				af[0] = *reinterpret_cast<const uint32_t *>(dlt + ra * MLP_STRIDE + k);
+				af[1] = *reinterpret_cast<const uint32_t *>(dlt + (ra + 8) * MLP_STRIDE + k);
+				af[2] = *reinterpret_cast<const uint32_t *>(dlt + ra * MLP_STRIDE + k + 8);
+				af[3] = *reinterpret_cast<const uint32_t *>(dlt + (ra + 8) * MLP_STRIDE + k + 8);
 #pragma unroll
 				for (int j = 0; j < 8; j++) {
-					int nn = 8 * j + g, k = 16 * kk + 2 * t;
+					int nn = 8 * j + g;
 					uint32_t b[2];
 					b[0] = gather2(w + k * MLP_STRIDE + nn, w + (k + 1) * MLP_STRIDE + nn);
 					b[1] = gather2(w + (k + 8) * MLP_STRIDE + nn, w + (k + 9) * MLP_STRIDE + nn);
-					HalfOps<T>::mma(acc[0][j], af[0], b);
-					HalfOps<T>::mma(acc[1][j], af[1], b);
+					HalfOps<T>::mma(acc[j], af, b);
 				}
 			}
-			__syncwarp();
+			/* every warp has read the whole delta tile for dW */
+			__syncthreads();
 #pragma unroll
-			for (int mt = 0; mt < 2; mt++)
+			for (int j = 0; j < 8; j++) {
+				int c = 8 * j + 2 * t;
 #pragma unroll
-				for (int j = 0; j < 8; j++) {
-					int ra = lr0 + 16 * mt + g, c = 8 * j + 2 * t;
-#pragma unroll
-					for (int e = 0; e < 4; e++) {
-						int rr = ra + (e >> 1) * 8, cc = c + (e & 1);
-						float av = HalfOps<T>::to_float(A[rr * MLP_STRIDE + cc]);
-						float d = av > 0.0f ? acc[mt][j][e] : 0.0f;
-						dlt[rr * MLP_STRIDE + cc] = HalfOps<T>::from_float(d);
-					}
+				for (int e = 0; e < 4; e++) {
+					int rr = lr0 + g + (e >> 1) * 8, cc = c + (e & 1);
+					float av = HalfOps<T>::to_float(A[rr * MLP_STRIDE + cc]);
+					float d = av > 0.0f ? acc[j][e] : 0.0f;
+					dlt[rr * MLP_STRIDE + cc] = HalfOps<T>::from_float(d);
 				}
-			__syncwarp();
+			}
+			__syncthreads();
 			ncols = MLP_W;
 		}
-		__syncwarp();
+		/* the next tile overwrites act and dlt */
+		__syncthreads();
 	}
+	float *dst = partial + (size_t)blockIdx.x * MLP_LAYERS * MLP_W * MLP_W;
+	for (int i = threadIdx.x; i < MLP_LAYERS * MLP_W * MLP_W / 4; i += blockDim.x)
+		reinterpret_cast<float4 *>(dst)[i] = reinterpret_cast<const float4 *>(gacc)[i];
 	for (int off = 16; off > 0; off >>= 1)
 		lsum += __shfl_down_sync(0xffffffffu, lsum, off);
 	if (lane == 0)
 		atomicAdd(loss_sum, lsum);
+}
+
+/* grad[k] = sum over blocks b (in order) of partial[b][k]. */
+__global__ void reduce_partials_kernel(const float *__restrict__ partial, int blocks, float *__restrict__ grad)
+{
+	int k = blockIdx.x * blockDim.x + threadIdx.x;
+	if (k >= MLP_LAYERS * MLP_W * MLP_W)
+		return;
+	float s = 0.0f;
+	for (int b = 0; b < blocks; b++)
+		s += partial[(size_t)b * MLP_LAYERS * MLP_W * MLP_W + k];
+	grad[k] = s;
 }
 
 /* Adam on the FP32 master weights, then the half-precision copies in both
@@ -484,7 +517,7 @@ size_t infer_smem() { return (size_t)MLP_LAYERS * MLP_W * MLP_STRIDE * 2; }
 size_t train_smem()
 {
 	return (size_t)MLP_LAYERS * MLP_W * MLP_STRIDE * 2 + (size_t)MLP_LAYERS * TRAIN_ROWS * MLP_STRIDE * 2
-		+ (size_t)TRAIN_ROWS * MLP_STRIDE * 2;
+		+ (size_t)TRAIN_ROWS * MLP_STRIDE * 2 + (size_t)MLP_LAYERS * MLP_W * MLP_W * 4;
 }
 
 template <class K>
@@ -518,26 +551,31 @@ void mlp_infer(const MlpParams &mp, const void *x, uint32_t n, float4 *out, cuda
 void mlp_gradients(const MlpParams &mp, const void *x, const float4 *target, uint32_t n, float *grad, float *loss,
 		cudaStream_t st, const uint32_t *n_dev)
 {
-	KGR_CUDA(cudaMemsetAsync(grad, 0, sizeof(float) * MLP_LAYERS * MLP_W * MLP_W, st));
 	KGR_CUDA(cudaMemsetAsync(loss, 0, sizeof(float), st));
-	if (n == 0)
+	if (n == 0) {
+		KGR_CUDA(cudaMemsetAsync(grad, 0, sizeof(float) * MLP_LAYERS * MLP_W * MLP_W, st));
 		return;
+	}
 	size_t sm = train_smem();
-	int grid = device_sm_count();
+	int grid = mp.partial_blocks;
 	long long tiles = ((long long)n + TRAIN_ROWS - 1) / TRAIN_ROWS;
 	if (tiles < grid)
 		grid = (int)tiles;
+	KGR_REQUIRE(grid >= 1 && mp.partial, KGR_ERR_INTERNAL, "MLP gradient scratch missing");
 	if (mp.dtype == KGR_MLP_BF16) {
 		static bool once = (set_smem(mlp_train_kernel<__nv_bfloat16>, sm), true);
 		(void)once;
 		mlp_train_kernel<__nv_bfloat16><<<grid, 128, sm, st>>>(static_cast<const __nv_bfloat16 *>(mp.wt),
-			static_cast<const __nv_bfloat16 *>(x), target, n, grad, loss, n_dev);
+			static_cast<const __nv_bfloat16 *>(x), target, n, mp.partial, loss, n_dev);
 	} else {
 		static bool once = (set_smem(mlp_train_kernel<__half>, sm), true);
 		(void)once;
 		mlp_train_kernel<__half><<<grid, 128, sm, st>>>(static_cast<const __half *>(mp.wt),
-			static_cast<const __half *>(x), target, n, grad, loss, n_dev);
+			static_cast<const __half *>(x), target, n, mp.partial, loss, n_dev);
 	}
+	KGR_CUDA(cudaGetLastError());
+	int np = MLP_LAYERS * MLP_W * MLP_W;
+	reduce_partials_kernel<<<(np + 255) / 256, 256, 0, st>>>(mp.partial, grid, grad);
 	KGR_CUDA(cudaGetLastError());
 }
 

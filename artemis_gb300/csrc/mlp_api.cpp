@@ -50,6 +50,8 @@ void alloc_all(kgr_mlp *m)
 	m->loss.alloc(1);
 	m->wn.alloc(KGR_MLP_PARAMS);
 	m->wt.alloc(KGR_MLP_PARAMS);
+	m->partial_blocks = kgr::device_sm_count();
+	m->partial.alloc((size_t)m->partial_blocks * KGR_MLP_PARAMS);
 	KGR_CUDA(cudaMemset(m->m.ptr, 0, KGR_MLP_PARAMS * 4));
 	KGR_CUDA(cudaMemset(m->v.ptr, 0, KGR_MLP_PARAMS * 4));
 	KGR_CUDA(cudaMemset(m->wn.ptr, 0, KGR_MLP_PARAMS * 2));

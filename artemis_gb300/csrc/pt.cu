@@ -9,6 +9,7 @@
  * roulette of source/optix/naive_path_tracer.cu:294-303 as an option.
  */
 #include "kgr_device.cuh"
+#include "kgr_shade.cuh"
 #include "kgr_wavefront.h"
 
 /* Resident 128-thread blocks per SM the traversal kernels are compiled for
@@ -121,6 +122,48 @@ __global__ void __launch_bounds__(128) trace_closest_kernel(DeviceScene s, PathB
 		add_visits(pb.visits, cnt);
 }
 
+/* Writes one shaded vertex into the path state of path p. */
+struct WavefrontSink {
+	const PathBuffers &pb;
+	uint32_t p;
+	int depth, gi_capture;
+	f3 albedo;
+	bool shadow = false, cont = false;
+	__device__ __forceinline__ void vertex(const f3 &x, const f3 &n)
+	{
+		if (depth == 0) {
+			pb.aov_n[p] = f4_of(n, 0.0f);
+			pb.aov_a[p] = f4_of(albedo, 0.0f);
+			pb.aov_p[p] = f4_of(x, 0.0f);
+		} else if (depth == 1 && gi_capture) {
+			/* the secondary vertex of a ReSTIR GI sample */
+			pb.aov_n[p] = f4_of(n, 0.0f);
+			pb.aov_p[p] = f4_of(x, 1.0f);
+		}
+	}
+	__device__ __forceinline__ void emit(const f3 &add)
+	{
+		float4 Lv = pb.L[p];
+		pb.L[p] = f4_of(mk(Lv.x, Lv.y, Lv.z) + add, 0.0f);
+	}
+	__device__ __forceinline__ void nee(float4 c, float4 e, float4 b, float4 o, float4 d)
+	{
+		pb.pend_c[p] = c;
+		pb.pend_e[p] = e;
+		pb.pend_b[p] = b;
+		pb.sh_o[p] = o;
+		pb.sh_d[p] = d;
+		shadow = true;
+	}
+	__device__ __forceinline__ void next(const f3 &x, const f3 &wi, const f3 &beta)
+	{
+		pb.ray_o[p] = f4_of(x, 0.0f);
+		pb.ray_d[p] = f4_of(wi, 1e16f);
+		pb.beta[p] = f4_of(beta, 0.0f);
+		cont = true;
+	}
+};
+
 /* One vertex of amadeus_path_tracer.cu:133-201 for every queued path. */
 __global__ void __launch_bounds__(128) shade_kernel(DeviceScene s, PathBuffers pb, FrameParams fp,
 		int depth, int q, int final_seed)
@@ -147,74 +190,13 @@ __global__ void __launch_bounds__(128) shade_kernel(DeviceScene s, PathBuffers p
 			f3 dir = mk(dv.x, dv.y, dv.z);
 			SurfaceHit sh;
 			if (h.prim >= 0 && surface(s, h, dir, sh)) {
-				f3 n3 = sh.n;
-				float sgn = sh.mat.type == KGR_SHADING_TRANSMISSION ? -1.0f : 1.0f;
-				sh.x = sh.x + sgn * n3 * KGR_OFFSET_EPS;
-				if (depth == 0) {
-					pb.aov_n[p] = f4_of(n3, 0.0f);
-					pb.aov_a[p] = f4_of(sh.mat.diffuse, 0.0f);
-					pb.aov_p[p] = f4_of(sh.x, 0.0f);
-				} else if (depth == 1 && fp.gi_capture) {
-					/* the secondary vertex of a ReSTIR GI sample */
-					pb.aov_n[p] = f4_of(n3, 0.0f);
-					pb.aov_p[p] = f4_of(sh.x, 1.0f);
-				}
+				WavefrontSink out{pb, p, depth, fp.gi_capture, sh.mat.diffuse};
 				float4 sv = pb.seed[p];
 				f3 seed = mk(sv.x, sv.y, sv.z);
 				float4 bv = pb.beta[p];
-				f3 beta = mk(bv.x, bv.y, bv.z);
-				/* Ld (amadeus_common.cuh:256-286) with Ld_light (lighting.cuh:
-				 * 149-174); visibility is resolved by the shadow stage */
-				if (s.light_count == 0) {
-					f3 direct = sh.mat.emission + mk(0.0f);
-					float4 Lv = pb.L[p];
-					pb.L[p] = f4_of(mk(Lv.x, Lv.y, Lv.z) + beta * direct, 0.0f);
-				} else {
-					int total_count = (int)s.light_count;
-					unsigned int li = (unsigned int)(rand_uniform(seed) * total_count);
-					float pdf = 1.0f / total_count;
-					TriLight light = load_light(s.lights, li < s.light_count ? li : s.light_count - 1);
-					float light_pdf = 1.0f / light.area();
-					f3 lpos = sample_area_light(light, seed);
-					f3 wi = normalize(lpos - sh.x);
-					float R = length(lpos - sh.x);
-					f3 f = brdf(sh, wi);
-					float ldot = fabsf(dot(light.normal(), wi));
-					float geometric = ldot * fabsf(dot(sh.n, wi)) / (R * R);
-					f3 contr = f * light.intensity * geometric;
-					pdf *= light_pdf;
-					pb.pend_c[p] = f4_of(contr, pdf);
-					pb.pend_e[p] = f4_of(sh.mat.emission, 0.0f);
-					pb.pend_b[p] = f4_of(beta, 0.0f);
-					pb.sh_o[p] = f4_of(sh.x, 0.0f);
-					pb.sh_d[p] = f4_of(wi, R - KGR_SHADOW_EPS);
-					shadow = true;
-				}
-				/* continuation (eval, brdf.cuh:573-589) */
-				if (depth < fp.max_depth || final_seed) {
-					f3 wi;
-					float pdf = 0.0f;
-					f3 f = eval(sh, wi, pdf, seed);
-					if (pdf > 0) {
-						f3 T = f * fabsf(dot(wi, n3)) / pdf;
-						beta = beta * T;
-						bool alive = true;
-						if (fp.russian_roulette && depth >= fp.rr_start_depth) {
-							float qq = 1.0f - kmin(kmax(0.05f, beta.y), 1.0f);
-							float r = fract(seed.x);
-							if (r < qq)
-								alive = false;
-							else
-								beta = beta / (1.0f - qq);
-						}
-						if (alive && depth < fp.max_depth) {
-							pb.ray_o[p] = f4_of(sh.x, 0.0f);
-							pb.ray_d[p] = f4_of(wi, 1e16f);
-							pb.beta[p] = f4_of(beta, 0.0f);
-							cont = true;
-						}
-					}
-				}
+				shade_surface(s, fp, depth, final_seed, sh, mk(bv.x, bv.y, bv.z), seed, out);
+				shadow = out.shadow;
+				cont = out.cont;
 				pb.seed[p] = f4_of(seed, 0.0f);
 			}
 		}
@@ -254,11 +236,7 @@ __global__ void __launch_bounds__(128, KGR_TRACE_MIN_BLOCKS) shadow_resolve_kern
  * L += beta * (Le + Ld) in the order of the recursion. */
 __device__ __forceinline__ void resolve_shadow(const PathBuffers &pb, uint32_t p, bool occ)
 {
-	float4 c = pb.pend_c[p], e = pb.pend_e[p], be = pb.pend_b[p];
-	f3 contr = occ ? mk(0.0f) : mk(c.x, c.y, c.z);
-	f3 direct = mk(e.x, e.y, e.z) + contr / c.w;
-	float4 Lv = pb.L[p];
-	pb.L[p] = f4_of(mk(Lv.x, Lv.y, Lv.z) + mk(be.x, be.y, be.z) * direct, 0.0f);
+	pb.L[p] = nee_add(pb.L[p], pb.pend_c[p], pb.pend_e[p], pb.pend_b[p], occ);
 }
 
 /* Persistent traversal of the fast layout: each lane takes a new ray from the

@@ -10,7 +10,10 @@ is Mrays/s (camera + bounce + shadow rays) with the scene resident on the
 device; `e2e` is the same metric through the C ABI with the frame read back
 to pinned host memory every step.  The roofline entry is computed live from
 CUDA events the library records after every launch on the render stream and
-from the traversal visit counts of one counting frame.
+from the traversal visit counts of one counting frame.  `equal_relmse`
+compares the radiance-cached tracer with the plain tracer on the same scene
+and resolution: ms/frame and relMSE against an FP64-accumulated 4096-spp
+render, and the speed-up at equal or lower relMSE.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -63,6 +66,9 @@ def parse():
     ap.add_argument("--layout", default="fast", choices=["fast", "threaded"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU sample time per measurement")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-quality", action="store_true",
+                    help="skip the cached-vs-plain comparison at equal relMSE")
+    ap.add_argument("--ref-spp", type=int, default=4096, help="spp of the FP64-accumulated reference image")
     return ap.parse_args()
 
 
@@ -221,6 +227,97 @@ def make_scene_cpu(name):
     return g, CpuScene(g)
 
 
+def relmse_compare(args, g, sc, W, H, stream, sptr):
+    """ms/frame and relMSE of the plain and the radiance-cached tracer against
+    an FP64-accumulated plain render of `--ref-spp` samples per pixel.
+
+    relMSE = mean over pixels and RGB of (x - ref)^2 / (ref^2 + 0.01).  Each
+    cached configuration is compared with the costliest plain configuration
+    whose relMSE is still at or above its own, so the speed-up is at equal or
+    lower error; the cache trains online (one Adam step per frame) for 300
+    frames first and keeps training while it is timed."""
+    import torch
+
+    from artemis_gb300 import kgr
+
+    cam = kgr.camera(g.eye, g.target, g.fov, W / H)
+    bufs = [torch.zeros((W * H, 4), dtype=torch.float32, device="cuda") for _ in range(4)]
+    ptrs = [b.data_ptr() for b in bufs]
+
+    def make(spp, cache=False):
+        a = kgr.Attachment("path_tracer")
+        a.attach(W, H)
+        a.load()
+        a.set_option("spp", spp)
+        a.set_option("russian_roulette", True)
+        a.set_option("rr_start_depth", 3)
+        a.set_option("layout", args.layout)
+        if cache:
+            a.set_option("cache", True)
+        return a
+
+    def info(f):
+        return kgr.launch_info(cam, W, H, ptrs, max_depth=args.max_depth, frame=f)
+
+    t0 = time.perf_counter()
+    per = 16
+    ref = torch.zeros((W * H, 3), dtype=torch.float64, device="cuda")
+    a = make(per)
+    frames = max(1, args.ref_spp // per)
+    for f in range(frames):
+        a.render(info(1 << 20 | f), sc, sptr)
+        ref += bufs[0][:, :3].double()
+    ref /= frames
+    a.close()
+    torch.cuda.synchronize()
+    ref_s = time.perf_counter() - t0
+
+    def relmse():
+        d = bufs[0][:, :3].double() - ref
+        return (d * d / (ref * ref + 1e-2)).mean().item()
+
+    def measure(a, first, n=8, warm=3):
+        for f in range(warm):
+            a.render(info(first + f), sc, sptr)
+        ms, err = [], []
+        for f in range(n):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            a.render(info(first + warm + f), sc, sptr)
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+            err.append(relmse())
+        return round(float(np.median(ms)), 3), round(float(np.mean(err)), 4)
+
+    plain = {}
+    for spp in (1, 2, 4, 8, 16, 32):
+        a = make(spp)
+        plain[spp] = measure(a, 1000 * spp)
+        a.close()
+    cached = {}
+    for spp in (1, 2, 4):
+        a = make(spp, cache=True)
+        for f in range(300):
+            a.render(info(50000 + f), sc, sptr)
+        cached[spp] = measure(a, 60000)
+        a.close()
+    compare = []
+    for spp, (ms, err) in cached.items():
+        worse = [k for k, (_, e) in plain.items() if e >= err]
+        if worse:
+            k = max(worse)
+            compare.append({"cached_spp": spp, "cached_ms": ms, "cached_relmse": err, "plain_spp": k,
+                            "plain_ms": plain[k][0], "plain_relmse": plain[k][1],
+                            "speedup": round(plain[k][0] / ms, 2)})
+    best = max(compare, key=lambda c: c["speedup"]) if compare else None
+    return {"scene": args.scene, "resolution": [W, H], "reference": f"plain PT, {frames * per} spp, FP64 mean",
+            "reference_s": round(ref_s, 1), "relmse": "mean (x - ref)^2 / (ref^2 + 0.01)",
+            "plain": {str(k): {"ms": v[0], "relmse": v[1]} for k, v in plain.items()},
+            "cached_bf16": {str(k): {"ms": v[0], "relmse": v[1]} for k, v in cached.items()},
+            "at_equal_or_lower_relmse": compare, "best_speedup": best and best["speedup"]}
+
+
 def bench_ours(args):
     import torch
 
@@ -348,6 +445,10 @@ def bench_ours(args):
                                "hbm_frac": round(own / hbm, 4)},
                 "visits_per_frame": {"reference": list(visits["threaded"]), args.layout: list(visits[args.layout])}}
 
+    quality = None
+    if rank == 0 and not args.no_quality:
+        quality = relmse_compare(args, g, sc, W, H, stream, sptr)
+
     cpu_base = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
@@ -374,6 +475,7 @@ def bench_ours(args):
                 "rays_per_frame": int(rays / args.steps / max(1, ws)),
                 "stage_ms_per_frame": stage_ms,
                 "roofline": roofline,
+                "equal_relmse": quality,
                 "cpu_baseline": cpu_base,
                 "e2e": {"value": round(e2e_value, 2), "unit": "Mrays/s",
                         "h2d_bytes_per_step": ctypes.sizeof(kgr.LaunchInfo),

@@ -72,6 +72,10 @@ static kgr_status guarded(F &&f)
 	}
 }
 
+static int resolve_device(int device);
+
+int pick_device_ordinal(int device) { return resolve_device(device); }
+
 static int resolve_device(int device)
 {
 	int count = 0;
@@ -711,6 +715,32 @@ struct kgr_attachment {
 	}
 
 	/* path buffers of the cache's training paths */
+	/* Forget the temporal history -- reservoirs, per-pixel materials, the
+	 * previous camera -- as load() leaves it (asynchronous on st). */
+	void reset_history(cudaStream_t st)
+	{
+		size_t npix = (size_t)width * height;
+		if (kind == KIND_RESTIR_DI && res_a[0].ptr) {
+			for (int k = 0; k < 2; k++) {
+				KGR_CUDA(cudaMemsetAsync(res_a[k].ptr, 0xff, npix * sizeof(float4), st));
+				KGR_CUDA(cudaMemsetAsync(res_b[k].ptr, 0, npix * sizeof(float4), st));
+			}
+			KGR_CUDA(cudaMemsetAsync(pixel_materials.ptr, 0, npix * sizeof(kgr_material), st));
+			prev_index = 1;
+		}
+		if (kind == KIND_RESTIR_GI && gi_a[0].ptr) {
+			for (int k = 0; k < 3; k++) {
+				KGR_CUDA(cudaMemsetAsync(gi_a[k].ptr, 0, npix * sizeof(float4), st));
+				KGR_CUDA(cudaMemsetAsync(gi_b[k].ptr, 0, npix * sizeof(float4), st));
+			}
+			for (DevBuf<float4> *b : {&g_pos, &g_nrm, &g_ppos, &g_pnrm, &g_direct, &g_dir, &auxiliary})
+				KGR_CUDA(cudaMemsetAsync(b->ptr, 0, npix * sizeof(float4), st));
+			KGR_CUDA(cudaMemsetAsync(pixel_materials.ptr, 0, npix * sizeof(kgr_material), st));
+			gi_prev = 0;
+		}
+		have_prev_camera = false;
+	}
+
 	void ensure_side_stream()
 	{
 		if (side)
@@ -1307,7 +1337,7 @@ static const std::map<std::string, OptionValue> &option_defaults()
 		{"gi_temporal", true}, {"gi_mcap", 30}, {"gi_spatial_iterations", 3}, {"gi_neighbors", 8},
 		{"gi_radius", 30},
 		{"cache", false}, {"cache_train", true}, {"cache_train_paths", 16384}, {"cache_lr", 1e-3f},
-		{"cache_dtype", std::string("bf16")}};
+		{"cache_dtype", std::string("bf16")}, {"reset_history", false}};
 	return d;
 }
 
@@ -1374,6 +1404,10 @@ kgr_status kgr_render(kgr_attachment *att, const kgr_launch_info *info, const kg
 		check_launch(att, info, sc);
 		DeviceGuard g(att->device);
 		cudaStream_t st = (cudaStream_t)stream;
+		if (att->opt_int("reset_history", 0)) {
+			att->reset_history(st);
+			att->options.erase("reset_history");
+		}
 		switch (att->kind) {
 		case KIND_PT:
 			if (att->opt_int("cache", 0))

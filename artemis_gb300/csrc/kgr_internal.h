@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <new>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -39,6 +40,30 @@ void set_last_error(const std::string &msg);
 		if (!(cond))                                                           \
 			throw ::kgr::Error((status), (msg));                            \
 	} while (0)
+
+/* Run f and return its status: a thrown Error becomes its code and message
+ * (kgr_last_error); the C ABI never lets an exception out. */
+template <class F>
+inline kgr_status guard_call(F &&f)
+{
+	try {
+		f();
+		return KGR_OK;
+	} catch (const Error &e) {
+		set_last_error(e.what());
+		return e.status;
+	} catch (const std::bad_alloc &) {
+		set_last_error("host allocation failed");
+		return KGR_ERR_OUT_OF_MEMORY;
+	} catch (const std::exception &e) {
+		set_last_error(e.what());
+		return KGR_ERR_INTERNAL;
+	}
+}
+
+/* The CUDA ordinal to use: device, or the current one when device < 0
+ * (KGR_ERR_NO_DEVICE without a GPU). */
+int pick_device_ordinal(int device);
 
 /* Sets the device for the lifetime of the guard and restores the caller's. */
 struct DeviceGuard {

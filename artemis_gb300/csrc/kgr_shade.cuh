@@ -73,6 +73,58 @@ __device__ __forceinline__ void shade_surface(const DeviceScene &s, const FrameP
 	}
 }
 
+/* make_ray (amadeus_path_tracer.cu:25-56): one pcg3f draw for the jitter;
+ * the ReSTIR variant (amadeus_restir.cu:30-65) draws it but uses -0.5. */
+__device__ __forceinline__ void camera_ray(const float *center, const float *Uc, const float *Vc, const float *Wc,
+		uint32_t width, uint32_t height, int jitter, uint32_t ix, uint32_t iy, f3 &seed, f3 &origin,
+		f3 &direction)
+{
+	f3 U = mk(Uc[0], Uc[1], Uc[2]), V = mk(Vc[0], Vc[1], Vc[2]), W = mk(Wc[0], Wc[1], Wc[2]);
+	pcg3f(seed);
+	float xoffset = jitter ? (fract(seed.x) - 0.5f) : -0.5f;
+	float yoffset = jitter ? (fract(seed.y) - 0.5f) : -0.5f;
+	float ax = ((float)ix + xoffset) / (float)width;
+	float ay = ((float)iy + yoffset) / (float)height;
+	float dx = 2.0f * ax - 1.0f;
+	float dy = 2.0f * ay - 1.0f;
+	origin = mk(center[0], center[1], center[2]);
+	direction = normalize(dx * U + dy * V + W);
+}
+
+/* Progressive mean dst = (prev * n + s) / (n + 1) (amadeus_path_tracer.cu:59-70). */
+__device__ __forceinline__ void accumulate4(float4 *buf, uint32_t i, float4 v, bool acc, float count)
+{
+	if (acc) {
+		float4 d = buf[i];
+		d.x = (d.x * count + v.x) / (count + 1);
+		d.y = (d.y * count + v.y) / (count + 1);
+		d.z = (d.z * count + v.z) / (count + 1);
+		d.w = (d.w * count + v.w) / (count + 1);
+		buf[i] = d;
+	} else {
+		buf[i] = v;
+	}
+}
+
+/* One finished path into the frame's buffers: sample `count` of pixel pix
+ * (acc: blend with the previous mean); NaN radiance shows as magenta. */
+__device__ __forceinline__ void accumulate_path(const OutputBuffers &out, const PathBuffers &pb, uint32_t p,
+		uint32_t pix, bool acc, float count)
+{
+	float4 L = pb.L[p];
+	f3 c = mk(L.x, L.y, L.z);
+	if (anynan(c))
+		c = mk(1.0f, 0.0f, 1.0f);
+	if (out.color)
+		accumulate4(out.color, pix, f4_of(c, 1.0f), acc, count);
+	if (out.normal)
+		accumulate4(out.normal, pix, pb.aov_n[p], acc, count);
+	if (out.albedo)
+		accumulate4(out.albedo, pix, pb.aov_a[p], acc, count);
+	if (out.position)
+		out.position[pix] = pb.aov_p[p];
+}
+
 /* L += beta * (Le + Ld) once the shadow ray is resolved, in the order of
  * the recursion (Ld = contribution / pdf, zero when occluded). */
 __device__ __forceinline__ float4 nee_add(float4 L, float4 c, float4 e, float4 be, bool occ)

@@ -41,21 +41,10 @@ inline int grid_for(uint32_t n, int block, int per_sm = 16)
 
 __device__ __forceinline__ f3 v3(const float *p) { return mk(p[0], p[1], p[2]); }
 
-/* make_ray (amadeus_path_tracer.cu:25-56): one pcg3f draw for the jitter;
- * the ReSTIR variant (amadeus_restir.cu:30-65) draws it but uses -0.5. */
 __device__ __forceinline__ void make_ray(const FrameParams &fp, uint32_t ix, uint32_t iy, f3 &seed,
 		f3 &origin, f3 &direction)
 {
-	f3 U = v3(fp.U), V = v3(fp.V), W = v3(fp.W);
-	pcg3f(seed);
-	float xoffset = fp.jitter ? (fract(seed.x) - 0.5f) : -0.5f;
-	float yoffset = fp.jitter ? (fract(seed.y) - 0.5f) : -0.5f;
-	float ax = ((float)ix + xoffset) / (float)fp.width;
-	float ay = ((float)iy + yoffset) / (float)fp.height;
-	float dx = 2.0f * ax - 1.0f;
-	float dy = 2.0f * ay - 1.0f;
-	origin = v3(fp.center);
-	direction = normalize(dx * U + dy * V + W);
+	camera_ray(fp.center, fp.U, fp.V, fp.W, fp.width, fp.height, fp.jitter, ix, iy, seed, origin, direction);
 }
 
 __global__ void generate_kernel(PathBuffers pb, FrameParams fp)
@@ -340,20 +329,6 @@ int resident_grid(K kernel, int block)
 	return per_sm * device_sm_count();
 }
 
-__device__ __forceinline__ void accumulate4(float4 *buf, uint32_t i, float4 v, bool acc, float count)
-{
-	if (acc) {
-		float4 d = buf[i];
-		d.x = (d.x * count + v.x) / (count + 1);
-		d.y = (d.y * count + v.y) / (count + 1);
-		d.z = (d.z * count + v.z) / (count + 1);
-		d.w = (d.w * count + v.w) / (count + 1);
-		buf[i] = d;
-	} else {
-		buf[i] = v;
-	}
-}
-
 /* accumulate (amadeus_path_tracer.cu:59-70), the frame's samples in order */
 __global__ void accumulate_kernel(PathBuffers pb, FrameParams fp, OutputBuffers out)
 {
@@ -361,21 +336,9 @@ __global__ void accumulate_kernel(PathBuffers pb, FrameParams fp, OutputBuffers 
 	if (pix >= fp.npix)
 		return;
 	for (uint32_t sidx = 0; sidx < fp.spp; sidx++) {
-		uint32_t p = sidx * fp.npix + pix;
-		float4 L = pb.L[p];
-		f3 c = mk(L.x, L.y, L.z);
-		if (anynan(c))
-			c = mk(1.0f, 0.0f, 1.0f);
 		bool acc = fp.accumulate || sidx > 0;
 		float count = (float)(fp.accumulate ? fp.samples + (int)sidx : (int)sidx);
-		if (out.color)
-			accumulate4(out.color, pix, f4_of(c, 1.0f), acc, count);
-		if (out.normal)
-			accumulate4(out.normal, pix, pb.aov_n[p], acc, count);
-		if (out.albedo)
-			accumulate4(out.albedo, pix, pb.aov_a[p], acc, count);
-		if (out.position)
-			out.position[pix] = pb.aov_p[p];
+		accumulate_path(out, pb, sidx * fp.npix + pix, pix, acc, count);
 	}
 }
 

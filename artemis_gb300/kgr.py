@@ -140,6 +140,17 @@ def lib():
             "kgr_generated_get": (c_i32, [vp, vp]),
             "kgr_generated_destroy": (c_i32, [vp]),
             "kgr_camera_setup": (c_i32, [vp, vp, vp, c_f, c_f, vp]),
+            "kgr_batcher_create": (c_i32, [c_i32, c_u32, c_u32, vp]),
+            "kgr_batcher_render": (c_i32, [vp, vp, vp, c_u32, vp, vp]),
+            "kgr_batcher_ray_counts": (c_i32, [vp, vp]),
+            "kgr_batcher_launch_info": (c_i32, [vp, vp, vp]),
+            "kgr_batcher_destroy": (c_i32, [vp]),
+            "kgr_server_create": (c_i32, [vp, vp]),
+            "kgr_server_add_scene": (c_i32, [vp, vp, vp]),
+            "kgr_server_submit": (c_i32, [vp, vp, vp]),
+            "kgr_server_wait": (c_i32, [vp, c_u64, ctypes.c_double, vp]),
+            "kgr_server_stats_get": (c_i32, [vp, vp]),
+            "kgr_server_destroy": (c_i32, [vp]),
         }
         for name, (res, args) in sigs.items():
             fn = getattr(L, name)
@@ -449,3 +460,150 @@ def launch_info(cam_info, width, height, buffers, max_depth=2, samples=0, accumu
     info.accumulate = 1 if accumulate else 0
     info.frame = frame
     return info
+
+
+# ------------------------------------------------------------ batching / serving (include/kgr_serve.h)
+
+class BatchJob(ctypes.Structure):
+    _fields_ = [("width", c_u32), ("height", c_u32), ("spp", c_u32), ("sample_begin", c_u32),
+                ("sample_count", c_u32), ("frame", c_u32), ("accumulate", c_i32), ("samples", c_i32),
+                ("center", c_f * 3), ("ax_u", c_f * 3), ("ax_v", c_f * 3), ("ax_w", c_f * 3),
+                ("color", vp), ("normal", vp), ("albedo", vp), ("position", vp)]
+
+
+class BatchOptions(ctypes.Structure):
+    _fields_ = [("max_depth", c_i32), ("russian_roulette", c_i32), ("rr_start_depth", c_i32), ("layout", c_i32),
+                ("use_graph", c_i32), ("reserved", c_i32 * 3)]
+
+
+REQUEST_PATH_TRACER, REQUEST_RESTIR_DI = 0, 1
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("device", c_i32), ("path_capacity", c_u32), ("max_jobs", c_u32), ("spp_per_tick", c_u32),
+                ("memory_budget", c_u64), ("layout", c_i32), ("use_graph", c_i32), ("reserved", c_i32 * 2)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("scene", c_u32), ("kind", c_i32), ("width", c_u32), ("height", c_u32), ("spp", c_u32),
+                ("max_depth", c_u32), ("frame", c_u32), ("russian_roulette", c_i32), ("rr_start_depth", c_i32),
+                ("eye", c_f * 3), ("target", c_f * 3), ("fov_deg", c_f), ("host_color", vp)]
+
+
+class RequestResult(ctypes.Structure):
+    _fields_ = [("status", c_i32), ("done", c_i32), ("queue_ms", ctypes.c_double), ("latency_ms", ctypes.c_double),
+                ("service_ms", ctypes.c_double), ("ticks", c_u32), ("reserved", c_u32)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", c_u64), ("completed", c_u64), ("failed", c_u64), ("rays", c_u64), ("ticks", c_u64),
+                ("busy_ms", ctypes.c_double), ("latency_p50_ms", ctypes.c_double),
+                ("latency_p90_ms", ctypes.c_double), ("latency_p99_ms", ctypes.c_double),
+                ("latency_max_ms", ctypes.c_double), ("mean_jobs_per_tick", ctypes.c_double),
+                ("peak_budget_bytes", c_u64), ("graph_replays", c_u64)]
+
+
+def batch_job(cam_info, width, height, spp, color, sample_begin=0, sample_count=None, frame=0,
+              normal=None, albedo=None, position=None):
+    """A BatchJob for a camera LaunchInfo (kgr.camera) and device pointers."""
+    j = BatchJob()
+    j.width, j.height, j.spp, j.frame = width, height, spp, frame
+    j.sample_begin = sample_begin
+    j.sample_count = spp - sample_begin if sample_count is None else sample_count
+    c = cam_info.camera
+    j.center[:], j.ax_u[:], j.ax_v[:], j.ax_w[:] = list(c.center), list(c.ax_u), list(c.ax_v), list(c.ax_w)
+    j.color, j.normal, j.albedo, j.position = color, normal, albedo, position
+    return j
+
+
+class Batcher:
+    """kgr_batcher: several path-traced jobs per shared wavefront frame."""
+
+    def __init__(self, path_capacity, max_jobs=256, device=-1):
+        h = vp()
+        check(lib().kgr_batcher_create(device, path_capacity, max_jobs, ctypes.byref(h)))
+        self.handle = h
+
+    def render(self, scene, jobs, max_depth=8, russian_roulette=True, rr_start_depth=3, layout=LAYOUT_FAST,
+               use_graph=True, stream=None):
+        arr = (BatchJob * len(jobs))(*jobs)
+        opt = BatchOptions(max_depth, 1 if russian_roulette else 0, rr_start_depth, layout, 1 if use_graph else 0)
+        check(lib().kgr_batcher_render(self.handle, scene.handle, arr, len(jobs), ctypes.byref(opt), stream))
+
+    def ray_counts(self):
+        c = (c_u64 * 3)()
+        check(lib().kgr_batcher_ray_counts(self.handle, c))
+        return list(c)
+
+    def launch_info(self):
+        n, g = c_u32(), c_i32()
+        check(lib().kgr_batcher_launch_info(self.handle, ctypes.byref(n), ctypes.byref(g)))
+        return n.value, bool(g.value)
+
+    def close(self):
+        if self.handle:
+            lib().kgr_batcher_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """kgr_server: the render request loop (host thread inside libkgr)."""
+
+    def __init__(self, path_capacity=1 << 24, max_jobs=256, spp_per_tick=0, memory_budget=120 << 30,
+                 layout=LAYOUT_FAST, use_graph=True, device=-1):
+        cfg = ServerConfig(device, path_capacity, max_jobs, spp_per_tick, memory_budget, layout,
+                           1 if use_graph else 0)
+        h = vp()
+        check(lib().kgr_server_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self.handle = h
+        self._keep = {}
+
+    def add_scene(self, scene):
+        i = c_u32()
+        check(lib().kgr_server_add_scene(self.handle, scene.handle, ctypes.byref(i)))
+        self._keep[("scene", i.value)] = scene
+        return i.value
+
+    def submit(self, scene_id, width, height, spp, eye, target, fov, out=None, kind=REQUEST_PATH_TRACER,
+               max_depth=8, frame=0, russian_roulette=True, rr_start_depth=3):
+        """Queue a request; `out` (float32 numpy array of width*height*4, kept
+        alive here) receives the image."""
+        q = Request(scene_id, kind, width, height, spp, max_depth, frame, 1 if russian_roulette else 0,
+                    rr_start_depth)
+        q.eye[:], q.target[:], q.fov_deg = list(map(float, eye)), list(map(float, target)), float(fov)
+        q.host_color = None if out is None else out.ctypes.data_as(vp)
+        rid = c_u64()
+        check(lib().kgr_server_submit(self.handle, ctypes.byref(q), ctypes.byref(rid)))
+        if out is not None:
+            self._keep[rid.value] = out
+        return rid.value
+
+    def wait(self, rid, timeout_ms=-1.0):
+        """RequestResult of a request; raises KgrError on timeout."""
+        r = RequestResult()
+        st = lib().kgr_server_wait(self.handle, rid, timeout_ms, ctypes.byref(r))
+        if st not in (0,):
+            raise KgrError(st, lib().kgr_last_error().decode(errors="replace"))
+        return r
+
+    def stats(self):
+        s = ServerStats()
+        check(lib().kgr_server_stats_get(self.handle, ctypes.byref(s)))
+        return s
+
+    def close(self):
+        if self.handle:
+            lib().kgr_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -14,16 +14,16 @@ from oracle import pyoracle
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def declared_functions():
-    text = open(os.path.join(ROOT, "include", "kgr.h")).read()
+def declared_functions(header="kgr.h"):
+    text = open(os.path.join(ROOT, "include", header)).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     return sorted(set(re.findall(r"\b(kgr_\w+)\s*\(", text)))
 
 
 def test_library_exports_every_declared_symbol():
     L = kgr.lib()
-    names = declared_functions()
-    assert len(names) >= 30
+    names = declared_functions("kgr.h") + declared_functions("kgr_serve.h")
+    assert len(names) >= 45
     missing = [n for n in names if not hasattr(L, n)]
     assert not missing, missing
     assert L.kgr_abi_version() == 1

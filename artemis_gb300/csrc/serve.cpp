@@ -209,13 +209,8 @@ struct kgr_server {
 		uint64_t total_paths = 0;
 		for (auto &j : t.jobs)
 			total_paths += (uint64_t)j.r->req.width * j.r->req.height * j.k;
-		if (t.restir) {
-			kgr_render_stats st;
-			if (kgr_get_render_stats(t.restir, &st) == KGR_OK) {
-				uint64_t per = st.camera_rays + st.bounce_rays + st.shadow_rays;
-				counts[0] = per * (t.jobs.empty() ? 1 : t.jobs[0].k);
-			}
-		}
+		/* ReSTIR ticks add no rays: the reuse passes' shadow rays are not
+		 * counted on the device */
 		uint64_t tick_rays = counts[0] + counts[1] + counts[2];
 		for (auto &j : t.jobs) {
 			Request *r = j.r;

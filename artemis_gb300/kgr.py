@@ -590,6 +590,7 @@ class Server:
         st = lib().kgr_server_wait(self.handle, rid, timeout_ms, ctypes.byref(r))
         if st not in (0,):
             raise KgrError(st, lib().kgr_last_error().decode(errors="replace"))
+        self._keep.pop(rid, None)  # the library no longer writes the output array
         return r
 
     def stats(self):

@@ -69,6 +69,8 @@ def parse():
     ap.add_argument("--no-quality", action="store_true",
                     help="skip the cached-vs-plain comparison at equal relMSE")
     ap.add_argument("--ref-spp", type=int, default=4096, help="spp of the FP64-accumulated reference image")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving run")
+    ap.add_argument("--serve-seconds", type=float, default=1.0, help="arrival window of the 200 req/s phase")
     return ap.parse_args()
 
 
@@ -318,6 +320,94 @@ def relmse_compare(args, g, sc, W, H, stream, sptr):
             "at_equal_or_lower_relmse": compare, "best_speedup": best and best["speedup"]}
 
 
+SERVE_RES = [(320, 240), (640, 480), (1280, 720), (1920, 1080), (3840, 2160)]
+SERVE_SCENES = ("terrain_s", "terrain_m", "terrain_l")  # 0.26M, 1.0M, 4.1M triangles
+
+
+def serve_run(args):
+    """The render server under a Poisson request stream: resolution uniform
+    over SERVE_RES, spp uniform in [1, 16], scene uniform over three
+    resident procedural scenes, half path-tracer and half ReSTIR DI requests
+    (ReSTIR: spp frames accumulated), depth 8 with Russian roulette from 3,
+    admission by a 120 GB budget.  Phase 1 offers 200 req/s for
+    --serve-seconds; phase 2 offers half the request rate phase 1 completed,
+    for 10 s.  `mpaths_per_s` counts pixels x spp of every completed request;
+    `mrays_per_s_pt` the camera, bounce and shadow rays of the path-tracer
+    ticks (ReSTIR's reuse passes do not count their shadow rays).  Latency = submission to image in host memory;
+    `latency_per_mpath` divides it by the request's paths (pixels x spp),
+    which removes the 1700x spread of request sizes."""
+    from artemis_gb300 import kgr
+
+    t_build = time.perf_counter()
+    gens = [kgr.Generated(n, 1) for n in SERVE_SCENES]
+    scenes = [kgr.Scene.from_generated(g) for g in gens]
+    build_s = time.perf_counter() - t_build
+    srv = kgr.Server(path_capacity=1 << 24, max_jobs=256, spp_per_tick=4, memory_budget=120 << 30)
+    sids = [srv.add_scene(sc) for sc in scenes]
+
+    def submit(i, w, h, spp, kind, frame):
+        g = gens[i]
+        out = np.empty((w * h, 4), np.float32)
+        return srv.submit(sids[i], w, h, spp, g.eye, g.target, g.fov, out, kind=kind, max_depth=8, frame=frame,
+                          russian_roulette=True, rr_start_depth=3)
+
+    # warm-up: every resolution and kind once (ReSTIR attachments, graphs)
+    warm = [submit(0, w, h, 1, k, 0) for (w, h) in SERVE_RES for k in (kgr.REQUEST_PATH_TRACER, kgr.REQUEST_RESTIR_DI)]
+    for r in warm:
+        srv.wait(r, 600000.0)
+
+    def phase(rate, seconds, seed):
+        rng = np.random.default_rng(seed)
+        t, arrivals = 0.0, []
+        while True:
+            t += rng.exponential(1.0 / rate)
+            if t > seconds:
+                break
+            w, h = SERVE_RES[rng.integers(len(SERVE_RES))]
+            arrivals.append((t, int(rng.integers(3)), w, h, int(rng.integers(1, 17)),
+                             kgr.REQUEST_PATH_TRACER if rng.random() < 0.5 else kgr.REQUEST_RESTIR_DI))
+        s0 = srv.stats()
+        t0 = time.perf_counter()
+        ids = []
+        for k, (ta, sc, w, h, spp, kind) in enumerate(arrivals):
+            dt = ta - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            ids.append(submit(sc, w, h, spp, kind, k))
+        res = [srv.wait(r, 1200000.0) for r in ids]
+        wall = time.perf_counter() - t0
+        s1 = srv.stats()
+        ok = [r for r in res if r.status == 0]
+        lat = np.array([r.latency_ms for r in ok])
+        mpaths = np.array([w * h * spp / 1e6 for (_, _, w, h, spp, _), r in zip(arrivals, res) if r.status == 0])
+        norm = lat / mpaths
+        q = lambda a, p: round(float(np.percentile(a, p)), 2) if len(a) else None
+        return {"offered_rps": rate, "window_s": seconds, "requests": len(arrivals), "completed": len(ok),
+                "failed": len(res) - len(ok), "wall_s": round(wall, 2),
+                "completed_rps": round(len(ok) / wall, 2),
+                "mpaths_per_s": round(float(mpaths.sum()) / wall, 1),
+                "mrays_per_s_pt": round((s1.rays - s0.rays) / wall / 1e6, 1),
+                "latency_ms": {"p50": q(lat, 50), "p90": q(lat, 90), "p99": q(lat, 99), "max": q(lat, 100)},
+                "latency_per_mpath_ms": {"p50": q(norm, 50), "p99": q(norm, 99)},
+                "queue_ms_p50": q(np.array([r.queue_ms for r in ok]), 50),
+                "ticks": int(s1.ticks - s0.ticks)}
+
+    p1 = phase(200.0, args.serve_seconds, 1)
+    p2 = phase(max(0.5, 0.5 * p1["completed_rps"]), 10.0, 2)
+    st = srv.stats()
+    out = {"scenes": {n: sc.info().triangle_count for n, sc in zip(SERVE_SCENES, scenes)},
+           "scene_build_s": round(build_s, 1),
+           "server": {"path_capacity": 1 << 24, "max_jobs": 256, "spp_per_tick": 4, "memory_budget_gb": 120,
+                      "graphs": True},
+           "mean_jobs_per_tick": round(st.mean_jobs_per_tick, 2), "graph_replays": int(st.graph_replays),
+           "peak_budget_gb": round(st.peak_budget_bytes / 2 ** 30, 2),
+           "phase_200rps": p1, "phase_sustainable": p2}
+    srv.close()
+    for sc in scenes:
+        sc.close()
+    return out
+
+
 def bench_ours(args):
     import torch
 
@@ -448,6 +538,9 @@ def bench_ours(args):
     quality = None
     if rank == 0 and not args.no_quality:
         quality = relmse_compare(args, g, sc, W, H, stream, sptr)
+    serve = None
+    if rank == 0 and not args.no_serve:
+        serve = serve_run(args)
 
     cpu_base = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -476,6 +569,7 @@ def bench_ours(args):
                 "stage_ms_per_frame": stage_ms,
                 "roofline": roofline,
                 "equal_relmse": quality,
+                "serve": serve,
                 "cpu_baseline": cpu_base,
                 "e2e": {"value": round(e2e_value, 2), "unit": "Mrays/s",
                         "h2d_bytes_per_step": ctypes.sizeof(kgr.LaunchInfo),

@@ -121,7 +121,7 @@ typedef struct kgr_request_result {
 
 typedef struct kgr_server_stats {
 	uint64_t submitted, completed, failed;
-	uint64_t rays;            /* camera + bounce + shadow rays of all ticks */
+	uint64_t rays;            /* camera + bounce + shadow rays of the path-tracer ticks */
 	uint64_t ticks;
 	double busy_ms;           /* wall time from the first submission to the last completion */
 	double latency_p50_ms, latency_p90_ms, latency_p99_ms, latency_max_ms;

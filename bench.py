@@ -70,6 +70,7 @@ def parse():
                     help="skip the cached-vs-plain comparison at equal relMSE")
     ap.add_argument("--ref-spp", type=int, default=4096, help="spp of the FP64-accumulated reference image")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving run")
+    ap.add_argument("--no-restir", action="store_true", help="skip the ReSTIR DI (256^2) and GI (1080p) runs")
     ap.add_argument("--serve-seconds", type=float, default=1.0, help="arrival window of the 200 req/s phase")
     return ap.parse_args()
 
@@ -320,6 +321,136 @@ def relmse_compare(args, g, sc, W, H, stream, sptr):
             "at_equal_or_lower_relmse": compare, "best_speedup": best and best["speedup"]}
 
 
+def restir_runs(args):
+    """ReSTIR DI on the box scene (12 + 4096 + 128 triangles, 64 ceiling
+    quads) at 256x256, 1 spp, 32 candidates, temporal reuse (M-cap 20), one
+    spatial pass (5 neighbours, 30 px), depth 2: GPU ms/frame, and the
+    oracle's per-pixel CPU frame on all host cores.
+
+    ReSTIR GI on the 4.1M-triangle scene (65,536 emissive triangles,
+    log-uniform radiance) at 1920x1080 over 16 frames of a camera orbit of
+    0.5 degrees per frame with sub-pixel jitter: 32 DI candidates, one GI
+    sample per pixel, temporal reuse (M-cap 30), 3 spatial iterations x 8
+    neighbours, depth 8 with Russian roulette from 3.  ms/frame (median), and
+    the relMSE of the last frame -- and of 1-spp and 4-spp plain frames -- against
+    an FP64-accumulated plain render of `--ref-spp` samples at that camera."""
+    import torch
+
+    from oracle import pyoracle
+
+    from artemis_gb300 import kgr
+
+    out = {}
+    stream = torch.cuda.current_stream()
+    sptr = ctypes.c_void_p(stream.cuda_stream)
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1)
+
+    # --- ReSTIR DI, 256^2
+    g = kgr.Generated("box4k", 0x4B4F4252)
+    sc = kgr.Scene.from_generated(g)
+    W = H = 256
+    cam = kgr.camera(g.eye, g.target, g.fov, 1.0)
+    bufs = [torch.zeros((W * H, 4), dtype=torch.float32, device="cuda") for _ in range(4)]
+    opts = {"candidates": 32, "temporal": True, "temporal_mcap": 20, "spatial_passes": 1,
+            "spatial_neighbors": 5, "spatial_radius": 30}
+    att = kgr.Attachment("restir_di")
+    att.attach(W, H)
+    att.load()
+    for k, v in opts.items():
+        att.set_option(k, v)
+    info = lambda f: kgr.launch_info(cam, W, H, [b.data_ptr() for b in bufs], max_depth=2, frame=f)
+    for f in range(5):
+        att.render(info(f), sc, sptr)
+    ms = [timed(lambda f=f: att.render(info(5 + f), sc, sptr)) for f in range(20)]
+    att.close()
+    osc = pyoracle.Scene(g.positions, g.normals, g.tris4(), g.materials_raw, sc.lights(), sc.bvh())
+    state = pyoracle.RestirBuffers(W * H)
+    t0 = time.perf_counter()
+    p = pyoracle.render_params(W, H, kgr.camera_dict(cam), max_depth=2, spp=1, frame=0, candidates=32, temporal=1,
+                               temporal_mcap=20, spatial_passes=1, spatial_neighbors=5, spatial_radius=30)
+    pyoracle.render_restir(osc, p, state)
+    cpu_s = time.perf_counter() - t0
+    out["restir_di_256"] = {"gpu_ms_per_frame": round(float(np.median(ms)), 3),
+                            "cpu_oracle_ms_per_frame": round(cpu_s * 1e3, 1), "cpu_cores": os.cpu_count(),
+                            "scene_triangles": sc.info().triangle_count}
+    sc.close()
+
+    # --- ReSTIR GI, 1080p, 16-frame orbit
+    g = kgr.Generated("terrain_l", 1)
+    sc = kgr.Scene.from_generated(g)
+    W, H = 1920, 1080
+    bufs = [torch.zeros((W * H, 4), dtype=torch.float32, device="cuda") for _ in range(4)]
+    ptrs = [b.data_ptr() for b in bufs]
+    eye0, tgt = np.array(g.eye, np.float64), np.array(g.target, np.float64)
+
+    def orbit(f):
+        a = np.radians(0.5 * f)
+        d = eye0 - tgt
+        e = tgt + np.array([d[0] * np.cos(a) + d[2] * np.sin(a), d[1], -d[0] * np.sin(a) + d[2] * np.cos(a)])
+        return kgr.camera(e.astype(np.float32), g.target, g.fov, W / H)
+
+    att = kgr.Attachment("restir_gi")
+    att.attach(W, H)
+    att.load()
+    for k, v in {"candidates": 32, "gi_mcap": 30, "gi_spatial_iterations": 3, "gi_neighbors": 8,
+                 "russian_roulette": True, "rr_start_depth": 3}.items():
+        att.set_option(k, v)
+    gi_ms = []
+    for f in range(16):
+        c = orbit(f)
+        gi_ms.append(timed(lambda: att.render(kgr.launch_info(c, W, H, ptrs, max_depth=8, frame=f), sc, sptr)))
+    last = bufs[0][:, :3].double().clone()
+    att.close()
+    cam = orbit(15)
+    ref = torch.zeros((W * H, 3), dtype=torch.float64, device="cuda")
+
+    def plain(spp, frames, first):
+        a = kgr.Attachment("path_tracer")
+        a.attach(W, H)
+        a.load()
+        a.set_option("spp", spp)
+        a.set_option("russian_roulette", True)
+        a.set_option("rr_start_depth", 3)
+        return a
+
+    per = 16
+    a = plain(per, 0, 0)
+    nref = max(1, args.ref_spp // per)
+    for f in range(nref):
+        a.render(kgr.launch_info(cam, W, H, ptrs, max_depth=8, frame=1 << 20 | f), sc, sptr)
+        ref += bufs[0][:, :3].double()
+    a.close()
+    ref /= nref
+
+    def relmse(x):
+        d = x - ref
+        return round((d * d / (ref * ref + 1e-2)).mean().item(), 4)
+
+    res = {}
+    for spp in (1, 4):
+        a = plain(spp, 0, 0)
+        a.render(kgr.launch_info(cam, W, H, ptrs, max_depth=8, frame=777), sc, sptr)
+        ms_p = timed(lambda: a.render(kgr.launch_info(cam, W, H, ptrs, max_depth=8, frame=778), sc, sptr))
+        res[spp] = (round(ms_p, 3), relmse(bufs[0][:, :3].double()))
+        a.close()
+    out["restir_gi_1080p"] = {"scene_triangles": sc.info().triangle_count, "lights": sc.info().light_count,
+                              "frames": 16, "ms_per_frame_median": round(float(np.median(gi_ms)), 3),
+                              "ms_first_frame": round(gi_ms[0], 3),
+                              "relmse_last_frame": relmse(last),
+                              "plain_1spp": {"ms": res[1][0], "relmse": res[1][1]},
+                              "plain_4spp": {"ms": res[4][0], "relmse": res[4][1]},
+                              "reference": f"plain PT, {nref * per} spp, FP64 mean, camera of frame 15"}
+    sc.close()
+    return out
+
+
 SERVE_RES = [(320, 240), (640, 480), (1280, 720), (1920, 1080), (3840, 2160)]
 SERVE_SCENES = ("terrain_s", "terrain_m", "terrain_l")  # 0.26M, 1.0M, 4.1M triangles
 
@@ -541,6 +672,9 @@ def bench_ours(args):
     serve = None
     if rank == 0 and not args.no_serve:
         serve = serve_run(args)
+    restir = None
+    if rank == 0 and not args.no_restir:
+        restir = restir_runs(args)
 
     cpu_base = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -570,6 +704,7 @@ def bench_ours(args):
                 "roofline": roofline,
                 "equal_relmse": quality,
                 "serve": serve,
+                "restir": restir,
                 "cpu_baseline": cpu_base,
                 "e2e": {"value": round(e2e_value, 2), "unit": "Mrays/s",
                         "h2d_bytes_per_step": ctypes.sizeof(kgr.LaunchInfo),

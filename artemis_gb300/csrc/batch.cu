@@ -106,9 +106,9 @@ void batch_frame(const DeviceScene &s, const PathBuffers &pb, const FrameParams 
 		int q = d & 1;
 		if (d > 0)
 			reset_counters(pb, (1 << (q ^ 1)) | (1 << CNT_SHADOW), st);
-		pt_trace_closest(s, pb, q, fp.layout, st);
+		pt_trace_closest(s, pb, q, fp.layout, fp.tune, st);
 		pt_shade(s, pb, fp, d, q, st);
-		pt_shadow_resolve(s, pb, fp.layout, st);
+		pt_shadow_resolve(s, pb, fp.layout, fp.tune, st);
 	}
 	batch_accumulate(pb, hdr, jobs, st);
 }

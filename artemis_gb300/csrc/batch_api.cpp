@@ -44,7 +44,8 @@ void kgr_batcher::render(const kgr_scene *scene, const kgr_batch_job *jobs, uint
 	KGR_REQUIRE(n >= 1 && n <= max_jobs, KGR_ERR_INVALID_ARGUMENT, "job count must be 1..max_jobs");
 	KGR_REQUIRE(jobs, KGR_ERR_INVALID_ARGUMENT, "NULL job list");
 	KGR_REQUIRE(opt.max_depth >= 0 && opt.max_depth <= 64, KGR_ERR_INVALID_ARGUMENT, "max_depth must be 0..64");
-	KGR_REQUIRE(opt.layout == KGR_LAYOUT_FAST || opt.layout == KGR_LAYOUT_THREADED, KGR_ERR_INVALID_ARGUMENT,
+	KGR_REQUIRE(opt.layout == KGR_LAYOUT_FAST || opt.layout == KGR_LAYOUT_THREADED || opt.layout == KGR_LAYOUT_WIDE,
+		KGR_ERR_INVALID_ARGUMENT,
 		"unknown layout");
 
 	/* the staging slot is free once the frame that last used it is done */
@@ -107,7 +108,8 @@ void kgr_batcher::render(const kgr_scene *scene, const kgr_batch_job *jobs, uint
 	fp.max_depth = opt.max_depth;
 	fp.russian_roulette = opt.russian_roulette ? 1 : 0;
 	fp.rr_start_depth = opt.rr_start_depth;
-	fp.layout = opt.layout;
+	fp.layout = layout_for(opt.layout, scene);
+	fp.tune = tune;
 	DeviceScene s = scene->view();
 	PathBuffers pb = path_buffers();
 	const BatchHeader *dh = reinterpret_cast<const BatchHeader *>(table.ptr);
@@ -117,11 +119,13 @@ void kgr_batcher::render(const kgr_scene *scene, const kgr_batch_job *jobs, uint
 	if (opt.use_graph) {
 		for (auto &e : graphs)
 			if (e.scene == scene && e.max_depth == fp.max_depth && e.rr == fp.russian_roulette &&
-					e.rr_start == fp.rr_start_depth && e.layout == fp.layout)
+					e.rr_start == fp.rr_start_depth && e.layout == fp.layout &&
+					e.tune.shadow == tune.shadow &&
+					e.tune.block == tune.block)
 				g = &e;
 		if (!g) {
-			graphs.push_back(Graph{scene, fp.max_depth, fp.russian_roulette, fp.rr_start_depth, fp.layout, 0,
-				nullptr});
+			graphs.push_back(Graph{scene, fp.max_depth, fp.russian_roulette, fp.rr_start_depth, fp.layout, tune,
+				0, nullptr});
 			g = &graphs.back();
 		}
 	}

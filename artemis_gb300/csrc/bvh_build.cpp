@@ -623,4 +623,97 @@ void build_fast(const Tree &tree, const std::vector<PrimBox> &boxes, const float
 	emit_node(0);
 }
 
+void build_wide(const Tree &tree, std::vector<WideNode> &nodes, uint32_t &max_stack)
+{
+	nodes.clear();
+	max_stack = 0;
+	if (tree.nodes.empty() || tree.nodes[0].count)
+		return;
+	/* record index of every leaf: the fast layout emits leaves depth-first,
+	 * left child first */
+	std::vector<uint32_t> first_record(tree.nodes.size(), 0);
+	{
+		uint32_t next = 0;
+		std::vector<int32_t> st(1, 0);
+		while (!st.empty()) {
+			int32_t i = st.back();
+			st.pop_back();
+			const TreeNode &n = tree.nodes[i];
+			if (n.count) {
+				first_record[i] = next;
+				next += (uint32_t)n.count;
+			} else {
+				st.push_back(n.right);
+				st.push_back(n.left);
+			}
+		}
+	}
+	auto leaf_ref = [&](int32_t i) -> int32_t {
+		const TreeNode &n = tree.nodes[i];
+		return ~(int32_t)((first_record[i] << 3) | (uint32_t)(n.count - 1));
+	};
+	/* returns the node index and the stack need of its subtree */
+	std::function<int32_t(int32_t, uint32_t &)> emit = [&](int32_t i, uint32_t &need) -> int32_t {
+		int32_t kids[4] = {tree.nodes[i].left, tree.nodes[i].right, -1, -1};
+		int nk = 2;
+		while (nk < 4) {
+			int best = -1;
+			float best_area = -1.0f;
+			for (int k = 0; k < nk; k++) {
+				const TreeNode &c = tree.nodes[kids[k]];
+				if (c.count)
+					continue;
+				float a = surface_area(c.bmin, c.bmax);
+				if (a > best_area) {
+					best_area = a;
+					best = k;
+				}
+			}
+			if (best < 0)
+				break;
+			const TreeNode &c = tree.nodes[kids[best]];
+			for (int k = nk; k > best + 1; k--)
+				kids[k] = kids[k - 1];
+			kids[best] = c.left;
+			kids[best + 1] = c.right;
+			nk++;
+		}
+		int32_t me = (int32_t)nodes.size();
+		nodes.push_back(WideNode());
+		WideNode w;
+		float *lo[3] = {&w.lox.x, &w.loy.x, &w.loz.x}, *hi[3] = {&w.hix.x, &w.hiy.x, &w.hiz.x};
+		int32_t *refs = &w.refs.x;
+		memset(&w, 0, sizeof(w));
+		uint32_t child_need = 0;
+		for (int k = 0; k < 4; k++) {
+			if (k >= nk) {
+				for (int a = 0; a < 3; a++) {
+					lo[a][k] = 0.0f;
+					hi[a][k] = 0.0f;
+				}
+				refs[k] = KGR_WIDE_EMPTY;
+				continue;
+			}
+			const TreeNode &c = tree.nodes[kids[k]];
+			float pmn[3], pmx[3];
+			pad_box(c.bmin, c.bmax, pmn, pmx);
+			for (int a = 0; a < 3; a++) {
+				lo[a][k] = pmn[a];
+				hi[a][k] = pmx[a];
+			}
+			if (c.count) {
+				refs[k] = leaf_ref(kids[k]);
+			} else {
+				uint32_t cn = 0;
+				refs[k] = emit(kids[k], cn);
+				child_need = cn > child_need ? cn : child_need;
+			}
+		}
+		nodes[me] = w;
+		need = (uint32_t)(nk - 1) + child_need;
+		return me;
+	};
+	emit(0, max_stack);
+}
+
 } /* namespace kgr */

@@ -146,7 +146,7 @@ struct RegisterSink {
 	f3 x, L_add, next_d, next_beta;
 	float4 pend_c, pend_e, pend_b, sh_o, sh_d;
 	bool add_L = false, shadow = false, cont = false;
-	__device__ __forceinline__ void vertex(const f3 &xv, const f3 &) { x = xv; }
+	__device__ __forceinline__ void vertex(const f3 &xv, const f3 &, const Material &) { x = xv; }
 	__device__ __forceinline__ void emit(const f3 &add)
 	{
 		L_add = add;

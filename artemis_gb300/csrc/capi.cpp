@@ -107,19 +107,21 @@ kgr::DeviceScene kgr_scene::view() const
 	s.bvh = d_bvh.ptr;
 	s.fast_nodes = d_fast_nodes.ptr;
 	s.fast_tris = d_fast_tris.ptr;
+	s.wide_nodes = d_wide_nodes.ptr;
 	s.materials = d_materials.ptr;
 	s.lights = d_lights.ptr;
 	s.triangle_count = (uint32_t)(tris4.size() / 4);
 	s.light_count = (uint32_t)lights.size();
 	s.bvh_vec4_count = (uint32_t)(bvh.size() / 4);
 	s.fast_node_count = fast_node_count;
+	s.wide_node_count = wide_node_count;
 	return s;
 }
 
 uint64_t kgr_scene::device_bytes() const
 {
 	return d_positions.bytes() + d_normals.bytes() + d_tris.bytes() + d_bvh.bytes() + d_fast_tris.bytes()
-		+ d_fast_nodes.bytes() + d_materials.bytes() + d_lights.bytes();
+		+ d_fast_nodes.bytes() + d_wide_nodes.bytes() + d_materials.bytes() + d_lights.bytes();
 }
 
 namespace {
@@ -263,6 +265,13 @@ void finish_scene(kgr_scene *sc, const Tree &tree, const std::vector<PrimBox> &b
 	std::vector<float4> tri_records;
 	build_fast(tree, boxes, sc->positions.data(), sc->tris4.data(), nodes, tri_records);
 	sc->fast_node_count = (uint32_t)nodes.size();
+	std::vector<WideNode> wide;
+	uint32_t wide_stack = 0;
+	build_wide(tree, wide, wide_stack);
+	if (wide_stack >= KGR_STACK_DEPTH_HOST)
+		wide.clear(); /* a walk could overflow the stack: fast layout only */
+	sc->wide_node_count = (uint32_t)wide.size();
+	sc->wide_max_stack = wide.empty() ? 0 : wide_stack;
 	size_t nv = sc->positions.size() / 3, nt = sc->tris4.size() / 4;
 	std::vector<float4> p4(nv), n4(nv);
 	for (size_t v = 0; v < nv; v++) {
@@ -274,6 +283,8 @@ void finish_scene(kgr_scene *sc, const Tree &tree, const std::vector<PrimBox> &b
 	sc->d_tris.upload(reinterpret_cast<const uint4 *>(sc->tris4.data()), nt);
 	sc->d_bvh.upload(reinterpret_cast<const float4 *>(sc->bvh.data()), sc->bvh.size() / 4);
 	sc->d_fast_nodes.upload(nodes);
+	if (!wide.empty())
+		sc->d_wide_nodes.upload(wide);
 	sc->d_fast_tris.upload(tri_records);
 	sc->d_materials.upload(sc->materials);
 	sc->d_lights.upload(sc->lights);
@@ -408,6 +419,8 @@ kgr_status kgr_scene_info_get(const kgr_scene *sc, kgr_scene_info *info)
 		info->build_ms = sc->build_ms;
 		memcpy(info->bounds_min, sc->bounds_min, 12);
 		memcpy(info->bounds_max, sc->bounds_max, 12);
+		info->wide_node_count = sc->wide_node_count;
+		info->wide_max_stack = sc->wide_max_stack;
 	});
 }
 
@@ -448,6 +461,18 @@ kgr_status kgr_scene_destroy(kgr_scene *sc)
 
 /* ============================================================ traversal == */
 
+namespace {
+
+void check_layout(const kgr_scene *sc, int32_t layout)
+{
+	KGR_REQUIRE(layout == KGR_LAYOUT_FAST || layout == KGR_LAYOUT_THREADED || layout == KGR_LAYOUT_WIDE,
+		KGR_ERR_INVALID_ARGUMENT, "unknown layout");
+	KGR_REQUIRE(layout != KGR_LAYOUT_WIDE || sc->wide_node_count, KGR_ERR_UNSUPPORTED,
+		"the scene's wide layout was not built (its worst-case walk exceeds the traversal stack)");
+}
+
+} /* namespace */
+
 kgr_status kgr_trace_closest(const kgr_scene *sc, const float *rays, uint32_t n, kgr_hit *hits, int32_t layout,
 		void *stream)
 {
@@ -455,7 +480,7 @@ kgr_status kgr_trace_closest(const kgr_scene *sc, const float *rays, uint32_t n,
 		KGR_REQUIRE(sc, KGR_ERR_INVALID_ARGUMENT, "scene is NULL");
 		KGR_REQUIRE(n == 0 || (rays && hits), KGR_ERR_INVALID_ARGUMENT, "NULL buffer");
 		KGR_REQUIRE(aligned16(rays) && aligned16(hits), KGR_ERR_INVALID_ARGUMENT, "buffers must be 16-byte aligned");
-		KGR_REQUIRE(layout == KGR_LAYOUT_FAST || layout == KGR_LAYOUT_THREADED, KGR_ERR_INVALID_ARGUMENT, "unknown layout");
+		check_layout(sc, layout);
 		DeviceGuard guard(sc->device);
 		launch_trace_closest(sc->view(), reinterpret_cast<const float4 *>(rays), n, hits, layout,
 			(cudaStream_t)stream);
@@ -469,7 +494,7 @@ kgr_status kgr_trace_any(const kgr_scene *sc, const float *rays, uint32_t n, uin
 		KGR_REQUIRE(sc, KGR_ERR_INVALID_ARGUMENT, "scene is NULL");
 		KGR_REQUIRE(n == 0 || (rays && occluded), KGR_ERR_INVALID_ARGUMENT, "NULL buffer");
 		KGR_REQUIRE(aligned16(rays), KGR_ERR_INVALID_ARGUMENT, "rays must be 16-byte aligned");
-		KGR_REQUIRE(layout == KGR_LAYOUT_FAST || layout == KGR_LAYOUT_THREADED, KGR_ERR_INVALID_ARGUMENT, "unknown layout");
+		check_layout(sc, layout);
 		DeviceGuard guard(sc->device);
 		launch_trace_any(sc->view(), reinterpret_cast<const float4 *>(rays), n, occluded, layout,
 			(cudaStream_t)stream);
@@ -481,7 +506,7 @@ kgr_status kgr_trace_closest_host(const kgr_scene *sc, const float *rays, uint32
 	return guarded([&] {
 		KGR_REQUIRE(sc, KGR_ERR_INVALID_ARGUMENT, "scene is NULL");
 		KGR_REQUIRE(n == 0 || (rays && hits), KGR_ERR_INVALID_ARGUMENT, "NULL buffer");
-		KGR_REQUIRE(layout == KGR_LAYOUT_FAST || layout == KGR_LAYOUT_THREADED, KGR_ERR_INVALID_ARGUMENT, "unknown layout");
+		check_layout(sc, layout);
 		if (n == 0)
 			return;
 		DeviceGuard guard(sc->device);
@@ -499,7 +524,7 @@ kgr_status kgr_trace_any_host(const kgr_scene *sc, const float *rays, uint32_t n
 	return guarded([&] {
 		KGR_REQUIRE(sc, KGR_ERR_INVALID_ARGUMENT, "scene is NULL");
 		KGR_REQUIRE(n == 0 || (rays && occluded), KGR_ERR_INVALID_ARGUMENT, "NULL buffer");
-		KGR_REQUIRE(layout == KGR_LAYOUT_FAST || layout == KGR_LAYOUT_THREADED, KGR_ERR_INVALID_ARGUMENT, "unknown layout");
+		check_layout(sc, layout);
 		if (n == 0)
 			return;
 		DeviceGuard guard(sc->device);
@@ -652,7 +677,38 @@ struct kgr_attachment {
 			return *p;
 		return def;
 	}
-	int layout() const { return opt_str("layout", "fast") == "threaded" ? KGR_LAYOUT_THREADED : KGR_LAYOUT_FAST; }
+	/* The layout option ("fast" | "threaded" | "wide"); unset, the layout
+	 * kgr_autotune chose (fast when nothing was tuned). */
+	int tuned_layout = KGR_LAYOUT_FAST;
+	int layout() const
+	{
+		std::string l = opt_str("layout", "");
+		if (l == "threaded")
+			return KGR_LAYOUT_THREADED;
+		if (l == "fast")
+			return KGR_LAYOUT_FAST;
+		if (l == "wide")
+			return KGR_LAYOUT_WIDE;
+		return tuned_layout;
+	}
+
+	/* Launch shape of the fast/wide traversal: the shape kgr_autotune chose
+	 * (or the default), with any field the options set overriding it:
+	 * trace_shadow "grid" | "persistent", trace_block 64 | 128 | 256. */
+	TraceTune tuned = default_trace_tune();
+	TraceTune trace_tune() const
+	{
+		TraceTune t = tuned;
+		std::string a = opt_str("trace_shadow", "");
+		if (a == "grid")
+			t.shadow = TRACE_GRID;
+		else if (a == "persistent")
+			t.shadow = TRACE_PERSISTENT;
+		int b = opt_int("trace_block", 0);
+		if (b == 64 || b == 128 || b == 256)
+			t.block = (int16_t)b;
+		return t;
+	}
 
 	PathBuffers path_buffers()
 	{
@@ -799,7 +855,7 @@ void check_launch(const kgr_attachment *att, const kgr_launch_info *info, const 
 	KGR_REQUIRE(info->max_depth >= 0 && info->max_depth <= 64, KGR_ERR_INVALID_ARGUMENT, "max_depth out of range");
 }
 
-FrameParams frame_params(const kgr_attachment *att, const kgr_launch_info *info)
+FrameParams frame_params(const kgr_attachment *att, const kgr_launch_info *info, const kgr_scene *sc)
 {
 	FrameParams fp;
 	memset(&fp, 0, sizeof(fp));
@@ -817,7 +873,8 @@ FrameParams frame_params(const kgr_attachment *att, const kgr_launch_info *info)
 	fp.frame = info->frame;
 	fp.accumulate = info->accumulate ? 1 : 0;
 	fp.samples = info->samples;
-	fp.layout = att->layout();
+	fp.layout = layout_for(att->layout(), sc);
+	fp.tune = att->trace_tune();
 	fp.candidates = att->opt_int("candidates", 32);
 	fp.temporal = att->opt_int("temporal", 1);
 	fp.temporal_mcap = att->opt_int("temporal_mcap", 200);
@@ -850,7 +907,7 @@ void prepare_visits(kgr_attachment *att, cudaStream_t st)
 
 void render_pt(kgr_attachment *att, const kgr_launch_info *info, const kgr_scene *sc, cudaStream_t st)
 {
-	FrameParams fp = frame_params(att, info);
+	FrameParams fp = frame_params(att, info, sc);
 	int spp = att->opt_int("spp", 1);
 	KGR_REQUIRE(spp >= 1 && spp <= 4096, KGR_ERR_INVALID_ARGUMENT, "spp out of range");
 	uint64_t paths = (uint64_t)fp.npix * (uint64_t)spp;
@@ -876,11 +933,11 @@ void render_pt(kgr_attachment *att, const kgr_launch_info *info, const kgr_scene
 			reset_counters(pb, (1 << (q ^ 1)) | (1 << CNT_SHADOW), st);
 			att->mark(-1, st);
 		}
-		pt_trace_closest(s, pb, q, fp.layout, st);
+		pt_trace_closest(s, pb, q, fp.layout, fp.tune, st);
 		att->mark(STAGE_TRACE_CLOSEST, st);
 		pt_shade(s, pb, fp, d, q, st);
 		att->mark(STAGE_SHADE, st);
-		pt_shadow_resolve(s, pb, fp.layout, st);
+		pt_shadow_resolve(s, pb, fp.layout, fp.tune, st);
 		att->mark(STAGE_SHADOW, st);
 		launches += 3;
 	}
@@ -894,7 +951,7 @@ void render_pt(kgr_attachment *att, const kgr_launch_info *info, const kgr_scene
 
 void render_restir_di(kgr_attachment *att, const kgr_launch_info *info, const kgr_scene *sc, cudaStream_t st)
 {
-	FrameParams fp = frame_params(att, info);
+	FrameParams fp = frame_params(att, info, sc);
 	fp.spp = 1;
 	fp.paths = fp.npix;
 	fp.jitter = 0;
@@ -932,7 +989,7 @@ void render_restir_di(kgr_attachment *att, const kgr_launch_info *info, const kg
 	att->mark(-1, st);
 	pt_generate(pb, fp, st);
 	att->mark(STAGE_GENERATE, st);
-	pt_trace_closest(s, pb, 0, fp.layout, st);
+	pt_trace_closest(s, pb, 0, fp.layout, fp.tune, st);
 	att->mark(STAGE_TRACE_CLOSEST, st);
 	restir_primary(s, pb, fp, rb, cur, st);
 	att->mark(STAGE_RESTIR_PRIMARY, st);
@@ -941,11 +998,11 @@ void render_restir_di(kgr_attachment *att, const kgr_launch_info *info, const kg
 		int q = d & 1;
 		reset_counters(pb, (1 << (q ^ 1)) | (1 << CNT_SHADOW), st);
 		att->mark(-1, st);
-		pt_trace_closest(s, pb, q, fp.layout, st);
+		pt_trace_closest(s, pb, q, fp.layout, fp.tune, st);
 		att->mark(STAGE_TRACE_CLOSEST, st);
 		pt_shade_final_seed(s, pb, fp, d, q, st);
 		att->mark(STAGE_SHADE, st);
-		pt_shadow_resolve(s, pb, fp.layout, st);
+		pt_shadow_resolve(s, pb, fp.layout, fp.tune, st);
 		att->mark(STAGE_SHADOW, st);
 		launches += 3;
 	}
@@ -980,7 +1037,7 @@ void render_restir_di(kgr_attachment *att, const kgr_launch_info *info, const kg
  * with a network query; training paths (plain, full depth) train it. */
 void render_pt_cached(kgr_attachment *att, const kgr_launch_info *info, const kgr_scene *sc, cudaStream_t st)
 {
-	FrameParams fp = frame_params(att, info);
+	FrameParams fp = frame_params(att, info, sc);
 	int spp = att->opt_int("spp", 1);
 	KGR_REQUIRE(spp >= 1 && spp <= 4096, KGR_ERR_INVALID_ARGUMENT, "spp out of range");
 	KGR_REQUIRE(fp.max_depth >= 1, KGR_ERR_INVALID_ARGUMENT, "the cached tracer needs max_depth >= 1");
@@ -1065,15 +1122,15 @@ void render_pt_cached(kgr_attachment *att, const kgr_launch_info *info, const kg
 	att->mark(-1, st);
 	pt_generate(pb, fp, st);
 	att->mark(STAGE_GENERATE, st);
-	pt_trace_closest(s, pb, 0, fp.layout, st);
+	pt_trace_closest(s, pb, 0, fp.layout, fp.tune, st);
 	att->mark(STAGE_TRACE_CLOSEST, st);
 	pt_shade(s, pb, fp, 0, 0, st);
 	att->mark(STAGE_SHADE, st);
-	pt_shadow_resolve(s, pb, fp.layout, st);
+	pt_shadow_resolve(s, pb, fp.layout, fp.tune, st);
 	att->mark(STAGE_SHADOW, st);
 	reset_counters(pb, (1 << CNT_Q0) | (1 << CNT_SHADOW), st);
 	att->mark(-1, st);
-	pt_trace_closest(s, pb, 1, fp.layout, st);
+	pt_trace_closest(s, pb, 1, fp.layout, fp.tune, st);
 	att->mark(STAGE_TRACE_CLOSEST, st);
 	cache_query(s, pb, 1, cp, att->q_feat.ptr, att->q_le.ptr, st);
 	mlp_infer(mp, att->q_feat.ptr, att->capacity, att->q_out.ptr, st, pb.counters + CNT_Q1);
@@ -1106,7 +1163,7 @@ void render_pt_cached(kgr_attachment *att, const kgr_launch_info *info, const kg
  * temporal reuse, spatial iterations (ping-pong), final shading. */
 void render_restir_gi(kgr_attachment *att, const kgr_launch_info *info, const kgr_scene *sc, cudaStream_t st)
 {
-	FrameParams fp = frame_params(att, info);
+	FrameParams fp = frame_params(att, info, sc);
 	fp.spp = 1;
 	fp.paths = fp.npix;
 	fp.jitter = 1;
@@ -1151,7 +1208,7 @@ void render_restir_gi(kgr_attachment *att, const kgr_launch_info *info, const kg
 	att->mark(-1, st);
 	pt_generate(pb, fp, st);
 	att->mark(STAGE_GENERATE, st);
-	pt_trace_closest(s, pb, 0, fp.layout, st);
+	pt_trace_closest(s, pb, 0, fp.layout, fp.tune, st);
 	att->mark(STAGE_TRACE_CLOSEST, st);
 	gi_primary(s, pb, fp, gb, st);
 	att->mark(STAGE_RESTIR_PRIMARY, st);
@@ -1160,11 +1217,11 @@ void render_restir_gi(kgr_attachment *att, const kgr_launch_info *info, const kg
 		int q = d & 1;
 		reset_counters(pb, (1 << (q ^ 1)) | (1 << CNT_SHADOW), st);
 		att->mark(-1, st);
-		pt_trace_closest(s, pb, q, fp.layout, st);
+		pt_trace_closest(s, pb, q, fp.layout, fp.tune, st);
 		att->mark(STAGE_TRACE_CLOSEST, st);
 		pt_shade_final_seed(s, pb, fp, d, q, st);
 		att->mark(STAGE_SHADE, st);
-		pt_shadow_resolve(s, pb, fp.layout, st);
+		pt_shadow_resolve(s, pb, fp.layout, fp.tune, st);
 		att->mark(STAGE_SHADOW, st);
 		launches += 3;
 	}
@@ -1337,7 +1394,8 @@ static const std::map<std::string, OptionValue> &option_defaults()
 		{"gi_temporal", true}, {"gi_mcap", 30}, {"gi_spatial_iterations", 3}, {"gi_neighbors", 8},
 		{"gi_radius", 30},
 		{"cache", false}, {"cache_train", true}, {"cache_train_paths", 16384}, {"cache_lr", 1e-3f},
-		{"cache_dtype", std::string("bf16")}, {"reset_history", false}};
+		{"cache_dtype", std::string("bf16")}, {"reset_history", false},
+		{"trace_shadow", std::string("")}, {"trace_block", 0}};
 	return d;
 }
 
@@ -1362,7 +1420,8 @@ kgr_status kgr_set_option(kgr_attachment *att, const char *name, const kgr_value
 		KGR_REQUIRE(v.index() == it->second.index(), KGR_ERR_TYPE, std::string("wrong type for option ") + name);
 		if (std::string(name) == "layout") {
 			const std::string &s = std::get<std::string>(v);
-			KGR_REQUIRE(s == "fast" || s == "threaded", KGR_ERR_INVALID_ARGUMENT, "layout is fast or threaded");
+			KGR_REQUIRE(s == "fast" || s == "threaded" || s == "wide", KGR_ERR_INVALID_ARGUMENT,
+				"layout is fast, threaded or wide");
 		}
 		att->options[name] = v;
 	});

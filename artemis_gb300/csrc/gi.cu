@@ -4,29 +4,57 @@
  * The reference has no working ReSTIR GI (its PathSample reservoirs in
  * include/optix/parameters.cuh:34-60 are never read by compiled code; a
  * dormant sketch lies in source/layers/optix_rt.cu:670-856).  This follows
- * that sketch where it is specific -- target function = the largest
- * component of the sample radiance, neighbours rejected when their normals
- * differ by more than 10 degrees or their depth by more than 10% -- and
- * otherwise the reconnection-shift formulation of ReSTIR GI:
+ * that sketch where it is specific -- neighbours rejected when their
+ * normals differ by more than 10 degrees or their depth by more than 10% --
+ * and otherwise the reconnection-shift formulation of ReSTIR GI:
  *
  *  sample     x_s, n_s: the secondary vertex; L_o: radiance leaving x_s
  *             toward the primary vertex x_v (emission + NEE + the rest of
  *             the path, max depth as configured)
+ *  target     p^_q(s) = sum_rgb(f_q(w) L_o) |n_q . w|, w = x_s - x_q
+ *             normalised: the sample's contribution at receiver q.  The
+ *             sketch's target (the largest component of L_o alone) leaves
+ *             the receiver's BSDF out, so a neighbour's sample that lands in
+ *             a narrow GGX lobe of q gets weight ~1/pdf of another surface
+ *             and shades as a firefly; with the BSDF in the target the
+ *             shaded value f L_o |n.w| W is w_sum / Z up to colour.
  *  initial    BSDF-sampled direction at x_v, source pdf p;
- *             w = p^(L_o) / p, M = 1
+ *             w = p^_v(s) / p, M = 1
  *  shift      reusing a sample created at receiver x_r for receiver x_q
  *             multiplies its weight by the Jacobian
  *             |J| = (|cos phi_q| / |cos phi_r|) (|x_r - x_s|^2 / |x_q - x_s|^2),
  *             phi the angle at x_s between n_s and the receiver
  *  temporal   previous frame's reservoir at the reprojected pixel, M capped
- *  spatial    k neighbours in a disk, shadow ray to each reused sample,
- *             bias correction over the neighbours that can see the result
- *  weights    W = w_sum / (Z p^(sample)) evaluated in FP64
+ *  spatial    k neighbours in a disk, shadow ray to each reused sample
+ *  weights    candidates are resampled with w_i = p^_q(y_i) |J_i| W_i M_i;
+ *             the selected y (from domain j) gets the balance-heuristic
+ *             contribution weight (Bitterli et al. 2020, the MIS form of
+ *             their unbiased combination, with confidence weights M):
+ *               W = p^<-j(y) w_sum / (p^_q(y) D),
+ *               D = sum_i M_i p^<-i(y),  p^<-i(y) = p^_i(y) |J_q->i| v_i(y)
+ *             over the centre, and the history or the neighbours; v_i is
+ *             a visibility ray from receiver i (taken as 1 for the
+ *             history).  The uniform 1/Z weight it replaces keeps W ~
+ *             1/p^_q(y), which a neighbour with a much larger p^ for the
+ *             same sample turns into an unbounded contribution; here the
+ *             small p^_q(y) cancels in the neighbour's weight.  Normalised
+ *             in FP64.
  *  shading    f(x_v, w) L_o |n_v . w| W with a visibility ray, plus the
  *             primary vertex's emission and its ReSTIR DI direct light
  *
+ *  reconnect  only samples whose secondary vertex is rough (gi_reconnectable)
+ *             move to another pixel's receiver: spatial candidates that are
+ *             not are skipped, and a selected sample that is not can only
+ *             have come from the centre.  The history at the reprojected
+ *             pixel is reused whatever its vertex (the receiver moves by
+ *             less than a pixel).
+ *
  * Reservoirs are 32 bytes in two 16-byte SoA arrays:
- *   a = {x_s.xyz, bits(n_s octahedral 12+12, M 8)},  b = {L_o.rgb, W}.
+ *   a = {x_s.xyz, bits(n_s octahedral 12+12, M 8)},
+ *   b = {L_o.rgb, W with its sign bit set when the sample is not
+ *        reconnectable}.
+ * The G-buffer position's w holds the pixel's material index + 1 (0: no
+ * hit), so the history's receiver is known one frame later.
  */
 #include "kgr_device.cuh"
 #include "kgr_gi.h"
@@ -37,12 +65,20 @@ namespace {
 
 #define KGR_GI_RIS_SALT 0x9E3779B9u
 #define KGR_GI_COS_10DEG 0.984807753f
+/* A shift whose Jacobian leaves [1/10, 10] is invalid: reconnecting to a
+ * secondary vertex much nearer one receiver than the other (a crease, a
+ * contact) scales the sample's weight without bound.  The range is closed
+ * under inversion, so the bias correction -- which shifts the selected
+ * sample back to each neighbour -- sees the same domains. */
+#define KGR_GI_JACOBIAN_MIN 0.1f
+#define KGR_GI_JACOBIAN_MAX 10.0f
 
 __device__ __forceinline__ f3 v3(const float *p) { return mk(p[0], p[1], p[2]); }
 
 struct GiSample {
 	f3 xs, ns, Lo;
 	bool valid;
+	bool rc; /* reconnectable */
 };
 
 struct GiRes {
@@ -60,7 +96,8 @@ __device__ __forceinline__ GiRes load_gi(const GiReservoirs &r, uint32_t i)
 	g.s.ns = unpack_normal(w);
 	g.s.Lo = mk(b.x, b.y, b.z);
 	g.s.valid = true;
-	g.W = b.w;
+	g.s.rc = !signbit(b.w);
+	g.W = fabsf(b.w);
 	g.M = unpack_m(w);
 	return g;
 }
@@ -68,31 +105,37 @@ __device__ __forceinline__ GiRes load_gi(const GiReservoirs &r, uint32_t i)
 __device__ __forceinline__ void store_gi(const GiReservoirs &r, uint32_t i, const GiSample &s, float W, int32_t M)
 {
 	r.a[i] = make_float4(s.xs.x, s.xs.y, s.xs.z, __uint_as_float(pack_normal_m(s.ns, M)));
-	r.b[i] = make_float4(s.Lo.x, s.Lo.y, s.Lo.z, W);
+	r.b[i] = make_float4(s.Lo.x, s.Lo.y, s.Lo.z, s.rc ? W : -W);
 }
 
-/* Weighted reservoir over GI samples (reservoir.cuh:43-56 update rule). */
+/* Weighted reservoir over GI samples (reservoir.cuh:43-56 update rule);
+ * src records the domain of the selected sample (-1: the centre). */
 struct GiMerge {
 	GiSample sel;
 	float w;
+	int32_t src;
 	f3 seed;
 	__device__ __forceinline__ void init(const f3 &s)
 	{
 		sel.xs = sel.ns = sel.Lo = mk(0.0f);
 		sel.valid = false;
+		sel.rc = true;
 		w = 0.0f;
+		src = -1;
 		seed = s;
 	}
-	__device__ __forceinline__ void update(const GiSample &s, float weight)
+	__device__ __forceinline__ void update(const GiSample &s, float weight, int32_t from)
 	{
 		w += weight;
 		float eta = rand_uniform(seed);
-		if ((eta * w) < weight)
+		if ((eta * w) < weight) {
 			sel = s;
+			src = from;
+		}
 	}
 };
 
-/* W = w_sum / (Z p^) in double precision */
+/* W = w_sum / p^ of a single candidate (M = 1), in double precision */
 __device__ __forceinline__ float gi_normalise(float w_sum, int32_t Z, float target)
 {
 	if (!(target > 0.0f) || Z <= 0)
@@ -100,7 +143,16 @@ __device__ __forceinline__ float gi_normalise(float w_sum, int32_t Z, float targ
 	return (float)((double)w_sum / ((double)Z * (double)target));
 }
 
-/* Solid-angle Jacobian of moving a sample's receiver from xr to xq. */
+/* Balance-heuristic contribution weight W = num w_sum / (D p^_q), FP64. */
+__device__ __forceinline__ float gi_mis_weight(float w_sum, float num, float D, float target)
+{
+	if (!(target > 0.0f) || !(D > 0.0f))
+		return 0.0f;
+	return (float)(((double)num * (double)w_sum) / ((double)D * (double)target));
+}
+
+/* Solid-angle Jacobian of moving a sample's receiver from xr to xq; 0 for
+ * an invalid shift. */
 __device__ __forceinline__ float gi_jacobian(const f3 &xq, const f3 &xr, const GiSample &s)
 {
 	f3 dq = xq - s.xs, dr = xr - s.xs;
@@ -108,7 +160,7 @@ __device__ __forceinline__ float gi_jacobian(const f3 &xq, const f3 &xr, const G
 	float cq = fabsf(dot(s.ns, dq)) / ksqrt(lq2);
 	float cr = fabsf(dot(s.ns, dr)) / ksqrt(lr2);
 	float j = (cq / cr) * (lr2 / lq2);
-	return (j > 0.0f && j < 1e30f) ? j : 0.0f;
+	return (j >= KGR_GI_JACOBIAN_MIN && j <= KGR_GI_JACOBIAN_MAX) ? j : 0.0f;
 }
 
 __device__ __forceinline__ bool visible(const DeviceScene &s, int layout, const f3 &from, const f3 &to)
@@ -122,6 +174,7 @@ __device__ __forceinline__ bool visible(const DeviceScene &s, int layout, const 
 struct GBuf {
 	f3 x, n;
 	bool hit;
+	uint32_t mat; /* material index (valid when hit) */
 };
 
 __device__ __forceinline__ GBuf gbuf(const float4 *pos, const float4 *nrm, uint32_t i)
@@ -131,6 +184,7 @@ __device__ __forceinline__ GBuf gbuf(const float4 *pos, const float4 *nrm, uint3
 	g.x = mk(p.x, p.y, p.z);
 	g.n = mk(n.x, n.y, n.z);
 	g.hit = p.w > 0.0f;
+	g.mat = g.hit ? (uint32_t)p.w - 1u : 0u;
 	return g;
 }
 
@@ -155,6 +209,30 @@ __device__ __forceinline__ SurfaceHit receiver(const FrameParams &fp, const GiFr
 	h.wo = normalize(v3(fp.center) - g.x);
 	h.x = g.x;
 	return h;
+}
+
+/* The receiver of the previous frame's pixel: its material by index, the
+ * direction toward the previous camera centre. */
+__device__ __forceinline__ SurfaceHit receiver_prev(const DeviceScene &s, const FrameParams &fp, const GBuf &g)
+{
+	SurfaceHit h;
+	h.mat = load_material(s.materials, g.mat);
+	h.entering = false;
+	h.n = g.n;
+	h.wo = normalize(v3(fp.prev_center) - g.x);
+	h.x = g.x;
+	return h;
+}
+
+/* Target function of sample s at receiver h: sum_rgb(f L_o) |n.w|. */
+__device__ __forceinline__ float gi_target(const SurfaceHit &h, const GiSample &s)
+{
+	f3 D = s.xs - h.x;
+	float d = length(D);
+	f3 w = D / d;
+	f3 v = brdf(h, w) * s.Lo * fabsf(dot(h.n, w));
+	float t = v.x + v.y + v.z;
+	return (t > 0.0f && t < 1e30f) ? t : 0.0f;
 }
 
 /* Primary vertex: G-buffer, ReSTIR DI candidates for direct light, and the
@@ -188,9 +266,9 @@ __global__ void __launch_bounds__(128) gi_primary_kernel(DeviceScene s, PathBuff
 				f3 n3 = sh.n;
 				float sgn = sh.mat.type == KGR_SHADING_TRANSMISSION ? -1.0f : 1.0f;
 				sh.x = sh.x + sgn * n3 * KGR_OFFSET_EPS;
-				gb.position[p] = f4_of(sh.x, 1.0f);
-				gb.normal[p] = f4_of(n3, 0.0f);
 				uint4 tr = __ldg(&s.tris[h.prim]);
+				gb.position[p] = f4_of(sh.x, (float)(tr.w + 1u));
+				gb.normal[p] = f4_of(n3, 0.0f);
 				const float4 *src = reinterpret_cast<const float4 *>(s.materials + tr.w);
 				float4 *dst = reinterpret_cast<float4 *>(gb.materials + p);
 				for (int k = 0; k < 4; k++)
@@ -274,15 +352,18 @@ __global__ void gi_initial_kernel(PathBuffers pb, FrameParams fp, GiFrameBuffers
 	smp.xs = mk(xs.x, xs.y, xs.z);
 	smp.ns = mk(ns.x, ns.y, ns.z);
 	smp.Lo = mk(L.x, L.y, L.z);
-	bool valid = dir.w > 0.0f && xs.w > 0.0f && !anynan(smp.Lo);
+	smp.rc = ns.w > 0.0f;
+	GBuf g = gbuf(gb.position, gb.normal, pix);
+	bool valid = g.hit && dir.w > 0.0f && xs.w > 0.0f && !anynan(smp.Lo);
 	float W = 0.0f;
 	if (valid) {
-		float target = max3(smp.Lo);
+		float target = gi_target(receiver(fp, gb, pix, g), smp);
 		float w = target / dir.w;
 		W = gi_normalise(w, 1, target);
 	} else {
 		smp.xs = smp.Lo = mk(0.0f);
 		smp.ns = mk(0.0f, 0.0f, 1.0f);
+		smp.rc = true;
 	}
 	store_gi(gb.res[cur], pix, smp, W, 1);
 	float4 sv = pb.seed[pix];
@@ -330,15 +411,26 @@ __global__ void __launch_bounds__(128) gi_temporal_kernel(DeviceScene s, FramePa
 		return;
 	GiRes C = load_gi(gb.res[cur], pix);
 	int32_t pM = P.M < fp.gi_mcap ? P.M : fp.gi_mcap;
+	SurfaceHit h = receiver(fp, gb, pix, g);
 	float4 av = gb.auxiliary[pix];
 	GiMerge r;
 	r.init(mk(av.x, av.y, av.z));
-	r.update(C.s, max3(C.s.Lo) * C.W * C.M);
+	r.update(C.s, gi_target(h, C.s) * C.W * C.M, -1);
 	float J = gi_jacobian(g.x, gp.x, P.s);
-	float wp = max3(P.s.Lo) * J * P.W * pM;
-	r.update(P.s, wp);
-	int32_t M = C.M + (wp > 0.0f ? pM : 0);
-	float W = gi_normalise(r.w, M, max3(r.sel.Lo));
+	float wp = gi_target(h, P.s) * J * P.W * pM;
+	r.update(P.s, wp, 0);
+	/* The history counts toward the normalisation whether or not its own
+	 * sample carries weight: an empty history reservoir (its GI ray found
+	 * nothing) is pM candidates of the same domain that all came out zero.
+	 * Dropping it -- the DI rule of counting the previous M only when its
+	 * sample's target is positive -- divides by too few candidates and
+	 * brightens pixels whose GI samples are often empty. */
+	int32_t M = C.M + pM;
+	float tq = gi_target(h, r.sel);
+	float jp = gi_jacobian(gp.x, g.x, r.sel);
+	float tp = jp > 0.0f ? gi_target(receiver_prev(s, fp, gp), r.sel) * jp : 0.0f;
+	float D = (float)C.M * tq + (float)pM * tp;
+	float W = gi_mis_weight(r.w, r.src < 0 ? tq : tp, D, tq);
 	store_gi(gb.res[cur], pix, r.sel, W, M);
 }
 
@@ -375,10 +467,11 @@ __global__ void __launch_bounds__(128) gi_spatial_kernel(DeviceScene s, FramePar
 		return;
 	}
 	float depth = length(g.x - v3(fp.center));
+	SurfaceHit h = receiver(fp, gb, pix, g);
 	float4 av = gb.auxiliary[pix];
 	GiMerge r;
 	r.init(mk(av.x, av.y, av.z));
-	r.update(C.s, max3(C.s.Lo) * C.W * C.M);
+	r.update(C.s, gi_target(h, C.s) * C.W * C.M, -1);
 	int32_t nidx[KGR_GI_MAX_NEIGHBORS];
 	int32_t nM[KGR_GI_MAX_NEIGHBORS];
 	int32_t Msum = C.M;
@@ -395,26 +488,32 @@ __global__ void __launch_bounds__(128) gi_spatial_kernel(DeviceScene s, FramePar
 		nidx[k] = index0;
 		nM[k] = N.M;
 		Msum += N.M;
-		float J = gi_jacobian(g.x, gn.x, N.s);
-		float wn = max3(N.s.Lo) * J * N.W * N.M;
+		float J = N.s.rc ? gi_jacobian(g.x, gn.x, N.s) : 0.0f;
+		float wn = J > 0.0f ? gi_target(h, N.s) * J * N.W * N.M : 0.0f;
 		if (wn > 0.0f && !visible(s, fp.layout, g.x, N.s.xs))
 			wn = 0.0f;
-		r.update(N.s, wn);
+		r.update(N.s, wn, k);
 	}
-	/* bias correction: the centre and every neighbour whose receiver sees
-	 * the selected sample through a valid shift */
-	int32_t Z = C.M;
-	float target = max3(r.sel.Lo);
-	if (target > 0.0f) {
+	/* balance heuristic over the centre and every neighbour domain: the
+	 * selected sample shifted back to each receiver, with its visibility */
+	float target = gi_target(h, r.sel);
+	float D = (float)C.M * target;
+	float num = r.src < 0 ? target : 0.0f;
+	if (target > 0.0f && r.sel.rc) {
 		for (int k = 0; k < fp.gi_neighbors; k++) {
 			if (nidx[k] < 0)
 				continue;
 			GBuf gn = gbuf(gb.position, gb.normal, (uint32_t)nidx[k]);
-			if (gi_jacobian(gn.x, g.x, r.sel) > 0.0f && visible(s, fp.layout, gn.x, r.sel.xs))
-				Z += nM[k];
+			float jn = gi_jacobian(gn.x, g.x, r.sel);
+			float tn = jn > 0.0f ? gi_target(receiver(fp, gb, (uint32_t)nidx[k], gn), r.sel) * jn : 0.0f;
+			if (tn > 0.0f && !visible(s, fp.layout, gn.x, r.sel.xs))
+				tn = 0.0f;
+			D += (float)nM[k] * tn;
+			if (k == r.src)
+				num = tn;
 		}
 	}
-	float W = gi_normalise(r.w, Z, target);
+	float W = gi_mis_weight(r.w, num, D, target);
 	store_gi(gb.res[out], pix, r.sel, W, Msum);
 }
 

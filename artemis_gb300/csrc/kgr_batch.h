@@ -59,9 +59,12 @@ struct kgr_batcher {
 	cudaEvent_t done[RING] = {};
 	int ring = 0, last = -1;
 	cudaStream_t capture_stream = nullptr;
+	/* launch shape of the traversal stages (kgr_batcher_set_tune) */
+	kgr::TraceTune tune = kgr::default_trace_tune();
 	struct Graph {
 		const kgr_scene *scene;
 		int max_depth, rr, rr_start, layout;
+		kgr::TraceTune tune;
 		int eager_runs;
 		cudaGraphExec_t exec;
 	};

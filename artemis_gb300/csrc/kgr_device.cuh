@@ -210,50 +210,142 @@ __device__ __forceinline__ int fast_node(const DeviceScene &s, const FastRay &r,
 	return (hl || hr) ? 1 : 0;
 }
 
-/* The triangles of one leaf.  Closest hit: a triangle replaces the best when
- * 0 < t < best, or t == best and its rank (position in the threaded walk)
- * is lower -- the primitive the reference's strict `t < best` walk keeps.
- * Any hit: returns true at the first triangle with 0 < t < tmax. */
+/* One triangle (record `idx` of the walk-ordered triangle array).  Closest
+ * hit: it replaces the best when 0 < t < best, or t == best and its rank
+ * (position in the threaded walk) is lower -- the primitive the reference's
+ * strict `t < best` walk keeps.  Any hit: returns true when 0 < t < tmax. */
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ bool fast_triangle(const DeviceScene &s, const FastRay &r, uint32_t idx,
+		kgr_hit &best, int32_t &best_rank, TraceCounters *cnt)
+{
+	if (COUNT)
+		cnt->tris++;
+	const float4 *tp = s.fast_tris + 3 * (size_t)idx;
+	float4 a = __ldg(tp + 0);
+	float4 e1 = __ldg(tp + 1);
+	float4 e2 = __ldg(tp + 2);
+	float b1 = 0.0f, b2 = 0.0f;
+	float tt = mt_test(f3_of(a), f3_of(e1), f3_of(e2), r.o, r.d, b1, b2);
+	if (ANY) {
+		if (tt > 0.0f && tt < best.t) {
+			best.prim = ibits(a.w);
+			best.t = tt;
+			return true;
+		}
+		return false;
+	}
+	int32_t rank = (int32_t)idx;
+	if (tt > 0.0f && (tt < best.t || (tt == best.t && rank < best_rank))) {
+		best.prim = ibits(a.w);
+		best.t = tt;
+		best.b1 = b1;
+		best.b2 = b2;
+		best_rank = rank;
+	}
+	return false;
+}
+
+/* The triangles of one leaf (fast_triangle for each).  Any hit: returns true
+ * at the first triangle with 0 < t < tmax. */
 template <bool ANY, bool COUNT>
 __device__ __forceinline__ bool fast_leaf(const DeviceScene &s, const FastRay &r, int32_t ref, kgr_hit &best,
 		int32_t &best_rank, TraceCounters *cnt)
 {
 	uint32_t code = ~(uint32_t)ref;
 	uint32_t start = code >> 3, n = (code & 7u) + 1u;
-	const float4 *tp = s.fast_tris + 3 * (size_t)start;
-	for (uint32_t k = 0; k < n; k++) {
-		if (COUNT)
-			cnt->tris++;
-		float4 a = __ldg(tp + 3 * k + 0);
-		float4 e1 = __ldg(tp + 3 * k + 1);
-		float4 e2 = __ldg(tp + 3 * k + 2);
-		float b1 = 0.0f, b2 = 0.0f;
-		float tt = mt_test(f3_of(a), f3_of(e1), f3_of(e2), r.o, r.d, b1, b2);
-		if (ANY) {
-			if (tt > 0.0f && tt < best.t) {
-				best.prim = ibits(a.w);
-				best.t = tt;
-				return true;
-			}
-			continue;
-		}
-		int32_t rank = (int32_t)(start + k);
-		if (tt > 0.0f && (tt < best.t || (tt == best.t && rank < best_rank))) {
-			best.prim = ibits(a.w);
-			best.t = tt;
-			best.b1 = b1;
-			best.b2 = b2;
-			best_rank = rank;
-		}
-	}
+	for (uint32_t k = 0; k < n; k++)
+		if (fast_triangle<ANY, COUNT>(s, r, start + k, best, best_rank, cnt))
+			return true;
 	return false;
 }
 
-/* Ordered descent over 64-byte child-pair nodes with a per-thread stack.
- * Box culling keeps every child whose padded slab interval reaches
- * [0, best]; the build pads boxes so that no triangle the exact test accepts
- * is culled. */
-template <bool ANY, bool COUNT>
+/* Slab test of one child of a wide node, the arithmetic of fast_node:
+ * its near distance when the ray reaches the padded box within
+ * [0, best_t], +inf otherwise (or for an unused slot). */
+__device__ __forceinline__ float wide_child(const FastRay &r, float lx, float hx, float ly, float hy, float lz,
+		float hz, int32_t ref, float best_t)
+{
+	float x0 = __fmaf_rn(lx, r.ix, -r.ox), x1 = __fmaf_rn(hx, r.ix, -r.ox);
+	float y0 = __fmaf_rn(ly, r.iy, -r.oy), y1 = __fmaf_rn(hy, r.iy, -r.oy);
+	float z0 = __fmaf_rn(lz, r.iz, -r.oz), z1 = __fmaf_rn(hz, r.iz, -r.oz);
+	float tn = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), 0.0f));
+	float tf = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fmaxf(z0, z1));
+	return (ref != KGR_WIDE_EMPTY && tn <= tf && tn <= best_t) ? tn : __int_as_float(0x7f800000);
+}
+
+/* Order two (distance, reference) pairs, nearer first. */
+__device__ __forceinline__ void order_pair(float &ta, int32_t &ca, float &tb, int32_t &cb)
+{
+	bool s = tb < ta;
+	float t = s ? tb : ta;
+	int32_t c = s ? cb : ca;
+	tb = s ? ta : tb;
+	cb = s ? ca : cb;
+	ta = t;
+	ca = c;
+}
+
+/* One interior node of the fast (BVH2) or wide (BVH4) layout: `ref`
+ * becomes the nearest child whose padded box the ray reaches within
+ * [0, best_t] and the other reached children are pushed, farthest first;
+ * with none reached, `ref` is popped.  Returns false when there was nothing
+ * to pop: the walk is over. */
+template <int LAYOUT>
+__device__ __forceinline__ bool node_step(const DeviceScene &s, const FastRay &r, int32_t &ref, float best_t,
+		int32_t *stack, int &sp)
+{
+	if (LAYOUT == KGR_LAYOUT_WIDE) {
+		const float4 *np = reinterpret_cast<const float4 *>(s.wide_nodes + ref);
+		float4 lx = __ldg(np + 0), hx = __ldg(np + 1), ly = __ldg(np + 2);
+		float4 hy = __ldg(np + 3), lz = __ldg(np + 4), hz = __ldg(np + 5);
+		int4 rf = __ldg(reinterpret_cast<const int4 *>(np + 6));
+		float t0 = wide_child(r, lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, rf.x, best_t);
+		float t1 = wide_child(r, lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, rf.y, best_t);
+		float t2 = wide_child(r, lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, rf.z, best_t);
+		float t3 = wide_child(r, lx.w, hx.w, ly.w, hy.w, lz.w, hz.w, rf.w, best_t);
+		int32_t c0 = rf.x, c1 = rf.y, c2 = rf.z, c3 = rf.w;
+		order_pair(t0, c0, t1, c1);
+		order_pair(t2, c2, t3, c3);
+		order_pair(t0, c0, t2, c2);
+		order_pair(t1, c1, t3, c3);
+		order_pair(t1, c1, t2, c2);
+		const float inf = __int_as_float(0x7f800000);
+		if (!(t0 < inf)) {
+			if (sp == 0)
+				return false;
+			ref = stack[--sp];
+			return true;
+		}
+		if (t3 < inf)
+			stack[sp++] = c3;
+		if (t2 < inf)
+			stack[sp++] = c2;
+		if (t1 < inf)
+			stack[sp++] = c1;
+		ref = c0;
+		return true;
+	}
+	int32_t first, second;
+	int hits = fast_node(s, r, ref, best_t, first, second);
+	if (hits == 2) {
+		stack[sp++] = second;
+		ref = first;
+	} else if (hits == 1) {
+		ref = first;
+	} else {
+		if (sp == 0)
+			return false;
+		ref = stack[--sp];
+	}
+	return true;
+}
+
+/* Ordered descent over the fast (64-byte child-pair) or wide (128-byte
+ * four-child) nodes with a per-thread stack.  Box culling keeps every child
+ * whose padded slab interval reaches [0, best]; the build pads boxes so that
+ * no triangle the exact test accepts is culled.  Both layouts share the
+ * triangle records, so they return the same hit. */
+template <bool ANY, bool COUNT, int LAYOUT = KGR_LAYOUT_FAST>
 __device__ __forceinline__ bool trace_fast(const DeviceScene &s, const f3 &o, const f3 &d,
 		float tmax, kgr_hit &best, TraceCounters *cnt = nullptr)
 {
@@ -270,18 +362,8 @@ __device__ __forceinline__ bool trace_fast(const DeviceScene &s, const f3 &o, co
 		while (ref >= 0) {
 			if (COUNT)
 				cnt->nodes++;
-			int32_t first, second;
-			int hits = fast_node(s, r, ref, best.t, first, second);
-			if (hits == 2) {
-				stack[sp++] = second;
-				ref = first;
-			} else if (hits == 1) {
-				ref = first;
-			} else {
-				if (sp == 0)
-					return best.prim >= 0;
-				ref = stack[--sp];
-			}
+			if (!node_step<LAYOUT>(s, r, ref, best.t, stack, sp))
+				return best.prim >= 0;
 		}
 		if (fast_leaf<ANY, COUNT>(s, r, ref, best, best_rank, cnt))
 			return true;
@@ -297,6 +379,8 @@ __device__ __forceinline__ bool trace(const DeviceScene &s, int layout, const f3
 {
 	if (layout == KGR_LAYOUT_THREADED)
 		return trace_threaded<ANY, false>(s, o, d, tmax, best);
+	if (layout == KGR_LAYOUT_WIDE)
+		return trace_fast<ANY, false, KGR_LAYOUT_WIDE>(s, o, d, tmax, best);
 	return trace_fast<ANY, false>(s, o, d, tmax, best);
 }
 
@@ -422,6 +506,17 @@ __device__ __forceinline__ f3 ggx_sample(const Material &mat, f3 n, const f3 &wo
 __device__ __forceinline__ f3 brdf(const SurfaceHit &sh, const f3 &wi)
 {
 	return sh.mat.diffuse / KGR_PI_DEV + ggx_brdf(sh.mat, sh.n, wi, sh.wo);
+}
+
+/* A ReSTIR GI secondary vertex whose outgoing radiance may be reused toward
+ * another receiver (the reconnection shift): no transmission and a GGX
+ * lobe of roughness >= 0.3, so that the radiance it scatters changes slowly
+ * with direction.  A glossier vertex sends its radiance mostly one way, and
+ * reusing the value that was bright toward one receiver for another would
+ * brighten the image. */
+__device__ __forceinline__ bool gi_reconnectable(const Material &m)
+{
+	return m.type != KGR_SHADING_TRANSMISSION && m.roughness >= 0.3f;
 }
 
 /* eval() (brdf.cuh:573-589): GGX, or Glass::sample (:154-175) for

@@ -135,6 +135,18 @@ struct FastNode {
 	int4 refs;   /* left ref, right ref, unused, unused */
 };
 
+/* 128-byte four-child node of the wide layout: the padded boxes of up to
+ * four children in SoA form (component c of each float4 belongs to child
+ * c) and their references, encoded as in FastNode; KGR_WIDE_EMPTY marks an
+ * unused slot.  The boxes are the fast layout's, bit for bit, so a slab
+ * test of a child here is the slab test of the same child there. */
+struct WideNode {
+	float4 lox, hix, loy, hiy, loz, hiz;
+	int4 refs;
+	int4 unused;
+};
+#define KGR_WIDE_EMPTY ((int32_t)0x80000000)
+
 /* Host builders (bvh_build.cpp). */
 struct PrimBox {
 	float bmin[3], bmax[3];
@@ -154,6 +166,12 @@ void parse_threaded(const float *vec4, uint32_t count, uint32_t prim_count,
 void build_fast(const Tree &tree, const std::vector<PrimBox> &boxes,
 		const float *positions, const uint32_t *tris4, std::vector<FastNode> &nodes,
 		std::vector<float4> &tri_records);
+/* Wide layout from the same tree: each node gathers up to four children by
+ * repeatedly opening its largest-area interior child (left-to-right order
+ * kept), leaf references identical to the fast layout's so both share its
+ * triangle records.  max_stack: the most stack entries a walk can hold
+ * (over every root-to-node path, the sum of children - 1). */
+void build_wide(const Tree &tree, std::vector<WideNode> &nodes, uint32_t &max_stack);
 
 /* ---------------------------------------------------------------- scene -- */
 
@@ -164,12 +182,14 @@ struct DeviceScene {
 	const float4 *bvh;        /* threaded layout, 3 per node */
 	const FastNode *fast_nodes;
 	const float4 *fast_tris;  /* 3 per triangle, leaf order */
+	const WideNode *wide_nodes;
 	const kgr_material *materials;
 	const kgr_triangle_light *lights;
 	uint32_t triangle_count;
 	uint32_t light_count;
 	uint32_t bvh_vec4_count;
 	uint32_t fast_node_count;
+	uint32_t wide_node_count;
 };
 
 } /* namespace kgr */
@@ -192,12 +212,14 @@ struct kgr_scene {
 	std::vector<kgr_triangle_light> lights;
 	std::vector<float> bvh;                /* threaded, 4 floats per vec4 */
 	uint32_t fast_node_count = 0;
+	uint32_t wide_node_count = 0, wide_max_stack = 0;
 	float bounds_min[3] = {0, 0, 0}, bounds_max[3] = {0, 0, 0};
 	double build_ms = 0.0;
 
 	kgr::DevBuf<float4> d_positions, d_normals, d_bvh, d_fast_tris;
 	kgr::DevBuf<uint4> d_tris;
 	kgr::DevBuf<kgr::FastNode> d_fast_nodes;
+	kgr::DevBuf<kgr::WideNode> d_wide_nodes;
 	kgr::DevBuf<kgr_material> d_materials;
 	kgr::DevBuf<kgr_triangle_light> d_lights;
 
@@ -206,6 +228,14 @@ struct kgr_scene {
 };
 
 namespace kgr {
+
+/* A scene whose wide layout was not built (its worst-case walk would not fit
+ * the traversal stack) is walked on the fast layout: the same boxes, the
+ * same triangle records, the same hits. */
+inline int layout_for(int layout, const kgr_scene *sc)
+{
+	return (layout == KGR_LAYOUT_WIDE && sc && !sc->wide_node_count) ? KGR_LAYOUT_FAST : layout;
+}
 
 /* ------------------------------------------------------ kernel launchers -- */
 

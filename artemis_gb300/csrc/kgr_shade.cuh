@@ -18,7 +18,7 @@ namespace kgr {
  * naive_path_tracer.cu:294-303).  `seed` advances in place.  At the last
  * depth the continuation is sampled only when final_seed is set (ReSTIR
  * keeps that seed).  Results go to `out` as they are produced:
- *   out.vertex(x, n)      offset hit point and shading normal
+ *   out.vertex(x, n, m)   offset hit point, shading normal and material
  *   out.emit(add)         beta * emission (scene without lights)
  *   out.nee(c, e, b, o, d) NEE record {contribution, pdf}, emission, beta,
  *                         shadow ray origin and {direction, tmax}
@@ -30,7 +30,7 @@ __device__ __forceinline__ void shade_surface(const DeviceScene &s, const FrameP
 	f3 n3 = sh.n;
 	float sgn = sh.mat.type == KGR_SHADING_TRANSMISSION ? -1.0f : 1.0f;
 	sh.x = sh.x + sgn * n3 * KGR_OFFSET_EPS;
-	out.vertex(sh.x, n3);
+	out.vertex(sh.x, n3, sh.mat);
 	if (s.light_count == 0) {
 		f3 direct = sh.mat.emission + mk(0.0f);
 		out.emit(beta * direct);

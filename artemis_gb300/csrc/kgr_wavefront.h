@@ -66,6 +66,30 @@ enum StageKind {
 /* Streaming read of a buffer with 16-byte loads (bandwidth probe). */
 void launch_read_probe(const float4 *buf, size_t n, float4 *sink, int iters, cudaStream_t st);
 
+/* Launch shape of the traversal stages of the fast and wide layouts.  Every
+ * shape gives the same hits (the per-ray walk is the same; only the
+ * scheduling of rays onto threads differs), so the autotuner may pick any. */
+enum TraceKernel {
+	TRACE_GRID = 0,      /* one ray per thread, grid-stride loop */
+	TRACE_PERSISTENT = 1 /* lanes refill from the queue as their rays end */
+};
+
+struct TraceTune {
+	int16_t shadow; /* TraceKernel of the shadow stage (closest hit is always persistent) */
+	int16_t block;  /* threads per block: 64, 128 or 256 */
+	int16_t pad[2];
+};
+
+/* The shape used when nothing was tuned. */
+inline TraceTune default_trace_tune()
+{
+	TraceTune t;
+	t.shadow = TRACE_GRID;
+	t.block = 128;
+	t.pad[0] = t.pad[1] = 0;
+	return t;
+}
+
 struct FrameParams {
 	uint32_t width, height, npix, spp, paths;
 	float center[3], U[3], V[3], W[3];
@@ -82,6 +106,7 @@ struct FrameParams {
 	int32_t gi_capture; /* shade records the depth-1 vertex in aov_p/aov_n */
 	int32_t gi_mcap, gi_neighbors, gi_radius;
 	float prev_center[3];
+	TraceTune tune;
 };
 
 /* 32-byte reservoir in two 16-byte SoA arrays:
@@ -105,14 +130,16 @@ struct OutputBuffers {
 
 /* --- path tracer (pt.cu) --- */
 void pt_generate(const PathBuffers &pb, const FrameParams &fp, cudaStream_t st);
-void pt_trace_closest(const DeviceScene &s, const PathBuffers &pb, int q, int layout, cudaStream_t st);
+void pt_trace_closest(const DeviceScene &s, const PathBuffers &pb, int q, int layout, const TraceTune &tune,
+		cudaStream_t st);
 void pt_shade(const DeviceScene &s, const PathBuffers &pb, const FrameParams &fp, int depth, int q,
 		cudaStream_t st);
 /* shade that also advances the RNG at the last depth (ReSTIR keeps the
  * path's final seed as its auxiliary seed) */
 void pt_shade_final_seed(const DeviceScene &s, const PathBuffers &pb, const FrameParams &fp, int depth,
 		int q, cudaStream_t st);
-void pt_shadow_resolve(const DeviceScene &s, const PathBuffers &pb, int layout, cudaStream_t st);
+void pt_shadow_resolve(const DeviceScene &s, const PathBuffers &pb, int layout, const TraceTune &tune,
+		cudaStream_t st);
 void pt_accumulate(const PathBuffers &pb, const FrameParams &fp, const OutputBuffers &out, cudaStream_t st);
 void reset_counters(const PathBuffers &pb, int which_mask, cudaStream_t st);
 

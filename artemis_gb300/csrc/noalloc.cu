@@ -129,6 +129,7 @@ extern "C" kgr_status kgr_render_pt_noalloc(const kgr_scene *sc, const kgr_launc
 		fp.accumulate = info->accumulate ? 1 : 0;
 		fp.samples = info->samples;
 		fp.layout = KGR_LAYOUT_FAST;
+		fp.tune = default_trace_tune();
 		fp.jitter = 1;
 
 		DeviceScene s = sc->view();
@@ -150,9 +151,9 @@ extern "C" kgr_status kgr_render_pt_noalloc(const kgr_scene *sc, const kgr_launc
 			int q = d & 1;
 			if (d > 0)
 				reset_counters(pb, (1 << (q ^ 1)) | (1 << CNT_SHADOW), st);
-			pt_trace_closest(s, pb, q, fp.layout, st);
+			pt_trace_closest(s, pb, q, fp.layout, fp.tune, st);
 			pt_shade(s, pb, fp, d, q, st);
-			pt_shadow_resolve(s, pb, fp.layout, st);
+			pt_shadow_resolve(s, pb, fp.layout, fp.tune, st);
 		}
 		pt_accumulate(pb, fp, out, st);
 		return KGR_OK;

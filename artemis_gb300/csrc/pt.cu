@@ -12,12 +12,6 @@
 #include "kgr_shade.cuh"
 #include "kgr_wavefront.h"
 
-/* Resident 128-thread blocks per SM the traversal kernels are compiled for
- * (bounds their registers). */
-#ifndef KGR_TRACE_MIN_BLOCKS
-#define KGR_TRACE_MIN_BLOCKS 1
-#endif
-
 namespace kgr {
 
 int device_sm_count()
@@ -118,15 +112,16 @@ struct WavefrontSink {
 	int depth, gi_capture;
 	f3 albedo;
 	bool shadow = false, cont = false;
-	__device__ __forceinline__ void vertex(const f3 &x, const f3 &n)
+	__device__ __forceinline__ void vertex(const f3 &x, const f3 &n, const Material &m)
 	{
 		if (depth == 0) {
 			pb.aov_n[p] = f4_of(n, 0.0f);
 			pb.aov_a[p] = f4_of(albedo, 0.0f);
 			pb.aov_p[p] = f4_of(x, 0.0f);
 		} else if (depth == 1 && gi_capture) {
-			/* the secondary vertex of a ReSTIR GI sample */
-			pb.aov_n[p] = f4_of(n, 0.0f);
+			/* the secondary vertex of a ReSTIR GI sample; w = 1 when its
+			 * radiance may be reused toward other receivers */
+			pb.aov_n[p] = f4_of(n, gi_reconnectable(m) ? 1.0f : 0.0f);
 			pb.aov_p[p] = f4_of(x, 1.0f);
 		}
 	}
@@ -195,9 +190,10 @@ __global__ void __launch_bounds__(128) shade_kernel(DeviceScene s, PathBuffers p
 }
 
 /* is_occluded for every queued shadow ray, then Ld = contr / pdf and
- * L += beta * (Le + Ld) in the order of the recursion. */
-template <int LAYOUT, bool COUNT>
-__global__ void __launch_bounds__(128, KGR_TRACE_MIN_BLOCKS) shadow_resolve_kernel(DeviceScene s, PathBuffers pb)
+ * L += beta * (Le + Ld) in the order of the recursion.  One ray per thread,
+ * grid-stride over the queue. */
+template <int LAYOUT, bool COUNT, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) shadow_resolve_kernel(DeviceScene s, PathBuffers pb)
 {
 	const uint32_t n = pb.counters[CNT_SHADOW];
 	uint32_t stride = gridDim.x * blockDim.x;
@@ -210,7 +206,7 @@ __global__ void __launch_bounds__(128, KGR_TRACE_MIN_BLOCKS) shadow_resolve_kern
 		if (LAYOUT == KGR_LAYOUT_THREADED)
 			occ = trace_threaded<true, COUNT>(s, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), b.w, h, &cnt);
 		else
-			occ = trace_fast<true, COUNT>(s, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), b.w, h, &cnt);
+			occ = trace_fast<true, COUNT, LAYOUT>(s, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), b.w, h, &cnt);
 		float4 c = pb.pend_c[p], e = pb.pend_e[p], be = pb.pend_b[p];
 		f3 contr = occ ? mk(0.0f) : mk(c.x, c.y, c.z);
 		f3 direct = mk(e.x, e.y, e.z) + contr / c.w;
@@ -228,14 +224,14 @@ __device__ __forceinline__ void resolve_shadow(const PathBuffers &pb, uint32_t p
 	pb.L[p] = nee_add(pb.L[p], pb.pend_c[p], pb.pend_e[p], pb.pend_b[p], occ);
 }
 
-/* Persistent traversal of the fast layout: each lane takes a new ray from the
- * queue (one atomic per warp) as soon as its current ray is finished, so a
- * lane whose ray ends early does not idle until the longest ray of its warp
- * is done.  One loop iteration descends to a leaf and tests it.  ANY: shadow
- * rays, resolved into the path radiance.  The grid is sized to the resident
- * capacity of the GPU. */
-template <bool ANY, bool COUNT>
-__global__ void __launch_bounds__(128, KGR_TRACE_MIN_BLOCKS) fast_persistent_kernel(DeviceScene s, PathBuffers pb, int q)
+/* Persistent traversal of the fast or wide layout: each lane takes a new ray
+ * from the queue (one atomic per warp) as soon as its current ray is
+ * finished, so a lane whose ray ends early does not idle until the longest
+ * ray of its warp is done.  One loop iteration descends to a leaf and tests
+ * it.  ANY: shadow rays, resolved into the path radiance.  The grid is sized
+ * to the resident capacity of the GPU. */
+template <bool ANY, bool COUNT, int LAYOUT, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) fast_persistent_kernel(DeviceScene s, PathBuffers pb, int q)
 {
 	const uint32_t n = ANY ? pb.counters[CNT_SHADOW] : pb.counters[q == 0 ? CNT_Q0 : CNT_Q1];
 	const uint32_t *queue = ANY ? pb.shadow_queue : pb.queue[q];
@@ -287,18 +283,9 @@ __global__ void __launch_bounds__(128, KGR_TRACE_MIN_BLOCKS) fast_persistent_ker
 		while (ref >= 0) {
 			if (COUNT)
 				cnt.nodes++;
-			int32_t first, second;
-			int hits = fast_node(s, r, ref, best.t, first, second);
-			if (hits == 2) {
-				stack[sp++] = second;
-				ref = first;
-			} else if (hits == 1) {
-				ref = first;
-			} else if (sp == 0) {
+			if (!node_step<LAYOUT>(s, r, ref, best.t, stack, sp)) {
 				done = true;
 				break;
-			} else {
-				ref = stack[--sp];
 			}
 		}
 		if (!done) {
@@ -329,6 +316,44 @@ int resident_grid(K kernel, int block)
 	return per_sm * device_sm_count();
 }
 
+/* One launch of a persistent traversal kernel over a resident grid (the
+ * grid of each instantiation is computed once). */
+template <bool ANY, bool COUNT, int LAYOUT, int BLOCK>
+void launch_persistent(const DeviceScene &s, const PathBuffers &pb, int q, cudaStream_t st)
+{
+	static const int g = resident_grid(fast_persistent_kernel<ANY, COUNT, LAYOUT, BLOCK>, BLOCK);
+	fast_persistent_kernel<ANY, COUNT, LAYOUT, BLOCK><<<g, BLOCK, 0, st>>>(s, pb, q);
+}
+
+template <bool ANY, int LAYOUT>
+void launch_persistent_block(const DeviceScene &s, const PathBuffers &pb, int q, int block, cudaStream_t st)
+{
+	if (block == 64)
+		launch_persistent<ANY, false, LAYOUT, 64>(s, pb, q, st);
+	else if (block == 256)
+		launch_persistent<ANY, false, LAYOUT, 256>(s, pb, q, st);
+	else
+		launch_persistent<ANY, false, LAYOUT, 128>(s, pb, q, st);
+}
+
+template <bool COUNT, int LAYOUT, int BLOCK>
+void launch_shadow_grid(const DeviceScene &s, const PathBuffers &pb, cudaStream_t st)
+{
+	static const int g = resident_grid(shadow_resolve_kernel<LAYOUT, COUNT, BLOCK>, BLOCK);
+	shadow_resolve_kernel<LAYOUT, COUNT, BLOCK><<<g, BLOCK, 0, st>>>(s, pb);
+}
+
+template <int LAYOUT>
+void launch_shadow_grid_block(const DeviceScene &s, const PathBuffers &pb, int block, cudaStream_t st)
+{
+	if (block == 64)
+		launch_shadow_grid<false, LAYOUT, 64>(s, pb, st);
+	else if (block == 256)
+		launch_shadow_grid<false, LAYOUT, 256>(s, pb, st);
+	else
+		launch_shadow_grid<false, LAYOUT, 128>(s, pb, st);
+}
+
 /* accumulate (amadeus_path_tracer.cu:59-70), the frame's samples in order */
 __global__ void accumulate_kernel(PathBuffers pb, FrameParams fp, OutputBuffers out)
 {
@@ -357,22 +382,28 @@ void pt_generate(const PathBuffers &pb, const FrameParams &fp, cudaStream_t st)
 	KGR_CUDA(cudaGetLastError());
 }
 
-void pt_trace_closest(const DeviceScene &s, const PathBuffers &pb, int q, int layout, cudaStream_t st)
+void pt_trace_closest(const DeviceScene &s, const PathBuffers &pb, int q, int layout, const TraceTune &tune,
+		cudaStream_t st)
 {
-	int grid = grid_for(pb.capacity, 128);
 	bool c = pb.visits != nullptr;
-	if (layout == KGR_LAYOUT_THREADED && c)
-		trace_closest_kernel<KGR_LAYOUT_THREADED, true><<<grid, 128, 0, st>>>(s, pb, q);
-	else if (layout == KGR_LAYOUT_THREADED)
-		trace_closest_kernel<KGR_LAYOUT_THREADED, false><<<grid, 128, 0, st>>>(s, pb, q);
-	else {
+	if (layout == KGR_LAYOUT_THREADED) {
+		int grid = grid_for(pb.capacity, 128);
+		if (c)
+			trace_closest_kernel<KGR_LAYOUT_THREADED, true><<<grid, 128, 0, st>>>(s, pb, q);
+		else
+			trace_closest_kernel<KGR_LAYOUT_THREADED, false><<<grid, 128, 0, st>>>(s, pb, q);
+	} else {
 		KGR_CUDA(cudaMemsetAsync(pb.counters + CNT_FETCH_CLOSEST, 0, sizeof(uint32_t), st));
-		if (c) {
-			static const int g = resident_grid(fast_persistent_kernel<false, true>, 128);
-			fast_persistent_kernel<false, true><<<g, 128, 0, st>>>(s, pb, q);
+		if (layout == KGR_LAYOUT_WIDE) {
+			if (c)
+				launch_persistent<false, true, KGR_LAYOUT_WIDE, 128>(s, pb, q, st);
+			else
+				launch_persistent_block<false, KGR_LAYOUT_WIDE>(s, pb, q, tune.block, st);
 		} else {
-			static const int g = resident_grid(fast_persistent_kernel<false, false>, 128);
-			fast_persistent_kernel<false, false><<<g, 128, 0, st>>>(s, pb, q);
+			if (c)
+				launch_persistent<false, true, KGR_LAYOUT_FAST, 128>(s, pb, q, st);
+			else
+				launch_persistent_block<false, KGR_LAYOUT_FAST>(s, pb, q, tune.block, st);
 		}
 	}
 	KGR_CUDA(cudaGetLastError());
@@ -394,22 +425,31 @@ void pt_shade_final_seed(const DeviceScene &s, const PathBuffers &pb, const Fram
 	KGR_CUDA(cudaGetLastError());
 }
 
-void pt_shadow_resolve(const DeviceScene &s, const PathBuffers &pb, int layout, cudaStream_t st)
+void pt_shadow_resolve(const DeviceScene &s, const PathBuffers &pb, int layout, const TraceTune &tune,
+		cudaStream_t st)
 {
-	int grid = grid_for(pb.capacity, 128);
 	bool c = pb.visits != nullptr;
-	if (layout == KGR_LAYOUT_THREADED && c)
-		shadow_resolve_kernel<KGR_LAYOUT_THREADED, true><<<grid, 128, 0, st>>>(s, pb);
-	else if (layout == KGR_LAYOUT_THREADED)
-		shadow_resolve_kernel<KGR_LAYOUT_THREADED, false><<<grid, 128, 0, st>>>(s, pb);
-	else if (c) {
-		/* shadow rays are short: a grid-stride loop over a resident grid
-		 * beats per-lane refill, whose bookkeeping costs more than it saves */
-		static const int g = resident_grid(shadow_resolve_kernel<KGR_LAYOUT_FAST, true>, 128);
-		shadow_resolve_kernel<KGR_LAYOUT_FAST, true><<<g, 128, 0, st>>>(s, pb);
+	if (layout == KGR_LAYOUT_THREADED) {
+		int grid = grid_for(pb.capacity, 128);
+		if (c)
+			shadow_resolve_kernel<KGR_LAYOUT_THREADED, true, 128><<<grid, 128, 0, st>>>(s, pb);
+		else
+			shadow_resolve_kernel<KGR_LAYOUT_THREADED, false, 128><<<grid, 128, 0, st>>>(s, pb);
+	} else if (c) {
+		if (layout == KGR_LAYOUT_WIDE)
+			launch_shadow_grid<true, KGR_LAYOUT_WIDE, 128>(s, pb, st);
+		else
+			launch_shadow_grid<true, KGR_LAYOUT_FAST, 128>(s, pb, st);
+	} else if (tune.shadow == TRACE_PERSISTENT) {
+		KGR_CUDA(cudaMemsetAsync(pb.counters + CNT_FETCH_SHADOW, 0, sizeof(uint32_t), st));
+		if (layout == KGR_LAYOUT_WIDE)
+			launch_persistent_block<true, KGR_LAYOUT_WIDE>(s, pb, 0, tune.block, st);
+		else
+			launch_persistent_block<true, KGR_LAYOUT_FAST>(s, pb, 0, tune.block, st);
+	} else if (layout == KGR_LAYOUT_WIDE) {
+		launch_shadow_grid_block<KGR_LAYOUT_WIDE>(s, pb, tune.block, st);
 	} else {
-		static const int g = resident_grid(shadow_resolve_kernel<KGR_LAYOUT_FAST, false>, 128);
-		shadow_resolve_kernel<KGR_LAYOUT_FAST, false><<<g, 128, 0, st>>>(s, pb);
+		launch_shadow_grid_block<KGR_LAYOUT_FAST>(s, pb, tune.block, st);
 	}
 	KGR_CUDA(cudaGetLastError());
 }

@@ -24,7 +24,7 @@ __global__ void __launch_bounds__(128) trace_rays_kernel(DeviceScene s, const fl
 		if (LAYOUT == KGR_LAYOUT_THREADED)
 			r = trace_threaded<ANY, false>(s, o, d, b.w, h);
 		else
-			r = trace_fast<ANY, false>(s, o, d, b.w, h);
+			r = trace_fast<ANY, false, LAYOUT>(s, o, d, b.w, h);
 		if (ANY) {
 			occluded[i] = r ? 1u : 0u;
 		} else {
@@ -99,6 +99,8 @@ void launch_trace_closest(const DeviceScene &s, const float4 *rays, uint32_t n, 
 	int grid = grid_for(n, 128);
 	if (layout == KGR_LAYOUT_THREADED)
 		trace_rays_kernel<false, KGR_LAYOUT_THREADED><<<grid, 128, 0, stream>>>(s, rays, n, hits, nullptr);
+	else if (layout == KGR_LAYOUT_WIDE)
+		trace_rays_kernel<false, KGR_LAYOUT_WIDE><<<grid, 128, 0, stream>>>(s, rays, n, hits, nullptr);
 	else
 		trace_rays_kernel<false, KGR_LAYOUT_FAST><<<grid, 128, 0, stream>>>(s, rays, n, hits, nullptr);
 	KGR_CUDA(cudaGetLastError());
@@ -112,6 +114,8 @@ void launch_trace_any(const DeviceScene &s, const float4 *rays, uint32_t n, uint
 	int grid = grid_for(n, 128);
 	if (layout == KGR_LAYOUT_THREADED)
 		trace_rays_kernel<true, KGR_LAYOUT_THREADED><<<grid, 128, 0, stream>>>(s, rays, n, nullptr, occluded);
+	else if (layout == KGR_LAYOUT_WIDE)
+		trace_rays_kernel<true, KGR_LAYOUT_WIDE><<<grid, 128, 0, stream>>>(s, rays, n, nullptr, occluded);
 	else
 		trace_rays_kernel<true, KGR_LAYOUT_FAST><<<grid, 128, 0, stream>>>(s, rays, n, nullptr, occluded);
 	KGR_CUDA(cudaGetLastError());

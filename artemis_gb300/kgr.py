@@ -17,7 +17,7 @@ from . import build as _build
 c_u32, c_i32, c_u64, c_f = ctypes.c_uint32, ctypes.c_int32, ctypes.c_uint64, ctypes.c_float
 vp = ctypes.c_void_p
 
-LAYOUT_FAST, LAYOUT_THREADED = 0, 1
+LAYOUT_FAST, LAYOUT_THREADED, LAYOUT_WIDE = 0, 1, 2
 BUILDER_SAH, BUILDER_KOBRA = 0, 1
 VALUE_NONE, VALUE_INT, VALUE_FLOAT, VALUE_BOOL, VALUE_STRING = range(5)
 
@@ -41,7 +41,8 @@ class SceneInfo(ctypes.Structure):
     _fields_ = [("vertex_count", c_u32), ("triangle_count", c_u32), ("light_count", c_u32),
                 ("material_count", c_u32), ("bvh_vec4_count", c_u32), ("fast_node_count", c_u32),
                 ("device_bytes", c_u64), ("build_ms", ctypes.c_double),
-                ("bounds_min", c_f * 3), ("bounds_max", c_f * 3)]
+                ("bounds_min", c_f * 3), ("bounds_max", c_f * 3),
+                ("wide_node_count", c_u32), ("wide_max_stack", c_u32)]
 
 
 class Value(ctypes.Structure):

@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define KGR_ABI_VERSION 1
+#define KGR_ABI_VERSION 2
 
 typedef enum kgr_status {
 	KGR_OK = 0,
@@ -137,6 +137,8 @@ typedef struct kgr_scene_info {
 	double build_ms;
 	float bounds_min[3];
 	float bounds_max[3];
+	uint32_t wide_node_count; /* 128-byte four-child nodes; 0 when the wide layout is not built */
+	uint32_t wide_max_stack;  /* most traversal stack entries a walk of the wide layout can hold */
 } kgr_scene_info;
 
 /* Build the BVH on the host and upload the scene to the device.  Emissive
@@ -193,7 +195,11 @@ enum {
 	/* child-pair BVH2 with ordered descent and a short stack (default) */
 	KGR_LAYOUT_FAST = 0,
 	/* the threaded bvh.cpp layout, walked exactly as bvh.glsl:52-99 does */
-	KGR_LAYOUT_THREADED = 1
+	KGR_LAYOUT_THREADED = 1,
+	/* four-child BVH4 over the same padded boxes and triangle records as the
+	 * fast layout: half the dependent node fetches per ray; built when the
+	 * walk's worst-case stack fits the traversal stack */
+	KGR_LAYOUT_WIDE = 2
 };
 
 /* Closest hit for n rays.  `rays` (device) holds 8 floats per ray:

@@ -1397,10 +1397,20 @@ void oracle_render_restir(const oracle_scene *s, const oracle_render_params *p,
 namespace {
 
 const float GI_COS_10DEG = 0.984807753f;
+/* shifts with a Jacobian outside [1/10, 10] are invalid (gi.cu) */
+#define KGR_GI_JACOBIAN_MIN 0.1f
+#define KGR_GI_JACOBIAN_MAX 10.0f
 
 struct GiS {
 	f3 xs, ns, Lo;
+	bool rc = true; /* reconnectable: W is stored with its sign bit set when not */
 };
+
+/* gi_reconnectable (kgr_device.cuh): no transmission, roughness >= 0.3 */
+inline bool gi_rc(const Material &m)
+{
+	return m.type != KGR_SHADING_TRANSMISSION && m.roughness >= 0.3f;
+}
 
 inline void gi_load(const float *a, const float *b, size_t i, GiS &s, float &W, int &M)
 {
@@ -1408,7 +1418,8 @@ inline void gi_load(const float *a, const float *b, size_t i, GiS &s, float &W, 
 	s.xs = mk(a[4 * i], a[4 * i + 1], a[4 * i + 2]);
 	s.ns = unpack_normal(w);
 	s.Lo = mk(b[4 * i], b[4 * i + 1], b[4 * i + 2]);
-	W = b[4 * i + 3];
+	s.rc = !std::signbit(b[4 * i + 3]);
+	W = fabsf(b[4 * i + 3]);
 	M = unpack_m(w);
 }
 
@@ -1416,7 +1427,7 @@ inline void gi_store(float *a, float *b, size_t i, const GiS &s, float W, int M)
 {
 	a[4 * i] = s.xs.x; a[4 * i + 1] = s.xs.y; a[4 * i + 2] = s.xs.z;
 	a[4 * i + 3] = u2f(pack_normal_m(s.ns, M));
-	b[4 * i] = s.Lo.x; b[4 * i + 1] = s.Lo.y; b[4 * i + 2] = s.Lo.z; b[4 * i + 3] = W;
+	b[4 * i] = s.Lo.x; b[4 * i + 1] = s.Lo.y; b[4 * i + 2] = s.Lo.z; b[4 * i + 3] = s.rc ? W : -W;
 }
 
 inline float gi_norm(float w_sum, int Z, float target)
@@ -1433,25 +1444,39 @@ inline float gi_jac(const f3 &xq, const f3 &xr, const GiS &s)
 	float cq = fabsf(dot(s.ns, dq)) / ksqrt(lq2);
 	float cr = fabsf(dot(s.ns, dr)) / ksqrt(lr2);
 	float j = (cq / cr) * (lr2 / lq2);
-	return (j > 0.0f && j < 1e30f) ? j : 0.0f;
+	return (j >= KGR_GI_JACOBIAN_MIN && j <= KGR_GI_JACOBIAN_MAX) ? j : 0.0f;
 }
 
+/* src: domain of the selected sample (-1 the centre) */
 struct GiMergeO {
 	GiS sel;
 	float w = 0.0f;
+	int src = -1;
 	f3 seed;
-	void update(const GiS &s, float weight)
+	void update(const GiS &s, float weight, int from)
 	{
 		w += weight;
 		float eta = rand_uniform(seed);
-		if ((eta * w) < weight)
+		if ((eta * w) < weight) {
 			sel = s;
+			src = from;
+		}
 	}
 };
 
+/* balance-heuristic contribution weight W = num w_sum / (D p^_q) (gi.cu) */
+inline float gi_mis(float w_sum, float num, float D, float target)
+{
+	if (!(target > 0.0f) || !(D > 0.0f))
+		return 0.0f;
+	return (float)(((double)num * (double)w_sum) / ((double)D * (double)target));
+}
+
+/* G-buffer entry; position.w = material index + 1 (0: no hit) */
 struct GB {
 	f3 x, n;
 	bool hit;
+	uint32_t mat;
 };
 
 inline GB gb_at(const float *pos, const float *nrm, size_t i)
@@ -1460,6 +1485,7 @@ inline GB gb_at(const float *pos, const float *nrm, size_t i)
 	g.x = mk(pos[4 * i], pos[4 * i + 1], pos[4 * i + 2]);
 	g.n = mk(nrm[4 * i], nrm[4 * i + 1], nrm[4 * i + 2]);
 	g.hit = pos[4 * i + 3] > 0.0f;
+	g.mat = g.hit ? (uint32_t)pos[4 * i + 3] - 1u : 0u;
 	return g;
 }
 
@@ -1482,6 +1508,30 @@ inline bool gi_visible(Ctx &ctx, const f3 &from, const f3 &to)
 int gi_neighbor(const oracle_render_params *p, int index, f3 &seed, int radius)
 {
 	return spatial_neighbor(p, index, seed, radius);
+}
+
+/* The receiver of a GI sample at a pixel: its material, shading normal and
+ * the direction toward the camera centre. */
+inline SurfaceHit gi_receiver(const kgr_material &m, const GB &g, const f3 &center)
+{
+	SurfaceHit h;
+	h.mat = load_material(m);
+	h.entering = false;
+	h.n = g.n;
+	h.wo = normalize(center - g.x);
+	h.x = g.x;
+	return h;
+}
+
+/* Target function of sample s at receiver h: sum_rgb(f L_o) |n.w|. */
+inline float gi_target(const SurfaceHit &h, const GiS &s)
+{
+	f3 D = s.xs - h.x;
+	float d = length(D);
+	f3 w = D / d;
+	f3 v = brdf(h, w) * s.Lo * fabsf(dot(h.n, w));
+	float t = v.x + v.y + v.z;
+	return (t > 0.0f && t < 1e30f) ? t : 0.0f;
 }
 
 } /* namespace */
@@ -1516,14 +1566,14 @@ extern "C" void oracle_render_gi(const oracle_scene *s, const oracle_render_para
 			ctx.stats.camera_rays++;
 			kgr_hit h = trace_closest(s, o, d, 1e16f, &ctx.internal, &ctx.leaves);
 			SurfaceHit sh;
-			GiS smp = {mk(0.0f), mk(0.0f, 0.0f, 1.0f), mk(0.0f)};
+			GiS smp = {mk(0.0f), mk(0.0f, 0.0f, 1.0f), mk(0.0f), true};
 			bool valid = false;
 			float gpdf = 0.0f;
 			if (h.prim >= 0 && surface(s, h, d, sh)) {
 				f3 n3 = sh.n;
 				float sgn = sh.mat.type == KGR_SHADING_TRANSMISSION ? -1.0f : 1.0f;
 				sh.x = sh.x + sgn * n3 * OFFSET_EPS;
-				store4(pos.data(), pix, sh.x, 1.0f);
+				store4(pos.data(), pix, sh.x, (float)(s->tris[4 * (size_t)h.prim + 3] + 1u));
 				store4(nrm.data(), pix, n3, 0.0f);
 				mats[pix] = s->materials[s->tris[4 * (size_t)h.prim + 3]];
 				/* DI candidates */
@@ -1593,6 +1643,7 @@ extern "C" void oracle_render_gi(const oracle_scene *s, const oracle_render_para
 						if (depth == 1) {
 							smp.xs = s2.x;
 							smp.ns = n2;
+							smp.rc = gi_rc(s2.mat);
 							captured = true;
 						}
 						f3 dir2 = s2.mat.emission + ctx.Ld(s2, seed);
@@ -1619,11 +1670,12 @@ extern "C" void oracle_render_gi(const oracle_scene *s, const oracle_render_para
 			store4(aux.data(), pix, seed, 1.0f);
 			float W = 0.0f;
 			if (valid) {
-				float target = max3(smp.Lo);
+				float target = gi_target(gi_receiver(mats[pix], gb_at(pos.data(), nrm.data(), pix), center), smp);
 				W = gi_norm(target / gpdf, 1, target);
 			} else {
 				smp.xs = smp.Lo = mk(0.0f);
 				smp.ns = mk(0.0f, 0.0f, 1.0f);
+				smp.rc = true;
 			}
 			gi_store(cur_a.data(), cur_b.data(), pix, smp, W, 1);
 		}
@@ -1673,15 +1725,21 @@ extern "C" void oracle_render_gi(const oracle_scene *s, const oracle_render_para
 					continue;
 				gi_load(cur_a.data(), cur_b.data(), pix, cs, cW, cM);
 				int pMc = pM < st->gi_mcap ? pM : st->gi_mcap;
+				SurfaceHit h = gi_receiver(mats[pix], g, center);
 				GiMergeO r;
-				r.sel = {mk(0.0f), mk(0.0f), mk(0.0f)};
+				r.sel = {mk(0.0f), mk(0.0f), mk(0.0f), true};
 				r.seed = load4(aux.data(), pix);
-				r.update(cs, max3(cs.Lo) * cW * cM);
+				r.update(cs, gi_target(h, cs) * cW * cM, -1);
 				float J = gi_jac(g.x, gp.x, ps);
-				float wp = max3(ps.Lo) * J * pW * pMc;
-				r.update(ps, wp);
-				int Mt = cM + (wp > 0.0f ? pMc : 0);
-				float W = gi_norm(r.w, Mt, max3(r.sel.Lo));
+				float wp = gi_target(h, ps) * J * pW * pMc;
+				r.update(ps, wp, 0);
+				/* the history counts whether or not its sample carries weight */
+				int Mt = cM + pMc;
+				float tq = gi_target(h, r.sel);
+				float jp = gi_jac(gp.x, g.x, r.sel);
+				float tp = jp > 0.0f ? gi_target(gi_receiver(s->materials[gp.mat], gp, pcenter), r.sel) * jp : 0.0f;
+				float D = (float)cM * tq + (float)pMc * tp;
+				float W = gi_mis(r.w, r.src < 0 ? tq : tp, D, tq);
 				gi_store(cur_a.data(), cur_b.data(), pix, r.sel, W, Mt);
 			}
 #pragma omp critical
@@ -1712,10 +1770,11 @@ extern "C" void oracle_render_gi(const oracle_scene *s, const oracle_render_para
 					continue;
 				}
 				float depth = length(g.x - center);
+				SurfaceHit h = gi_receiver(mats[pix], g, center);
 				GiMergeO r;
-				r.sel = {mk(0.0f), mk(0.0f), mk(0.0f)};
+				r.sel = {mk(0.0f), mk(0.0f), mk(0.0f), true};
 				r.seed = load4(aux.data(), pix);
-				r.update(cs, max3(cs.Lo) * cW * cM);
+				r.update(cs, gi_target(h, cs) * cW * cM, -1);
 				int Msum = cM;
 				for (int i = 0; i < st->gi_neighbors; i++) {
 					int index0 = gi_neighbor(p, (int)pix, r.seed, st->gi_radius);
@@ -1733,24 +1792,32 @@ extern "C" void oracle_render_gi(const oracle_scene *s, const oracle_render_para
 					nidx[i] = index0;
 					nM[i] = nMi;
 					Msum += nMi;
-					float J = gi_jac(g.x, gn.x, ns);
-					float wn = max3(ns.Lo) * J * nW * nMi;
+					float J = ns.rc ? gi_jac(g.x, gn.x, ns) : 0.0f;
+					float wn = J > 0.0f ? gi_target(h, ns) * J * nW * nMi : 0.0f;
 					if (wn > 0.0f && !gi_visible(ctx, g.x, ns.xs))
 						wn = 0.0f;
-					r.update(ns, wn);
+					r.update(ns, wn, i);
 				}
-				int Z = cM;
-				float target = max3(r.sel.Lo);
-				if (target > 0.0f) {
+				/* balance heuristic over the centre and the neighbour domains */
+				float target = gi_target(h, r.sel);
+				float D = (float)cM * target;
+				float num = r.src < 0 ? target : 0.0f;
+				if (target > 0.0f && r.sel.rc) {
 					for (int i = 0; i < st->gi_neighbors; i++) {
 						if (nidx[i] < 0)
 							continue;
 						GB gn = gb_at(pos.data(), nrm.data(), (size_t)nidx[i]);
-						if (gi_jac(gn.x, g.x, r.sel) > 0.0f && gi_visible(ctx, gn.x, r.sel.xs))
-							Z += nM[i];
+						float jn = gi_jac(gn.x, g.x, r.sel);
+						float tn = jn > 0.0f
+							? gi_target(gi_receiver(mats[(size_t)nidx[i]], gn, center), r.sel) * jn : 0.0f;
+						if (tn > 0.0f && !gi_visible(ctx, gn.x, r.sel.xs))
+							tn = 0.0f;
+						D += (float)nM[i] * tn;
+						if (i == r.src)
+							num = tn;
 					}
 				}
-				gi_store(out_a, out_b, pix, r.sel, gi_norm(r.w, Z, target), Msum);
+				gi_store(out_a, out_b, pix, r.sel, gi_mis(r.w, num, D, target), Msum);
 			}
 #pragma omp critical
 			merge_stats(&total, ctx.stats);

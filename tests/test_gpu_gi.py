@@ -27,7 +27,7 @@ def rel_ok(a, b, rtol=1e-4, atol=1e-6):
     return np.abs(a - b) <= rtol * np.maximum(np.abs(a), np.abs(b)) + atol
 
 
-@pytest.mark.parametrize("layout", ["fast", "threaded"])
+@pytest.mark.parametrize("layout", ["fast", "threaded", "wide"])
 def test_restir_gi_matches_oracle(layout):
     g, sc, osc = helpers.both("box4k", 1)
     W, H, frames = 64, 64, 3

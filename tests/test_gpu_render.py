@@ -45,7 +45,7 @@ def render_pt_gpu(g, sc, W, H, opts, frames=1, layout="fast", **kw):
     return cam, [b.cpu().numpy() for b in bufs], st
 
 
-@pytest.mark.parametrize("layout", ["fast", "threaded"])
+@pytest.mark.parametrize("layout", ["fast", "threaded", "wide"])
 def test_path_tracer_matches_oracle(box4k, layout):
     g, sc, osc = box4k
     W, H = 96, 96
@@ -99,7 +99,7 @@ def restir_gpu(g, sc, W, H, frames, opts, max_depth=2):
     return cam, [b.cpu().numpy() for b in bufs], res_a, res_b, inter, st
 
 
-@pytest.mark.parametrize("passes,layout", [(1, "fast"), (2, "threaded")])
+@pytest.mark.parametrize("passes,layout", [(1, "fast"), (2, "threaded"), (1, "wide")])
 def test_restir_di_matches_oracle(box4k, passes, layout):
     g, sc, osc = box4k
     W, H = 96, 96

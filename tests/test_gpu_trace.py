@@ -1,5 +1,5 @@
 """GPU traversal parity: hit primitive ids, distances and barycentrics of
-both device layouts against the oracle's GLSL threaded walk
+the device layouts (fast BVH2, wide BVH4, threaded) against the oracle's GLSL threaded walk
 (shaders/rt/modules/bvh.glsl:52-99) on the same rays -- bit for bit -- and
 occlusion flags of the any-hit walk (amadeus_common.cuh:190-212)."""
 import numpy as np
@@ -39,7 +39,7 @@ def box4k():
     return helpers.both("box4k", 1)
 
 
-@pytest.mark.parametrize("layout", [kgr.LAYOUT_FAST, kgr.LAYOUT_THREADED])
+@pytest.mark.parametrize("layout", [kgr.LAYOUT_FAST, kgr.LAYOUT_THREADED, kgr.LAYOUT_WIDE])
 def test_camera_rays_bit_exact(box4k, layout):
     g, sc, osc = box4k
     cam = kgr.camera(g.eye, g.target, g.fov, 1.0)
@@ -50,7 +50,7 @@ def test_camera_rays_bit_exact(box4k, layout):
     assert (ref["prim"] >= 0).all()
 
 
-@pytest.mark.parametrize("layout", [kgr.LAYOUT_FAST, kgr.LAYOUT_THREADED])
+@pytest.mark.parametrize("layout", [kgr.LAYOUT_FAST, kgr.LAYOUT_THREADED, kgr.LAYOUT_WIDE])
 def test_random_rays_bit_exact(box4k, layout):
     g, sc, osc = box4k
     rays = helpers.random_rays(g, 50000, 11)
@@ -58,7 +58,7 @@ def test_random_rays_bit_exact(box4k, layout):
     assert_hits_equal(gpu_closest(sc, rays, layout), ref["raw"])
 
 
-@pytest.mark.parametrize("layout", [kgr.LAYOUT_FAST, kgr.LAYOUT_THREADED])
+@pytest.mark.parametrize("layout", [kgr.LAYOUT_FAST, kgr.LAYOUT_THREADED, kgr.LAYOUT_WIDE])
 def test_any_hit_bit_exact(box4k, layout):
     g, sc, osc = box4k
     rays = helpers.random_rays(g, 50000, 12)
@@ -82,7 +82,7 @@ def test_reference_builder_buffer_drops_in(box4k):
     rays = np.concatenate([helpers.random_rays(g, 20000, 13),
                            helpers.camera_rays(kgr.camera(g.eye, g.target, g.fov, 1.0), 128, 128)])
     ref, _ = osc.trace_closest(rays)
-    for layout in (kgr.LAYOUT_FAST, kgr.LAYOUT_THREADED):
+    for layout in (kgr.LAYOUT_FAST, kgr.LAYOUT_THREADED, kgr.LAYOUT_WIDE):
         assert_hits_equal(gpu_closest(sc, rays, layout), ref["raw"])
 
 
@@ -105,20 +105,34 @@ def test_edge_cases(box4k):
     rays[:, 0:3] = [[0, 0, 0], [0.5, 0, 0.5], [-2, 0, 0], [0, 0, 2], [1.5, 1.5, 1.5], [0, -1.9, 0], [0, 0, 0], [0, 0, 0]]
     rays[:, 7] = [np.inf] * 6 + [0.0, np.inf]
     ref, _ = osc.trace_closest(rays)
-    for layout in (kgr.LAYOUT_FAST, kgr.LAYOUT_THREADED):
+    for layout in (kgr.LAYOUT_FAST, kgr.LAYOUT_THREADED, kgr.LAYOUT_WIDE):
         assert_hits_equal(sc.trace_closest_host(rays, layout), ref["raw"])
     assert ref["prim"][6] == -1
 
 
 @pytest.mark.parametrize("name", ["terrain_s"])
 def test_terrain_fast_equals_threaded(name):
-    """On a 0.25M-triangle scene the fast layout agrees with the threaded
-    walk on the GPU, and both with the oracle on a subset."""
+    """On a 0.25M-triangle scene the fast and wide layouts agree with the
+    threaded walk on the GPU, and all with the oracle on a subset."""
     g, sc, osc = helpers.both(name, 1)
     cam = kgr.camera(g.eye, g.target, g.fov, 16 / 9)
     rays = np.concatenate([helpers.camera_rays(cam, 320, 180), helpers.random_rays(g, 40000, 15)])
     fast = gpu_closest(sc, rays, kgr.LAYOUT_FAST)
     thr = gpu_closest(sc, rays, kgr.LAYOUT_THREADED)
+    wide = gpu_closest(sc, rays, kgr.LAYOUT_WIDE)
     assert_hits_equal(fast, thr)
+    assert_hits_equal(wide, thr)
     ref, _ = osc.trace_closest(rays[::7])
     assert_hits_equal(fast[::7], ref["raw"])
+
+
+@pytest.mark.parametrize("name", ["box4k", "terrain_s", "terrain"])
+def test_wide_layout_is_built(name):
+    """The wide layout exists for the benchmark scenes and its worst-case
+    walk fits the 64-entry traversal stack."""
+    g = kgr.Generated(name, 1)
+    sc = kgr.Scene.from_generated(g)
+    info = sc.info()
+    assert info.wide_node_count > 0
+    assert 0 < info.wide_max_stack < 64
+    assert info.wide_node_count < info.fast_node_count

@@ -1237,7 +1237,7 @@ void render_restir_gi(kgr_attachment *att, const kgr_launch_info *info, const kg
 	KGR_REQUIRE(iters >= 0 && iters <= 16, KGR_ERR_INVALID_ARGUMENT, "gi_spatial_iterations must be 0..16");
 	int in = cur, outb = tmp;
 	for (int k = 0; k < iters; k++) {
-		gi_spatial(s, fp, gb, in, outb, st);
+		gi_spatial(s, fp, gb, in, outb, k, st);
 		att->mark(STAGE_RESTIR_SPATIAL, st);
 		std::swap(in, outb);
 		launches++;

@@ -64,6 +64,12 @@ namespace kgr {
 namespace {
 
 #define KGR_GI_RIS_SALT 0x9E3779B9u
+/* Random streams of the reuse passes: the temporal pass and spatial
+ * iteration i draw from pixel_seed(pixel, frame, salt + pass).  Every pass
+ * has its own stream; a pass that replayed another pass's uniforms would
+ * resample candidates that already depend on those uniforms, and the
+ * selection would no longer be independent of the candidates. */
+#define KGR_GI_REUSE_SALT 0x47495255u
 #define KGR_GI_COS_10DEG 0.984807753f
 /* A shift whose Jacobian leaves [1/10, 10] is invalid: reconnecting to a
  * secondary vertex much nearer one receiver than the other (a crease, a
@@ -412,9 +418,8 @@ __global__ void __launch_bounds__(128) gi_temporal_kernel(DeviceScene s, FramePa
 	GiRes C = load_gi(gb.res[cur], pix);
 	int32_t pM = P.M < fp.gi_mcap ? P.M : fp.gi_mcap;
 	SurfaceHit h = receiver(fp, gb, pix, g);
-	float4 av = gb.auxiliary[pix];
 	GiMerge r;
-	r.init(mk(av.x, av.y, av.z));
+	r.init(pixel_seed(pix, fp.frame, KGR_GI_REUSE_SALT));
 	r.update(C.s, gi_target(h, C.s) * C.W * C.M, -1);
 	float J = gi_jacobian(g.x, gp.x, P.s);
 	float wp = gi_target(h, P.s) * J * P.W * pM;
@@ -455,7 +460,7 @@ __device__ __forceinline__ int gi_neighbor(const FrameParams &fp, int index, f3 
 #define KGR_GI_MAX_NEIGHBORS 16
 
 __global__ void __launch_bounds__(128) gi_spatial_kernel(DeviceScene s, FrameParams fp, GiFrameBuffers gb,
-		int in, int out)
+		int in, int out, int iteration)
 {
 	uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
 	if (pix >= fp.npix)
@@ -468,9 +473,8 @@ __global__ void __launch_bounds__(128) gi_spatial_kernel(DeviceScene s, FramePar
 	}
 	float depth = length(g.x - v3(fp.center));
 	SurfaceHit h = receiver(fp, gb, pix, g);
-	float4 av = gb.auxiliary[pix];
 	GiMerge r;
-	r.init(mk(av.x, av.y, av.z));
+	r.init(pixel_seed(pix, fp.frame, KGR_GI_REUSE_SALT + 1u + (uint32_t)iteration));
 	r.update(C.s, gi_target(h, C.s) * C.W * C.M, -1);
 	int32_t nidx[KGR_GI_MAX_NEIGHBORS];
 	int32_t nM[KGR_GI_MAX_NEIGHBORS];
@@ -593,9 +597,9 @@ void gi_temporal(const DeviceScene &s, const FrameParams &fp, const GiFrameBuffe
 }
 
 void gi_spatial(const DeviceScene &s, const FrameParams &fp, const GiFrameBuffers &gb, int in, int out,
-		cudaStream_t st)
+		int iteration, cudaStream_t st)
 {
-	gi_spatial_kernel<<<(fp.npix + 127) / 128, 128, 0, st>>>(s, fp, gb, in, out);
+	gi_spatial_kernel<<<(fp.npix + 127) / 128, 128, 0, st>>>(s, fp, gb, in, out, iteration);
 	KGR_CUDA(cudaGetLastError());
 }
 

@@ -33,7 +33,7 @@ void gi_primary(const DeviceScene &s, const PathBuffers &pb, const FrameParams &
 void gi_initial(const PathBuffers &pb, const FrameParams &fp, const GiFrameBuffers &gb, int cur, cudaStream_t st);
 void gi_temporal(const DeviceScene &s, const FrameParams &fp, const GiFrameBuffers &gb, int cur, int prev,
 		cudaStream_t st);
-void gi_spatial(const DeviceScene &s, const FrameParams &fp, const GiFrameBuffers &gb, int in, int out,
+void gi_spatial(const DeviceScene &s, const FrameParams &fp, const GiFrameBuffers &gb, int in, int out, int iteration,
 		cudaStream_t st);
 void gi_final(const DeviceScene &s, const FrameParams &fp, const GiFrameBuffers &gb, const OutputBuffers &out,
 		int fin, cudaStream_t st);

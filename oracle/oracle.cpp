@@ -1397,6 +1397,7 @@ void oracle_render_restir(const oracle_scene *s, const oracle_render_params *p,
 namespace {
 
 const float GI_COS_10DEG = 0.984807753f;
+const uint32_t GI_REUSE_SALT = 0x47495255u; /* streams of the reuse passes (gi.cu) */
 /* shifts with a Jacobian outside [1/10, 10] are invalid (gi.cu) */
 #define KGR_GI_JACOBIAN_MIN 0.1f
 #define KGR_GI_JACOBIAN_MAX 10.0f
@@ -1728,7 +1729,7 @@ extern "C" void oracle_render_gi(const oracle_scene *s, const oracle_render_para
 				SurfaceHit h = gi_receiver(mats[pix], g, center);
 				GiMergeO r;
 				r.sel = {mk(0.0f), mk(0.0f), mk(0.0f), true};
-				r.seed = load4(aux.data(), pix);
+				r.seed = pixel_seed((uint32_t)pix, p->frame, GI_REUSE_SALT);
 				r.update(cs, gi_target(h, cs) * cW * cM, -1);
 				float J = gi_jac(g.x, gp.x, ps);
 				float wp = gi_target(h, ps) * J * pW * pMc;
@@ -1773,7 +1774,7 @@ extern "C" void oracle_render_gi(const oracle_scene *s, const oracle_render_para
 				SurfaceHit h = gi_receiver(mats[pix], g, center);
 				GiMergeO r;
 				r.sel = {mk(0.0f), mk(0.0f), mk(0.0f), true};
-				r.seed = load4(aux.data(), pix);
+				r.seed = pixel_seed((uint32_t)pix, p->frame, GI_REUSE_SALT + 1u + (uint32_t)it);
 				r.update(cs, gi_target(h, cs) * cW * cM, -1);
 				int Msum = cM;
 				for (int i = 0; i < st->gi_neighbors; i++) {

@@ -235,6 +235,58 @@ kgr_status kgr_batcher_render(kgr_batcher *b, const kgr_scene *scene, const kgr_
 	});
 }
 
+kgr_status kgr_batcher_autotune(kgr_batcher *b, const kgr_scene *scene, const kgr_batch_job *jobs, uint32_t n,
+		const kgr_batch_options *options, int32_t frames, void *stream, kgr_autotune_result *result)
+{
+	return guard_call([&] {
+		KGR_REQUIRE(b && options && scene, KGR_ERR_INVALID_ARGUMENT, "NULL argument");
+		KGR_REQUIRE(frames >= 1 && frames <= 256, KGR_ERR_INVALID_ARGUMENT, "frames must be 1..256");
+		DeviceGuard guard(b->device);
+		cudaStream_t st = static_cast<cudaStream_t>(stream);
+		kgr_batch_options opt = *options;
+		TraceTune old = b->tune;
+		kgr_autotune_result res;
+		memset(&res, 0, sizeof(res));
+		try {
+			double best = -1.0;
+			for (const kgr_trace_tune &c : tune_candidates(scene)) {
+				opt.layout = c.layout;
+				b->tune.shadow = (int16_t)c.shadow;
+				b->tune.block = (int16_t)c.block;
+				double ms = time_frames([&] { b->render(scene, jobs, n, opt, st); }, frames, st);
+				if (c.layout == KGR_LAYOUT_FAST && c.shadow == KGR_TRACE_GRID && c.block == 128)
+					res.default_ms = ms;
+				if (best < 0.0 || ms < best) {
+					best = ms;
+					res.best = c;
+				}
+				res.candidates++;
+			}
+			res.best_ms = best;
+		} catch (...) {
+			b->tune = old;
+			throw;
+		}
+		b->tune.shadow = (int16_t)res.best.shadow;
+		b->tune.block = (int16_t)res.best.block;
+		if (result)
+			*result = res;
+	});
+}
+
+kgr_status kgr_batcher_set_tune(kgr_batcher *b, const kgr_trace_tune *tune)
+{
+	return guard_call([&] {
+		KGR_REQUIRE(b && tune, KGR_ERR_INVALID_ARGUMENT, "NULL argument");
+		KGR_REQUIRE(tune->shadow == KGR_TRACE_GRID || tune->shadow == KGR_TRACE_PERSISTENT,
+			KGR_ERR_INVALID_ARGUMENT, "unknown shadow kernel");
+		KGR_REQUIRE(tune->block == 64 || tune->block == 128 || tune->block == 256, KGR_ERR_INVALID_ARGUMENT,
+			"block must be 64, 128 or 256");
+		b->tune.shadow = (int16_t)tune->shadow;
+		b->tune.block = (int16_t)tune->block;
+	});
+}
+
 kgr_status kgr_batcher_ray_counts(kgr_batcher *b, uint64_t counts[3])
 {
 	return guard_call([&] {

@@ -1457,27 +1457,102 @@ kgr_status kgr_get_option(const kgr_attachment *att, const char *name, kgr_value
 	});
 }
 
+namespace {
+
+/* One frame of an attachment on `st` (the body of kgr_render). */
+void render_frame(kgr_attachment *att, const kgr_launch_info *info, const kgr_scene *sc, cudaStream_t st)
+{
+	if (att->opt_int("reset_history", 0)) {
+		att->reset_history(st);
+		att->options.erase("reset_history");
+	}
+	switch (att->kind) {
+	case KIND_PT:
+		if (att->opt_int("cache", 0))
+			render_pt_cached(att, info, sc, st);
+		else
+			render_pt(att, info, sc, st);
+		break;
+	case KIND_RESTIR_DI: render_restir_di(att, info, sc, st); break;
+	case KIND_RESTIR_GI: render_restir_gi(att, info, sc, st); break;
+	default: throw Error(KGR_ERR_UNSUPPORTED, "attachment kind not built");
+	}
+}
+
+} /* namespace */
+
 kgr_status kgr_render(kgr_attachment *att, const kgr_launch_info *info, const kgr_scene *sc, void *stream)
 {
 	return guarded([&] {
 		check_launch(att, info, sc);
 		DeviceGuard g(att->device);
+		render_frame(att, info, sc, (cudaStream_t)stream);
+	});
+}
+
+kgr_status kgr_autotune(kgr_attachment *att, const kgr_launch_info *info, const kgr_scene *sc, int32_t frames,
+		void *stream, kgr_autotune_result *result)
+{
+	return guarded([&] {
+		check_launch(att, info, sc);
+		KGR_REQUIRE(frames >= 1 && frames <= 256, KGR_ERR_INVALID_ARGUMENT, "frames must be 1..256");
+		DeviceGuard g(att->device);
 		cudaStream_t st = (cudaStream_t)stream;
-		if (att->opt_int("reset_history", 0)) {
-			att->reset_history(st);
-			att->options.erase("reset_history");
+		/* the options override the tuned shape: set them aside while tuning */
+		std::map<std::string, OptionValue> held;
+		for (const char *k : {"layout", "trace_shadow", "trace_block"}) {
+			auto it = att->options.find(k);
+			if (it != att->options.end()) {
+				held[k] = it->second;
+				att->options.erase(it);
+			}
 		}
-		switch (att->kind) {
-		case KIND_PT:
-			if (att->opt_int("cache", 0))
-				render_pt_cached(att, info, sc, st);
-			else
-				render_pt(att, info, sc, st);
-			break;
-		case KIND_RESTIR_DI: render_restir_di(att, info, sc, st); break;
-		case KIND_RESTIR_GI: render_restir_gi(att, info, sc, st); break;
-		default: throw Error(KGR_ERR_UNSUPPORTED, "attachment kind not built");
+		int old_layout = att->tuned_layout;
+		TraceTune old_tune = att->tuned;
+		kgr_autotune_result res;
+		memset(&res, 0, sizeof(res));
+		try {
+			double best = -1.0;
+			for (const kgr_trace_tune &c : tune_candidates(sc)) {
+				att->tuned_layout = c.layout;
+				att->tuned.shadow = (int16_t)c.shadow;
+				att->tuned.block = (int16_t)c.block;
+				double ms = time_frames([&] { render_frame(att, info, sc, st); }, frames, st);
+				if (c.layout == KGR_LAYOUT_FAST && c.shadow == KGR_TRACE_GRID && c.block == 128)
+					res.default_ms = ms;
+				if (best < 0.0 || ms < best) {
+					best = ms;
+					res.best = c;
+				}
+				res.candidates++;
+			}
+			res.best_ms = best;
+			att->tuned_layout = res.best.layout;
+			att->tuned.shadow = (int16_t)res.best.shadow;
+			att->tuned.block = (int16_t)res.best.block;
+		} catch (...) {
+			att->tuned_layout = old_layout;
+			att->tuned = old_tune;
+			for (auto &kv : held)
+				att->options[kv.first] = kv.second;
+			throw;
 		}
+		for (auto &kv : held)
+			att->options[kv.first] = kv.second;
+		if (result)
+			*result = res;
+	});
+}
+
+kgr_status kgr_get_trace_tune(const kgr_attachment *att, kgr_trace_tune *tune)
+{
+	return guarded([&] {
+		KGR_REQUIRE(att && tune, KGR_ERR_INVALID_ARGUMENT, "NULL argument");
+		TraceTune t = att->trace_tune();
+		tune->layout = att->layout();
+		tune->shadow = t.shadow;
+		tune->block = t.block;
+		tune->reserved = 0;
 	});
 }
 

@@ -237,6 +237,49 @@ inline int layout_for(int layout, const kgr_scene *sc)
 	return (layout == KGR_LAYOUT_WIDE && sc && !sc->wide_node_count) ? KGR_LAYOUT_FAST : layout;
 }
 
+/* Every launch shape the autotuner tries on a scene. */
+inline std::vector<kgr_trace_tune> tune_candidates(const kgr_scene *sc)
+{
+	std::vector<kgr_trace_tune> c;
+	for (int layout : {KGR_LAYOUT_FAST, KGR_LAYOUT_WIDE}) {
+		if (layout == KGR_LAYOUT_WIDE && !sc->wide_node_count)
+			continue;
+		for (int shadow : {KGR_TRACE_GRID, KGR_TRACE_PERSISTENT})
+			for (int block : {64, 128, 256})
+				c.push_back(kgr_trace_tune{layout, shadow, block, 0});
+	}
+	return c;
+}
+
+/* Time `frames` calls of `frame` on `st` (one untimed call first): ms per
+ * call from CUDA events. */
+template <class F>
+inline double time_frames(F frame, int frames, cudaStream_t st)
+{
+	frame();
+	cudaEvent_t e0, e1;
+	KGR_CUDA(cudaEventCreate(&e0));
+	KGR_CUDA(cudaEventCreate(&e1));
+	double ms = 0.0;
+	try {
+		KGR_CUDA(cudaEventRecord(e0, st));
+		for (int f = 0; f < frames; f++)
+			frame();
+		KGR_CUDA(cudaEventRecord(e1, st));
+		KGR_CUDA(cudaEventSynchronize(e1));
+		float t = 0.0f;
+		KGR_CUDA(cudaEventElapsedTime(&t, e0, e1));
+		ms = (double)t / frames;
+	} catch (...) {
+		cudaEventDestroy(e0);
+		cudaEventDestroy(e1);
+		throw;
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	return ms;
+}
+
 /* ------------------------------------------------------ kernel launchers -- */
 
 /* Traversal of a ray buffer (8 floats per ray) into hits or occlusion flags. */

@@ -49,6 +49,8 @@
 using namespace kgr;
 using Clock = std::chrono::steady_clock;
 
+#define KGR_SERVER_MAX_SCENES 256
+
 namespace {
 
 double ms_between(Clock::time_point a, Clock::time_point b)
@@ -67,6 +69,8 @@ struct Request {
 	Clock::time_point t_submit, t_admit, t_first, t_done;
 	bool launched = false;
 	uint32_t scheduled = 0, completed = 0, ticks = 0;
+	double credit = 0.0;     /* FAIR: paths banked toward the next slice */
+	uint64_t last_tick = 0;  /* FAIR: tick number of the last slice (0: none yet) */
 	uint64_t bytes = 0;
 	float4 *color = nullptr; /* device accumulation, width * height */
 	float4 *aov = nullptr;   /* ReSTIR: normal, albedo, position */
@@ -88,9 +92,13 @@ struct Tick {
 	kgr_attachment *restir = nullptr;
 };
 
+/* A resident "restir_di" attachment of one resolution; `owner` is the
+ * request whose frames it renders (its temporal history is that request's),
+ * NULL while it waits in the pool. */
 struct RestirEntry {
 	uint32_t width, height;
 	kgr_attachment *att;
+	const void *owner;
 };
 
 uint64_t request_bytes(const kgr_request &q)
@@ -110,6 +118,12 @@ struct kgr_server {
 	kgr_batcher *batcher = nullptr;
 	cudaStream_t stream = nullptr, copy_stream = nullptr;
 	std::vector<const kgr_scene *> scenes;
+	/* per scene: tuned layout and launch shape (autotune), -1 = not yet */
+	struct SceneTune {
+		int layout = -1;
+		kgr_trace_tune tune = {KGR_LAYOUT_FAST, KGR_TRACE_GRID, 128, 0};
+	};
+	std::vector<SceneTune> scene_tune;
 
 	std::mutex mu; /* guards everything callers touch */
 	std::condition_variable cv_done, cv_work;
@@ -172,6 +186,9 @@ struct kgr_server {
 		if (r->aov)
 			cudaFreeAsync(r->aov, stream);
 		r->color = r->aov = nullptr;
+		for (auto &e : restir)
+			if (e.owner == r)
+				e.owner = nullptr; /* back to the pool: later work on it is stream-ordered */
 		if (r->copied) {
 			event_pool.push_back(r->copied);
 			r->copied = nullptr;
@@ -252,11 +269,18 @@ struct kgr_server {
 		event_pool.push_back(t.ev);
 	}
 
-	kgr_attachment *restir_for(uint32_t w, uint32_t h)
+	/* the attachment rendering request r: its own, or a free one of its
+	 * resolution from the pool, or a new one */
+	kgr_attachment *restir_for(const Request *r, uint32_t w, uint32_t h)
 	{
 		for (auto &e : restir)
-			if (e.width == w && e.height == h)
+			if (e.owner == r)
 				return e.att;
+		for (auto &e : restir)
+			if (!e.owner && e.width == w && e.height == h) {
+				e.owner = r;
+				return e.att;
+			}
 		kgr_attachment *att = nullptr;
 		KGR_REQUIRE(kgr_create("restir_di", &att) == KGR_OK, KGR_ERR_INTERNAL, kgr_last_error());
 		kgr_context ctx = {w, h, device, 0};
@@ -265,7 +289,7 @@ struct kgr_server {
 			kgr_destroy(att);
 			throw Error(KGR_ERR_OUT_OF_MEMORY, "ReSTIR attachment: " + msg);
 		}
-		restir.push_back(RestirEntry{w, h, att});
+		restir.push_back(RestirEntry{w, h, att, r});
 		return att;
 	}
 
@@ -275,13 +299,17 @@ struct kgr_server {
 		KGR_REQUIRE(kgr_set_option(att, name, &val) == KGR_OK, KGR_ERR_INTERNAL, kgr_last_error());
 	}
 
-	/* one ReSTIR DI request as its own tick */
+	/* frames of one ReSTIR DI request as a tick of their own: all of them
+	 * (FCFS) or one (FAIR, so that other requests run between its frames) */
 	void launch_restir(Request *r)
 	{
 		Tick t;
 		const kgr_request &q = r->req;
-		kgr_attachment *att = restir_for(q.width, q.height);
-		set_opt_int(att, "reset_history", 1, KGR_VALUE_BOOL);
+		kgr_attachment *att = restir_for(r, q.width, q.height);
+		uint32_t first = r->scheduled;
+		uint32_t count = cfg.policy == KGR_SCHEDULE_FAIR ? 1u : q.spp - first;
+		if (first == 0)
+			set_opt_int(att, "reset_history", 1, KGR_VALUE_BOOL);
 		set_opt_int(att, "russian_roulette", q.russian_roulette ? 1 : 0, KGR_VALUE_BOOL);
 		set_opt_int(att, "rr_start_depth", q.rr_start_depth, KGR_VALUE_INT);
 		size_t npix = (size_t)q.width * q.height;
@@ -291,14 +319,15 @@ struct kgr_server {
 		info.buffers.albedo = reinterpret_cast<float *>(r->aov + npix);
 		info.buffers.position = reinterpret_cast<float *>(r->aov + 2 * npix);
 		info.max_depth = (int32_t)q.max_depth;
-		for (uint32_t i = 0; i < q.spp; i++) {
+		for (uint32_t i = first; i < first + count; i++) {
 			info.frame = q.frame + i;
 			info.accumulate = i > 0;
 			info.samples = (int32_t)i;
 			KGR_REQUIRE(kgr_render(att, &info, scenes[q.scene], stream) == KGR_OK, KGR_ERR_CUDA, kgr_last_error());
 		}
-		r->scheduled = q.spp;
-		t.jobs.push_back(TickJob{r, q.spp});
+		r->scheduled = first + count;
+		r->last_tick = ticks + 1;
+		t.jobs.push_back(TickJob{r, count});
 		t.restir = att;
 		t.ev = take_event();
 		KGR_CUDA(cudaEventRecord(t.ev, stream));
@@ -321,14 +350,106 @@ struct kgr_server {
 		jobs_in_ticks += t.jobs.size();
 	}
 
+	/* Tune scene `id` (loop thread, nothing in flight): the autotuner over a
+	 * 1280x720 batch of a slice of samples into a scratch buffer. */
+	void tune_scene(uint32_t id, const kgr_request &like)
+	{
+		SceneTune &t = scene_tune[id];
+		const uint32_t w = 1280, h = 720;
+		uint32_t k = cfg.spp_per_tick ? cfg.spp_per_tick : 4;
+		while (k > 1 && (uint64_t)w * h * k > cfg.path_capacity)
+			k--;
+		float4 *buf = nullptr;
+		KGR_CUDA(cudaMallocAsync((void **)&buf, (size_t)w * h * sizeof(float4), stream));
+		kgr_launch_info cam;
+		memset(&cam, 0, sizeof(cam));
+		const float up[3] = {0.0f, 1.0f, 0.0f};
+		kgr_camera_setup(like.eye, like.target, up, like.fov_deg, (float)w / (float)h, &cam);
+		kgr_batch_job j;
+		memset(&j, 0, sizeof(j));
+		j.width = w;
+		j.height = h;
+		j.spp = k;
+		j.sample_count = k;
+		memcpy(j.center, cam.camera.center, 12);
+		memcpy(j.ax_u, cam.camera.ax_u, 12);
+		memcpy(j.ax_v, cam.camera.ax_v, 12);
+		memcpy(j.ax_w, cam.camera.ax_w, 12);
+		j.color = reinterpret_cast<float *>(buf);
+		kgr_batch_options opt;
+		memset(&opt, 0, sizeof(opt));
+		opt.max_depth = (int32_t)like.max_depth;
+		opt.russian_roulette = like.russian_roulette ? 1 : 0;
+		opt.rr_start_depth = like.rr_start_depth;
+		opt.use_graph = cfg.use_graph;
+		kgr_autotune_result res;
+		kgr_status st = kgr_batcher_autotune(batcher, scenes[id], &j, 1, &opt, 2, stream, &res);
+		cudaFreeAsync(buf, stream);
+		KGR_REQUIRE(st == KGR_OK, st, std::string("autotune: ") + kgr_last_error());
+		t.layout = res.best.layout;
+		t.tune = res.best;
+	}
+
+	/* FAIR composition over the requests of one scene (see KGR_SCHEDULE_FAIR). */
+	void compose_fair(const std::vector<Request *> &group, std::vector<uint32_t> &slice)
+	{
+		size_t n = group.size();
+		slice.assign(n, 0);
+		double share = (double)cfg.path_capacity / (double)n;
+		uint64_t room = cfg.path_capacity;
+		for (size_t i = 0; i < n; i++) {
+			Request *r = group[i];
+			uint64_t npix = (uint64_t)r->req.width * r->req.height;
+			uint32_t left = r->req.spp - r->scheduled;
+			r->credit = std::min(r->credit + share, (double)npix * left);
+			uint64_t k = (uint64_t)(r->credit / (double)npix);
+			k = std::min<uint64_t>(k, left);
+			if (cfg.spp_per_tick)
+				k = std::min<uint64_t>(k, cfg.spp_per_tick);
+			k = std::min<uint64_t>(k, room / npix);
+			slice[i] = (uint32_t)k;
+			room -= k * npix;
+			r->credit -= (double)(k * npix);
+		}
+		/* leftover capacity: requests nearest to a whole sample first */
+		std::vector<size_t> order(n);
+		for (size_t i = 0; i < n; i++)
+			order[i] = i;
+		std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+			auto need = [&](size_t i) {
+				Request *r = group[i];
+				return (double)r->req.width * r->req.height - r->credit;
+			};
+			return need(a) < need(b);
+		});
+		for (size_t i : order) {
+			Request *r = group[i];
+			uint64_t npix = (uint64_t)r->req.width * r->req.height;
+			uint32_t left = r->req.spp - r->scheduled - slice[i];
+			uint64_t k = std::min<uint64_t>(left, room / npix);
+			if (cfg.spp_per_tick)
+				k = std::min<uint64_t>(k, cfg.spp_per_tick - std::min(cfg.spp_per_tick, slice[i]));
+			if (!k)
+				continue;
+			slice[i] += (uint32_t)k;
+			room -= k * npix;
+			r->credit -= (double)(k * npix);
+		}
+	}
+
 	/* compose and launch one tick; false when nothing is left to schedule */
 	bool launch_tick()
 	{
 		Request *head = nullptr;
 		for (Request *r : active)
 			if (r->scheduled < r->req.spp) {
-				head = r;
-				break;
+				if (cfg.policy != KGR_SCHEDULE_FAIR) {
+					head = r;
+					break;
+				}
+				/* FAIR: the request served longest ago (never served first) */
+				if (!head || r->last_tick < head->last_tick)
+					head = r;
 			}
 		if (!head)
 			return false;
@@ -342,15 +463,37 @@ struct kgr_server {
 			return true;
 		}
 		const kgr_request &h = head->req;
-		std::vector<kgr_batch_job> jobs;
-		Tick t;
-		uint64_t paths = 0;
+		if (cfg.autotune && scene_tune[h.scene].layout < 0) {
+			if (!inflight.empty())
+				return false; /* tune with nothing in flight: its frames reuse the batcher's ring */
+			try {
+				tune_scene(h.scene, h);
+			} catch (const Error &e) {
+				set_last_error(e.what());
+				scene_tune[h.scene].layout = cfg.layout; /* keep the configured shape */
+			}
+		}
+		std::vector<Request *> group;
 		for (Request *r : active) {
 			const kgr_request &q = r->req;
 			if (q.kind != KGR_REQUEST_PATH_TRACER || r->scheduled >= q.spp || q.scene != h.scene ||
 					q.max_depth != h.max_depth || (q.russian_roulette != 0) != (h.russian_roulette != 0) ||
 					q.rr_start_depth != h.rr_start_depth)
 				continue;
+			group.push_back(r);
+		}
+		if (cfg.policy == KGR_SCHEDULE_FAIR)
+			std::stable_sort(group.begin(), group.end(),
+				[](const Request *a, const Request *b) { return a->last_tick < b->last_tick; });
+		std::vector<uint32_t> fair;
+		if (cfg.policy == KGR_SCHEDULE_FAIR)
+			compose_fair(group, fair);
+		std::vector<kgr_batch_job> jobs;
+		Tick t;
+		uint64_t paths = 0;
+		for (size_t gi = 0; gi < group.size(); gi++) {
+			Request *r = group[gi];
+			const kgr_request &q = r->req;
 			uint64_t npix = (uint64_t)q.width * q.height;
 			uint32_t k = q.spp - r->scheduled;
 			if (cfg.spp_per_tick)
@@ -358,6 +501,8 @@ struct kgr_server {
 			uint64_t fit = (cfg.path_capacity - paths) / npix;
 			if (fit < k)
 				k = (uint32_t)fit;
+			if (cfg.policy == KGR_SCHEDULE_FAIR)
+				k = std::min(k, fair[gi]);
 			if (k == 0)
 				continue;
 			kgr_batch_job j;
@@ -386,6 +531,18 @@ struct kgr_server {
 		opt.rr_start_depth = h.rr_start_depth;
 		opt.layout = cfg.layout;
 		opt.use_graph = cfg.use_graph;
+		if (cfg.autotune) {
+			const SceneTune &st = scene_tune[h.scene];
+			opt.layout = st.layout;
+			batcher->tune.shadow = (int16_t)st.tune.shadow;
+			batcher->tune.block = (int16_t)st.tune.block;
+		}
+		if (jobs.empty()) {
+			/* FAIR: every share of this scene is still banking toward a
+			 * sample; serve the head alone */
+			head->last_tick = ticks + 1;
+			return true;
+		}
 		try {
 			batcher->render(scenes[h.scene], jobs.data(), (uint32_t)jobs.size(), opt, stream);
 			t.batch_slot = batcher->last;
@@ -397,8 +554,10 @@ struct kgr_server {
 				fail_active(j.r, e.status);
 			return true;
 		}
-		for (auto &j : t.jobs)
+		for (auto &j : t.jobs) {
 			j.r->scheduled += j.k;
+			j.r->last_tick = ticks + 1;
+		}
 		note_launch(t);
 		inflight.push_back(std::move(t));
 		return true;
@@ -544,11 +703,16 @@ kgr_status kgr_server_create(const kgr_server_config *config, kgr_server **out)
 		KGR_REQUIRE(config->layout == KGR_LAYOUT_FAST || config->layout == KGR_LAYOUT_THREADED ||
 				config->layout == KGR_LAYOUT_WIDE,
 			KGR_ERR_INVALID_ARGUMENT, "unknown layout");
+		KGR_REQUIRE(config->policy == KGR_SCHEDULE_FCFS || config->policy == KGR_SCHEDULE_FAIR,
+			KGR_ERR_INVALID_ARGUMENT, "unknown scheduling policy");
 		int dev = pick_device_ordinal(config->device);
 		DeviceGuard g(dev);
 		std::unique_ptr<kgr_server> s(new kgr_server());
 		s->cfg = *config;
 		s->device = dev;
+		/* the loop thread reads these without the lock: no reallocation */
+		s->scenes.reserve(KGR_SERVER_MAX_SCENES);
+		s->scene_tune.reserve(KGR_SERVER_MAX_SCENES);
 		kgr_status st = kgr_batcher_create(dev, config->path_capacity, config->max_jobs, &s->batcher);
 		KGR_REQUIRE(st == KGR_OK, st, std::string("batcher: ") + kgr_last_error());
 		KGR_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
@@ -570,7 +734,9 @@ kgr_status kgr_server_add_scene(kgr_server *s, const kgr_scene *scene, uint32_t 
 		KGR_REQUIRE(s && scene && id, KGR_ERR_INVALID_ARGUMENT, "NULL argument");
 		KGR_REQUIRE(scene->device == s->device, KGR_ERR_INVALID_ARGUMENT, "scene on another device");
 		std::lock_guard<std::mutex> lk(s->mu);
+		KGR_REQUIRE(s->scenes.size() < KGR_SERVER_MAX_SCENES, KGR_ERR_INVALID_ARGUMENT, "too many scenes");
 		s->scenes.push_back(scene);
+		s->scene_tune.emplace_back();
 		*id = (uint32_t)(s->scenes.size() - 1);
 	});
 }

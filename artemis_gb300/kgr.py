@@ -45,6 +45,23 @@ class SceneInfo(ctypes.Structure):
                 ("wide_node_count", c_u32), ("wide_max_stack", c_u32)]
 
 
+class TraceTune(ctypes.Structure):
+    _fields_ = [("layout", c_i32), ("shadow", c_i32), ("block", c_i32), ("reserved", c_i32)]
+
+    def as_dict(self):
+        return {"layout": {0: "fast", 1: "threaded", 2: "wide"}[self.layout],
+                "shadow": {0: "grid", 1: "persistent"}[self.shadow], "block": self.block}
+
+
+class AutotuneResult(ctypes.Structure):
+    _fields_ = [("best", TraceTune), ("best_ms", ctypes.c_double), ("default_ms", ctypes.c_double),
+                ("candidates", c_u32), ("reserved", c_u32)]
+
+    def as_dict(self):
+        return {"best": self.best.as_dict(), "best_ms": round(self.best_ms, 3),
+                "default_ms": round(self.default_ms, 3), "candidates": self.candidates}
+
+
 class Value(ctypes.Structure):
     _fields_ = [("tag", c_i32), ("i", c_i32), ("f", c_f), ("b", c_i32), ("s", ctypes.c_char_p)]
 
@@ -143,6 +160,10 @@ def lib():
             "kgr_camera_setup": (c_i32, [vp, vp, vp, c_f, c_f, vp]),
             "kgr_batcher_create": (c_i32, [c_i32, c_u32, c_u32, vp]),
             "kgr_batcher_render": (c_i32, [vp, vp, vp, c_u32, vp, vp]),
+            "kgr_batcher_autotune": (c_i32, [vp, vp, vp, c_u32, vp, c_i32, vp, vp]),
+            "kgr_batcher_set_tune": (c_i32, [vp, vp]),
+            "kgr_autotune": (c_i32, [vp, vp, vp, c_i32, vp, vp]),
+            "kgr_get_trace_tune": (c_i32, [vp, vp]),
             "kgr_batcher_ray_counts": (c_i32, [vp, vp]),
             "kgr_batcher_launch_info": (c_i32, [vp, vp, vp]),
             "kgr_batcher_destroy": (c_i32, [vp]),
@@ -418,6 +439,18 @@ class Attachment:
         check(lib().kgr_get_render_stats(self.handle, ctypes.byref(s)))
         return s
 
+    def autotune(self, info, scene, frames=3, stream=None):
+        """kgr_autotune: time every traversal launch shape on `frames` real
+        frames of `info`, keep the fastest; returns the result as a dict."""
+        r = AutotuneResult()
+        check(lib().kgr_autotune(self.handle, ctypes.byref(info), scene.handle, frames, stream, ctypes.byref(r)))
+        return r.as_dict()
+
+    def trace_tune(self):
+        t = TraceTune()
+        check(lib().kgr_get_trace_tune(self.handle, ctypes.byref(t)))
+        return t.as_dict()
+
     STAGES = ("generate", "trace_closest", "shade", "shadow", "accumulate", "restir_primary",
               "restir_temporal", "restir_spatial", "restir_finalize", "cache_infer", "cache_train")
 
@@ -482,7 +515,11 @@ REQUEST_PATH_TRACER, REQUEST_RESTIR_DI = 0, 1
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("device", c_i32), ("path_capacity", c_u32), ("max_jobs", c_u32), ("spp_per_tick", c_u32),
-                ("memory_budget", c_u64), ("layout", c_i32), ("use_graph", c_i32), ("reserved", c_i32 * 2)]
+                ("memory_budget", c_u64), ("layout", c_i32), ("use_graph", c_i32), ("autotune", c_i32),
+                ("policy", c_i32)]
+
+
+SCHEDULE_FCFS, SCHEDULE_FAIR = 0, 1
 
 
 class Request(ctypes.Structure):
@@ -531,6 +568,17 @@ class Batcher:
         opt = BatchOptions(max_depth, 1 if russian_roulette else 0, rr_start_depth, layout, 1 if use_graph else 0)
         check(lib().kgr_batcher_render(self.handle, scene.handle, arr, len(jobs), ctypes.byref(opt), stream))
 
+    def autotune(self, scene, jobs, frames=3, max_depth=8, russian_roulette=True, rr_start_depth=3,
+                 use_graph=True, stream=None):
+        """kgr_batcher_autotune; returns the result dict (best["layout"] is the
+        layout to render with from then on)."""
+        arr = (BatchJob * len(jobs))(*jobs)
+        opt = BatchOptions(max_depth, 1 if russian_roulette else 0, rr_start_depth, LAYOUT_FAST, 1 if use_graph else 0)
+        r = AutotuneResult()
+        check(lib().kgr_batcher_autotune(self.handle, scene.handle, arr, len(jobs), ctypes.byref(opt), frames, stream,
+                                         ctypes.byref(r)))
+        return r.as_dict()
+
     def ray_counts(self):
         c = (c_u64 * 3)()
         check(lib().kgr_batcher_ray_counts(self.handle, c))
@@ -557,9 +605,9 @@ class Server:
     """kgr_server: the render request loop (host thread inside libkgr)."""
 
     def __init__(self, path_capacity=1 << 24, max_jobs=256, spp_per_tick=0, memory_budget=120 << 30,
-                 layout=LAYOUT_FAST, use_graph=True, device=-1):
+                 layout=LAYOUT_FAST, use_graph=True, device=-1, autotune=False, policy=SCHEDULE_FCFS):
         cfg = ServerConfig(device, path_capacity, max_jobs, spp_per_tick, memory_budget, layout,
-                           1 if use_graph else 0)
+                           1 if use_graph else 0, 1 if autotune else 0, policy)
         h = vp()
         check(lib().kgr_server_create(ctypes.byref(cfg), ctypes.byref(h)))
         self.handle = h

@@ -42,10 +42,14 @@ WORKLOAD = ("plain PT 1920x1080 4spp, max depth 8, RR from depth 3, NEE over 102
             "procedural terrain 1.16M tris (512^2 height field + 2000 icospheres), SAH leaves<=4")
 
 # Kernel behind each traversal stage, per layout.
-KERNELS = {("trace_closest", "fast"): "fast_persistent_kernel<false>",
-           ("shadow", "fast"): "shadow_resolve_kernel<fast>",
+KERNELS = {("trace_closest", "fast"): "fast_persistent_kernel<closest, fast>",
+           ("shadow", "fast"): "shadow_resolve_kernel<fast> | fast_persistent_kernel<any, fast>",
+           ("trace_closest", "wide"): "fast_persistent_kernel<closest, wide>",
+           ("shadow", "wide"): "shadow_resolve_kernel<wide> | fast_persistent_kernel<any, wide>",
            ("trace_closest", "threaded"): "trace_closest_kernel<threaded>",
            ("shadow", "threaded"): "shadow_resolve_kernel<threaded>"}
+# bytes a visit reads on each layout: (node, triangle)
+LAYOUT_BYTES = {"fast": (64, 48), "wide": (128, 48), "threaded": (48, 80)}
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
 # traversal kernels at this workload, from one ncu capture of a smaller frame
 # of the same scene scaled by the rays it traced; None where not captured.
@@ -63,7 +67,8 @@ def parse():
     ap.add_argument("--spp", type=int, default=4)
     ap.add_argument("--max-depth", type=int, default=8)
     ap.add_argument("--scene", default="terrain")
-    ap.add_argument("--layout", default="fast", choices=["fast", "threaded"])
+    ap.add_argument("--layout", default="auto", choices=["auto", "fast", "wide", "threaded"],
+                    help="auto: the autotuner picks layout, shadow kernel and block size before warm-up")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU sample time per measurement")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-quality", action="store_true",
@@ -254,7 +259,8 @@ def relmse_compare(args, g, sc, W, H, stream, sptr):
         a.set_option("spp", spp)
         a.set_option("russian_roulette", True)
         a.set_option("rr_start_depth", 3)
-        a.set_option("layout", args.layout)
+        for k, v in args.trace_options.items():
+            a.set_option(k, v)
         if cache:
             a.set_option("cache", True)
         return a
@@ -466,14 +472,18 @@ def serve_run(args):
     `mrays_per_s_pt` the camera, bounce and shadow rays of the path-tracer
     ticks (ReSTIR's reuse passes do not count their shadow rays).  Latency = submission to image in host memory;
     `latency_per_mpath` divides it by the request's paths (pixels x spp),
-    which removes the 1700x spread of request sizes."""
+    which removes the 1700x spread of request sizes; `by_resolution` gives
+    p50/p99 per resolution class.  The server schedules with processor
+    sharing (KGR_SCHEDULE_FAIR) and tunes each scene's traversal launch shape
+    before its first tick (the warm-up requests trigger it)."""
     from artemis_gb300 import kgr
 
     t_build = time.perf_counter()
     gens = [kgr.Generated(n, 1) for n in SERVE_SCENES]
     scenes = [kgr.Scene.from_generated(g) for g in gens]
     build_s = time.perf_counter() - t_build
-    srv = kgr.Server(path_capacity=1 << 24, max_jobs=256, spp_per_tick=4, memory_budget=120 << 30)
+    srv = kgr.Server(path_capacity=1 << 24, max_jobs=256, spp_per_tick=4, memory_budget=120 << 30,
+                     policy=kgr.SCHEDULE_FAIR, autotune=True)
     sids = [srv.add_scene(sc) for sc in scenes]
 
     def submit(i, w, h, spp, kind, frame):
@@ -513,6 +523,12 @@ def serve_run(args):
         mpaths = np.array([w * h * spp / 1e6 for (_, _, w, h, spp, _), r in zip(arrivals, res) if r.status == 0])
         norm = lat / mpaths
         q = lambda a, p: round(float(np.percentile(a, p)), 2) if len(a) else None
+        res_of = [(w, h) for (_, _, w, h, _, _), r in zip(arrivals, res) if r.status == 0]
+        by_res = {}
+        for (w, h) in SERVE_RES:
+            a = np.array([x for x, wh in zip(lat, res_of) if wh == (w, h)])
+            if len(a):
+                by_res[f"{w}x{h}"] = {"n": len(a), "p50": q(a, 50), "p99": q(a, 99)}
         return {"offered_rps": rate, "window_s": seconds, "requests": len(arrivals), "completed": len(ok),
                 "failed": len(res) - len(ok), "wall_s": round(wall, 2),
                 "completed_rps": round(len(ok) / wall, 2),
@@ -520,6 +536,7 @@ def serve_run(args):
                 "mrays_per_s_pt": round((s1.rays - s0.rays) / wall / 1e6, 1),
                 "latency_ms": {"p50": q(lat, 50), "p90": q(lat, 90), "p99": q(lat, 99), "max": q(lat, 100)},
                 "latency_per_mpath_ms": {"p50": q(norm, 50), "p99": q(norm, 99)},
+                "by_resolution": by_res,
                 "queue_ms_p50": q(np.array([r.queue_ms for r in ok]), 50),
                 "ticks": int(s1.ticks - s0.ticks)}
 
@@ -529,7 +546,7 @@ def serve_run(args):
     out = {"scenes": {n: sc.info().triangle_count for n, sc in zip(SERVE_SCENES, scenes)},
            "scene_build_s": round(build_s, 1),
            "server": {"path_capacity": 1 << 24, "max_jobs": 256, "spp_per_tick": 4, "memory_budget_gb": 120,
-                      "graphs": True},
+                      "graphs": True, "policy": "fair (processor sharing)", "autotune": True},
            "mean_jobs_per_tick": round(st.mean_jobs_per_tick, 2), "graph_replays": int(st.graph_replays),
            "peak_budget_gb": round(st.peak_budget_bytes / 2 ** 30, 2),
            "phase_200rps": p1, "phase_sustainable": p2}
@@ -561,7 +578,6 @@ def bench_ours(args):
     att.set_option("spp", args.spp)
     att.set_option("russian_roulette", True)
     att.set_option("rr_start_depth", 3)
-    att.set_option("layout", args.layout)
     stream = torch.cuda.current_stream()
     sptr = ctypes.c_void_p(stream.cuda_stream)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -570,6 +586,16 @@ def bench_ours(args):
         return kgr.launch_info(cam, W, H, [b.data_ptr() for b in bufs], max_depth=args.max_depth,
                                samples=samples, accumulate=False, frame=step)
 
+    tuned = None
+    if args.layout == "auto":
+        tuned = att.autotune(info_for(0), sc, frames=2, stream=sptr)
+        layout = tuned["best"]["layout"]
+    else:
+        layout = args.layout
+    att.set_option("layout", layout)
+    t = att.trace_tune()
+    # the comparison runs and the cached tracer use the same launch shape
+    args.trace_options = {"layout": layout, "trace_shadow": t["shadow"], "trace_block": t["block"]}
     for s in range(args.warmup):
         att.render(info_for(s), sc, sptr)
     torch.cuda.synchronize()
@@ -578,14 +604,14 @@ def bench_ours(args):
     # the reference's threaded layout: both layouts give bit-identical paths,
     # so the second count is the reference walk over the same rays
     visits = {}
-    for lay in dict.fromkeys((args.layout, "threaded")):
+    for lay in dict.fromkeys((layout, "threaded")):
         att.set_option("layout", lay)
         att.set_option("count_visits", True)
         att.render(info_for(0), sc, sptr)
         torch.cuda.synchronize()
         visits[lay] = att.visit_counts()
     att.set_option("count_visits", False)
-    att.set_option("layout", args.layout)
+    att.set_option("layout", layout)
     att.stats()
 
     # timed region
@@ -648,8 +674,8 @@ def bench_ours(args):
     def stage_bytes(v, node_b, tri_b):
         return {"trace_closest": v[0] * node_b + v[1] * tri_b, "shadow": v[2] * node_b + v[3] * tri_b}
 
-    ref_bytes = stage_bytes(visits["threaded"], 48, 80)
-    own_bytes = stage_bytes(visits[args.layout], *((64, 48) if args.layout == "fast" else (48, 80)))
+    ref_bytes = stage_bytes(visits["threaded"], *LAYOUT_BYTES["threaded"])
+    own_bytes = stage_bytes(visits[layout], *LAYOUT_BYTES[layout])
     dom = max(("trace_closest", "shadow"), key=lambda k: stages[k][0])
     ms_dom, n_dom = stages[dom]
     launches_frame = n_dom / max(1, args.steps)
@@ -658,13 +684,13 @@ def bench_ours(args):
     own = own_bytes[dom] / max(1, launches_frame) / launch_s / 1e9
     hbm = peaks.get("hbm_gbs")
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-                "frac": round(achieved / hbm, 4), "traffic": TRAFFIC.get((dom, args.layout)),
-                "kernel": KERNELS.get((dom, args.layout), dom), "peak_source": peak_kind,
+                "frac": round(achieved / hbm, 4), "traffic": TRAFFIC.get((dom, layout)),
+                "kernel": KERNELS.get((dom, layout), dom), "peak_source": peak_kind,
                 "work_unit": "reference threaded walk: 48 B per interior record, 80 B per leaf record",
                 "l2": {"peak_measured_read_gbs": round(l2_gbs, 1), "frac": round(achieved / l2_gbs, 4)},
                 "own_layout": {"achieved": round(own, 1), "l2_frac": round(own / l2_gbs, 4),
                                "hbm_frac": round(own / hbm, 4)},
-                "visits_per_frame": {"reference": list(visits["threaded"]), args.layout: list(visits[args.layout])}}
+                "visits_per_frame": {"reference": list(visits["threaded"]), layout: list(visits[layout])}}
 
     quality = None
     if rank == 0 and not args.no_quality:
@@ -695,7 +721,8 @@ def bench_ours(args):
                 "data": "synthetic (seeded procedural scene, random-free camera)",
                 "config": {"workload": WORKLOAD, "scene": args.scene, "triangles": info_s.triangle_count,
                            "lights": info_s.light_count, "resolution": [W, H], "spp": args.spp,
-                           "max_depth": args.max_depth, "layout": args.layout,
+                           "max_depth": args.max_depth, "layout": layout, "trace_tune": att.trace_tune(),
+                           "autotune": tuned,
                            "l2_flush": "256 MB buffer written between timed steps",
                            "parallelism": "replicas" if ws > 1 else "1 GPU"},
                 "ms_per_frame": round(total_ms / args.steps, 3),

@@ -330,6 +330,45 @@ kgr_status kgr_get_render_stats(const kgr_attachment *att, kgr_render_stats *sta
  * the last event, then resets the totals. */
 kgr_status kgr_get_stage_times(kgr_attachment *att, double *ms, uint32_t *launches, uint32_t count);
 
+/* ------------------------------------------------------------- autotuner -- */
+
+/* Launch shape of the traversal stages on the fast and wide layouts.  All
+ * shapes return the same hits -- the per-ray walk is the same, only the
+ * mapping of rays onto threads and of children onto nodes changes -- so the
+ * choice is one of speed alone.  No counterpart in the reference, whose
+ * traversal runs inside OptiX. */
+enum { KGR_TRACE_GRID = 0, KGR_TRACE_PERSISTENT = 1 };
+typedef struct kgr_trace_tune {
+	int32_t layout; /* KGR_LAYOUT_FAST or KGR_LAYOUT_WIDE */
+	int32_t shadow; /* shadow stage: KGR_TRACE_GRID (a ray per thread, grid-stride)
+	                 * or KGR_TRACE_PERSISTENT (lanes refill as their rays end);
+	                 * the closest-hit stage is always persistent */
+	int32_t block;  /* threads per block of both stages: 64, 128 or 256 */
+	int32_t reserved;
+} kgr_trace_tune;
+
+typedef struct kgr_autotune_result {
+	kgr_trace_tune best;
+	double best_ms;       /* ms per frame of the chosen shape */
+	double default_ms;    /* ms per frame of the untuned shape {fast, grid, 128} */
+	uint32_t candidates;  /* shapes timed */
+	uint32_t reserved;
+} kgr_autotune_result;
+
+/* The project's autotuner: renders `frames` frames of `info` (after one
+ * untimed frame) with every launch shape the scene admits -- layouts fast
+ * and wide (when built) x shadow kernel x block size -- times each on
+ * `stream` with CUDA events, and keeps the fastest as this attachment's
+ * shape.  The options "layout", "trace_shadow" and "trace_block" still
+ * override it field by field.  The frames are real renders: they write
+ * info's buffers and advance ReSTIR history and radiance-cache training.
+ * Synchronous. */
+kgr_status kgr_autotune(kgr_attachment *att, const kgr_launch_info *info, const kgr_scene *scene,
+		int32_t frames, void *stream, kgr_autotune_result *result);
+/* The shape an attachment renders with now (tuned or default, options
+ * applied). */
+kgr_status kgr_get_trace_tune(const kgr_attachment *att, kgr_trace_tune *tune);
+
 /* Traversal visit counts of the last frame rendered with the
  * "count_visits" option: {closest nodes, closest triangles, shadow nodes,
  * shadow triangles} on the layout the frame used. */

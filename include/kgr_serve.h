@@ -72,6 +72,15 @@ kgr_status kgr_batcher_create(int32_t device, uint32_t path_capacity, uint32_t m
  * the frame's end. */
 kgr_status kgr_batcher_render(kgr_batcher *b, const kgr_scene *scene, const kgr_batch_job *jobs, uint32_t n,
 		const kgr_batch_options *options, void *stream);
+/* The autotuner (kgr_autotune) for a batch: times `frames` frames of these
+ * jobs with every launch shape the scene admits and keeps the fastest
+ * shadow kernel and block size for later frames; result->best.layout is the
+ * layout to pass in kgr_batch_options from then on.  The frames are real
+ * renders into the jobs' buffers.  Synchronous. */
+kgr_status kgr_batcher_autotune(kgr_batcher *b, const kgr_scene *scene, const kgr_batch_job *jobs, uint32_t n,
+		const kgr_batch_options *options, int32_t frames, void *stream, kgr_autotune_result *result);
+/* Set the shadow kernel and block size directly (layout goes in the options). */
+kgr_status kgr_batcher_set_tune(kgr_batcher *b, const kgr_trace_tune *tune);
 /* Rays of the last frame: camera, bounce and shadow (waits for the frame). */
 kgr_status kgr_batcher_ray_counts(kgr_batcher *b, uint64_t counts[3]);
 /* Launches of the last frame and whether it ran as a graph replay. */
@@ -82,15 +91,27 @@ kgr_status kgr_batcher_destroy(kgr_batcher *b);
 
 enum { KGR_REQUEST_PATH_TRACER = 0, KGR_REQUEST_RESTIR_DI = 1 };
 
+/* Tick composition.  FCFS: the oldest request with samples left picks the
+ * tick's scene, then requests of that scene join oldest first, each with as
+ * many samples as fit.  FAIR: processor sharing -- the tick goes to the
+ * scene of the request served longest ago, its requests share the path
+ * capacity equally (a request too large for its share banks the share until
+ * a whole sample fits), and capacity left over goes to the requests closest
+ * to their next sample; latency then grows with a request's size instead of
+ * with the size of the requests queued before it. */
+enum { KGR_SCHEDULE_FCFS = 0, KGR_SCHEDULE_FAIR = 1 };
+
 typedef struct kgr_server_config {
 	int32_t device;
 	uint32_t path_capacity;   /* paths of one tick's shared frame */
 	uint32_t max_jobs;        /* requests in one tick */
 	uint32_t spp_per_tick;    /* samples a request advances per tick; 0 = as many as fit */
 	uint64_t memory_budget;   /* bytes of request buffers (accumulation, reservoirs) admitted at once */
-	int32_t layout;           /* KGR_LAYOUT_* */
+	int32_t layout;           /* KGR_LAYOUT_*; with autotune, the layout tuned per scene */
 	int32_t use_graph;
-	int32_t reserved[2];
+	int32_t autotune;         /* tune each scene's traversal launch shape (kgr_batcher_autotune on a
+	                           * 1280x720 batch) before its first tick */
+	int32_t policy;           /* KGR_SCHEDULE_* */
 } kgr_server_config;
 
 typedef struct kgr_request {

@@ -36,10 +36,15 @@ def eye_of(g, i):
     return (np.array(g.eye, np.float32) + np.float32(0.05) * i).tolist()
 
 
-def test_same_image_alone_and_in_the_mix():
+@pytest.mark.parametrize("policy,autotune", [(kgr.SCHEDULE_FCFS, False), (kgr.SCHEDULE_FAIR, False),
+                                             (kgr.SCHEDULE_FAIR, True)])
+def test_same_image_alone_and_in_the_mix(policy, autotune):
+    """Under either scheduling policy, with or without per-scene tuning of
+    the traversal launch shape, a request gives the same image alone, in a
+    mix, and as the attachment renders it."""
     g, sc, _ = helpers.both("box4k", 1)
     w, h, spp, frame = 80, 60, 5, 11
-    srv = kgr.Server(path_capacity=1 << 15, max_jobs=8, spp_per_tick=2)
+    srv = kgr.Server(path_capacity=1 << 15, max_jobs=8, spp_per_tick=2, policy=policy, autotune=autotune)
     sid = srv.add_scene(sc)
     alone = np.zeros((w * h, 4), np.float32)
     r = srv.wait(srv.submit(sid, w, h, spp, eye_of(g, 0), g.target, g.fov, alone, max_depth=DEPTH, frame=frame),
@@ -138,3 +143,24 @@ def test_restir_request_equals_attachment_frames():
     ref = attachment_render(sc, g, w, h, 1, frame, g.eye, kind="restir_di", rr=False, frames=frames)
     assert np.array_equal(outs[0], ref)
     assert np.array_equal(outs[1], ref)
+
+
+def test_fair_policy_serves_small_requests_beside_a_large_one():
+    """Processor sharing: small requests submitted behind a large one finish
+    first; under FCFS the large one holds the ticks until it is done."""
+    g, sc, _ = helpers.both("box4k", 1)
+    lat = {}
+    for policy in (kgr.SCHEDULE_FCFS, kgr.SCHEDULE_FAIR):
+        srv = kgr.Server(path_capacity=1 << 16, max_jobs=8, spp_per_tick=2, policy=policy)
+        sid = srv.add_scene(sc)
+        big = srv.submit(sid, 256, 256, 16, g.eye, g.target, g.fov, max_depth=DEPTH, frame=1)
+        small = [srv.submit(sid, 32, 32, 2, eye_of(g, i), g.target, g.fov, max_depth=DEPTH, frame=2 + i)
+                 for i in range(4)]
+        rb = srv.wait(big, 120000.0)
+        rs = [srv.wait(i, 120000.0) for i in small]
+        srv.close()
+        assert rb.status == 0 and all(r.status == 0 for r in rs)
+        lat[policy] = (rb.latency_ms, max(r.latency_ms for r in rs))
+    # FCFS: the small requests wait for the large one; FAIR: they do not
+    assert lat[kgr.SCHEDULE_FCFS][1] >= 0.5 * lat[kgr.SCHEDULE_FCFS][0]
+    assert lat[kgr.SCHEDULE_FAIR][1] < 0.5 * lat[kgr.SCHEDULE_FAIR][0]

@@ -120,7 +120,7 @@ void kgr_batcher::render(const kgr_scene *scene, const kgr_batch_job *jobs, uint
 		for (auto &e : graphs)
 			if (e.scene == scene && e.max_depth == fp.max_depth && e.rr == fp.russian_roulette &&
 					e.rr_start == fp.rr_start_depth && e.layout == fp.layout &&
-					e.tune.shadow == tune.shadow &&
+					e.tune.shadow == tune.shadow && e.tune.occupancy == tune.occupancy &&
 					e.tune.block == tune.block)
 				g = &e;
 		if (!g) {
@@ -253,8 +253,9 @@ kgr_status kgr_batcher_autotune(kgr_batcher *b, const kgr_scene *scene, const kg
 				opt.layout = c.layout;
 				b->tune.shadow = (int16_t)c.shadow;
 				b->tune.block = (int16_t)c.block;
+				b->tune.occupancy = (int16_t)c.occupancy;
 				double ms = time_frames([&] { b->render(scene, jobs, n, opt, st); }, frames, st);
-				if (c.layout == KGR_LAYOUT_FAST && c.shadow == KGR_TRACE_GRID && c.block == 128)
+				if (c.layout == KGR_LAYOUT_FAST && c.shadow == KGR_TRACE_GRID && c.block == 128 && !c.occupancy)
 					res.default_ms = ms;
 				if (best < 0.0 || ms < best) {
 					best = ms;
@@ -269,6 +270,7 @@ kgr_status kgr_batcher_autotune(kgr_batcher *b, const kgr_scene *scene, const kg
 		}
 		b->tune.shadow = (int16_t)res.best.shadow;
 		b->tune.block = (int16_t)res.best.block;
+		b->tune.occupancy = (int16_t)res.best.occupancy;
 		if (result)
 			*result = res;
 	});
@@ -282,8 +284,10 @@ kgr_status kgr_batcher_set_tune(kgr_batcher *b, const kgr_trace_tune *tune)
 			KGR_ERR_INVALID_ARGUMENT, "unknown shadow kernel");
 		KGR_REQUIRE(tune->block == 64 || tune->block == 128 || tune->block == 256, KGR_ERR_INVALID_ARGUMENT,
 			"block must be 64, 128 or 256");
+		KGR_REQUIRE(tune->occupancy == 0 || tune->occupancy == 1, KGR_ERR_INVALID_ARGUMENT, "occupancy is 0 or 1");
 		b->tune.shadow = (int16_t)tune->shadow;
 		b->tune.block = (int16_t)tune->block;
+		b->tune.occupancy = (int16_t)tune->occupancy;
 	});
 }
 

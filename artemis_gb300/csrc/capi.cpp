@@ -285,6 +285,10 @@ void finish_scene(kgr_scene *sc, const Tree &tree, const std::vector<PrimBox> &b
 	sc->d_fast_nodes.upload(nodes);
 	if (!wide.empty())
 		sc->d_wide_nodes.upload(wide);
+	/* the traversal reads nodes with 32-byte vector loads */
+	static_assert(sizeof(FastNode) == 64 && sizeof(WideNode) == 128, "node sizes");
+	KGR_REQUIRE(((uintptr_t)sc->d_fast_nodes.ptr & 31) == 0 && ((uintptr_t)sc->d_wide_nodes.ptr & 31) == 0,
+		KGR_ERR_INTERNAL, "node arrays are not 32-byte aligned");
 	sc->d_fast_tris.upload(tri_records);
 	sc->d_materials.upload(sc->materials);
 	sc->d_lights.upload(sc->lights);
@@ -694,7 +698,8 @@ struct kgr_attachment {
 
 	/* Launch shape of the fast/wide traversal: the shape kgr_autotune chose
 	 * (or the default), with any field the options set overriding it:
-	 * trace_shadow "grid" | "persistent", trace_block 64 | 128 | 256. */
+	 * trace_shadow "grid" | "persistent", trace_block 64 | 128 | 256,
+	 * trace_occupancy 0 | 1. */
 	TraceTune tuned = default_trace_tune();
 	TraceTune trace_tune() const
 	{
@@ -707,6 +712,9 @@ struct kgr_attachment {
 		int b = opt_int("trace_block", 0);
 		if (b == 64 || b == 128 || b == 256)
 			t.block = (int16_t)b;
+		int o = opt_int("trace_occupancy", -1);
+		if (o == 0 || o == 1)
+			t.occupancy = (int16_t)o;
 		return t;
 	}
 
@@ -1395,7 +1403,7 @@ static const std::map<std::string, OptionValue> &option_defaults()
 		{"gi_radius", 30},
 		{"cache", false}, {"cache_train", true}, {"cache_train_paths", 16384}, {"cache_lr", 1e-3f},
 		{"cache_dtype", std::string("bf16")}, {"reset_history", false},
-		{"trace_shadow", std::string("")}, {"trace_block", 0}};
+		{"trace_shadow", std::string("")}, {"trace_block", 0}, {"trace_occupancy", -1}};
 	return d;
 }
 
@@ -1500,7 +1508,7 @@ kgr_status kgr_autotune(kgr_attachment *att, const kgr_launch_info *info, const 
 		cudaStream_t st = (cudaStream_t)stream;
 		/* the options override the tuned shape: set them aside while tuning */
 		std::map<std::string, OptionValue> held;
-		for (const char *k : {"layout", "trace_shadow", "trace_block"}) {
+		for (const char *k : {"layout", "trace_shadow", "trace_block", "trace_occupancy"}) {
 			auto it = att->options.find(k);
 			if (it != att->options.end()) {
 				held[k] = it->second;
@@ -1517,8 +1525,9 @@ kgr_status kgr_autotune(kgr_attachment *att, const kgr_launch_info *info, const 
 				att->tuned_layout = c.layout;
 				att->tuned.shadow = (int16_t)c.shadow;
 				att->tuned.block = (int16_t)c.block;
+				att->tuned.occupancy = (int16_t)c.occupancy;
 				double ms = time_frames([&] { render_frame(att, info, sc, st); }, frames, st);
-				if (c.layout == KGR_LAYOUT_FAST && c.shadow == KGR_TRACE_GRID && c.block == 128)
+				if (c.layout == KGR_LAYOUT_FAST && c.shadow == KGR_TRACE_GRID && c.block == 128 && !c.occupancy)
 					res.default_ms = ms;
 				if (best < 0.0 || ms < best) {
 					best = ms;
@@ -1530,6 +1539,7 @@ kgr_status kgr_autotune(kgr_attachment *att, const kgr_launch_info *info, const 
 			att->tuned_layout = res.best.layout;
 			att->tuned.shadow = (int16_t)res.best.shadow;
 			att->tuned.block = (int16_t)res.best.block;
+			att->tuned.occupancy = (int16_t)res.best.occupancy;
 		} catch (...) {
 			att->tuned_layout = old_layout;
 			att->tuned = old_tune;
@@ -1552,7 +1562,7 @@ kgr_status kgr_get_trace_tune(const kgr_attachment *att, kgr_trace_tune *tune)
 		tune->layout = att->layout();
 		tune->shadow = t.shadow;
 		tune->block = t.block;
-		tune->reserved = 0;
+		tune->occupancy = t.occupancy;
 	});
 }
 

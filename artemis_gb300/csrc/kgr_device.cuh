@@ -178,16 +178,27 @@ __device__ __forceinline__ FastRay fast_ray(const f3 &o, const f3 &d)
 	return r;
 }
 
+/* 32-byte load through the read-only path: one 256-bit vector load
+ * (ld.global.nc.v8.f32, sm_100 and later) instead of two 128-bit ones.  p
+ * must be 32-byte aligned: node arrays come from cudaMalloc (256-byte
+ * aligned) and nodes are 64 or 128 bytes, which the scene build checks. */
+__device__ __forceinline__ void ldg256(const float4 *p, float4 &a, float4 &b)
+{
+	asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+		: "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+		: "l"(p));
+}
+
 /* One child-pair node: which children the ray reaches within [0, best_t],
  * nearer one first.  Returns the number of children hit (0, 1 or 2). */
 __device__ __forceinline__ int fast_node(const DeviceScene &s, const FastRay &r, int32_t ref, float best_t,
 		int32_t &first, int32_t &second)
 {
 	const float4 *np = reinterpret_cast<const float4 *>(s.fast_nodes + ref);
-	float4 lxy = __ldg(np + 0);
-	float4 rxy = __ldg(np + 1);
-	float4 lrz = __ldg(np + 2);
-	int4 refs = __ldg(reinterpret_cast<const int4 *>(np + 3));
+	float4 lxy, rxy, lrz, rv;
+	ldg256(np, lxy, rxy);
+	ldg256(np + 2, lrz, rv);
+	int4 refs = make_int4(__float_as_int(rv.x), __float_as_int(rv.y), __float_as_int(rv.z), __float_as_int(rv.w));
 	float l0x = __fmaf_rn(lxy.x, r.ix, -r.ox), l1x = __fmaf_rn(lxy.y, r.ix, -r.ox);
 	float l0y = __fmaf_rn(lxy.z, r.iy, -r.oy), l1y = __fmaf_rn(lxy.w, r.iy, -r.oy);
 	float l0z = __fmaf_rn(lrz.x, r.iz, -r.oz), l1z = __fmaf_rn(lrz.y, r.iz, -r.oz);
@@ -296,9 +307,12 @@ __device__ __forceinline__ bool node_step(const DeviceScene &s, const FastRay &r
 {
 	if (LAYOUT == KGR_LAYOUT_WIDE) {
 		const float4 *np = reinterpret_cast<const float4 *>(s.wide_nodes + ref);
-		float4 lx = __ldg(np + 0), hx = __ldg(np + 1), ly = __ldg(np + 2);
-		float4 hy = __ldg(np + 3), lz = __ldg(np + 4), hz = __ldg(np + 5);
-		int4 rf = __ldg(reinterpret_cast<const int4 *>(np + 6));
+		float4 lx, hx, ly, hy, lz, hz, rr, unused;
+		ldg256(np + 0, lx, hx);
+		ldg256(np + 2, ly, hy);
+		ldg256(np + 4, lz, hz);
+		ldg256(np + 6, rr, unused);
+		int4 rf = make_int4(__float_as_int(rr.x), __float_as_int(rr.y), __float_as_int(rr.z), __float_as_int(rr.w));
 		float t0 = wide_child(r, lx.x, hx.x, ly.x, hy.x, lz.x, hz.x, rf.x, best_t);
 		float t1 = wide_child(r, lx.y, hx.y, ly.y, hy.y, lz.y, hz.y, rf.y, best_t);
 		float t2 = wide_child(r, lx.z, hx.z, ly.z, hy.z, lz.z, hz.z, rf.z, best_t);

@@ -246,7 +246,8 @@ inline std::vector<kgr_trace_tune> tune_candidates(const kgr_scene *sc)
 			continue;
 		for (int shadow : {KGR_TRACE_GRID, KGR_TRACE_PERSISTENT})
 			for (int block : {64, 128, 256})
-				c.push_back(kgr_trace_tune{layout, shadow, block, 0});
+				for (int occ : {0, 1})
+					c.push_back(kgr_trace_tune{layout, shadow, block, occ});
 	}
 	return c;
 }

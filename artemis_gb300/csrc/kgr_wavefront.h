@@ -75,9 +75,10 @@ enum TraceKernel {
 };
 
 struct TraceTune {
-	int16_t shadow; /* TraceKernel of the shadow stage (closest hit is always persistent) */
-	int16_t block;  /* threads per block: 64, 128 or 256 */
-	int16_t pad[2];
+	int16_t shadow;    /* TraceKernel of the shadow stage (closest hit is always persistent) */
+	int16_t block;     /* threads per block: 64, 128 or 256 */
+	int16_t occupancy; /* 1: registers capped so that 48 warps fit an SM */
+	int16_t pad;
 };
 
 /* The shape used when nothing was tuned. */
@@ -86,7 +87,8 @@ inline TraceTune default_trace_tune()
 	TraceTune t;
 	t.shadow = TRACE_GRID;
 	t.block = 128;
-	t.pad[0] = t.pad[1] = 0;
+	t.occupancy = 0;
+	t.pad = 0;
 	return t;
 }
 

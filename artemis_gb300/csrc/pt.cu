@@ -192,8 +192,12 @@ __global__ void __launch_bounds__(128) shade_kernel(DeviceScene s, PathBuffers p
 /* is_occluded for every queued shadow ray, then Ld = contr / pdf and
  * L += beta * (Le + Ld) in the order of the recursion.  One ray per thread,
  * grid-stride over the queue. */
-template <int LAYOUT, bool COUNT, int BLOCK>
-__global__ void __launch_bounds__(BLOCK) shadow_resolve_kernel(DeviceScene s, PathBuffers pb)
+/* Minimum resident blocks per SM a launch shape asks the compiler for:
+ * OCC = 1 caps registers so that 1536 threads (48 warps) fit an SM. */
+#define KGR_MIN_BLOCKS(BLOCK, OCC) ((OCC) ? 1536 / (BLOCK) : 1)
+
+template <int LAYOUT, bool COUNT, int BLOCK, int OCC = 0>
+__global__ void __launch_bounds__(BLOCK, KGR_MIN_BLOCKS(BLOCK, OCC)) shadow_resolve_kernel(DeviceScene s, PathBuffers pb)
 {
 	const uint32_t n = pb.counters[CNT_SHADOW];
 	uint32_t stride = gridDim.x * blockDim.x;
@@ -230,8 +234,9 @@ __device__ __forceinline__ void resolve_shadow(const PathBuffers &pb, uint32_t p
  * ray of its warp is done.  One loop iteration descends to a leaf and tests
  * it.  ANY: shadow rays, resolved into the path radiance.  The grid is sized
  * to the resident capacity of the GPU. */
-template <bool ANY, bool COUNT, int LAYOUT, int BLOCK>
-__global__ void __launch_bounds__(BLOCK) fast_persistent_kernel(DeviceScene s, PathBuffers pb, int q)
+template <bool ANY, bool COUNT, int LAYOUT, int BLOCK, int OCC = 0>
+__global__ void __launch_bounds__(BLOCK, KGR_MIN_BLOCKS(BLOCK, OCC)) fast_persistent_kernel(DeviceScene s,
+		PathBuffers pb, int q)
 {
 	const uint32_t n = ANY ? pb.counters[CNT_SHADOW] : pb.counters[q == 0 ? CNT_Q0 : CNT_Q1];
 	const uint32_t *queue = ANY ? pb.shadow_queue : pb.queue[q];
@@ -318,40 +323,59 @@ int resident_grid(K kernel, int block)
 
 /* One launch of a persistent traversal kernel over a resident grid (the
  * grid of each instantiation is computed once). */
-template <bool ANY, bool COUNT, int LAYOUT, int BLOCK>
+template <bool ANY, bool COUNT, int LAYOUT, int BLOCK, int OCC = 0>
 void launch_persistent(const DeviceScene &s, const PathBuffers &pb, int q, cudaStream_t st)
 {
-	static const int g = resident_grid(fast_persistent_kernel<ANY, COUNT, LAYOUT, BLOCK>, BLOCK);
-	fast_persistent_kernel<ANY, COUNT, LAYOUT, BLOCK><<<g, BLOCK, 0, st>>>(s, pb, q);
+	static const int g = resident_grid(fast_persistent_kernel<ANY, COUNT, LAYOUT, BLOCK, OCC>, BLOCK);
+	fast_persistent_kernel<ANY, COUNT, LAYOUT, BLOCK, OCC><<<g, BLOCK, 0, st>>>(s, pb, q);
+}
+
+template <bool ANY, int LAYOUT, int OCC>
+void launch_persistent_occ(const DeviceScene &s, const PathBuffers &pb, int q, int block, cudaStream_t st)
+{
+	if (block == 64)
+		launch_persistent<ANY, false, LAYOUT, 64, OCC>(s, pb, q, st);
+	else if (block == 256)
+		launch_persistent<ANY, false, LAYOUT, 256, OCC>(s, pb, q, st);
+	else
+		launch_persistent<ANY, false, LAYOUT, 128, OCC>(s, pb, q, st);
 }
 
 template <bool ANY, int LAYOUT>
-void launch_persistent_block(const DeviceScene &s, const PathBuffers &pb, int q, int block, cudaStream_t st)
+void launch_persistent_block(const DeviceScene &s, const PathBuffers &pb, int q, const TraceTune &t,
+		cudaStream_t st)
 {
-	if (block == 64)
-		launch_persistent<ANY, false, LAYOUT, 64>(s, pb, q, st);
-	else if (block == 256)
-		launch_persistent<ANY, false, LAYOUT, 256>(s, pb, q, st);
+	if (t.occupancy)
+		launch_persistent_occ<ANY, LAYOUT, 1>(s, pb, q, t.block, st);
 	else
-		launch_persistent<ANY, false, LAYOUT, 128>(s, pb, q, st);
+		launch_persistent_occ<ANY, LAYOUT, 0>(s, pb, q, t.block, st);
 }
 
-template <bool COUNT, int LAYOUT, int BLOCK>
+template <bool COUNT, int LAYOUT, int BLOCK, int OCC = 0>
 void launch_shadow_grid(const DeviceScene &s, const PathBuffers &pb, cudaStream_t st)
 {
-	static const int g = resident_grid(shadow_resolve_kernel<LAYOUT, COUNT, BLOCK>, BLOCK);
-	shadow_resolve_kernel<LAYOUT, COUNT, BLOCK><<<g, BLOCK, 0, st>>>(s, pb);
+	static const int g = resident_grid(shadow_resolve_kernel<LAYOUT, COUNT, BLOCK, OCC>, BLOCK);
+	shadow_resolve_kernel<LAYOUT, COUNT, BLOCK, OCC><<<g, BLOCK, 0, st>>>(s, pb);
+}
+
+template <int LAYOUT, int OCC>
+void launch_shadow_grid_occ(const DeviceScene &s, const PathBuffers &pb, int block, cudaStream_t st)
+{
+	if (block == 64)
+		launch_shadow_grid<false, LAYOUT, 64, OCC>(s, pb, st);
+	else if (block == 256)
+		launch_shadow_grid<false, LAYOUT, 256, OCC>(s, pb, st);
+	else
+		launch_shadow_grid<false, LAYOUT, 128, OCC>(s, pb, st);
 }
 
 template <int LAYOUT>
-void launch_shadow_grid_block(const DeviceScene &s, const PathBuffers &pb, int block, cudaStream_t st)
+void launch_shadow_grid_block(const DeviceScene &s, const PathBuffers &pb, const TraceTune &t, cudaStream_t st)
 {
-	if (block == 64)
-		launch_shadow_grid<false, LAYOUT, 64>(s, pb, st);
-	else if (block == 256)
-		launch_shadow_grid<false, LAYOUT, 256>(s, pb, st);
+	if (t.occupancy)
+		launch_shadow_grid_occ<LAYOUT, 1>(s, pb, t.block, st);
 	else
-		launch_shadow_grid<false, LAYOUT, 128>(s, pb, st);
+		launch_shadow_grid_occ<LAYOUT, 0>(s, pb, t.block, st);
 }
 
 /* accumulate (amadeus_path_tracer.cu:59-70), the frame's samples in order */
@@ -398,12 +422,12 @@ void pt_trace_closest(const DeviceScene &s, const PathBuffers &pb, int q, int la
 			if (c)
 				launch_persistent<false, true, KGR_LAYOUT_WIDE, 128>(s, pb, q, st);
 			else
-				launch_persistent_block<false, KGR_LAYOUT_WIDE>(s, pb, q, tune.block, st);
+				launch_persistent_block<false, KGR_LAYOUT_WIDE>(s, pb, q, tune, st);
 		} else {
 			if (c)
 				launch_persistent<false, true, KGR_LAYOUT_FAST, 128>(s, pb, q, st);
 			else
-				launch_persistent_block<false, KGR_LAYOUT_FAST>(s, pb, q, tune.block, st);
+				launch_persistent_block<false, KGR_LAYOUT_FAST>(s, pb, q, tune, st);
 		}
 	}
 	KGR_CUDA(cudaGetLastError());
@@ -443,13 +467,13 @@ void pt_shadow_resolve(const DeviceScene &s, const PathBuffers &pb, int layout, 
 	} else if (tune.shadow == TRACE_PERSISTENT) {
 		KGR_CUDA(cudaMemsetAsync(pb.counters + CNT_FETCH_SHADOW, 0, sizeof(uint32_t), st));
 		if (layout == KGR_LAYOUT_WIDE)
-			launch_persistent_block<true, KGR_LAYOUT_WIDE>(s, pb, 0, tune.block, st);
+			launch_persistent_block<true, KGR_LAYOUT_WIDE>(s, pb, 0, tune, st);
 		else
-			launch_persistent_block<true, KGR_LAYOUT_FAST>(s, pb, 0, tune.block, st);
+			launch_persistent_block<true, KGR_LAYOUT_FAST>(s, pb, 0, tune, st);
 	} else if (layout == KGR_LAYOUT_WIDE) {
-		launch_shadow_grid_block<KGR_LAYOUT_WIDE>(s, pb, tune.block, st);
+		launch_shadow_grid_block<KGR_LAYOUT_WIDE>(s, pb, tune, st);
 	} else {
-		launch_shadow_grid_block<KGR_LAYOUT_FAST>(s, pb, tune.block, st);
+		launch_shadow_grid_block<KGR_LAYOUT_FAST>(s, pb, tune, st);
 	}
 	KGR_CUDA(cudaGetLastError());
 }

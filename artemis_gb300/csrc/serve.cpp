@@ -300,14 +300,19 @@ struct kgr_server {
 	}
 
 	/* frames of one ReSTIR DI request as a tick of their own: all of them
-	 * (FCFS) or one (FAIR, so that other requests run between its frames) */
+	 * (FCFS), or as many as a path-tracer tick holds paths (FAIR, at least
+	 * one), so that other requests run between the frames of a large one */
 	void launch_restir(Request *r)
 	{
 		Tick t;
 		const kgr_request &q = r->req;
 		kgr_attachment *att = restir_for(r, q.width, q.height);
 		uint32_t first = r->scheduled;
-		uint32_t count = cfg.policy == KGR_SCHEDULE_FAIR ? 1u : q.spp - first;
+		uint32_t count = q.spp - first;
+		if (cfg.policy == KGR_SCHEDULE_FAIR) {
+			uint64_t fit = cfg.path_capacity / ((uint64_t)q.width * q.height);
+			count = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(count, fit));
+		}
 		if (first == 0)
 			set_opt_int(att, "reset_history", 1, KGR_VALUE_BOOL);
 		set_opt_int(att, "russian_roulette", q.russian_roulette ? 1 : 0, KGR_VALUE_BOOL);
@@ -536,6 +541,7 @@ struct kgr_server {
 			opt.layout = st.layout;
 			batcher->tune.shadow = (int16_t)st.tune.shadow;
 			batcher->tune.block = (int16_t)st.tune.block;
+			batcher->tune.occupancy = (int16_t)st.tune.occupancy;
 		}
 		if (jobs.empty()) {
 			/* FAIR: every share of this scene is still banking toward a

@@ -46,11 +46,12 @@ class SceneInfo(ctypes.Structure):
 
 
 class TraceTune(ctypes.Structure):
-    _fields_ = [("layout", c_i32), ("shadow", c_i32), ("block", c_i32), ("reserved", c_i32)]
+    _fields_ = [("layout", c_i32), ("shadow", c_i32), ("block", c_i32), ("occupancy", c_i32)]
 
     def as_dict(self):
         return {"layout": {0: "fast", 1: "threaded", 2: "wide"}[self.layout],
-                "shadow": {0: "grid", 1: "persistent"}[self.shadow], "block": self.block}
+                "shadow": {0: "grid", 1: "persistent"}[self.shadow], "block": self.block,
+                "occupancy": self.occupancy}
 
 
 class AutotuneResult(ctypes.Structure):

@@ -51,9 +51,10 @@ KERNELS = {("trace_closest", "fast"): "fast_persistent_kernel<closest, fast>",
 # bytes a visit reads on each layout: (node, triangle)
 LAYOUT_BYTES = {"fast": (64, 48), "wide": (128, 48), "threaded": (48, 80)}
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
-# traversal kernels at this workload, from one ncu capture of a smaller frame
-# of the same scene scaled by the rays it traced; None where not captured.
-TRAFFIC = {}
+# traversal kernels at this workload: one ncu capture of the 9 closest-hit
+# launches of a timed 1080p frame (--cache-control none), averaged per
+# launch; None where not captured.
+TRAFFIC = {("trace_closest", "fast"): 168.1e6}
 
 
 def parse():
@@ -595,7 +596,8 @@ def bench_ours(args):
     att.set_option("layout", layout)
     t = att.trace_tune()
     # the comparison runs and the cached tracer use the same launch shape
-    args.trace_options = {"layout": layout, "trace_shadow": t["shadow"], "trace_block": t["block"]}
+    args.trace_options = {"layout": layout, "trace_shadow": t["shadow"], "trace_block": t["block"],
+                          "trace_occupancy": t["occupancy"]}
     for s in range(args.warmup):
         att.render(info_for(s), sc, sptr)
     torch.cuda.synchronize()

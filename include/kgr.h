@@ -344,20 +344,21 @@ typedef struct kgr_trace_tune {
 	                 * or KGR_TRACE_PERSISTENT (lanes refill as their rays end);
 	                 * the closest-hit stage is always persistent */
 	int32_t block;  /* threads per block of both stages: 64, 128 or 256 */
-	int32_t reserved;
+	int32_t occupancy; /* 0: registers as the compiler chooses; 1: capped so that
+	                    * 48 warps fit an SM (more rays in flight per SM) */
 } kgr_trace_tune;
 
 typedef struct kgr_autotune_result {
 	kgr_trace_tune best;
 	double best_ms;       /* ms per frame of the chosen shape */
-	double default_ms;    /* ms per frame of the untuned shape {fast, grid, 128} */
+	double default_ms;    /* ms per frame of the untuned shape {fast, grid, 128, 0} */
 	uint32_t candidates;  /* shapes timed */
 	uint32_t reserved;
 } kgr_autotune_result;
 
 /* The project's autotuner: renders `frames` frames of `info` (after one
  * untimed frame) with every launch shape the scene admits -- layouts fast
- * and wide (when built) x shadow kernel x block size -- times each on
+ * and wide (when built) x shadow kernel x block size x occupancy -- times each on
  * `stream` with CUDA events, and keeps the fastest as this attachment's
  * shape.  The options "layout", "trace_shadow" and "trace_block" still
  * override it field by field.  The frames are real renders: they write

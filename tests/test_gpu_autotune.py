@@ -1,5 +1,5 @@
 """The autotuner: every traversal launch shape (layout fast or wide, shadow
-kernel, block size) renders the same image, so tuning changes speed only --
+kernel, block size, occupancy) renders the same image, so tuning changes speed only --
 the frame after kgr_autotune is bit-identical to the frame before it, for an
 attachment and for the batcher; options still override the tuned shape."""
 import numpy as np
@@ -27,12 +27,12 @@ def test_attachment_autotune_keeps_the_image(kind):
         att.set_option("temporal", False)
     att.set_option("russian_roulette", True)
     info = helpers.launch(cam, W, H, bufs, frame=5, max_depth=4)
-    assert att.trace_tune() == {"layout": "fast", "shadow": "grid", "block": 128}
+    assert att.trace_tune() == {"layout": "fast", "shadow": "grid", "block": 128, "occupancy": 0}
     att.render(info, sc)
     torch.cuda.synchronize()
     before = bufs[0].clone()
     res = att.autotune(info, sc, frames=2)
-    assert res["candidates"] == 12  # fast and wide x 2 shadow kernels x 3 block sizes
+    assert res["candidates"] == 24  # fast and wide x 2 shadow kernels x 3 block sizes x 2 occupancies
     assert 0 < res["best_ms"] <= res["default_ms"]
     assert att.trace_tune() == res["best"]
     att.render(info, sc)
@@ -57,7 +57,7 @@ def test_batcher_autotune_keeps_the_image():
     torch.cuda.synchronize()
     before = [o.clone() for o in outs]
     res = b.autotune(sc, jobs, frames=2, max_depth=4)
-    assert res["candidates"] == 12 and 0 < res["best_ms"] <= res["default_ms"]
+    assert res["candidates"] == 24 and 0 < res["best_ms"] <= res["default_ms"]
     layout = {"fast": kgr.LAYOUT_FAST, "wide": kgr.LAYOUT_WIDE}[res["best"]["layout"]]
     b.render(sc, jobs, max_depth=4, layout=layout)
     torch.cuda.synchronize()

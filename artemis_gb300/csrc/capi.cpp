@@ -1068,6 +1068,7 @@ void render_pt_cached(kgr_attachment *att, const kgr_launch_info *info, const kg
 		KGR_REQUIRE(kgr_mlp_create(dtype, 1, att->device, &att->cache_mlp) == KGR_OK, KGR_ERR_CUDA,
 			std::string("radiance cache: ") + kgr_last_error());
 	}
+	att->cache_mlp->infer = att->opt_str("cache_infer", "tcgen05") == "mma" ? KGR_MLP_INFER_MMA : KGR_MLP_INFER_TCGEN05;
 	MlpParams mp = att->cache_mlp->params();
 	CacheParams cp;
 	cp.dtype = dtype;
@@ -1402,7 +1403,7 @@ static const std::map<std::string, OptionValue> &option_defaults()
 		{"gi_temporal", true}, {"gi_mcap", 30}, {"gi_spatial_iterations", 3}, {"gi_neighbors", 8},
 		{"gi_radius", 30},
 		{"cache", false}, {"cache_train", true}, {"cache_train_paths", 16384}, {"cache_lr", 1e-3f},
-		{"cache_dtype", std::string("bf16")}, {"reset_history", false},
+		{"cache_dtype", std::string("bf16")}, {"cache_infer", std::string("tcgen05")}, {"reset_history", false},
 		{"trace_shadow", std::string("")}, {"trace_block", 0}, {"trace_occupancy", -1}};
 	return d;
 }

@@ -20,11 +20,17 @@ struct MlpParams {
 	void *wn, *wt;
 	float *partial;     /* per-block gradient slices [partial_blocks][6][64][64] */
 	int partial_blocks;
+	int infer;          /* KGR_MLP_INFER_MMA or KGR_MLP_INFER_TCGEN05 */
+	uint32_t *tc_err;   /* error word of the tcgen05 inference (bit 0: a wait ran out) */
 };
 
 /* out[i] = {r, g, b, 0} for the n rows of x ([n][64] half precision); with
  * n_dev, the row count is min(n, *n_dev) read on the device. */
 void mlp_infer(const MlpParams &mp, const void *x, uint32_t n, float4 *out, cudaStream_t st,
+		const uint32_t *n_dev = nullptr);
+/* The same on the fifth-generation tensor cores (mlp_tc.cu): tcgen05.mma
+ * with TMEM accumulators; sets bit 0 of *err if an mbarrier wait ran out. */
+void mlp_infer_tc(const MlpParams &mp, const void *x, uint32_t n, float4 *out, uint32_t *err, cudaStream_t st,
 		const uint32_t *n_dev = nullptr);
 /* grad (FP32, [6][64][64]) = d loss / d W over n rows; loss = sum of the
  * relative L2 terms (not divided by n).  Uses mp.partial as scratch; the
@@ -44,11 +50,14 @@ struct kgr_mlp {
 	int dtype = 0;
 	int step = 0;
 	int partial_blocks = 0;
+	int infer = KGR_MLP_INFER_TCGEN05;
 	kgr::DevBuf<float> master, m, v, grad, loss, partial;
 	kgr::DevBuf<uint16_t> wn, wt;
+	kgr::DevBuf<uint32_t> tc_err;
 	kgr::MlpParams params()
 	{
-		return kgr::MlpParams{dtype, master.ptr, m.ptr, v.ptr, wn.ptr, wt.ptr, partial.ptr, partial_blocks};
+		return kgr::MlpParams{dtype, master.ptr, m.ptr, v.ptr, wn.ptr, wt.ptr, partial.ptr, partial_blocks, infer,
+			tc_err.ptr};
 	}
 };
 

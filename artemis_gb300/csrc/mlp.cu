@@ -532,6 +532,10 @@ void mlp_infer(const MlpParams &mp, const void *x, uint32_t n, float4 *out, cuda
 {
 	if (n == 0)
 		return;
+	if (mp.infer == KGR_MLP_INFER_TCGEN05) {
+		mlp_infer_tc(mp, x, n, out, mp.tc_err, st, n_dev);
+		return;
+	}
 	int grid = device_sm_count() * 4;
 	size_t sm = infer_smem();
 	if (mp.dtype == KGR_MLP_BF16) {

@@ -52,6 +52,8 @@ void alloc_all(kgr_mlp *m)
 	m->wt.alloc(KGR_MLP_PARAMS);
 	m->partial_blocks = kgr::device_sm_count();
 	m->partial.alloc((size_t)m->partial_blocks * KGR_MLP_PARAMS);
+	m->tc_err.alloc(1);
+	KGR_CUDA(cudaMemset(m->tc_err.ptr, 0, sizeof(uint32_t)));
 	KGR_CUDA(cudaMemset(m->m.ptr, 0, KGR_MLP_PARAMS * 4));
 	KGR_CUDA(cudaMemset(m->v.ptr, 0, KGR_MLP_PARAMS * 4));
 	KGR_CUDA(cudaMemset(m->wn.ptr, 0, KGR_MLP_PARAMS * 2));
@@ -151,6 +153,31 @@ kgr_status kgr_mlp_train_step(kgr_mlp *m, const void *x, const float *targets, u
 		mlp_gradients(m->params(), x, reinterpret_cast<const float4 *>(targets), n, m->grad.ptr, m->loss.ptr, st);
 		m->step++;
 		mlp_adam(m->params(), m->grad.ptr, lr, m->step, st);
+	});
+}
+
+kgr_status kgr_mlp_set_inference(kgr_mlp *m, int32_t kernel)
+{
+	return guard([&] {
+		KGR_REQUIRE(m, KGR_ERR_INVALID_ARGUMENT, "NULL network");
+		KGR_REQUIRE(kernel == KGR_MLP_INFER_MMA || kernel == KGR_MLP_INFER_TCGEN05, KGR_ERR_INVALID_ARGUMENT,
+			"unknown inference kernel");
+		m->infer = kernel;
+	});
+}
+
+kgr_status kgr_mlp_check(kgr_mlp *m)
+{
+	return guard([&] {
+		KGR_REQUIRE(m, KGR_ERR_INVALID_ARGUMENT, "NULL network");
+		DeviceGuard g(m->device);
+		uint32_t e = 0;
+		KGR_CUDA(cudaDeviceSynchronize());
+		KGR_CUDA(cudaMemcpy(&e, m->tc_err.ptr, sizeof(e), cudaMemcpyDeviceToHost));
+		if (e) {
+			KGR_CUDA(cudaMemset(m->tc_err.ptr, 0, sizeof(uint32_t)));
+			throw Error(KGR_ERR_CUDA, "tensor-core inference: an mbarrier wait ran out of its iteration limit");
+		}
 	});
 }
 

@@ -1,0 +1,400 @@
+/*
+ * mlp_tc.cu -- radiance-cache network inference on the fifth-generation
+ * tensor cores: tcgen05.mma with the accumulator in tensor memory (TMEM).
+ *
+ * The network is the one of mlp.cu (64 inputs -> 5 x 64 ReLU -> 3 outputs,
+ * BF16 or FP16 weights and activations, FP32 accumulation); this kernel is
+ * an alternative to its mma.sync inference and computes the same function.
+ *
+ * One CTA of 128 threads works on tiles of 128 rows (the MMA's M):
+ *   weights        the six layers (B operands, N x K) in shared memory in
+ *                  the canonical K-major layout without swizzle: 8 x 8 core
+ *                  matrices of 128 contiguous bytes, K neighbours 128 bytes
+ *                  apart (leading byte offset), 8-row groups 1024 bytes apart
+ *                  (stride byte offset);
+ *   activations    two 128 x 64 tiles (A operands) in the K-major layout
+ *                  with the 128-byte swizzle: row r at r x 128 bytes, its
+ *                  16-byte chunk c at chunk c ^ (r mod 8).  A tile arrives by
+ *                  one TMA load (cp.async.bulk.tensor.2d, the tensor map's
+ *                  128-byte swizzle writes exactly this layout; rows past the
+ *                  end read as zero), and the next tile's load runs while the
+ *                  current one goes through the network;
+ *   TMEM           a 128-lane x 64-column FP32 accumulator, row i in lane i;
+ *   per layer      one thread issues four tcgen05.mma (K = 16 each; the A
+ *                  start address advances 32 bytes inside the swizzled row)
+ *                  and a tcgen05.commit to an mbarrier; after it every warp
+ *                  reads its 32 lanes with tcgen05.ld (32x32b), applies ReLU,
+ *                  rounds to half precision and writes the row back into the
+ *                  tile, swizzled, as the next layer's A operand.
+ *
+ * Every wait on an mbarrier is bounded.  A wait that runs out sets bit 0 of
+ * the error word; the block stops at the next layer boundary (the decision
+ * is taken by all its threads together), waits (bounded) for its TMA load in
+ * flight, frees its TMEM and returns; the host reads the word with
+ * kgr_mlp_check.
+ */
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <cuda.h>
+
+#include <mutex>
+#include <type_traits>
+
+#include "kgr_mlp.h"
+
+namespace kgr {
+
+namespace {
+
+#define TC_ROWS 128                 /* rows per tile: the MMA's M */
+#define TC_W 64                     /* hidden width and input width */
+#define TC_OUT 16                   /* N of the last layer (3 outputs used) */
+#define TC_LAYERS 6
+#define TC_LBO 128u                 /* bytes between K-neighbour core matrices */
+#define TC_SBO 1024u                /* bytes between 8-row groups (64-wide K) */
+#define TC_LAYER_BYTES 8192u        /* 64 x 64 half-precision weights */
+#define TC_W_BYTES (5u * TC_LAYER_BYTES + 2048u)
+#define TC_X_OFF 43008u             /* = TC_W_BYTES, a multiple of 1024 (swizzle atom) */
+#define TC_X_BYTES (TC_ROWS * TC_W * 2u)
+#define TC_BAR_OFF (TC_X_OFF + 2u * TC_X_BYTES)  /* MMA barrier, then one TMA barrier per tile */
+#define TC_SLOT_OFF (TC_BAR_OFF + 24u)
+#define TC_SMEM (TC_SLOT_OFF + 8u)              /* 75,808 bytes: three CTAs fit an SM */
+#define TC_TMEM_COLS 64u
+#define TC_WAIT_LIMIT (1u << 24)    /* mbarrier polls before a wait gives up */
+
+/* Byte offset of element (r, k) of an R x 64 K-major operand without
+ * swizzle (the weights). */
+__device__ __forceinline__ uint32_t core_off(uint32_t r, uint32_t k)
+{
+	return (r >> 3) * TC_SBO + (k >> 3) * TC_LBO + (r & 7u) * 16u + (k & 7u) * 2u;
+}
+
+/* Byte offset of the 16-byte chunk c of row r of a 128-byte-swizzled tile
+ * (the activations). */
+__device__ __forceinline__ uint32_t sw128_off(uint32_t r, uint32_t c)
+{
+	return r * 128u + ((c ^ (r & 7u)) << 4);
+}
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p)
+{
+	return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+/* Shared-memory matrix descriptor: start address, leading and stride byte
+ * offsets (all in 16-byte units), descriptor version 1, layout type (0: no
+ * swizzle; 2: 128-byte swizzle, whose leading offset is unused). */
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo, uint32_t layout)
+{
+	uint64_t d = (uint64_t)((addr >> 4) & 0x3FFFu);
+	d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+	d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+	d |= (uint64_t)1u << 46;
+	d |= (uint64_t)layout << 61;
+	return d;
+}
+
+/* Arm a TMA barrier with the bytes of one tile and start the tile's load:
+ * rows [row0, row0 + 128) of the [n][64] input, all 64 columns (x = 0). */
+__device__ __forceinline__ void tma_tile(const CUtensorMap *map, uint32_t dst, uint32_t bar, int row0)
+{
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(bar), "r"(TC_X_BYTES) : "memory");
+	asm volatile(
+		"cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+		:: "r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(row0), "r"(bar) : "memory");
+}
+
+/* Instruction descriptor of kind::f16: FP32 accumulator, A and B both BF16
+ * (or both FP16), both K-major, N and M. */
+__device__ __forceinline__ uint32_t instr_desc(bool bf16, uint32_t n, uint32_t m)
+{
+	uint32_t f = bf16 ? 1u : 0u;
+	return (1u << 4) | (f << 7) | (f << 10) | ((n >> 3) << 17) | ((m >> 4) << 24);
+}
+
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+	asm volatile(
+		"{\n\t.reg .pred p;\n\t"
+		"setp.ne.b32 p, %4, 0;\n\t"
+		"tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t"
+		"}"
+		:: "r"(tmem), "l"(a), "l"(b), "r"(idesc), "r"(acc) : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t bar)
+{
+	asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(bar)
+		: "memory");
+}
+
+/* Poll the mbarrier for the completion of `parity`, at most TC_WAIT_LIMIT
+ * times.  Returns false when it gave up. */
+__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity)
+{
+	for (uint32_t i = 0; i < TC_WAIT_LIMIT; i++) {
+		uint32_t done;
+		asm volatile(
+			"{\n\t.reg .pred p;\n\t"
+			"mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+			"selp.u32 %0, 1, 0, p;\n\t"
+			"}"
+			: "=r"(done) : "r"(bar), "r"(parity) : "memory");
+		if (done)
+			return true;
+	}
+	return false;
+}
+
+#define TC_R8(i) "=r"(v[i]), "=r"(v[i + 1]), "=r"(v[i + 2]), "=r"(v[i + 3]), "=r"(v[i + 4]), "=r"(v[i + 5]), \
+	"=r"(v[i + 6]), "=r"(v[i + 7])
+
+/* 64 consecutive FP32 columns of this thread's TMEM lane. */
+__device__ __forceinline__ void tmem_ld64(uint32_t taddr, uint32_t (&v)[64])
+{
+	asm volatile("tcgen05.ld.sync.aligned.32x32b.x64.b32 "
+		"{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+		"%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, "
+		"%32, %33, %34, %35, %36, %37, %38, %39, %40, %41, %42, %43, %44, %45, %46, %47, "
+		"%48, %49, %50, %51, %52, %53, %54, %55, %56, %57, %58, %59, %60, %61, %62, %63}, [%64];"
+		: TC_R8(0), TC_R8(8), TC_R8(16), TC_R8(24), TC_R8(32), TC_R8(40), TC_R8(48), TC_R8(56)
+		: "r"(taddr) : "memory");
+}
+
+/* 16 consecutive FP32 columns of this thread's TMEM lane. */
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16])
+{
+	asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+		"{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+		: TC_R8(0), TC_R8(8) : "r"(taddr) : "memory");
+}
+
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+template <class T>
+__device__ __forceinline__ uint32_t pack_relu(uint32_t lo, uint32_t hi);
+
+template <>
+__device__ __forceinline__ uint32_t pack_relu<__nv_bfloat16>(uint32_t lo, uint32_t hi)
+{
+	__nv_bfloat162 h = __floats2bfloat162_rn(fmaxf(__uint_as_float(lo), 0.0f), fmaxf(__uint_as_float(hi), 0.0f));
+	return *reinterpret_cast<uint32_t *>(&h);
+}
+
+template <>
+__device__ __forceinline__ uint32_t pack_relu<__half>(uint32_t lo, uint32_t hi)
+{
+	__half2 h = __floats2half2_rn(fmaxf(__uint_as_float(lo), 0.0f), fmaxf(__uint_as_float(hi), 0.0f));
+	return *reinterpret_cast<uint32_t *>(&h);
+}
+
+template <class T>
+__global__ void __launch_bounds__(128) mlp_infer_tc_kernel(const T *__restrict__ wt_g,
+		const __grid_constant__ CUtensorMap xmap, uint32_t n, float4 *__restrict__ out,
+		const uint32_t *__restrict__ n_dev, uint32_t *__restrict__ err)
+{
+	if (n_dev) {
+		uint32_t c = *n_dev;
+		n = c < n ? c : n;
+	}
+	extern __shared__ __align__(1024) unsigned char sm[];
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	/* the 128-byte swizzle repeats every 1024 bytes; the kernel has no static
+	 * shared memory, so its dynamic block starts on such a boundary.  If it
+	 * did not, report it (bit 1) and do nothing. */
+	if (smem_addr(sm) & 1023u) {
+		if (tid == 0)
+			atomicOr(err, 2u);
+		return;
+	}
+	const bool bf16 = std::is_same<T, __nv_bfloat16>::value;
+	const uint32_t bar = smem_addr(sm + TC_BAR_OFF);
+	const uint32_t tbar[2] = {bar + 8u, bar + 16u};
+	uint32_t *slot = reinterpret_cast<uint32_t *>(sm + TC_SLOT_OFF);
+	const uint32_t tiles = (n + TC_ROWS - 1) / TC_ROWS;
+
+	/* weights: global [l][rows][64] row-major -> canonical layout */
+	for (int l = 0; l < TC_LAYERS; l++) {
+		int rows = l == TC_LAYERS - 1 ? TC_OUT : TC_W;
+		const uint4 *src = reinterpret_cast<const uint4 *>(wt_g + (size_t)l * TC_W * TC_W);
+		unsigned char *dst = sm + l * TC_LAYER_BYTES;
+		for (int c = tid; c < rows * 8; c += 128) {
+			uint32_t r = (uint32_t)c >> 3, kb = (uint32_t)c & 7u;
+			*reinterpret_cast<uint4 *>(dst + core_off(r, kb * 8u)) = __ldg(src + c);
+		}
+	}
+	if (tid == 0) {
+		for (int i = 0; i < 3; i++)
+			asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(bar + 8u * i), "r"(1u) : "memory");
+		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+	}
+	if (warp == 0) {
+		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+			:: "r"(smem_addr(slot)), "r"(TC_TMEM_COLS) : "memory");
+		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+	}
+	fence_async_smem();
+	tc_before();
+	__syncthreads();
+	tc_after();
+	const uint32_t tmem = *slot;
+	const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+	const uint32_t wbase = smem_addr(sm), xbase0 = smem_addr(sm + TC_X_OFF);
+	const uint32_t id_hidden = instr_desc(bf16, TC_W, TC_ROWS), id_out = instr_desc(bf16, TC_OUT, TC_ROWS);
+	uint32_t parity = 0;
+	bool ok = true;
+	/* the TMA load issued but not yet waited for: its barrier and parity */
+	bool pending = false;
+	uint32_t pend_bar = 0, pend_parity = 0;
+
+	uint32_t t = blockIdx.x;
+	if (tid == 0 && t < tiles)
+		tma_tile(&xmap, xbase0, tbar[0], (int)(t * TC_ROWS));
+	for (uint32_t i = 0; ok && t < tiles; i++, t += gridDim.x) {
+		const uint32_t buf = i & 1u;
+		const uint32_t xbase = xbase0 + buf * TC_X_BYTES;
+		unsigned char *xs = sm + TC_X_OFF + buf * TC_X_BYTES;
+		/* start the next tile's load into the other buffer, whose last tile
+		 * is finished (and fenced) */
+		uint32_t tn = t + gridDim.x;
+		if (tid == 0 && tn < tiles)
+			tma_tile(&xmap, xbase0 + (buf ^ 1u) * TC_X_BYTES, tbar[buf ^ 1u], (int)(tn * TC_ROWS));
+		pending = tn < tiles;
+		pend_bar = tbar[buf ^ 1u];
+		pend_parity = ((i + 1u) >> 1) & 1u;
+		bool got = bar_wait(tbar[buf], (i >> 1) & 1u);
+		ok = __syncthreads_and(got) != 0;
+		if (!ok)
+			break;
+		const uint64_t lo_sw = 2u; /* layout type: 128-byte swizzle */
+		for (int l = 0; l < TC_LAYERS; l++) {
+			const bool last = l == TC_LAYERS - 1;
+			if (tid == 0) {
+				for (uint32_t kc = 0; kc < 4; kc++)
+					tc_mma(tmem, smem_desc(xbase + kc * 32u, 16u, 1024u, (uint32_t)lo_sw),
+						smem_desc(wbase + l * TC_LAYER_BYTES + kc * 256u, TC_LBO, TC_SBO, 0u),
+						last ? id_out : id_hidden, kc > 0 ? 1u : 0u);
+				tc_commit(bar);
+			}
+			got = bar_wait(bar, parity);
+			parity ^= 1u;
+			ok = __syncthreads_and(got) != 0;
+			tc_after();
+			if (!ok)
+				break;
+			uint32_t r = (uint32_t)(warp * 32 + lane);
+			if (!last) {
+				uint32_t v[64];
+				tmem_ld64(lane_addr, v);
+				tmem_wait_ld();
+#pragma unroll
+				for (uint32_t kb = 0; kb < 8; kb++) {
+					uint4 p;
+					p.x = pack_relu<T>(v[8 * kb + 0], v[8 * kb + 1]);
+					p.y = pack_relu<T>(v[8 * kb + 2], v[8 * kb + 3]);
+					p.z = pack_relu<T>(v[8 * kb + 4], v[8 * kb + 5]);
+					p.w = pack_relu<T>(v[8 * kb + 6], v[8 * kb + 7]);
+					*reinterpret_cast<uint4 *>(xs + sw128_off(r, kb)) = p;
+				}
+				fence_async_smem();
+			} else {
+				uint32_t v[16];
+				tmem_ld16(lane_addr, v);
+				tmem_wait_ld();
+				size_t row = (size_t)t * TC_ROWS + r;
+				if (row < n)
+					out[row] = make_float4(__uint_as_float(v[0]), __uint_as_float(v[1]), __uint_as_float(v[2]), 0.0f);
+			}
+			tc_before();
+			__syncthreads();
+			tc_after();
+		}
+	}
+	if (!ok) {
+		if (tid == 0)
+			atomicOr(err, 1u);
+		/* the next tile's load may still be in flight: give it its
+		 * (bounded) time before the block exits */
+		if (pending)
+			bar_wait(pend_bar, pend_parity);
+	}
+	tc_before();
+	__syncthreads();
+	tc_after();
+	if (warp == 0)
+		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(TC_TMEM_COLS)
+			: "memory");
+}
+
+template <class K>
+void set_tc_smem(K kernel)
+{
+	KGR_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM));
+}
+
+/* cuTensorMapEncodeTiled, looked up once through the runtime (no link
+ * against the driver library). */
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+		const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+		CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled()
+{
+	static EncodeTiledFn fn = nullptr;
+	static std::once_flag once;
+	std::call_once(once, [] {
+		void *p = nullptr;
+		cudaDriverEntryPointQueryResult q;
+		if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+				cudaSuccess && q == cudaDriverEntryPointSuccess)
+			fn = reinterpret_cast<EncodeTiledFn>(p);
+		cudaGetLastError();
+	});
+	KGR_REQUIRE(fn, KGR_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+	return fn;
+}
+
+} /* namespace */
+
+void mlp_infer_tc(const MlpParams &mp, const void *x, uint32_t n, float4 *out, uint32_t *err, cudaStream_t st,
+		const uint32_t *n_dev)
+{
+	if (n == 0)
+		return;
+	KGR_REQUIRE(((uintptr_t)x & 15u) == 0, KGR_ERR_INVALID_ARGUMENT, "inputs must be 16-byte aligned");
+	/* the input as a 2-D tensor: 64 elements (128 bytes) per row, n rows;
+	 * one box is a 128 x 64 tile, swizzled by 128 bytes on its way in */
+	CUtensorMap map;
+	cuuint64_t dims[2] = {TC_W, n};
+	cuuint64_t strides[1] = {TC_W * 2};
+	cuuint32_t box[2] = {TC_W, TC_ROWS};
+	cuuint32_t estr[2] = {1, 1};
+	CUresult r = encode_tiled()(&map,
+		mp.dtype == KGR_MLP_BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2,
+		const_cast<void *>(x), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+		CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+	KGR_REQUIRE(r == CUDA_SUCCESS, KGR_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+	/* three CTAs fit an SM (75.8 KB of shared memory, 64 TMEM columns each) */
+	long long tiles = ((long long)n + TC_ROWS - 1) / TC_ROWS;
+	long long cap = (long long)device_sm_count() * 3;
+	int grid = (int)(tiles < cap ? tiles : cap);
+	if (mp.dtype == KGR_MLP_BF16) {
+		static bool once = (set_tc_smem(mlp_infer_tc_kernel<__nv_bfloat16>), true);
+		(void)once;
+		mlp_infer_tc_kernel<__nv_bfloat16><<<grid, 128, TC_SMEM, st>>>(
+			static_cast<const __nv_bfloat16 *>(mp.wt), map, n, out, n_dev, err);
+	} else {
+		static bool once = (set_tc_smem(mlp_infer_tc_kernel<__half>), true);
+		(void)once;
+		mlp_infer_tc_kernel<__half><<<grid, 128, TC_SMEM, st>>>(static_cast<const __half *>(mp.wt), map, n, out,
+			n_dev, err);
+	}
+	KGR_CUDA(cudaGetLastError());
+}
+
+} /* namespace kgr */

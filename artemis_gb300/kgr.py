@@ -152,6 +152,8 @@ def lib():
             "kgr_mlp_gradients": (c_i32, [vp, vp, vp, c_u32, vp, vp]),
             "kgr_mlp_train_step": (c_i32, [vp, vp, vp, c_u32, c_f, vp]),
             "kgr_mlp_destroy": (c_i32, [vp]),
+            "kgr_mlp_set_inference": (c_i32, [vp, c_i32]),
+            "kgr_mlp_check": (c_i32, [vp]),
             "kgr_get_visit_counts": (c_i32, [vp, vp]),
             "kgr_measure_read_bandwidth": (c_i32, [c_i32, c_u64, c_i32, vp]),
             "kgr_load_attachment": (PluginRet, [ctypes.c_char_p]),
@@ -373,6 +375,14 @@ class Mlp:
 
     def train_step(self, x_ptr, t_ptr, n, lr=1e-3, stream=None):
         check(lib().kgr_mlp_train_step(self.handle, x_ptr, t_ptr, n, lr, stream))
+
+    def set_inference(self, kernel):
+        """"mma" (warp-level mma.sync) or "tcgen05" (tensor memory accumulators)."""
+        check(lib().kgr_mlp_set_inference(self.handle, {"mma": 0, "tcgen05": 1}[kernel]))
+
+    def check(self):
+        """Raise if a tcgen05 inference gave up on an mbarrier wait."""
+        check(lib().kgr_mlp_check(self.handle))
 
     def close(self):
         if self.handle:

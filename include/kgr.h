@@ -423,6 +423,18 @@ kgr_status kgr_mlp_train_step(kgr_mlp *mlp, const void *x, const float *targets,
 		float lr, void *stream);
 kgr_status kgr_mlp_destroy(kgr_mlp *mlp);
 
+/* Inference kernel of kgr_mlp_forward and of the radiance cache:
+ * KGR_MLP_INFER_TCGEN05 (the default: tcgen05.mma with the accumulator in
+ * tensor memory, operands staged in shared memory) or KGR_MLP_INFER_MMA
+ * (warp-level mma.sync, activations kept in registers).  Same network, same rounding points;
+ * the results differ only in FP32 summation order.  No counterpart in the
+ * reference, whose only network is an unused FP32 forward pass. */
+enum { KGR_MLP_INFER_MMA = 0, KGR_MLP_INFER_TCGEN05 = 1 };
+kgr_status kgr_mlp_set_inference(kgr_mlp *mlp, int32_t kernel);
+/* Synchronise the device and report a tcgen05 inference whose mbarrier wait
+ * ran out (KGR_ERR_CUDA; the flag is then cleared).  KGR_OK otherwise. */
+kgr_status kgr_mlp_check(kgr_mlp *mlp);
+
 /* ------------------------------------------------------ procedural scenes -- */
 
 /* Seeded procedural scenes used by the tests and the benchmark.  The

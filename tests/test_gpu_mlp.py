@@ -22,6 +22,7 @@ def half_tensor(x, dtype):
 @pytest.mark.parametrize("dtype,tol", [("bf16", 2e-2), ("fp16", 2e-3)])
 def test_forward_matches_oracle(dtype, tol):
     net = kgr.Mlp(dtype, seed=3)
+    net.set_inference("mma")
     W = net.weights()
     rng = np.random.default_rng(0)
     n = 5000  # not a multiple of the 128-row tile

@@ -1,0 +1,68 @@
+"""Radiance-cache network inference on the fifth-generation tensor cores
+(tcgen05.mma, accumulators in tensor memory) against the NumPy oracle with
+the same half-precision rounding points, and against the mma.sync kernel of
+the same network.  Tolerances as for the mma.sync forward: 2e-2 (BF16) and
+2e-3 (FP16) of the output scale; the two kernels differ only in the order of
+FP32 summation, which can move a half-precision rounding of an activation by
+one step."""
+import numpy as np
+import pytest
+
+from artemis_gb300 import kgr
+from oracle import mlp_ref
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def half_tensor(x, dtype):
+    return torch.from_numpy(mlp_ref.to_bits(x, dtype).view(np.int16)).cuda()
+
+
+@pytest.mark.parametrize("dtype,tol", [("bf16", 2e-2), ("fp16", 2e-3)])
+def test_tcgen05_forward_matches_oracle_and_mma(dtype, tol):
+    net = kgr.Mlp(dtype, seed=3)
+    W = net.weights()
+    rng = np.random.default_rng(0)
+    for n in (5000, 3 * 128, 77):  # ragged, whole tiles, less than one tile
+        x = mlp_ref.encode_inputs(rng, n, dtype)
+        xd = half_tensor(x, dtype)
+        outs = {}
+        for kernel in ("mma", "tcgen05", "tcgen05"):  # the second tcgen05 call reuses freed TMEM
+            net.set_inference(kernel)
+            out = torch.full((n, 4), -7.0, dtype=torch.float32, device="cuda")
+            net.forward(xd.data_ptr(), n, out.data_ptr())
+            net.check()
+            outs.setdefault(kernel, []).append(out.cpu().numpy())
+        ref, _ = mlp_ref.forward(W, x, dtype)
+        scale = np.abs(ref).max()
+        for y in outs["tcgen05"]:
+            assert np.all(y[:, 3] == 0)
+            assert np.abs(y[:, :3] - ref).max() <= tol * scale + 1e-6, n
+            assert np.abs(y[:, :3] - outs["mma"][0][:, :3]).max() <= tol * scale + 1e-6, n
+        np.testing.assert_array_equal(outs["tcgen05"][0], outs["tcgen05"][1])
+
+
+def test_tcgen05_inference_speed_beside_mma():
+    """Both kernels over 2M rows of the radiance cache's query size (printed;
+    the assertion only checks that both ran)."""
+    net = kgr.Mlp("bf16", seed=1)
+    n = 1920 * 1080
+    x = torch.randint(-2000, 2000, (n, 64), dtype=torch.int16, device="cuda")  # finite BF16 bit patterns
+    out = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    times = {}
+    for kernel in ("mma", "tcgen05"):
+        net.set_inference(kernel)
+        for _ in range(3):
+            net.forward(x.data_ptr(), n, out.data_ptr())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(10):
+            net.forward(x.data_ptr(), n, out.data_ptr())
+        e1.record()
+        e1.synchronize()
+        net.check()
+        times[kernel] = e0.elapsed_time(e1) / 10
+    flops = 2.0 * (5 * 64 * 64 + 64 * 16) * n
+    print({k: f"{v:.3f} ms, {flops / v / 1e9:.1f} TFLOP/s" for k, v in times.items()})
+    assert all(v > 0 for v in times.values())

@@ -221,11 +221,19 @@ void build_kobra(const std::vector<PrimBox> &boxes, Tree &tree)
 
 /* ========================================================= SAH builder == */
 
-void build_sah(const std::vector<PrimBox> &boxes, int max_leaf, Tree &tree)
+void build_sah(const std::vector<PrimBox> &boxes_in, int max_leaf, Tree &tree)
 {
 	const int BINS = 32;
 	tree.nodes.clear();
-	size_t n = boxes.size();
+	size_t n = boxes_in.size();
+	/* canonical zeros (-0 -> +0): every min and max below is then a
+	 * function of the set of values, not of their order */
+	std::vector<PrimBox> boxes(boxes_in);
+	for (PrimBox &b : boxes)
+		for (int k = 0; k < 3; k++) {
+			b.bmin[k] += 0.0f;
+			b.bmax[k] += 0.0f;
+		}
 	tree.prim_order.resize(n);
 	if (n == 0)
 		return;
@@ -345,7 +353,10 @@ void build_sah(const std::vector<PrimBox> &boxes, int max_leaf, Tree &tree)
 			float scale = BINS / (cmx[best_axis] - cmn[best_axis]);
 			float c0 = cmn[best_axis];
 			const float *cp = cen.data();
-			uint32_t *m = std::partition(order + t.begin, order + t.end, [&](uint32_t p) {
+			/* stable: each side keeps the parent's order, so the tree is a
+			 * function of the primitive sets alone (the GPU builder in
+			 * bvh_gpu.cu reproduces it) */
+			uint32_t *m = std::stable_partition(order + t.begin, order + t.end, [&](uint32_t p) {
 				int b = (int)((cp[3 * p + best_axis] - c0) * scale);
 				b = b < 0 ? 0 : (b >= BINS ? BINS - 1 : b);
 				return b < best_split;

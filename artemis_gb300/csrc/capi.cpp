@@ -334,7 +334,8 @@ kgr_status kgr_scene_create(const kgr_mesh *meshes, uint32_t mesh_count, const k
 			opt = *options;
 		int max_leaf = opt.max_leaf_size ? opt.max_leaf_size : 4;
 		KGR_REQUIRE(max_leaf >= 1 && max_leaf <= 8, KGR_ERR_INVALID_ARGUMENT, "max_leaf_size must be 1..8");
-		KGR_REQUIRE(opt.builder == KGR_BUILDER_SAH || opt.builder == KGR_BUILDER_KOBRA,
+		KGR_REQUIRE(opt.builder == KGR_BUILDER_SAH || opt.builder == KGR_BUILDER_KOBRA ||
+				opt.builder == KGR_BUILDER_SAH_HOST,
 			KGR_ERR_INVALID_ARGUMENT, "unknown builder");
 		int device = resolve_device(opt.device);
 		DeviceGuard guard(device);
@@ -346,8 +347,10 @@ kgr_status kgr_scene_create(const kgr_mesh *meshes, uint32_t mesh_count, const k
 		Tree tree;
 		if (opt.builder == KGR_BUILDER_KOBRA)
 			build_kobra(boxes, tree);
-		else
+		else if (opt.builder == KGR_BUILDER_SAH_HOST)
 			build_sah(boxes, max_leaf, tree);
+		else
+			build_sah_gpu(boxes, max_leaf, tree, 0);
 		serialize_threaded(tree, boxes, sc->bvh);
 		sc->build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 		finish_scene(sc.get(), tree, boxes);

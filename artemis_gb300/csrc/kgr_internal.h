@@ -153,6 +153,9 @@ struct PrimBox {
 };
 
 void build_sah(const std::vector<PrimBox> &boxes, int max_leaf, Tree &tree);
+/* The same tree built on the GPU (bvh_gpu.cu): same splits, same leaves,
+ * same primitive order; node numbering differs. */
+void build_sah_gpu(const std::vector<PrimBox> &boxes, int max_leaf, Tree &tree, cudaStream_t st);
 void build_kobra(const std::vector<PrimBox> &boxes, Tree &tree);
 /* Threaded bvh.cpp layout, leaves as chains of one-primitive records. */
 void serialize_threaded(const Tree &tree, const std::vector<PrimBox> &boxes,

@@ -18,7 +18,7 @@ c_u32, c_i32, c_u64, c_f = ctypes.c_uint32, ctypes.c_int32, ctypes.c_uint64, cty
 vp = ctypes.c_void_p
 
 LAYOUT_FAST, LAYOUT_THREADED, LAYOUT_WIDE = 0, 1, 2
-BUILDER_SAH, BUILDER_KOBRA = 0, 1
+BUILDER_SAH, BUILDER_KOBRA, BUILDER_SAH_HOST = 0, 1, 2
 VALUE_NONE, VALUE_INT, VALUE_FLOAT, VALUE_BOOL, VALUE_STRING = range(5)
 
 

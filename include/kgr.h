@@ -110,11 +110,14 @@ typedef struct kgr_mesh {
 /* BVH builders. */
 enum {
 	/* binned SAH (32 bins) with leaves of at most max_leaf_size triangles,
-	 * written as chains of one-triangle leaf records in the bvh.cpp layout */
+	 * written as chains of one-triangle leaf records in the bvh.cpp layout;
+	 * kgr_scene_create runs it on the GPU */
 	KGR_BUILDER_SAH = 0,
 	/* the reference builder: partition() of source/bvh.cpp:102-210 (SAH over
 	 * 10 bins of the largest primitive's extent, one triangle per leaf) */
-	KGR_BUILDER_KOBRA = 1
+	KGR_BUILDER_KOBRA = 1,
+	/* KGR_BUILDER_SAH on the host: the same tree, bit for bit */
+	KGR_BUILDER_SAH_HOST = 2
 };
 
 typedef struct kgr_scene_options {

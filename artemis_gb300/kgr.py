@@ -153,6 +153,12 @@ def lib():
             "kgr_mlp_train_step": (c_i32, [vp, vp, vp, c_u32, c_f, vp]),
             "kgr_mlp_destroy": (c_i32, [vp]),
             "kgr_mlp_set_inference": (c_i32, [vp, c_i32]),
+            "kgr_tonemap": (c_i32, [vp, vp, c_u32, c_u32, c_i32, vp]),
+            "kgr_denoiser_create": (c_i32, [c_u32, c_u32, c_i32, c_i32, vp]),
+            "kgr_denoise": (c_i32, [vp, vp, vp, vp]),
+            "kgr_denoiser_result": (c_i32, [vp, vp]),
+            "kgr_denoiser_destroy": (c_i32, [vp]),
+            "kgr_denoiser_copy_result": (c_i32, [vp, vp, c_u64]),
             "kgr_mlp_check": (c_i32, [vp]),
             "kgr_get_visit_counts": (c_i32, [vp, vp]),
             "kgr_measure_read_bandwidth": (c_i32, [c_i32, c_u64, c_i32, vp]),
@@ -345,6 +351,61 @@ def camera_dict(info):
     c = info.camera
     return {"center": list(c.center), "ax_u": list(c.ax_u), "ax_v": list(c.ax_v), "ax_w": list(c.ax_w),
             "projection": list(c.projection), "view": list(c.view)}
+
+
+TONEMAP_ACES, TONEMAP_SRGB = 0, 1
+DENOISE_NONE, DENOISE_NORMAL, DENOISE_ALBEDO, DENOISE_POSITION = 0, 1, 2, 4
+
+
+def tonemap(hdr_ptr, ldr_ptr, width, height, mode=TONEMAP_ACES, stream=None):
+    """kgr_tonemap: float4 HDR (device) -> packed RGBA8 (device), rows bottom to top."""
+    check(lib().kgr_tonemap(hdr_ptr, ldr_ptr, width, height, mode, stream))
+
+
+class DenoiseParams(ctypes.Structure):
+    _fields_ = [("iterations", c_i32), ("sigma_color", c_f), ("normal_power", c_f), ("sigma_position", c_f),
+                ("reserved", c_i32 * 4)]
+
+
+class DenoiseInput(ctypes.Structure):
+    _fields_ = [("color", vp), ("normal", vp), ("albedo", vp), ("position", vp)]
+
+
+class Denoiser:
+    """kgr_denoiser: the a-trous denoiser over the AOV buffers (device pointers)."""
+
+    def __init__(self, width, height, guides=DENOISE_NORMAL | DENOISE_ALBEDO | DENOISE_POSITION, device=-1):
+        h = vp()
+        check(lib().kgr_denoiser_create(width, height, guides, device, ctypes.byref(h)))
+        self.handle = h
+
+    def denoise(self, color, normal, albedo=None, position=None, iterations=5, sigma_color=1.0, normal_power=64.0,
+                sigma_position=0.2, stream=None):
+        inp = DenoiseInput(color, normal, albedo, position)
+        p = DenoiseParams(iterations, sigma_color, normal_power, sigma_position)
+        check(lib().kgr_denoise(self.handle, ctypes.byref(inp), ctypes.byref(p), stream))
+
+    def result(self):
+        """Device pointer of the result (float4 per pixel)."""
+        r = vp()
+        check(lib().kgr_denoiser_result(self.handle, ctypes.byref(r)))
+        return r.value
+
+    def copy_result(self, out):
+        """Copy the result into a float32 host array of W x H x 4 values."""
+        check(lib().kgr_denoiser_copy_result(self.handle, _ptr(out), out.nbytes))
+        return out
+
+    def close(self):
+        if self.handle:
+            lib().kgr_denoiser_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Mlp:

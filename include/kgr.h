@@ -438,6 +438,58 @@ kgr_status kgr_mlp_set_inference(kgr_mlp *mlp, int32_t kernel);
  * ran out (KGR_ERR_CUDA; the flag is then cleared).  KGR_OK otherwise. */
 kgr_status kgr_mlp_check(kgr_mlp *mlp);
 
+/* ------------------------------------------------------ after the frame -- */
+
+/* HDR -> LDR: hdr_to_ldr (include/cuda/color.cuh:84-118).  hdr is the
+ * float4 colour buffer (W x H, row 0 at the top), ldr receives one packed
+ * pixel per entry, to_ui32 (include/cuda/cast.cuh:16-20) of make_color
+ * (color.cuh:57-66), rows written bottom to top as the reference kernel
+ * does.  Asynchronous on `stream`. */
+enum { KGR_TONEMAP_ACES = 0, KGR_TONEMAP_SRGB = 1 }; /* eTonemappingACES, eTonemappingSRGB (color.cuh:76-79) */
+kgr_status kgr_tonemap(const float *hdr, uint32_t *ldr, uint32_t width, uint32_t height, int32_t mode,
+		void *stream);
+
+/* Denoiser: replaces layers::Denoiser (include/layers/denoiser.cuh:14-55,
+ * source/layers/denoiser.cu:9-149), whose OptiX AI denoiser is a closed
+ * library, with this project's edge-avoiding a-trous filter (post.cu).  The
+ * guides are the reference's Guides bits plus a position guide. */
+enum {
+	KGR_DENOISE_NONE = 0,
+	KGR_DENOISE_NORMAL = 1,   /* eNormal */
+	KGR_DENOISE_ALBEDO = 2,   /* eAlbedo: filter colour / albedo, multiply back */
+	KGR_DENOISE_POSITION = 4  /* this project's: stop at depth and plane changes */
+};
+typedef struct kgr_denoise_params {
+	int32_t iterations;     /* a-trous passes, 1..8 (step 1, 2, 4, ...); default 5 */
+	float sigma_color;      /* relative luminance scale of the first pass, halved each pass; default 1 */
+	float normal_power;     /* exponent of the normal cosine; default 64 */
+	float sigma_position;   /* scale of the off-plane distance per unit separation; default 0.2 */
+	int32_t reserved[4];
+} kgr_denoise_params;
+/* Denoiser::Input (denoiser.cuh:40-45) plus a position buffer; device float4
+ * W x H each.  The normal buffer is always required (a zero normal marks a
+ * pixel without a hit; hits and misses are never averaged together); the
+ * albedo and position buffers are required when their guide is on. */
+typedef struct kgr_denoise_input {
+	const float *color;
+	const float *normal;
+	const float *albedo;
+	const float *position;
+} kgr_denoise_input;
+typedef struct kgr_denoiser kgr_denoiser;
+/* Denoiser::make (denoiser.cu:9-68): width x height, guides a KGR_DENOISE_*
+ * mask; allocates the result and a scratch image. */
+kgr_status kgr_denoiser_create(uint32_t width, uint32_t height, int32_t guides, int32_t device, kgr_denoiser **out);
+/* denoise (denoiser.cu:71-149): the result lands in the denoiser's own
+ * buffer (kgr_denoiser_result), as the reference's layer.result.  params
+ * NULL: the defaults.  Asynchronous on `stream`. */
+kgr_status kgr_denoise(kgr_denoiser *d, const kgr_denoise_input *input, const kgr_denoise_params *params,
+		void *stream);
+kgr_status kgr_denoiser_result(const kgr_denoiser *d, float **result);
+/* Copy the result to host memory (synchronous; bytes = W x H x 16). */
+kgr_status kgr_denoiser_copy_result(const kgr_denoiser *d, float *host, uint64_t bytes);
+kgr_status kgr_denoiser_destroy(kgr_denoiser *d);
+
 /* ------------------------------------------------------ procedural scenes -- */
 
 /* Seeded procedural scenes used by the tests and the benchmark.  The

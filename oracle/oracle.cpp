@@ -1957,3 +1957,51 @@ void oracle_kat_math(const float *x, int n, float *out)
 }
 
 } /* extern "C" */
+
+/* ========================================================== tonemapping == */
+
+namespace {
+
+/* clamp (include/cuda/math.cuh:101-104) */
+inline float clamp_ref(float f, float a, float b) { return fmaxf(a, fminf(f, b)); }
+
+/* aces (include/cuda/color.cuh:33-39), one channel */
+inline float aces1(float c)
+{
+	float a = c * (c * 2.51f + 0.03f);
+	float b = c * (c * 2.43f + 0.59f) + 0.14f;
+	return clamp_ref(a / b, 0.0f, 1.0f);
+}
+
+/* srgb (color.cuh:13-30), one channel */
+inline float srgb1(float c)
+{
+	float powed = powf(c, 1.0f / 2.4f);
+	float s = c < 0.0031308f ? 12.92f * c : 1.055f * powed - 0.055f;
+	return clamp_ref(s, 0.0f, 1.0f);
+}
+
+/* quantize_unsigned_8_bits (color.cuh:42-55) */
+inline uint32_t quantize8(float x)
+{
+	x = clamp_ref(x, 0.0f, 1.0f);
+	uint32_t q = (uint32_t)(x * 256.0f);
+	return q < 255u ? q : 255u;
+}
+
+} /* namespace */
+
+/* hdr_to_ldr_kernel (color.cuh:84-103): make_color + to_ui32 (cast.cuh:16-20)
+ * of every pixel, rows written bottom to top. */
+extern "C" void oracle_tonemap(const float *hdr, uint32_t *ldr, uint32_t width, uint32_t height, int mode)
+{
+	for (uint32_t y = 0; y < height; y++)
+		for (uint32_t x = 0; x < width; x++) {
+			const float *c = hdr + 4 * ((size_t)y * width + x);
+			float r = mode == 0 ? aces1(c[0]) : srgb1(c[0]);
+			float g = mode == 0 ? aces1(c[1]) : srgb1(c[1]);
+			float b = mode == 0 ? aces1(c[2]) : srgb1(c[2]);
+			ldr[(size_t)(height - y - 1) * width + x] =
+				(255u << 24) | (quantize8(b) << 16) | (quantize8(g) << 8) | quantize8(r);
+		}
+}

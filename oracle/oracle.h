@@ -154,6 +154,10 @@ void oracle_kat_brdf_eval(const kgr_material *m, const float *n, const float *wo
 void oracle_kat_brdf(const kgr_material *m, const float *n, const float *wo, const float *wi, float *f_pdf);
 void oracle_kat_math(const float *x, int n, float *sin_cos_tan_atan_acos);
 
+/* hdr_to_ldr of include/cuda/color.cuh:84-103: mode 0 ACES, 1 sRGB; ldr rows
+ * bottom to top, packed as to_ui32 (cast.cuh:16-20). */
+void oracle_tonemap(const float *hdr, uint32_t *ldr, uint32_t width, uint32_t height, int mode);
+
 #ifdef __cplusplus
 }
 #endif

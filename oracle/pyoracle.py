@@ -121,6 +121,7 @@ def lib():
         L.oracle_render_gi.argtypes = [ctypes.POINTER(OracleScene), ctypes.POINTER(RenderParams),
                                        ctypes.POINTER(GiStateC), vp, vp, ctypes.POINTER(RenderStats)]
         L.oracle_kat_rng.argtypes = [ctypes.c_float] * 3 + [ctypes.c_int, vp]
+        L.oracle_tonemap.argtypes = [vp, vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int]
         L.oracle_kat_intersect.restype = ctypes.c_float
         L.oracle_kat_intersect.argtypes = [vp] * 6
         L.oracle_kat_sample_light.argtypes = [vp] * 4
@@ -259,3 +260,12 @@ def render_restir(scene, params, state, bufs=None):
     lib().oracle_render_restir(ctypes.byref(scene.c), ctypes.byref(params), ctypes.byref(state.c),
                                *[ptr(b) for b in bufs], ctypes.byref(st))
     return bufs, st
+
+
+def tonemap(hdr, mode=0):
+    """hdr: float32 (H, W, 4) -> uint32 (H, W), rows bottom to top (color.cuh:84-103)."""
+    hdr = np.ascontiguousarray(hdr, np.float32)
+    h, w = hdr.shape[:2]
+    out = np.zeros((h, w), np.uint32)
+    lib().oracle_tonemap(ptr(hdr), ptr(out), w, h, mode)
+    return out

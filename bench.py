@@ -244,7 +244,9 @@ def relmse_compare(args, g, sc, W, H, stream, sptr):
     cached configuration is compared with the costliest plain configuration
     whose relMSE is still at or above its own, so the speed-up is at equal or
     lower error; the cache trains online (one Adam step per frame) for 300
-    frames first and keeps training while it is timed."""
+    frames first and keeps training while it is timed.  `denoised` gives the
+    relMSE of the same frames after the a-trous denoiser and the denoiser's
+    own time (a post-process beside the comparison, not part of it)."""
     import torch
 
     from artemis_gb300 import kgr
@@ -286,32 +288,56 @@ def relmse_compare(args, g, sc, W, H, stream, sptr):
         d = bufs[0][:, :3].double() - ref
         return (d * d / (ref * ref + 1e-2)).mean().item()
 
-    def measure(a, first, n=8, warm=3):
+    dn = kgr.Denoiser(W, H)
+    dout = torch.zeros((W * H, 4), dtype=torch.float32, device="cuda")
+
+    def relmse_of(x):
+        d = x[:, :3].double() - ref
+        return (d * d / (ref * ref + 1e-2)).mean().item()
+
+    def measure(a, first, n=8, warm=3, denoise=False):
         for f in range(warm):
             a.render(info(first + f), sc, sptr)
-        ms, err = [], []
+        ms, err, dms, derr = [], [], [], []
         for f in range(n):
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
             e0.record(stream)
             a.render(info(first + warm + f), sc, sptr)
             e1.record(stream)
-            e1.synchronize()
+            if denoise:
+                dn.denoise(ptrs[0], ptrs[1], ptrs[2], ptrs[3], stream=sptr)
+            e2.record(stream)
+            e2.synchronize()
             ms.append(e0.elapsed_time(e1))
             err.append(relmse())
-        return round(float(np.median(ms)), 3), round(float(np.mean(err)), 4)
+            if denoise:
+                dms.append(e1.elapsed_time(e2))
+                dn.copy_result(dhost)
+                derr.append(relmse_of(torch.from_numpy(dhost).cuda()))
+        r = (round(float(np.median(ms)), 3), round(float(np.mean(err)), 4))
+        if denoise:
+            r += (round(float(np.median(dms)), 3), round(float(np.mean(derr)), 4))
+        return r
 
-    plain = {}
+    dhost = np.zeros((W * H, 4), np.float32)
+    plain, plain_dn = {}, {}
     for spp in (1, 2, 4, 8, 16, 32):
         a = make(spp)
-        plain[spp] = measure(a, 1000 * spp)
+        r = measure(a, 1000 * spp, denoise=spp <= 4)
+        plain[spp] = r[:2]
+        if spp <= 4:
+            plain_dn[spp] = r[2:]
         a.close()
-    cached = {}
+    cached, cached_dn = {}, {}
     for spp in (1, 2, 4):
         a = make(spp, cache=True)
         for f in range(300):
             a.render(info(50000 + f), sc, sptr)
-        cached[spp] = measure(a, 60000)
+        r = measure(a, 60000, denoise=True)
+        cached[spp] = r[:2]
+        cached_dn[spp] = r[2:]
         a.close()
+    dn.close()
     compare = []
     for spp, (ms, err) in cached.items():
         worse = [k for k, (_, e) in plain.items() if e >= err]
@@ -325,7 +351,10 @@ def relmse_compare(args, g, sc, W, H, stream, sptr):
             "reference_s": round(ref_s, 1), "relmse": "mean (x - ref)^2 / (ref^2 + 0.01)",
             "plain": {str(k): {"ms": v[0], "relmse": v[1]} for k, v in plain.items()},
             "cached_bf16": {str(k): {"ms": v[0], "relmse": v[1]} for k, v in cached.items()},
-            "at_equal_or_lower_relmse": compare, "best_speedup": best and best["speedup"]}
+            "at_equal_or_lower_relmse": compare, "best_speedup": best and best["speedup"],
+            "denoised": {"denoiser": "a-trous, 5 passes, normal + albedo + position guides",
+                         "plain": {str(k): {"denoise_ms": v[0], "relmse": v[1]} for k, v in plain_dn.items()},
+                         "cached_bf16": {str(k): {"denoise_ms": v[0], "relmse": v[1]} for k, v in cached_dn.items()}}}
 
 
 def restir_runs(args):

@@ -400,7 +400,7 @@ void emit(std::vector<float> &out, float leaf, int32_t object, int32_t hit, int3
 }
 
 void serialize_node(const Tree &tree, const std::vector<PrimBox> &boxes, int32_t i, int32_t miss,
-		std::vector<uint32_t> &memo, std::vector<float> &out)
+		std::vector<uint32_t> &memo, std::vector<float> &out, std::vector<int32_t> *rec_node)
 {
 	const TreeNode &n = tree.nodes[i];
 	int32_t size = (int32_t)(out.size() / 4);
@@ -409,26 +409,33 @@ void serialize_node(const Tree &tree, const std::vector<PrimBox> &boxes, int32_t
 			uint32_t prim = tree.prim_order[n.first + k];
 			int32_t next = k + 1 < n.count ? size + 3 * (k + 1) : miss;
 			emit(out, 1.0f, (int32_t)prim, next, next, boxes[prim].bmin, boxes[prim].bmax);
+			if (rec_node)
+				rec_node->push_back(~(int32_t)prim);
 		}
 		return;
 	}
 	int32_t after = size + 3;
 	int32_t right_index = after + 3 * (int32_t)subtree_records(tree, n.left, memo);
 	emit(out, 0.0f, -1, after, miss, n.bmin, n.bmax);
-	serialize_node(tree, boxes, n.left, right_index, memo, out);
-	serialize_node(tree, boxes, n.right, miss, memo, out);
+	if (rec_node)
+		rec_node->push_back(i);
+	serialize_node(tree, boxes, n.left, right_index, memo, out, rec_node);
+	serialize_node(tree, boxes, n.right, miss, memo, out, rec_node);
 }
 
 } /* namespace */
 
-void serialize_threaded(const Tree &tree, const std::vector<PrimBox> &boxes, std::vector<float> &out)
+void serialize_threaded(const Tree &tree, const std::vector<PrimBox> &boxes, std::vector<float> &out,
+		std::vector<int32_t> *rec_node)
 {
 	out.clear();
+	if (rec_node)
+		rec_node->clear();
 	if (tree.nodes.empty())
 		return;
 	std::vector<uint32_t> memo(tree.nodes.size(), 0);
 	out.reserve((size_t)subtree_records(tree, 0, memo) * 12);
-	serialize_node(tree, boxes, 0, -1, memo, out);
+	serialize_node(tree, boxes, 0, -1, memo, out, rec_node);
 }
 
 /* Parse a threaded buffer: the children of an internal record are the
@@ -437,11 +444,13 @@ void serialize_threaded(const Tree &tree, const std::vector<PrimBox> &boxes, std
  * more than two children become a right-leaning chain of extra nodes, which
  * keeps the walk order of the primitives. */
 void parse_threaded(const float *vec4, uint32_t count, uint32_t prim_count,
-		const std::vector<PrimBox> &boxes, Tree &tree)
+		const std::vector<PrimBox> &boxes, Tree &tree, std::vector<int32_t> *rec_node)
 {
 	tree.nodes.clear();
 	tree.prim_order.clear();
 	KGR_REQUIRE(count % 3 == 0, KGR_ERR_BVH_FORMAT, "bvh buffer length is not a multiple of 3 vec4");
+	if (rec_node)
+		rec_node->assign(count / 3, KGR_REC_UNREACHED);
 	if (count == 0)
 		return;
 	uint32_t records = count / 3;
@@ -488,10 +497,17 @@ void parse_threaded(const float *vec4, uint32_t count, uint32_t prim_count,
 		return (int32_t)tree.nodes.size() - 1;
 	};
 
+	auto note = [&](int32_t idx, int32_t v) {
+		if (rec_node)
+			(*rec_node)[idx / 3] = v;
+	};
 	std::function<int32_t(int32_t)> parse = [&](int32_t idx) -> int32_t {
 		const float *h = rec(idx);
-		if (ibits(h[1]) != -1)
-			return add_leaf_prims({take_prim(h)});
+		if (ibits(h[1]) != -1) {
+			uint32_t p = take_prim(h);
+			note(idx, ~(int32_t)p);
+			return add_leaf_prims({p});
+		}
 		int32_t miss = ibits(h[3]);
 		std::vector<int32_t> kids;
 		std::vector<uint32_t> run;
@@ -506,6 +522,7 @@ void parse_threaded(const float *vec4, uint32_t count, uint32_t prim_count,
 			const float *ch = rec(c);
 			if (ibits(ch[1]) != -1) {
 				run.push_back(take_prim(ch));
+				note(c, ~(int32_t)run.back());
 				if (run.size() == 8)
 					flush();
 			} else {
@@ -524,6 +541,7 @@ void parse_threaded(const float *vec4, uint32_t count, uint32_t prim_count,
 			memcpy(tree.nodes[acc].bmin, h + 4, 12);
 			memcpy(tree.nodes[acc].bmax, h + 8, 12);
 		}
+		note(idx, acc);
 		return acc;
 	};
 	int32_t root = parse(0);
@@ -542,6 +560,13 @@ void parse_threaded(const float *vec4, uint32_t count, uint32_t prim_count,
 					*c = root;
 			}
 		}
+		if (rec_node)
+			for (int32_t &r : *rec_node) {
+				if (r == root)
+					r = 0;
+				else if (r == 0)
+					r = root;
+			}
 	}
 }
 
@@ -564,11 +589,14 @@ inline void pad_box(const float *mn, const float *mx, float *pmn, float *pmx)
 } /* namespace */
 
 void build_fast(const Tree &tree, const std::vector<PrimBox> &boxes, const float *positions,
-		const uint32_t *tris4, std::vector<FastNode> &nodes, std::vector<float4> &tri_records)
+		const uint32_t *tris4, std::vector<FastNode> &nodes, std::vector<float4> &tri_records,
+		std::vector<int2> *kids)
 {
 	(void)boxes;
 	nodes.clear();
 	tri_records.clear();
+	if (kids)
+		kids->clear();
 	if (tree.nodes.empty())
 		return;
 	tri_records.reserve(3 * tree.prim_order.size());
@@ -615,6 +643,8 @@ void build_fast(const Tree &tree, const std::vector<PrimBox> &boxes, const float
 		fn.lrz.w = -inf;
 		fn.refs.y = 0;
 		nodes.push_back(fn);
+		if (kids)
+			kids->push_back(make_int2(0, -1));
 		return;
 	}
 	/* depth-first, left child first: the same order serialize_threaded emits
@@ -624,6 +654,8 @@ void build_fast(const Tree &tree, const std::vector<PrimBox> &boxes, const float
 		nodes.push_back(FastNode());
 		memset(&nodes[me], 0, sizeof(FastNode));
 		const TreeNode &n = tree.nodes[i];
+		if (kids)
+			kids->push_back(make_int2(n.left, n.right));
 		for (int side = 0; side < 2; side++) {
 			const TreeNode &c = tree.nodes[side == 0 ? n.left : n.right];
 			int32_t ref = c.count ? leaf_ref(c) : emit_node(side == 0 ? n.left : n.right);
@@ -634,10 +666,12 @@ void build_fast(const Tree &tree, const std::vector<PrimBox> &boxes, const float
 	emit_node(0);
 }
 
-void build_wide(const Tree &tree, std::vector<WideNode> &nodes, uint32_t &max_stack)
+void build_wide(const Tree &tree, std::vector<WideNode> &nodes, uint32_t &max_stack, std::vector<int4> *kids_out)
 {
 	nodes.clear();
 	max_stack = 0;
+	if (kids_out)
+		kids_out->clear();
 	if (tree.nodes.empty() || tree.nodes[0].count)
 		return;
 	/* record index of every leaf: the fast layout emits leaves depth-first,
@@ -691,6 +725,11 @@ void build_wide(const Tree &tree, std::vector<WideNode> &nodes, uint32_t &max_st
 		}
 		int32_t me = (int32_t)nodes.size();
 		nodes.push_back(WideNode());
+		if (kids_out) {
+			kids_out->resize(nodes.size());
+			(*kids_out)[me] = make_int4(nk > 0 ? kids[0] : -1, nk > 1 ? kids[1] : -1, nk > 2 ? kids[2] : -1,
+				nk > 3 ? kids[3] : -1);
+		}
 		WideNode w;
 		float *lo[3] = {&w.lox.x, &w.loy.x, &w.loz.x}, *hi[3] = {&w.hix.x, &w.hiy.x, &w.hiz.x};
 		int32_t *refs = &w.refs.x;

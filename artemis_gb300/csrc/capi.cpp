@@ -148,11 +148,31 @@ void gather_meshes(kgr_scene *sc, const kgr_mesh *meshes, uint32_t mesh_count, c
 	sc->positions.resize(3 * vtotal);
 	sc->normals.resize(3 * vtotal);
 	sc->tris4.resize(4 * ttotal);
+	RefitPlan &pl = sc->plan;
+	pl.obj_positions.resize(3 * vtotal);
+	pl.obj_normals.assign(3 * vtotal, 0.0f);
+	pl.vertex_mesh.resize(vtotal);
+	pl.normal_src.assign(vtotal, KGR_NORMAL_ZERO);
+	pl.models.assign(16 * (size_t)mesh_count, 0.0f);
+	pl.has_model.assign(mesh_count, 0);
 	uint64_t vb = 0, tb = 0;
 	for (uint32_t m = 0; m < mesh_count; m++) {
 		const kgr_mesh &me = meshes[m];
 		KGR_REQUIRE(me.vertex_count == 0 || me.positions, KGR_ERR_INVALID_ARGUMENT, "mesh positions are NULL");
 		KGR_REQUIRE(me.triangle_count == 0 || me.indices, KGR_ERR_INVALID_ARGUMENT, "mesh indices are NULL");
+		if (me.model) {
+			memcpy(&pl.models[16 * (size_t)m], me.model, 64);
+			pl.has_model[m] = 1;
+		}
+		if (me.vertex_count)
+			memcpy(&pl.obj_positions[3 * vb], me.positions, 12 * (size_t)me.vertex_count);
+		if (me.vertex_count && me.normals)
+			memcpy(&pl.obj_normals[3 * vb], me.normals, 12 * (size_t)me.vertex_count);
+		for (uint32_t v = 0; v < me.vertex_count; v++) {
+			pl.vertex_mesh[vb + v] = m;
+			if (me.normals)
+				pl.normal_src[vb + v] = KGR_NORMAL_OWN;
+		}
 		for (uint32_t v = 0; v < me.vertex_count; v++) {
 			float *pp = &sc->positions[3 * (vb + v)];
 			float *nn = &sc->normals[3 * (vb + v)];
@@ -185,8 +205,10 @@ void gather_meshes(kgr_scene *sc, const kgr_mesh *meshes, uint32_t mesh_count, c
 				float e2[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
 				float n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
 					e1[0] * e2[1] - e1[1] * e2[0]};
-				for (int k = 0; k < 3; k++)
+				for (int k = 0; k < 3; k++) {
 					memcpy(&sc->normals[3 * o[k]], n, 12);
+					pl.normal_src[o[k]] = (int32_t)(tb + t);
+				}
 			}
 		}
 		vb += me.vertex_count;
@@ -194,6 +216,7 @@ void gather_meshes(kgr_scene *sc, const kgr_mesh *meshes, uint32_t mesh_count, c
 	}
 	/* triangle lights in triangle order (armada.cu:98-212) */
 	sc->lights.clear();
+	pl.light_tri.clear();
 	for (uint64_t t = 0; t < ttotal; t++) {
 		const uint32_t *o = &sc->tris4[4 * t];
 		const kgr_material &m = sc->materials[o[3]];
@@ -208,6 +231,7 @@ void gather_meshes(kgr_scene *sc, const kgr_mesh *meshes, uint32_t mesh_count, c
 			l.intensity[k] = m.emission[k];
 		}
 		sc->lights.push_back(l);
+		pl.light_tri.push_back((uint32_t)t);
 	}
 	for (int k = 0; k < 3; k++) {
 		sc->bounds_min[k] = INFINITY;
@@ -257,19 +281,56 @@ uint32_t tree_depth(const Tree &t)
 	return best;
 }
 
-void finish_scene(kgr_scene *sc, const Tree &tree, const std::vector<PrimBox> &boxes)
+/* The tree half of the refit plan: nodes, primitive order, nodes grouped by
+ * depth (deepest first, so a level's children are done before it). */
+void plan_tree(RefitPlan &pl, const Tree &tree, std::vector<int32_t> &&rec_node)
+{
+	size_t n = tree.nodes.size();
+	pl.nodes.resize(n);
+	for (size_t i = 0; i < n; i++) {
+		const TreeNode &t = tree.nodes[i];
+		pl.nodes[i] = t.count ? make_int4(-1, -1, t.first, t.count) : make_int4(t.left, t.right, 0, 0);
+	}
+	pl.prim_order = tree.prim_order;
+	pl.rec_node = std::move(rec_node);
+	std::vector<std::vector<uint32_t>> levels;
+	if (n) {
+		std::vector<uint32_t> cur(1, 0u), next;
+		while (!cur.empty()) {
+			levels.push_back(cur);
+			next.clear();
+			for (uint32_t i : cur)
+				if (!tree.nodes[i].count) {
+					next.push_back((uint32_t)tree.nodes[i].left);
+					next.push_back((uint32_t)tree.nodes[i].right);
+				}
+			cur.swap(next);
+		}
+	}
+	pl.level_order.clear();
+	pl.level_begin.assign(1, 0u);
+	for (size_t l = levels.size(); l-- > 0;) {
+		pl.level_order.insert(pl.level_order.end(), levels[l].begin(), levels[l].end());
+		pl.level_begin.push_back((uint32_t)pl.level_order.size());
+	}
+}
+
+void finish_scene(kgr_scene *sc, const Tree &tree, const std::vector<PrimBox> &boxes, std::vector<int32_t> &&rec_node)
 {
 	KGR_REQUIRE(tree_depth(tree) < KGR_STACK_DEPTH_HOST, KGR_ERR_UNSUPPORTED,
 		"BVH deeper than the traversal stack (" + std::to_string(tree_depth(tree)) + " levels)");
 	std::vector<FastNode> nodes;
 	std::vector<float4> tri_records;
-	build_fast(tree, boxes, sc->positions.data(), sc->tris4.data(), nodes, tri_records);
+	build_fast(tree, boxes, sc->positions.data(), sc->tris4.data(), nodes, tri_records, &sc->plan.fast_kids);
 	sc->fast_node_count = (uint32_t)nodes.size();
 	std::vector<WideNode> wide;
 	uint32_t wide_stack = 0;
-	build_wide(tree, wide, wide_stack);
-	if (wide_stack >= KGR_STACK_DEPTH_HOST)
+	build_wide(tree, wide, wide_stack, &sc->plan.wide_kids);
+	if (wide_stack >= KGR_STACK_DEPTH_HOST) {
 		wide.clear(); /* a walk could overflow the stack: fast layout only */
+		sc->plan.wide_kids.clear();
+	}
+	plan_tree(sc->plan, tree, std::move(rec_node));
 	sc->wide_node_count = (uint32_t)wide.size();
 	sc->wide_max_stack = wide.empty() ? 0 : wide_stack;
 	size_t nv = sc->positions.size() / 3, nt = sc->tris4.size() / 4;
@@ -351,9 +412,10 @@ kgr_status kgr_scene_create(const kgr_mesh *meshes, uint32_t mesh_count, const k
 			build_sah(boxes, max_leaf, tree);
 		else
 			build_sah_gpu(boxes, max_leaf, tree, 0);
-		serialize_threaded(tree, boxes, sc->bvh);
+		std::vector<int32_t> rec_node;
+		serialize_threaded(tree, boxes, sc->bvh, &rec_node);
 		sc->build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-		finish_scene(sc.get(), tree, boxes);
+		finish_scene(sc.get(), tree, boxes, std::move(rec_node));
 		*out = sc.release();
 	});
 }
@@ -374,10 +436,11 @@ kgr_status kgr_scene_create_from_bvh(const kgr_mesh *meshes, uint32_t mesh_count
 		auto t0 = std::chrono::steady_clock::now();
 		std::vector<PrimBox> boxes = prim_boxes(sc.get());
 		Tree tree;
-		parse_threaded(bvh_vec4, bvh_vec4_count, (uint32_t)boxes.size(), boxes, tree);
+		std::vector<int32_t> rec_node;
+		parse_threaded(bvh_vec4, bvh_vec4_count, (uint32_t)boxes.size(), boxes, tree, &rec_node);
 		sc->bvh.assign(bvh_vec4, bvh_vec4 + 4 * (size_t)bvh_vec4_count);
 		sc->build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-		finish_scene(sc.get(), tree, boxes);
+		finish_scene(sc.get(), tree, boxes, std::move(rec_node));
 		*out = sc.release();
 	});
 }
@@ -431,6 +494,8 @@ kgr_status kgr_scene_info_get(const kgr_scene *sc, kgr_scene_info *info)
 	});
 }
 
+/* The host copies of the threaded buffer and the lights hold the scene as
+ * created; after a refit the device holds the current ones. */
 kgr_status kgr_scene_copy_bvh(const kgr_scene *sc, float *out_vec4, uint32_t capacity, uint32_t *count)
 {
 	return guarded([&] {
@@ -439,7 +504,13 @@ kgr_status kgr_scene_copy_bvh(const kgr_scene *sc, float *out_vec4, uint32_t cap
 		*count = n;
 		if (out_vec4) {
 			KGR_REQUIRE(capacity >= n, KGR_ERR_INVALID_ARGUMENT, "capacity too small");
-			memcpy(out_vec4, sc->bvh.data(), sc->bvh.size() * sizeof(float));
+			if (sc->refits && n) {
+				DeviceGuard guard(sc->device);
+				KGR_CUDA(cudaDeviceSynchronize());
+				KGR_CUDA(cudaMemcpy(out_vec4, sc->d_bvh.ptr, (size_t)n * 16, cudaMemcpyDeviceToHost));
+			} else {
+				memcpy(out_vec4, sc->bvh.data(), sc->bvh.size() * sizeof(float));
+			}
 		}
 	});
 }
@@ -451,8 +522,92 @@ kgr_status kgr_scene_copy_lights(const kgr_scene *sc, kgr_triangle_light *out, u
 		*count = (uint32_t)sc->lights.size();
 		if (out) {
 			KGR_REQUIRE(capacity >= sc->lights.size(), KGR_ERR_INVALID_ARGUMENT, "capacity too small");
-			memcpy(out, sc->lights.data(), sc->lights.size() * sizeof(kgr_triangle_light));
+			if (sc->refits && !sc->lights.empty()) {
+				DeviceGuard guard(sc->device);
+				KGR_CUDA(cudaDeviceSynchronize());
+				KGR_CUDA(cudaMemcpy(out, sc->d_lights.ptr, sc->d_lights.bytes(), cudaMemcpyDeviceToHost));
+			} else {
+				memcpy(out, sc->lights.data(), sc->lights.size() * sizeof(kgr_triangle_light));
+			}
 		}
+	});
+}
+
+kgr_status kgr_scene_copy_vertices(const kgr_scene *sc, float *positions, float *normals)
+{
+	return guarded([&] {
+		KGR_REQUIRE(sc, KGR_ERR_INVALID_ARGUMENT, "NULL scene");
+		size_t nv = sc->positions.size() / 3;
+		if (!nv)
+			return;
+		DeviceGuard guard(sc->device);
+		KGR_CUDA(cudaDeviceSynchronize());
+		std::vector<float4> tmp(nv);
+		for (int pass = 0; pass < 2; pass++) {
+			float *out = pass == 0 ? positions : normals;
+			if (!out)
+				continue;
+			const float4 *src = pass == 0 ? sc->d_positions.ptr : sc->d_normals.ptr;
+			KGR_CUDA(cudaMemcpy(tmp.data(), src, nv * sizeof(float4), cudaMemcpyDeviceToHost));
+			for (size_t v = 0; v < nv; v++) {
+				out[3 * v] = tmp[v].x;
+				out[3 * v + 1] = tmp[v].y;
+				out[3 * v + 2] = tmp[v].z;
+			}
+		}
+	});
+}
+
+kgr_status kgr_scene_copy_array(const kgr_scene *sc, int32_t which, void *out, uint64_t capacity_bytes,
+		uint64_t *bytes)
+{
+	return guarded([&] {
+		KGR_REQUIRE(sc && bytes, KGR_ERR_INVALID_ARGUMENT, "NULL argument");
+		const void *src = nullptr;
+		size_t n = 0;
+		switch (which) {
+		case KGR_ARRAY_THREADED: src = sc->d_bvh.ptr; n = sc->d_bvh.bytes(); break;
+		case KGR_ARRAY_FAST_NODES: src = sc->d_fast_nodes.ptr; n = sc->d_fast_nodes.bytes(); break;
+		case KGR_ARRAY_WIDE_NODES: src = sc->d_wide_nodes.ptr; n = sc->d_wide_nodes.bytes(); break;
+		case KGR_ARRAY_TRIANGLE_RECORDS: src = sc->d_fast_tris.ptr; n = sc->d_fast_tris.bytes(); break;
+		default: throw Error(KGR_ERR_INVALID_ARGUMENT, "unknown scene array");
+		}
+		*bytes = n;
+		if (out && n) {
+			KGR_REQUIRE(capacity_bytes >= n, KGR_ERR_INVALID_ARGUMENT, "capacity too small");
+			DeviceGuard guard(sc->device);
+			KGR_CUDA(cudaDeviceSynchronize());
+			KGR_CUDA(cudaMemcpy(out, src, n, cudaMemcpyDeviceToHost));
+		}
+	});
+}
+
+kgr_status kgr_scene_set_transforms(kgr_scene *sc, const uint32_t *mesh_ids, const float *models, uint32_t count,
+		void *stream)
+{
+	return guarded([&] {
+		KGR_REQUIRE(sc, KGR_ERR_INVALID_ARGUMENT, "NULL scene");
+		KGR_REQUIRE(count == 0 || (mesh_ids && models), KGR_ERR_INVALID_ARGUMENT, "NULL argument");
+		RefitPlan &pl = sc->plan;
+		for (uint32_t i = 0; i < count; i++)
+			KGR_REQUIRE(mesh_ids[i] < pl.has_model.size(), KGR_ERR_INVALID_ARGUMENT,
+				"mesh index out of range: " + std::to_string(mesh_ids[i]));
+		for (uint32_t i = 0; i < count; i++) {
+			memcpy(&pl.models[16 * (size_t)mesh_ids[i]], models + 16 * (size_t)i, 64);
+			pl.has_model[mesh_ids[i]] = 1;
+		}
+		DeviceGuard guard(sc->device);
+		refit_scene(sc, REFIT_TRANSFORM, nullptr, nullptr, (cudaStream_t)stream);
+	});
+}
+
+kgr_status kgr_scene_refit(kgr_scene *sc, const float *positions, const float *normals, void *stream)
+{
+	return guarded([&] {
+		KGR_REQUIRE(sc, KGR_ERR_INVALID_ARGUMENT, "NULL scene");
+		KGR_REQUIRE(positions || sc->positions.empty(), KGR_ERR_INVALID_ARGUMENT, "positions is NULL");
+		DeviceGuard guard(sc->device);
+		refit_scene(sc, REFIT_POSITIONS, positions, normals, (cudaStream_t)stream);
 	});
 }
 

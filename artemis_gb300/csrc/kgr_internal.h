@@ -157,24 +157,29 @@ void build_sah(const std::vector<PrimBox> &boxes, int max_leaf, Tree &tree);
  * same primitive order; node numbering differs. */
 void build_sah_gpu(const std::vector<PrimBox> &boxes, int max_leaf, Tree &tree, cudaStream_t st);
 void build_kobra(const std::vector<PrimBox> &boxes, Tree &tree);
-/* Threaded bvh.cpp layout, leaves as chains of one-primitive records. */
+/* Threaded bvh.cpp layout, leaves as chains of one-primitive records.
+ * rec_node (optional) receives, per record, the tree node whose box the
+ * record holds, or ~prim for a leaf record (the refit map). */
 void serialize_threaded(const Tree &tree, const std::vector<PrimBox> &boxes,
-		std::vector<float> &out_vec4);
-/* Parse a threaded buffer back into a tree (for caller-supplied buffers). */
+		std::vector<float> &out_vec4, std::vector<int32_t> *rec_node = nullptr);
+/* Parse a threaded buffer back into a tree (for caller-supplied buffers);
+ * rec_node as above, KGR_REC_UNREACHED for records no walk reaches. */
+#define KGR_REC_UNREACHED ((int32_t)0x80000000)
 void parse_threaded(const float *vec4, uint32_t count, uint32_t prim_count,
-		const std::vector<PrimBox> &boxes, Tree &tree);
+		const std::vector<PrimBox> &boxes, Tree &tree, std::vector<int32_t> *rec_node = nullptr);
 /* Fast layout from a tree: nodes + leaf-ordered triangle records
  * {v0.xyz, prim}, {e1}, {e2}.  Boxes are padded outward so that culling is
  * conservative with respect to the exact triangle test. */
 void build_fast(const Tree &tree, const std::vector<PrimBox> &boxes,
 		const float *positions, const uint32_t *tris4, std::vector<FastNode> &nodes,
-		std::vector<float4> &tri_records);
+		std::vector<float4> &tri_records, std::vector<int2> *kids = nullptr);
 /* Wide layout from the same tree: each node gathers up to four children by
  * repeatedly opening its largest-area interior child (left-to-right order
  * kept), leaf references identical to the fast layout's so both share its
  * triangle records.  max_stack: the most stack entries a walk can hold
  * (over every root-to-node path, the sum of children - 1). */
-void build_wide(const Tree &tree, std::vector<WideNode> &nodes, uint32_t &max_stack);
+void build_wide(const Tree &tree, std::vector<WideNode> &nodes, uint32_t &max_stack,
+		std::vector<int4> *kids = nullptr);
 
 /* ---------------------------------------------------------------- scene -- */
 
@@ -207,6 +212,47 @@ struct kgr_generated {
 
 #define KGR_STACK_DEPTH_HOST 64
 
+namespace kgr {
+
+/* What a refit needs, recorded when the scene is created; the topology of
+ * every layout stays fixed, only coordinates change. */
+struct RefitPlan {
+	/* vertices, in the concatenated order of kgr_scene_create */
+	std::vector<float> obj_positions, obj_normals; /* 3 per vertex, as the meshes gave them */
+	std::vector<uint32_t> vertex_mesh;
+	/* >= 0: the vertex takes the face normal of that triangle (meshes
+	 * without normals; the last triangle that names the vertex);
+	 * KGR_NORMAL_OWN: the mesh's own normal; KGR_NORMAL_ZERO: zero */
+	std::vector<int32_t> normal_src;
+	std::vector<float> models;     /* 16 per mesh, column-major (glm::mat4) */
+	std::vector<int32_t> has_model; /* per mesh: 0 = vertices taken as given */
+	std::vector<uint32_t> light_tri; /* triangle of each light */
+	/* tree: node {left, right, first, count}; count > 0 marks a leaf over
+	 * prim_order[first, first + count) */
+	std::vector<int4> nodes;
+	std::vector<uint32_t> prim_order;
+	std::vector<uint32_t> level_order; /* node ids, deepest level first */
+	std::vector<uint32_t> level_begin; /* level l = level_order[level_begin[l], level_begin[l + 1]) */
+	std::vector<int32_t> rec_node;     /* threaded record -> node, ~prim for leaf records */
+	std::vector<int2> fast_kids;       /* fast node -> its two child nodes (-1: none) */
+	std::vector<int4> wide_kids;       /* wide node -> its child nodes (-1: empty slot) */
+};
+#define KGR_NORMAL_OWN (-1)
+#define KGR_NORMAL_ZERO (-2)
+
+/* The plan on the device, uploaded by the first refit. */
+struct RefitDevice {
+	bool ready = false;
+	DevBuf<float4> obj_positions, obj_normals, boxes;
+	DevBuf<uint32_t> vertex_mesh, light_tri, prim_order, level_order;
+	DevBuf<int32_t> normal_src, has_model, rec_node;
+	DevBuf<float> models;
+	DevBuf<int4> nodes, wide_kids;
+	DevBuf<int2> fast_kids;
+};
+
+} /* namespace kgr */
+
 struct kgr_scene {
 	int device = 0;
 	std::vector<float> positions, normals; /* 3 per vertex */
@@ -225,6 +271,10 @@ struct kgr_scene {
 	kgr::DevBuf<kgr::WideNode> d_wide_nodes;
 	kgr::DevBuf<kgr_material> d_materials;
 	kgr::DevBuf<kgr_triangle_light> d_lights;
+
+	kgr::RefitPlan plan;
+	kgr::RefitDevice refit;
+	uint32_t refits = 0;
 
 	kgr::DeviceScene view() const;
 	uint64_t device_bytes() const;
@@ -285,6 +335,14 @@ inline double time_frames(F frame, int frames, cudaStream_t st)
 }
 
 /* ------------------------------------------------------ kernel launchers -- */
+
+/* Refit (refit.cu).  REFIT_TRANSFORM: every vertex from the object-space
+ * vertices and the current models; REFIT_POSITIONS: world-space positions
+ * (and normals, if given) from device arrays of 3 floats per vertex.  Then
+ * normals of meshes without normals, triangle lights, and every layout's
+ * boxes and triangle records, in place, on st. */
+enum { REFIT_TRANSFORM = 0, REFIT_POSITIONS = 1 };
+void refit_scene(kgr_scene *sc, int mode, const float *positions, const float *normals, cudaStream_t st);
 
 /* Traversal of a ray buffer (8 floats per ray) into hits or occlusion flags. */
 void launch_trace_closest(const DeviceScene &s, const float4 *rays, uint32_t n,

@@ -19,6 +19,7 @@ vp = ctypes.c_void_p
 
 LAYOUT_FAST, LAYOUT_THREADED, LAYOUT_WIDE = 0, 1, 2
 BUILDER_SAH, BUILDER_KOBRA, BUILDER_SAH_HOST = 0, 1, 2
+ARRAY_THREADED, ARRAY_FAST_NODES, ARRAY_WIDE_NODES, ARRAY_TRIANGLE_RECORDS = 0, 1, 2, 3
 VALUE_NONE, VALUE_INT, VALUE_FLOAT, VALUE_BOOL, VALUE_STRING = range(5)
 
 
@@ -127,6 +128,10 @@ def lib():
             "kgr_bvh_build_host": (c_i32, [vp, c_u32, vp, c_u32, c_i32, c_i32, vp, c_u32, vp]),
             "kgr_scene_copy_bvh": (c_i32, [vp, vp, c_u32, vp]),
             "kgr_scene_copy_lights": (c_i32, [vp, vp, c_u32, vp]),
+            "kgr_scene_copy_vertices": (c_i32, [vp, vp, vp]),
+            "kgr_scene_copy_array": (c_i32, [vp, c_i32, vp, c_u64, vp]),
+            "kgr_scene_set_transforms": (c_i32, [vp, vp, vp, c_u32, vp]),
+            "kgr_scene_refit": (c_i32, [vp, vp, vp, vp]),
             "kgr_scene_destroy": (c_i32, [vp]),
             "kgr_trace_closest": (c_i32, [vp, vp, c_u32, vp, c_i32, vp]),
             "kgr_trace_any": (c_i32, [vp, vp, c_u32, vp, c_i32, vp]),
@@ -256,20 +261,32 @@ class Scene:
     """A device-resident scene: triangles, materials, lights and both BVH layouts."""
 
     def __init__(self, positions, indices, materials_raw, normals=None, material_indices=None,
-                 builder=BUILDER_SAH, max_leaf=4, device=-1, bvh=None):
-        self._keep = [_f32(positions), None if normals is None else _f32(normals), _u32(indices),
-                      None if material_indices is None else _u32(material_indices),
-                      _f32(materials_raw)]
-        pos, nrm, idx, mid, mats = self._keep
-        mesh = Mesh(_ptr(pos), _ptr(nrm), len(pos), _ptr(idx), _ptr(mid), len(idx), None)
+                 builder=BUILDER_SAH, max_leaf=4, device=-1, bvh=None, meshes=None):
+        """One mesh from positions/indices/normals/material_indices, or
+        several: meshes = [dict(positions=, indices=, normals=None,
+        material_indices=None, model=None (4x4, applied as glm's column-major
+        mat4 * vec4, i.e. model @ [p, 1]))]; positions/indices are then None."""
+        if meshes is None:
+            meshes = [dict(positions=positions, indices=indices, normals=normals,
+                           material_indices=material_indices)]
+        self._keep = [_f32(materials_raw)]
+        arr = (Mesh * len(meshes))()
+        for k, m in enumerate(meshes):
+            pos, idx = _f32(m["positions"]), _u32(m["indices"])
+            nrm = None if m.get("normals") is None else _f32(m["normals"])
+            mid = None if m.get("material_indices") is None else _u32(m["material_indices"])
+            model = None if m.get("model") is None else _f32(np.asarray(m["model"], np.float32).T)
+            self._keep += [pos, idx, nrm, mid, model]
+            arr[k] = Mesh(_ptr(pos), _ptr(nrm), len(pos), _ptr(idx), _ptr(mid), len(idx), _ptr(model))
+        mats = self._keep[0]
         h = vp()
         if bvh is None:
             opt = SceneOptions(builder, max_leaf, device, 0)
-            check(lib().kgr_scene_create(ctypes.byref(mesh), 1, _ptr(mats), len(mats), ctypes.byref(opt),
+            check(lib().kgr_scene_create(arr, len(meshes), _ptr(mats), len(mats), ctypes.byref(opt),
                                          ctypes.byref(h)))
         else:
             b = _f32(bvh)
-            check(lib().kgr_scene_create_from_bvh(ctypes.byref(mesh), 1, _ptr(mats), len(mats), _ptr(b),
+            check(lib().kgr_scene_create_from_bvh(arr, len(meshes), _ptr(mats), len(mats), _ptr(b),
                                                   len(b), device, ctypes.byref(h)))
         self.handle = h
 
@@ -296,6 +313,32 @@ class Scene:
         out = np.zeros((n.value, 12), np.float32)
         check(lib().kgr_scene_copy_lights(self.handle, _ptr(out), n.value, ctypes.byref(n)))
         return out
+
+    def vertices(self):
+        """(positions, normals) as (V, 3) float32, read from the device."""
+        n = self.info().vertex_count
+        p, q = np.zeros((n, 3), np.float32), np.zeros((n, 3), np.float32)
+        check(lib().kgr_scene_copy_vertices(self.handle, _ptr(p), _ptr(q)))
+        return p, q
+
+    def array(self, which):
+        """Raw bytes (uint8) of one device array: ARRAY_THREADED, ARRAY_FAST_NODES,
+        ARRAY_WIDE_NODES or ARRAY_TRIANGLE_RECORDS."""
+        n = c_u64()
+        check(lib().kgr_scene_copy_array(self.handle, which, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value, np.uint8)
+        check(lib().kgr_scene_copy_array(self.handle, which, _ptr(out), n.value, ctypes.byref(n)))
+        return out
+
+    def set_transforms(self, mesh_ids, models, stream=None):
+        """New 4x4 model matrices (model @ [p, 1]) for the listed meshes, then a refit."""
+        ids = _u32(mesh_ids)
+        ms = _f32(np.stack([np.asarray(m, np.float32).T for m in models])) if len(ids) else None
+        check(lib().kgr_scene_set_transforms(self.handle, _ptr(ids), _ptr(ms), len(ids), stream))
+
+    def refit(self, positions_ptr, normals_ptr=None, stream=None):
+        """New world-space positions (device pointer, 3 floats per vertex), then a refit."""
+        check(lib().kgr_scene_refit(self.handle, positions_ptr, normals_ptr, stream))
 
     def trace_closest(self, rays_ptr, n, hits_ptr, layout=LAYOUT_FAST, stream=None):
         check(lib().kgr_trace_closest(self.handle, rays_ptr, n, hits_ptr, layout, stream))

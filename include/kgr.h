@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define KGR_ABI_VERSION 2
+#define KGR_ABI_VERSION 3
 
 typedef enum kgr_status {
 	KGR_OK = 0,
@@ -179,6 +179,48 @@ kgr_status kgr_scene_copy_bvh(const kgr_scene *scene, float *out_vec4,
 /* Host copy of the triangle lights. */
 kgr_status kgr_scene_copy_lights(const kgr_scene *scene, kgr_triangle_light *out,
 		uint32_t capacity, uint32_t *count);
+
+/* Host copy of the current vertices (3 floats per vertex, concatenated
+ * mesh order); either pointer may be NULL. */
+kgr_status kgr_scene_copy_vertices(const kgr_scene *scene, float *positions, float *normals);
+
+/* Raw bytes of one device array of the scene (diagnostics and tests). */
+enum {
+	KGR_ARRAY_THREADED = 0,         /* float4 x 3 per record, bvh.cpp layout */
+	KGR_ARRAY_FAST_NODES = 1,       /* 64-byte child-pair nodes */
+	KGR_ARRAY_WIDE_NODES = 2,       /* 128-byte four-child nodes */
+	KGR_ARRAY_TRIANGLE_RECORDS = 3  /* float4 x 3 per triangle in walk order: {v0, prim}, e1, e2 */
+};
+kgr_status kgr_scene_copy_array(const kgr_scene *scene, int32_t which, void *out,
+		uint64_t capacity_bytes, uint64_t *bytes);
+
+/* Animated instances.  The reference moves an instance by giving its GAS a
+ * new transform in the TLAS (include/amadeus/accelerator.cuh:145-230) and
+ * re-applies Transform::matrix() to the vertices of emissive submeshes for
+ * the light buffer (source/amadeus/armada.cu:160-205).  Here the scene is
+ * one world-space BVH, so a transform change is a refit: set the model
+ * matrix of `count` meshes (16 floats each, column-major like glm::mat4 and
+ * kgr_mesh.model; meshes are numbered in kgr_scene_create order), recompute
+ * every vertex, normal and triangle light on the device from the meshes'
+ * object-space data, then recompute the boxes of every BVH layout and the
+ * triangle records in place.  The topology is kept: traversal stays exact,
+ * but a tree refitted far from its build shape walks more nodes (create the
+ * scene again to rebuild it).  Each box equals what the builder would
+ * compute over the same tree from the new vertices.  Asynchronous on
+ * `stream`; order refits and renders of one scene on one stream (or with
+ * events).  A captured CUDA graph of a frame stays valid: arrays are
+ * updated in place.  bounds_min/max of kgr_scene_info keep their values
+ * from creation (the radiance cache's input frame). */
+kgr_status kgr_scene_set_transforms(kgr_scene *scene, const uint32_t *mesh_ids,
+		const float *models, uint32_t count, void *stream);
+
+/* Deformed geometry: new world-space positions for every vertex (DEVICE
+ * array, 3 floats per vertex in kgr_scene_create order) and, optionally,
+ * normals (NULL keeps the current normals, except that meshes created
+ * without normals get their face normals recomputed).  Then the same refit
+ * as kgr_scene_set_transforms.  A later kgr_scene_set_transforms starts
+ * again from the object-space vertices. */
+kgr_status kgr_scene_refit(kgr_scene *scene, const float *positions, const float *normals, void *stream);
 
 kgr_status kgr_scene_destroy(kgr_scene *scene);
 

@@ -1890,7 +1890,8 @@ kgr_status kgr_camera_setup(const float eye[3], const float target[3], const flo
 		nrm(u);
 		crs(u, w, v);
 		nrm(v);
-		float half = (float)(fov_deg * 0.01745329251994329576923690768489) / 2.0f;
+		/* glm::radians(fov) / 2: a float product with the float constant */
+		float half = fov_deg * (float)0.01745329251994329576923690768489 / 2.0f;
 		float vlen = wlen * tanf(half);
 		for (int k = 0; k < 3; k++)
 			v[k] *= vlen;

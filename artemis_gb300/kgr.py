@@ -172,6 +172,17 @@ def lib():
             "kgr_generated_get": (c_i32, [vp, vp]),
             "kgr_generated_destroy": (c_i32, [vp]),
             "kgr_camera_setup": (c_i32, [vp, vp, vp, c_f, c_f, vp]),
+            "kgr_transform_matrix": (c_i32, [vp, vp, vp, vp]),
+            "kgr_project_open": (c_i32, [ctypes.c_char_p, vp]),
+            "kgr_project_scene_count": (c_i32, [vp, vp]),
+            "kgr_project_scene_file": (c_i32, [vp, c_u32, vp]),
+            "kgr_project_read_scene": (c_i32, [vp, c_i32, vp]),
+            "kgr_project_scene_info_get": (c_i32, [vp, vp]),
+            "kgr_project_scene_meshes": (c_i32, [vp, vp, vp, vp, vp]),
+            "kgr_project_scene_entity": (c_i32, [vp, c_u32, vp]),
+            "kgr_project_scene_camera": (c_i32, [vp, c_u32, c_f, vp]),
+            "kgr_project_scene_destroy": (c_i32, [vp]),
+            "kgr_project_close": (c_i32, [vp]),
             "kgr_batcher_create": (c_i32, [c_i32, c_u32, c_u32, vp]),
             "kgr_batcher_render": (c_i32, [vp, vp, vp, c_u32, vp, vp]),
             "kgr_batcher_autotune": (c_i32, [vp, vp, vp, c_u32, vp, c_i32, vp, vp]),
@@ -279,16 +290,31 @@ class Scene:
             self._keep += [pos, idx, nrm, mid, model]
             arr[k] = Mesh(_ptr(pos), _ptr(nrm), len(pos), _ptr(idx), _ptr(mid), len(idx), _ptr(model))
         mats = self._keep[0]
+        self.handle = self._create(ctypes.cast(arr, vp), len(meshes), _ptr(mats), len(mats), builder, max_leaf,
+                                   device, bvh)
+
+    @staticmethod
+    def _create(meshes_ptr, mesh_count, materials_ptr, material_count, builder, max_leaf, device, bvh=None):
         h = vp()
         if bvh is None:
             opt = SceneOptions(builder, max_leaf, device, 0)
-            check(lib().kgr_scene_create(arr, len(meshes), _ptr(mats), len(mats), ctypes.byref(opt),
+            check(lib().kgr_scene_create(meshes_ptr, mesh_count, materials_ptr, material_count, ctypes.byref(opt),
                                          ctypes.byref(h)))
         else:
             b = _f32(bvh)
-            check(lib().kgr_scene_create_from_bvh(arr, len(meshes), _ptr(mats), len(mats), _ptr(b),
+            check(lib().kgr_scene_create_from_bvh(meshes_ptr, mesh_count, materials_ptr, material_count, _ptr(b),
                                                   len(b), device, ctypes.byref(h)))
-        self.handle = h
+        return h
+
+    @classmethod
+    def from_project(cls, project_scene, builder=BUILDER_SAH, max_leaf=4, device=-1, bvh=None):
+        """A device scene from a ProjectScene's meshes and materials (mesh k of
+        the project scene is mesh k here)."""
+        ms, n, mats, nm = project_scene.mesh_array()
+        self = cls.__new__(cls)
+        self._keep = [project_scene]
+        self.handle = cls._create(ms, n, mats, nm, builder, max_leaf, device, bvh)
+        return self
 
     @classmethod
     def from_generated(cls, g, **kw):
@@ -609,6 +635,194 @@ def launch_info(cam_info, width, height, buffers, max_depth=2, samples=0, accumu
     info.accumulate = 1 if accumulate else 0
     info.frame = frame
     return info
+
+
+# ------------------------------------------------------------ Kobra projects
+
+class ProjectSceneInfo(ctypes.Structure):
+    _fields_ = [("entity_count", c_u32), ("mesh_count", c_u32), ("vertex_count", c_u32),
+                ("triangle_count", c_u32), ("material_count", c_u32), ("textured_materials", c_u32),
+                ("missing_meshes", c_u32), ("camera_entity", c_i32)]
+
+
+class ProjectEntity(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char_p), ("position", c_f * 3), ("rotation", c_f * 3), ("scale", c_f * 3),
+                ("model", c_f * 16), ("renderable", c_i32), ("has_camera", c_i32), ("fov", c_f), ("aspect", c_f),
+                ("mesh_first", c_u32), ("mesh_count", c_u32)]
+
+    def as_dict(self):
+        return {"name": self.name.decode(), "position": list(self.position), "rotation": list(self.rotation),
+                "scale": list(self.scale), "model": np.array(self.model[:], np.float32).reshape(4, 4).T,
+                "renderable": bool(self.renderable), "has_camera": bool(self.has_camera), "fov": self.fov,
+                "aspect": self.aspect, "mesh_first": self.mesh_first, "mesh_count": self.mesh_count}
+
+
+def transform_matrix(position, rotation_deg, scale):
+    """Transform::matrix() as a 4x4 array M with M @ [p, 1] the world point."""
+    p, r, s_ = _f32(position), _f32(rotation_deg), _f32(scale)
+    out = np.zeros(16, np.float32)
+    check(lib().kgr_transform_matrix(_ptr(p), _ptr(r), _ptr(s_), _ptr(out)))
+    return out.reshape(4, 4).T.copy()
+
+
+class Project:
+    """A Kobra project directory (project.den, .kobra scenes, .cache meshes, assets/*.mat)."""
+
+    def __init__(self, directory):
+        h = vp()
+        check(lib().kgr_project_open(str(directory).encode(), ctypes.byref(h)))
+        self.handle = h
+
+    def scene_files(self):
+        n = c_u32()
+        check(lib().kgr_project_scene_count(self.handle, ctypes.byref(n)))
+        out = []
+        for i in range(n.value):
+            name = ctypes.c_char_p()
+            check(lib().kgr_project_scene_file(self.handle, i, ctypes.byref(name)))
+            out.append(name.value.decode())
+        return out
+
+    def read_scene(self, index=-1):
+        h = vp()
+        check(lib().kgr_project_read_scene(self.handle, index, ctypes.byref(h)))
+        return ProjectScene(h)
+
+    def close(self):
+        if self.handle:
+            lib().kgr_project_close(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class ProjectScene:
+    """Host arrays of one scene read from a project."""
+
+    def __init__(self, handle):
+        self.handle = handle
+
+    def info(self):
+        i = ProjectSceneInfo()
+        check(lib().kgr_project_scene_info_get(self.handle, ctypes.byref(i)))
+        return i
+
+    def entities(self):
+        out = []
+        for k in range(self.info().entity_count):
+            e = ProjectEntity()
+            check(lib().kgr_project_scene_entity(self.handle, k, ctypes.byref(e)))
+            out.append(e.as_dict())
+        return out
+
+    def mesh_array(self):
+        ms, n, mats, nm = vp(), c_u32(), vp(), c_u32()
+        check(lib().kgr_project_scene_meshes(self.handle, ctypes.byref(ms), ctypes.byref(n), ctypes.byref(mats),
+                                             ctypes.byref(nm)))
+        return ms, n.value, mats, nm.value
+
+    def meshes(self):
+        """Each mesh as a dict of numpy copies: positions, normals, indices,
+        material_indices (object space) and model (4x4, M @ [p, 1])."""
+        ms, n, _, _ = self.mesh_array()
+        arr = ctypes.cast(ms, ctypes.POINTER(Mesh))
+        out = []
+        for k in range(n):
+            m = arr[k]
+            V, T = m.vertex_count, m.triangle_count
+            get = lambda ptr, ct, cnt: np.ctypeslib.as_array((ct * cnt).from_address(ptr)).copy()
+            out.append({"positions": get(m.positions, c_f, 3 * V).reshape(V, 3),
+                        "normals": get(m.normals, c_f, 3 * V).reshape(V, 3),
+                        "indices": get(m.indices, c_u32, 3 * T).reshape(T, 3),
+                        "material_indices": get(m.material_indices, c_u32, T),
+                        "model": get(m.model, c_f, 16).reshape(4, 4).T.copy()})
+        return out
+
+    def materials_raw(self):
+        _, _, mats, nm = self.mesh_array()
+        return np.ctypeslib.as_array((c_f * (16 * nm)).from_address(mats.value)).reshape(nm, 16).copy()
+
+    def camera(self, entity=None, aspect=0.0):
+        """Launch camera of a camera entity (the first one by default)."""
+        if entity is None:
+            entity = self.info().camera_entity
+        info = LaunchInfo()
+        check(lib().kgr_project_scene_camera(self.handle, entity, aspect, ctypes.byref(info)))
+        return info
+
+    def close(self):
+        if self.handle:
+            lib().kgr_project_scene_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def write_project(directory, scenes, materials):
+    """Write a Kobra project in the layout Project::save produces
+    (source/project.cpp:63-205): .cache/<submesh> files (int32 vertex and
+    index counts, 56-byte Vertex records, uint32 indices), assets/<name>.mat
+    (the material_fmt text), one <scene>.kobra per scene and project.den.
+
+    scenes: {scene name: [entity]}, entity = dict(name, position, rotation
+    (degrees), scale, submeshes=[dict(positions, normals, indices,
+    material)], renderable=True, camera=None or (fov, aspect)); a submesh
+    whose positions is None is listed but not written (a missing cache
+    file).  materials: {name: dict(diffuse, specular, emission, roughness,
+    refraction, type)}.  Transforms are written with nine significant
+    digits, so they read back exactly."""
+    import os
+    os.makedirs(os.path.join(directory, ".cache"), exist_ok=True)
+    os.makedirs(os.path.join(directory, "assets"), exist_ok=True)
+    for name, m in materials.items():
+        d, sp, e = (m.get(k, (0.0, 0.0, 0.0)) for k in ("diffuse", "specular", "emission"))
+        text = ("name: %s\ndiffuse: %f,%f,%f\nspecular: %f,%f,%f\nemission: %f,%f,%f\nroughness: %f\n"
+                "refraction: %f\ntype: %d\nalbedo_texture: \nnormal_texture: \nroughness_texture: " %
+                (name, *d, *sp, *e, m.get("roughness", 0.001), m.get("refraction", 1.0), m.get("type", 4)))
+        with open(os.path.join(directory, "assets", name + ".mat"), "w") as f:
+            f.write(text)
+    sid = 0
+    g = lambda v: " ".join("%.9g" % float(x) for x in v)
+    for scene_name, entities in scenes.items():
+        lines = []
+        for ent in entities:
+            lines.append("")
+            lines.append("@entity " + ent["name"])
+            lines.append(".transform %s %s %s" % (g(ent.get("position", (0, 0, 0))), g(ent.get("rotation", (0, 0, 0))),
+                                                  g(ent.get("scale", (1, 1, 1)))))
+            subs = ent.get("submeshes", [])
+            if subs:
+                lines.append(".mesh %d" % len(subs))
+                for sm in subs:
+                    fname = "submesh-%d.submesh" % sid
+                    sid += 1
+                    if sm["positions"] is not None:
+                        p = _f32(sm["positions"])
+                        n = _f32(sm["normals"])
+                        idx = _u32(sm["indices"]).ravel()
+                        vert = np.zeros((len(p), 14), np.float32)
+                        vert[:, 0:3], vert[:, 3:6] = p, n
+                        with open(os.path.join(directory, ".cache", fname), "wb") as f:
+                            f.write(np.array([len(p), len(idx)], np.int32).tobytes())
+                            f.write(vert.tobytes())
+                            f.write(idx.tobytes())
+                    lines.append("\t%s, %s.mat" % (fname, sm["material"]))
+            if ent.get("renderable", True) and subs:
+                lines.append(".renderable")
+            if ent.get("camera") is not None:
+                lines.append(".camera %s" % g(ent["camera"]))
+        with open(os.path.join(directory, scene_name + ".kobra"), "w") as f:
+            f.write("\n".join(lines) + "\n")
+    with open(os.path.join(directory, "project.den"), "w") as f:
+        f.write("@scenes %d\n" % len(scenes) + "".join(s + ".kobra\n" for s in scenes))
 
 
 # ------------------------------------------------------------ batching / serving (include/kgr_serve.h)

@@ -562,6 +562,69 @@ kgr_status kgr_generate_scene(const char *name, uint64_t seed, kgr_generated **o
 kgr_status kgr_generated_get(const kgr_generated *g, kgr_generated_view *view);
 kgr_status kgr_generated_destroy(kgr_generated *g);
 
+/* ------------------------------------------------------ Kobra projects -- */
+
+/* A Kobra project directory as Project::save writes it
+ * (source/project.cpp:63-205): project.den lists the scenes; a .kobra scene
+ * file lists entities with a transform, submeshes from the .cache mesh
+ * cache with .mat materials from assets/, a renderable flag and a camera.
+ * kgr_project_open is Project::load_project (include/project.hpp:58-92);
+ * kgr_project_read_scene is Project::load_scene (source/project.cpp:
+ * 242-560) into host arrays, one kgr_mesh per submesh of a renderable
+ * entity with the entity's Transform::matrix() as its model.  Pass the
+ * meshes and materials to kgr_scene_create; mesh k of the list is mesh k
+ * of the scene, so kgr_scene_set_transforms moves entity e by its
+ * [mesh_first, mesh_first + mesh_count) range.  Host only: no device. */
+typedef struct kgr_project kgr_project;
+typedef struct kgr_project_scene kgr_project_scene;
+
+typedef struct kgr_project_scene_info {
+	uint32_t entity_count;
+	uint32_t mesh_count;         /* submeshes of renderable entities that were found */
+	uint32_t vertex_count;
+	uint32_t triangle_count;
+	uint32_t material_count;     /* distinct by name, as the material daemon keeps them */
+	uint32_t textured_materials; /* materials naming a texture (textures are not sampled) */
+	uint32_t missing_meshes;     /* submesh files that were absent: skipped, as the reference skips them */
+	int32_t camera_entity;       /* first entity with a camera, -1 if none */
+} kgr_project_scene_info;
+
+typedef struct kgr_project_entity {
+	const char *name;     /* valid while the kgr_project_scene lives */
+	float position[3];
+	float rotation[3];    /* degrees, Euler x, y, z */
+	float scale[3];
+	float model[16];      /* Transform::matrix(), column-major */
+	int32_t renderable;
+	int32_t has_camera;
+	float fov, aspect;    /* Camera component, when has_camera */
+	uint32_t mesh_first;  /* its meshes in kgr_project_scene_meshes' list */
+	uint32_t mesh_count;
+} kgr_project_entity;
+
+kgr_status kgr_project_open(const char *directory, kgr_project **out);
+kgr_status kgr_project_scene_count(const kgr_project *p, uint32_t *count);
+kgr_status kgr_project_scene_file(const kgr_project *p, uint32_t index, const char **name);
+/* index < 0: the default scene (the first) */
+kgr_status kgr_project_read_scene(const kgr_project *p, int32_t index, kgr_project_scene **out);
+kgr_status kgr_project_scene_info_get(const kgr_project_scene *s, kgr_project_scene_info *info);
+/* Pointers into the kgr_project_scene, valid while it lives. */
+kgr_status kgr_project_scene_meshes(const kgr_project_scene *s, const kgr_mesh **meshes, uint32_t *mesh_count,
+		const kgr_material **materials, uint32_t *material_count);
+kgr_status kgr_project_scene_entity(const kgr_project_scene *s, uint32_t index, kgr_project_entity *out);
+/* The launch camera of a camera entity: uvw_frame (include/camera.hpp:
+ * 45-63) from Transform::forward()/up() (include/transform.hpp:98-112),
+ * aspect <= 0 taking the entity's own. */
+kgr_status kgr_project_scene_camera(const kgr_project_scene *s, uint32_t entity, float aspect,
+		kgr_launch_info *info);
+kgr_status kgr_project_scene_destroy(kgr_project_scene *s);
+kgr_status kgr_project_close(kgr_project *p);
+
+/* Transform::matrix() (include/transform.hpp:67-72): translate(position) *
+ * mat4_cast(quat(radians(rotation))) * scale(scale), column-major. */
+kgr_status kgr_transform_matrix(const float position[3], const float rotation_deg[3], const float scale[3],
+		float out[16]);
+
 /* Camera helper: uvw_frame of include/camera.hpp:45-63 plus the glm
  * perspective/lookAt matrices of camera.hpp:20-34 (near 0.1, far 1000). */
 kgr_status kgr_camera_setup(const float eye[3], const float target[3], const float up[3],

@@ -11,9 +11,11 @@ device; `e2e` is the same metric through the C ABI with the frame read back
 to pinned host memory every step.  The roofline entry is computed live from
 CUDA events the library records after every launch on the render stream and
 from the traversal visit counts of one counting frame.  `equal_relmse`
-compares the radiance-cached tracer with the plain tracer on the same scene
-and resolution: ms/frame and relMSE against an FP64-accumulated 4096-spp
-render, and the speed-up at equal or lower relMSE.
+compares the radiance-cached tracer (BF16 and FP16 networks) with the plain
+tracer on the radiance cache's own configuration, the ReSTIR DI box scene
+at 1080p: ms/frame and relMSE against an FP64-accumulated 4096-spp render,
+and the speed-up at equal or lower relMSE; `equal_relmse_terrain` repeats
+it on the headline terrain frame.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -75,6 +77,8 @@ def parse():
     ap.add_argument("--no-quality", action="store_true",
                     help="skip the cached-vs-plain comparison at equal relMSE")
     ap.add_argument("--ref-spp", type=int, default=4096, help="spp of the FP64-accumulated reference image")
+    ap.add_argument("--quality-scene", default="box4k",
+                    help="scene of the radiance-cache comparison (the ReSTIR DI box scene at 1080p)")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving run")
     ap.add_argument("--no-restir", action="store_true", help="skip the ReSTIR DI (256^2) and GI (1080p) runs")
     ap.add_argument("--serve-seconds", type=float, default=1.0, help="arrival window of the 200 req/s phase")
@@ -236,9 +240,11 @@ def make_scene_cpu(name):
     return g, CpuScene(g)
 
 
-def relmse_compare(args, g, sc, W, H, stream, sptr):
-    """ms/frame and relMSE of the plain and the radiance-cached tracer against
-    an FP64-accumulated plain render of `--ref-spp` samples per pixel.
+def relmse_compare(args, scene_name, g, sc, W, H, stream, sptr):
+    """ms/frame and relMSE of the plain and the radiance-cached tracer (BF16
+    and FP16 networks) against an FP64-accumulated plain render of
+    `--ref-spp` samples per pixel, on `scene_name` (g, sc: that scene, or
+    None to generate it).
 
     relMSE = mean over pixels and RGB of (x - ref)^2 / (ref^2 + 0.01).  Each
     cached configuration is compared with the costliest plain configuration
@@ -251,11 +257,15 @@ def relmse_compare(args, g, sc, W, H, stream, sptr):
 
     from artemis_gb300 import kgr
 
+    own = g is None
+    if own:
+        g = kgr.Generated(scene_name, 1)
+        sc = kgr.Scene.from_generated(g)
     cam = kgr.camera(g.eye, g.target, g.fov, W / H)
     bufs = [torch.zeros((W * H, 4), dtype=torch.float32, device="cuda") for _ in range(4)]
     ptrs = [b.data_ptr() for b in bufs]
 
-    def make(spp, cache=False):
+    def make(spp, cache=None):
         a = kgr.Attachment("path_tracer")
         a.attach(W, H)
         a.load()
@@ -266,6 +276,7 @@ def relmse_compare(args, g, sc, W, H, stream, sptr):
             a.set_option(k, v)
         if cache:
             a.set_option("cache", True)
+            a.set_option("cache_dtype", cache)
         return a
 
     def info(f):
@@ -328,29 +339,35 @@ def relmse_compare(args, g, sc, W, H, stream, sptr):
         if spp <= 4:
             plain_dn[spp] = r[2:]
         a.close()
-    cached, cached_dn = {}, {}
-    for spp in (1, 2, 4):
-        a = make(spp, cache=True)
-        for f in range(300):
-            a.render(info(50000 + f), sc, sptr)
-        r = measure(a, 60000, denoise=True)
-        cached[spp] = r[:2]
-        cached_dn[spp] = r[2:]
-        a.close()
+    cached, cached_dn = {"bf16": {}, "fp16": {}}, {}
+    for dtype in ("bf16", "fp16"):
+        for spp in (1, 2, 4):
+            a = make(spp, cache=dtype)
+            for f in range(300):
+                a.render(info(50000 + f), sc, sptr)
+            r = measure(a, 60000, denoise=dtype == "bf16")
+            cached[dtype][spp] = r[:2]
+            if dtype == "bf16":
+                cached_dn[spp] = r[2:]
+            a.close()
     dn.close()
     compare = []
-    for spp, (ms, err) in cached.items():
-        worse = [k for k, (_, e) in plain.items() if e >= err]
-        if worse:
-            k = max(worse)
-            compare.append({"cached_spp": spp, "cached_ms": ms, "cached_relmse": err, "plain_spp": k,
-                            "plain_ms": plain[k][0], "plain_relmse": plain[k][1],
-                            "speedup": round(plain[k][0] / ms, 2)})
+    for dtype in ("bf16", "fp16"):
+        for spp, (ms, err) in cached[dtype].items():
+            worse = [k for k, (_, e) in plain.items() if e >= err]
+            if worse:
+                k = max(worse)
+                compare.append({"dtype": dtype, "cached_spp": spp, "cached_ms": ms, "cached_relmse": err,
+                                "plain_spp": k, "plain_ms": plain[k][0], "plain_relmse": plain[k][1],
+                                "speedup": round(plain[k][0] / ms, 2)})
     best = max(compare, key=lambda c: c["speedup"]) if compare else None
-    return {"scene": args.scene, "resolution": [W, H], "reference": f"plain PT, {frames * per} spp, FP64 mean",
+    if own:
+        sc.close()
+    return {"scene": scene_name, "resolution": [W, H], "reference": f"plain PT, {frames * per} spp, FP64 mean",
             "reference_s": round(ref_s, 1), "relmse": "mean (x - ref)^2 / (ref^2 + 0.01)",
             "plain": {str(k): {"ms": v[0], "relmse": v[1]} for k, v in plain.items()},
-            "cached_bf16": {str(k): {"ms": v[0], "relmse": v[1]} for k, v in cached.items()},
+            "cached_bf16": {str(k): {"ms": v[0], "relmse": v[1]} for k, v in cached["bf16"].items()},
+            "cached_fp16": {str(k): {"ms": v[0], "relmse": v[1]} for k, v in cached["fp16"].items()},
             "at_equal_or_lower_relmse": compare, "best_speedup": best and best["speedup"],
             "denoised": {"denoiser": "a-trous, 5 passes, normal + albedo + position guides",
                          "plain": {str(k): {"denoise_ms": v[0], "relmse": v[1]} for k, v in plain_dn.items()},
@@ -723,9 +740,14 @@ def bench_ours(args):
                                "hbm_frac": round(own / hbm, 4)},
                 "visits_per_frame": {"reference": list(visits["threaded"]), layout: list(visits[layout])}}
 
-    quality = None
+    quality = quality_terrain = None
     if rank == 0 and not args.no_quality:
-        quality = relmse_compare(args, g, sc, W, H, stream, sptr)
+        # the radiance-cache comparison on its own configuration (the
+        # ReSTIR DI box scene at 1080p), then on the headline workload
+        quality = relmse_compare(args, args.quality_scene, *((g, sc) if args.quality_scene == args.scene
+                                                              else (None, None)), W, H, stream, sptr)
+        if args.quality_scene != args.scene:
+            quality_terrain = relmse_compare(args, args.scene, g, sc, W, H, stream, sptr)
     serve = None
     if rank == 0 and not args.no_serve:
         serve = serve_run(args)
@@ -761,6 +783,7 @@ def bench_ours(args):
                 "stage_ms_per_frame": stage_ms,
                 "roofline": roofline,
                 "equal_relmse": quality,
+                "equal_relmse_terrain": quality_terrain,
                 "serve": serve,
                 "restir": restir,
                 "cpu_baseline": cpu_base,

@@ -121,7 +121,7 @@ void kgr_batcher::render(const kgr_scene *scene, const kgr_batch_job *jobs, uint
 			if (e.scene == scene && e.max_depth == fp.max_depth && e.rr == fp.russian_roulette &&
 					e.rr_start == fp.rr_start_depth && e.layout == fp.layout &&
 					e.tune.shadow == tune.shadow && e.tune.occupancy == tune.occupancy &&
-					e.tune.block == tune.block)
+					e.tune.block == tune.block && e.tune.stack == tune.stack)
 				g = &e;
 		if (!g) {
 			graphs.push_back(Graph{scene, fp.max_depth, fp.russian_roulette, fp.rr_start_depth, fp.layout, tune,
@@ -254,6 +254,7 @@ kgr_status kgr_batcher_autotune(kgr_batcher *b, const kgr_scene *scene, const kg
 				b->tune.shadow = (int16_t)c.shadow;
 				b->tune.block = (int16_t)c.block;
 				b->tune.occupancy = (int16_t)c.occupancy;
+				b->tune.stack = (int16_t)c.stack;
 				double ms = time_frames([&] { b->render(scene, jobs, n, opt, st); }, frames, st);
 				if (c.layout == KGR_LAYOUT_FAST && c.shadow == KGR_TRACE_GRID && c.block == 128 && !c.occupancy)
 					res.default_ms = ms;
@@ -263,6 +264,23 @@ kgr_status kgr_batcher_autotune(kgr_batcher *b, const kgr_scene *scene, const kg
 				}
 				res.candidates++;
 			}
+			/* second stage: the best shape with a shared-memory short stack */
+			const kgr_trace_tune first = res.best;
+			for (int k : kTuneStacks) {
+				kgr_trace_tune c = first;
+				c.stack = k;
+				opt.layout = c.layout;
+				b->tune.shadow = (int16_t)c.shadow;
+				b->tune.block = (int16_t)c.block;
+				b->tune.occupancy = (int16_t)c.occupancy;
+				b->tune.stack = (int16_t)k;
+				double ms = time_frames([&] { b->render(scene, jobs, n, opt, st); }, frames, st);
+				res.candidates++;
+				if (ms < best) {
+					best = ms;
+					res.best = c;
+				}
+			}
 			res.best_ms = best;
 		} catch (...) {
 			b->tune = old;
@@ -271,6 +289,7 @@ kgr_status kgr_batcher_autotune(kgr_batcher *b, const kgr_scene *scene, const kg
 		b->tune.shadow = (int16_t)res.best.shadow;
 		b->tune.block = (int16_t)res.best.block;
 		b->tune.occupancy = (int16_t)res.best.occupancy;
+		b->tune.stack = (int16_t)res.best.stack;
 		if (result)
 			*result = res;
 	});
@@ -285,9 +304,12 @@ kgr_status kgr_batcher_set_tune(kgr_batcher *b, const kgr_trace_tune *tune)
 		KGR_REQUIRE(tune->block == 64 || tune->block == 128 || tune->block == 256, KGR_ERR_INVALID_ARGUMENT,
 			"block must be 64, 128 or 256");
 		KGR_REQUIRE(tune->occupancy == 0 || tune->occupancy == 1, KGR_ERR_INVALID_ARGUMENT, "occupancy is 0 or 1");
+		KGR_REQUIRE(tune->stack == 0 || tune->stack == 8 || tune->stack == 16, KGR_ERR_INVALID_ARGUMENT,
+			"stack is 0, 8 or 16");
 		b->tune.shadow = (int16_t)tune->shadow;
 		b->tune.block = (int16_t)tune->block;
 		b->tune.occupancy = (int16_t)tune->occupancy;
+		b->tune.stack = (int16_t)tune->stack;
 	});
 }
 

@@ -857,7 +857,7 @@ struct kgr_attachment {
 	/* Launch shape of the fast/wide traversal: the shape kgr_autotune chose
 	 * (or the default), with any field the options set overriding it:
 	 * trace_shadow "grid" | "persistent", trace_block 64 | 128 | 256,
-	 * trace_occupancy 0 | 1. */
+	 * trace_occupancy 0 | 1, trace_stack 0 | 8 | 16. */
 	TraceTune tuned = default_trace_tune();
 	TraceTune trace_tune() const
 	{
@@ -873,6 +873,9 @@ struct kgr_attachment {
 		int o = opt_int("trace_occupancy", -1);
 		if (o == 0 || o == 1)
 			t.occupancy = (int16_t)o;
+		int k = opt_int("trace_stack", -1);
+		if (k == 0 || k == 8 || k == 16)
+			t.stack = (int16_t)k;
 		return t;
 	}
 
@@ -1562,7 +1565,7 @@ static const std::map<std::string, OptionValue> &option_defaults()
 		{"gi_radius", 30},
 		{"cache", false}, {"cache_train", true}, {"cache_train_paths", 16384}, {"cache_lr", 1e-3f},
 		{"cache_dtype", std::string("bf16")}, {"cache_infer", std::string("tcgen05")}, {"reset_history", false},
-		{"trace_shadow", std::string("")}, {"trace_block", 0}, {"trace_occupancy", -1}};
+		{"trace_shadow", std::string("")}, {"trace_block", 0}, {"trace_occupancy", -1}, {"trace_stack", -1}};
 	return d;
 }
 
@@ -1667,7 +1670,7 @@ kgr_status kgr_autotune(kgr_attachment *att, const kgr_launch_info *info, const 
 		cudaStream_t st = (cudaStream_t)stream;
 		/* the options override the tuned shape: set them aside while tuning */
 		std::map<std::string, OptionValue> held;
-		for (const char *k : {"layout", "trace_shadow", "trace_block", "trace_occupancy"}) {
+		for (const char *k : {"layout", "trace_shadow", "trace_block", "trace_occupancy", "trace_stack"}) {
 			auto it = att->options.find(k);
 			if (it != att->options.end()) {
 				held[k] = it->second;
@@ -1685,6 +1688,7 @@ kgr_status kgr_autotune(kgr_attachment *att, const kgr_launch_info *info, const 
 				att->tuned.shadow = (int16_t)c.shadow;
 				att->tuned.block = (int16_t)c.block;
 				att->tuned.occupancy = (int16_t)c.occupancy;
+				att->tuned.stack = (int16_t)c.stack;
 				double ms = time_frames([&] { render_frame(att, info, sc, st); }, frames, st);
 				if (c.layout == KGR_LAYOUT_FAST && c.shadow == KGR_TRACE_GRID && c.block == 128 && !c.occupancy)
 					res.default_ms = ms;
@@ -1694,11 +1698,29 @@ kgr_status kgr_autotune(kgr_attachment *att, const kgr_launch_info *info, const 
 				}
 				res.candidates++;
 			}
+			/* second stage: the best shape with a shared-memory short stack */
+			const kgr_trace_tune first = res.best;
+			for (int k : kTuneStacks) {
+				kgr_trace_tune c = first;
+				c.stack = k;
+				att->tuned_layout = c.layout;
+				att->tuned.shadow = (int16_t)c.shadow;
+				att->tuned.block = (int16_t)c.block;
+				att->tuned.occupancy = (int16_t)c.occupancy;
+				att->tuned.stack = (int16_t)k;
+				double ms = time_frames([&] { render_frame(att, info, sc, st); }, frames, st);
+				res.candidates++;
+				if (ms < best) {
+					best = ms;
+					res.best = c;
+				}
+			}
 			res.best_ms = best;
 			att->tuned_layout = res.best.layout;
 			att->tuned.shadow = (int16_t)res.best.shadow;
 			att->tuned.block = (int16_t)res.best.block;
 			att->tuned.occupancy = (int16_t)res.best.occupancy;
+			att->tuned.stack = (int16_t)res.best.stack;
 		} catch (...) {
 			att->tuned_layout = old_layout;
 			att->tuned = old_tune;
@@ -1722,6 +1744,7 @@ kgr_status kgr_get_trace_tune(const kgr_attachment *att, kgr_trace_tune *tune)
 		tune->shadow = t.shadow;
 		tune->block = t.block;
 		tune->occupancy = t.occupancy;
+		tune->stack = t.stack;
 	});
 }
 

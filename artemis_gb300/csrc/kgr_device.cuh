@@ -296,14 +296,59 @@ __device__ __forceinline__ void order_pair(float &ta, int32_t &ca, float &tb, in
 	ca = c;
 }
 
+/* Per-thread traversal stack in local memory: `a` is the caller's array of
+ * KGR_STACK_DEPTH entries (the builder rejects trees whose walk could need
+ * more).  The object holds only the pointer and the depth, so the depth
+ * stays in a register. */
+struct LocalStack {
+	int32_t *a;
+	int sp;
+	__device__ __forceinline__ LocalStack(int32_t *shared_column, int32_t *local) : a(local), sp(0)
+	{
+		(void)shared_column;
+	}
+	__device__ __forceinline__ bool empty() const { return sp == 0; }
+	__device__ __forceinline__ void clear() { sp = 0; }
+	__device__ __forceinline__ void push(int32_t v) { a[sp++] = v; }
+	__device__ __forceinline__ int32_t pop() { return a[--sp]; }
+};
+
+/* Short stack: the first SHORT entries of each thread in shared memory,
+ * deeper ones in the caller's local array of KGR_STACK_DEPTH - SHORT.
+ * `col` is the thread's column of a SHORT x BLOCK block array: entry k of
+ * thread t sits at k * BLOCK + t, so the 32 lanes of a warp touch 32
+ * different banks whatever depths they are at. */
+template <int SHORT, int BLOCK>
+struct ShortStack {
+	int32_t *col;
+	int32_t *deep;
+	int sp;
+	__device__ __forceinline__ ShortStack(int32_t *column, int32_t *local) : col(column), deep(local), sp(0) {}
+	__device__ __forceinline__ bool empty() const { return sp == 0; }
+	__device__ __forceinline__ void clear() { sp = 0; }
+	__device__ __forceinline__ void push(int32_t v)
+	{
+		if (sp < SHORT)
+			col[sp * BLOCK] = v;
+		else
+			deep[sp - SHORT] = v;
+		sp++;
+	}
+	__device__ __forceinline__ int32_t pop()
+	{
+		--sp;
+		return sp < SHORT ? col[sp * BLOCK] : deep[sp - SHORT];
+	}
+};
+
 /* One interior node of the fast (BVH2) or wide (BVH4) layout: `ref`
  * becomes the nearest child whose padded box the ray reaches within
  * [0, best_t] and the other reached children are pushed, farthest first;
  * with none reached, `ref` is popped.  Returns false when there was nothing
  * to pop: the walk is over. */
-template <int LAYOUT>
+template <int LAYOUT, class STACK>
 __device__ __forceinline__ bool node_step(const DeviceScene &s, const FastRay &r, int32_t &ref, float best_t,
-		int32_t *stack, int &sp)
+		STACK &stack)
 {
 	if (LAYOUT == KGR_LAYOUT_WIDE) {
 		const float4 *np = reinterpret_cast<const float4 *>(s.wide_nodes + ref);
@@ -325,31 +370,31 @@ __device__ __forceinline__ bool node_step(const DeviceScene &s, const FastRay &r
 		order_pair(t1, c1, t2, c2);
 		const float inf = __int_as_float(0x7f800000);
 		if (!(t0 < inf)) {
-			if (sp == 0)
+			if (stack.empty())
 				return false;
-			ref = stack[--sp];
+			ref = stack.pop();
 			return true;
 		}
 		if (t3 < inf)
-			stack[sp++] = c3;
+			stack.push(c3);
 		if (t2 < inf)
-			stack[sp++] = c2;
+			stack.push(c2);
 		if (t1 < inf)
-			stack[sp++] = c1;
+			stack.push(c1);
 		ref = c0;
 		return true;
 	}
 	int32_t first, second;
 	int hits = fast_node(s, r, ref, best_t, first, second);
 	if (hits == 2) {
-		stack[sp++] = second;
+		stack.push(second);
 		ref = first;
 	} else if (hits == 1) {
 		ref = first;
 	} else {
-		if (sp == 0)
+		if (stack.empty())
 			return false;
-		ref = stack[--sp];
+		ref = stack.pop();
 	}
 	return true;
 }
@@ -359,9 +404,9 @@ __device__ __forceinline__ bool node_step(const DeviceScene &s, const FastRay &r
  * whose padded slab interval reaches [0, best]; the build pads boxes so that
  * no triangle the exact test accepts is culled.  Both layouts share the
  * triangle records, so they return the same hit. */
-template <bool ANY, bool COUNT, int LAYOUT = KGR_LAYOUT_FAST>
-__device__ __forceinline__ bool trace_fast(const DeviceScene &s, const f3 &o, const f3 &d,
-		float tmax, kgr_hit &best, TraceCounters *cnt = nullptr)
+template <bool ANY, bool COUNT, int LAYOUT, class STACK>
+__device__ __forceinline__ bool trace_fast_stack(const DeviceScene &s, const f3 &o, const f3 &d,
+		float tmax, kgr_hit &best, STACK &stack, TraceCounters *cnt = nullptr)
 {
 	best.prim = -1;
 	best.t = tmax;
@@ -369,22 +414,30 @@ __device__ __forceinline__ bool trace_fast(const DeviceScene &s, const f3 &o, co
 	best.b2 = 0.0f;
 	int32_t best_rank = 0x7fffffff;
 	FastRay r = fast_ray(o, d);
-	int32_t stack[KGR_STACK_DEPTH];
-	int sp = 0;
+	stack.clear();
 	int32_t ref = 0;
 	for (;;) {
 		while (ref >= 0) {
 			if (COUNT)
 				cnt->nodes++;
-			if (!node_step<LAYOUT>(s, r, ref, best.t, stack, sp))
+			if (!node_step<LAYOUT>(s, r, ref, best.t, stack))
 				return best.prim >= 0;
 		}
 		if (fast_leaf<ANY, COUNT>(s, r, ref, best, best_rank, cnt))
 			return true;
-		if (sp == 0)
+		if (stack.empty())
 			return best.prim >= 0;
-		ref = stack[--sp];
+		ref = stack.pop();
 	}
+}
+
+template <bool ANY, bool COUNT, int LAYOUT = KGR_LAYOUT_FAST>
+__device__ __forceinline__ bool trace_fast(const DeviceScene &s, const f3 &o, const f3 &d,
+		float tmax, kgr_hit &best, TraceCounters *cnt = nullptr)
+{
+	int32_t entries[KGR_STACK_DEPTH];
+	LocalStack stack(nullptr, entries);
+	return trace_fast_stack<ANY, COUNT, LAYOUT>(s, o, d, tmax, best, stack, cnt);
 }
 
 template <bool ANY>

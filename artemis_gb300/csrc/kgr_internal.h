@@ -300,10 +300,14 @@ inline std::vector<kgr_trace_tune> tune_candidates(const kgr_scene *sc)
 		for (int shadow : {KGR_TRACE_GRID, KGR_TRACE_PERSISTENT})
 			for (int block : {64, 128, 256})
 				for (int occ : {0, 1})
-					c.push_back(kgr_trace_tune{layout, shadow, block, occ});
+					c.push_back(kgr_trace_tune{layout, shadow, block, occ, 0});
 	}
 	return c;
 }
+
+/* Shared-memory stack sizes the autotuner's second stage tries on the best
+ * shape of the first. */
+static const int kTuneStacks[2] = {8, 16};
 
 /* Time `frames` calls of `frame` on `st` (one untimed call first): ms per
  * call from CUDA events. */

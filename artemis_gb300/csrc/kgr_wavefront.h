@@ -78,7 +78,7 @@ struct TraceTune {
 	int16_t shadow;    /* TraceKernel of the shadow stage (closest hit is always persistent) */
 	int16_t block;     /* threads per block: 64, 128 or 256 */
 	int16_t occupancy; /* 1: registers capped so that 48 warps fit an SM */
-	int16_t pad;
+	int16_t stack;     /* traversal stack entries a thread keeps in shared memory: 0, 8 or 16 */
 };
 
 /* The shape used when nothing was tuned. */
@@ -88,7 +88,7 @@ inline TraceTune default_trace_tune()
 	t.shadow = TRACE_GRID;
 	t.block = 128;
 	t.occupancy = 0;
-	t.pad = 0;
+	t.stack = 0;
 	return t;
 }
 

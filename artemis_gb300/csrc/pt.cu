@@ -196,9 +196,24 @@ __global__ void __launch_bounds__(128) shade_kernel(DeviceScene s, PathBuffers p
  * OCC = 1 caps registers so that 1536 threads (48 warps) fit an SM. */
 #define KGR_MIN_BLOCKS(BLOCK, OCC) ((OCC) ? 1536 / (BLOCK) : 1)
 
-template <int LAYOUT, bool COUNT, int BLOCK, int OCC = 0>
+/* The traversal stack of a kernel instantiation: SHORT entries a thread in
+ * shared memory (the rest in local memory), or all in local memory. */
+template <int SHORT, int BLOCK>
+struct StackOf {
+	typedef ShortStack<SHORT, BLOCK> type;
+};
+template <int BLOCK>
+struct StackOf<0, BLOCK> {
+	typedef LocalStack type;
+};
+
+
+template <int LAYOUT, bool COUNT, int BLOCK, int OCC = 0, int SHORT = 0>
 __global__ void __launch_bounds__(BLOCK, KGR_MIN_BLOCKS(BLOCK, OCC)) shadow_resolve_kernel(DeviceScene s, PathBuffers pb)
 {
+	__shared__ int32_t short_stack[SHORT > 0 ? SHORT * BLOCK : 1];
+	int32_t local_stack[KGR_STACK_DEPTH - SHORT];
+	typename StackOf<SHORT, BLOCK>::type stack(short_stack + threadIdx.x, local_stack);
 	const uint32_t n = pb.counters[CNT_SHADOW];
 	uint32_t stride = gridDim.x * blockDim.x;
 	TraceCounters cnt = {0, 0};
@@ -210,7 +225,8 @@ __global__ void __launch_bounds__(BLOCK, KGR_MIN_BLOCKS(BLOCK, OCC)) shadow_reso
 		if (LAYOUT == KGR_LAYOUT_THREADED)
 			occ = trace_threaded<true, COUNT>(s, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), b.w, h, &cnt);
 		else
-			occ = trace_fast<true, COUNT, LAYOUT>(s, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), b.w, h, &cnt);
+			occ = trace_fast_stack<true, COUNT, LAYOUT>(s, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), b.w, h, stack,
+				&cnt);
 		float4 c = pb.pend_c[p], e = pb.pend_e[p], be = pb.pend_b[p];
 		f3 contr = occ ? mk(0.0f) : mk(c.x, c.y, c.z);
 		f3 direct = mk(e.x, e.y, e.z) + contr / c.w;
@@ -234,10 +250,11 @@ __device__ __forceinline__ void resolve_shadow(const PathBuffers &pb, uint32_t p
  * ray of its warp is done.  One loop iteration descends to a leaf and tests
  * it.  ANY: shadow rays, resolved into the path radiance.  The grid is sized
  * to the resident capacity of the GPU. */
-template <bool ANY, bool COUNT, int LAYOUT, int BLOCK, int OCC = 0>
+template <bool ANY, bool COUNT, int LAYOUT, int BLOCK, int OCC = 0, int SHORT = 0>
 __global__ void __launch_bounds__(BLOCK, KGR_MIN_BLOCKS(BLOCK, OCC)) fast_persistent_kernel(DeviceScene s,
 		PathBuffers pb, int q)
 {
+	__shared__ int32_t short_stack[SHORT > 0 ? SHORT * BLOCK : 1];
 	const uint32_t n = ANY ? pb.counters[CNT_SHADOW] : pb.counters[q == 0 ? CNT_Q0 : CNT_Q1];
 	const uint32_t *queue = ANY ? pb.shadow_queue : pb.queue[q];
 	uint32_t *fetch = pb.counters + (ANY ? CNT_FETCH_SHADOW : CNT_FETCH_CLOSEST);
@@ -248,8 +265,8 @@ __global__ void __launch_bounds__(BLOCK, KGR_MIN_BLOCKS(BLOCK, OCC)) fast_persis
 	FastRay r;
 	kgr_hit best;
 	int32_t best_rank = 0x7fffffff;
-	int32_t stack[KGR_STACK_DEPTH];
-	int sp = 0;
+	int32_t local_stack[KGR_STACK_DEPTH - SHORT];
+	typename StackOf<SHORT, BLOCK>::type stack(short_stack + threadIdx.x, local_stack);
 	int32_t ref = 0;
 	for (;;) {
 		bool need = !have && !exhausted;
@@ -272,7 +289,7 @@ __global__ void __launch_bounds__(BLOCK, KGR_MIN_BLOCKS(BLOCK, OCC)) fast_persis
 					best.b1 = 0.0f;
 					best.b2 = 0.0f;
 					best_rank = 0x7fffffff;
-					sp = 0;
+					stack.clear();
 					ref = 0;
 					have = true;
 				} else {
@@ -288,17 +305,17 @@ __global__ void __launch_bounds__(BLOCK, KGR_MIN_BLOCKS(BLOCK, OCC)) fast_persis
 		while (ref >= 0) {
 			if (COUNT)
 				cnt.nodes++;
-			if (!node_step<LAYOUT>(s, r, ref, best.t, stack, sp)) {
+			if (!node_step<LAYOUT>(s, r, ref, best.t, stack)) {
 				done = true;
 				break;
 			}
 		}
 		if (!done) {
 			occ = fast_leaf<ANY, COUNT>(s, r, ref, best, best_rank, &cnt);
-			if (occ || sp == 0)
+			if (occ || stack.empty())
 				done = true;
 			else
-				ref = stack[--sp];
+				ref = stack.pop();
 		}
 		if (done) {
 			if (ANY)
@@ -323,22 +340,34 @@ int resident_grid(K kernel, int block)
 
 /* One launch of a persistent traversal kernel over a resident grid (the
  * grid of each instantiation is computed once). */
-template <bool ANY, bool COUNT, int LAYOUT, int BLOCK, int OCC = 0>
+template <bool ANY, bool COUNT, int LAYOUT, int BLOCK, int OCC = 0, int SHORT = 0>
 void launch_persistent(const DeviceScene &s, const PathBuffers &pb, int q, cudaStream_t st)
 {
-	static const int g = resident_grid(fast_persistent_kernel<ANY, COUNT, LAYOUT, BLOCK, OCC>, BLOCK);
-	fast_persistent_kernel<ANY, COUNT, LAYOUT, BLOCK, OCC><<<g, BLOCK, 0, st>>>(s, pb, q);
+	static const int g = resident_grid(fast_persistent_kernel<ANY, COUNT, LAYOUT, BLOCK, OCC, SHORT>, BLOCK);
+	fast_persistent_kernel<ANY, COUNT, LAYOUT, BLOCK, OCC, SHORT><<<g, BLOCK, 0, st>>>(s, pb, q);
+}
+
+template <bool ANY, int LAYOUT, int OCC, int BLOCK>
+void launch_persistent_stack(const DeviceScene &s, const PathBuffers &pb, int q, int stack, cudaStream_t st)
+{
+	if (stack == 16)
+		launch_persistent<ANY, false, LAYOUT, BLOCK, OCC, 16>(s, pb, q, st);
+	else if (stack == 8)
+		launch_persistent<ANY, false, LAYOUT, BLOCK, OCC, 8>(s, pb, q, st);
+	else
+		launch_persistent<ANY, false, LAYOUT, BLOCK, OCC, 0>(s, pb, q, st);
 }
 
 template <bool ANY, int LAYOUT, int OCC>
-void launch_persistent_occ(const DeviceScene &s, const PathBuffers &pb, int q, int block, cudaStream_t st)
+void launch_persistent_occ(const DeviceScene &s, const PathBuffers &pb, int q, int block, int stack,
+		cudaStream_t st)
 {
 	if (block == 64)
-		launch_persistent<ANY, false, LAYOUT, 64, OCC>(s, pb, q, st);
+		launch_persistent_stack<ANY, LAYOUT, OCC, 64>(s, pb, q, stack, st);
 	else if (block == 256)
-		launch_persistent<ANY, false, LAYOUT, 256, OCC>(s, pb, q, st);
+		launch_persistent_stack<ANY, LAYOUT, OCC, 256>(s, pb, q, stack, st);
 	else
-		launch_persistent<ANY, false, LAYOUT, 128, OCC>(s, pb, q, st);
+		launch_persistent_stack<ANY, LAYOUT, OCC, 128>(s, pb, q, stack, st);
 }
 
 template <bool ANY, int LAYOUT>
@@ -346,36 +375,47 @@ void launch_persistent_block(const DeviceScene &s, const PathBuffers &pb, int q,
 		cudaStream_t st)
 {
 	if (t.occupancy)
-		launch_persistent_occ<ANY, LAYOUT, 1>(s, pb, q, t.block, st);
+		launch_persistent_occ<ANY, LAYOUT, 1>(s, pb, q, t.block, t.stack, st);
 	else
-		launch_persistent_occ<ANY, LAYOUT, 0>(s, pb, q, t.block, st);
+		launch_persistent_occ<ANY, LAYOUT, 0>(s, pb, q, t.block, t.stack, st);
 }
 
-template <bool COUNT, int LAYOUT, int BLOCK, int OCC = 0>
+template <bool COUNT, int LAYOUT, int BLOCK, int OCC = 0, int SHORT = 0>
 void launch_shadow_grid(const DeviceScene &s, const PathBuffers &pb, cudaStream_t st)
 {
-	static const int g = resident_grid(shadow_resolve_kernel<LAYOUT, COUNT, BLOCK, OCC>, BLOCK);
-	shadow_resolve_kernel<LAYOUT, COUNT, BLOCK, OCC><<<g, BLOCK, 0, st>>>(s, pb);
+	static const int g = resident_grid(shadow_resolve_kernel<LAYOUT, COUNT, BLOCK, OCC, SHORT>, BLOCK);
+	shadow_resolve_kernel<LAYOUT, COUNT, BLOCK, OCC, SHORT><<<g, BLOCK, 0, st>>>(s, pb);
+}
+
+template <int LAYOUT, int OCC, int BLOCK>
+void launch_shadow_grid_stack(const DeviceScene &s, const PathBuffers &pb, int stack, cudaStream_t st)
+{
+	if (stack == 16)
+		launch_shadow_grid<false, LAYOUT, BLOCK, OCC, 16>(s, pb, st);
+	else if (stack == 8)
+		launch_shadow_grid<false, LAYOUT, BLOCK, OCC, 8>(s, pb, st);
+	else
+		launch_shadow_grid<false, LAYOUT, BLOCK, OCC, 0>(s, pb, st);
 }
 
 template <int LAYOUT, int OCC>
-void launch_shadow_grid_occ(const DeviceScene &s, const PathBuffers &pb, int block, cudaStream_t st)
+void launch_shadow_grid_occ(const DeviceScene &s, const PathBuffers &pb, int block, int stack, cudaStream_t st)
 {
 	if (block == 64)
-		launch_shadow_grid<false, LAYOUT, 64, OCC>(s, pb, st);
+		launch_shadow_grid_stack<LAYOUT, OCC, 64>(s, pb, stack, st);
 	else if (block == 256)
-		launch_shadow_grid<false, LAYOUT, 256, OCC>(s, pb, st);
+		launch_shadow_grid_stack<LAYOUT, OCC, 256>(s, pb, stack, st);
 	else
-		launch_shadow_grid<false, LAYOUT, 128, OCC>(s, pb, st);
+		launch_shadow_grid_stack<LAYOUT, OCC, 128>(s, pb, stack, st);
 }
 
 template <int LAYOUT>
 void launch_shadow_grid_block(const DeviceScene &s, const PathBuffers &pb, const TraceTune &t, cudaStream_t st)
 {
 	if (t.occupancy)
-		launch_shadow_grid_occ<LAYOUT, 1>(s, pb, t.block, st);
+		launch_shadow_grid_occ<LAYOUT, 1>(s, pb, t.block, t.stack, st);
 	else
-		launch_shadow_grid_occ<LAYOUT, 0>(s, pb, t.block, st);
+		launch_shadow_grid_occ<LAYOUT, 0>(s, pb, t.block, t.stack, st);
 }
 
 /* accumulate (amadeus_path_tracer.cu:59-70), the frame's samples in order */

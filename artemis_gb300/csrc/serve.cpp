@@ -121,7 +121,7 @@ struct kgr_server {
 	/* per scene: tuned layout and launch shape (autotune), -1 = not yet */
 	struct SceneTune {
 		int layout = -1;
-		kgr_trace_tune tune = {KGR_LAYOUT_FAST, KGR_TRACE_GRID, 128, 0};
+		kgr_trace_tune tune = {KGR_LAYOUT_FAST, KGR_TRACE_GRID, 128, 0, 0};
 	};
 	std::vector<SceneTune> scene_tune;
 
@@ -542,6 +542,7 @@ struct kgr_server {
 			batcher->tune.shadow = (int16_t)st.tune.shadow;
 			batcher->tune.block = (int16_t)st.tune.block;
 			batcher->tune.occupancy = (int16_t)st.tune.occupancy;
+			batcher->tune.stack = (int16_t)st.tune.stack;
 		}
 		if (jobs.empty()) {
 			/* FAIR: every share of this scene is still banking toward a

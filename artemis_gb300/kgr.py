@@ -18,6 +18,7 @@ c_u32, c_i32, c_u64, c_f = ctypes.c_uint32, ctypes.c_int32, ctypes.c_uint64, cty
 vp = ctypes.c_void_p
 
 LAYOUT_FAST, LAYOUT_THREADED, LAYOUT_WIDE = 0, 1, 2
+TRACE_GRID, TRACE_PERSISTENT = 0, 1
 BUILDER_SAH, BUILDER_KOBRA, BUILDER_SAH_HOST = 0, 1, 2
 ARRAY_THREADED, ARRAY_FAST_NODES, ARRAY_WIDE_NODES, ARRAY_TRIANGLE_RECORDS = 0, 1, 2, 3
 VALUE_NONE, VALUE_INT, VALUE_FLOAT, VALUE_BOOL, VALUE_STRING = range(5)
@@ -47,12 +48,12 @@ class SceneInfo(ctypes.Structure):
 
 
 class TraceTune(ctypes.Structure):
-    _fields_ = [("layout", c_i32), ("shadow", c_i32), ("block", c_i32), ("occupancy", c_i32)]
+    _fields_ = [("layout", c_i32), ("shadow", c_i32), ("block", c_i32), ("occupancy", c_i32), ("stack", c_i32)]
 
     def as_dict(self):
         return {"layout": {0: "fast", 1: "threaded", 2: "wide"}[self.layout],
                 "shadow": {0: "grid", 1: "persistent"}[self.shadow], "block": self.block,
-                "occupancy": self.occupancy}
+                "occupancy": self.occupancy, "stack": self.stack}
 
 
 class AutotuneResult(ctypes.Structure):
@@ -907,6 +908,11 @@ class Batcher:
         check(lib().kgr_batcher_autotune(self.handle, scene.handle, arr, len(jobs), ctypes.byref(opt), frames, stream,
                                          ctypes.byref(r)))
         return r.as_dict()
+
+    def set_tune(self, shadow=0, block=128, occupancy=0, stack=0):
+        """Launch shape of the traversal stages (the layout is a render argument)."""
+        t = TraceTune(LAYOUT_FAST, shadow, block, occupancy, stack)
+        check(lib().kgr_batcher_set_tune(self.handle, ctypes.byref(t)))
 
     def ray_counts(self):
         c = (c_u64 * 3)()

@@ -643,7 +643,7 @@ def bench_ours(args):
     t = att.trace_tune()
     # the comparison runs and the cached tracer use the same launch shape
     args.trace_options = {"layout": layout, "trace_shadow": t["shadow"], "trace_block": t["block"],
-                          "trace_occupancy": t["occupancy"]}
+                          "trace_occupancy": t["occupancy"], "trace_stack": t["stack"]}
     for s in range(args.warmup):
         att.render(info_for(s), sc, sptr)
     torch.cuda.synchronize()

@@ -391,6 +391,8 @@ typedef struct kgr_trace_tune {
 	int32_t block;  /* threads per block of both stages: 64, 128 or 256 */
 	int32_t occupancy; /* 0: registers as the compiler chooses; 1: capped so that
 	                    * 48 warps fit an SM (more rays in flight per SM) */
+	int32_t stack;     /* traversal stack entries a thread keeps in shared memory
+	                    * (0, 8 or 16; deeper entries in local memory) */
 } kgr_trace_tune;
 
 typedef struct kgr_autotune_result {
@@ -403,10 +405,11 @@ typedef struct kgr_autotune_result {
 
 /* The project's autotuner: renders `frames` frames of `info` (after one
  * untimed frame) with every launch shape the scene admits -- layouts fast
- * and wide (when built) x shadow kernel x block size x occupancy -- times each on
- * `stream` with CUDA events, and keeps the fastest as this attachment's
- * shape.  The options "layout", "trace_shadow" and "trace_block" still
- * override it field by field.  The frames are real renders: they write
+ * and wide (when built) x shadow kernel x block size x occupancy -- then the
+ * fastest of those with 8 and with 16 stack entries in shared memory, times
+ * each on `stream` with CUDA events, and keeps the fastest as this
+ * attachment's shape.  The options "layout", "trace_shadow", "trace_block",
+ * "trace_occupancy" and "trace_stack" still override it field by field.  The frames are real renders: they write
  * info's buffers and advance ReSTIR history and radiance-cache training.
  * Synchronous. */
 kgr_status kgr_autotune(kgr_attachment *att, const kgr_launch_info *info, const kgr_scene *scene,

@@ -59,7 +59,7 @@ LAYOUT_BYTES = {"fast": (64, 48), "wide": (128, 48), "threaded": (48, 80)}
 TRAFFIC = {("trace_closest", "fast"): 168.1e6}
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=60)
@@ -82,7 +82,7 @@ def parse():
     ap.add_argument("--no-serve", action="store_true", help="skip the serving run")
     ap.add_argument("--no-restir", action="store_true", help="skip the ReSTIR DI (256^2) and GI (1080p) runs")
     ap.add_argument("--serve-seconds", type=float, default=1.0, help="arrival window of the 200 req/s phase")
-    return ap.parse_args()
+    return ap.parse_args(argv)
 
 
 def dist_env():
@@ -90,6 +90,20 @@ def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return ws, rank, local
+
+
+def aggregate_ranks(ms, rays, ws, device):
+    """Whole-job totals of a timed region run on every rank: (the slowest
+    rank's milliseconds, the rays of all ranks).  Identity on one rank."""
+    if ws <= 1:
+        return ms, rays
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(ms), float(rays)], dtype=torch.float64, device=device)
+    tmax = t.clone()
+    dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(tmax[0]), float(t[1])
 
 
 def measured_peaks():
@@ -688,18 +702,14 @@ def bench_ours(args):
     stages = att.stage_times()
     att.set_option("profile", False)
     launches_per_frame = st.kernel_launches
-    total_ms = float(sum(step_ms))
-    if ws > 1:
-        t = torch.tensor([total_ms, float(rays)], dtype=torch.float64, device="cuda")
-        tmax = t.clone()
-        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
-        total_ms, rays = float(tmax[0]), float(t[1])
+    total_ms, rays = aggregate_ranks(float(sum(step_ms)), rays, ws, "cuda")
     value = rays / (total_ms * 1e-3) / 1e6
 
     # end to end through the C ABI with the frame read back to pinned host memory
     host = torch.empty((W * H, 4), dtype=torch.float32, pin_memory=True)
     torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
     t0 = time.perf_counter()
     e2e_rays = 0
     for s in range(args.steps):
@@ -709,7 +719,10 @@ def bench_ours(args):
         st = att.stats()
         e2e_rays += st.camera_rays + st.bounce_rays + st.shadow_rays
     e2e_s = time.perf_counter() - t0
-    e2e_value = e2e_rays / e2e_s / 1e6
+    if ws > 1:
+        torch.distributed.barrier()
+    e2e_ms, e2e_rays = aggregate_ranks(e2e_s * 1e3, e2e_rays, ws, "cuda")
+    e2e_value = e2e_rays / (e2e_ms * 1e-3) / 1e6
 
     peaks, peak_kind = measured_peaks()
     l2_gbs = kgr.read_bandwidth(64 << 20, 50, dev)

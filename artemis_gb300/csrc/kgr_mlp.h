@@ -29,9 +29,11 @@ struct MlpParams {
 void mlp_infer(const MlpParams &mp, const void *x, uint32_t n, float4 *out, cudaStream_t st,
 		const uint32_t *n_dev = nullptr);
 /* The same on the fifth-generation tensor cores (mlp_tc.cu): tcgen05.mma
- * with TMEM accumulators; sets bit 0 of *err if an mbarrier wait ran out. */
+ * with TMEM accumulators; sets bit 0 of *err if an mbarrier wait ran out.
+ * withhold_first: a test of that path (every block's first load is not
+ * issued, so its wait runs out; no output row is written). */
 void mlp_infer_tc(const MlpParams &mp, const void *x, uint32_t n, float4 *out, uint32_t *err, cudaStream_t st,
-		const uint32_t *n_dev = nullptr);
+		const uint32_t *n_dev = nullptr, bool withhold_first = false);
 /* grad (FP32, [6][64][64]) = d loss / d W over n rows; loss = sum of the
  * relative L2 terms (not divided by n).  Uses mp.partial as scratch; the
  * result does not depend on block scheduling. */

@@ -166,6 +166,18 @@ kgr_status kgr_mlp_set_inference(kgr_mlp *m, int32_t kernel)
 	});
 }
 
+kgr_status kgr_mlp_test_wait_timeout(kgr_mlp *m, const void *x, uint32_t n, float *out, void *stream)
+{
+	return guard([&] {
+		KGR_REQUIRE(m && n > 0 && x && out, KGR_ERR_INVALID_ARGUMENT, "NULL argument");
+		KGR_REQUIRE(((uintptr_t)x & 15u) == 0 && ((uintptr_t)out & 15u) == 0, KGR_ERR_INVALID_ARGUMENT,
+			"buffers must be 16-byte aligned");
+		DeviceGuard g(m->device);
+		mlp_infer_tc(m->params(), x, n, reinterpret_cast<float4 *>(out), m->tc_err.ptr, (cudaStream_t)stream,
+			nullptr, true);
+	});
+}
+
 kgr_status kgr_mlp_check(kgr_mlp *m)
 {
 	return guard([&] {

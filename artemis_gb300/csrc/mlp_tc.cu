@@ -31,7 +31,9 @@
  * the error word; the block stops at the next layer boundary (the decision
  * is taken by all its threads together), waits (bounded) for its TMA load in
  * flight, frees its TMEM and returns; the host reads the word with
- * kgr_mlp_check.
+ * kgr_mlp_check.  kgr_mlp_test_wait_timeout exercises that path: its launch
+ * withholds each block's first load, so the wait on it runs out (after
+ * TC_WAIT_TEST_LIMIT polls) before any MMA was issued.
  */
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -62,6 +64,7 @@ namespace {
 #define TC_SMEM (TC_SLOT_OFF + 8u)              /* 75,808 bytes: three CTAs fit an SM */
 #define TC_TMEM_COLS 64u
 #define TC_WAIT_LIMIT (1u << 24)    /* mbarrier polls before a wait gives up */
+#define TC_WAIT_TEST_LIMIT (1u << 16) /* the same, in a launch that tests the give-up path */
 
 /* Byte offset of element (r, k) of an R x 64 K-major operand without
  * swizzle (the weights). */
@@ -133,11 +136,11 @@ __device__ __forceinline__ void tc_commit(uint32_t bar)
 		: "memory");
 }
 
-/* Poll the mbarrier for the completion of `parity`, at most TC_WAIT_LIMIT
- * times.  Returns false when it gave up. */
-__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity)
+/* Poll the mbarrier for the completion of `parity`, at most `limit` times.
+ * Returns false when it gave up. */
+__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity, uint32_t limit)
 {
-	for (uint32_t i = 0; i < TC_WAIT_LIMIT; i++) {
+	for (uint32_t i = 0; i < limit; i++) {
 		uint32_t done;
 		asm volatile(
 			"{\n\t.reg .pred p;\n\t"
@@ -196,8 +199,9 @@ __device__ __forceinline__ uint32_t pack_relu<__half>(uint32_t lo, uint32_t hi)
 template <class T>
 __global__ void __launch_bounds__(128) mlp_infer_tc_kernel(const T *__restrict__ wt_g,
 		const __grid_constant__ CUtensorMap xmap, uint32_t n, float4 *__restrict__ out,
-		const uint32_t *__restrict__ n_dev, uint32_t *__restrict__ err)
+		const uint32_t *__restrict__ n_dev, uint32_t *__restrict__ err, uint32_t withhold_first)
 {
+	const uint32_t limit = withhold_first ? TC_WAIT_TEST_LIMIT : TC_WAIT_LIMIT;
 	if (n_dev) {
 		uint32_t c = *n_dev;
 		n = c < n ? c : n;
@@ -253,7 +257,7 @@ __global__ void __launch_bounds__(128) mlp_infer_tc_kernel(const T *__restrict__
 	uint32_t pend_bar = 0, pend_parity = 0;
 
 	uint32_t t = blockIdx.x;
-	if (tid == 0 && t < tiles)
+	if (tid == 0 && t < tiles && !withhold_first)
 		tma_tile(&xmap, xbase0, tbar[0], (int)(t * TC_ROWS));
 	for (uint32_t i = 0; ok && t < tiles; i++, t += gridDim.x) {
 		const uint32_t buf = i & 1u;
@@ -267,7 +271,7 @@ __global__ void __launch_bounds__(128) mlp_infer_tc_kernel(const T *__restrict__
 		pending = tn < tiles;
 		pend_bar = tbar[buf ^ 1u];
 		pend_parity = ((i + 1u) >> 1) & 1u;
-		bool got = bar_wait(tbar[buf], (i >> 1) & 1u);
+		bool got = bar_wait(tbar[buf], (i >> 1) & 1u, limit);
 		ok = __syncthreads_and(got) != 0;
 		if (!ok)
 			break;
@@ -281,7 +285,7 @@ __global__ void __launch_bounds__(128) mlp_infer_tc_kernel(const T *__restrict__
 						last ? id_out : id_hidden, kc > 0 ? 1u : 0u);
 				tc_commit(bar);
 			}
-			got = bar_wait(bar, parity);
+			got = bar_wait(bar, parity, limit);
 			parity ^= 1u;
 			ok = __syncthreads_and(got) != 0;
 			tc_after();
@@ -321,7 +325,7 @@ __global__ void __launch_bounds__(128) mlp_infer_tc_kernel(const T *__restrict__
 		/* the next tile's load may still be in flight: give it its
 		 * (bounded) time before the block exits */
 		if (pending)
-			bar_wait(pend_bar, pend_parity);
+			bar_wait(pend_bar, pend_parity, limit);
 	}
 	tc_before();
 	__syncthreads();
@@ -362,7 +366,7 @@ EncodeTiledFn encode_tiled()
 } /* namespace */
 
 void mlp_infer_tc(const MlpParams &mp, const void *x, uint32_t n, float4 *out, uint32_t *err, cudaStream_t st,
-		const uint32_t *n_dev)
+		const uint32_t *n_dev, bool withhold_first)
 {
 	if (n == 0)
 		return;
@@ -387,12 +391,12 @@ void mlp_infer_tc(const MlpParams &mp, const void *x, uint32_t n, float4 *out, u
 		static bool once = (set_tc_smem(mlp_infer_tc_kernel<__nv_bfloat16>), true);
 		(void)once;
 		mlp_infer_tc_kernel<__nv_bfloat16><<<grid, 128, TC_SMEM, st>>>(
-			static_cast<const __nv_bfloat16 *>(mp.wt), map, n, out, n_dev, err);
+			static_cast<const __nv_bfloat16 *>(mp.wt), map, n, out, n_dev, err, withhold_first ? 1u : 0u);
 	} else {
 		static bool once = (set_tc_smem(mlp_infer_tc_kernel<__half>), true);
 		(void)once;
 		mlp_infer_tc_kernel<__half><<<grid, 128, TC_SMEM, st>>>(static_cast<const __half *>(mp.wt), map, n, out,
-			n_dev, err);
+			n_dev, err, withhold_first ? 1u : 0u);
 	}
 	KGR_CUDA(cudaGetLastError());
 }

@@ -166,6 +166,7 @@ def lib():
             "kgr_denoiser_destroy": (c_i32, [vp]),
             "kgr_denoiser_copy_result": (c_i32, [vp, vp, c_u64]),
             "kgr_mlp_check": (c_i32, [vp]),
+            "kgr_mlp_test_wait_timeout": (c_i32, [vp, vp, c_u32, vp, vp]),
             "kgr_get_visit_counts": (c_i32, [vp, vp]),
             "kgr_measure_read_bandwidth": (c_i32, [c_i32, c_u64, c_i32, vp]),
             "kgr_load_attachment": (PluginRet, [ctypes.c_char_p]),
@@ -514,6 +515,10 @@ class Mlp:
     def check(self):
         """Raise if a tcgen05 inference gave up on an mbarrier wait."""
         check(lib().kgr_mlp_check(self.handle))
+
+    def test_wait_timeout(self, x_ptr, n, out_ptr, stream=None):
+        """One tcgen05 inference whose loads are withheld, so its waits run out (a test of that path)."""
+        check(lib().kgr_mlp_test_wait_timeout(self.handle, x_ptr, n, out_ptr, stream))
 
     def close(self):
         if self.handle:

@@ -482,6 +482,12 @@ kgr_status kgr_mlp_set_inference(kgr_mlp *mlp, int32_t kernel);
 /* Synchronise the device and report a tcgen05 inference whose mbarrier wait
  * ran out (KGR_ERR_CUDA; the flag is then cleared).  KGR_OK otherwise. */
 kgr_status kgr_mlp_check(kgr_mlp *mlp);
+/* A test of the timeout path: one tcgen05 inference over x (n rows) whose
+ * blocks never issue their first tile's load, so each block's wait on it
+ * runs out after 65,536 polls; the blocks set the error word, free their
+ * tensor memory and return without writing `out`.  kgr_mlp_check then
+ * reports KGR_ERR_CUDA, and the network stays usable. */
+kgr_status kgr_mlp_test_wait_timeout(kgr_mlp *mlp, const void *x, uint32_t n, float *out, void *stream);
 
 /* ------------------------------------------------------ after the frame -- */
 

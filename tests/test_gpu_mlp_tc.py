@@ -66,3 +66,27 @@ def test_tcgen05_inference_speed_beside_mma():
     flops = 2.0 * (5 * 64 * 64 + 64 * 16) * n
     print({k: f"{v:.3f} ms, {flops / v / 1e9:.1f} TFLOP/s" for k, v in times.items()})
     assert all(v > 0 for v in times.values())
+
+
+def test_tcgen05_wait_timeout_is_reported_and_the_network_recovers():
+    """A launch whose tile loads are withheld: every block's wait on its first
+    load runs out (65,536 polls), the error word is set and kgr_mlp_check
+    raises; the blocks free their tensor memory, nothing is written, and the
+    next ordinary inference is correct."""
+    net = kgr.Mlp("bf16", seed=5)
+    W = net.weights()
+    rng = np.random.default_rng(1)
+    n = 3000
+    x = mlp_ref.encode_inputs(rng, n, "bf16")
+    xd = half_tensor(x, "bf16")
+    out = torch.full((n, 4), -7.0, dtype=torch.float32, device="cuda")
+    net.set_inference("tcgen05")
+    net.test_wait_timeout(xd.data_ptr(), n, out.data_ptr())
+    with pytest.raises(kgr.KgrError, match="iteration limit"):
+        net.check()
+    assert torch.all(out == -7.0)
+    net.check()  # the flag was cleared
+    net.forward(xd.data_ptr(), n, out.data_ptr())
+    net.check()
+    ref, _ = mlp_ref.forward(W, x, "bf16")
+    assert np.abs(out.cpu().numpy()[:, :3] - ref).max() <= 2e-2 * np.abs(ref).max() + 1e-6

@@ -404,6 +404,61 @@ __device__ __forceinline__ bool node_step(const DeviceScene &s, const FastRay &r
  * whose padded slab interval reaches [0, best]; the build pads boxes so that
  * no triangle the exact test accepts is culled.  Both layouts share the
  * triangle records, so they return the same hit. */
+/* A walk with nothing left to visit. */
+#define KGR_REF_NONE ((int32_t)0x80000000)
+
+/* Descend until every active lane of the warp holds a leaf, or has no node
+ * left (the postponed-leaf traversal of Aila and Laine, "Understanding the
+ * Efficiency of Ray Traversal on GPUs", HPG 2009).  A lane that reaches a
+ * leaf parks it in `leaf` and keeps descending from the next stacked node
+ * while other lanes are still looking for theirs, so the warp then tests
+ * leaves together instead of alternating between node steps and triangle
+ * tests lane by lane.  On return `leaf` is 0 or a parked leaf, and `ref` is
+ * an interior node (the lane ran ahead), a second leaf, or KGR_REF_NONE.
+ * The extra nodes a lane visits ahead are culled against a best distance
+ * that its parked leaf may still shorten, so the walk tests a superset of
+ * the nodes and triangles of the plain order; the closest hit, a minimum
+ * over (t, rank), and occlusion are unchanged. */
+template <int LAYOUT, bool COUNT, class STACK>
+__device__ __forceinline__ void speculative_descend(const DeviceScene &s, const FastRay &r, int32_t &ref,
+		int32_t &leaf, float best_t, STACK &stack, TraceCounters *cnt)
+{
+	for (;;) {
+		if (ref >= 0) {
+			if (COUNT)
+				cnt->nodes++;
+			if (!node_step<LAYOUT>(s, r, ref, best_t, stack))
+				ref = KGR_REF_NONE;
+		}
+		if (ref < 0 && ref != KGR_REF_NONE && leaf == 0) {
+			leaf = ref;
+			ref = stack.empty() ? KGR_REF_NONE : stack.pop();
+		}
+		/* a lane stops only once it holds a leaf or is out of nodes, so the
+		 * vote over the lanes executing here never ends another lane's
+		 * search early */
+		if (!__any_sync(__activemask(), leaf == 0 && ref >= 0))
+			return;
+	}
+}
+
+/* Test the parked leaf and, when the descent stopped on a second one, that
+ * one too (then take the next stacked node).  Returns true on an occluding
+ * hit (ANY). */
+template <bool ANY, bool COUNT, class STACK>
+__device__ __forceinline__ bool test_leaves(const DeviceScene &s, const FastRay &r, int32_t &ref, int32_t leaf,
+		kgr_hit &best, int32_t &best_rank, STACK &stack, TraceCounters *cnt)
+{
+	if (leaf != 0 && fast_leaf<ANY, COUNT>(s, r, leaf, best, best_rank, cnt))
+		return true;
+	if (ref < 0 && ref != KGR_REF_NONE) {
+		if (fast_leaf<ANY, COUNT>(s, r, ref, best, best_rank, cnt))
+			return true;
+		ref = stack.empty() ? KGR_REF_NONE : stack.pop();
+	}
+	return false;
+}
+
 template <bool ANY, bool COUNT, int LAYOUT, class STACK>
 __device__ __forceinline__ bool trace_fast_stack(const DeviceScene &s, const f3 &o, const f3 &d,
 		float tmax, kgr_hit &best, STACK &stack, TraceCounters *cnt = nullptr)
@@ -417,17 +472,12 @@ __device__ __forceinline__ bool trace_fast_stack(const DeviceScene &s, const f3 
 	stack.clear();
 	int32_t ref = 0;
 	for (;;) {
-		while (ref >= 0) {
-			if (COUNT)
-				cnt->nodes++;
-			if (!node_step<LAYOUT>(s, r, ref, best.t, stack))
-				return best.prim >= 0;
-		}
-		if (fast_leaf<ANY, COUNT>(s, r, ref, best, best_rank, cnt))
+		int32_t leaf = 0;
+		speculative_descend<LAYOUT, COUNT>(s, r, ref, leaf, best.t, stack, cnt);
+		if (test_leaves<ANY, COUNT>(s, r, ref, leaf, best, best_rank, stack, cnt))
 			return true;
-		if (stack.empty())
+		if (ref == KGR_REF_NONE)
 			return best.prim >= 0;
-		ref = stack.pop();
 	}
 }
 

@@ -301,22 +301,12 @@ __global__ void __launch_bounds__(BLOCK, KGR_MIN_BLOCKS(BLOCK, OCC)) fast_persis
 			break;
 		if (!have)
 			continue;
-		bool done = false, occ = false;
-		while (ref >= 0) {
-			if (COUNT)
-				cnt.nodes++;
-			if (!node_step<LAYOUT>(s, r, ref, best.t, stack)) {
-				done = true;
-				break;
-			}
-		}
-		if (!done) {
-			occ = fast_leaf<ANY, COUNT>(s, r, ref, best, best_rank, &cnt);
-			if (occ || stack.empty())
-				done = true;
-			else
-				ref = stack.pop();
-		}
+		/* descend with the postponed-leaf rule (speculative_descend), then
+		 * test the leaves the descent collected */
+		int32_t leaf = 0;
+		speculative_descend<LAYOUT, COUNT>(s, r, ref, leaf, best.t, stack, &cnt);
+		bool occ = test_leaves<ANY, COUNT>(s, r, ref, leaf, best, best_rank, stack, &cnt);
+		bool done = occ || ref == KGR_REF_NONE;
 		if (done) {
 			if (ANY)
 				resolve_shadow(pb, p, occ);

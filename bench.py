@@ -53,10 +53,10 @@ KERNELS = {("trace_closest", "fast"): "fast_persistent_kernel<closest, fast>",
 # bytes a visit reads on each layout: (node, triangle)
 LAYOUT_BYTES = {"fast": (64, 48), "wide": (128, 48), "threaded": (48, 80)}
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
-# traversal kernels at this workload: one ncu capture of the 9 closest-hit
-# launches of a timed 1080p frame (--cache-control none), averaged per
-# launch; None where not captured.
-TRAFFIC = {("trace_closest", "fast"): 168.1e6}
+# traversal kernels at this workload: one ncu capture of the 9 closest-hit and
+# 9 shadow launches of a timed 1080p frame (--cache-control none), averaged
+# per launch; None where not captured.
+TRAFFIC = {("trace_closest", "fast"): 173.3e6, ("shadow", "fast"): 279.0e6}
 
 
 def parse(argv=None):
@@ -72,6 +72,10 @@ def parse(argv=None):
     ap.add_argument("--scene", default="terrain")
     ap.add_argument("--layout", default="auto", choices=["auto", "fast", "wide", "threaded"],
                     help="auto: the autotuner picks layout, shadow kernel and block size before warm-up")
+    ap.add_argument("--trace-shadow", choices=["grid", "persistent"], help="shadow kernel (with --layout)")
+    ap.add_argument("--trace-block", type=int, choices=[64, 128, 256], help="traversal block size (with --layout)")
+    ap.add_argument("--trace-occupancy", type=int, choices=[0, 1], help="register cap (with --layout)")
+    ap.add_argument("--trace-stack", type=int, choices=[0, 8, 16], help="shared-memory stack entries (with --layout)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU sample time per measurement")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-quality", action="store_true",
@@ -653,6 +657,10 @@ def bench_ours(args):
         layout = tuned["best"]["layout"]
     else:
         layout = args.layout
+        for opt, v in (("trace_shadow", args.trace_shadow), ("trace_block", args.trace_block),
+                       ("trace_occupancy", args.trace_occupancy), ("trace_stack", args.trace_stack)):
+            if v is not None:
+                att.set_option(opt, v)
     att.set_option("layout", layout)
     t = att.trace_tune()
     # the comparison runs and the cached tracer use the same launch shape

@@ -766,6 +766,9 @@ struct kgr_attachment {
 	 * frame's inference -> Adam -> join */
 	cudaStream_t side = nullptr;
 	cudaEvent_t ev_fork = nullptr, ev_infer = nullptr, ev_train = nullptr;
+	/* the plain tracer's overlap of a bounce's shadow rays with the next
+	 * bounce's closest hits (render_pt) */
+	cudaEvent_t ev_shaded = nullptr, ev_shadowed = nullptr;
 
 	kgr_render_stats stats = {0, 0, 0, 0, 0};
 	uint32_t last_paths = 0;
@@ -974,6 +977,8 @@ struct kgr_attachment {
 		KGR_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
 		KGR_CUDA(cudaEventCreateWithFlags(&ev_infer, cudaEventDisableTiming));
 		KGR_CUDA(cudaEventCreateWithFlags(&ev_train, cudaEventDisableTiming));
+		KGR_CUDA(cudaEventCreateWithFlags(&ev_shaded, cudaEventDisableTiming));
+		KGR_CUDA(cudaEventCreateWithFlags(&ev_shadowed, cudaEventDisableTiming));
 	}
 
 	~kgr_attachment()
@@ -981,7 +986,7 @@ struct kgr_attachment {
 		release_all();
 		if (cache_mlp)
 			kgr_mlp_destroy(cache_mlp);
-		for (cudaEvent_t e : {ev_fork, ev_infer, ev_train})
+		for (cudaEvent_t e : {ev_fork, ev_infer, ev_train, ev_shaded, ev_shadowed})
 			if (e)
 				cudaEventDestroy(e);
 		if (side)
@@ -1092,23 +1097,58 @@ void render_pt(kgr_attachment *att, const kgr_launch_info *info, const kgr_scene
 		reinterpret_cast<float4 *>(info->buffers.position)};
 	uint32_t launches = 0;
 	prepare_visits(att, st);
-	att->mark(-1, st);
+	int m = att->mark(-1, st);
 	pt_generate(pb, fp, st);
-	att->mark(STAGE_GENERATE, st);
+	m = att->mark(STAGE_GENERATE, st, m);
 	launches++;
-	for (int d = 0; d <= fp.max_depth; d++) {
-		int q = d & 1;
-		if (d > 0) {
-			reset_counters(pb, (1 << (q ^ 1)) | (1 << CNT_SHADOW), st);
-			att->mark(-1, st);
+	if (att->opt_int("trace_overlap", 1)) {
+		/* bounce d's shadow rays on the side stream while bounce d + 1's
+		 * closest hits run here: the two persistent launches share the GPU,
+		 * and each fills the SMs the other's tail leaves idle.  They touch
+		 * disjoint arrays and counters; the next shade waits for both, so
+		 * every path's radiance is still summed in the order of the
+		 * recursion. */
+		att->ensure_side_stream();
+		cudaStream_t side = att->side;
+		pt_trace_closest(s, pb, 0, fp.layout, fp.tune, st);
+		m = att->mark(STAGE_TRACE_CLOSEST, st, m);
+		for (int d = 0; d <= fp.max_depth; d++) {
+			int q = d & 1;
+			if (d > 0) {
+				reset_counters(pb, (1 << (q ^ 1)) | (1 << CNT_SHADOW), st);
+				m = att->mark(-1, st);
+			}
+			pt_shade(s, pb, fp, d, q, st);
+			m = att->mark(STAGE_SHADE, st, m);
+			KGR_CUDA(cudaEventRecord(att->ev_shaded, st));
+			KGR_CUDA(cudaStreamWaitEvent(side, att->ev_shaded, 0));
+			int ms = att->mark(-1, side);
+			pt_shadow_resolve(s, pb, fp.layout, fp.tune, side);
+			att->mark(STAGE_SHADOW, side, ms);
+			KGR_CUDA(cudaEventRecord(att->ev_shadowed, side));
+			if (d < fp.max_depth) {
+				pt_trace_closest(s, pb, q ^ 1, fp.layout, fp.tune, st);
+				m = att->mark(STAGE_TRACE_CLOSEST, st, m);
+			}
+			KGR_CUDA(cudaStreamWaitEvent(st, att->ev_shadowed, 0));
+			m = att->mark(-1, st);
+			launches += 3;
 		}
-		pt_trace_closest(s, pb, q, fp.layout, fp.tune, st);
-		att->mark(STAGE_TRACE_CLOSEST, st);
-		pt_shade(s, pb, fp, d, q, st);
-		att->mark(STAGE_SHADE, st);
-		pt_shadow_resolve(s, pb, fp.layout, fp.tune, st);
-		att->mark(STAGE_SHADOW, st);
-		launches += 3;
+	} else {
+		for (int d = 0; d <= fp.max_depth; d++) {
+			int q = d & 1;
+			if (d > 0) {
+				reset_counters(pb, (1 << (q ^ 1)) | (1 << CNT_SHADOW), st);
+				m = att->mark(-1, st);
+			}
+			pt_trace_closest(s, pb, q, fp.layout, fp.tune, st);
+			m = att->mark(STAGE_TRACE_CLOSEST, st, m);
+			pt_shade(s, pb, fp, d, q, st);
+			m = att->mark(STAGE_SHADE, st, m);
+			pt_shadow_resolve(s, pb, fp.layout, fp.tune, st);
+			m = att->mark(STAGE_SHADOW, st, m);
+			launches += 3;
+		}
 	}
 	pt_accumulate(pb, fp, out, st);
 	att->mark(STAGE_ACCUMULATE, st);
@@ -1565,7 +1605,8 @@ static const std::map<std::string, OptionValue> &option_defaults()
 		{"gi_radius", 30},
 		{"cache", false}, {"cache_train", true}, {"cache_train_paths", 16384}, {"cache_lr", 1e-3f},
 		{"cache_dtype", std::string("bf16")}, {"cache_infer", std::string("tcgen05")}, {"reset_history", false},
-		{"trace_shadow", std::string("")}, {"trace_block", 0}, {"trace_occupancy", -1}, {"trace_stack", -1}};
+		{"trace_shadow", std::string("")}, {"trace_block", 0}, {"trace_occupancy", -1}, {"trace_stack", -1},
+		{"trace_overlap", true}};
 	return d;
 }
 

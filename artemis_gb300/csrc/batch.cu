@@ -99,16 +99,36 @@ void batch_accumulate(const PathBuffers &pb, const BatchHeader *hdr, const Batch
 }
 
 void batch_frame(const DeviceScene &s, const PathBuffers &pb, const FrameParams &fp, const BatchHeader *hdr,
-		const BatchJob *jobs, cudaStream_t st)
+		const BatchJob *jobs, cudaStream_t st, const StreamPair &side)
 {
 	batch_generate(pb, hdr, jobs, st);
-	for (int d = 0; d <= fp.max_depth; d++) {
-		int q = d & 1;
-		if (d > 0)
-			reset_counters(pb, (1 << (q ^ 1)) | (1 << CNT_SHADOW), st);
-		pt_trace_closest(s, pb, q, fp.layout, fp.tune, st);
-		pt_shade(s, pb, fp, d, q, st);
-		pt_shadow_resolve(s, pb, fp.layout, fp.tune, st);
+	if (side.stream) {
+		/* the plain tracer's overlap (render_pt): bounce d's shadow rays on
+		 * the side stream, bounce d + 1's closest hits here, joined before
+		 * the next shade */
+		pt_trace_closest(s, pb, 0, fp.layout, fp.tune, st);
+		for (int d = 0; d <= fp.max_depth; d++) {
+			int q = d & 1;
+			if (d > 0)
+				reset_counters(pb, (1 << (q ^ 1)) | (1 << CNT_SHADOW), st);
+			pt_shade(s, pb, fp, d, q, st);
+			KGR_CUDA(cudaEventRecord(side.shaded, st));
+			KGR_CUDA(cudaStreamWaitEvent(side.stream, side.shaded, 0));
+			pt_shadow_resolve(s, pb, fp.layout, fp.tune, side.stream);
+			KGR_CUDA(cudaEventRecord(side.shadowed, side.stream));
+			if (d < fp.max_depth)
+				pt_trace_closest(s, pb, q ^ 1, fp.layout, fp.tune, st);
+			KGR_CUDA(cudaStreamWaitEvent(st, side.shadowed, 0));
+		}
+	} else {
+		for (int d = 0; d <= fp.max_depth; d++) {
+			int q = d & 1;
+			if (d > 0)
+				reset_counters(pb, (1 << (q ^ 1)) | (1 << CNT_SHADOW), st);
+			pt_trace_closest(s, pb, q, fp.layout, fp.tune, st);
+			pt_shade(s, pb, fp, d, q, st);
+			pt_shadow_resolve(s, pb, fp.layout, fp.tune, st);
+		}
 	}
 	batch_accumulate(pb, hdr, jobs, st);
 }

@@ -136,7 +136,7 @@ void kgr_batcher::render(const kgr_scene *scene, const kgr_batch_job *jobs, uint
 		cudaGraph_t graph = nullptr;
 		KGR_CUDA(cudaStreamBeginCapture(capture_stream, cudaStreamCaptureModeThreadLocal));
 		try {
-			batch_frame(s, pb, fp, dh, djobs, capture_stream);
+			batch_frame(s, pb, fp, dh, djobs, capture_stream, side);
 		} catch (...) {
 			cudaStreamEndCapture(capture_stream, &graph);
 			if (graph)
@@ -153,7 +153,7 @@ void kgr_batcher::render(const kgr_scene *scene, const kgr_batch_job *jobs, uint
 		last_graph = 1;
 		graph_replays++;
 	} else {
-		batch_frame(s, pb, fp, dh, djobs, st);
+		batch_frame(s, pb, fp, dh, djobs, st, side);
 		if (g)
 			g->eager_runs++;
 	}
@@ -189,6 +189,13 @@ kgr_batcher::~kgr_batcher()
 			cudaGraphExecDestroy(g.exec);
 	if (capture_stream)
 		cudaStreamDestroy(capture_stream);
+	if (side.stream) {
+		cudaStreamSynchronize(side.stream);
+		cudaStreamDestroy(side.stream);
+	}
+	for (cudaEvent_t e : {side.shaded, side.shadowed})
+		if (e)
+			cudaEventDestroy(e);
 }
 
 extern "C" {
@@ -221,6 +228,9 @@ kgr_status kgr_batcher_create(int32_t device, uint32_t path_capacity, uint32_t m
 			KGR_CUDA(cudaEventCreateWithFlags(&b->done[r], cudaEventDisableTiming));
 		}
 		KGR_CUDA(cudaStreamCreateWithFlags(&b->capture_stream, cudaStreamNonBlocking));
+		KGR_CUDA(cudaStreamCreateWithFlags(&b->side.stream, cudaStreamNonBlocking));
+		KGR_CUDA(cudaEventCreateWithFlags(&b->side.shaded, cudaEventDisableTiming));
+		KGR_CUDA(cudaEventCreateWithFlags(&b->side.shadowed, cudaEventDisableTiming));
 		*out = b.release();
 	});
 }

@@ -36,10 +36,19 @@ inline size_t batch_table_bytes(uint32_t max_jobs) { return 16 + (size_t)max_job
 void batch_generate(const PathBuffers &pb, const BatchHeader *hdr, const BatchJob *jobs, cudaStream_t st);
 void batch_accumulate(const PathBuffers &pb, const BatchHeader *hdr, const BatchJob *jobs, cudaStream_t st);
 
+/* A second stream and two events: with them, batch_frame runs a bounce's
+ * shadow rays on `stream` while the next bounce's closest hits run on the
+ * frame's stream (forked and joined by events, so a captured frame keeps
+ * the fork in its graph).  stream = nullptr: everything in order. */
+struct StreamPair {
+	cudaStream_t stream;
+	cudaEvent_t shaded, shadowed;
+};
+
 /* One frame of every job in the table: generate, depth loop, accumulate.
  * fp supplies max_depth, Russian roulette and the layout. */
 void batch_frame(const DeviceScene &s, const PathBuffers &pb, const FrameParams &fp, const BatchHeader *hdr,
-		const BatchJob *jobs, cudaStream_t st);
+		const BatchJob *jobs, cudaStream_t st, const StreamPair &side);
 
 } /* namespace kgr */
 
@@ -59,6 +68,7 @@ struct kgr_batcher {
 	cudaEvent_t done[RING] = {};
 	int ring = 0, last = -1;
 	cudaStream_t capture_stream = nullptr;
+	kgr::StreamPair side = {nullptr, nullptr, nullptr};
 	/* launch shape of the traversal stages (kgr_batcher_set_tune) */
 	kgr::TraceTune tune = kgr::default_trace_tune();
 	struct Graph {

@@ -769,6 +769,8 @@ struct kgr_attachment {
 	/* the plain tracer's overlap of a bounce's shadow rays with the next
 	 * bounce's closest hits (render_pt) */
 	cudaEvent_t ev_shaded = nullptr, ev_shadowed = nullptr;
+	/* the cached frame's shadow rays, beside the side stream's training */
+	cudaStream_t side2 = nullptr;
 
 	kgr_render_stats stats = {0, 0, 0, 0, 0};
 	uint32_t last_paths = 0;
@@ -915,6 +917,8 @@ struct kgr_attachment {
 	{
 		if (side)
 			cudaStreamSynchronize(side);
+		if (side2)
+			cudaStreamSynchronize(side2);
 		for (auto &b : f4)
 			b.release();
 		for (auto &q : queues)
@@ -979,6 +983,7 @@ struct kgr_attachment {
 		KGR_CUDA(cudaEventCreateWithFlags(&ev_train, cudaEventDisableTiming));
 		KGR_CUDA(cudaEventCreateWithFlags(&ev_shaded, cudaEventDisableTiming));
 		KGR_CUDA(cudaEventCreateWithFlags(&ev_shadowed, cudaEventDisableTiming));
+		KGR_CUDA(cudaStreamCreateWithFlags(&side2, cudaStreamNonBlocking));
 	}
 
 	~kgr_attachment()
@@ -991,6 +996,8 @@ struct kgr_attachment {
 				cudaEventDestroy(e);
 		if (side)
 			cudaStreamDestroy(side);
+		if (side2)
+			cudaStreamDestroy(side2);
 		visits.release();
 		if (ev_start)
 			cudaEventDestroy(ev_start);
@@ -1328,28 +1335,45 @@ void render_pt_cached(kgr_attachment *att, const kgr_launch_info *info, const kg
 		launches += 4;
 	}
 
-	/* render: primary vertex, first bounce, cache */
-	att->mark(-1, st);
+	/* render: primary vertex, first bounce, cache.  The primary vertex's
+	 * shadow rays run on a second side stream while the first bounce is
+	 * traced and queried (the overlap of render_pt); they join before the
+	 * cache's radiance is added, so each path's radiance is summed in the
+	 * order of the recursion. */
+	const bool overlap = att->opt_int("trace_overlap", 1) != 0;
+	if (overlap)
+		att->ensure_side_stream();
+	int m = att->mark(-1, st);
 	pt_generate(pb, fp, st);
-	att->mark(STAGE_GENERATE, st);
+	m = att->mark(STAGE_GENERATE, st, m);
 	pt_trace_closest(s, pb, 0, fp.layout, fp.tune, st);
-	att->mark(STAGE_TRACE_CLOSEST, st);
+	m = att->mark(STAGE_TRACE_CLOSEST, st, m);
 	pt_shade(s, pb, fp, 0, 0, st);
-	att->mark(STAGE_SHADE, st);
-	pt_shadow_resolve(s, pb, fp.layout, fp.tune, st);
-	att->mark(STAGE_SHADOW, st);
-	reset_counters(pb, (1 << CNT_Q0) | (1 << CNT_SHADOW), st);
-	att->mark(-1, st);
+	m = att->mark(STAGE_SHADE, st, m);
+	if (overlap) {
+		KGR_CUDA(cudaEventRecord(att->ev_shaded, st));
+		KGR_CUDA(cudaStreamWaitEvent(att->side2, att->ev_shaded, 0));
+		int ms = att->mark(-1, att->side2);
+		pt_shadow_resolve(s, pb, fp.layout, fp.tune, att->side2);
+		att->mark(STAGE_SHADOW, att->side2, ms);
+		KGR_CUDA(cudaEventRecord(att->ev_shadowed, att->side2));
+	} else {
+		pt_shadow_resolve(s, pb, fp.layout, fp.tune, st);
+		m = att->mark(STAGE_SHADOW, st, m);
+	}
 	pt_trace_closest(s, pb, 1, fp.layout, fp.tune, st);
-	att->mark(STAGE_TRACE_CLOSEST, st);
+	m = att->mark(STAGE_TRACE_CLOSEST, st, m);
 	cache_query(s, pb, 1, cp, att->q_feat.ptr, att->q_le.ptr, st);
 	mlp_infer(mp, att->q_feat.ptr, att->capacity, att->q_out.ptr, st, pb.counters + CNT_Q1);
 	if (train)
 		KGR_CUDA(cudaEventRecord(att->ev_infer, st));
+	if (overlap)
+		KGR_CUDA(cudaStreamWaitEvent(st, att->ev_shadowed, 0));
+	reset_counters(pb, (1 << CNT_Q0) | (1 << CNT_SHADOW), st);
 	cache_apply(pb, 1, att->q_out.ptr, att->q_le.ptr, st);
-	att->mark(STAGE_CACHE_INFER, st);
+	m = att->mark(STAGE_CACHE_INFER, st, m);
 	pt_accumulate(pb, fp, out, st);
-	att->mark(STAGE_ACCUMULATE, st);
+	att->mark(STAGE_ACCUMULATE, st, m);
 	launches += 10;
 
 	/* Adam once this frame's inference is done, then join */

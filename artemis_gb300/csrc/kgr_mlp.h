@@ -36,9 +36,11 @@ void mlp_infer_tc(const MlpParams &mp, const void *x, uint32_t n, float4 *out, u
 		const uint32_t *n_dev = nullptr, bool withhold_first = false);
 /* grad (FP32, [6][64][64]) = d loss / d W over n rows; loss = sum of the
  * relative L2 terms (not divided by n).  Uses mp.partial as scratch; the
- * result does not depend on block scheduling. */
+ * result does not depend on block scheduling.  max_blocks > 0 caps the grid
+ * (each block takes one SM's shared memory): training that runs beside a
+ * frame leaves the other SMs to the frame. */
 void mlp_gradients(const MlpParams &mp, const void *x, const float4 *target, uint32_t n, float *grad, float *loss,
-		cudaStream_t st, const uint32_t *n_dev = nullptr);
+		cudaStream_t st, const uint32_t *n_dev = nullptr, int max_blocks = 0);
 /* One Adam step (lr, bias correction for `step`); step <= 0 only refreshes
  * the half-precision copies from the master weights. */
 void mlp_adam(const MlpParams &mp, const float *grad, float lr, int step, cudaStream_t st);

@@ -553,7 +553,7 @@ void mlp_infer(const MlpParams &mp, const void *x, uint32_t n, float4 *out, cuda
 }
 
 void mlp_gradients(const MlpParams &mp, const void *x, const float4 *target, uint32_t n, float *grad, float *loss,
-		cudaStream_t st, const uint32_t *n_dev)
+		cudaStream_t st, const uint32_t *n_dev, int max_blocks)
 {
 	KGR_CUDA(cudaMemsetAsync(loss, 0, sizeof(float), st));
 	if (n == 0) {
@@ -562,6 +562,8 @@ void mlp_gradients(const MlpParams &mp, const void *x, const float4 *target, uin
 	}
 	size_t sm = train_smem();
 	int grid = mp.partial_blocks;
+	if (max_blocks > 0 && max_blocks < grid)
+		grid = max_blocks;
 	long long tiles = ((long long)n + TRAIN_ROWS - 1) / TRAIN_ROWS;
 	if (tiles < grid)
 		grid = (int)tiles;

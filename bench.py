@@ -76,6 +76,8 @@ def parse(argv=None):
     ap.add_argument("--trace-block", type=int, choices=[64, 128, 256], help="traversal block size (with --layout)")
     ap.add_argument("--trace-occupancy", type=int, choices=[0, 1], help="register cap (with --layout)")
     ap.add_argument("--trace-stack", type=int, choices=[0, 8, 16], help="shared-memory stack entries (with --layout)")
+    ap.add_argument("--trace-overlap", type=int, choices=[0, 1], default=1,
+                    help="1: a bounce's shadow rays overlap the next bounce's closest hits (two streams)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU sample time per measurement")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-quality", action="store_true",
@@ -662,10 +664,12 @@ def bench_ours(args):
             if v is not None:
                 att.set_option(opt, v)
     att.set_option("layout", layout)
+    att.set_option("trace_overlap", bool(args.trace_overlap))
     t = att.trace_tune()
     # the comparison runs and the cached tracer use the same launch shape
     args.trace_options = {"layout": layout, "trace_shadow": t["shadow"], "trace_block": t["block"],
-                          "trace_occupancy": t["occupancy"], "trace_stack": t["stack"]}
+                          "trace_occupancy": t["occupancy"], "trace_stack": t["stack"],
+                          "trace_overlap": bool(args.trace_overlap)}
     for s in range(args.warmup):
         att.render(info_for(s), sc, sptr)
     torch.cuda.synchronize()

@@ -251,3 +251,38 @@ def test_refit_time_terrain():
     for a, b in zip(before, [sc.array(a) for a in ARRAYS]):
         assert np.array_equal(a, b)
     sc.close()
+
+
+def test_refit_of_a_one_triangle_scene():
+    """The root is a leaf: the fast layout's single node keeps its empty right
+    slot, there is no wide layout, and the threaded buffer is one record."""
+    mats = np.zeros((1, 16), np.float32)
+    mats[0, 0:3] = 0.5
+    mats[0, 15:16].view(np.int32)[0] = 4
+    tri = dict(positions=np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32),
+               normals=np.array([[0, 0, 1]] * 3, np.float32), indices=np.array([[0, 1, 2]], np.uint32))
+    sc = kgr.Scene(None, None, mats, meshes=[dict(tri)])
+    assert sc.info().wide_node_count == 0 and sc.info().fast_node_count == 1
+    before = snapshot(sc)
+    sc.set_transforms([0], [translate((0.0, 0.0, 0.0))])
+    after = snapshot(sc)
+    # an identity model re-derives every vertex (x + 0 == x here) and box
+    for name, a, b in zip(("threaded", "fast", "wide", "tris"), before[:4], after[:4]):
+        assert np.array_equal(a, b), name
+    m = rot_y(30.0, 2.0, (0.5, -0.25, 1.0))
+    sc.set_transforms([0], [m])
+    pos, nrm, tris, _ = refit_ref.gather([dict(tri, model=m)], mats)
+    p, _ = sc.vertices()
+    assert np.array_equal(p.view(np.uint32), pos.view(np.uint32))
+    assert np.array_equal(sc.bvh().view(np.uint32), refit_ref.refit_threaded(before[0].view(np.float32).reshape(-1, 4),
+                                                                            pos, tris).view(np.uint32))
+    rays = np.zeros((3, 8), np.float32)
+    c = pos.mean(axis=0)
+    rays[:, 0:3] = c + np.array([[0, 0, 3], [0, 3, 0], [3, 0, 0]], np.float32)
+    rays[:, 4:7] = -np.array([[0, 0, 3], [0, 3, 0], [3, 0, 0]], np.float32) / 3.0
+    rays[:, 7] = np.inf
+    osc = pyoracle.Scene(pos, nrm, tris, mats, sc.lights(), sc.bvh())
+    ref, _ = osc.trace_closest(rays)
+    for layout in (kgr.LAYOUT_FAST, kgr.LAYOUT_THREADED):
+        assert np.array_equal(gpu_closest(sc, rays, layout).view(np.uint32), ref["raw"].view(np.uint32))
+    sc.close()

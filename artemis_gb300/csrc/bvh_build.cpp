@@ -637,11 +637,17 @@ void build_fast(const Tree &tree, const std::vector<PrimBox> &boxes, const float
 		FastNode fn;
 		memset(&fn, 0, sizeof(fn));
 		set_child(fn, 0, root.bmin, root.bmax, leaf_ref(root));
-		float inf = INFINITY;
-		fn.rxy = make_float4(inf, -inf, inf, -inf);
-		fn.lrz.z = inf;
-		fn.lrz.w = -inf;
-		fn.refs.y = 0;
+		/* The right slot is empty.  An inverted box (min +inf, max -inf)
+		 * would not do: fast_node's slab test takes the min and max of the
+		 * two plane distances, so an inverted box reads as all of space.
+		 * NaN planes make the far distance NaN, and `near <= far` is false
+		 * for every ray.  The slot names the same leaf, never the root, so
+		 * no walk can return to node 0. */
+		float nan = NAN;
+		fn.rxy = make_float4(nan, nan, nan, nan);
+		fn.lrz.z = nan;
+		fn.lrz.w = nan;
+		fn.refs.y = fn.refs.x;
 		nodes.push_back(fn);
 		if (kids)
 			kids->push_back(make_int2(0, -1));

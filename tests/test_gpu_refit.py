@@ -276,13 +276,22 @@ def test_refit_of_a_one_triangle_scene():
     assert np.array_equal(p.view(np.uint32), pos.view(np.uint32))
     assert np.array_equal(sc.bvh().view(np.uint32), refit_ref.refit_threaded(before[0].view(np.float32).reshape(-1, 4),
                                                                             pos, tris).view(np.uint32))
-    rays = np.zeros((3, 8), np.float32)
+    # toward the triangle from three sides, then away from it (misses)
+    toward = np.array([[0, 0, 3], [0, 3, 0], [3, 0, 0]], np.float32)
+    rays = np.zeros((6, 8), np.float32)
     c = pos.mean(axis=0)
-    rays[:, 0:3] = c + np.array([[0, 0, 3], [0, 3, 0], [3, 0, 0]], np.float32)
-    rays[:, 4:7] = -np.array([[0, 0, 3], [0, 3, 0], [3, 0, 0]], np.float32) / 3.0
+    rays[:, 0:3] = c + np.concatenate([toward, toward])
+    rays[:3, 4:7] = -toward / 3.0
+    rays[3:, 4:7] = toward / 3.0
     rays[:, 7] = np.inf
     osc = pyoracle.Scene(pos, nrm, tris, mats, sc.lights(), sc.bvh())
     ref, _ = osc.trace_closest(rays)
+    assert (ref["prim"][3:] < 0).all()
+    short = rays.copy()
+    short[:, 7] = 3.5
+    occ, _ = osc.trace_any(short)
+    assert occ[:3].any() and not occ[3:].any()
     for layout in (kgr.LAYOUT_FAST, kgr.LAYOUT_THREADED):
         assert np.array_equal(gpu_closest(sc, rays, layout).view(np.uint32), ref["raw"].view(np.uint32))
+        assert np.array_equal(gpu_any(sc, short, layout), occ)
     sc.close()

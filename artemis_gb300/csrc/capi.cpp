@@ -753,6 +753,8 @@ struct kgr_attachment {
 
 	/* ReSTIR GI state */
 	DevBuf<float4> gi_a[3], gi_b[3], g_pos, g_nrm, g_ppos, g_pnrm, g_direct, g_dir;
+	DevBuf<float4> gi_selection;
+	DevBuf<int2> gi_neighbours;
 	int gi_prev = 0;
 
 	/* radiance cache: network, query rows, training paths, records, batch */
@@ -937,6 +939,8 @@ struct kgr_attachment {
 		}
 		for (DevBuf<float4> *b : {&g_pos, &g_nrm, &g_ppos, &g_pnrm, &g_direct, &g_dir})
 			b->release();
+		gi_selection.release();
+		gi_neighbours.release();
 		for (DevBuf<uint16_t> *b : {&q_feat, &r_feat, &b_x})
 			b->release();
 		for (DevBuf<float4> *b : {&q_le, &q_out, &r_beta, &r_lb, &r_le, &b_t})
@@ -1407,7 +1411,8 @@ void render_restir_gi(kgr_attachment *att, const kgr_launch_info *info, const kg
 	fp.gi_mcap = att->opt_int("gi_mcap", 30);
 	fp.gi_neighbors = att->opt_int("gi_neighbors", 8);
 	fp.gi_radius = att->opt_int("gi_radius", 30);
-	KGR_REQUIRE(fp.gi_neighbors >= 0 && fp.gi_neighbors <= 16, KGR_ERR_INVALID_ARGUMENT, "gi_neighbors must be 0..16");
+	KGR_REQUIRE(fp.gi_neighbors >= 0 && fp.gi_neighbors <= KGR_GI_MAX_NEIGHBORS, KGR_ERR_INVALID_ARGUMENT,
+		"gi_neighbors must be 0..16");
 	KGR_REQUIRE(fp.candidates >= 1 && fp.candidates <= 1024, KGR_ERR_INVALID_ARGUMENT, "candidates must be 1..1024");
 	KGR_REQUIRE(fp.max_depth >= 1, KGR_ERR_INVALID_ARGUMENT, "ReSTIR GI needs max_depth >= 1");
 	if (!att->have_prev_camera) {
@@ -1437,6 +1442,8 @@ void render_restir_gi(kgr_attachment *att, const kgr_launch_info *info, const kg
 	gb.direct = att->g_direct.ptr;
 	gb.gi_dir = att->g_dir.ptr;
 	gb.auxiliary = att->auxiliary.ptr;
+	gb.selection = att->gi_selection.ptr;
+	gb.neighbours = att->gi_neighbours.ptr;
 	int prev = att->gi_prev, cur = (prev + 1) % 3, tmp = (prev + 2) % 3;
 	uint32_t launches = 0;
 
@@ -1579,6 +1586,8 @@ kgr_status kgr_load(kgr_attachment *att)
 				}
 				att->pixel_materials.alloc(npix);
 				KGR_CUDA(cudaMemset(att->pixel_materials.ptr, 0, npix * sizeof(kgr_material)));
+				att->gi_selection.alloc(npix);
+				att->gi_neighbours.alloc(npix * KGR_GI_MAX_NEIGHBORS);
 				att->gi_prev = 0;
 				att->ensure_paths((uint32_t)npix);
 			}

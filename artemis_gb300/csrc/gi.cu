@@ -457,9 +457,17 @@ __device__ __forceinline__ int gi_neighbor(const FrameParams &fp, int index, f3 
 	return x0 + y0 * width;
 }
 
-#define KGR_GI_MAX_NEIGHBORS 16
-
-__global__ void __launch_bounds__(128) gi_spatial_kernel(DeviceScene s, FrameParams fp, GiFrameBuffers gb,
+/* Spatial reuse in two launches, the halves of one resampling step: the
+ * first resamples, the second weights.  Splitting it keeps each kernel's
+ * live state (and registers) small while its visibility rays are walked;
+ * the state in between is the selection {w_sum, domain, M sum} and each
+ * neighbour's {pixel, M} (GiFrameBuffers::selection, ::neighbours).  The
+ * arithmetic and its order are those of one pass over both loops.
+ *
+ * First half: the centre reservoir and up to fp.gi_neighbors neighbours
+ * that pass the geometric test are resampled with w_i = p^_q(y_i) |J_i|
+ * W_i M_i, each candidate with a positive weight behind a visibility ray. */
+__global__ void __launch_bounds__(128) gi_spatial_select_kernel(DeviceScene s, FrameParams fp, GiFrameBuffers gb,
 		int in, int out, int iteration)
 {
 	uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
@@ -476,21 +484,18 @@ __global__ void __launch_bounds__(128) gi_spatial_kernel(DeviceScene s, FramePar
 	GiMerge r;
 	r.init(pixel_seed(pix, fp.frame, KGR_GI_REUSE_SALT + 1u + (uint32_t)iteration));
 	r.update(C.s, gi_target(h, C.s) * C.W * C.M, -1);
-	int32_t nidx[KGR_GI_MAX_NEIGHBORS];
-	int32_t nM[KGR_GI_MAX_NEIGHBORS];
 	int32_t Msum = C.M;
 	for (int k = 0; k < fp.gi_neighbors; k++) {
 		int index0 = gi_neighbor(fp, (int)pix, r.seed);
-		nidx[k] = -1;
-		nM[k] = 0;
+		int2 *slot = gb.neighbours + (size_t)k * fp.npix + pix;
+		*slot = make_int2(-1, 0);
 		GBuf gn = gbuf(gb.position, gb.normal, (uint32_t)index0);
 		if (!similar(g, depth, gn, length(gn.x - v3(fp.center))))
 			continue;
 		GiRes N = load_gi(gb.res[in], (uint32_t)index0);
 		if (N.M <= 0)
 			continue;
-		nidx[k] = index0;
-		nM[k] = N.M;
+		*slot = make_int2(index0, N.M);
 		Msum += N.M;
 		float J = N.s.rc ? gi_jacobian(g.x, gn.x, N.s) : 0.0f;
 		float wn = J > 0.0f ? gi_target(h, N.s) * J * N.W * N.M : 0.0f;
@@ -498,27 +503,58 @@ __global__ void __launch_bounds__(128) gi_spatial_kernel(DeviceScene s, FramePar
 			wn = 0.0f;
 		r.update(N.s, wn, k);
 	}
-	/* balance heuristic over the centre and every neighbour domain: the
-	 * selected sample shifted back to each receiver, with its visibility */
-	float target = gi_target(h, r.sel);
-	float D = (float)C.M * target;
-	float num = r.src < 0 ? target : 0.0f;
-	if (target > 0.0f && r.sel.rc) {
+	/* domain of the selection: -1 the centre, k a neighbour, -2 nothing
+	 * selected (every weight zero: the empty sample of GiMerge::init) */
+	int32_t domain = r.sel.valid ? r.src : -2;
+	gb.selection[pix] = make_float4(r.w, __int_as_float(domain), __int_as_float(Msum), 0.0f);
+}
+
+/* Second half: the balance heuristic over the centre and every neighbour
+ * domain -- the selected sample shifted back to each receiver, with its
+ * visibility -- and the reservoir {y, W, M sum}. */
+__global__ void __launch_bounds__(128) gi_spatial_weight_kernel(DeviceScene s, FrameParams fp, GiFrameBuffers gb,
+		int in, int out)
+{
+	uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+	if (pix >= fp.npix)
+		return;
+	GBuf g = gbuf(gb.position, gb.normal, pix);
+	if (!g.hit)
+		return; /* the first half stored the centre reservoir */
+	SurfaceHit h = receiver(fp, gb, pix, g);
+	float4 st = gb.selection[pix];
+	float w_sum = st.x;
+	int32_t domain = __float_as_int(st.y), Msum = __float_as_int(st.z);
+	GiSample sel;
+	if (domain == -2) {
+		sel.xs = sel.ns = sel.Lo = mk(0.0f);
+		sel.valid = false;
+		sel.rc = true;
+	} else {
+		uint32_t from = domain < 0 ? pix : (uint32_t)gb.neighbours[(size_t)domain * fp.npix + pix].x;
+		sel = load_gi(gb.res[in], from).s;
+	}
+	int32_t CM = unpack_m(__float_as_uint(gb.res[in].a[pix].w));
+	float target = gi_target(h, sel);
+	float D = (float)CM * target;
+	float num = domain < 0 ? target : 0.0f;
+	if (target > 0.0f && sel.rc) {
 		for (int k = 0; k < fp.gi_neighbors; k++) {
-			if (nidx[k] < 0)
+			int2 nb = gb.neighbours[(size_t)k * fp.npix + pix];
+			if (nb.x < 0)
 				continue;
-			GBuf gn = gbuf(gb.position, gb.normal, (uint32_t)nidx[k]);
-			float jn = gi_jacobian(gn.x, g.x, r.sel);
-			float tn = jn > 0.0f ? gi_target(receiver(fp, gb, (uint32_t)nidx[k], gn), r.sel) * jn : 0.0f;
-			if (tn > 0.0f && !visible(s, fp.layout, gn.x, r.sel.xs))
+			GBuf gn = gbuf(gb.position, gb.normal, (uint32_t)nb.x);
+			float jn = gi_jacobian(gn.x, g.x, sel);
+			float tn = jn > 0.0f ? gi_target(receiver(fp, gb, (uint32_t)nb.x, gn), sel) * jn : 0.0f;
+			if (tn > 0.0f && !visible(s, fp.layout, gn.x, sel.xs))
 				tn = 0.0f;
-			D += (float)nM[k] * tn;
-			if (k == r.src)
+			D += (float)nb.y * tn;
+			if (k == domain)
 				num = tn;
 		}
 	}
-	float W = gi_mis_weight(r.w, num, D, target);
-	store_gi(gb.res[out], pix, r.sel, W, Msum);
+	float W = gi_mis_weight(w_sum, num, D, target);
+	store_gi(gb.res[out], pix, sel, W, Msum);
 }
 
 __device__ __forceinline__ void accumulate4(float4 *buf, uint32_t i, float4 v, bool acc, float count)
@@ -599,7 +635,9 @@ void gi_temporal(const DeviceScene &s, const FrameParams &fp, const GiFrameBuffe
 void gi_spatial(const DeviceScene &s, const FrameParams &fp, const GiFrameBuffers &gb, int in, int out,
 		int iteration, cudaStream_t st)
 {
-	gi_spatial_kernel<<<(fp.npix + 127) / 128, 128, 0, st>>>(s, fp, gb, in, out, iteration);
+	gi_spatial_select_kernel<<<(fp.npix + 127) / 128, 128, 0, st>>>(s, fp, gb, in, out, iteration);
+	KGR_CUDA(cudaGetLastError());
+	gi_spatial_weight_kernel<<<(fp.npix + 127) / 128, 128, 0, st>>>(s, fp, gb, in, out);
 	KGR_CUDA(cudaGetLastError());
 }
 

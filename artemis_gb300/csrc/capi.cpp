@@ -755,6 +755,8 @@ struct kgr_attachment {
 	DevBuf<float4> gi_a[3], gi_b[3], g_pos, g_nrm, g_ppos, g_pnrm, g_direct, g_dir;
 	DevBuf<float4> gi_selection;
 	DevBuf<int2> gi_neighbours;
+	DevBuf<float> gi_weights;
+	DevBuf<uint32_t> gi_vis_queue[2], gi_vis_count;
 	int gi_prev = 0;
 
 	/* radiance cache: network, query rows, training paths, records, batch */
@@ -941,6 +943,10 @@ struct kgr_attachment {
 			b->release();
 		gi_selection.release();
 		gi_neighbours.release();
+		gi_weights.release();
+		gi_vis_queue[0].release();
+		gi_vis_queue[1].release();
+		gi_vis_count.release();
 		for (DevBuf<uint16_t> *b : {&q_feat, &r_feat, &b_x})
 			b->release();
 		for (DevBuf<float4> *b : {&q_le, &q_out, &r_beta, &r_lb, &r_le, &b_t})
@@ -1444,6 +1450,10 @@ void render_restir_gi(kgr_attachment *att, const kgr_launch_info *info, const kg
 	gb.auxiliary = att->auxiliary.ptr;
 	gb.selection = att->gi_selection.ptr;
 	gb.neighbours = att->gi_neighbours.ptr;
+	gb.weights = att->gi_weights.ptr;
+	gb.vis_queue[0] = att->gi_vis_queue[0].ptr;
+	gb.vis_queue[1] = att->gi_vis_queue[1].ptr;
+	gb.vis_count = att->gi_vis_count.ptr;
 	int prev = att->gi_prev, cur = (prev + 1) % 3, tmp = (prev + 2) % 3;
 	uint32_t launches = 0;
 
@@ -1483,7 +1493,7 @@ void render_restir_gi(kgr_attachment *att, const kgr_launch_info *info, const kg
 		gi_spatial(s, fp, gb, in, outb, k, st);
 		att->mark(STAGE_RESTIR_SPATIAL, st);
 		std::swap(in, outb);
-		launches++;
+		launches += KGR_GI_SPATIAL_LAUNCHES;
 	}
 	gi_final(s, fp, gb, out, in, st);
 	att->mark(STAGE_ACCUMULATE, st);
@@ -1588,6 +1598,10 @@ kgr_status kgr_load(kgr_attachment *att)
 				KGR_CUDA(cudaMemset(att->pixel_materials.ptr, 0, npix * sizeof(kgr_material)));
 				att->gi_selection.alloc(npix);
 				att->gi_neighbours.alloc(npix * KGR_GI_MAX_NEIGHBORS);
+				att->gi_weights.alloc(npix * KGR_GI_MAX_NEIGHBORS);
+				att->gi_vis_queue[0].alloc(npix * KGR_GI_MAX_NEIGHBORS);
+				att->gi_vis_queue[1].alloc(npix * KGR_GI_MAX_NEIGHBORS);
+				att->gi_vis_count.alloc(2);
 				att->gi_prev = 0;
 				att->ensure_paths((uint32_t)npix);
 			}

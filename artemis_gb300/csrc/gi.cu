@@ -130,11 +130,16 @@ struct GiMerge {
 		src = -1;
 		seed = s;
 	}
-	__device__ __forceinline__ void update(const GiSample &s, float weight, int32_t from)
+	/* the update rule's draw: true when the candidate replaces the selection */
+	__device__ __forceinline__ bool take(float weight)
 	{
 		w += weight;
 		float eta = rand_uniform(seed);
-		if ((eta * w) < weight) {
+		return (eta * w) < weight;
+	}
+	__device__ __forceinline__ void update(const GiSample &s, float weight, int32_t from)
+	{
+		if (take(weight)) {
 			sel = s;
 			src = from;
 		}
@@ -457,18 +462,25 @@ __device__ __forceinline__ int gi_neighbor(const FrameParams &fp, int index, f3 
 	return x0 + y0 * width;
 }
 
-/* Spatial reuse in two launches, the halves of one resampling step: the
- * first resamples, the second weights.  Splitting it keeps each kernel's
- * live state (and registers) small while its visibility rays are walked;
- * the state in between is the selection {w_sum, domain, M sum} and each
- * neighbour's {pixel, M} (GiFrameBuffers::selection, ::neighbours).  The
- * arithmetic and its order are those of one pass over both loops.
+/* Spatial reuse as a wavefront of five launches per iteration.  The
+ * visibility rays of one resampling step -- one per weighted candidate, one
+ * per neighbour domain of the balance-heuristic denominator -- are queued
+ * and walked by their own kernel, one ray per thread, instead of inside the
+ * per-pixel loops, where a warp's lanes wait on each other's rays and the
+ * loops' live state costs occupancy.  The state between the launches is per
+ * neighbour slot (k-major, slot = k * npix + pixel): {pixel or -1, M} and a
+ * weight; per pixel: {w_sum, bits(domain), bits(M sum), target}.  Every
+ * value is computed by the same expressions in the same order as one pass
+ * over both loops would, and the random stream is replayed draw for draw,
+ * so the reservoirs are those of the single-pass formulation bit for bit.
  *
- * First half: the centre reservoir and up to fp.gi_neighbors neighbours
- * that pass the geometric test are resampled with w_i = p^_q(y_i) |J_i|
- * W_i M_i, each candidate with a positive weight behind a visibility ray. */
-__global__ void __launch_bounds__(128) gi_spatial_select_kernel(DeviceScene s, FrameParams fp, GiFrameBuffers gb,
-		int in, int out, int iteration)
+ * gather: the neighbours that pass the geometric test, their resampling
+ * weights w_i = p^_q(y_i) |J_i| W_i M_i, and a visibility ray queued for
+ * each positive weight.  The pixel's random stream advances as the
+ * resampling will draw it: one uniform for the centre, three for each
+ * neighbour's offset, one for each neighbour that is resampled. */
+__global__ void __launch_bounds__(128) gi_spatial_gather_kernel(FrameParams fp, GiFrameBuffers gb, int in, int out,
+		int iteration)
 {
 	uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
 	if (pix >= fp.npix)
@@ -481,49 +493,133 @@ __global__ void __launch_bounds__(128) gi_spatial_select_kernel(DeviceScene s, F
 	}
 	float depth = length(g.x - v3(fp.center));
 	SurfaceHit h = receiver(fp, gb, pix, g);
-	GiMerge r;
-	r.init(pixel_seed(pix, fp.frame, KGR_GI_REUSE_SALT + 1u + (uint32_t)iteration));
-	r.update(C.s, gi_target(h, C.s) * C.W * C.M, -1);
+	f3 seed = pixel_seed(pix, fp.frame, KGR_GI_REUSE_SALT + 1u + (uint32_t)iteration);
+	float wC = gi_target(h, C.s) * C.W * C.M;
+	rand_uniform(seed);
 	int32_t Msum = C.M;
 	for (int k = 0; k < fp.gi_neighbors; k++) {
-		int index0 = gi_neighbor(fp, (int)pix, r.seed);
-		int2 *slot = gb.neighbours + (size_t)k * fp.npix + pix;
-		*slot = make_int2(-1, 0);
+		int index0 = gi_neighbor(fp, (int)pix, seed);
+		uint32_t slot = (uint32_t)k * fp.npix + pix;
+		int2 nb = make_int2(-1, 0);
+		float wn = 0.0f;
 		GBuf gn = gbuf(gb.position, gb.normal, (uint32_t)index0);
-		if (!similar(g, depth, gn, length(gn.x - v3(fp.center))))
-			continue;
-		GiRes N = load_gi(gb.res[in], (uint32_t)index0);
-		if (N.M <= 0)
-			continue;
-		*slot = make_int2(index0, N.M);
-		Msum += N.M;
-		float J = N.s.rc ? gi_jacobian(g.x, gn.x, N.s) : 0.0f;
-		float wn = J > 0.0f ? gi_target(h, N.s) * J * N.W * N.M : 0.0f;
-		if (wn > 0.0f && !visible(s, fp.layout, g.x, N.s.xs))
-			wn = 0.0f;
-		r.update(N.s, wn, k);
+		if (similar(g, depth, gn, length(gn.x - v3(fp.center)))) {
+			GiRes N = load_gi(gb.res[in], (uint32_t)index0);
+			if (N.M > 0) {
+				nb = make_int2(index0, N.M);
+				Msum += N.M;
+				float J = N.s.rc ? gi_jacobian(g.x, gn.x, N.s) : 0.0f;
+				wn = J > 0.0f ? gi_target(h, N.s) * J * N.W * N.M : 0.0f;
+				rand_uniform(seed);
+			}
+		}
+		gb.neighbours[slot] = nb;
+		gb.weights[slot] = wn;
+		queue_append(gb.vis_queue[0], gb.vis_count + 0, slot, wn > 0.0f);
 	}
-	/* domain of the selection: -1 the centre, k a neighbour, -2 nothing
-	 * selected (every weight zero: the empty sample of GiMerge::init) */
-	int32_t domain = r.sel.valid ? r.src : -2;
-	gb.selection[pix] = make_float4(r.w, __int_as_float(domain), __int_as_float(Msum), 0.0f);
+	gb.selection[pix] = make_float4(wC, 0.0f, __int_as_float(Msum), 0.0f);
 }
 
-/* Second half: the balance heuristic over the centre and every neighbour
- * domain -- the selected sample shifted back to each receiver, with its
- * visibility -- and the reservoir {y, W, M sum}. */
-__global__ void __launch_bounds__(128) gi_spatial_weight_kernel(DeviceScene s, FrameParams fp, GiFrameBuffers gb,
-		int in, int out)
+/* The receiver of neighbour slot `slot`'s selected sample (second round):
+ * the sample the pixel selected, from the centre or a neighbour. */
+__device__ __forceinline__ uint32_t selected_from(const GiFrameBuffers &gb, uint32_t npix, uint32_t pix,
+		int32_t domain)
+{
+	return domain < 0 ? pix : (uint32_t)gb.neighbours[(size_t)domain * npix + pix].x;
+}
+
+/* visibility of queued slots; a blocked ray's weight becomes 0.  Round 0:
+ * from the pixel's receiver to the neighbour's sample.  Round 1: from the
+ * neighbour's receiver to the pixel's selected sample. */
+__global__ void __launch_bounds__(128) gi_visibility_kernel(DeviceScene s, FrameParams fp, GiFrameBuffers gb, int in,
+		int round)
+{
+	const uint32_t n = gb.vis_count[round];
+	const uint32_t *queue = gb.vis_queue[round];
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		uint32_t slot = queue[i];
+		uint32_t pix = slot % fp.npix;
+		uint32_t idx = (uint32_t)gb.neighbours[slot].x;
+		f3 from, to;
+		if (round == 0) {
+			from = f3_of(gb.position[pix]);
+			to = f3_of(gb.res[in].a[idx]);
+		} else {
+			int32_t domain = __float_as_int(gb.selection[pix].y);
+			from = f3_of(gb.position[idx]);
+			to = f3_of(gb.res[in].a[selected_from(gb, fp.npix, pix, domain)]);
+		}
+		if (!visible(s, fp.layout, from, to))
+			gb.weights[slot] = 0.0f;
+	}
+}
+
+/* resample: the weighted reservoir over the centre and the neighbours with
+ * their visibility-tested weights (GiMerge's rule, the same draws), then
+ * the selected sample shifted back to every neighbour receiver,
+ * p^_i(y) |J_q->i|, with a visibility ray queued for each positive one. */
+__global__ void __launch_bounds__(128) gi_spatial_resample_kernel(FrameParams fp, GiFrameBuffers gb, int in,
+		int iteration)
 {
 	uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
 	if (pix >= fp.npix)
 		return;
 	GBuf g = gbuf(gb.position, gb.normal, pix);
 	if (!g.hit)
-		return; /* the first half stored the centre reservoir */
-	SurfaceHit h = receiver(fp, gb, pix, g);
+		return;
 	float4 st = gb.selection[pix];
-	float w_sum = st.x;
+	GiMerge r;
+	r.init(pixel_seed(pix, fp.frame, KGR_GI_REUSE_SALT + 1u + (uint32_t)iteration));
+	bool chosen = r.take(st.x);
+	for (int k = 0; k < fp.gi_neighbors; k++) {
+		rand_uniform_3f(r.seed);
+		uint32_t slot = (uint32_t)k * fp.npix + pix;
+		if (gb.neighbours[slot].x < 0)
+			continue;
+		if (r.take(gb.weights[slot])) {
+			r.src = k;
+			chosen = true;
+		}
+	}
+	int32_t domain = chosen ? r.src : -2;
+	GiSample sel;
+	if (chosen) {
+		sel = load_gi(gb.res[in], selected_from(gb, fp.npix, pix, domain)).s;
+	} else {
+		sel.xs = sel.ns = sel.Lo = mk(0.0f);
+		sel.valid = false;
+		sel.rc = true;
+	}
+	SurfaceHit h = receiver(fp, gb, pix, g);
+	float target = gi_target(h, sel);
+	if (target > 0.0f && sel.rc) {
+		for (int k = 0; k < fp.gi_neighbors; k++) {
+			uint32_t slot = (uint32_t)k * fp.npix + pix;
+			int2 nb = gb.neighbours[slot];
+			if (nb.x < 0)
+				continue;
+			GBuf gn = gbuf(gb.position, gb.normal, (uint32_t)nb.x);
+			float jn = gi_jacobian(gn.x, g.x, sel);
+			float tn = jn > 0.0f ? gi_target(receiver(fp, gb, (uint32_t)nb.x, gn), sel) * jn : 0.0f;
+			gb.weights[slot] = tn;
+			queue_append(gb.vis_queue[1], gb.vis_count + 1, slot, tn > 0.0f);
+		}
+	}
+	gb.selection[pix] = make_float4(r.w, __int_as_float(domain), st.z, target);
+}
+
+/* finish: the balance-heuristic weight W = p^<-j(y) w_sum / (p^_q(y) D),
+ * D = sum_i M_i p^<-i(y) with each neighbour's visibility, and the
+ * reservoir {y, W, M sum}. */
+__global__ void __launch_bounds__(128) gi_spatial_finish_kernel(FrameParams fp, GiFrameBuffers gb, int in, int out)
+{
+	uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+	if (pix >= fp.npix)
+		return;
+	if (!(gb.position[pix].w > 0.0f))
+		return; /* gather stored the centre reservoir */
+	float4 st = gb.selection[pix];
+	float w_sum = st.x, target = st.w;
 	int32_t domain = __float_as_int(st.y), Msum = __float_as_int(st.z);
 	GiSample sel;
 	if (domain == -2) {
@@ -531,23 +627,18 @@ __global__ void __launch_bounds__(128) gi_spatial_weight_kernel(DeviceScene s, F
 		sel.valid = false;
 		sel.rc = true;
 	} else {
-		uint32_t from = domain < 0 ? pix : (uint32_t)gb.neighbours[(size_t)domain * fp.npix + pix].x;
-		sel = load_gi(gb.res[in], from).s;
+		sel = load_gi(gb.res[in], selected_from(gb, fp.npix, pix, domain)).s;
 	}
 	int32_t CM = unpack_m(__float_as_uint(gb.res[in].a[pix].w));
-	float target = gi_target(h, sel);
 	float D = (float)CM * target;
 	float num = domain < 0 ? target : 0.0f;
 	if (target > 0.0f && sel.rc) {
 		for (int k = 0; k < fp.gi_neighbors; k++) {
-			int2 nb = gb.neighbours[(size_t)k * fp.npix + pix];
+			uint32_t slot = (uint32_t)k * fp.npix + pix;
+			int2 nb = gb.neighbours[slot];
 			if (nb.x < 0)
 				continue;
-			GBuf gn = gbuf(gb.position, gb.normal, (uint32_t)nb.x);
-			float jn = gi_jacobian(gn.x, g.x, sel);
-			float tn = jn > 0.0f ? gi_target(receiver(fp, gb, (uint32_t)nb.x, gn), sel) * jn : 0.0f;
-			if (tn > 0.0f && !visible(s, fp.layout, gn.x, sel.xs))
-				tn = 0.0f;
+			float tn = gb.weights[slot];
 			D += (float)nb.y * tn;
 			if (k == domain)
 				num = tn;
@@ -635,9 +726,14 @@ void gi_temporal(const DeviceScene &s, const FrameParams &fp, const GiFrameBuffe
 void gi_spatial(const DeviceScene &s, const FrameParams &fp, const GiFrameBuffers &gb, int in, int out,
 		int iteration, cudaStream_t st)
 {
-	gi_spatial_select_kernel<<<(fp.npix + 127) / 128, 128, 0, st>>>(s, fp, gb, in, out, iteration);
-	KGR_CUDA(cudaGetLastError());
-	gi_spatial_weight_kernel<<<(fp.npix + 127) / 128, 128, 0, st>>>(s, fp, gb, in, out);
+	unsigned grid = (fp.npix + 127) / 128;
+	int vis_grid = device_sm_count() * 8;
+	KGR_CUDA(cudaMemsetAsync(gb.vis_count, 0, 2 * sizeof(uint32_t), st));
+	gi_spatial_gather_kernel<<<grid, 128, 0, st>>>(fp, gb, in, out, iteration);
+	gi_visibility_kernel<<<vis_grid, 128, 0, st>>>(s, fp, gb, in, 0);
+	gi_spatial_resample_kernel<<<grid, 128, 0, st>>>(fp, gb, in, iteration);
+	gi_visibility_kernel<<<vis_grid, 128, 0, st>>>(s, fp, gb, in, 1);
+	gi_spatial_finish_kernel<<<grid, 128, 0, st>>>(fp, gb, in, out);
 	KGR_CUDA(cudaGetLastError());
 }
 

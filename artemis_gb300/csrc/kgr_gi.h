@@ -26,15 +26,22 @@ struct GiFrameBuffers {
 	float4 *direct;         /* ReSTIR DI direct light of the primary vertex */
 	float4 *gi_dir;         /* GI direction xyz, source pdf */
 	float4 *auxiliary;      /* final path seed (reuse RNG) */
-	/* between the two halves of a spatial iteration: per pixel {w_sum,
-	 * bits(domain), bits(M sum), 0}; per neighbour slot k (k-major,
-	 * k * npix + pixel) {neighbour pixel or -1, its M} */
+	/* between the launches of a spatial iteration: per pixel {w_sum,
+	 * bits(domain), bits(M sum), target}; per neighbour slot (k-major,
+	 * k * npix + pixel) {neighbour pixel or -1, its M} and its weight; the
+	 * queues of visibility rays (slots) of the two rounds and their counts */
 	float4 *selection;
 	int2 *neighbours;
+	float *weights;
+	uint32_t *vis_queue[2];
+	uint32_t *vis_count;
 };
 
 /* Most neighbours a spatial iteration takes (the gi_neighbors option). */
 #define KGR_GI_MAX_NEIGHBORS 16
+/* Kernels one spatial iteration launches (gather, visibility, resample,
+ * visibility, finish). */
+#define KGR_GI_SPATIAL_LAUNCHES 5
 
 void gi_primary(const DeviceScene &s, const PathBuffers &pb, const FrameParams &fp, const GiFrameBuffers &gb,
 		cudaStream_t st);

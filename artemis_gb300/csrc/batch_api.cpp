@@ -266,7 +266,7 @@ kgr_status kgr_batcher_autotune(kgr_batcher *b, const kgr_scene *scene, const kg
 				b->tune.occupancy = (int16_t)c.occupancy;
 				b->tune.stack = (int16_t)c.stack;
 				double ms = time_frames([&] { b->render(scene, jobs, n, opt, st); }, frames, st);
-				if (c.layout == KGR_LAYOUT_FAST && c.shadow == KGR_TRACE_GRID && c.block == 128 && !c.occupancy)
+				if (is_default_shape(c))
 					res.default_ms = ms;
 				if (best < 0.0 || ms < best) {
 					best = ms;

@@ -1780,7 +1780,7 @@ kgr_status kgr_autotune(kgr_attachment *att, const kgr_launch_info *info, const 
 				att->tuned.occupancy = (int16_t)c.occupancy;
 				att->tuned.stack = (int16_t)c.stack;
 				double ms = time_frames([&] { render_frame(att, info, sc, st); }, frames, st);
-				if (c.layout == KGR_LAYOUT_FAST && c.shadow == KGR_TRACE_GRID && c.block == 128 && !c.occupancy)
+				if (is_default_shape(c))
 					res.default_ms = ms;
 				if (best < 0.0 || ms < best) {
 					best = ms;

@@ -121,7 +121,7 @@ struct kgr_server {
 	/* per scene: tuned layout and launch shape (autotune), -1 = not yet */
 	struct SceneTune {
 		int layout = -1;
-		kgr_trace_tune tune = {KGR_LAYOUT_FAST, KGR_TRACE_GRID, 128, 0, 0};
+		kgr_trace_tune tune = {KGR_LAYOUT_FAST, KGR_TRACE_PERSISTENT, 128, 0, 0};
 	};
 	std::vector<SceneTune> scene_tune;
 

@@ -398,7 +398,7 @@ typedef struct kgr_trace_tune {
 typedef struct kgr_autotune_result {
 	kgr_trace_tune best;
 	double best_ms;       /* ms per frame of the chosen shape */
-	double default_ms;    /* ms per frame of the untuned shape {fast, grid, 128, 0} */
+	double default_ms;    /* ms per frame of the untuned shape {fast, persistent, 128, 0, 0} */
 	uint32_t candidates;  /* shapes timed */
 	uint32_t reserved;
 } kgr_autotune_result;

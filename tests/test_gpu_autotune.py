@@ -27,7 +27,7 @@ def test_attachment_autotune_keeps_the_image(kind):
         att.set_option("temporal", False)
     att.set_option("russian_roulette", True)
     info = helpers.launch(cam, W, H, bufs, frame=5, max_depth=4)
-    assert att.trace_tune() == {"layout": "fast", "shadow": "grid", "block": 128, "occupancy": 0, "stack": 0}
+    assert att.trace_tune() == {"layout": "fast", "shadow": "persistent", "block": 128, "occupancy": 0, "stack": 0}
     att.render(info, sc)
     torch.cuda.synchronize()
     before = bufs[0].clone()

@@ -1465,7 +1465,7 @@ void render_restir_gi(kgr_attachment *att, const kgr_launch_info *info, const kg
 	att->mark(STAGE_TRACE_CLOSEST, st);
 	gi_primary(s, pb, fp, gb, st);
 	att->mark(STAGE_RESTIR_PRIMARY, st);
-	launches += 3;
+	launches += 4; /* generate, closest hit, primary vertex, its shadow rays */
 	for (int d = 1; d <= fp.max_depth; d++) {
 		int q = d & 1;
 		reset_counters(pb, (1 << (q ^ 1)) | (1 << CNT_SHADOW), st);

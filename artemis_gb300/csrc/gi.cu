@@ -260,7 +260,7 @@ __global__ void __launch_bounds__(128) gi_primary_kernel(DeviceScene s, PathBuff
 		uint32_t i = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
 		bool active = i < n;
 		uint32_t p = active ? pb.queue[0][i] : 0;
-		bool cont = false;
+		bool cont = false, shadow = false;
 		if (active) {
 			float4 hv = pb.hit[p];
 			kgr_hit h;
@@ -314,20 +314,23 @@ __global__ void __launch_bounds__(128) gi_primary_kernel(DeviceScene s, PathBuff
 					}
 					M++;
 				}
+				/* the selected light's contribution, with its shadow ray
+				 * queued for gi_direct_visibility_kernel, which zeroes the
+				 * contribution when the ray is blocked */
 				f3 direct = mk(0.0f);
 				if (sel >= 0) {
 					TriLight l = load_light(s.lights, (uint32_t)sel);
 					f3 D = selp - sh.x;
 					float d = length(D);
 					f3 Dn = D / d;
-					kgr_hit hh;
-					if (!trace<true>(s, fp.layout, sh.x, Dn, d - KGR_SHADOW_EPS, hh)) {
-						f3 Li = direct_unoccluded(sh, l.intensity, l.normal(), Dn, d);
-						float tgt = Li.x + Li.y + Li.z;
-						float dd = tgt * M;
-						float W = (dd > 0) ? wsum / dd : 0.0f;
-						direct = Li * W;
-					}
+					f3 Li = direct_unoccluded(sh, l.intensity, l.normal(), Dn, d);
+					float tgt = Li.x + Li.y + Li.z;
+					float dd = tgt * M;
+					float W = (dd > 0) ? wsum / dd : 0.0f;
+					direct = Li * W;
+					pb.sh_o[p] = f4_of(sh.x, 0.0f);
+					pb.sh_d[p] = f4_of(Dn, d - KGR_SHADOW_EPS);
+					shadow = true;
 				}
 				gb.direct[p] = f4_of(direct, 0.0f);
 				/* GI direction (eval, brdf.cuh:573-589) */
@@ -346,6 +349,23 @@ __global__ void __launch_bounds__(128) gi_primary_kernel(DeviceScene s, PathBuff
 			}
 		}
 		queue_append(pb.queue[1], out_counter, p, cont, pb.counters + CNT_BOUNCE_TOTAL);
+		queue_append(gb.vis_queue[0], gb.vis_count + 0, p, shadow);
+	}
+}
+
+/* The primary vertices' ReSTIR DI shadow rays (queued by gi_primary_kernel
+ * in the shadow-ray arrays, free until the first bounce is shaded): a
+ * blocked ray zeroes the pixel's direct light. */
+__global__ void __launch_bounds__(128) gi_direct_visibility_kernel(DeviceScene s, PathBuffers pb, FrameParams fp,
+		GiFrameBuffers gb)
+{
+	const uint32_t n = gb.vis_count[0];
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		uint32_t p = gb.vis_queue[0][i];
+		float4 a = pb.sh_o[p], b = pb.sh_d[p];
+		kgr_hit hh;
+		if (trace<true>(s, fp.layout, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), b.w, hh))
+			gb.direct[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 	}
 }
 
@@ -706,7 +726,9 @@ void gi_primary(const DeviceScene &s, const PathBuffers &pb, const FrameParams &
 {
 	int grid = (int)((pb.capacity + 127) / 128);
 	int cap = device_sm_count() * 16;
+	KGR_CUDA(cudaMemsetAsync(gb.vis_count, 0, sizeof(uint32_t), st));
 	gi_primary_kernel<<<grid < cap ? grid : cap, 128, 0, st>>>(s, pb, fp, gb);
+	gi_direct_visibility_kernel<<<device_sm_count() * 8, 128, 0, st>>>(s, pb, fp, gb);
 	KGR_CUDA(cudaGetLastError());
 }
 

@@ -753,6 +753,9 @@ struct kgr_attachment {
 
 	/* ReSTIR GI state */
 	DevBuf<float4> gi_a[3], gi_b[3], g_pos, g_nrm, g_ppos, g_pnrm, g_direct, g_dir;
+	DevBuf<int2> di_neighbours;
+	DevBuf<float> di_targets;
+	DevBuf<uint32_t> di_vis_queue[2], di_vis_count;
 	DevBuf<float4> gi_selection;
 	DevBuf<int2> gi_neighbours;
 	DevBuf<float> gi_weights;
@@ -941,6 +944,11 @@ struct kgr_attachment {
 		}
 		for (DevBuf<float4> *b : {&g_pos, &g_nrm, &g_ppos, &g_pnrm, &g_direct, &g_dir})
 			b->release();
+		di_neighbours.release();
+		di_targets.release();
+		di_vis_queue[0].release();
+		di_vis_queue[1].release();
+		di_vis_count.release();
 		gi_selection.release();
 		gi_neighbours.release();
 		gi_weights.release();
@@ -1181,7 +1189,7 @@ void render_restir_di(kgr_attachment *att, const kgr_launch_info *info, const kg
 	fp.spp = 1;
 	fp.paths = fp.npix;
 	fp.jitter = 0;
-	KGR_REQUIRE(fp.spatial_neighbors >= 0 && fp.spatial_neighbors <= 16, KGR_ERR_INVALID_ARGUMENT,
+	KGR_REQUIRE(fp.spatial_neighbors >= 0 && fp.spatial_neighbors <= KGR_MAX_NEIGHBORS, KGR_ERR_INVALID_ARGUMENT,
 		"spatial_neighbors must be 0..16");
 	KGR_REQUIRE(fp.candidates >= 1 && fp.candidates <= 1024, KGR_ERR_INVALID_ARGUMENT, "candidates must be 1..1024");
 	KGR_REQUIRE(info->buffers.normal && info->buffers.albedo && info->buffers.position, KGR_ERR_INVALID_ARGUMENT,
@@ -1206,6 +1214,11 @@ void render_restir_di(kgr_attachment *att, const kgr_launch_info *info, const kg
 	rb.materials = att->pixel_materials.ptr;
 	rb.intermediate = att->intermediate.ptr;
 	rb.auxiliary = att->auxiliary.ptr;
+	rb.neighbours = att->di_neighbours.ptr;
+	rb.targets = att->di_targets.ptr;
+	rb.vis_queue[0] = att->di_vis_queue[0].ptr;
+	rb.vis_queue[1] = att->di_vis_queue[1].ptr;
+	rb.vis_count = att->di_vis_count.ptr;
 	int prev = att->prev_index, cur = 1 - prev;
 	uint32_t launches = 0;
 
@@ -1249,7 +1262,7 @@ void render_restir_di(kgr_attachment *att, const kgr_launch_info *info, const kg
 		restir_spatial(s, fp, rb, out, in, outb, st);
 		att->mark(STAGE_RESTIR_SPATIAL, st);
 		std::swap(in, outb);
-		launches++;
+		launches += KGR_RESTIR_SPATIAL_LAUNCHES;
 	}
 	att->prev_index = in;
 	memcpy(att->prev_projection, info->camera.projection, 64);
@@ -1579,6 +1592,11 @@ kgr_status kgr_load(kgr_attachment *att)
 				att->auxiliary.alloc(npix);
 				att->pixel_materials.alloc(npix);
 				KGR_CUDA(cudaMemset(att->pixel_materials.ptr, 0, npix * sizeof(kgr_material)));
+				att->di_neighbours.alloc(npix * KGR_MAX_NEIGHBORS);
+				att->di_targets.alloc(npix * (KGR_MAX_NEIGHBORS + 1));
+				att->di_vis_queue[0].alloc(npix * KGR_MAX_NEIGHBORS);
+				att->di_vis_queue[1].alloc(npix * (KGR_MAX_NEIGHBORS + 1));
+				att->di_vis_count.alloc(2);
 				att->prev_index = 1;
 				att->ensure_paths((uint32_t)npix);
 			}

@@ -135,7 +135,20 @@ struct RestirFrameBuffers {
 	kgr_material *materials; /* per pixel */
 	float4 *intermediate;
 	float4 *auxiliary;
+	/* between the launches of a spatial pass: per neighbour slot (k-major,
+	 * k * npix + pixel) {neighbour pixel, M}; targets per slot, then one
+	 * row of npix for the lighting rays; the shadow-ray queues of the two
+	 * rounds (entries index targets) and their counts */
+	int2 *neighbours;
+	float *targets;
+	uint32_t *vis_queue[2];
+	uint32_t *vis_count;
 };
+
+/* Most neighbours a ReSTIR DI spatial pass takes (spatial_neighbors). */
+#define KGR_MAX_NEIGHBORS 16
+/* Kernels one ReSTIR DI spatial pass launches. */
+#define KGR_RESTIR_SPATIAL_LAUNCHES 5
 
 struct OutputBuffers {
 	float4 *color, *normal, *albedo, *position;

@@ -356,73 +356,196 @@ __device__ __forceinline__ int spatial_neighbor(const FrameParams &fp, int index
 	return x0 + y0 * width;
 }
 
-#define KGR_MAX_NEIGHBORS 16
+/* Spatial reuse (amadeus_restir.cu:367-433) as a wavefront of five launches
+ * per pass.  Its shadow rays -- one per neighbour reservoir (occluded_target
+ * at this pixel), one per neighbour for the bias correction (the selected
+ * sample seen from the neighbour's surface) and the final lighting ray --
+ * are queued and walked by restir_visibility_kernel, one ray per thread,
+ * instead of inside the per-pixel loops.  Between the launches: per
+ * neighbour slot (k-major, slot = i * npix + pixel) {neighbour pixel, M}
+ * and a target value that a blocked ray sets to 0 (occluded_target's
+ * result); row KGR_MAX_NEIGHBORS of the target array holds the lighting
+ * ray's 1 (visible) or 0; the merged reservoir sits in the output buffer
+ * between resample and finish.  Every value is computed by the reference's
+ * expressions in its order, and each pixel's random stream is replayed
+ * draw for draw, so the result is the single-pass kernel's bit for bit.
+ *
+ * gather: the neighbours and, for each one with M > 0 and a light, the
+ * unoccluded target at this pixel, with its shadow ray queued.  The random
+ * stream advances as the resampling will draw it: one uniform for the
+ * centre, three for each neighbour's offset, one for each neighbour with
+ * M > 0. */
+__global__ void __launch_bounds__(128) restir_gather_kernel(DeviceScene s, FrameParams fp, RestirFrameBuffers rb,
+		OutputBuffers out, int inb)
+{
+	uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+	if (pix >= fp.npix)
+		return;
+	ReservoirBuffers IN = rb.res[inb];
+	Sample cs;
+	float cw, cW;
+	int32_t cM;
+	load_res(IN, pix, cs, cw, cW, cM);
+	if (cM <= 0)
+		return;
+	SurfaceHit hit = gbuffer_hit(fp, rb, out, pix);
+	float4 av = rb.auxiliary[pix];
+	f3 seed = mk(av.x, av.y, av.z);
+	rand_uniform(seed);
+	for (int i = 0; i < fp.spatial_neighbors; i++) {
+		int index0 = spatial_neighbor(fp, (int)pix, seed);
+		uint32_t slot = (uint32_t)i * fp.npix + pix;
+		Sample ns;
+		float nw, nW;
+		int32_t nM;
+		load_res(IN, (uint32_t)index0, ns, nw, nW, nM);
+		float t = 0.0f;
+		bool ray = false;
+		if (nM > 0) {
+			if (ns.light >= 0) {
+				t = target(s, ns, hit);
+				/* +0 stays +0 whatever the ray; -0 would become +0 if blocked */
+				ray = __float_as_uint(t) != 0u;
+			}
+			rand_uniform(seed);
+		}
+		rb.neighbours[slot] = make_int2(index0, nM);
+		rb.targets[slot] = t;
+		queue_append(rb.vis_queue[0], rb.vis_count + 0, slot, ray);
+	}
+}
 
-__global__ void __launch_bounds__(128) spatial_kernel(DeviceScene s, FrameParams fp, RestirFrameBuffers rb,
+/* Shadow rays of the queued entries; a blocked ray sets its target to 0.
+ * Round 0: this pixel's surface to a neighbour reservoir's light sample.
+ * Round 1: a neighbour's surface to this pixel's selected sample (entries
+ * below KGR_MAX_NEIGHBORS * npix), or this pixel's surface to it (the
+ * lighting ray, entries above). */
+__global__ void __launch_bounds__(128) restir_visibility_kernel(DeviceScene s, FrameParams fp,
+		RestirFrameBuffers rb, OutputBuffers out, int inb, int outb, int round)
+{
+	const uint32_t n = rb.vis_count[round];
+	const uint32_t *queue = rb.vis_queue[round];
+	const uint32_t lighting = (uint32_t)KGR_MAX_NEIGHBORS * fp.npix;
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		uint32_t e = queue[i];
+		uint32_t pix = e < lighting ? e % fp.npix : e - lighting;
+		f3 from, to;
+		if (round == 0) {
+			from = f3_of(out.position[pix]);
+			to = f3_of(rb.res[inb].a[rb.neighbours[e].x]);
+		} else {
+			uint32_t at = e < lighting ? (uint32_t)rb.neighbours[e].x : pix;
+			from = f3_of(out.position[at]);
+			to = f3_of(rb.res[outb].a[pix]);
+		}
+		f3 D = to - from;
+		float d = length(D);
+		f3 Dn = D / d;
+		if (occluded(s, fp.layout, from, Dn, d))
+			rb.targets[e] = 0.0f;
+	}
+}
+
+/* resample: the merged reservoir over the centre and the neighbours with
+ * their occluded targets (Reservoir::update, the same draws), then the
+ * bias correction's targets of the selected sample at each neighbour's
+ * surface with their shadow rays queued, and the lighting ray queued. */
+__global__ void __launch_bounds__(128) restir_resample_kernel(DeviceScene s, FrameParams fp, RestirFrameBuffers rb,
 		OutputBuffers out, int inb, int outb)
 {
 	uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
 	if (pix >= fp.npix)
 		return;
 	ReservoirBuffers IN = rb.res[inb], OUT = rb.res[outb];
-	SurfaceHit hit = gbuffer_hit(fp, rb, out, pix);
 	Sample cs;
 	float cw, cW;
 	int32_t cM;
 	load_res(IN, pix, cs, cw, cW, cM);
-	f3 direct = mk(0.0f);
-	if (cM > 0) {
-		float4 av = rb.auxiliary[pix];
-		Reservoir merged;
-		merged.init(mk(av.x, av.y, av.z));
-		float t_current = target(s, cs, hit);
-		merged.update(cs, t_current * cW * cM);
-		int K = fp.spatial_neighbors;
-		int32_t nidx[KGR_MAX_NEIGHBORS];
-		int32_t sizes[KGR_MAX_NEIGHBORS];
-		int32_t count = 0;
-		for (int i = 0; i < K; i++) {
-			int index0 = spatial_neighbor(fp, (int)pix, merged.seed);
+	if (cM <= 0)
+		return;
+	SurfaceHit hit = gbuffer_hit(fp, rb, out, pix);
+	float4 av = rb.auxiliary[pix];
+	Reservoir merged;
+	merged.init(mk(av.x, av.y, av.z));
+	float t_current = target(s, cs, hit);
+	merged.update(cs, t_current * cW * cM);
+	int K = fp.spatial_neighbors;
+	int32_t count = 0;
+	for (int i = 0; i < K; i++) {
+		rand_uniform_3f(merged.seed);
+		uint32_t slot = (uint32_t)i * fp.npix + pix;
+		int2 nb = rb.neighbours[slot];
+		if (nb.y > 0) {
 			Sample ns;
 			float nw, nW;
 			int32_t nM;
-			load_res(IN, (uint32_t)index0, ns, nw, nW, nM);
-			if (nM > 0) {
-				float t_neighbor = occluded_target(s, fp.layout, ns, hit);
-				merged.update(ns, t_neighbor * nW * nM);
-			}
-			nidx[i] = index0;
-			sizes[i] = nM;
-			count += nM;
+			load_res(IN, (uint32_t)nb.x, ns, nw, nW, nM);
+			merged.update(ns, rb.targets[slot] * nW * nM);
 		}
-		merged.M = cM + count;
-		/* bias correction (:387-393): neighbours whose surface sees the
-		 * selected sample count towards Z */
-		int32_t Z = cM;
-		for (int i = 0; i < K; i++) {
-			if (sizes[i] <= 0)
-				continue;
-			SurfaceHit h0 = gbuffer_hit(fp, rb, out, (uint32_t)nidx[i]);
+		count += nb.y;
+	}
+	merged.M = cM + count;
+	for (int i = 0; i < K; i++) {
+		uint32_t slot = (uint32_t)i * fp.npix + pix;
+		int2 nb = rb.neighbours[slot];
+		if (nb.y <= 0)
+			continue;
+		float t = 0.0f;
+		if (merged.data.light >= 0) {
+			SurfaceHit h0 = gbuffer_hit(fp, rb, out, (uint32_t)nb.x);
 			h0.wo = hit.wo;
 			h0.entering = true;
-			float t_neighbor = occluded_target(s, fp.layout, merged.data, h0);
-			if (t_neighbor > 0.0f)
-				Z += sizes[i];
+			t = target(s, merged.data, h0);
 		}
-		float t_merged = target(s, merged.data, hit);
+		rb.targets[slot] = t;
+		queue_append(rb.vis_queue[1], rb.vis_count + 1, slot, t > 0.0f);
+	}
+	uint32_t lit = (uint32_t)KGR_MAX_NEIGHBORS * fp.npix + pix;
+	rb.targets[lit] = merged.data.light >= 0 ? 1.0f : 0.0f;
+	queue_append(rb.vis_queue[1], rb.vis_count + 1, lit, merged.data.light >= 0);
+	store_res(OUT, pix, merged.data, merged.w, 0.0f, merged.M);
+}
+
+/* finish: Z = M of the centre and of every neighbour whose surface sees
+ * the selected sample, W = w / (p^ Z), the shaded direct light and the
+ * blend into the output (amadeus_restir.cu:387-433). */
+__global__ void __launch_bounds__(128) restir_finish_kernel(DeviceScene s, FrameParams fp, RestirFrameBuffers rb,
+		OutputBuffers out, int inb, int outb)
+{
+	uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+	if (pix >= fp.npix)
+		return;
+	ReservoirBuffers IN = rb.res[inb], OUT = rb.res[outb];
+	int32_t cM = __float_as_int(IN.b[pix].z);
+	f3 direct = mk(0.0f);
+	if (cM > 0) {
+		SurfaceHit hit = gbuffer_hit(fp, rb, out, pix);
+		Sample data;
+		float w, W0;
+		int32_t M;
+		load_res(OUT, pix, data, w, W0, M);
+		int32_t Z = cM;
+		for (int i = 0; i < fp.spatial_neighbors; i++) {
+			uint32_t slot = (uint32_t)i * fp.npix + pix;
+			int32_t size = rb.neighbours[slot].y;
+			if (size <= 0)
+				continue;
+			if (rb.targets[slot] > 0.0f)
+				Z += size;
+		}
+		float t_merged = target(s, data, hit);
 		float denominator = t_merged * Z;
-		merged.W = (denominator > 0.0f) ? merged.w / denominator : 0.0f;
+		float W = (denominator > 0.0f) ? w / denominator : 0.0f;
 		f3 lighting = mk(0.0f);
-		if (merged.data.light >= 0) {
-			TriLight l = load_light(s.lights, (uint32_t)merged.data.light);
-			f3 D = merged.data.point - hit.x;
+		if (data.light >= 0 && rb.targets[(uint32_t)KGR_MAX_NEIGHBORS * fp.npix + pix] > 0.0f) {
+			TriLight l = load_light(s.lights, (uint32_t)data.light);
+			f3 D = data.point - hit.x;
 			float d = length(D);
 			f3 Dn = D / d;
-			if (!occluded(s, fp.layout, hit.x, Dn, d))
-				lighting = direct_unoccluded(hit, l.intensity, l.normal(), Dn, d);
+			lighting = direct_unoccluded(hit, l.intensity, l.normal(), Dn, d);
 		}
-		direct = hit.mat.emission + lighting * merged.W;
-		store_res(OUT, pix, merged.data, merged.w, merged.W, merged.M);
+		direct = hit.mat.emission + lighting * W;
+		store_res(OUT, pix, data, w, W, M);
 	} else {
 		float4 b = OUT.b[pix];
 		OUT.b[pix] = make_float4(0.0f, 0.0f, __int_as_float(0), b.w);
@@ -465,7 +588,14 @@ void restir_temporal(const DeviceScene &s, const FrameParams &fp, const RestirFr
 void restir_spatial(const DeviceScene &s, const FrameParams &fp, const RestirFrameBuffers &rb,
 		const OutputBuffers &out, int in, int outbuf, cudaStream_t st)
 {
-	spatial_kernel<<<(fp.npix + 127) / 128, 128, 0, st>>>(s, fp, rb, out, in, outbuf);
+	unsigned grid = (fp.npix + 127) / 128;
+	int vis_grid = device_sm_count() * 8;
+	KGR_CUDA(cudaMemsetAsync(rb.vis_count, 0, 2 * sizeof(uint32_t), st));
+	restir_gather_kernel<<<grid, 128, 0, st>>>(s, fp, rb, out, in);
+	restir_visibility_kernel<<<vis_grid, 128, 0, st>>>(s, fp, rb, out, in, outbuf, 0);
+	restir_resample_kernel<<<grid, 128, 0, st>>>(s, fp, rb, out, in, outbuf);
+	restir_visibility_kernel<<<vis_grid, 128, 0, st>>>(s, fp, rb, out, in, outbuf, 1);
+	restir_finish_kernel<<<grid, 128, 0, st>>>(s, fp, rb, out, in, outbuf);
 	KGR_CUDA(cudaGetLastError());
 }
 

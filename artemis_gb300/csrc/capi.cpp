@@ -1232,7 +1232,7 @@ void render_restir_di(kgr_attachment *att, const kgr_launch_info *info, const kg
 	att->mark(STAGE_TRACE_CLOSEST, st);
 	restir_primary(s, pb, fp, rb, cur, st);
 	att->mark(STAGE_RESTIR_PRIMARY, st);
-	launches += 3;
+	launches += 4; /* generate, closest hit, primary vertex, its shadow rays */
 	for (int d = 1; d <= fp.max_depth; d++) {
 		int q = d & 1;
 		reset_counters(pb, (1 << (q ^ 1)) | (1 << CNT_SHADOW), st);
@@ -1252,7 +1252,7 @@ void render_restir_di(kgr_attachment *att, const kgr_launch_info *info, const kg
 	if (fp.temporal) {
 		restir_temporal(s, fp, rb, out, cur, prev, st);
 		att->mark(STAGE_RESTIR_TEMPORAL, st);
-		launches++;
+		launches += 3;
 	}
 	/* spatial passes with the ping-pong of restir.cuh:280-300 */
 	int passes = att->opt_int("spatial_passes", 2);

@@ -93,22 +93,11 @@ __device__ __forceinline__ float target(const DeviceScene &s, const Sample &smp,
 	return Li.x + Li.y + Li.z;
 }
 
-/* occluded_target (amadeus_restir.cu:163-178) via direct_occluded
- * (amadeus_common.cuh:399-421) */
-__device__ __forceinline__ float occluded_target(const DeviceScene &s, int layout, const Sample &smp,
-		const SurfaceHit &hit)
-{
-	if (smp.light < 0)
-		return 0.0f;
-	TriLight l = load_light(s.lights, (uint32_t)smp.light);
-	f3 D = smp.point - hit.x;
-	float d = length(D);
-	f3 Dn = D / d;
-	if (occluded(s, layout, hit.x, Dn, d))
-		return 0.0f;
-	f3 Li = direct_unoccluded(hit, l.intensity, l.normal(), Dn, d);
-	return Li.x + Li.y + Li.z;
-}
+/* occluded_target (amadeus_restir.cu:163-178, via direct_occluded of
+ * amadeus_common.cuh:399-421) is target() when the shadow ray from the
+ * surface to the sample, occluded() over D / |D| and |D|, is unblocked, and
+ * 0 when it is blocked.  The reuse kernels compute target() and queue that
+ * ray; the visibility kernels set the target to 0 when the ray is blocked. */
 
 __device__ __forceinline__ f3 v3(const float *p) { return mk(p[0], p[1], p[2]); }
 
@@ -143,7 +132,7 @@ __global__ void __launch_bounds__(128) primary_kernel(DeviceScene s, PathBuffers
 		uint32_t i = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
 		bool active = i < n;
 		uint32_t p = active ? pb.queue[0][i] : 0;
-		bool cont = false;
+		bool cont = false, shadow = false;
 		if (active) {
 			float4 hv = pb.hit[p];
 			kgr_hit h;
@@ -186,22 +175,24 @@ __global__ void __launch_bounds__(128) primary_kernel(DeviceScene s, PathBuffers
 					res.update(smp, (pdf > 0) ? tgt / pdf : 0);
 				}
 				/* direct_occluded of the selection, resample, and the second
-				 * visibility test of :522-523 (the same ray, so the same answer) */
+				 * visibility test of :522-523 (the same ray, so the same
+				 * answer).  The reservoir is stored as if the selection were
+				 * visible and its shadow ray queued: a blocked ray makes the
+				 * target 0, so resample and the visibility factor give W = +0,
+				 * which primary_visibility_kernel writes. */
 				float tgt = 0.0f;
-				bool occ = false;
 				if (res.data.light >= 0) {
 					TriLight l = load_light(s.lights, (uint32_t)res.data.light);
 					f3 D = res.data.point - sh.x;
 					float d = length(D);
 					f3 Dn = D / d;
-					occ = occluded(s, fp.layout, sh.x, Dn, d);
-					if (!occ) {
-						f3 Li = direct_unoccluded(sh, l.intensity, l.normal(), Dn, d);
-						tgt = Li.x + Li.y + Li.z;
-					}
+					f3 Li = direct_unoccluded(sh, l.intensity, l.normal(), Dn, d);
+					tgt = Li.x + Li.y + Li.z;
+					pb.sh_o[p] = f4_of(sh.x, 0.0f);
+					pb.sh_d[p] = f4_of(Dn, d - KGR_SHADOW_EPS);
+					shadow = true;
 				}
-				res.resample(tgt);
-				res.W *= 1.0f - (occ ? 1.0f : 0.0f);
+				res.resample(tgt); /* the visibility factor of a visible selection is 1 */
 				store_res(R, p, res.data, res.w, res.W, res.M);
 				/* per-pixel material (:526) */
 				uint4 tr = __ldg(&s.tris[h.prim]);
@@ -236,6 +227,23 @@ __global__ void __launch_bounds__(128) primary_kernel(DeviceScene s, PathBuffers
 			}
 		}
 		queue_append(pb.queue[1], out_counter, p, cont, pb.counters + CNT_BOUNCE_TOTAL);
+		queue_append(rb.vis_queue[0], rb.vis_count + 0, p, shadow);
+	}
+}
+
+/* The selections' shadow rays queued by primary_kernel (in the shadow-ray
+ * arrays, free until the first bounce is shaded): a blocked one sets the
+ * reservoir's W to +0. */
+__global__ void __launch_bounds__(128) primary_visibility_kernel(DeviceScene s, PathBuffers pb, FrameParams fp,
+		RestirFrameBuffers rb, int cur)
+{
+	const uint32_t n = rb.vis_count[0];
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		uint32_t p = rb.vis_queue[0][i];
+		float4 a = pb.sh_o[p], b = pb.sh_d[p];
+		kgr_hit h;
+		if (trace<true>(s, fp.layout, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), b.w, h))
+			rb.res[cur].b[p].y = 0.0f;
 	}
 }
 
@@ -298,7 +306,15 @@ __device__ __forceinline__ int reproject(const FrameParams &fp, int index, const
 	return iy * (int)fp.width + ix;
 }
 
-__global__ void __launch_bounds__(128) temporal_kernel(DeviceScene s, FrameParams fp, RestirFrameBuffers rb,
+/* Temporal reuse (amadeus_restir.cu:316-365) in three launches: the two
+ * occluded targets -- the current reservoir's and the reprojected previous
+ * one's -- are computed unoccluded with their shadow rays queued
+ * (temporal_gather_kernel), the rays walked (temporal_visibility_kernel: a
+ * blocked ray sets its target to 0, occluded_target's result), then the
+ * merge (temporal_merge_kernel).  Targets sit in rows 0 (current) and 1
+ * (previous) of the spatial pass's target array, the reprojected pixel and
+ * its M in the neighbour array: both are free until spatial reuse starts. */
+__global__ void __launch_bounds__(128) temporal_gather_kernel(DeviceScene s, FrameParams fp, RestirFrameBuffers rb,
 		OutputBuffers out, int cur, int prev)
 {
 	uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
@@ -313,20 +329,71 @@ __global__ void __launch_bounds__(128) temporal_kernel(DeviceScene s, FrameParam
 		return;
 	SurfaceHit hit = gbuffer_hit(fp, rb, out, pix);
 	int pindex = reproject(fp, (int)pix, hit.x);
-	float4 av = rb.auxiliary[pix];
-	Reservoir merged;
-	merged.init(mk(av.x, av.y, av.z));
-	float t_current = occluded_target(s, fp.layout, cs, hit);
-	merged.update(cs, t_current * cW * cM);
-	int32_t N = cM;
+	float t_current = target(s, cs, hit);
+	rb.targets[pix] = t_current;
+	/* +0 stays +0 whatever the ray; anything else is traced */
+	queue_append(rb.vis_queue[0], rb.vis_count + 0, pix, __float_as_uint(t_current) != 0u);
+	int32_t pM = 0;
 	if (pindex >= 0) {
 		Sample ps;
 		float pw, pW;
-		int32_t pM;
 		load_res(P, (uint32_t)pindex, ps, pw, pW, pM);
 		if (pM > 0) {
+			float t_previous = target(s, ps, hit);
+			rb.targets[fp.npix + pix] = t_previous;
+			queue_append(rb.vis_queue[0], rb.vis_count + 0, fp.npix + pix, __float_as_uint(t_previous) != 0u);
+		}
+	}
+	rb.neighbours[pix] = make_int2(pindex, pM);
+}
+
+__global__ void __launch_bounds__(128) temporal_visibility_kernel(DeviceScene s, FrameParams fp,
+		RestirFrameBuffers rb, OutputBuffers out, int cur, int prev)
+{
+	const uint32_t n = rb.vis_count[0];
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		uint32_t e = rb.vis_queue[0][i];
+		bool previous = e >= fp.npix;
+		uint32_t pix = previous ? e - fp.npix : e;
+		f3 from = f3_of(out.position[pix]);
+		f3 to = previous ? f3_of(rb.res[prev].a[rb.neighbours[pix].x]) : f3_of(rb.res[cur].a[pix]);
+		f3 D = to - from;
+		float d = length(D);
+		f3 Dn = D / d;
+		if (occluded(s, fp.layout, from, Dn, d))
+			rb.targets[e] = 0.0f;
+	}
+}
+
+__global__ void __launch_bounds__(128) temporal_merge_kernel(DeviceScene s, FrameParams fp, RestirFrameBuffers rb,
+		OutputBuffers out, int cur, int prev)
+{
+	uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+	if (pix >= fp.npix)
+		return;
+	ReservoirBuffers C = rb.res[cur], P = rb.res[prev];
+	Sample cs;
+	float cw, cW;
+	int32_t cM;
+	load_res(C, pix, cs, cw, cW, cM);
+	if (cM <= 0)
+		return;
+	SurfaceHit hit = gbuffer_hit(fp, rb, out, pix);
+	int2 pr = rb.neighbours[pix];
+	float4 av = rb.auxiliary[pix];
+	Reservoir merged;
+	merged.init(mk(av.x, av.y, av.z));
+	float t_current = rb.targets[pix];
+	merged.update(cs, t_current * cW * cM);
+	int32_t N = cM;
+	if (pr.x >= 0) {
+		Sample ps;
+		float pw, pW;
+		int32_t pM;
+		load_res(P, (uint32_t)pr.x, ps, pw, pW, pM);
+		if (pM > 0) {
 			pM = pM < fp.temporal_mcap ? pM : fp.temporal_mcap;
-			float t_previous = occluded_target(s, fp.layout, ps, hit);
+			float t_previous = rb.targets[fp.npix + pix];
 			merged.update(ps, t_previous * pW * pM);
 			N += (t_previous > 0) * pM;
 		}
@@ -567,7 +634,9 @@ void restir_primary(const DeviceScene &s, const PathBuffers &pb, const FramePara
 {
 	int grid = (int)((pb.capacity + 127) / 128);
 	int cap = device_sm_count() * 16;
+	KGR_CUDA(cudaMemsetAsync(rb.vis_count, 0, sizeof(uint32_t), st));
 	primary_kernel<<<grid < cap ? grid : cap, 128, 0, st>>>(s, pb, fp, rb, cur);
+	primary_visibility_kernel<<<device_sm_count() * 8, 128, 0, st>>>(s, pb, fp, rb, cur);
 	KGR_CUDA(cudaGetLastError());
 }
 
@@ -581,7 +650,11 @@ void restir_finalize(const PathBuffers &pb, const FrameParams &fp, const RestirF
 void restir_temporal(const DeviceScene &s, const FrameParams &fp, const RestirFrameBuffers &rb,
 		const OutputBuffers &out, int cur, int prev, cudaStream_t st)
 {
-	temporal_kernel<<<(fp.npix + 127) / 128, 128, 0, st>>>(s, fp, rb, out, cur, prev);
+	unsigned grid = (fp.npix + 127) / 128;
+	KGR_CUDA(cudaMemsetAsync(rb.vis_count, 0, sizeof(uint32_t), st));
+	temporal_gather_kernel<<<grid, 128, 0, st>>>(s, fp, rb, out, cur, prev);
+	temporal_visibility_kernel<<<device_sm_count() * 8, 128, 0, st>>>(s, fp, rb, out, cur, prev);
+	temporal_merge_kernel<<<grid, 128, 0, st>>>(s, fp, rb, out, cur, prev);
 	KGR_CUDA(cudaGetLastError());
 }
 

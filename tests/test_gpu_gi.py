@@ -27,8 +27,9 @@ def rel_ok(a, b, rtol=1e-4, atol=1e-6):
     return np.abs(a - b) <= rtol * np.maximum(np.abs(a), np.abs(b)) + atol
 
 
-@pytest.mark.parametrize("layout", ["fast", "threaded", "wide"])
-def test_restir_gi_matches_oracle(layout):
+# 16 neighbours: the most an iteration allows, every neighbour slot in use
+@pytest.mark.parametrize("layout,neighbors", [("fast", 8), ("threaded", 8), ("wide", 8), ("fast", 16)])
+def test_restir_gi_matches_oracle(layout, neighbors):
     g, sc, osc = helpers.both("box4k", 1)
     W, H, frames = 64, 64, 3
     bufs = helpers.device_buffers(torch, W * H)
@@ -36,7 +37,8 @@ def test_restir_gi_matches_oracle(layout):
     att.attach(W, H)
     att.load()
     att.set_option("layout", layout)
-    state = pyoracle.GiState(W * H, temporal=True, mcap=30, iterations=3, neighbors=8, radius=30)
+    att.set_option("gi_neighbors", neighbors)
+    state = pyoracle.GiState(W * H, temporal=True, mcap=30, iterations=3, neighbors=neighbors, radius=30)
     ocolor = np.zeros((W * H, 4), np.float32)
     prev = None
     for f in range(frames):
@@ -55,7 +57,7 @@ def test_restir_gi_matches_oracle(layout):
     ra = att.debug_copy("gi_reservoir_a", np.zeros((W * H, 4), np.float32))
     rb = att.debug_copy("gi_reservoir_b", np.zeros((W * H, 4), np.float32))
     same = np.all(ra.view(np.uint32) == state.arrays["res_a"].view(np.uint32), axis=1).mean()
-    print(f"GI {layout}: colour exact {exact:.6f}, within 1e-4 {close:.6f}, reservoirs equal {same:.6f}")
+    print(f"GI {layout}/{neighbors}: colour exact {exact:.6f}, within 1e-4 {close:.6f}, reservoirs equal {same:.6f}")
     assert close >= 0.999
     assert same >= 0.999
     assert np.all(rel_ok(rb, state.arrays["res_b"]), axis=1).mean() >= 0.999

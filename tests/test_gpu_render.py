@@ -99,12 +99,15 @@ def restir_gpu(g, sc, W, H, frames, opts, max_depth=2):
     return cam, [b.cpu().numpy() for b in bufs], res_a, res_b, inter, st
 
 
-@pytest.mark.parametrize("passes,layout", [(1, "fast"), (2, "threaded"), (1, "wide")])
-def test_restir_di_matches_oracle(box4k, passes, layout):
+# the last case takes the most neighbours a pass allows (16): every neighbour
+# slot and the largest shadow-ray queues of the reuse kernels in use
+@pytest.mark.parametrize("passes,layout,neighbors", [(1, "fast", 5), (2, "threaded", 5), (1, "wide", 5),
+                                                     (2, "fast", 16)])
+def test_restir_di_matches_oracle(box4k, passes, layout, neighbors):
     g, sc, osc = box4k
     W, H = 96, 96
     opts = {"candidates": 32, "temporal": True, "temporal_mcap": 20, "spatial_passes": passes,
-            "spatial_neighbors": 5, "spatial_radius": 30, "layout": layout}
+            "spatial_neighbors": neighbors, "spatial_radius": 30, "layout": layout}
     cam, out, res_a, res_b, inter, st = restir_gpu(g, sc, W, H, 2, opts)
     n = W * H
     state = pyoracle.RestirBuffers(n)
@@ -112,7 +115,7 @@ def test_restir_di_matches_oracle(box4k, passes, layout):
     for f in range(2):
         p = helpers.oracle_params(cam, W, H, max_depth=2, spp=1, frame=f, samples=0, accumulate=0,
                                   candidates=32, temporal=1, temporal_mcap=20, spatial_passes=passes,
-                                  spatial_neighbors=5, spatial_radius=30)
+                                  spatial_neighbors=neighbors, spatial_radius=30)
         pyoracle.render_restir(osc, p, state, ref)
     A = state.arrays
     light_gpu = res_a[:, 3].view(np.int32)

@@ -106,8 +106,11 @@ uint64_t request_bytes(const kgr_request &q)
 	uint64_t npix = (uint64_t)q.width * q.height;
 	/* path tracer: the color accumulation; ReSTIR DI: color and three AOVs,
 	 * two 32-byte reservoirs, the per-pixel material, intermediate and
-	 * auxiliary terms */
-	return q.kind == KGR_REQUEST_RESTIR_DI ? npix * (64 + 64 + 64 + 32) : npix * 16;
+	 * auxiliary terms, and the reuse passes' scratch for up to 16
+	 * neighbours: {pixel, M} and a target per neighbour slot, a row of
+	 * lighting targets, the two shadow-ray queues (16 * 8 + 17 * 4 +
+	 * 16 * 4 + 17 * 4 = 328 bytes) */
+	return q.kind == KGR_REQUEST_RESTIR_DI ? npix * (64 + 64 + 64 + 32 + 328) : npix * 16;
 }
 
 } /* namespace */

@@ -1596,7 +1596,7 @@ kgr_status kgr_load(kgr_attachment *att)
 				att->di_targets.alloc(npix * (KGR_MAX_NEIGHBORS + 1));
 				att->di_vis_queue[0].alloc(npix * KGR_MAX_NEIGHBORS);
 				att->di_vis_queue[1].alloc(npix * (KGR_MAX_NEIGHBORS + 1));
-				att->di_vis_count.alloc(2);
+				att->di_vis_count.alloc(4); /* two queue counts, two fetch counters */
 				att->prev_index = 1;
 				att->ensure_paths((uint32_t)npix);
 			}
@@ -1619,7 +1619,7 @@ kgr_status kgr_load(kgr_attachment *att)
 				att->gi_weights.alloc(npix * KGR_GI_MAX_NEIGHBORS);
 				att->gi_vis_queue[0].alloc(npix * KGR_GI_MAX_NEIGHBORS);
 				att->gi_vis_queue[1].alloc(npix * KGR_GI_MAX_NEIGHBORS);
-				att->gi_vis_count.alloc(2);
+				att->gi_vis_count.alloc(4); /* two queue counts, two fetch counters */
 				att->gi_prev = 0;
 				att->ensure_paths((uint32_t)npix);
 			}

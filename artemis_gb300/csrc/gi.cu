@@ -359,14 +359,13 @@ __global__ void __launch_bounds__(128) gi_primary_kernel(DeviceScene s, PathBuff
 __global__ void __launch_bounds__(128) gi_direct_visibility_kernel(DeviceScene s, PathBuffers pb, FrameParams fp,
 		GiFrameBuffers gb)
 {
-	const uint32_t n = gb.vis_count[0];
-	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+	for_each_queued(gb.vis_count[0], gb.vis_count + 2, [&](uint32_t i) {
 		uint32_t p = gb.vis_queue[0][i];
 		float4 a = pb.sh_o[p], b = pb.sh_d[p];
 		kgr_hit hh;
 		if (trace<true>(s, fp.layout, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), b.w, hh))
 			gb.direct[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-	}
+	});
 }
 
 /* Initial reservoir from the finished path: one candidate, W in FP64. */
@@ -554,9 +553,8 @@ __device__ __forceinline__ uint32_t selected_from(const GiFrameBuffers &gb, uint
 __global__ void __launch_bounds__(128) gi_visibility_kernel(DeviceScene s, FrameParams fp, GiFrameBuffers gb, int in,
 		int round)
 {
-	const uint32_t n = gb.vis_count[round];
 	const uint32_t *queue = gb.vis_queue[round];
-	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+	for_each_queued(gb.vis_count[round], gb.vis_count + 2 + round, [&](uint32_t i) {
 		uint32_t slot = queue[i];
 		uint32_t pix = slot % fp.npix;
 		uint32_t idx = (uint32_t)gb.neighbours[slot].x;
@@ -571,7 +569,7 @@ __global__ void __launch_bounds__(128) gi_visibility_kernel(DeviceScene s, Frame
 		}
 		if (!visible(s, fp.layout, from, to))
 			gb.weights[slot] = 0.0f;
-	}
+	});
 }
 
 /* resample: the weighted reservoir over the centre and the neighbours with
@@ -726,7 +724,7 @@ void gi_primary(const DeviceScene &s, const PathBuffers &pb, const FrameParams &
 {
 	int grid = (int)((pb.capacity + 127) / 128);
 	int cap = device_sm_count() * 16;
-	KGR_CUDA(cudaMemsetAsync(gb.vis_count, 0, sizeof(uint32_t), st));
+	KGR_CUDA(cudaMemsetAsync(gb.vis_count, 0, 4 * sizeof(uint32_t), st));
 	gi_primary_kernel<<<grid < cap ? grid : cap, 128, 0, st>>>(s, pb, fp, gb);
 	gi_direct_visibility_kernel<<<device_sm_count() * 8, 128, 0, st>>>(s, pb, fp, gb);
 	KGR_CUDA(cudaGetLastError());
@@ -750,7 +748,7 @@ void gi_spatial(const DeviceScene &s, const FrameParams &fp, const GiFrameBuffer
 {
 	unsigned grid = (fp.npix + 127) / 128;
 	int vis_grid = device_sm_count() * 8;
-	KGR_CUDA(cudaMemsetAsync(gb.vis_count, 0, 2 * sizeof(uint32_t), st));
+	KGR_CUDA(cudaMemsetAsync(gb.vis_count, 0, 4 * sizeof(uint32_t), st));
 	gi_spatial_gather_kernel<<<grid, 128, 0, st>>>(fp, gb, in, out, iteration);
 	gi_visibility_kernel<<<vis_grid, 128, 0, st>>>(s, fp, gb, in, 0);
 	gi_spatial_resample_kernel<<<grid, 128, 0, st>>>(fp, gb, in, iteration);

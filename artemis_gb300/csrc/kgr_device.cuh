@@ -777,6 +777,27 @@ __device__ __forceinline__ void queue_append(uint32_t *queue, uint32_t *counter,
 		queue[base + __popc(ballot & ((1u << lane) - 1u))] = value;
 }
 
+/* Visit entries 0..n-1 of a queue in batches of 32 a warp: lane 0 takes the
+ * next batch from *fetch when the warp is done with its last, so warps that
+ * drew short rays take more batches and none is left with a fixed share of
+ * long ones at the end.  Every lane of the warp must call it (no lane may
+ * have returned). */
+template <class F>
+__device__ __forceinline__ void for_each_queued(uint32_t n, uint32_t *fetch, F f)
+{
+	const int lane = threadIdx.x & 31;
+	for (;;) {
+		uint32_t base = 0;
+		if (lane == 0)
+			base = atomicAdd(fetch, 32u);
+		base = __shfl_sync(0xffffffffu, base, 0);
+		if (base >= n)
+			return;
+		if (base + (uint32_t)lane < n)
+			f(base + (uint32_t)lane);
+	}
+}
+
 } /* namespace kgr */
 
 #endif

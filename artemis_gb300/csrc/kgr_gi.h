@@ -29,7 +29,8 @@ struct GiFrameBuffers {
 	/* between the launches of a spatial iteration: per pixel {w_sum,
 	 * bits(domain), bits(M sum), target}; per neighbour slot (k-major,
 	 * k * npix + pixel) {neighbour pixel or -1, its M} and its weight; the
-	 * queues of visibility rays (slots) of the two rounds and their counts */
+	 * queues of visibility rays (slots) of the two rounds, their counts and
+	 * (entries 2, 3) the visibility kernels' fetch counters */
 	float4 *selection;
 	int2 *neighbours;
 	float *weights;

@@ -138,7 +138,8 @@ struct RestirFrameBuffers {
 	/* between the launches of a spatial pass: per neighbour slot (k-major,
 	 * k * npix + pixel) {neighbour pixel, M}; targets per slot, then one
 	 * row of npix for the lighting rays; the shadow-ray queues of the two
-	 * rounds (entries index targets) and their counts */
+	 * rounds (entries index targets), their counts and (entries 2, 3) the
+	 * visibility kernels' fetch counters */
 	int2 *neighbours;
 	float *targets;
 	uint32_t *vis_queue[2];

@@ -237,14 +237,13 @@ __global__ void __launch_bounds__(128) primary_kernel(DeviceScene s, PathBuffers
 __global__ void __launch_bounds__(128) primary_visibility_kernel(DeviceScene s, PathBuffers pb, FrameParams fp,
 		RestirFrameBuffers rb, int cur)
 {
-	const uint32_t n = rb.vis_count[0];
-	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+	for_each_queued(rb.vis_count[0], rb.vis_count + 2, [&](uint32_t i) {
 		uint32_t p = rb.vis_queue[0][i];
 		float4 a = pb.sh_o[p], b = pb.sh_d[p];
 		kgr_hit h;
 		if (trace<true>(s, fp.layout, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), b.w, h))
 			rb.res[cur].b[p].y = 0.0f;
-	}
+	});
 }
 
 __device__ __forceinline__ void accumulate4(float4 *buf, uint32_t i, float4 v, bool acc, float count)
@@ -350,8 +349,7 @@ __global__ void __launch_bounds__(128) temporal_gather_kernel(DeviceScene s, Fra
 __global__ void __launch_bounds__(128) temporal_visibility_kernel(DeviceScene s, FrameParams fp,
 		RestirFrameBuffers rb, OutputBuffers out, int cur, int prev)
 {
-	const uint32_t n = rb.vis_count[0];
-	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+	for_each_queued(rb.vis_count[0], rb.vis_count + 2, [&](uint32_t i) {
 		uint32_t e = rb.vis_queue[0][i];
 		bool previous = e >= fp.npix;
 		uint32_t pix = previous ? e - fp.npix : e;
@@ -362,7 +360,7 @@ __global__ void __launch_bounds__(128) temporal_visibility_kernel(DeviceScene s,
 		f3 Dn = D / d;
 		if (occluded(s, fp.layout, from, Dn, d))
 			rb.targets[e] = 0.0f;
-	}
+	});
 }
 
 __global__ void __launch_bounds__(128) temporal_merge_kernel(DeviceScene s, FrameParams fp, RestirFrameBuffers rb,
@@ -490,10 +488,9 @@ __global__ void __launch_bounds__(128) restir_gather_kernel(DeviceScene s, Frame
 __global__ void __launch_bounds__(128) restir_visibility_kernel(DeviceScene s, FrameParams fp,
 		RestirFrameBuffers rb, OutputBuffers out, int inb, int outb, int round)
 {
-	const uint32_t n = rb.vis_count[round];
 	const uint32_t *queue = rb.vis_queue[round];
 	const uint32_t lighting = (uint32_t)KGR_MAX_NEIGHBORS * fp.npix;
-	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+	for_each_queued(rb.vis_count[round], rb.vis_count + 2 + round, [&](uint32_t i) {
 		uint32_t e = queue[i];
 		uint32_t pix = e < lighting ? e % fp.npix : e - lighting;
 		f3 from, to;
@@ -510,7 +507,7 @@ __global__ void __launch_bounds__(128) restir_visibility_kernel(DeviceScene s, F
 		f3 Dn = D / d;
 		if (occluded(s, fp.layout, from, Dn, d))
 			rb.targets[e] = 0.0f;
-	}
+	});
 }
 
 /* resample: the merged reservoir over the centre and the neighbours with
@@ -634,7 +631,7 @@ void restir_primary(const DeviceScene &s, const PathBuffers &pb, const FramePara
 {
 	int grid = (int)((pb.capacity + 127) / 128);
 	int cap = device_sm_count() * 16;
-	KGR_CUDA(cudaMemsetAsync(rb.vis_count, 0, sizeof(uint32_t), st));
+	KGR_CUDA(cudaMemsetAsync(rb.vis_count, 0, 4 * sizeof(uint32_t), st));
 	primary_kernel<<<grid < cap ? grid : cap, 128, 0, st>>>(s, pb, fp, rb, cur);
 	primary_visibility_kernel<<<device_sm_count() * 8, 128, 0, st>>>(s, pb, fp, rb, cur);
 	KGR_CUDA(cudaGetLastError());
@@ -651,7 +648,7 @@ void restir_temporal(const DeviceScene &s, const FrameParams &fp, const RestirFr
 		const OutputBuffers &out, int cur, int prev, cudaStream_t st)
 {
 	unsigned grid = (fp.npix + 127) / 128;
-	KGR_CUDA(cudaMemsetAsync(rb.vis_count, 0, sizeof(uint32_t), st));
+	KGR_CUDA(cudaMemsetAsync(rb.vis_count, 0, 4 * sizeof(uint32_t), st));
 	temporal_gather_kernel<<<grid, 128, 0, st>>>(s, fp, rb, out, cur, prev);
 	temporal_visibility_kernel<<<device_sm_count() * 8, 128, 0, st>>>(s, fp, rb, out, cur, prev);
 	temporal_merge_kernel<<<grid, 128, 0, st>>>(s, fp, rb, out, cur, prev);
@@ -663,7 +660,7 @@ void restir_spatial(const DeviceScene &s, const FrameParams &fp, const RestirFra
 {
 	unsigned grid = (fp.npix + 127) / 128;
 	int vis_grid = device_sm_count() * 8;
-	KGR_CUDA(cudaMemsetAsync(rb.vis_count, 0, 2 * sizeof(uint32_t), st));
+	KGR_CUDA(cudaMemsetAsync(rb.vis_count, 0, 4 * sizeof(uint32_t), st));
 	restir_gather_kernel<<<grid, 128, 0, st>>>(s, fp, rb, out, in);
 	restir_visibility_kernel<<<vis_grid, 128, 0, st>>>(s, fp, rb, out, in, outbuf, 0);
 	restir_resample_kernel<<<grid, 128, 0, st>>>(s, fp, rb, out, in, outbuf);

@@ -7,9 +7,9 @@
  * the queue counters) lives in one file-scope __device__ array instead of
  * buffers the attachment allocates in kgr_load.  It is meant for callers that
  * cannot call cudaMalloc at render time: a host that fixes its device memory
- * at start-up (a real-time loop with a hard budget, a plugin host that owns
- * the allocator), or code that renders while a stream is being captured into
- * a CUDA graph, where allocation calls are not permitted.
+ * at start-up and owns the allocator (a real-time loop with a hard memory
+ * budget, a plugin host that hands out device memory itself), where an
+ * allocation inside the plugin would break the host's accounting or fail.
  *
  * Limits and sharing:
  *  - at most KGR_NOALLOC_MAX_PATHS (65536) paths per call, i.e.
@@ -27,7 +27,10 @@
  *    cudaGetSymbolAddress (once per device, with that device current); make
  *    that first call before any stream capture begins.
  */
+#include <math.h>
 #include <string.h>
+
+#include <cmath>
 
 #include <mutex>
 
@@ -98,8 +101,14 @@ extern "C" kgr_status kgr_render_pt_noalloc(const kgr_scene *sc, const kgr_launc
 		KGR_REQUIRE(info->max_depth >= 0 && info->max_depth <= 64, KGR_ERR_INVALID_ARGUMENT,
 			"max_depth out of range");
 		KGR_REQUIRE(spp >= 1, KGR_ERR_INVALID_ARGUMENT, "spp must be at least 1");
-		uint64_t w = (uint64_t)info->resolution[0], h = (uint64_t)info->resolution[1];
-		KGR_REQUIRE(w >= 1 && h >= 1, KGR_ERR_INVALID_ARGUMENT, "empty resolution");
+		/* validate the float extent before any conversion: a negative, NaN or
+		 * huge value has no defined unsigned conversion */
+		for (int k = 0; k < 2; k++) {
+			float r = info->resolution[k];
+			KGR_REQUIRE(std::isfinite(r) && r >= 1.0f && r <= (float)KGR_NOALLOC_MAX_PATHS && r == floorf(r),
+				KGR_ERR_INVALID_ARGUMENT, "resolution must hold whole numbers in [1, 65536]");
+		}
+		uint64_t w = (uint64_t)(uint32_t)info->resolution[0], h = (uint64_t)(uint32_t)info->resolution[1];
 		uint64_t paths = w * h * (uint64_t)spp;
 		KGR_REQUIRE(paths <= KGR_NOALLOC_MAX_PATHS, KGR_ERR_INVALID_ARGUMENT,
 			"width * height * spp = " + std::to_string(paths) + " exceeds the no-allocation limit of "

@@ -344,12 +344,14 @@ kgr_status kgr_destroy(kgr_attachment *att);
 
 /* One path-traced frame that allocates no device memory.  No counterpart in
  * the reference: it exists for callers that cannot call cudaMalloc when they
- * render -- a host that fixes its device memory at start-up, or a renderer
- * running while its stream is captured into a CUDA graph.  The same kernels
+ * render: a host that fixes its device memory at start-up and hands it out
+ * itself, where an allocation inside the plugin would break the host's
+ * accounting or fail.  The same kernels
  * as the "path_tracer" attachment (fast layout) write one frame into the
  * caller's buffers of info->buffers; the per-path scratch is a fixed array of
  * about 14.8 MiB inside the library, so width * height * spp must be at most
- * 65536 (KGR_ERR_INVALID_ARGUMENT otherwise).  All calls on a device share
+ * 65536, and each resolution component a whole number in [1, 65536]
+ * (KGR_ERR_INVALID_ARGUMENT otherwise, before anything runs).  All calls on a device share
  * that array: calls that overlap on the GPU race, so order them on one
  * stream.  The first call on a device looks up the array's address
  * (cudaGetSymbolAddress); make it before any stream capture. */

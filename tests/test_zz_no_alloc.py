@@ -1,6 +1,6 @@
 """kgr_render_pt_noalloc: a path-traced frame for callers that cannot
-allocate device memory when they render (a host that fixes its memory at
-start-up, or a stream being captured into a CUDA graph).  Its scratch is a
+allocate device memory when they render (a host that fixes its device memory
+at start-up and hands it out itself).  Its scratch is a
 fixed array inside the library, so this checks, through the C ABI, that two
 calls in a row each give the same image as the path-tracer attachment (the
 existing entry point) within the 1e-4 relative tolerance of the parity
@@ -73,6 +73,12 @@ def test_noalloc_rejects_requests_over_the_limit():
     status = kgr.lib().kgr_render_pt_noalloc(sc.handle, ctypes.byref(info), 2, 0, 3, None)
     assert status == 1
     assert b"65536" in kgr.lib().kgr_last_error()
+    # extents that are not whole numbers in [1, 65536] are refused before any
+    # conversion or launch (-256 x -256 would otherwise wrap to 65536 paths)
+    for res in ((-256.0, -256.0), (float("nan"), 16.0), (16.5, 16.0), (0.0, 8.0), (1e30, 1.0)):
+        bad = helpers.launch(cam, W, H, bufs, max_depth=3)
+        bad.resolution[0], bad.resolution[1] = res
+        assert kgr.lib().kgr_render_pt_noalloc(sc.handle, ctypes.byref(bad), 1, 0, 3, None) == 1, res
     # the largest allowed request still works after the refusal
     kgr.check(kgr.lib().kgr_render_pt_noalloc(sc.handle, ctypes.byref(info), 1, 0, 3, None))
     torch.cuda.synchronize()

@@ -45,11 +45,22 @@ inline float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 inline V3 cross(V3 a, V3 b) { return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
 inline V3 normalize(V3 a) { float inv = 1.0f / sqrtf(dot(a, a)); return a * inv; }
 
+/* three draws in x, y, z order: the order in which a function's arguments
+ * are evaluated is unspecified in C++ (GCC takes them right to left on
+ * x86-64), so multi-draw values are sequenced through here */
+V3 draw3(Rng &r, float lo, float hi)
+{
+	float x = r.uniform(lo, hi);
+	float y = r.uniform(lo, hi);
+	float z = r.uniform(lo, hi);
+	return v3(x, y, z);
+}
+
 /* uniform direction by rejection from the cube (no transcendentals) */
 V3 random_unit(Rng &r)
 {
 	for (;;) {
-		V3 v = v3(r.uniform(-1, 1), r.uniform(-1, 1), r.uniform(-1, 1));
+		V3 v = draw3(r, -1, 1);
 		float l2 = dot(v, v);
 		if (l2 > 1e-4f && l2 <= 1.0f)
 			return normalize(v);
@@ -111,12 +122,12 @@ struct Builder {
 	}
 	uint32_t lambert(Rng &r)
 	{
-		V3 kd = v3(r.uniform(0.1f, 0.9f), r.uniform(0.1f, 0.9f), r.uniform(0.1f, 0.9f));
+		V3 kd = draw3(r, 0.1f, 0.9f);
 		return material(kd, v3(0, 0, 0), v3(0, 0, 0), 1.0f, KGR_SHADING_DIFFUSE);
 	}
 	uint32_t ggx(Rng &r)
 	{
-		V3 kd = v3(r.uniform(0.05f, 0.5f), r.uniform(0.05f, 0.5f), r.uniform(0.05f, 0.5f));
+		V3 kd = draw3(r, 0.05f, 0.5f);
 		float ks = r.uniform(0.2f, 0.9f);
 		float rough = r.uniform(0.05f, 0.8f);
 		return material(kd, v3(ks, ks, ks), v3(0, 0, 0), rough, KGR_SHADING_DIFFUSE);
@@ -145,7 +156,7 @@ void gen_box4k(kgr_generated *g, uint64_t seed, int random_tris)
 		b.quad(p[faces[f][0]], p[faces[f][1]], p[faces[f][2]], p[faces[f][3]], m);
 	}
 	for (int i = 0; i < random_tris; i++) {
-		V3 c = v3(r.uniform(-1.5f, 1.5f), r.uniform(-1.5f, 1.5f), r.uniform(-1.5f, 1.5f));
+		V3 c = draw3(r, -1.5f, 1.5f);
 		V3 u = random_unit(r);
 		V3 w = random_unit(r);
 		V3 q = w - u * dot(w, u);

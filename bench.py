@@ -180,20 +180,18 @@ def make_scene(name):
     return g, sc
 
 
-def cpu_sample(g, sc, args, target_s):
+def cpu_sample(osc, cam, args, target_s):
     """Oracle PT (reference per-pixel path, all host cores) on a crop of rows
-    of the same frame, sized to about target_s seconds.  Returns
-    (Mrays/s, cores, description, ms per full frame)."""
-    from artemis_gb300 import kgr
+    of the same frame, sized to about target_s seconds.  osc is an oracle
+    Scene and cam a camera dict {center, ax_u, ax_v, ax_w}.  Returns
+    (run(rows, frame) -> (seconds, rays, rows), rows, cores)."""
     from oracle import pyoracle
-    osc = pyoracle.Scene(g.positions, g.normals, g.tris4(), g.materials_raw, sc.lights(), sc.bvh())
-    cam = kgr.camera(g.eye, g.target, g.fov, args.width / args.height)
     cores = os.cpu_count() or 1
     mid = args.height // 2
 
     def run(rows, frame=0):
         r0 = max(0, mid - rows // 2)
-        p = pyoracle.render_params(args.width, args.height, kgr.camera_dict(cam), max_depth=args.max_depth,
+        p = pyoracle.render_params(args.width, args.height, cam, max_depth=args.max_depth,
                                    spp=args.spp, russian_roulette=1, rr_start_depth=3, frame=frame,
                                    row_begin=r0, row_end=min(args.height, r0 + rows), threads=cores)
         bufs = [np.zeros((args.width * args.height, 4), np.float32) for _ in range(4)]
@@ -208,13 +206,22 @@ def cpu_sample(g, sc, args, target_s):
 
 
 def bench_reference(args):
+    """The reference arm: the oracle's restatement of the reference's
+    per-pixel path tracer on all host cores.  Everything it uses -- the
+    procedural scene, the SAH BVH (leaves <= 4), the triangle lights and the
+    camera frame -- comes from the oracle library alone (oracle/scene_ref.cpp,
+    checked bit for bit against the product's by tests/test_oracle_scene.py);
+    the product library is never loaded on this arm."""
     ws, rank, local = dist_env()
     if rank != 0:
         return
-    g, sc = make_scene_cpu(args.scene)
+    from oracle import pyoracle
+    g = pyoracle.GeneratedScene(args.scene, 1)
+    osc = g.scene(max_leaf=4)
+    cam = pyoracle.camera(g.eye, g.target, g.fov, args.width / args.height)
     # bound the whole run to about 150 s of CPU work however many steps are asked
     per_step = min(args.cpu_seconds, 150.0 / max(1, args.steps + args.warmup))
-    run, rows, cores = cpu_sample(g, sc, args, per_step)
+    run, rows, cores = cpu_sample(osc, cam, args, per_step)
     for _ in range(args.warmup):
         run(max(4, rows // 8))
     times, rays_total, rows_done = [], 0, 0
@@ -229,35 +236,15 @@ def bench_reference(args):
     line = {"metric": METRIC, "value": round(mrays, 4), "unit": "Mrays/s", "impl": "reference",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(ms_frame, 2), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-            "config": {"workload": WORKLOAD, "crop": sample, "l2_flush": False},
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene, random-free camera)",
+            "config": {"workload": WORKLOAD, "scene": args.scene, "triangles": int(len(g.indices)),
+                       "lights": int(len(osc.lights)), "resolution": [args.width, args.height], "spp": args.spp,
+                       "max_depth": args.max_depth, "crop": sample, "l2_flush": False,
+                       "parallelism": f"{cores} host threads (OpenMP over pixels)"},
             "cpu_baseline": {"value": round(mrays, 4), "unit": "Mrays/s", "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(mrays, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
-
-
-def make_scene_cpu(name):
-    """Scene arrays and BVH without a device (the reference arm runs on CPU)."""
-    from artemis_gb300 import kgr
-
-    class CpuScene:
-        def __init__(self, g):
-            self._bvh = kgr.bvh_build_host(g.positions, g.indices, kgr.BUILDER_SAH, 4)
-            em = g.materials["emission"][g.material_indices]
-            lit = np.nonzero(em.max(axis=1) > 0)[0]
-            p = g.positions[g.indices[lit]]
-            self._lights = np.concatenate([p[:, 0], p[:, 1] - p[:, 0], p[:, 2] - p[:, 0], em[lit]],
-                                          axis=1).astype(np.float32)
-
-        def bvh(self):
-            return self._bvh
-
-        def lights(self):
-            return self._lights
-
-    g = kgr.Generated(name, 1)
-    return g, CpuScene(g)
 
 
 def relmse_compare(args, scene_name, g, sc, W, H, stream, sptr):
@@ -810,7 +797,9 @@ def bench_ours(args):
     cpu_base = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
-            run, rows, cores = cpu_sample(g, sc, args, args.cpu_seconds)
+            from oracle import pyoracle
+            osc = pyoracle.Scene(g.positions, g.normals, g.tris4(), g.materials_raw, sc.lights(), sc.bvh())
+            run, rows, cores = cpu_sample(osc, kgr.camera_dict(cam), args, args.cpu_seconds)
             dt, crays, r = run(rows)
             cpu_base = {"value": round(crays / dt / 1e6, 4), "unit": "Mrays/s", "cores": cores, "kind": "port",
                         "sample": f"{r} centre rows x {W} px x {args.spp} spp ({dt:.1f} s)"}

@@ -158,6 +158,39 @@ void oracle_kat_math(const float *x, int n, float *sin_cos_tan_atan_acos);
  * bottom to top, packed as to_ui32 (cast.cuh:16-20). */
 void oracle_tonemap(const float *hdr, uint32_t *ldr, uint32_t width, uint32_t height, int mode);
 
+/* ---- scene inputs of the CPU reference arm (scene_ref.cpp) ---- */
+
+/* Seeded procedural scene: "box4k", "box64", "terrain", "terrain_s",
+ * "terrain_m", "terrain_l".  Returns 0, or -1 for an unknown name. */
+typedef struct oracle_generated oracle_generated;
+typedef struct oracle_scene_arrays {
+	const float *positions;          /* 3 * vertex_count */
+	const float *normals;            /* 3 * vertex_count */
+	const uint32_t *indices;         /* 3 * triangle_count */
+	const uint32_t *material_indices; /* triangle_count */
+	const kgr_material *materials;
+	uint32_t vertex_count, triangle_count, material_count;
+	float eye[3], target[3], fov_deg;
+} oracle_scene_arrays;
+int oracle_generate_scene(const char *name, uint64_t seed, oracle_generated **out);
+void oracle_generated_view(const oracle_generated *g, oracle_scene_arrays *view);
+void oracle_generated_destroy(oracle_generated *g);
+
+/* Binned-SAH BVH with leaves of at most max_leaf triangles, in the threaded
+ * bvh.cpp layout (one record per leaf triangle).  With out_vec4 = NULL it
+ * returns the vec4 count; else -1 if capacity is too small. */
+int64_t oracle_build_sah(const float *positions, const uint32_t *indices, uint32_t triangle_count, int max_leaf,
+		float *out_vec4, uint64_t capacity);
+
+/* Triangle lights of the emissive triangles in triangle order; returns the
+ * count (out may be NULL to count). */
+uint32_t oracle_scene_lights(const float *positions, const uint32_t *indices, const uint32_t *material_indices,
+		uint32_t triangle_count, const kgr_material *materials, kgr_triangle_light *out);
+
+/* Pinhole camera frame of uvw_frame (include/camera.hpp:45-63). */
+void oracle_camera(const float eye[3], const float target[3], const float up[3], float fov_deg, float aspect,
+		float center[3], float ax_u[3], float ax_v[3], float ax_w[3]);
+
 #ifdef __cplusplus
 }
 #endif

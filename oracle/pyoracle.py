@@ -46,6 +46,14 @@ class RenderParams(ctypes.Structure):
                 ("row_end", ctypes.c_uint32), ("threads", ctypes.c_int32)]
 
 
+class SceneArrays(ctypes.Structure):
+    _fields_ = [("positions", ctypes.c_void_p), ("normals", ctypes.c_void_p), ("indices", ctypes.c_void_p),
+                ("material_indices", ctypes.c_void_p), ("materials", ctypes.c_void_p),
+                ("vertex_count", ctypes.c_uint32), ("triangle_count", ctypes.c_uint32),
+                ("material_count", ctypes.c_uint32), ("eye", ctypes.c_float * 3), ("target", ctypes.c_float * 3),
+                ("fov_deg", ctypes.c_float)]
+
+
 class RenderStats(ctypes.Structure):
     _fields_ = [("camera_rays", ctypes.c_uint64), ("bounce_rays", ctypes.c_uint64),
                 ("shadow_rays", ctypes.c_uint64)]
@@ -122,6 +130,15 @@ def lib():
                                        ctypes.POINTER(GiStateC), vp, vp, ctypes.POINTER(RenderStats)]
         L.oracle_kat_rng.argtypes = [ctypes.c_float] * 3 + [ctypes.c_int, vp]
         L.oracle_tonemap.argtypes = [vp, vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int]
+        L.oracle_generate_scene.restype = ctypes.c_int
+        L.oracle_generate_scene.argtypes = [ctypes.c_char_p, ctypes.c_uint64, ctypes.POINTER(vp)]
+        L.oracle_generated_view.argtypes = [vp, ctypes.POINTER(SceneArrays)]
+        L.oracle_generated_destroy.argtypes = [vp]
+        L.oracle_build_sah.restype = ctypes.c_int64
+        L.oracle_build_sah.argtypes = [vp, vp, ctypes.c_uint32, ctypes.c_int, vp, ctypes.c_uint64]
+        L.oracle_scene_lights.restype = ctypes.c_uint32
+        L.oracle_scene_lights.argtypes = [vp, vp, vp, ctypes.c_uint32, vp, vp]
+        L.oracle_camera.argtypes = [vp, vp, vp, ctypes.c_float, ctypes.c_float, vp, vp, vp, vp]
         L.oracle_kat_intersect.restype = ctypes.c_float
         L.oracle_kat_intersect.argtypes = [vp] * 6
         L.oracle_kat_sample_light.argtypes = [vp] * 4
@@ -260,6 +277,67 @@ def render_restir(scene, params, state, bufs=None):
     lib().oracle_render_restir(ctypes.byref(scene.c), ctypes.byref(params), ctypes.byref(state.c),
                                *[ptr(b) for b in bufs], ctypes.byref(st))
     return bufs, st
+
+
+class GeneratedScene:
+    """A seeded procedural scene generated by the oracle's own generator
+    (scene_ref.cpp), with the same fields as the product's generated scenes:
+    positions, normals (V,3) float32; indices (T,3) and material_indices (T,)
+    uint32; materials_raw (M,16) float32; eye, target, fov."""
+
+    def __init__(self, name, seed):
+        h = ctypes.c_void_p()
+        if lib().oracle_generate_scene(name.encode(), seed, ctypes.byref(h)) != 0:
+            raise ValueError(f"unknown procedural scene: {name}")
+        try:
+            v = SceneArrays()
+            lib().oracle_generated_view(h, ctypes.byref(v))
+            V, T, M = v.vertex_count, v.triangle_count, v.material_count
+
+            def arr(addr, ctype, n):
+                return np.ctypeslib.as_array((ctype * n).from_address(addr)).copy()
+            self.positions = arr(v.positions, ctypes.c_float, 3 * V).reshape(V, 3)
+            self.normals = arr(v.normals, ctypes.c_float, 3 * V).reshape(V, 3)
+            self.indices = arr(v.indices, ctypes.c_uint32, 3 * T).reshape(T, 3)
+            self.material_indices = arr(v.material_indices, ctypes.c_uint32, T)
+            self.materials_raw = arr(v.materials, ctypes.c_float, 16 * M).reshape(M, 16)
+            self.eye = np.array(v.eye[:], np.float32)
+            self.target = np.array(v.target[:], np.float32)
+            self.fov = float(v.fov_deg)
+        finally:
+            lib().oracle_generated_destroy(h)
+
+    def tris4(self):
+        return np.concatenate([self.indices, self.material_indices[:, None]], axis=1).astype(np.uint32)
+
+    def sah_bvh(self, max_leaf=4):
+        """Threaded bvh.cpp-layout buffer of the oracle's SAH builder."""
+        pos, idx = self.positions, np.ascontiguousarray(self.indices)
+        n = lib().oracle_build_sah(ptr(pos), ptr(idx), len(idx), max_leaf, None, 0)
+        out = np.zeros((n, 4), np.float32)
+        assert lib().oracle_build_sah(ptr(pos), ptr(idx), len(idx), max_leaf, ptr(out), n) == n
+        return out
+
+    def lights(self):
+        args = [ptr(self.positions), ptr(np.ascontiguousarray(self.indices)), ptr(self.material_indices),
+                len(self.indices), ptr(self.materials_raw)]
+        n = lib().oracle_scene_lights(*args, None)
+        out = np.zeros((n, 12), np.float32)
+        lib().oracle_scene_lights(*args, ptr(out))
+        return out
+
+    def scene(self, max_leaf=4):
+        return Scene(self.positions, self.normals, self.tris4(), self.materials_raw, self.lights(),
+                     self.sah_bvh(max_leaf))
+
+
+def camera(eye, target, fov, aspect, up=(0.0, 1.0, 0.0)):
+    """{center, ax_u, ax_v, ax_w} of uvw_frame (include/camera.hpp:45-63)."""
+    e, t, u = (np.ascontiguousarray(x, np.float32) for x in (eye, target, up))
+    c, U, V, W = (np.zeros(3, np.float32) for _ in range(4))
+    lib().oracle_camera(ptr(e), ptr(t), ptr(u), fov, aspect, ptr(c), ptr(U), ptr(V), ptr(W))
+    return {"center": c.tolist(), "ax_u": U.tolist(), "ax_v": V.tolist(), "ax_w": W.tolist(),
+            "projection": [0.0] * 16, "view": [0.0] * 16}
 
 
 def tonemap(hdr, mode=0):

@@ -1250,8 +1250,7 @@ void render_restir_di(kgr_attachment *att, const kgr_launch_info *info, const kg
 	launches++;
 	/* temporal pass */
 	if (fp.temporal) {
-		restir_temporal(s, fp, rb, out, cur, prev, st);
-		att->mark(STAGE_RESTIR_TEMPORAL, st);
+		restir_temporal(s, fp, rb, out, cur, prev, st, [&](int k) { att->mark(k, st); });
 		launches += 3;
 	}
 	/* spatial passes with the ping-pong of restir.cuh:280-300 */
@@ -1259,8 +1258,7 @@ void render_restir_di(kgr_attachment *att, const kgr_launch_info *info, const kg
 	KGR_REQUIRE(passes >= 0 && passes <= 16, KGR_ERR_INVALID_ARGUMENT, "spatial_passes must be 0..16");
 	int in = cur, outb = prev;
 	for (int k = 0; k < passes; k++) {
-		restir_spatial(s, fp, rb, out, in, outb, st);
-		att->mark(STAGE_RESTIR_SPATIAL, st);
+		restir_spatial(s, fp, rb, out, in, outb, st, [&](int k) { att->mark(k, st); });
 		std::swap(in, outb);
 		launches += KGR_RESTIR_SPATIAL_LAUNCHES;
 	}

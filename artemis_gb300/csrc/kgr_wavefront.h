@@ -10,6 +10,8 @@
 #ifndef KGR_WAVEFRONT_H_
 #define KGR_WAVEFRONT_H_
 
+#include <functional>
+
 #include "kgr_internal.h"
 
 namespace kgr {
@@ -60,8 +62,16 @@ enum StageKind {
 	STAGE_RESTIR_FINALIZE = 8,
 	STAGE_CACHE_INFER = 9,  /* radiance-cache query + network + apply */
 	STAGE_CACHE_TRAIN = 10, /* training paths + targets + gradient + Adam */
-	STAGE_COUNT = 11
+	/* the reuse passes' queued visibility rays; stages 6 and 7 then hold
+	 * only their resampling kernels (gather, resample/merge, finish) */
+	STAGE_RESTIR_TEMPORAL_VIS = 11,
+	STAGE_RESTIR_SPATIAL_VIS = 12,
+	STAGE_COUNT = 13
 };
+
+/* Called after each launch of a multi-kernel pass with the stage it belongs
+ * to (the attachment's per-launch event timing); may be empty. */
+typedef std::function<void(int)> StageMark;
 
 /* Streaming read of a buffer with 16-byte loads (bandwidth probe). */
 void launch_read_probe(const float4 *buf, size_t n, float4 *sink, int iters, cudaStream_t st);
@@ -176,9 +186,9 @@ void restir_primary(const DeviceScene &s, const PathBuffers &pb, const FramePara
 void restir_finalize(const PathBuffers &pb, const FrameParams &fp, const RestirFrameBuffers &rb,
 		const OutputBuffers &out, cudaStream_t st);
 void restir_temporal(const DeviceScene &s, const FrameParams &fp, const RestirFrameBuffers &rb,
-		const OutputBuffers &out, int cur, int prev, cudaStream_t st);
+		const OutputBuffers &out, int cur, int prev, cudaStream_t st, const StageMark &mark = StageMark());
 void restir_spatial(const DeviceScene &s, const FrameParams &fp, const RestirFrameBuffers &rb,
-		const OutputBuffers &out, int in, int outbuf, cudaStream_t st);
+		const OutputBuffers &out, int in, int outbuf, cudaStream_t st, const StageMark &mark = StageMark());
 
 int device_sm_count();
 

@@ -645,27 +645,43 @@ void restir_finalize(const PathBuffers &pb, const FrameParams &fp, const RestirF
 }
 
 void restir_temporal(const DeviceScene &s, const FrameParams &fp, const RestirFrameBuffers &rb,
-		const OutputBuffers &out, int cur, int prev, cudaStream_t st)
+		const OutputBuffers &out, int cur, int prev, cudaStream_t st, const StageMark &mark)
 {
 	unsigned grid = (fp.npix + 127) / 128;
+	auto done = [&](int stage) {
+		if (mark)
+			mark(stage);
+	};
 	KGR_CUDA(cudaMemsetAsync(rb.vis_count, 0, 4 * sizeof(uint32_t), st));
 	temporal_gather_kernel<<<grid, 128, 0, st>>>(s, fp, rb, out, cur, prev);
+	done(STAGE_RESTIR_TEMPORAL);
 	temporal_visibility_kernel<<<device_sm_count() * 8, 128, 0, st>>>(s, fp, rb, out, cur, prev);
+	done(STAGE_RESTIR_TEMPORAL_VIS);
 	temporal_merge_kernel<<<grid, 128, 0, st>>>(s, fp, rb, out, cur, prev);
+	done(STAGE_RESTIR_TEMPORAL);
 	KGR_CUDA(cudaGetLastError());
 }
 
 void restir_spatial(const DeviceScene &s, const FrameParams &fp, const RestirFrameBuffers &rb,
-		const OutputBuffers &out, int in, int outbuf, cudaStream_t st)
+		const OutputBuffers &out, int in, int outbuf, cudaStream_t st, const StageMark &mark)
 {
 	unsigned grid = (fp.npix + 127) / 128;
 	int vis_grid = device_sm_count() * 8;
+	auto done = [&](int stage) {
+		if (mark)
+			mark(stage);
+	};
 	KGR_CUDA(cudaMemsetAsync(rb.vis_count, 0, 4 * sizeof(uint32_t), st));
 	restir_gather_kernel<<<grid, 128, 0, st>>>(s, fp, rb, out, in);
+	done(STAGE_RESTIR_SPATIAL);
 	restir_visibility_kernel<<<vis_grid, 128, 0, st>>>(s, fp, rb, out, in, outbuf, 0);
+	done(STAGE_RESTIR_SPATIAL_VIS);
 	restir_resample_kernel<<<grid, 128, 0, st>>>(s, fp, rb, out, in, outbuf);
+	done(STAGE_RESTIR_SPATIAL);
 	restir_visibility_kernel<<<vis_grid, 128, 0, st>>>(s, fp, rb, out, in, outbuf, 1);
+	done(STAGE_RESTIR_SPATIAL_VIS);
 	restir_finish_kernel<<<grid, 128, 0, st>>>(s, fp, rb, out, in, outbuf);
+	done(STAGE_RESTIR_SPATIAL);
 	KGR_CUDA(cudaGetLastError());
 }
 

@@ -599,7 +599,8 @@ class Attachment:
         return t.as_dict()
 
     STAGES = ("generate", "trace_closest", "shade", "shadow", "accumulate", "restir_primary",
-              "restir_temporal", "restir_spatial", "restir_finalize", "cache_infer", "cache_train")
+              "restir_temporal", "restir_spatial", "restir_finalize", "cache_infer", "cache_train",
+              "restir_temporal_vis", "restir_spatial_vis")
 
     def stage_times(self):
         """{stage: (total ms, launches)} since the last call ("profile" option)."""

@@ -412,24 +412,78 @@ def restir_runs(args):
         e1.synchronize()
         return e0.elapsed_time(e1)
 
-    # --- ReSTIR DI, 256^2
+    # --- ReSTIR DI, 256^2 (and the same scene at 1080p for the resampling roofline)
     g = kgr.Generated("box4k", 0x4B4F4252)
     sc = kgr.Scene.from_generated(g)
-    W = H = 256
-    cam = kgr.camera(g.eye, g.target, g.fov, 1.0)
-    bufs = [torch.zeros((W * H, 4), dtype=torch.float32, device="cuda") for _ in range(4)]
     opts = {"candidates": 32, "temporal": True, "temporal_mcap": 20, "spatial_passes": 1,
             "spatial_neighbors": 5, "spatial_radius": 30}
-    att = kgr.Attachment("restir_di")
-    att.attach(W, H)
-    att.load()
-    for k, v in opts.items():
-        att.set_option(k, v)
-    info = lambda f: kgr.launch_info(cam, W, H, [b.data_ptr() for b in bufs], max_depth=2, frame=f)
-    for f in range(5):
-        att.render(info(f), sc, sptr)
-    ms = [timed(lambda f=f: att.render(info(5 + f), sc, sptr)) for f in range(20)]
-    att.close()
+    k_nb, passes = opts["spatial_neighbors"], opts["spatial_passes"]
+    l2_gbs = kgr.read_bandwidth(64 << 20, 50)
+    hbm = measured_peaks()[0].get("hbm_gbs")
+
+    def di_run(W, H, timed_frames):
+        cam = kgr.camera(g.eye, g.target, g.fov, W / H)
+        bufs = [torch.zeros((W * H, 4), dtype=torch.float32, device="cuda") for _ in range(4)]
+        att = kgr.Attachment("restir_di")
+        att.attach(W, H)
+        att.load()
+        for k, v in opts.items():
+            att.set_option(k, v)
+        info = lambda f: kgr.launch_info(cam, W, H, [b.data_ptr() for b in bufs], max_depth=2, frame=f)
+        for f in range(5):
+            att.render(info(f), sc, sptr)
+        ms = [timed(lambda f=f: att.render(info(5 + f), sc, sptr)) for f in range(timed_frames)]
+        # per-stage CUDA-event times of further frames: the resampling
+        # kernels apart from the reuse passes' visibility rays
+        att.set_option("profile", True)
+        att.stage_times()
+        nprof = 10
+        for f in range(nprof):
+            att.render(info(5 + timed_frames + f), sc, sptr)
+        stages = att.stage_times()
+        att.set_option("profile", False)
+        frame = bufs[0][:, :3].double().clone()
+        att.close()
+        npix = W * H
+        # algorithmic bytes per pixel per pass: temporal = two 32 B reservoir
+        # reads + a 32 B write + 48 B of G-buffer; spatial = (1 + k)(32 + 48) B
+        # + a 32 B write
+        temporal_b = npix * (2 * 32 + 32 + 48)
+        spatial_b = npix * ((1 + k_nb) * (32 + 48) + 32) * passes
+        entry = {"resolution": [W, H], "gpu_ms_per_frame": round(float(np.median(ms)), 3)}
+        for name, stage, nbytes in (("temporal", "restir_temporal", temporal_b),
+                                    ("spatial", "restir_spatial", spatial_b)):
+            t_ms = stages[stage][0] / nprof
+            gbs = nbytes / (t_ms * 1e-3) / 1e9
+            entry[name] = {"kernels_ms_per_frame": round(t_ms, 4), "bytes_per_frame": nbytes,
+                           "achieved_gbs": round(gbs, 1), "l2_frac": round(gbs / l2_gbs, 4),
+                           "hbm_frac": round(gbs / hbm, 4) if hbm else None,
+                           "visibility_ms_per_frame": round(stages[stage + "_vis"][0] / nprof, 4)}
+        return cam, frame, entry
+
+    cam, di_frame, di256 = di_run(256, 256, 20)
+    # relMSE of the ReSTIR DI frame against an FP64 mean of 4096 spp of the
+    # plain tracer at the same depth (direct + one indirect bounce)
+    W = H = 256
+    bufs = [torch.zeros((W * H, 4), dtype=torch.float32, device="cuda") for _ in range(4)]
+    ref = torch.zeros((W * H, 3), dtype=torch.float64, device="cuda")
+    a = kgr.Attachment("path_tracer")
+    a.attach(W, H)
+    a.load()
+    a.set_option("spp", 64)
+    for f in range(64):
+        a.render(kgr.launch_info(cam, W, H, [b.data_ptr() for b in bufs], max_depth=2, frame=1 << 20 | f), sc, sptr)
+        ref += bufs[0][:, :3].double()
+    ref /= 64
+    a.set_option("spp", 1)
+    a.render(kgr.launch_info(cam, W, H, [b.data_ptr() for b in bufs], max_depth=2, frame=4242), sc, sptr)
+    plain1 = bufs[0][:, :3].double().clone()
+    a.close()
+
+    def relmse_di(x):
+        d = x - ref
+        return round((d * d / (ref * ref + 1e-2)).mean().item(), 4)
+
     osc = pyoracle.Scene(g.positions, g.normals, g.tris4(), g.materials_raw, sc.lights(), sc.bvh())
     state = pyoracle.RestirBuffers(W * H)
     t0 = time.perf_counter()
@@ -437,9 +491,18 @@ def restir_runs(args):
                                temporal_mcap=20, spatial_passes=1, spatial_neighbors=5, spatial_radius=30)
     pyoracle.render_restir(osc, p, state)
     cpu_s = time.perf_counter() - t0
-    out["restir_di_256"] = {"gpu_ms_per_frame": round(float(np.median(ms)), 3),
+    _, _, di1080 = di_run(1920, 1080, 10)
+    out["restir_di_256"] = {"gpu_ms_per_frame": di256["gpu_ms_per_frame"],
                             "cpu_oracle_ms_per_frame": round(cpu_s * 1e3, 1), "cpu_cores": os.cpu_count(),
-                            "scene_triangles": sc.info().triangle_count}
+                            "scene_triangles": sc.info().triangle_count,
+                            "relmse": relmse_di(di_frame), "plain_1spp_relmse": relmse_di(plain1),
+                            "relmse_reference": "plain PT at depth 2, 4096 spp, FP64 mean, same camera"}
+    out["roofline_resampling"] = {
+        "bound": "l2", "unit": "GB/s", "peak_l2_read_gbs": round(l2_gbs, 1), "peak_hbm_gbs": hbm,
+        "work_unit": "per pixel per pass: temporal 2x32 + 32 + 48 B; spatial (1+k)(32+48) + 32 B, k = 5",
+        "timing": "CUDA events after each launch on the render stream; resampling kernels only (temporal gather "
+                  "and merge; spatial gather, resample and finish), the reuse passes' visibility rays apart",
+        "c1_256": di256, "box_1080p": di1080}
     sc.close()
 
     # --- ReSTIR GI, 1080p, 16-frame orbit
@@ -743,12 +806,17 @@ def bench_ours(args):
 
     peaks, peak_kind = measured_peaks()
     l2_gbs = kgr.read_bandwidth(64 << 20, 50, dev)
-    # dominant traversal stage and its algorithmic bytes per launch: the
-    # reference walk's reads for the same rays (threaded bvh.cpp layout: 48 B
-    # per interior record; 16 B leaf header + 64 B triangle = index vec4 and
-    # three position vec4s per leaf record), divided by the timed kernel's
-    # per-launch CUDA-event time.  `own_layout` gives the bytes the timed
-    # layout itself reads (fast: 64 B child-pair node, 48 B triangle record).
+    # Dominant traversal stage and its algorithmic bytes per launch.  The
+    # kernel's own layout fixes what one visit must read (fast BVH2: a 64 B
+    # child-pair node per interior visit, a 48 B triangle record per test;
+    # wide BVH4: 128 B nodes), times the visits the kernel itself makes
+    # (visit counts of one counting frame), divided by the timed kernel's
+    # per-launch CUDA-event time.  Its working set (nodes + triangle records,
+    # about 80 MB at this workload) stays in the 129 MB L2, so the bound is
+    # the L2 read bandwidth measured here by kgr_measure_read_bandwidth.
+    # The bytes of the reference's threaded walk over the same rays (48 B per
+    # interior record, 80 B per leaf record; 3.5x more visits) are kept as a
+    # labelled extra, not as the fraction.
     def stage_bytes(v, node_b, tri_b):
         return {"trace_closest": v[0] * node_b + v[1] * tri_b, "shadow": v[2] * node_b + v[3] * tri_b}
 
@@ -763,20 +831,26 @@ def bench_ours(args):
     ms_dom, n_dom = stages[dom]
     launches_frame = n_dom / max(1, args.steps)
     launch_s = ms_dom / max(1, n_dom) * 1e-3
-    achieved = ref_bytes[dom] / max(1, launches_frame) / launch_s / 1e9
     own = own_bytes[dom] / max(1, launches_frame) / launch_s / 1e9
+    ref_walk = ref_bytes[dom] / max(1, launches_frame) / launch_s / 1e9
     hbm = peaks.get("hbm_gbs")
-    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-                "frac": round(achieved / hbm, 4), "traffic": TRAFFIC.get((dom, layout)),
-                "kernel": KERNELS.get((dom, layout), dom), "peak_source": peak_kind,
-                "work_unit": "reference threaded walk: 48 B per interior record, 80 B per leaf record",
-                "note": ("achieved counts the bytes the reference's threaded walk reads for the same rays; "
-                         "this kernel's ordered, culled walk visits about 3.5x fewer nodes of its own layout "
-                         "(visits_per_frame), whose bytes give own_layout; the working set is L2-resident, "
-                         "so the L2 read bandwidth measured here (l2) is the ceiling that applies"),
-                "l2": {"peak_measured_read_gbs": round(l2_gbs, 1), "frac": round(achieved / l2_gbs, 4)},
-                "own_layout": {"achieved": round(own, 1), "l2_frac": round(own / l2_gbs, 4),
-                               "hbm_frac": round(own / hbm, 4)},
+    traffic = TRAFFIC.get((dom, layout))
+    roofline = {"bound": "l2", "achieved": round(own, 1), "peak": round(l2_gbs, 1), "unit": "GB/s",
+                "frac": round(own / l2_gbs, 4), "traffic": traffic,
+                "kernel": KERNELS.get((dom, layout), dom),
+                "peak_source": "L2 read bandwidth measured in this run by kgr_measure_read_bandwidth: a 64 MB "
+                               "buffer read 50 times with 16-byte L2-cached loads, best of 5, CUDA events",
+                "work_unit": f"{layout} layout: {LAYOUT_BYTES[layout][0]} B per node visit, "
+                             f"{LAYOUT_BYTES[layout][1]} B per triangle test, visits counted by the kernel",
+                "bytes_per_launch": int(own_bytes[dom] / max(1, launches_frame)),
+                "launch_ms": round(launch_s * 1e3, 4),
+                "hbm": {"peak": hbm, "peak_source": peak_kind, "frac": round(own / hbm, 4) if hbm else None,
+                        "dram_traffic_frac_of_algorithmic": round(traffic / (own_bytes[dom] / max(1, launches_frame)), 4)
+                        if traffic else None},
+                "reference_walk": {"achieved": round(ref_walk, 1), "l2_frac": round(ref_walk / l2_gbs, 4),
+                                   "note": "bytes the reference's threaded walk would read for the same rays "
+                                           "(48 B per interior record, 80 B per leaf record); it makes about "
+                                           "3.5x more visits than this kernel, so this is not a roofline"},
                 "visits_per_frame": {"reference": list(visits["threaded"]), layout: list(visits[layout])}}
 
     quality = quality_terrain = None

@@ -373,8 +373,11 @@ kgr_status kgr_get_render_stats(const kgr_attachment *att, kgr_render_stats *sta
  * after every launch, and the time between consecutive events is charged to
  * the stage that launched.  Stages: 0 generate, 1 closest-hit traversal,
  * 2 shade, 3 shadow rays (any-hit traversal + resolve), 4 accumulate,
- * 5 ReSTIR RIS, 6 temporal, 7 spatial, 8 ReSTIR finalise.  Synchronises on
- * the last event, then resets the totals. */
+ * 5 ReSTIR RIS, 6 temporal resampling (gather and merge kernels),
+ * 7 spatial resampling (gather, resample and finish kernels), 8 ReSTIR
+ * finalise, 9 radiance-cache inference, 10 radiance-cache training,
+ * 11 temporal-reuse visibility rays, 12 spatial-reuse visibility rays.
+ * Synchronises on the last event, then resets the totals. */
 kgr_status kgr_get_stage_times(kgr_attachment *att, double *ms, uint32_t *launches, uint32_t count);
 
 /* ------------------------------------------------------------- autotuner -- */

@@ -44,7 +44,8 @@ void kgr_batcher::render(const kgr_scene *scene, const kgr_batch_job *jobs, uint
 	KGR_REQUIRE(n >= 1 && n <= max_jobs, KGR_ERR_INVALID_ARGUMENT, "job count must be 1..max_jobs");
 	KGR_REQUIRE(jobs, KGR_ERR_INVALID_ARGUMENT, "NULL job list");
 	KGR_REQUIRE(opt.max_depth >= 0 && opt.max_depth <= 64, KGR_ERR_INVALID_ARGUMENT, "max_depth must be 0..64");
-	KGR_REQUIRE(opt.layout == KGR_LAYOUT_FAST || opt.layout == KGR_LAYOUT_THREADED || opt.layout == KGR_LAYOUT_WIDE,
+	KGR_REQUIRE(opt.layout == KGR_LAYOUT_FAST || opt.layout == KGR_LAYOUT_THREADED || opt.layout == KGR_LAYOUT_WIDE
+			|| opt.layout == KGR_LAYOUT_CW8,
 		KGR_ERR_INVALID_ARGUMENT,
 		"unknown layout");
 

@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <functional>
 
+#include "kgr_cw8.h"
 #include "kgr_internal.h"
 
 namespace kgr {
@@ -770,6 +771,171 @@ void build_wide(const Tree &tree, std::vector<WideNode> &nodes, uint32_t &max_st
 		return me;
 	};
 	emit(0, max_stack);
+}
+
+/* ======================================================== compressed == */
+
+bool build_cw8(const Tree &tree, const std::vector<float4> &fast_tris, std::vector<CwNode> &nodes,
+		std::vector<float4> &cw_tris, uint32_t &depth, std::vector<int32_t> *kids_out)
+{
+	nodes.clear();
+	cw_tris.clear();
+	depth = 0;
+	if (kids_out)
+		kids_out->clear();
+	if (tree.nodes.empty())
+		return false;
+	for (const TreeNode &n : tree.nodes)
+		if (n.count > 4)
+			return false;
+	/* walk rank of every leaf's first triangle: the fast layout emits
+	 * leaves depth-first, left child first */
+	std::vector<uint32_t> first_record(tree.nodes.size(), 0);
+	{
+		uint32_t next = 0;
+		std::vector<int32_t> st(1, 0);
+		while (!st.empty()) {
+			int32_t i = st.back();
+			st.pop_back();
+			const TreeNode &n = tree.nodes[i];
+			if (n.count) {
+				first_record[i] = next;
+				next += (uint32_t)n.count;
+			} else {
+				st.push_back(n.right);
+				st.push_back(n.left);
+			}
+		}
+	}
+	struct Job {
+		int32_t tree_node; /* a tree node whose children the compressed node gathers (or a root leaf) */
+		uint32_t index;
+		uint32_t level;
+	};
+	std::vector<Job> queue;
+	queue.push_back({0, 0, 1});
+	nodes.push_back(CwNode());
+	if (kids_out)
+		kids_out->assign(8, -1);
+	for (size_t qi = 0; qi < queue.size(); qi++) {
+		Job job = queue[qi];
+		depth = job.level > depth ? job.level : depth;
+		const TreeNode &tn = tree.nodes[job.tree_node];
+		/* gather: a root leaf is the node's only child; otherwise open the
+		 * largest-area interior child until eight children */
+		std::vector<int32_t> kids;
+		if (tn.count) {
+			kids.push_back(job.tree_node);
+		} else {
+			kids.push_back(tn.left);
+			kids.push_back(tn.right);
+			while (kids.size() < 8) {
+				int best = -1;
+				float best_area = -1.0f;
+				for (size_t k = 0; k < kids.size(); k++) {
+					const TreeNode &c = tree.nodes[kids[k]];
+					if (c.count)
+						continue;
+					float a = surface_area(c.bmin, c.bmax);
+					if (a > best_area) {
+						best_area = a;
+						best = (int)k;
+					}
+				}
+				if (best < 0)
+					break;
+				const TreeNode &c = tree.nodes[kids[best]];
+				int32_t l = c.left, r = c.right;
+				kids[best] = l;
+				kids.insert(kids.begin() + best + 1, r);
+			}
+		}
+		int nk = (int)kids.size();
+		/* slots: the child whose centroid lies furthest back along an
+		 * octant's direction goes to that octant's slot (greedy over the
+		 * cheapest (child, slot) pairs), so that a ray of octant o meets
+		 * slot o first */
+		float cen[8][3], node_c[3] = {0, 0, 0};
+		float bmn[3] = {INFINITY, INFINITY, INFINITY}, bmx[3] = {-INFINITY, -INFINITY, -INFINITY};
+		for (int k = 0; k < nk; k++) {
+			const TreeNode &c = tree.nodes[kids[k]];
+			for (int a = 0; a < 3; a++) {
+				cen[k][a] = (c.bmin[a] + c.bmax[a]) * 0.5f;
+				bmn[a] = c.bmin[a] < bmn[a] ? c.bmin[a] : bmn[a];
+				bmx[a] = c.bmax[a] > bmx[a] ? c.bmax[a] : bmx[a];
+			}
+		}
+		for (int a = 0; a < 3; a++)
+			node_c[a] = (bmn[a] + bmx[a]) * 0.5f;
+		int slot_of[8] = {-1, -1, -1, -1, -1, -1, -1, -1}, kid_in[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
+		{
+			struct Pair {
+				float cost;
+				int kid, slot;
+			};
+			std::vector<Pair> pairs;
+			for (int k = 0; k < nk; k++)
+				for (int sl = 0; sl < 8; sl++) {
+					float dx = (sl & 1) ? -1.0f : 1.0f, dy = (sl & 2) ? -1.0f : 1.0f, dz = (sl & 4) ? -1.0f : 1.0f;
+					float cost = (cen[k][0] - node_c[0]) * dx + (cen[k][1] - node_c[1]) * dy
+						+ (cen[k][2] - node_c[2]) * dz;
+					pairs.push_back({cost, k, sl});
+				}
+			std::stable_sort(pairs.begin(), pairs.end(), [](const Pair &x, const Pair &y) { return x.cost < y.cost; });
+			for (const Pair &pr : pairs)
+				if (slot_of[pr.kid] < 0 && kid_in[pr.slot] < 0) {
+					slot_of[pr.kid] = pr.slot;
+					kid_in[pr.slot] = pr.kid;
+				}
+		}
+		/* internal children: consecutive nodes in slot order; leaves: their
+		 * triangle records in slot order */
+		uint32_t first_child = (uint32_t)nodes.size(), first_tri = (uint32_t)(cw_tris.size() / 3);
+		uint32_t imask = 0, used = 0, meta[8] = {0, 0, 0, 0, 0, 0, 0, 0}, tri_off = 0;
+		float lo[8][3], hi[8][3];
+		int32_t slot_kids[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
+		for (int sl = 0; sl < 8; sl++) {
+			int k = kid_in[sl];
+			if (k < 0)
+				continue;
+			int32_t ti = kids[k];
+			const TreeNode &c = tree.nodes[ti];
+			slot_kids[sl] = ti;
+			used |= 1u << sl;
+			pad_box(c.bmin, c.bmax, lo[sl], hi[sl]);
+			if (c.count) {
+				meta[sl] = (uint32_t)c.count << 5 | tri_off;
+				for (int32_t t = 0; t < c.count; t++) {
+					uint32_t rank = first_record[ti] + (uint32_t)t;
+					float4 r0 = fast_tris[3 * (size_t)rank], r1 = fast_tris[3 * (size_t)rank + 1],
+					       r2 = fast_tris[3 * (size_t)rank + 2];
+					r1.w = fbits((int32_t)rank);
+					cw_tris.push_back(r0);
+					cw_tris.push_back(r1);
+					cw_tris.push_back(r2);
+				}
+				tri_off += (uint32_t)c.count;
+			} else {
+				imask |= 1u << sl;
+				uint32_t idx = (uint32_t)nodes.size();
+				nodes.push_back(CwNode());
+				if (kids_out)
+					kids_out->insert(kids_out->end(), 8, -1);
+				queue.push_back({ti, idx, job.level + 1});
+			}
+		}
+		KGR_REQUIRE(tri_off <= 32, KGR_ERR_INTERNAL, "compressed node with more than 32 triangles");
+		KGR_REQUIRE(nodes.size() < (1u << 31) && cw_tris.size() / 3 < (1u << 31), KGR_ERR_UNSUPPORTED,
+			"scene too large for the compressed layout");
+		CwNode &n = nodes[job.index];
+		cw_quantize(lo, hi, used, imask, n.origin, n.qa, n.qb, n.qc);
+		n.base = make_uint4(first_child, first_tri, meta[0] | meta[1] << 8 | meta[2] << 16 | meta[3] << 24,
+			meta[4] | meta[5] << 8 | meta[6] << 16 | meta[7] << 24);
+		if (kids_out)
+			for (int sl = 0; sl < 8; sl++)
+				(*kids_out)[8 * (size_t)job.index + sl] = slot_kids[sl];
+	}
+	return true;
 }
 
 } /* namespace kgr */

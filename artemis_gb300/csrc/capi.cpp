@@ -115,13 +115,22 @@ kgr::DeviceScene kgr_scene::view() const
 	s.bvh_vec4_count = (uint32_t)(bvh.size() / 4);
 	s.fast_node_count = fast_node_count;
 	s.wide_node_count = wide_node_count;
+	s.cw_nodes = d_cw_nodes.ptr;
+	s.cw_tris = d_cw_tris.ptr;
+	s.cw_node_count = cw_node_count;
+	s.quads = nullptr;
+	s.quad_count = 0;
+	s.has_env = 0;
+	s.env_flip_v = 0;
+	s.env = 0;
 	return s;
 }
 
 uint64_t kgr_scene::device_bytes() const
 {
 	return d_positions.bytes() + d_normals.bytes() + d_tris.bytes() + d_bvh.bytes() + d_fast_tris.bytes()
-		+ d_fast_nodes.bytes() + d_wide_nodes.bytes() + d_materials.bytes() + d_lights.bytes();
+		+ d_fast_nodes.bytes() + d_wide_nodes.bytes() + d_cw_nodes.bytes() + d_cw_tris.bytes() + d_materials.bytes()
+		+ d_lights.bytes();
 }
 
 namespace {
@@ -351,6 +360,19 @@ void finish_scene(kgr_scene *sc, const Tree &tree, const std::vector<PrimBox> &b
 	KGR_REQUIRE(((uintptr_t)sc->d_fast_nodes.ptr & 31) == 0 && ((uintptr_t)sc->d_wide_nodes.ptr & 31) == 0,
 		KGR_ERR_INTERNAL, "node arrays are not 32-byte aligned");
 	sc->d_fast_tris.upload(tri_records);
+	std::vector<CwNode> cw;
+	std::vector<float4> cw_tris;
+	uint32_t cw_depth = 0;
+	if (build_cw8(tree, tri_records, cw, cw_tris, cw_depth, &sc->plan.cw_kids) && 2 * cw_depth + 2 <= KGR_CW_STACK) {
+		sc->d_cw_nodes.upload(cw);
+		sc->d_cw_tris.upload(cw_tris);
+		sc->cw_node_count = (uint32_t)cw.size();
+		sc->cw_depth = cw_depth;
+		static_assert(sizeof(CwNode) == 80, "compressed node size");
+		KGR_REQUIRE(((uintptr_t)sc->d_cw_nodes.ptr & 15) == 0, KGR_ERR_INTERNAL, "compressed nodes misaligned");
+	} else {
+		sc->plan.cw_kids.clear();
+	}
 	sc->d_materials.upload(sc->materials);
 	sc->d_lights.upload(sc->lights);
 }
@@ -491,6 +513,8 @@ kgr_status kgr_scene_info_get(const kgr_scene *sc, kgr_scene_info *info)
 		memcpy(info->bounds_max, sc->bounds_max, 12);
 		info->wide_node_count = sc->wide_node_count;
 		info->wide_max_stack = sc->wide_max_stack;
+		info->cw8_node_count = sc->cw_node_count;
+		info->cw8_depth = sc->cw_depth;
 	});
 }
 
@@ -569,6 +593,8 @@ kgr_status kgr_scene_copy_array(const kgr_scene *sc, int32_t which, void *out, u
 		case KGR_ARRAY_THREADED: src = sc->d_bvh.ptr; n = sc->d_bvh.bytes(); break;
 		case KGR_ARRAY_FAST_NODES: src = sc->d_fast_nodes.ptr; n = sc->d_fast_nodes.bytes(); break;
 		case KGR_ARRAY_WIDE_NODES: src = sc->d_wide_nodes.ptr; n = sc->d_wide_nodes.bytes(); break;
+		case KGR_ARRAY_CW8_NODES: src = sc->d_cw_nodes.ptr; n = sc->d_cw_nodes.bytes(); break;
+		case KGR_ARRAY_CW8_TRIANGLES: src = sc->d_cw_tris.ptr; n = sc->d_cw_tris.bytes(); break;
 		case KGR_ARRAY_TRIANGLE_RECORDS: src = sc->d_fast_tris.ptr; n = sc->d_fast_tris.bytes(); break;
 		default: throw Error(KGR_ERR_INVALID_ARGUMENT, "unknown scene array");
 		}
@@ -627,10 +653,13 @@ namespace {
 
 void check_layout(const kgr_scene *sc, int32_t layout)
 {
-	KGR_REQUIRE(layout == KGR_LAYOUT_FAST || layout == KGR_LAYOUT_THREADED || layout == KGR_LAYOUT_WIDE,
+	KGR_REQUIRE(layout == KGR_LAYOUT_FAST || layout == KGR_LAYOUT_THREADED || layout == KGR_LAYOUT_WIDE
+			|| layout == KGR_LAYOUT_CW8,
 		KGR_ERR_INVALID_ARGUMENT, "unknown layout");
 	KGR_REQUIRE(layout != KGR_LAYOUT_WIDE || sc->wide_node_count, KGR_ERR_UNSUPPORTED,
 		"the scene's wide layout was not built (its worst-case walk exceeds the traversal stack)");
+	KGR_REQUIRE(layout != KGR_LAYOUT_CW8 || sc->cw_node_count, KGR_ERR_UNSUPPORTED,
+		"the scene's compressed layout is not available (leaves over 4 triangles, or dropped by a refit)");
 }
 
 } /* namespace */
@@ -851,7 +880,7 @@ struct kgr_attachment {
 			return *p;
 		return def;
 	}
-	/* The layout option ("fast" | "threaded" | "wide"); unset, the layout
+	/* The layout option ("fast" | "threaded" | "wide" | "cw8"); unset, the layout
 	 * kgr_autotune chose (fast when nothing was tuned). */
 	int tuned_layout = KGR_LAYOUT_FAST;
 	int layout() const
@@ -863,6 +892,8 @@ struct kgr_attachment {
 			return KGR_LAYOUT_FAST;
 		if (l == "wide")
 			return KGR_LAYOUT_WIDE;
+		if (l == "cw8")
+			return KGR_LAYOUT_CW8;
 		return tuned_layout;
 	}
 
@@ -1045,8 +1076,12 @@ void check_launch(const kgr_attachment *att, const kgr_launch_info *info, const 
 	KGR_REQUIRE(sc->device == att->device, KGR_ERR_INVALID_ARGUMENT, "scene and attachment are on different devices");
 	KGR_REQUIRE((uint32_t)info->resolution[0] == att->width && (uint32_t)info->resolution[1] == att->height,
 		KGR_ERR_INVALID_ARGUMENT, "resolution differs from the attached extent");
-	KGR_REQUIRE(!info->has_environment_map, KGR_ERR_UNSUPPORTED, "environment maps are not supported");
-	KGR_REQUIRE(info->lights.quad_count == 0, KGR_ERR_UNSUPPORTED, "quad lights are not supported");
+	KGR_REQUIRE(info->lights.quad_count >= 0 && info->lights.tri_count >= 0, KGR_ERR_INVALID_ARGUMENT,
+		"negative light count");
+	KGR_REQUIRE(info->lights.quad_count == 0 || (info->lights.quad_lights && aligned16(info->lights.quad_lights)),
+		KGR_ERR_INVALID_ARGUMENT, "quad_lights must be a 16-byte aligned device array when quad_count > 0");
+	KGR_REQUIRE(!info->has_environment_map || info->environment_map, KGR_ERR_INVALID_ARGUMENT,
+		"has_environment_map is set but environment_map is 0");
 	KGR_REQUIRE(info->buffers.color, KGR_ERR_INVALID_ARGUMENT, "color buffer is NULL");
 	const void *bufs[4] = {info->buffers.color, info->buffers.normal, info->buffers.albedo, info->buffers.position};
 	for (const void *b : bufs)
@@ -1082,7 +1117,10 @@ FrameParams frame_params(const kgr_attachment *att, const kgr_launch_info *info,
 	return fp;
 }
 
-DeviceScene scene_for_launch(const kgr_scene *sc, const kgr_launch_info *info)
+/* The scene as a launch sees it: the caller's triangle lights and materials
+ * when given, its quad lights and environment map.  flip_v: the miss
+ * program's (u, 1 - v) of the path tracer rather than ReSTIR's (u, v). */
+DeviceScene scene_for_launch(const kgr_scene *sc, const kgr_launch_info *info, bool flip_v = false)
 {
 	DeviceScene s = sc->view();
 	if (info->lights.tri_lights) {
@@ -1091,6 +1129,15 @@ DeviceScene scene_for_launch(const kgr_scene *sc, const kgr_launch_info *info)
 	}
 	if (info->materials)
 		s.materials = info->materials;
+	if (info->lights.quad_count > 0) {
+		s.quads = info->lights.quad_lights;
+		s.quad_count = (uint32_t)info->lights.quad_count;
+	}
+	if (info->has_environment_map) {
+		s.has_env = 1;
+		s.env = (unsigned long long)info->environment_map;
+		s.env_flip_v = flip_v ? 1 : 0;
+	}
 	return s;
 }
 
@@ -1116,10 +1163,13 @@ void render_pt(kgr_attachment *att, const kgr_launch_info *info, const kgr_scene
 	fp.jitter = 1;
 	att->ensure_paths(fp.paths);
 	PathBuffers pb = att->path_buffers();
-	DeviceScene s = scene_for_launch(sc, info);
+	DeviceScene s = scene_for_launch(sc, info, true);
 	OutputBuffers out = {reinterpret_cast<float4 *>(info->buffers.color),
 		reinterpret_cast<float4 *>(info->buffers.normal), reinterpret_cast<float4 *>(info->buffers.albedo),
 		reinterpret_cast<float4 *>(info->buffers.position)};
+	/* with an environment map one more bounce is traced: its misses see the
+	 * map, its hits add nothing */
+	const int last = fp.max_depth + (s.has_env ? 1 : 0);
 	uint32_t launches = 0;
 	prepare_visits(att, st);
 	int m = att->mark(-1, st);
@@ -1137,7 +1187,7 @@ void render_pt(kgr_attachment *att, const kgr_launch_info *info, const kgr_scene
 		cudaStream_t side = att->side;
 		pt_trace_closest(s, pb, 0, fp.layout, fp.tune, st);
 		m = att->mark(STAGE_TRACE_CLOSEST, st, m);
-		for (int d = 0; d <= fp.max_depth; d++) {
+		for (int d = 0; d <= last; d++) {
 			int q = d & 1;
 			if (d > 0) {
 				reset_counters(pb, (1 << (q ^ 1)) | (1 << CNT_SHADOW), st);
@@ -1151,7 +1201,7 @@ void render_pt(kgr_attachment *att, const kgr_launch_info *info, const kgr_scene
 			pt_shadow_resolve(s, pb, fp.layout, fp.tune, side);
 			att->mark(STAGE_SHADOW, side, ms);
 			KGR_CUDA(cudaEventRecord(att->ev_shadowed, side));
-			if (d < fp.max_depth) {
+			if (d < last) {
 				pt_trace_closest(s, pb, q ^ 1, fp.layout, fp.tune, st);
 				m = att->mark(STAGE_TRACE_CLOSEST, st, m);
 			}
@@ -1160,7 +1210,7 @@ void render_pt(kgr_attachment *att, const kgr_launch_info *info, const kgr_scene
 			launches += 3;
 		}
 	} else {
-		for (int d = 0; d <= fp.max_depth; d++) {
+		for (int d = 0; d <= last; d++) {
 			int q = d & 1;
 			if (d > 0) {
 				reset_counters(pb, (1 << (q ^ 1)) | (1 << CNT_SHADOW), st);
@@ -1233,7 +1283,8 @@ void render_restir_di(kgr_attachment *att, const kgr_launch_info *info, const kg
 	restir_primary(s, pb, fp, rb, cur, st);
 	att->mark(STAGE_RESTIR_PRIMARY, st);
 	launches += 4; /* generate, closest hit, primary vertex, its shadow rays */
-	for (int d = 1; d <= fp.max_depth; d++) {
+	/* with an environment map one more bounce is traced for its misses */
+	for (int d = 1; d <= fp.max_depth + (s.has_env ? 1 : 0); d++) {
 		int q = d & 1;
 		reset_counters(pb, (1 << (q ^ 1)) | (1 << CNT_SHADOW), st);
 		att->mark(-1, st);
@@ -1696,8 +1747,8 @@ kgr_status kgr_set_option(kgr_attachment *att, const char *name, const kgr_value
 		KGR_REQUIRE(v.index() == it->second.index(), KGR_ERR_TYPE, std::string("wrong type for option ") + name);
 		if (std::string(name) == "layout") {
 			const std::string &s = std::get<std::string>(v);
-			KGR_REQUIRE(s == "fast" || s == "threaded" || s == "wide", KGR_ERR_INVALID_ARGUMENT,
-				"layout is fast, threaded or wide");
+			KGR_REQUIRE(s == "fast" || s == "threaded" || s == "wide" || s == "cw8", KGR_ERR_INVALID_ARGUMENT,
+				"layout is fast, threaded, wide or cw8");
 		}
 		att->options[name] = v;
 	});
@@ -1742,6 +1793,11 @@ void render_frame(kgr_attachment *att, const kgr_launch_info *info, const kgr_sc
 		att->reset_history(st);
 		att->options.erase("reset_history");
 	}
+	/* the radiance cache and ReSTIR GI have no reference counterpart; they
+	 * light with the scene's triangles only */
+	bool extra_lights = info->lights.quad_count > 0 || info->has_environment_map;
+	KGR_REQUIRE(!(extra_lights && (att->kind == KIND_RESTIR_GI || (att->kind == KIND_PT && att->opt_int("cache", 0)))),
+		KGR_ERR_UNSUPPORTED, "quad lights and environment maps are supported by the plain path tracer and ReSTIR DI");
 	switch (att->kind) {
 	case KIND_PT:
 		if (att->opt_int("cache", 0))

@@ -481,10 +481,211 @@ __device__ __forceinline__ bool trace_fast_stack(const DeviceScene &s, const f3 
 	}
 }
 
+/* ------------------------------------------------- compressed layout -- */
+
+/* The walk of the compressed eight-child layout (CwNode), after Ylitie,
+ * Karras and Laine (HPG 2017).  A node group {first internal child, bits}
+ * holds in bits 24-31 the internal children a node visit found reached, in
+ * visiting order (highest bit first), and in bits 0-7 the node's imask;
+ * slot j of a node sits at bit 24 + (j ^ oi), oi = 7 ^ octant, so slot
+ * `octant` comes first.  A triangle group {first record, mask} holds the
+ * reached leaves' triangles.  The stack holds node groups only. */
+struct CwStack {
+	uint2 a[KGR_CW_STACK];
+	int sp;
+	__device__ __forceinline__ bool empty() const { return sp == 0; }
+	__device__ __forceinline__ void clear() { sp = 0; }
+	__device__ __forceinline__ void push(uint2 v) { a[sp++] = v; }
+	__device__ __forceinline__ uint2 pop() { return a[--sp]; }
+};
+
+struct CwWalk {
+	FastRay r;
+	uint32_t oi;
+	uint2 node;           /* the node group being expanded */
+	uint2 park, cur;      /* triangle groups: the postponed one and the one that stopped the descent */
+};
+
+__device__ __forceinline__ void cw_begin(CwWalk &w, const f3 &o, const f3 &d, CwStack &stack)
+{
+	w.r = fast_ray(o, d);
+	uint32_t oct = (w.r.ix < 0.0f ? 1u : 0u) | (w.r.iy < 0.0f ? 2u : 0u) | (w.r.iz < 0.0f ? 4u : 0u);
+	w.oi = 7u ^ oct;
+	/* the root as the only reached child of a group with imask 0: rank 0 */
+	w.node = make_uint2(0u, 0x80000000u);
+	w.park = make_uint2(0u, 0u);
+	w.cur = make_uint2(0u, 0u);
+	stack.clear();
+}
+
+__device__ __forceinline__ float cw_byte(uint32_t lo4, uint32_t hi4, int j)
+{
+	uint32_t w = j < 4 ? lo4 : hi4;
+	return __uint2float_rn((w >> (8 * (j & 3))) & 0xffu);
+}
+
+/* One node: the reached internal children become the node group, the
+ * reached leaves' triangles a triangle group.  A child is reached when its
+ * quantised box meets [0, best_t]: the slab planes are p + q 2^e, and
+ * (p + q 2^e - o) / d is evaluated as q (2^e / d) + (p - o) / d. */
+__device__ __forceinline__ void cw_visit(const DeviceScene &s, const CwWalk &w, uint32_t child, float best_t,
+		uint2 &node, uint2 &tris)
+{
+	const float4 *np = reinterpret_cast<const float4 *>(s.cw_nodes + child);
+	float4 o4 = __ldg(np);
+	float4 b4 = __ldg(np + 1), a4 = __ldg(np + 2), c4 = __ldg(np + 3), d4 = __ldg(np + 4);
+	uint4 base = make_uint4(__float_as_uint(b4.x), __float_as_uint(b4.y), __float_as_uint(b4.z), __float_as_uint(b4.w));
+	uint4 qa = make_uint4(__float_as_uint(a4.x), __float_as_uint(a4.y), __float_as_uint(a4.z), __float_as_uint(a4.w));
+	uint4 qb = make_uint4(__float_as_uint(c4.x), __float_as_uint(c4.y), __float_as_uint(c4.z), __float_as_uint(c4.w));
+	uint4 qc = make_uint4(__float_as_uint(d4.x), __float_as_uint(d4.y), __float_as_uint(d4.z), __float_as_uint(d4.w));
+	uint32_t eb = __float_as_uint(o4.w);
+	uint32_t imask = eb >> 24;
+	float scx = __uint_as_float((eb & 0xffu) << 23) * w.r.ix;
+	float scy = __uint_as_float(((eb >> 8) & 0xffu) << 23) * w.r.iy;
+	float scz = __uint_as_float(((eb >> 16) & 0xffu) << 23) * w.r.iz;
+	float adx = (o4.x - w.r.o.x) * w.r.ix;
+	float ady = (o4.y - w.r.o.y) * w.r.iy;
+	float adz = (o4.z - w.r.o.z) * w.r.iz;
+	uint32_t hits = 0u, tmask = 0u;
+#pragma unroll
+	for (int j = 0; j < 8; j++) {
+		uint32_t meta = ((j < 4 ? base.z : base.w) >> (8 * (j & 3))) & 0xffu;
+		bool internal = (imask >> j) & 1u;
+		if (!internal && meta == 0u)
+			continue;
+		float x0 = __fmaf_rn(cw_byte(qa.x, qa.y, j), scx, adx), x1 = __fmaf_rn(cw_byte(qb.z, qb.w, j), scx, adx);
+		float y0 = __fmaf_rn(cw_byte(qa.z, qa.w, j), scy, ady), y1 = __fmaf_rn(cw_byte(qc.x, qc.y, j), scy, ady);
+		float z0 = __fmaf_rn(cw_byte(qb.x, qb.y, j), scz, adz), z1 = __fmaf_rn(cw_byte(qc.z, qc.w, j), scz, adz);
+		float tn = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), 0.0f));
+		float tf = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fmaxf(z0, z1));
+		if (tn <= tf && tn <= best_t) {
+			if (internal)
+				hits |= 1u << (24u + ((uint32_t)j ^ w.oi));
+			else
+				tmask |= ((1u << (meta >> 5)) - 1u) << (meta & 31u);
+		}
+	}
+	node = make_uint2(base.x, hits | imask);
+	tris = make_uint2(base.y, tmask);
+}
+
+/* One triangle record of the compressed layout: fast_triangle with the walk
+ * rank read from the record. */
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ bool cw_triangle(const DeviceScene &s, const FastRay &r, uint32_t idx, kgr_hit &best,
+		int32_t &best_rank, TraceCounters *cnt)
+{
+	if (COUNT)
+		cnt->tris++;
+	const float4 *tp = s.cw_tris + 3 * (size_t)idx;
+	float4 a = __ldg(tp + 0);
+	float4 e1 = __ldg(tp + 1);
+	float4 e2 = __ldg(tp + 2);
+	float b1 = 0.0f, b2 = 0.0f;
+	float tt = mt_test(f3_of(a), f3_of(e1), f3_of(e2), r.o, r.d, b1, b2);
+	if (ANY) {
+		if (tt > 0.0f && tt < best.t) {
+			best.prim = ibits(a.w);
+			best.t = tt;
+			return true;
+		}
+		return false;
+	}
+	int32_t rank = __float_as_int(e1.w);
+	if (tt > 0.0f && (tt < best.t || (tt == best.t && rank < best_rank))) {
+		best.prim = ibits(a.w);
+		best.t = tt;
+		best.b1 = b1;
+		best.b2 = b2;
+		best_rank = rank;
+	}
+	return false;
+}
+
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ bool cw_triangles(const DeviceScene &s, const FastRay &r, uint2 &g, kgr_hit &best,
+		int32_t &best_rank, TraceCounters *cnt)
+{
+	while (g.y) {
+		uint32_t k = (uint32_t)__ffs(g.y) - 1u;
+		g.y &= g.y - 1u;
+		if (cw_triangle<ANY, COUNT>(s, r, g.x + k, best, best_rank, cnt))
+			return true;
+	}
+	return false;
+}
+
+/* One step of the walk: descend with the postponed-leaf rule (a lane parks
+ * its first triangle group and keeps descending until it finds a second
+ * one, or runs out of nodes, while any lane of the warp is still looking),
+ * then test the held triangles.  Returns true on an occluding hit (ANY);
+ * `done` when nothing is left to visit. */
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ bool cw_step(const DeviceScene &s, CwWalk &w, kgr_hit &best, int32_t &best_rank,
+		CwStack &stack, TraceCounters *cnt, bool &done)
+{
+	for (;;) {
+		if (w.cur.y == 0u) {
+			if (w.node.y & 0xff000000u) {
+				uint32_t b = 31u - (uint32_t)__clz(w.node.y);
+				uint32_t slot = (b - 24u) ^ w.oi;
+				w.node.y &= ~(1u << b);
+				uint32_t child = w.node.x + (uint32_t)__popc(w.node.y & 0xffu & ((1u << slot) - 1u));
+				if (w.node.y & 0xff000000u)
+					stack.push(w.node);
+				if (COUNT)
+					cnt->nodes++;
+				uint2 t;
+				cw_visit(s, w, child, best.t, w.node, t);
+				if (t.y) {
+					if (w.park.y == 0u)
+						w.park = t;
+					else
+						w.cur = t;
+				}
+			} else if (!stack.empty()) {
+				w.node = stack.pop();
+			}
+		}
+		bool looking = w.cur.y == 0u && ((w.node.y & 0xff000000u) || !stack.empty());
+		if (!__any_sync(__activemask(), looking))
+			break;
+	}
+	if (cw_triangles<ANY, COUNT>(s, w.r, w.park, best, best_rank, cnt))
+		return true;
+	if (cw_triangles<ANY, COUNT>(s, w.r, w.cur, best, best_rank, cnt))
+		return true;
+	done = !(w.node.y & 0xff000000u) && stack.empty();
+	return false;
+}
+
+template <bool ANY, bool COUNT>
+__device__ __forceinline__ bool trace_cw(const DeviceScene &s, const f3 &o, const f3 &d, float tmax, kgr_hit &best,
+		TraceCounters *cnt = nullptr)
+{
+	best.prim = -1;
+	best.t = tmax;
+	best.b1 = 0.0f;
+	best.b2 = 0.0f;
+	int32_t best_rank = 0x7fffffff;
+	CwStack stack;
+	CwWalk w;
+	cw_begin(w, o, d, stack);
+	for (;;) {
+		bool done = false;
+		if (cw_step<ANY, COUNT>(s, w, best, best_rank, stack, cnt, done))
+			return true;
+		if (done)
+			return best.prim >= 0;
+	}
+}
+
 template <bool ANY, bool COUNT, int LAYOUT = KGR_LAYOUT_FAST>
 __device__ __forceinline__ bool trace_fast(const DeviceScene &s, const f3 &o, const f3 &d,
 		float tmax, kgr_hit &best, TraceCounters *cnt = nullptr)
 {
+	if (LAYOUT == KGR_LAYOUT_CW8)
+		return trace_cw<ANY, COUNT>(s, o, d, tmax, best, cnt);
 	int32_t entries[KGR_STACK_DEPTH];
 	LocalStack stack(nullptr, entries);
 	return trace_fast_stack<ANY, COUNT, LAYOUT>(s, o, d, tmax, best, stack, cnt);
@@ -498,6 +699,8 @@ __device__ __forceinline__ bool trace(const DeviceScene &s, int layout, const f3
 		return trace_threaded<ANY, false>(s, o, d, tmax, best);
 	if (layout == KGR_LAYOUT_WIDE)
 		return trace_fast<ANY, false, KGR_LAYOUT_WIDE>(s, o, d, tmax, best);
+	if (layout == KGR_LAYOUT_CW8)
+		return trace_cw<ANY, false>(s, o, d, tmax, best);
 	return trace_fast<ANY, false>(s, o, d, tmax, best);
 }
 
@@ -716,6 +919,144 @@ __device__ __forceinline__ f3 direct_unoccluded(const SurfaceHit &sh, const f3 &
 	float geometric = fabsf(dot(sh.n, D));
 	float ldot = fabsf(dot(normal, D));
 	geometric *= ldot / (d * d);
+	return rho * Le * geometric;
+}
+
+/* ------------------------------------------ quad lights, environment map -- */
+
+/* QuadLight (lighting.cuh:57-94): the parallelogram a + u ab + v ac. */
+struct QuadLight {
+	f3 a, ab, ac, intensity;
+	__device__ __forceinline__ float area() const { return length(cross(ab, ac)); }
+	__device__ __forceinline__ f3 normal() const { return normalize(cross(ab, ac)); }
+};
+
+__device__ __forceinline__ QuadLight load_quad(const kgr_quad_light *quads, uint32_t i)
+{
+	const float4 *p = reinterpret_cast<const float4 *>(quads + i);
+	float4 a = __ldg(p + 0), b = __ldg(p + 1), c = __ldg(p + 2);
+	QuadLight l;
+	l.a = mk(a.x, a.y, a.z);
+	l.ab = mk(a.w, b.x, b.y);
+	l.ac = mk(b.z, b.w, c.x);
+	l.intensity = mk(c.y, c.z, c.w);
+	return l;
+}
+
+/* sample_area_light(QuadLight) (lighting.cuh:123-131): no reflection */
+__device__ __forceinline__ f3 sample_area_light(const QuadLight &light, f3 &seed)
+{
+	f3 r = pcg3f(seed);
+	float u = fract(r.x);
+	float v = fract(r.y);
+	return light.a + u * light.ab + v * light.ac;
+}
+
+#define KGR_WORLD_RADIUS 10000.0f /* Ld_Environment, amadeus_common.cuh:218 */
+#define KGR_PI_D 3.14159265358979323846 /* M_PI, a double */
+
+/* Texture coordinates of a direction (amadeus_path_tracer.cu:209-210):
+ * u = atan2(d.x, d.z) / (2 pi) + 0.5, v = asin(d.y) / pi + 0.5; M_PI is a
+ * double, so the division and the offset are double and round once. */
+__device__ __forceinline__ void env_uv(const f3 &d, float &u, float &v)
+{
+	u = (float)((double)katan2(d.x, d.z) / (2.0 * KGR_PI_D) + 0.5);
+	v = (float)((double)kasin(d.y) / KGR_PI_D + 0.5);
+}
+
+__device__ __forceinline__ f3 env_fetch(const DeviceScene &s, float u, float v)
+{
+	float4 c = tex2D<float4>((cudaTextureObject_t)s.env, u, v);
+	return mk(c.x, c.y, c.z);
+}
+
+/* The miss program's radiance along d: the map at (u, 1 - v) for the path
+ * tracer, (u, v) for ReSTIR; black without a map. */
+__device__ __forceinline__ f3 env_miss(const DeviceScene &s, const f3 &d)
+{
+	if (!s.has_env)
+		return mk(0.0f);
+	float u, v;
+	env_uv(d, u, v);
+	return env_fetch(s, u, s.env_flip_v ? 1.0f - v : v);
+}
+
+/* The environment light's direction (Ld_Environment,
+ * amadeus_common.cuh:215-238; sample_direct, :343-374): seed =
+ * rand_uniform_3f(seed), theta = acos(sqrt(1 - seed.x)), phi = 2 pi
+ * seed.y -- in float with brdf.cuh's float PI in Ld_Environment, in double
+ * with M_PI in sample_direct. */
+__device__ __forceinline__ f3 env_direction(f3 &seed, bool phi_double)
+{
+	seed = rand_uniform_3f(seed);
+	float theta = kacos(ksqrt(1.0f - fract(seed.x)));
+	float phi = phi_double ? (float)(2.0 * KGR_PI_D * (double)fract(seed.y)) : 2.0f * KGR_PI_F * fract(seed.y);
+	float st = ksin(theta);
+	return mk(st * kcos(phi), st * ksin(phi), kcos(theta));
+}
+
+/* One light of the launch by its place in [quads | triangles | env]: what
+ * sample_direct (amadeus_common.cuh:301-377) records in FullLightSample.
+ * type 0 quad, 1 triangle, 2 environment. */
+struct LightPoint {
+	f3 Le, normal, point;
+	float pdf;
+	int type;
+	float env_u, env_v;
+};
+
+/* sample_direct: a uniform pick over quads + triangles + the environment,
+ * then a point on it.  index < 0 when there is nothing to pick. */
+__device__ __forceinline__ int sample_direct(const DeviceScene &s, const f3 &x, f3 &seed, LightPoint &lp)
+{
+	unsigned int total = s.quad_count + s.light_count + (s.has_env ? 1u : 0u);
+	unsigned int li = (unsigned int)(rand_uniform(seed) * total);
+	lp.env_u = lp.env_v = 0.0f;
+	if (li < s.quad_count) {
+		QuadLight l = load_quad(s.quads, li);
+		lp.point = sample_area_light(l, seed);
+		lp.Le = l.intensity;
+		lp.normal = l.normal();
+		lp.pdf = 1.0f / (l.area() * total);
+		lp.type = 0;
+		return (int)li;
+	}
+	if (li < s.quad_count + s.light_count) {
+		TriLight l = load_light(s.lights, li - s.quad_count);
+		lp.point = sample_area_light(l, seed);
+		lp.Le = l.intensity;
+		lp.normal = l.normal();
+		lp.pdf = 1.0f / (l.area() * total);
+		lp.type = 1;
+		return (int)li;
+	}
+	if (li < total) {
+		f3 wi = env_direction(seed, true);
+		lp.point = x + wi * KGR_WORLD_RADIUS;
+		env_uv(wi, lp.env_u, lp.env_v);
+		lp.Le = env_fetch(s, lp.env_u, lp.env_v);
+		lp.normal = -wi;
+		lp.pdf = (float)(1.0 / (4.0 * KGR_PI_D * (double)total));
+		lp.type = 2;
+		return (int)li;
+	}
+	lp.point = mk(0.0f);
+	lp.pdf = 0.0f;
+	lp.type = -1;
+	return -1;
+}
+
+/* direct_unoccluded (amadeus_common.cuh:380-397) for any light type: the
+ * environment (type 2) drops the light's cosine and 1/d^2 */
+__device__ __forceinline__ f3 direct_unoccluded_typed(const SurfaceHit &sh, const f3 &Le, const f3 &normal,
+		int type, const f3 &D, float d)
+{
+	f3 rho = brdf(sh, D);
+	float geometric = fabsf(dot(sh.n, D));
+	if (type != 2) {
+		float ldot = fabsf(dot(normal, D));
+		geometric *= ldot / (d * d);
+	}
 	return rho * Le * geometric;
 }
 

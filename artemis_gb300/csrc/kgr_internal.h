@@ -147,6 +147,30 @@ struct WideNode {
 };
 #define KGR_WIDE_EMPTY ((int32_t)0x80000000)
 
+/* 80-byte eight-child node of the compressed wide layout (after Ylitie,
+ * Karras and Laine, "Efficient Incoherent Ray Traversal on GPUs Through
+ * Compressed Wide BVHs", HPG 2017).  Child boxes are the fast layout's
+ * padded boxes quantised to 8 bits a plane on the node's grid p + q * 2^e,
+ * rounded outward by at least half a grid step, so culling stays
+ * conservative.  Slot j of a node is internal when bit j of imask is set
+ * (its node index: first_child + the number of internal slots before j), a
+ * leaf when meta[j] != 0 (meta = count << 5 | offset: `count` triangle
+ * records from first_tri + offset), empty otherwise.  Children sit in the
+ * slots that order them front to back for rays of each octant: a ray whose
+ * direction signs form octant o visits slot o first, then o ^ 1, o ^ 2, ...
+ * Triangle records are the fast layout's, copied in node order, each with
+ * its walk rank (the fast layout's record index) in e1.w for the tie-break
+ * of equal distances. */
+struct CwNode {
+	float4 origin; /* p.x, p.y, p.z, bits(ex | ey << 8 | ez << 16 | imask << 24); 2^(e - 127) */
+	uint4 base;    /* first internal child, first triangle record, meta[0..3], meta[4..7] */
+	uint4 qa;      /* lo.x[0..7], lo.y[0..7] */
+	uint4 qb;      /* lo.z[0..7], hi.x[0..7] */
+	uint4 qc;      /* hi.y[0..7], hi.z[0..7] */
+};
+/* traversal stack entries of the compressed layout (node groups) */
+#define KGR_CW_STACK 32
+
 /* Host builders (bvh_build.cpp). */
 struct PrimBox {
 	float bmin[3], bmax[3];
@@ -180,6 +204,13 @@ void build_fast(const Tree &tree, const std::vector<PrimBox> &boxes,
  * (over every root-to-node path, the sum of children - 1). */
 void build_wide(const Tree &tree, std::vector<WideNode> &nodes, uint32_t &max_stack,
 		std::vector<int4> *kids = nullptr);
+/* Compressed wide layout from the same tree (leaves of at most 4
+ * triangles): each node gathers up to eight children by opening its
+ * largest-area interior child; `fast_tris` are the fast layout's records.
+ * depth: the most nodes on a root-to-leaf path.  Returns false (nothing
+ * built) when a leaf holds more than 4 triangles. */
+bool build_cw8(const Tree &tree, const std::vector<float4> &fast_tris, std::vector<CwNode> &nodes,
+		std::vector<float4> &cw_tris, uint32_t &depth, std::vector<int32_t> *kids = nullptr);
 
 /* ---------------------------------------------------------------- scene -- */
 
@@ -198,6 +229,18 @@ struct DeviceScene {
 	uint32_t bvh_vec4_count;
 	uint32_t fast_node_count;
 	uint32_t wide_node_count;
+	const CwNode *cw_nodes;
+	const float4 *cw_tris; /* 3 per triangle, compressed-layout node order */
+	uint32_t cw_node_count;
+	/* lights of the launch beyond the scene's triangles: quad lights
+	 * (sampled only, never traced) and an environment texture */
+	const kgr_quad_light *quads;
+	uint32_t quad_count;
+	int32_t has_env;
+	/* the miss program's v: 1 - v in the path tracer
+	 * (amadeus_path_tracer.cu:216), v in ReSTIR (amadeus_restir.cu:574) */
+	int32_t env_flip_v;
+	unsigned long long env; /* cudaTextureObject_t */
 };
 
 } /* namespace kgr */
@@ -236,6 +279,7 @@ struct RefitPlan {
 	std::vector<int32_t> rec_node;     /* threaded record -> node, ~prim for leaf records */
 	std::vector<int2> fast_kids;       /* fast node -> its two child nodes (-1: none) */
 	std::vector<int4> wide_kids;       /* wide node -> its child nodes (-1: empty slot) */
+	std::vector<int32_t> cw_kids;      /* compressed node -> 8 child tree nodes by slot (-1: empty) */
 };
 #define KGR_NORMAL_OWN (-1)
 #define KGR_NORMAL_ZERO (-2)
@@ -248,6 +292,7 @@ struct RefitDevice {
 	DevBuf<int32_t> normal_src, has_model, rec_node;
 	DevBuf<float> models;
 	DevBuf<int4> nodes, wide_kids;
+	DevBuf<int32_t> cw_kids;
 	DevBuf<int2> fast_kids;
 };
 
@@ -262,6 +307,7 @@ struct kgr_scene {
 	std::vector<float> bvh;                /* threaded, 4 floats per vec4 */
 	uint32_t fast_node_count = 0;
 	uint32_t wide_node_count = 0, wide_max_stack = 0;
+	uint32_t cw_node_count = 0, cw_depth = 0;
 	float bounds_min[3] = {0, 0, 0}, bounds_max[3] = {0, 0, 0};
 	double build_ms = 0.0;
 
@@ -269,6 +315,8 @@ struct kgr_scene {
 	kgr::DevBuf<uint4> d_tris;
 	kgr::DevBuf<kgr::FastNode> d_fast_nodes;
 	kgr::DevBuf<kgr::WideNode> d_wide_nodes;
+	kgr::DevBuf<kgr::CwNode> d_cw_nodes;
+	kgr::DevBuf<float4> d_cw_tris;
 	kgr::DevBuf<kgr_material> d_materials;
 	kgr::DevBuf<kgr_triangle_light> d_lights;
 
@@ -287,15 +335,21 @@ namespace kgr {
  * same triangle records, the same hits. */
 inline int layout_for(int layout, const kgr_scene *sc)
 {
-	return (layout == KGR_LAYOUT_WIDE && sc && !sc->wide_node_count) ? KGR_LAYOUT_FAST : layout;
+	if (layout == KGR_LAYOUT_WIDE && sc && !sc->wide_node_count)
+		return KGR_LAYOUT_FAST;
+	if (layout == KGR_LAYOUT_CW8 && sc && !sc->cw_node_count)
+		return KGR_LAYOUT_FAST;
+	return layout;
 }
 
 /* Every launch shape the autotuner tries on a scene. */
 inline std::vector<kgr_trace_tune> tune_candidates(const kgr_scene *sc)
 {
 	std::vector<kgr_trace_tune> c;
-	for (int layout : {KGR_LAYOUT_FAST, KGR_LAYOUT_WIDE}) {
+	for (int layout : {KGR_LAYOUT_FAST, KGR_LAYOUT_WIDE, KGR_LAYOUT_CW8}) {
 		if (layout == KGR_LAYOUT_WIDE && !sc->wide_node_count)
+			continue;
+		if (layout == KGR_LAYOUT_CW8 && !sc->cw_node_count)
 			continue;
 		for (int shadow : {KGR_TRACE_GRID, KGR_TRACE_PERSISTENT})
 			for (int block : {64, 128, 256})

@@ -222,6 +222,30 @@ KGR_HD float kacos(float x)
 	return 2.0f * katan(ksqrt((1.0f - x) / (1.0f + x)));
 }
 
+/* atan2(y, x): katan(y / x) moved to the quadrant of (x, y); +-pi/2 on the
+ * y axis and 0 at the origin. */
+KGR_HD float katan2(float y, float x)
+{
+	if (kisnan(x) || kisnan(y))
+		return x + y;
+	if (x == 0.0f)
+		return y > 0.0f ? KGR_PIO2_F : (y < 0.0f ? -KGR_PIO2_F : 0.0f);
+	float r = katan(y / x);
+	if (x < 0.0f)
+		r = y < 0.0f ? r - KGR_PI_F : r + KGR_PI_F;
+	return r;
+}
+
+/* asin(x) = atan(x / sqrt(1 - x^2)) on (-1, 1), +-pi/2 at +-1; NaN outside. */
+KGR_HD float kasin(float x)
+{
+	if (!(x >= -1.0f && x <= 1.0f))
+		return (x - x) / (x - x);
+	if (x == 1.0f || x == -1.0f)
+		return x * KGR_PIO2_F;
+	return katan(x / ksqrt((1.0f - x) * (1.0f + x)));
+}
+
 /* powf(x, 2|4|5) for the three integer exponents brdf.cuh uses. */
 KGR_HD float kpow2(float x) { return x * x; }
 KGR_HD float kpow4(float x) { float x2 = x * x; return x2 * x2; }

@@ -13,7 +13,9 @@
 
 namespace kgr {
 
-/* Ld (amadeus_common.cuh:256-286) with Ld_light (lighting.cuh:149-174) and
+/* Ld (amadeus_common.cuh:256-286) -- a uniform pick over the quad lights,
+ * the triangle lights and the environment map -- with Ld_light
+ * (lighting.cuh:149-174) or Ld_Environment (amadeus_common.cuh:215-254), and
  * the continuation (eval, brdf.cuh:573-589; Russian roulette as in
  * naive_path_tracer.cu:294-303).  `seed` advances in place.  At the last
  * depth the continuation is sampled only when final_seed is set (ReSTIR
@@ -31,27 +33,61 @@ __device__ __forceinline__ void shade_surface(const DeviceScene &s, const FrameP
 	float sgn = sh.mat.type == KGR_SHADING_TRANSMISSION ? -1.0f : 1.0f;
 	sh.x = sh.x + sgn * n3 * KGR_OFFSET_EPS;
 	out.vertex(sh.x, n3, sh.mat);
-	if (s.light_count == 0) {
+	unsigned int total_count = s.quad_count + s.light_count + (s.has_env ? 1u : 0u);
+	if (total_count == 0) {
 		f3 direct = sh.mat.emission + mk(0.0f);
 		out.emit(beta * direct);
 	} else {
-		int total_count = (int)s.light_count;
 		unsigned int li = (unsigned int)(rand_uniform(seed) * total_count);
 		float pdf = 1.0f / total_count;
-		TriLight light = load_light(s.lights, li < s.light_count ? li : s.light_count - 1);
-		float light_pdf = 1.0f / light.area();
-		f3 lpos = sample_area_light(light, seed);
-		f3 wi = normalize(lpos - sh.x);
-		float R = length(lpos - sh.x);
-		f3 f = brdf(sh, wi);
-		float ldot = fabsf(dot(light.normal(), wi));
-		float geometric = ldot * fabsf(dot(sh.n, wi)) / (R * R);
-		f3 contr = f * light.intensity * geometric;
+		float light_pdf;
+		f3 contr, wi;
+		float tmax;
+		if (li < s.quad_count + s.light_count || !s.has_env) {
+			/* Ld_light (lighting.cuh:149-174) over a quad or a triangle */
+			f3 lpos, lnormal, Le;
+			if (li < s.quad_count) {
+				QuadLight light = load_quad(s.quads, li);
+				light_pdf = 1.0f / light.area();
+				lpos = sample_area_light(light, seed);
+				lnormal = light.normal();
+				Le = light.intensity;
+			} else {
+				uint32_t ti = li - s.quad_count;
+				TriLight light = load_light(s.lights, ti < s.light_count ? ti : s.light_count - 1);
+				light_pdf = 1.0f / light.area();
+				lpos = sample_area_light(light, seed);
+				lnormal = light.normal();
+				Le = light.intensity;
+			}
+			wi = normalize(lpos - sh.x);
+			float R = length(lpos - sh.x);
+			f3 f = brdf(sh, wi);
+			float ldot = fabsf(dot(lnormal, wi));
+			float geometric = ldot * fabsf(dot(sh.n, wi)) / (R * R);
+			contr = f * Le * geometric;
+			tmax = R - KGR_SHADOW_EPS;
+		} else {
+			/* Ld_Environment (amadeus_common.cuh:215-254): the map at (u, v),
+			 * a shadow ray to the world radius, pdf 1 / (4 pi) */
+			wi = env_direction(seed, false);
+			float u, v;
+			env_uv(wi, u, v);
+			f3 Li = env_fetch(s, u, v);
+			light_pdf = (float)(1.0 / (4.0 * KGR_PI_D));
+			f3 f = brdf(sh, wi) * fabsf(dot(sh.n, wi));
+			contr = f * Li;
+			tmax = KGR_WORLD_RADIUS - KGR_SHADOW_EPS;
+		}
 		pdf *= light_pdf;
 		out.nee(f4_of(contr, pdf), f4_of(sh.mat.emission, 0.0f), f4_of(beta, 0.0f), f4_of(sh.x, 0.0f),
-			f4_of(wi, R - KGR_SHADOW_EPS));
+			f4_of(wi, tmax));
 	}
-	if (depth < fp.max_depth || final_seed) {
+	/* with an environment map the ray past the last vertex is still cast:
+	 * a hit there adds nothing, a miss adds the map (the reference's miss
+	 * program has no depth test, amadeus_path_tracer.cu:204-220) */
+	int last = fp.max_depth + (s.has_env ? 1 : 0);
+	if (depth < last || final_seed) {
 		f3 wi;
 		float pdf = 0.0f;
 		f3 f = eval(sh, wi, pdf, seed);
@@ -67,7 +103,7 @@ __device__ __forceinline__ void shade_surface(const DeviceScene &s, const FrameP
 				else
 					beta = beta / (1.0f - qq);
 			}
-			if (alive && depth < fp.max_depth)
+			if (alive && depth < last)
 				out.next(sh.x, wi, beta);
 		}
 	}

@@ -200,7 +200,15 @@ __global__ void __launch_bounds__(128) shade_kernel(DeviceScene s, PathBuffers p
 			float4 dv = pb.ray_d[p];
 			f3 dir = mk(dv.x, dv.y, dv.z);
 			SurfaceHit sh;
-			if (h.prim >= 0 && surface(s, h, dir, sh)) {
+			if (h.prim < 0) {
+				/* __miss__ (amadeus_path_tracer.cu:204-220): the environment
+				 * map along the ray, weighted by the path throughput */
+				if (s.has_env) {
+					float4 bv = pb.beta[p], Lv = pb.L[p];
+					f3 add = mk(bv.x, bv.y, bv.z) * env_miss(s, dir);
+					pb.L[p] = f4_of(mk(Lv.x, Lv.y, Lv.z) + add, 0.0f);
+				}
+			} else if (depth <= fp.max_depth && surface(s, h, dir, sh)) {
 				WavefrontSink out{pb, p, depth, fp.gi_capture, sh.mat.diffuse};
 				float4 sv = pb.seed[p];
 				f3 seed = mk(sv.x, sv.y, sv.z);
@@ -251,6 +259,8 @@ __global__ void __launch_bounds__(BLOCK, KGR_MIN_BLOCKS(BLOCK, OCC)) shadow_reso
 		bool occ;
 		if (LAYOUT == KGR_LAYOUT_THREADED)
 			occ = trace_threaded<true, COUNT>(s, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), b.w, h, &cnt);
+		else if (LAYOUT == KGR_LAYOUT_CW8)
+			occ = trace_cw<true, COUNT>(s, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), b.w, h, &cnt);
 		else
 			occ = trace_fast_stack<true, COUNT, LAYOUT>(s, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), b.w, h, stack,
 				&cnt);
@@ -346,6 +356,69 @@ __global__ void __launch_bounds__(BLOCK, KGR_MIN_BLOCKS(BLOCK, OCC)) fast_persis
 		add_visits(pb.visits + (ANY ? 2 : 0), cnt);
 }
 
+/* The persistent traversal over the compressed eight-child layout: the
+ * refill of fast_persistent_kernel, one cw_step (descend with postponed
+ * leaves, then test) per iteration. */
+template <bool ANY, bool COUNT, int BLOCK, int OCC = 0>
+__global__ void __launch_bounds__(BLOCK, KGR_MIN_BLOCKS(BLOCK, OCC)) cw_persistent_kernel(DeviceScene s,
+		PathBuffers pb, int q)
+{
+	const uint32_t n = ANY ? pb.counters[CNT_SHADOW] : pb.counters[q == 0 ? CNT_Q0 : CNT_Q1];
+	const uint32_t *queue = ANY ? pb.shadow_queue : pb.queue[q];
+	uint32_t *fetch = pb.counters + (ANY ? CNT_FETCH_SHADOW : CNT_FETCH_CLOSEST);
+	const int lane = threadIdx.x & 31;
+	TraceCounters cnt = {0, 0};
+	uint32_t p = 0;
+	bool have = false, exhausted = false;
+	kgr_hit best;
+	int32_t best_rank = 0x7fffffff;
+	CwStack stack;
+	CwWalk w;
+	for (;;) {
+		bool need = !have && !exhausted;
+		unsigned m = __ballot_sync(0xffffffffu, need);
+		if (m) {
+			int leader = __ffs(m) - 1;
+			uint32_t base = 0;
+			if (lane == leader)
+				base = atomicAdd(fetch, (uint32_t)__popc(m));
+			base = __shfl_sync(0xffffffffu, base, leader);
+			if (need) {
+				uint32_t i = base + __popc(m & ((1u << lane) - 1u));
+				if (i < n) {
+					p = queue[i];
+					float4 a = ANY ? pb.sh_o[p] : pb.ray_o[p];
+					float4 b = ANY ? pb.sh_d[p] : pb.ray_d[p];
+					cw_begin(w, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), stack);
+					best.prim = -1;
+					best.t = b.w;
+					best.b1 = 0.0f;
+					best.b2 = 0.0f;
+					best_rank = 0x7fffffff;
+					have = true;
+				} else {
+					exhausted = true;
+				}
+			}
+		}
+		if (!__any_sync(0xffffffffu, have))
+			break;
+		if (!have)
+			continue;
+		bool done = false;
+		bool occ = cw_step<ANY, COUNT>(s, w, best, best_rank, stack, &cnt, done);
+		if (occ || done) {
+			if (ANY)
+				resolve_shadow(pb, p, occ);
+			else
+				pb.hit[p] = make_float4(__int_as_float(best.prim), best.t, best.b1, best.b2);
+			have = false;
+		}
+	}
+	if (COUNT)
+		add_visits(pb.visits + (ANY ? 2 : 0), cnt);
+}
+
 template <class K>
 int resident_grid(K kernel, int block)
 {
@@ -385,6 +458,36 @@ void launch_persistent_occ(const DeviceScene &s, const PathBuffers &pb, int q, i
 		launch_persistent_stack<ANY, LAYOUT, OCC, 256>(s, pb, q, stack, st);
 	else
 		launch_persistent_stack<ANY, LAYOUT, OCC, 128>(s, pb, q, stack, st);
+}
+
+template <bool ANY, bool COUNT, int BLOCK, int OCC = 0>
+void launch_cw_persistent(const DeviceScene &s, const PathBuffers &pb, int q, cudaStream_t st)
+{
+	static const int g = resident_grid(cw_persistent_kernel<ANY, COUNT, BLOCK, OCC>, BLOCK);
+	cw_persistent_kernel<ANY, COUNT, BLOCK, OCC><<<g, BLOCK, 0, st>>>(s, pb, q);
+}
+
+/* The compressed layout's stack is per thread (node groups): the stack
+ * knob does not apply. */
+template <bool ANY>
+void launch_cw_persistent_tuned(const DeviceScene &s, const PathBuffers &pb, int q, const TraceTune &t,
+		cudaStream_t st)
+{
+	if (t.occupancy) {
+		if (t.block == 64)
+			launch_cw_persistent<ANY, false, 64, 1>(s, pb, q, st);
+		else if (t.block == 256)
+			launch_cw_persistent<ANY, false, 256, 1>(s, pb, q, st);
+		else
+			launch_cw_persistent<ANY, false, 128, 1>(s, pb, q, st);
+	} else {
+		if (t.block == 64)
+			launch_cw_persistent<ANY, false, 64>(s, pb, q, st);
+		else if (t.block == 256)
+			launch_cw_persistent<ANY, false, 256>(s, pb, q, st);
+		else
+			launch_cw_persistent<ANY, false, 128>(s, pb, q, st);
+	}
 }
 
 template <bool ANY, int LAYOUT>
@@ -475,7 +578,12 @@ void pt_trace_closest(const DeviceScene &s, const PathBuffers &pb, int q, int la
 			trace_closest_kernel<KGR_LAYOUT_THREADED, false><<<grid, 128, 0, st>>>(s, pb, q);
 	} else {
 		KGR_CUDA(cudaMemsetAsync(pb.counters + CNT_FETCH_CLOSEST, 0, sizeof(uint32_t), st));
-		if (layout == KGR_LAYOUT_WIDE) {
+		if (layout == KGR_LAYOUT_CW8) {
+			if (c)
+				launch_cw_persistent<false, true, 128>(s, pb, q, st);
+			else
+				launch_cw_persistent_tuned<false>(s, pb, q, tune, st);
+		} else if (layout == KGR_LAYOUT_WIDE) {
 			if (c)
 				launch_persistent<false, true, KGR_LAYOUT_WIDE, 128>(s, pb, q, st);
 			else
@@ -519,16 +627,28 @@ void pt_shadow_resolve(const DeviceScene &s, const PathBuffers &pb, int layout, 
 	} else if (c) {
 		if (layout == KGR_LAYOUT_WIDE)
 			launch_shadow_grid<true, KGR_LAYOUT_WIDE, 128>(s, pb, st);
+		else if (layout == KGR_LAYOUT_CW8)
+			launch_shadow_grid<true, KGR_LAYOUT_CW8, 128>(s, pb, st);
 		else
 			launch_shadow_grid<true, KGR_LAYOUT_FAST, 128>(s, pb, st);
 	} else if (tune.shadow == TRACE_PERSISTENT) {
 		KGR_CUDA(cudaMemsetAsync(pb.counters + CNT_FETCH_SHADOW, 0, sizeof(uint32_t), st));
-		if (layout == KGR_LAYOUT_WIDE)
+		if (layout == KGR_LAYOUT_CW8)
+			launch_cw_persistent_tuned<true>(s, pb, 0, tune, st);
+		else if (layout == KGR_LAYOUT_WIDE)
 			launch_persistent_block<true, KGR_LAYOUT_WIDE>(s, pb, 0, tune, st);
 		else
 			launch_persistent_block<true, KGR_LAYOUT_FAST>(s, pb, 0, tune, st);
 	} else if (layout == KGR_LAYOUT_WIDE) {
 		launch_shadow_grid_block<KGR_LAYOUT_WIDE>(s, pb, tune, st);
+	} else if (layout == KGR_LAYOUT_CW8) {
+		/* one instantiation per block size; the stack knob does not apply */
+		if (tune.block == 64)
+			launch_shadow_grid<false, KGR_LAYOUT_CW8, 64>(s, pb, st);
+		else if (tune.block == 256)
+			launch_shadow_grid<false, KGR_LAYOUT_CW8, 256>(s, pb, st);
+		else
+			launch_shadow_grid<false, KGR_LAYOUT_CW8, 128>(s, pb, st);
 	} else {
 		launch_shadow_grid_block<KGR_LAYOUT_FAST>(s, pb, tune, st);
 	}

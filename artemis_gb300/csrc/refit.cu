@@ -28,6 +28,7 @@
  */
 #include <float.h>
 
+#include "kgr_cw8.h"
 #include "kgr_internal.h"
 #include "kgr_wavefront.h"
 
@@ -244,6 +245,33 @@ __global__ void wide_nodes_kernel(const int4 *__restrict__ kids, uint32_t nw, co
 	}
 }
 
+/* The compressed nodes requantised from their children's refitted boxes by
+ * the host builder's own rules (kgr_cw8.h): same slots, same child and
+ * triangle bases, new grid and planes. */
+__global__ void cw_nodes_kernel(const int32_t *__restrict__ kids, uint32_t nc, const float4 *__restrict__ boxes,
+		CwNode *nodes)
+{
+	for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+		float lo[8][3], hi[8][3];
+		uint32_t used = 0;
+		for (int j = 0; j < 8; j++) {
+			int32_t k = kids[8 * (size_t)c + j];
+			for (int a = 0; a < 3; a++) {
+				lo[j][a] = 0.0f;
+				hi[j][a] = 0.0f;
+			}
+			if (k < 0)
+				continue;
+			used |= 1u << j;
+			padded(boxes, k, lo[j], hi[j]);
+		}
+		CwNode n = nodes[c];
+		uint32_t imask = __float_as_uint(n.origin.w) >> 24;
+		cw_quantize(lo, hi, used, imask, n.origin, n.qa, n.qb, n.qc);
+		nodes[c] = n;
+	}
+}
+
 /* {v0, prim}, {v1 - v0}, {v2 - v0} in walk order; the primitive id stays */
 __global__ void triangle_records_kernel(uint32_t nt, const uint4 *__restrict__ tris, const float4 *__restrict__ pos,
 		float4 *rec)
@@ -254,6 +282,21 @@ __global__ void triangle_records_kernel(uint32_t nt, const uint4 *__restrict__ t
 		float4 a = pos[t.x], b = pos[t.y], c = pos[t.z];
 		rec[3 * (size_t)k] = make_float4(a.x, a.y, a.z, r0.w);
 		rec[3 * (size_t)k + 1] = make_float4(b.x - a.x, b.y - a.y, b.z - a.z, 0.0f);
+		rec[3 * (size_t)k + 2] = make_float4(c.x - a.x, c.y - a.y, c.z - a.z, 0.0f);
+	}
+}
+
+/* the compressed layout's copies of the records: the rank in e1.w stays */
+__global__ void cw_triangle_records_kernel(uint32_t nt, const uint4 *__restrict__ tris,
+		const float4 *__restrict__ pos, float4 *rec)
+{
+	for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nt; k += gridDim.x * blockDim.x) {
+		float4 r0 = rec[3 * (size_t)k];
+		float rank = rec[3 * (size_t)k + 1].w;
+		uint4 t = tris[(uint32_t)__float_as_int(r0.w)];
+		float4 a = pos[t.x], b = pos[t.y], c = pos[t.z];
+		rec[3 * (size_t)k] = make_float4(a.x, a.y, a.z, r0.w);
+		rec[3 * (size_t)k + 1] = make_float4(b.x - a.x, b.y - a.y, b.z - a.z, rank);
 		rec[3 * (size_t)k + 2] = make_float4(c.x - a.x, c.y - a.y, c.z - a.z, 0.0f);
 	}
 }
@@ -294,6 +337,7 @@ void upload_plan(kgr_scene *sc)
 	upload_vec(d.rec_node, pl.rec_node);
 	upload_vec(d.fast_kids, pl.fast_kids);
 	upload_vec(d.wide_kids, pl.wide_kids);
+	upload_vec(d.cw_kids, pl.cw_kids);
 	d.boxes.alloc(2 * pl.nodes.size());
 	d.ready = true;
 }
@@ -305,7 +349,8 @@ void refit_scene(kgr_scene *sc, int mode, const float *positions, const float *n
 	RefitPlan &pl = sc->plan;
 	RefitDevice &d = sc->refit;
 	KGR_REQUIRE(pl.vertex_mesh.size() == sc->positions.size() / 3 && pl.rec_node.size() == sc->bvh.size() / 12 &&
-			pl.fast_kids.size() == sc->fast_node_count && pl.wide_kids.size() == sc->wide_node_count,
+			pl.fast_kids.size() == sc->fast_node_count && pl.wide_kids.size() == sc->wide_node_count &&
+			pl.cw_kids.size() == 8 * (size_t)sc->cw_node_count,
 		KGR_ERR_INTERNAL, "refit plan does not match the scene");
 	if (!d.ready)
 		upload_plan(sc);
@@ -349,8 +394,13 @@ void refit_scene(kgr_scene *sc, int mode, const float *positions, const float *n
 	if (sc->wide_node_count)
 		wide_nodes_kernel<<<grid_for(sc->wide_node_count), REFIT_BLOCK, 0, st>>>(d.wide_kids.ptr,
 			sc->wide_node_count, d.boxes.ptr, sc->d_wide_nodes.ptr);
+	if (sc->cw_node_count)
+		cw_nodes_kernel<<<grid_for(sc->cw_node_count), REFIT_BLOCK, 0, st>>>(d.cw_kids.ptr, sc->cw_node_count,
+			d.boxes.ptr, sc->d_cw_nodes.ptr);
 	if (nt)
 		triangle_records_kernel<<<grid_for(nt), REFIT_BLOCK, 0, st>>>(nt, tris, pos, sc->d_fast_tris.ptr);
+	if (nt && sc->cw_node_count)
+		cw_triangle_records_kernel<<<grid_for(nt), REFIT_BLOCK, 0, st>>>(nt, tris, pos, sc->d_cw_tris.ptr);
 	KGR_CUDA(cudaGetLastError());
 	sc->refits++;
 }

@@ -20,10 +20,38 @@ namespace {
  * std::random_device on the host, reservoir.cuh:29-36). */
 #define KGR_RIS_SALT 0x9E3779B9u
 
+/* A light sample: `light` is its place among the launch's quad lights and
+ * triangle lights (quads first), -1 for none, or -- for a point on the
+ * environment map -- the bits of -u, negative and never -1, with v in
+ * env_v: the map is read again at (u, v), which gives the Le the reference
+ * stores in DirectLightingSample. */
 struct Sample {
 	int32_t light;
 	f3 point;
+	float env_v;
 };
+
+__device__ __forceinline__ bool has_light(const Sample &smp) { return smp.light != -1; }
+
+/* Le, light normal and type (0 quad, 1 triangle, 2 environment) of a sample */
+__device__ __forceinline__ int emitter(const DeviceScene &s, const Sample &smp, f3 &Le, f3 &normal)
+{
+	if (smp.light >= 0) {
+		if ((uint32_t)smp.light < s.quad_count) {
+			QuadLight l = load_quad(s.quads, (uint32_t)smp.light);
+			Le = l.intensity;
+			normal = l.normal();
+			return 0;
+		}
+		TriLight l = load_light(s.lights, (uint32_t)smp.light - s.quad_count);
+		Le = l.intensity;
+		normal = l.normal();
+		return 1;
+	}
+	Le = env_fetch(s, -__int_as_float(smp.light), smp.env_v);
+	normal = mk(0.0f);
+	return 2;
+}
 
 /* Reservoir<T>::update/resample (include/amadeus/reservoir.cuh:43-62) */
 struct Reservoir {
@@ -35,6 +63,7 @@ struct Reservoir {
 	{
 		data.light = -1;
 		data.point = mk(0.0f);
+		data.env_v = 0.0f;
 		w = 0.0f;
 		W = 0.0f;
 		M = 0;
@@ -63,6 +92,7 @@ __device__ __forceinline__ void load_res(const ReservoirBuffers &rb, uint32_t i,
 	float4 a = rb.a[i], b = rb.b[i];
 	smp.light = __float_as_int(a.w);
 	smp.point = mk(a.x, a.y, a.z);
+	smp.env_v = b.w;
 	w = b.x;
 	W = b.y;
 	M = __float_as_int(b.z);
@@ -72,7 +102,7 @@ __device__ __forceinline__ void store_res(const ReservoirBuffers &rb, uint32_t i
 		float w, float W, int32_t M)
 {
 	rb.a[i] = make_float4(smp.point.x, smp.point.y, smp.point.z, __int_as_float(smp.light));
-	rb.b[i] = make_float4(w, W, __int_as_float(M), 0.0f);
+	rb.b[i] = make_float4(w, W, __int_as_float(M), smp.env_v);
 }
 
 __device__ __forceinline__ bool occluded(const DeviceScene &s, int layout, const f3 &o, const f3 &d, float R)
@@ -84,12 +114,13 @@ __device__ __forceinline__ bool occluded(const DeviceScene &s, int layout, const
 /* target (amadeus_restir.cu:147-161) */
 __device__ __forceinline__ float target(const DeviceScene &s, const Sample &smp, const SurfaceHit &hit)
 {
-	if (smp.light < 0)
+	if (!has_light(smp))
 		return 0.0f;
-	TriLight l = load_light(s.lights, (uint32_t)smp.light);
+	f3 Le, ln;
+	int type = emitter(s, smp, Le, ln);
 	f3 D = smp.point - hit.x;
 	float d = length(D);
-	f3 Li = direct_unoccluded(hit, l.intensity, l.normal(), D / d, d);
+	f3 Li = direct_unoccluded_typed(hit, Le, ln, type, D / d, d);
 	return Li.x + Li.y + Li.z;
 }
 
@@ -142,7 +173,12 @@ __global__ void __launch_bounds__(128) primary_kernel(DeviceScene s, PathBuffers
 			h.b2 = hv.w;
 			float4 dv = pb.ray_d[p];
 			SurfaceHit sh;
-			if (h.prim >= 0 && surface(s, h, mk(dv.x, dv.y, dv.z), sh)) {
+			if (h.prim < 0) {
+				/* __miss__ (amadeus_restir.cu:561-578): the environment map at
+				 * (u, v) becomes the pixel's intermediate colour */
+				if (s.has_env)
+					pb.L[p] = f4_of(env_miss(s, mk(dv.x, dv.y, dv.z)), 0.0f);
+			} else if (surface(s, h, mk(dv.x, dv.y, dv.z), sh)) {
 				f3 n3 = sh.n;
 				float sgn = sh.mat.type == KGR_SHADING_TRANSMISSION ? -1.0f : 1.0f;
 				sh.x = sh.x + sgn * n3 * KGR_OFFSET_EPS;
@@ -153,24 +189,25 @@ __global__ void __launch_bounds__(128) primary_kernel(DeviceScene s, PathBuffers
 				f3 seed = mk(sv.x, sv.y, sv.z);
 				Reservoir res;
 				res.init(pixel_seed(p, fp.frame, KGR_RIS_SALT));
-				unsigned int total = s.light_count;
 				for (int c = 0; c < fp.candidates; c++) {
-					/* sample_direct (amadeus_common.cuh:301-377), triangle branch */
-					unsigned int li = (unsigned int)(rand_uniform(seed) * total);
+					/* sample_direct (amadeus_common.cuh:301-377) */
+					LightPoint lp;
+					int li = sample_direct(s, sh.x, seed, lp);
 					Sample smp;
 					float pdf = 0.0f, tgt = 0.0f;
-					if (li < total) {
-						TriLight l = load_light(s.lights, li);
-						smp.point = sample_area_light(l, seed);
-						pdf = 1.0f / (l.area() * total);
-						smp.light = (int32_t)li;
+					if (li >= 0) {
+						smp.light = lp.type == 2 ? __float_as_int(-lp.env_u) : (int32_t)li;
+						smp.point = lp.point;
+						smp.env_v = lp.env_v;
+						pdf = lp.pdf;
 						f3 D = smp.point - sh.x;
 						float d = length(D);
-						f3 Li = direct_unoccluded(sh, l.intensity, l.normal(), D / d, d);
+						f3 Li = direct_unoccluded_typed(sh, lp.Le, lp.normal, lp.type, D / d, d);
 						tgt = Li.x + Li.y + Li.z;
 					} else {
 						smp.light = -1;
 						smp.point = mk(0.0f);
+						smp.env_v = 0.0f;
 					}
 					res.update(smp, (pdf > 0) ? tgt / pdf : 0);
 				}
@@ -181,12 +218,13 @@ __global__ void __launch_bounds__(128) primary_kernel(DeviceScene s, PathBuffers
 				 * target 0, so resample and the visibility factor give W = +0,
 				 * which primary_visibility_kernel writes. */
 				float tgt = 0.0f;
-				if (res.data.light >= 0) {
-					TriLight l = load_light(s.lights, (uint32_t)res.data.light);
+				if (has_light(res.data)) {
+					f3 Le, ln;
+					int type = emitter(s, res.data, Le, ln);
 					f3 D = res.data.point - sh.x;
 					float d = length(D);
 					f3 Dn = D / d;
-					f3 Li = direct_unoccluded(sh, l.intensity, l.normal(), Dn, d);
+					f3 Li = direct_unoccluded_typed(sh, Le, ln, type, Dn, d);
 					tgt = Li.x + Li.y + Li.z;
 					pb.sh_o[p] = f4_of(sh.x, 0.0f);
 					pb.sh_d[p] = f4_of(Dn, d - KGR_SHADOW_EPS);
@@ -216,7 +254,7 @@ __global__ void __launch_bounds__(128) primary_kernel(DeviceScene s, PathBuffers
 						else
 							beta = beta / (1.0f - qq);
 					}
-					if (alive && 0 < fp.max_depth) {
+					if (alive && 0 < fp.max_depth + (s.has_env ? 1 : 0)) {
 						pb.ray_o[p] = f4_of(sh.x, 0.0f);
 						pb.ray_d[p] = f4_of(wi, 1e16f);
 						pb.beta[p] = f4_of(beta, 0.0f);
@@ -467,7 +505,7 @@ __global__ void __launch_bounds__(128) restir_gather_kernel(DeviceScene s, Frame
 		float t = 0.0f;
 		bool ray = false;
 		if (nM > 0) {
-			if (ns.light >= 0) {
+			if (has_light(ns)) {
 				t = target(s, ns, hit);
 				/* +0 stays +0 whatever the ray; -0 would become +0 if blocked */
 				ray = __float_as_uint(t) != 0u;
@@ -555,7 +593,7 @@ __global__ void __launch_bounds__(128) restir_resample_kernel(DeviceScene s, Fra
 		if (nb.y <= 0)
 			continue;
 		float t = 0.0f;
-		if (merged.data.light >= 0) {
+		if (has_light(merged.data)) {
 			SurfaceHit h0 = gbuffer_hit(fp, rb, out, (uint32_t)nb.x);
 			h0.wo = hit.wo;
 			h0.entering = true;
@@ -565,8 +603,8 @@ __global__ void __launch_bounds__(128) restir_resample_kernel(DeviceScene s, Fra
 		queue_append(rb.vis_queue[1], rb.vis_count + 1, slot, t > 0.0f);
 	}
 	uint32_t lit = (uint32_t)KGR_MAX_NEIGHBORS * fp.npix + pix;
-	rb.targets[lit] = merged.data.light >= 0 ? 1.0f : 0.0f;
-	queue_append(rb.vis_queue[1], rb.vis_count + 1, lit, merged.data.light >= 0);
+	rb.targets[lit] = has_light(merged.data) ? 1.0f : 0.0f;
+	queue_append(rb.vis_queue[1], rb.vis_count + 1, lit, has_light(merged.data));
 	store_res(OUT, pix, merged.data, merged.w, 0.0f, merged.M);
 }
 
@@ -601,12 +639,13 @@ __global__ void __launch_bounds__(128) restir_finish_kernel(DeviceScene s, Frame
 		float denominator = t_merged * Z;
 		float W = (denominator > 0.0f) ? w / denominator : 0.0f;
 		f3 lighting = mk(0.0f);
-		if (data.light >= 0 && rb.targets[(uint32_t)KGR_MAX_NEIGHBORS * fp.npix + pix] > 0.0f) {
-			TriLight l = load_light(s.lights, (uint32_t)data.light);
+		if (has_light(data) && rb.targets[(uint32_t)KGR_MAX_NEIGHBORS * fp.npix + pix] > 0.0f) {
+			f3 Le, ln;
+			int type = emitter(s, data, Le, ln);
 			f3 D = data.point - hit.x;
 			float d = length(D);
 			f3 Dn = D / d;
-			lighting = direct_unoccluded(hit, l.intensity, l.normal(), Dn, d);
+			lighting = direct_unoccluded_typed(hit, Le, ln, type, Dn, d);
 		}
 		direct = hit.mat.emission + lighting * W;
 		store_res(OUT, pix, data, w, W, M);

@@ -711,7 +711,7 @@ kgr_status kgr_server_create(const kgr_server_config *config, kgr_server **out)
 		KGR_REQUIRE(config->max_jobs >= 1, KGR_ERR_INVALID_ARGUMENT, "max_jobs must be >= 1");
 		KGR_REQUIRE(config->memory_budget >= 1, KGR_ERR_INVALID_ARGUMENT, "memory_budget must be > 0");
 		KGR_REQUIRE(config->layout == KGR_LAYOUT_FAST || config->layout == KGR_LAYOUT_THREADED ||
-				config->layout == KGR_LAYOUT_WIDE,
+				config->layout == KGR_LAYOUT_WIDE || config->layout == KGR_LAYOUT_CW8,
 			KGR_ERR_INVALID_ARGUMENT, "unknown layout");
 		KGR_REQUIRE(config->policy == KGR_SCHEDULE_FCFS || config->policy == KGR_SCHEDULE_FAIR,
 			KGR_ERR_INVALID_ARGUMENT, "unknown scheduling policy");

@@ -101,6 +101,8 @@ void launch_trace_closest(const DeviceScene &s, const float4 *rays, uint32_t n, 
 		trace_rays_kernel<false, KGR_LAYOUT_THREADED><<<grid, 128, 0, stream>>>(s, rays, n, hits, nullptr);
 	else if (layout == KGR_LAYOUT_WIDE)
 		trace_rays_kernel<false, KGR_LAYOUT_WIDE><<<grid, 128, 0, stream>>>(s, rays, n, hits, nullptr);
+	else if (layout == KGR_LAYOUT_CW8)
+		trace_rays_kernel<false, KGR_LAYOUT_CW8><<<grid, 128, 0, stream>>>(s, rays, n, hits, nullptr);
 	else
 		trace_rays_kernel<false, KGR_LAYOUT_FAST><<<grid, 128, 0, stream>>>(s, rays, n, hits, nullptr);
 	KGR_CUDA(cudaGetLastError());
@@ -116,6 +118,8 @@ void launch_trace_any(const DeviceScene &s, const float4 *rays, uint32_t n, uint
 		trace_rays_kernel<true, KGR_LAYOUT_THREADED><<<grid, 128, 0, stream>>>(s, rays, n, nullptr, occluded);
 	else if (layout == KGR_LAYOUT_WIDE)
 		trace_rays_kernel<true, KGR_LAYOUT_WIDE><<<grid, 128, 0, stream>>>(s, rays, n, nullptr, occluded);
+	else if (layout == KGR_LAYOUT_CW8)
+		trace_rays_kernel<true, KGR_LAYOUT_CW8><<<grid, 128, 0, stream>>>(s, rays, n, nullptr, occluded);
 	else
 		trace_rays_kernel<true, KGR_LAYOUT_FAST><<<grid, 128, 0, stream>>>(s, rays, n, nullptr, occluded);
 	KGR_CUDA(cudaGetLastError());

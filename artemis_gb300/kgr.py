@@ -17,10 +17,11 @@ from . import build as _build
 c_u32, c_i32, c_u64, c_f = ctypes.c_uint32, ctypes.c_int32, ctypes.c_uint64, ctypes.c_float
 vp = ctypes.c_void_p
 
-LAYOUT_FAST, LAYOUT_THREADED, LAYOUT_WIDE = 0, 1, 2
+LAYOUT_FAST, LAYOUT_THREADED, LAYOUT_WIDE, LAYOUT_CW8 = 0, 1, 2, 3
 TRACE_GRID, TRACE_PERSISTENT = 0, 1
 BUILDER_SAH, BUILDER_KOBRA, BUILDER_SAH_HOST = 0, 1, 2
 ARRAY_THREADED, ARRAY_FAST_NODES, ARRAY_WIDE_NODES, ARRAY_TRIANGLE_RECORDS = 0, 1, 2, 3
+ARRAY_CW8_NODES, ARRAY_CW8_TRIANGLES = 4, 5
 VALUE_NONE, VALUE_INT, VALUE_FLOAT, VALUE_BOOL, VALUE_STRING = range(5)
 
 
@@ -44,14 +45,15 @@ class SceneInfo(ctypes.Structure):
                 ("material_count", c_u32), ("bvh_vec4_count", c_u32), ("fast_node_count", c_u32),
                 ("device_bytes", c_u64), ("build_ms", ctypes.c_double),
                 ("bounds_min", c_f * 3), ("bounds_max", c_f * 3),
-                ("wide_node_count", c_u32), ("wide_max_stack", c_u32)]
+                ("wide_node_count", c_u32), ("wide_max_stack", c_u32),
+                ("cw8_node_count", c_u32), ("cw8_depth", c_u32)]
 
 
 class TraceTune(ctypes.Structure):
     _fields_ = [("layout", c_i32), ("shadow", c_i32), ("block", c_i32), ("occupancy", c_i32), ("stack", c_i32)]
 
     def as_dict(self):
-        return {"layout": {0: "fast", 1: "threaded", 2: "wide"}[self.layout],
+        return {"layout": {0: "fast", 1: "threaded", 2: "wide", 3: "cw8"}[self.layout],
                 "shadow": {0: "grid", 1: "persistent"}[self.shadow], "block": self.block,
                 "occupancy": self.occupancy, "stack": self.stack}
 
@@ -79,7 +81,7 @@ class _Camera(ctypes.Structure):
 
 
 class _Lights(ctypes.Structure):
-    _fields_ = [("tri_lights", vp), ("tri_count", c_i32), ("quad_count", c_i32)]
+    _fields_ = [("quad_lights", vp), ("tri_lights", vp), ("quad_count", c_i32), ("tri_count", c_i32)]
 
 
 class _Buffers(ctypes.Structure):
@@ -88,8 +90,8 @@ class _Buffers(ctypes.Structure):
 
 class LaunchInfo(ctypes.Structure):
     _fields_ = [("resolution", c_f * 2), ("camera", _Camera), ("lights", _Lights), ("buffers", _Buffers),
-                ("materials", vp), ("has_environment_map", c_i32), ("accumulate", c_i32), ("time", c_f),
-                ("max_depth", c_i32), ("samples", c_i32), ("frame", c_u32)]
+                ("materials", vp), ("environment_map", c_u64), ("has_environment_map", c_i32),
+                ("accumulate", c_i32), ("time", c_f), ("max_depth", c_i32), ("samples", c_i32), ("frame", c_u32)]
 
 
 class RenderStats(ctypes.Structure):
@@ -151,6 +153,10 @@ def lib():
             "kgr_debug_copy": (c_i32, [vp, ctypes.c_char_p, vp, c_u64]),
             "kgr_get_stage_times": (c_i32, [vp, vp, vp, c_u32]),
             "kgr_render_pt_noalloc": (c_i32, [vp, vp, c_i32, c_i32, c_i32, vp]),
+            "kgr_environment_create": (c_i32, [vp, c_u32, c_u32, c_i32, c_i32, vp]),
+            "kgr_environment_texture": (c_i32, [vp, vp]),
+            "kgr_environment_sample": (c_i32, [vp, vp, c_u32, vp, vp]),
+            "kgr_environment_destroy": (c_i32, [vp]),
             "kgr_mlp_create": (c_i32, [c_i32, c_u64, c_i32, vp]),
             "kgr_mlp_get_weights": (c_i32, [vp, vp]),
             "kgr_mlp_set_weights": (c_i32, [vp, vp]),
@@ -351,7 +357,7 @@ class Scene:
 
     def array(self, which):
         """Raw bytes (uint8) of one device array: ARRAY_THREADED, ARRAY_FAST_NODES,
-        ARRAY_WIDE_NODES or ARRAY_TRIANGLE_RECORDS."""
+        ARRAY_WIDE_NODES, ARRAY_TRIANGLE_RECORDS, ARRAY_CW8_NODES or ARRAY_CW8_TRIANGLES."""
         n = c_u64()
         check(lib().kgr_scene_copy_array(self.handle, which, None, 0, ctypes.byref(n)))
         out = np.zeros(n.value, np.uint8)
@@ -422,6 +428,55 @@ def camera_dict(info):
     c = info.camera
     return {"center": list(c.center), "ax_u": list(c.ax_u), "ax_v": list(c.ax_v), "ax_w": list(c.ax_w),
             "projection": list(c.projection), "view": list(c.view)}
+
+
+FILTER_LINEAR, FILTER_POINT = 0, 1
+
+
+class Environment:
+    """kgr_environment: an RGBA float environment map as a CUDA texture
+    object (normalised coordinates, wrap addressing; linear filtering as the
+    reference's set_envmap makes it, or point sampling)."""
+
+    def __init__(self, rgba, filter=FILTER_LINEAR, device=-1):
+        texels = np.ascontiguousarray(rgba, dtype=np.float32)
+        assert texels.ndim == 3 and texels.shape[2] == 4, "texels are (height, width, 4)"
+        self.height, self.width = texels.shape[:2]
+        self.texels = texels
+        self.filter = filter
+        h = vp()
+        check(lib().kgr_environment_create(_ptr(texels), self.width, self.height, filter, device, ctypes.byref(h)))
+        self.handle = h
+        t = c_u64()
+        check(lib().kgr_environment_texture(h, ctypes.byref(t)))
+        self.texture = t.value
+
+    def sample(self, uv_ptr, n, out_ptr, stream=None):
+        """tex2D<float4> at n (u, v) pairs: device arrays of 2 and 4 floats per entry."""
+        check(lib().kgr_environment_sample(self.handle, uv_ptr, n, out_ptr, stream))
+
+    def attach_to(self, info):
+        info.environment_map = self.texture
+        info.has_environment_map = 1
+        return info
+
+    def close(self):
+        if self.handle:
+            lib().kgr_environment_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def set_quad_lights(info, quads_ptr, count):
+    """Quad lights {a, ab, ac, intensity} (12 floats each, a device array) for a launch."""
+    info.lights.quad_lights = quads_ptr
+    info.lights.quad_count = count
+    return info
 
 
 TONEMAP_ACES, TONEMAP_SRGB = 0, 1

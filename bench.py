@@ -48,10 +48,12 @@ KERNELS = {("trace_closest", "fast"): "fast_persistent_kernel<closest, fast>",
            ("shadow", "fast"): "shadow_resolve_kernel<fast> | fast_persistent_kernel<any, fast>",
            ("trace_closest", "wide"): "fast_persistent_kernel<closest, wide>",
            ("shadow", "wide"): "shadow_resolve_kernel<wide> | fast_persistent_kernel<any, wide>",
+           ("trace_closest", "cw8"): "cw_persistent_kernel<closest>",
+           ("shadow", "cw8"): "shadow_resolve_kernel<cw8> | cw_persistent_kernel<any>",
            ("trace_closest", "threaded"): "trace_closest_kernel<threaded>",
            ("shadow", "threaded"): "shadow_resolve_kernel<threaded>"}
 # bytes a visit reads on each layout: (node, triangle)
-LAYOUT_BYTES = {"fast": (64, 48), "wide": (128, 48), "threaded": (48, 80)}
+LAYOUT_BYTES = {"fast": (64, 48), "wide": (128, 48), "cw8": (80, 48), "threaded": (48, 80)}
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
 # traversal kernels at this workload: one ncu capture of the 9 closest-hit and
 # 9 shadow launches of a timed 1080p frame (--cache-control none), averaged
@@ -70,7 +72,7 @@ def parse(argv=None):
     ap.add_argument("--spp", type=int, default=4)
     ap.add_argument("--max-depth", type=int, default=8)
     ap.add_argument("--scene", default="terrain")
-    ap.add_argument("--layout", default="auto", choices=["auto", "fast", "wide", "threaded"],
+    ap.add_argument("--layout", default="auto", choices=["auto", "fast", "wide", "cw8", "threaded"],
                     help="auto: the autotuner picks layout, shadow kernel and block size before warm-up")
     ap.add_argument("--trace-shadow", choices=["grid", "persistent"], help="shadow kernel (with --layout)")
     ap.add_argument("--trace-block", type=int, choices=[64, 128, 256], help="traversal block size (with --layout)")
@@ -492,11 +494,45 @@ def restir_runs(args):
     pyoracle.render_restir(osc, p, state)
     cpu_s = time.perf_counter() - t0
     _, _, di1080 = di_run(1920, 1080, 10)
+    # the direct light alone (max_depth 0), where ReSTIR's reuse acts: the
+    # DI frame against plain 1 spp, also on 99.9% of pixels (the 0.1% worst
+    # of each image trimmed: the reference's bias-corrected spatial weight
+    # leaves a few outliers)
+    ref0 = torch.zeros((W * H, 3), dtype=torch.float64, device="cuda")
+    a = kgr.Attachment("path_tracer")
+    a.attach(W, H)
+    a.load()
+    a.set_option("spp", 64)
+    for f in range(64):
+        a.render(kgr.launch_info(cam, W, H, [b.data_ptr() for b in bufs], max_depth=0, frame=1 << 21 | f), sc, sptr)
+        ref0 += bufs[0][:, :3].double()
+    ref0 /= 64
+    a.set_option("spp", 1)
+    a.render(kgr.launch_info(cam, W, H, [b.data_ptr() for b in bufs], max_depth=0, frame=4343), sc, sptr)
+    plain0 = bufs[0][:, :3].double().clone()
+    a.close()
+    att0 = kgr.Attachment("restir_di")
+    att0.attach(W, H)
+    att0.load()
+    for k, v in opts.items():
+        att0.set_option(k, v)
+    for f in range(30):
+        att0.render(kgr.launch_info(cam, W, H, [b.data_ptr() for b in bufs], max_depth=0, frame=f), sc, sptr)
+    di0 = bufs[0][:, :3].double().clone()
+    att0.close()
+
+    def relmse_pair(x, r):
+        e = ((x - r) ** 2 / (r * r + 1e-2)).mean(dim=1)
+        q = torch.quantile(e.float(), 0.999).item()
+        return {"all": round(e.mean().item(), 4), "trimmed_999": round(e[e <= q].mean().item(), 4)}
+
     out["restir_di_256"] = {"gpu_ms_per_frame": di256["gpu_ms_per_frame"],
                             "cpu_oracle_ms_per_frame": round(cpu_s * 1e3, 1), "cpu_cores": os.cpu_count(),
                             "scene_triangles": sc.info().triangle_count,
                             "relmse": relmse_di(di_frame), "plain_1spp_relmse": relmse_di(plain1),
-                            "relmse_reference": "plain PT at depth 2, 4096 spp, FP64 mean, same camera"}
+                            "relmse_reference": "plain PT at depth 2, 4096 spp, FP64 mean, same camera",
+                            "direct_only": {"restir_di": relmse_pair(di0, ref0), "plain_1spp": relmse_pair(plain0, ref0),
+                                            "reference": "plain PT at depth 0, 4096 spp, FP64 mean; DI frame 30"}}
     out["roofline_resampling"] = {
         "bound": "l2", "unit": "GB/s", "peak_l2_read_gbs": round(l2_gbs, 1), "peak_hbm_gbs": hbm,
         "work_unit": "per pixel per pass: temporal 2x32 + 32 + 48 B; spatial (1+k)(32+48) + 32 B, k = 5",

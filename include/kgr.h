@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define KGR_ABI_VERSION 3
+#define KGR_ABI_VERSION 4
 
 typedef enum kgr_status {
 	KGR_OK = 0,
@@ -93,6 +93,17 @@ typedef struct kgr_triangle_light {
 	float intensity[3];
 } kgr_triangle_light;
 
+/* Quad area light {a, ab, ac, intensity}: optix::QuadLight
+ * (include/optix/lighting.cuh:57-94), the parallelogram a + u ab + v ac for
+ * u, v in [0, 1].  Quads are lights only: they are sampled by next-event
+ * estimation and are not part of the traced geometry.  48 bytes. */
+typedef struct kgr_quad_light {
+	float a[3];
+	float ab[3];
+	float ac[3];
+	float intensity[3];
+} kgr_quad_light;
+
 /* One mesh of a scene.  Positions and normals are xyz triples; normals may be
  * NULL (the face normal is used).  `model` is an optional column-major 4x4
  * world transform (glm layout, the Hit::model of include/optix/sbt.cuh:14-21);
@@ -142,6 +153,8 @@ typedef struct kgr_scene_info {
 	float bounds_max[3];
 	uint32_t wide_node_count; /* 128-byte four-child nodes; 0 when the wide layout is not built */
 	uint32_t wide_max_stack;  /* most traversal stack entries a walk of the wide layout can hold */
+	uint32_t cw8_node_count;  /* 80-byte eight-child nodes; 0 when the compressed layout is not built */
+	uint32_t cw8_depth;       /* most compressed nodes on a root-to-leaf path */
 } kgr_scene_info;
 
 /* Build the BVH on the host and upload the scene to the device.  Emissive
@@ -189,7 +202,9 @@ enum {
 	KGR_ARRAY_THREADED = 0,         /* float4 x 3 per record, bvh.cpp layout */
 	KGR_ARRAY_FAST_NODES = 1,       /* 64-byte child-pair nodes */
 	KGR_ARRAY_WIDE_NODES = 2,       /* 128-byte four-child nodes */
-	KGR_ARRAY_TRIANGLE_RECORDS = 3  /* float4 x 3 per triangle in walk order: {v0, prim}, e1, e2 */
+	KGR_ARRAY_TRIANGLE_RECORDS = 3, /* float4 x 3 per triangle in walk order: {v0, prim}, e1, e2 */
+	KGR_ARRAY_CW8_NODES = 4,        /* 80-byte compressed eight-child nodes */
+	KGR_ARRAY_CW8_TRIANGLES = 5     /* float4 x 3 per triangle in compressed-node order: {v0, prim}, {e1, rank}, e2 */
 };
 kgr_status kgr_scene_copy_array(const kgr_scene *scene, int32_t which, void *out,
 		uint64_t capacity_bytes, uint64_t *bytes);
@@ -244,7 +259,12 @@ enum {
 	/* four-child BVH4 over the same padded boxes and triangle records as the
 	 * fast layout: half the dependent node fetches per ray; built when the
 	 * walk's worst-case stack fits the traversal stack */
-	KGR_LAYOUT_WIDE = 2
+	KGR_LAYOUT_WIDE = 2,
+	/* eight-child BVH8 with child boxes quantised to 8 bits a plane (80-byte
+	 * nodes, outward rounding) over the same padded boxes and triangles:
+	 * a third of the fast layout's dependent node fetches; built when the
+	 * leaves hold at most 4 triangles, requantised in place by a refit */
+	KGR_LAYOUT_CW8 = 3
 };
 
 /* Closest hit for n rays.  `rays` (device) holds 8 floats per ray:
@@ -312,9 +332,10 @@ typedef struct kgr_launch_info {
 		float view[16];
 	} camera;
 	struct {
+		const kgr_quad_light *quad_lights;     /* device; may be NULL when quad_count = 0 */
 		const kgr_triangle_light *tri_lights; /* device; NULL = the scene's */
+		int32_t quad_count;
 		int32_t tri_count;
-		int32_t quad_count; /* quad lights are not supported: must be 0 */
 	} lights;
 	struct {
 		float *color;
@@ -323,13 +344,36 @@ typedef struct kgr_launch_info {
 		float *position;
 	} buffers;
 	const kgr_material *materials; /* device; NULL = the scene's */
-	int32_t has_environment_map;   /* must be 0 */
+	/* cudaTextureObject_t of an RGBA float environment map (normalised
+	 * coordinates), e.g. from kgr_environment_create; read when
+	 * has_environment_map is set.  The "path_tracer" and "restir_di"
+	 * attachments light with it; the other consumers refuse it. */
+	uint64_t environment_map;
+	int32_t has_environment_map;
 	int32_t accumulate;
 	float time;
 	int32_t max_depth;
 	int32_t samples;
 	uint32_t frame; /* RNG stream index of this frame */
 } kgr_launch_info;
+
+/* Environment maps.  ArmadaRTX::set_envmap (source/amadeus/armada.cu:86-96)
+ * loads an image and imports it as a CUDA texture object with normalised
+ * coordinates and linear filtering (include/cuda/interop.cuh:96-135).  This
+ * makes the same kind of texture from host RGBA float texels (row 0 first,
+ * width * height * 4 floats): wrap addressing, KGR_FILTER_LINEAR as the
+ * reference does or KGR_FILTER_POINT.  The handle is what
+ * kgr_launch_info.environment_map takes. */
+enum { KGR_FILTER_LINEAR = 0, KGR_FILTER_POINT = 1 };
+typedef struct kgr_environment kgr_environment;
+kgr_status kgr_environment_create(const float *rgba, uint32_t width, uint32_t height, int32_t filter,
+		int32_t device, kgr_environment **out);
+kgr_status kgr_environment_texture(const kgr_environment *env, uint64_t *texture);
+/* tex2D<float4> of the texture at n (u, v) pairs (device arrays, 2 and 4
+ * floats per entry): what the kernels read for those coordinates. */
+kgr_status kgr_environment_sample(const kgr_environment *env, const float *uv, uint32_t n, float *rgba,
+		void *stream);
+kgr_status kgr_environment_destroy(kgr_environment *env);
 
 /* kind: "path_tracer", "restir_di" or "restir_gi". */
 kgr_status kgr_create(const char *kind, kgr_attachment **out);

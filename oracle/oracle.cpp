@@ -570,12 +570,101 @@ f3 sample_area_light(const TriLight &light, f3 &seed)
 	return light.a + u * light.ab + v * light.ac;
 }
 
+/* QuadLight (lighting.cuh:57-94): area = |ab x ac| */
+struct QuadLight {
+	f3 a, ab, ac, intensity;
+	float area() const { return length(cross(ab, ac)); }
+	f3 normal() const { return normalize(cross(ab, ac)); }
+};
+
+inline QuadLight load_quad(const kgr_quad_light &l)
+{
+	return QuadLight{mk(l.a[0], l.a[1], l.a[2]), mk(l.ab[0], l.ab[1], l.ab[2]),
+		mk(l.ac[0], l.ac[1], l.ac[2]), mk(l.intensity[0], l.intensity[1], l.intensity[2])};
+}
+
+/* sample_area_light(QuadLight) (lighting.cuh:123-131) */
+f3 sample_area_light(const QuadLight &light, f3 &seed)
+{
+	f3 r = pcg3f(seed);
+	float u = fract(r.x);
+	float v = fract(r.y);
+	return light.a + u * light.ab + v * light.ac;
+}
+
+const double PI_D = 3.14159265358979323846; /* M_PI */
+const float WORLD_RADIUS = 10000.0f;        /* Ld_Environment, amadeus_common.cuh:218 */
+
+/* u = atan2(d.x, d.z) / (2 M_PI) + 0.5, v = asin(d.y) / M_PI + 0.5
+ * (amadeus_path_tracer.cu:209-210): double arithmetic, one rounding. */
+inline void env_uv(const f3 &d, float &u, float &v)
+{
+	u = (float)((double)katan2(d.x, d.z) / (2.0 * PI_D) + 0.5);
+	v = (float)((double)kasin(d.y) / PI_D + 0.5);
+}
+
+/* tex2D<float4> of the environment map with normalised coordinates and wrap
+ * addressing, by the texture-fetching rules of the CUDA C++ Programming
+ * Guide: the coordinate's fraction times the extent; point sampling takes
+ * the texel it falls in, linear filtering blends the four texels around it
+ * (minus half a texel) with weights held in fixed point with 8 fractional
+ * bits. */
+f3 env_fetch(const oracle_scene *s, float u, float v)
+{
+	const int W = (int)s->env_width, H = (int)s->env_height;
+	float x = (u - floorf(u)) * (float)W;
+	float y = (v - floorf(v)) * (float)H;
+	auto texel = [&](int i, int j) {
+		i %= W;
+		j %= H;
+		if (i < 0)
+			i += W;
+		if (j < 0)
+			j += H;
+		const float *t = s->env + 4 * ((size_t)j * W + i);
+		return mk(t[0], t[1], t[2]);
+	};
+	if (s->env_filter == KGR_FILTER_POINT)
+		return texel((int)floorf(x), (int)floorf(y));
+	float xb = x - 0.5f, yb = y - 0.5f;
+	float i0 = floorf(xb), j0 = floorf(yb);
+	float a = roundf((xb - i0) * 256.0f) / 256.0f;
+	float b = roundf((yb - j0) * 256.0f) / 256.0f;
+	int i = (int)i0, j = (int)j0;
+	return ((1.0f - a) * (1.0f - b)) * texel(i, j) + (a * (1.0f - b)) * texel(i + 1, j)
+		+ ((1.0f - a) * b) * texel(i, j + 1) + (a * b) * texel(i + 1, j + 1);
+}
+
+/* The environment light's direction: seed = rand_uniform_3f(seed), theta =
+ * acos(sqrt(1 - seed.x)), phi = 2 pi seed.y -- float with brdf.cuh's PI in
+ * Ld_Environment (amadeus_common.cuh:215-238), double with M_PI in
+ * sample_direct (:343-374). */
+f3 env_direction(f3 &seed, bool phi_double)
+{
+	seed = rand_uniform_3f(seed);
+	float theta = kacos(ksqrt(1.0f - fract(seed.x)));
+	float phi = phi_double ? (float)(2.0 * PI_D * (double)fract(seed.y))
+		: 2.0f * 3.14159265358979323846f * fract(seed.y);
+	float st = ksin(theta);
+	return mk(st * kcos(phi), st * ksin(phi), kcos(theta));
+}
+
+/* FullLightSample of sample_direct (amadeus_common.cuh:289-377) */
+struct LightPoint {
+	f3 Le, normal, point;
+	float pdf;
+	int type; /* 0 quad, 1 triangle, 2 environment */
+	float env_u, env_v;
+};
+
 const float SHADOW_EPS = 0.05f; /* is_occluded, amadeus_common.cuh:193 */
 const float OFFSET_EPS = 1e-3f; /* amadeus_common.cuh:22 */
 
 struct Ctx {
 	const oracle_scene *s;
 	std::vector<TriLight> lights;
+	std::vector<QuadLight> quads;
+	bool env_flip_v = false; /* the path tracer's miss reads (u, 1 - v) */
 	oracle_render_stats stats;
 	uint64_t internal = 0, leaves = 0;
 	float tmax_closest = 1e16f;
@@ -586,50 +675,124 @@ struct Ctx {
 		return trace_any(s, o, d, R - SHADOW_EPS, &internal, &leaves);
 	}
 
-	/* Ld_light (lighting.cuh:149-174) + Ld (amadeus_common.cuh:256-286),
-	 * triangle lights only (no quads, no environment map). */
+	bool has_env() const { return s->env != nullptr; }
+
+	/* __miss__ (amadeus_path_tracer.cu:204-220, amadeus_restir.cu:561-578) */
+	f3 env_miss(const f3 &d) const
+	{
+		if (!has_env())
+			return mk(0.0f);
+		float u, v;
+		env_uv(d, u, v);
+		return env_fetch(s, u, env_flip_v ? 1.0f - v : v);
+	}
+
+	/* Ld (amadeus_common.cuh:256-286): a uniform pick over the quad lights,
+	 * the triangle lights and the environment, with Ld_light
+	 * (lighting.cuh:149-174) or Ld_Environment (amadeus_common.cuh:215-254). */
 	f3 Ld(const SurfaceHit &sh, f3 &seed)
 	{
-		int total_count = (int)lights.size();
+		unsigned int nq = (unsigned int)quads.size(), nt = (unsigned int)lights.size();
+		unsigned int total_count = nq + nt + (has_env() ? 1u : 0u);
 		if (total_count == 0)
 			return mk(0.0f);
 		unsigned int i = (unsigned int)(rand_uniform(seed) * total_count);
 		f3 contr = mk(0.0f);
 		float pdf = 1.0f / total_count;
 		float light_pdf = 0.0f;
-		if (i < (unsigned int)total_count) {
-			const TriLight &light = lights[i];
-			light_pdf = 1.0f / light.area();
-			f3 lpos = sample_area_light(light, seed);
+		if (i < nq + nt) {
+			f3 lpos, lnormal, Le;
+			if (i < nq) {
+				const QuadLight &light = quads[i];
+				light_pdf = 1.0f / light.area();
+				lpos = sample_area_light(light, seed);
+				lnormal = light.normal();
+				Le = light.intensity;
+			} else {
+				const TriLight &light = lights[i - nq];
+				light_pdf = 1.0f / light.area();
+				lpos = sample_area_light(light, seed);
+				lnormal = light.normal();
+				Le = light.intensity;
+			}
 			f3 wi = normalize(lpos - sh.x);
 			float R = length(lpos - sh.x);
 			if (!occluded(sh.x, wi, R)) {
 				f3 f = brdf(sh, wi);
-				float ldot = fabsf(dot(light.normal(), wi));
+				float ldot = fabsf(dot(lnormal, wi));
 				float geometric = ldot * fabsf(dot(sh.n, wi)) / (R * R);
-				contr = f * light.intensity * geometric;
+				contr = f * Le * geometric;
+			}
+		} else {
+			f3 wi = env_direction(seed, false);
+			float u, v;
+			env_uv(wi, u, v);
+			f3 Li = env_fetch(s, u, v);
+			light_pdf = (float)(1.0 / (4.0 * PI_D));
+			if (!occluded(sh.x, wi, WORLD_RADIUS)) {
+				f3 f = brdf(sh, wi) * fabsf(dot(sh.n, wi));
+				contr = f * Li;
 			}
 		}
 		pdf *= light_pdf;
 		return contr / pdf;
 	}
 
-	/* sample_direct (amadeus_common.cuh:301-377), triangle branch */
-	void sample_direct(const SurfaceHit &sh, f3 &seed, int &index, f3 &point, float &pdf)
+	/* sample_direct (amadeus_common.cuh:301-377).  Returns the light's place
+	 * among quads + triangles + environment, or -1 with nothing to pick. */
+	int sample_direct(const SurfaceHit &sh, f3 &seed, LightPoint &lp)
 	{
-		(void)sh;
-		unsigned int total_lights = (unsigned int)lights.size();
-		unsigned int light_index = (unsigned int)(rand_uniform(seed) * total_lights);
-		if (light_index < total_lights) {
-			const TriLight &light = lights[light_index];
-			point = sample_area_light(light, seed);
-			pdf = 1.0f / (light.area() * total_lights);
-			index = (int)light_index;
-		} else {
-			index = -1;
-			point = mk(0.0f);
-			pdf = 0.0f;
+		unsigned int nq = (unsigned int)quads.size(), nt = (unsigned int)lights.size();
+		unsigned int total = nq + nt + (has_env() ? 1u : 0u);
+		unsigned int li = (unsigned int)(rand_uniform(seed) * total);
+		lp.env_u = lp.env_v = 0.0f;
+		if (li < nq) {
+			const QuadLight &l = quads[li];
+			lp.point = sample_area_light(l, seed);
+			lp.Le = l.intensity;
+			lp.normal = l.normal();
+			lp.pdf = 1.0f / (l.area() * total);
+			lp.type = 0;
+			return (int)li;
 		}
+		if (li < nq + nt) {
+			const TriLight &l = lights[li - nq];
+			lp.point = sample_area_light(l, seed);
+			lp.Le = l.intensity;
+			lp.normal = l.normal();
+			lp.pdf = 1.0f / (l.area() * total);
+			lp.type = 1;
+			return (int)li;
+		}
+		if (li < total) {
+			f3 wi = env_direction(seed, true);
+			lp.point = sh.x + wi * WORLD_RADIUS;
+			env_uv(wi, lp.env_u, lp.env_v);
+			lp.Le = env_fetch(s, lp.env_u, lp.env_v);
+			lp.normal = -wi;
+			lp.pdf = (float)(1.0 / (4.0 * PI_D * (double)total));
+			lp.type = 2;
+			return (int)li;
+		}
+		lp.point = mk(0.0f);
+		lp.pdf = 0.0f;
+		lp.type = -1;
+		return -1;
+	}
+
+	/* direct_unoccluded / direct_occluded (amadeus_common.cuh:380-421): the
+	 * environment (type 2) has no light cosine and no 1/d^2 */
+	f3 direct_typed(const SurfaceHit &sh, const f3 &Le, const f3 &normal, int type, f3 D, float d, bool test)
+	{
+		if (test && occluded(sh.x, D, d))
+			return mk(0.0f);
+		f3 rho = brdf(sh, D);
+		float geometric = fabsf(dot(sh.n, D));
+		if (type != 2) {
+			float ldot = fabsf(dot(normal, D));
+			geometric *= ldot / (d * d);
+		}
+		return rho * Le * geometric;
 	}
 
 	/* direct_unoccluded (amadeus_common.cuh:380-397) */
@@ -735,15 +898,24 @@ PathResult trace_path(Ctx &ctx, const oracle_render_params *p, f3 o, f3 d, f3 &s
 	r.normal = r.albedo = r.position = mk(0.0f);
 	r.hit = false;
 	f3 beta = mk(1.0f);
+	/* with an environment map the ray past the last vertex is cast too: the
+	 * miss program has no depth test, so its miss sees the map, while its
+	 * hit adds nothing */
+	const int last = p->max_depth + (ctx.has_env() ? 1 : 0);
 	for (int depth = 0;; depth++) {
-		if (depth > p->max_depth)
+		if (depth > last)
 			break;
 		if (depth == 0)
 			ctx.stats.camera_rays++;
 		else
 			ctx.stats.bounce_rays++;
 		kgr_hit h = trace_closest(ctx.s, o, d, ctx.tmax_closest, &ctx.internal, &ctx.leaves);
-		if (h.prim < 0)
+		if (h.prim < 0) {
+			if (ctx.has_env())
+				r.L = r.L + beta * ctx.env_miss(d);
+			break;
+		}
+		if (depth > p->max_depth)
 			break;
 		SurfaceHit sh;
 		if (!surface(ctx.s, h, d, sh))
@@ -811,6 +983,14 @@ inline void accumulate4(float *buf, size_t i, const f3 &v, float w, bool acc, fl
 	}
 }
 
+std::vector<QuadLight> load_quads(const oracle_scene *s)
+{
+	std::vector<QuadLight> q;
+	for (uint32_t i = 0; i < s->quad_count; i++)
+		q.push_back(load_quad(s->quads[i]));
+	return q;
+}
+
 std::vector<TriLight> load_lights(const oracle_scene *s)
 {
 	std::vector<TriLight> v(s->light_count);
@@ -838,14 +1018,40 @@ int nthreads(int t)
 
 /* ============================================================== ReSTIR == */
 
+/* A light sample: `light` is the light's place among quads + triangles,
+ * -1 for none, or for the environment the bits of -u (negative, never -1)
+ * with v in env_v; the map is read again at (u, v) for its Le. */
 struct Sample {
 	int light;
 	f3 point;
+	float env_v;
 };
+
+inline bool has_light(const Sample &smp) { return smp.light != -1; }
+
+/* Le, normal and type of a sample's light */
+int emitter(const Ctx &ctx, const Sample &smp, f3 &Le, f3 &normal)
+{
+	if (smp.light >= 0) {
+		if ((size_t)smp.light < ctx.quads.size()) {
+			const QuadLight &l = ctx.quads[smp.light];
+			Le = l.intensity;
+			normal = l.normal();
+			return 0;
+		}
+		const TriLight &l = ctx.lights[smp.light - (int)ctx.quads.size()];
+		Le = l.intensity;
+		normal = l.normal();
+		return 1;
+	}
+	Le = env_fetch(ctx.s, -u2f((uint32_t)smp.light), smp.env_v);
+	normal = mk(0.0f);
+	return 2;
+}
 
 /* Reservoir<T> (include/amadeus/reservoir.cuh:19-75) */
 struct Reservoir {
-	Sample data = {-1, {0.0f, 0.0f, 0.0f}};
+	Sample data = {-1, {0.0f, 0.0f, 0.0f}, 0.0f};
 	float w = 0.0f, W = 0.0f;
 	int M = 0;
 	f3 seed;
@@ -879,12 +1085,13 @@ struct Reservoir {
 const uint32_t RIS_SALT = 0x9E3779B9u;
 
 struct RestirBufs {
-	int32_t *light; float *point; float *w; float *W; int32_t *M;
+	int32_t *light; float *point; float *w; float *W; int32_t *M; float *env_v;
 	Reservoir get(size_t i) const
 	{
 		Reservoir r;
 		r.data.light = light[i];
 		r.data.point = mk(point[3 * i], point[3 * i + 1], point[3 * i + 2]);
+		r.data.env_v = env_v[i];
 		r.w = w[i];
 		r.W = W[i];
 		r.M = M[i];
@@ -893,6 +1100,7 @@ struct RestirBufs {
 	void set(size_t i, const Reservoir &r) const
 	{
 		light[i] = r.data.light;
+		env_v[i] = r.data.env_v;
 		point[3 * i] = r.data.point.x;
 		point[3 * i + 1] = r.data.point.y;
 		point[3 * i + 2] = r.data.point.z;
@@ -911,24 +1119,26 @@ struct RestirBufs {
 /* target (amadeus_restir.cu:147-161) */
 float target(Ctx &ctx, const Sample &smp, const SurfaceHit &hit)
 {
-	if (smp.light < 0)
+	if (!has_light(smp))
 		return 0.0f;
-	const TriLight &l = ctx.lights[smp.light];
+	f3 Le, ln;
+	int type = emitter(ctx, smp, Le, ln);
 	f3 D = smp.point - hit.x;
 	float d = length(D);
-	f3 Li = ctx.direct_unoccluded(hit, l.intensity, l.normal(), D / d, d);
+	f3 Li = ctx.direct_typed(hit, Le, ln, type, D / d, d, false);
 	return Li.x + Li.y + Li.z;
 }
 
 /* occluded_target (amadeus_restir.cu:163-178) */
 float occluded_target(Ctx &ctx, const Sample &smp, const SurfaceHit &hit)
 {
-	if (smp.light < 0)
+	if (!has_light(smp))
 		return 0.0f;
-	const TriLight &l = ctx.lights[smp.light];
+	f3 Le, ln;
+	int type = emitter(ctx, smp, Le, ln);
 	f3 D = smp.point - hit.x;
 	float d = length(D);
-	f3 Li = ctx.direct_occluded(hit, l.intensity, l.normal(), D / d, d);
+	f3 Li = ctx.direct_typed(hit, Le, ln, type, D / d, d, true);
 	return Li.x + Li.y + Li.z;
 }
 
@@ -1113,6 +1323,8 @@ static void render_pt_rows(const oracle_scene *s, const oracle_render_params *p,
 		Ctx ctx;
 		ctx.s = s;
 		ctx.lights = lights;
+		ctx.quads = load_quads(s);
+		ctx.env_flip_v = true;
 		ctx.stats = {0, 0, 0};
 #pragma omp for schedule(dynamic, 64)
 		for (int64_t k = 0; k < npix; k++) {
@@ -1173,8 +1385,8 @@ void oracle_render_restir(const oracle_scene *s, const oracle_render_params *p,
 {
 	std::vector<TriLight> lights = load_lights(s);
 	int64_t npix = (int64_t)p->width * p->height;
-	RestirBufs A = {st->cur_light, st->cur_point, st->cur_w, st->cur_W, st->cur_M};
-	RestirBufs B = {st->prev_light, st->prev_point, st->prev_w, st->prev_W, st->prev_M};
+	RestirBufs A = {st->cur_light, st->cur_point, st->cur_w, st->cur_W, st->cur_M, st->cur_env_v};
+	RestirBufs B = {st->prev_light, st->prev_point, st->prev_w, st->prev_W, st->prev_M, st->prev_env_v};
 	oracle_render_stats total = {0, 0, 0};
 	float count = (float)p->samples;
 	bool acc = p->accumulate != 0;
@@ -1185,6 +1397,7 @@ void oracle_render_restir(const oracle_scene *s, const oracle_render_params *p,
 		Ctx ctx;
 		ctx.s = s;
 		ctx.lights = lights;
+		ctx.quads = load_quads(s);
 		ctx.stats = {0, 0, 0};
 #pragma omp for schedule(dynamic, 64)
 		for (int64_t k = 0; k < npix; k++) {
@@ -1199,28 +1412,37 @@ void oracle_render_restir(const oracle_scene *s, const oracle_render_params *p,
 				res.seed = pixel_seed(pix, p->frame, RIS_SALT);
 				res.data.light = -1;
 				res.data.point = mk(0.0f);
+				res.data.env_v = 0.0f;
 				for (int i = 0; i < p->candidates; i++) {
 					Sample smp;
-					float pdf;
-					ctx.sample_direct(sh, pseed, smp.light, smp.point, pdf);
-					float tgt = 0.0f;
-					if (smp.light >= 0) {
-						const TriLight &l = ctx.lights[smp.light];
+					LightPoint lp;
+					int li = ctx.sample_direct(sh, pseed, lp);
+					float pdf = 0.0f, tgt = 0.0f;
+					if (li >= 0) {
+						smp.light = lp.type == 2 ? (int)f2u(-lp.env_u) : li;
+						smp.point = lp.point;
+						smp.env_v = lp.env_v;
+						pdf = lp.pdf;
 						f3 D = smp.point - sh.x;
 						float dd = length(D);
-						f3 Li = ctx.direct_unoccluded(sh, l.intensity, l.normal(), D / dd, dd);
+						f3 Li = ctx.direct_typed(sh, lp.Le, lp.normal, lp.type, D / dd, dd, false);
 						tgt = Li.x + Li.y + Li.z;
+					} else {
+						smp.light = -1;
+						smp.point = mk(0.0f);
+						smp.env_v = 0.0f;
 					}
 					res.update(smp, (pdf > 0) ? tgt / pdf : 0);
 				}
 				float tgt = 0.0f;
 				f3 D = mk(0.0f);
 				float dd = 0.0f;
-				if (res.data.light >= 0) {
-					const TriLight &l = ctx.lights[res.data.light];
+				if (has_light(res.data)) {
+					f3 Le, ln;
+					int type = emitter(ctx, res.data, Le, ln);
 					D = res.data.point - sh.x;
 					dd = length(D);
-					f3 Li = ctx.direct_occluded(sh, l.intensity, l.normal(), D / dd, dd);
+					f3 Li = ctx.direct_typed(sh, Le, ln, type, D / dd, dd, true);
 					tgt = Li.x + Li.y + Li.z;
 				}
 				res.resample(tgt);
@@ -1259,6 +1481,7 @@ void oracle_render_restir(const oracle_scene *s, const oracle_render_params *p,
 			Ctx ctx;
 			ctx.s = s;
 			ctx.lights = lights;
+			ctx.quads = load_quads(s);
 			ctx.stats = {0, 0, 0};
 #pragma omp for schedule(dynamic, 64)
 			for (int64_t k = 0; k < npix; k++) {
@@ -1307,6 +1530,7 @@ void oracle_render_restir(const oracle_scene *s, const oracle_render_params *p,
 			Ctx ctx;
 			ctx.s = s;
 			ctx.lights = lights;
+			ctx.quads = load_quads(s);
 			ctx.stats = {0, 0, 0};
 			const int K = p->spatial_neighbors;
 			std::vector<SurfaceHit> hits(K);
@@ -1357,11 +1581,12 @@ void oracle_render_restir(const oracle_scene *s, const oracle_render_params *p,
 					float denominator = t_merged * Z;
 					merged.W = (denominator > 0.0f) ? merged.w / denominator : 0.0f;
 					f3 lighting = mk(0.0f);
-					if (merged.data.light >= 0) {
-						const TriLight &l = ctx.lights[merged.data.light];
+					if (has_light(merged.data)) {
+						f3 Le, ln;
+						int type = emitter(ctx, merged.data, Le, ln);
 						f3 D = merged.data.point - hit.x;
 						float dd = length(D);
-						lighting = ctx.direct_occluded(hit, l.intensity, l.normal(), D / dd, dd);
+						lighting = ctx.direct_typed(hit, Le, ln, type, D / dd, dd, true);
 					}
 					direct = hit.mat.emission + lighting * merged.W;
 					out.set(pix, merged);
@@ -1880,6 +2105,23 @@ extern "C" void oracle_render_gi(const oracle_scene *s, const oracle_render_para
 
 /* --------------------------------------------------------- known answers */
 
+void oracle_env_lookup(const float *texels, uint32_t width, uint32_t height, int filter, const float *uv,
+		uint32_t n, float *rgb)
+{
+	oracle_scene s;
+	memset(&s, 0, sizeof(s));
+	s.env = texels;
+	s.env_width = width;
+	s.env_height = height;
+	s.env_filter = filter;
+	for (uint32_t i = 0; i < n; i++) {
+		f3 c = env_fetch(&s, uv[2 * i], uv[2 * i + 1]);
+		rgb[3 * i] = c.x;
+		rgb[3 * i + 1] = c.y;
+		rgb[3 * i + 2] = c.z;
+	}
+}
+
 void oracle_kat_rng(float sx, float sy, float sz, int draws, float *out)
 {
 	f3 seed = mk(sx, sy, sz);
@@ -1953,6 +2195,14 @@ void oracle_kat_math(const float *x, int n, float *out)
 		out[5 * i + 2] = ktan(x[i]);
 		out[5 * i + 3] = katan(x[i]);
 		out[5 * i + 4] = kacos(x[i]);
+	}
+}
+
+void oracle_kat_atan2_asin(const float *y, const float *x, int n, float *out)
+{
+	for (int i = 0; i < n; i++) {
+		out[2 * i + 0] = katan2(y[i], x[i]);
+		out[2 * i + 1] = kasin(y[i]);
 	}
 }
 

@@ -40,6 +40,14 @@ typedef struct oracle_scene {
 	uint32_t light_count;
 	uint32_t bvh_vec4_count;
 	uint32_t pad;
+	/* quad lights and an environment map (NULL / 0 for none): RGBA float
+	 * texels, row 0 first, read with normalised coordinates and wrap
+	 * addressing, point-sampled or linearly filtered */
+	const kgr_quad_light *quads;
+	const float *env;
+	uint32_t quad_count;
+	uint32_t env_width, env_height;
+	int32_t env_filter; /* KGR_FILTER_LINEAR or KGR_FILTER_POINT */
 } oracle_scene;
 
 typedef struct oracle_trace_stats {
@@ -114,6 +122,8 @@ typedef struct oracle_restir_state {
 	kgr_material *materials;
 	float *intermediate; /* float4 */
 	float *auxiliary;    /* float4 */
+	/* v of environment samples (light < -1 holds the bits of -u) */
+	float *cur_env_v; float *prev_env_v;
 } oracle_restir_state;
 
 /* One ReSTIR DI frame: initial (amadeus_restir.cu:82-144,437-559), temporal
@@ -144,6 +154,11 @@ typedef struct oracle_gi_state {
 void oracle_render_gi(const oracle_scene *s, const oracle_render_params *p, oracle_gi_state *st,
 		float *color, float *direct, oracle_render_stats *stats);
 
+/* The environment map's texture read (normalised coordinates, wrap
+ * addressing) at n (u, v) pairs: rgb gets 3 floats per pair. */
+void oracle_env_lookup(const float *texels, uint32_t width, uint32_t height, int filter, const float *uv,
+		uint32_t n, float *rgb);
+
 /* Known-answer helpers exposed for the golden-vector tests. */
 void oracle_kat_rng(float seed_x, float seed_y, float seed_z, int draws, float *out);
 float oracle_kat_intersect(const float *v1, const float *v2, const float *v3,
@@ -153,6 +168,7 @@ void oracle_kat_brdf_eval(const kgr_material *m, const float *n, const float *wo
 		const float *seed_in, float *f_wi_pdf_seed);
 void oracle_kat_brdf(const kgr_material *m, const float *n, const float *wo, const float *wi, float *f_pdf);
 void oracle_kat_math(const float *x, int n, float *sin_cos_tan_atan_acos);
+void oracle_kat_atan2_asin(const float *y, const float *x, int n, float *atan2_asin);
 
 /* hdr_to_ldr of include/cuda/color.cuh:84-103: mode 0 ACES, 1 sRGB; ldr rows
  * bottom to top, packed as to_ui32 (cast.cuh:16-20). */

@@ -22,7 +22,9 @@ class OracleScene(ctypes.Structure):
                 ("lights", ctypes.c_void_p), ("bvh", ctypes.c_void_p),
                 ("vertex_count", ctypes.c_uint32), ("triangle_count", ctypes.c_uint32),
                 ("material_count", ctypes.c_uint32), ("light_count", ctypes.c_uint32),
-                ("bvh_vec4_count", ctypes.c_uint32), ("pad", ctypes.c_uint32)]
+                ("bvh_vec4_count", ctypes.c_uint32), ("pad", ctypes.c_uint32),
+                ("quads", ctypes.c_void_p), ("env", ctypes.c_void_p), ("quad_count", ctypes.c_uint32),
+                ("env_width", ctypes.c_uint32), ("env_height", ctypes.c_uint32), ("env_filter", ctypes.c_int32)]
 
 
 class TraceStats(ctypes.Structure):
@@ -63,7 +65,7 @@ class RestirState(ctypes.Structure):
     _fields_ = [(n, ctypes.c_void_p) for n in (
         "cur_light", "cur_point", "cur_w", "cur_W", "cur_M",
         "prev_light", "prev_point", "prev_w", "prev_W", "prev_M",
-        "materials", "intermediate", "auxiliary")]
+        "materials", "intermediate", "auxiliary", "cur_env_v", "prev_env_v")]
 
 
 class GiStateC(ctypes.Structure):
@@ -130,6 +132,7 @@ def lib():
                                        ctypes.POINTER(GiStateC), vp, vp, ctypes.POINTER(RenderStats)]
         L.oracle_kat_rng.argtypes = [ctypes.c_float] * 3 + [ctypes.c_int, vp]
         L.oracle_tonemap.argtypes = [vp, vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int]
+        L.oracle_env_lookup.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int, vp, ctypes.c_uint32, vp]
         L.oracle_generate_scene.restype = ctypes.c_int
         L.oracle_generate_scene.argtypes = [ctypes.c_char_p, ctypes.c_uint64, ctypes.POINTER(vp)]
         L.oracle_generated_view.argtypes = [vp, ctypes.POINTER(SceneArrays)]
@@ -145,6 +148,7 @@ def lib():
         L.oracle_kat_brdf_eval.argtypes = [vp] * 5
         L.oracle_kat_brdf.argtypes = [vp] * 5
         L.oracle_kat_math.argtypes = [vp, ctypes.c_int, vp]
+        L.oracle_kat_atan2_asin.argtypes = [vp, vp, ctypes.c_int, vp]
         _LIB = L
     return _LIB
 
@@ -160,17 +164,24 @@ class Scene:
     materials: structured kgr_material array as raw float32 (M,16);
     lights: (L,12) float32; bvh: (K,4) float32 threaded layout."""
 
-    def __init__(self, positions, normals, tris, materials, lights, bvh):
+    def __init__(self, positions, normals, tris, materials, lights, bvh, quads=None, env=None, env_filter=0):
+        """quads: (Q,12) float32 {a, ab, ac, intensity}; env: (H,W,4) float32 texels
+        of the environment map, env_filter 0 linear / 1 point."""
         self.positions = np.ascontiguousarray(positions, dtype=np.float32)
         self.normals = np.ascontiguousarray(normals, dtype=np.float32)
         self.tris = np.ascontiguousarray(tris, dtype=np.uint32)
         self.materials = np.ascontiguousarray(materials, dtype=np.float32)
         self.lights = np.ascontiguousarray(lights, dtype=np.float32)
         self.bvh = np.ascontiguousarray(bvh, dtype=np.float32)
+        self.quads = None if quads is None or len(quads) == 0 else np.ascontiguousarray(quads, np.float32)
+        self.env = None if env is None else np.ascontiguousarray(env, np.float32)
         self.c = OracleScene(ptr(self.positions), ptr(self.normals), ptr(self.tris),
                              ptr(self.materials), ptr(self.lights), ptr(self.bvh),
                              len(self.positions), len(self.tris), len(self.materials),
-                             len(self.lights), len(self.bvh), 0)
+                             len(self.lights), len(self.bvh), 0,
+                             ptr(self.quads), ptr(self.env), 0 if self.quads is None else len(self.quads),
+                             0 if self.env is None else self.env.shape[1],
+                             0 if self.env is None else self.env.shape[0], env_filter)
 
     def triangle_boxes(self):
         boxes = np.zeros((len(self.tris), 6), np.float32)
@@ -265,6 +276,7 @@ class RestirBuffers:
             "prev_M": np.zeros(n, np.int32),
             "materials": np.zeros((n, 16), np.float32),
             "intermediate": np.zeros((n, 4), np.float32), "auxiliary": np.zeros((n, 4), np.float32),
+            "cur_env_v": np.zeros(n, np.float32), "prev_env_v": np.zeros(n, np.float32),
         }
         self.c = RestirState(*[ptr(self.arrays[f[0]]) for f in RestirState._fields_])
 
@@ -329,6 +341,15 @@ class GeneratedScene:
     def scene(self, max_leaf=4):
         return Scene(self.positions, self.normals, self.tris4(), self.materials_raw, self.lights(),
                      self.sah_bvh(max_leaf))
+
+
+def env_lookup(texels, uv, filt=0):
+    """The oracle's texture read of an (H, W, 4) map at (N, 2) coordinates -> (N, 3)."""
+    t = np.ascontiguousarray(texels, np.float32)
+    uv = np.ascontiguousarray(uv, np.float32)
+    out = np.zeros((len(uv), 3), np.float32)
+    lib().oracle_env_lookup(ptr(t), t.shape[1], t.shape[0], filt, ptr(uv), len(uv), ptr(out))
+    return out
 
 
 def camera(eye, target, fov, aspect, up=(0.0, 1.0, 0.0)):

@@ -1,4 +1,4 @@
-"""The autotuner: every traversal launch shape (layout fast or wide, shadow
+"""The autotuner: every traversal launch shape (layout fast, wide or cw8, shadow
 kernel, block size, occupancy, shared-memory stack entries) renders the same image, so tuning changes speed only --
 the frame after kgr_autotune is bit-identical to the frame before it, for an
 attachment and for the batcher; options still override the tuned shape."""
@@ -32,9 +32,9 @@ def test_attachment_autotune_keeps_the_image(kind):
     torch.cuda.synchronize()
     before = bufs[0].clone()
     res = att.autotune(info, sc, frames=2)
-    # fast and wide x 2 shadow kernels x 3 block sizes x 2 occupancies, then the best with 8 and 16
-    # shared-memory stack entries
-    assert res["candidates"] == 26
+    # fast, wide and cw8 x 2 shadow kernels x 3 block sizes x 2 occupancies, then the best with 8
+    # and 16 shared-memory stack entries
+    assert res["candidates"] == 38
     assert 0 < res["best_ms"] <= res["default_ms"]
     assert att.trace_tune() == res["best"]
     att.render(info, sc)
@@ -59,8 +59,8 @@ def test_batcher_autotune_keeps_the_image():
     torch.cuda.synchronize()
     before = [o.clone() for o in outs]
     res = b.autotune(sc, jobs, frames=2, max_depth=4)
-    assert res["candidates"] == 26 and 0 < res["best_ms"] <= res["default_ms"]
-    layout = {"fast": kgr.LAYOUT_FAST, "wide": kgr.LAYOUT_WIDE}[res["best"]["layout"]]
+    assert res["candidates"] == 38 and 0 < res["best_ms"] <= res["default_ms"]
+    layout = {"fast": kgr.LAYOUT_FAST, "wide": kgr.LAYOUT_WIDE, "cw8": kgr.LAYOUT_CW8}[res["best"]["layout"]]
     b.render(sc, jobs, max_depth=4, layout=layout)
     torch.cuda.synchronize()
     for o, ref in zip(outs, before):

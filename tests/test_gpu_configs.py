@@ -67,7 +67,7 @@ def band_rows():
     return np.concatenate([np.arange(r0 * W2, r1 * W2) for r0, r1 in BANDS])
 
 
-@pytest.mark.parametrize("layout", ["fast", "wide", "threaded"])
+@pytest.mark.parametrize("layout", ["fast", "wide", "cw8", "threaded"])
 def test_pt_terrain_1080p_4spp_ggx_matches_oracle(terrain, terrain_oracle_bands, layout):
     """C2 as configured; tolerance 1e-4 relative on >= 99.9% of band pixels."""
     g, sc, osc = terrain
@@ -166,7 +166,7 @@ def orbit(g, f, deg=0.5):
     return np.array([ca * e[0] + sa * e[2], e[1], -sa * e[0] + ca * e[2]], np.float32) + g.target
 
 
-@pytest.mark.parametrize("layout", ["fast", "threaded"])
+@pytest.mark.parametrize("layout", ["fast", "cw8", "threaded"])
 def test_restir_gi_on_ggx_terrain_matches_oracle(layout):
     """ReSTIR GI with C3's reuse settings (M-cap 30, 3 spatial iterations of
     8 neighbours) on the GGX terrain, three orbit frames, depth 8 with

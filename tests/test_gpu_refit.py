@@ -295,3 +295,37 @@ def test_refit_of_a_one_triangle_scene():
         assert np.array_equal(gpu_closest(sc, rays, layout).view(np.uint32), ref["raw"].view(np.uint32))
         assert np.array_equal(gpu_any(sc, short, layout), occ)
     sc.close()
+
+
+def test_refit_requantises_the_compressed_layout(gen):
+    """The compressed layout is refitted in place: its nodes are requantised
+    from the refitted boxes by the builder's own rules, its triangle records
+    move with the vertices, and every hit stays equal to the threaded walk
+    and the oracle on the moved scene."""
+    sc = kgr.Scene(None, None, gen.materials_raw, meshes=split_meshes(gen, M0))
+    n = sc.info().cw8_node_count
+    assert n > 0
+    before = sc.array(kgr.ARRAY_CW8_NODES).copy()
+    sc.set_transforms([1, 2], [M1[1], M1[2]])
+    assert sc.info().cw8_node_count == n
+    after = sc.array(kgr.ARRAY_CW8_NODES)
+    assert not np.array_equal(before, after)
+    # the slots, child and triangle bases do not move
+    b16, a16 = before.view(np.uint32).reshape(n, 20), after.view(np.uint32).reshape(n, 20)
+    np.testing.assert_array_equal(b16[:, 4:8], a16[:, 4:8])
+    np.testing.assert_array_equal(b16[:, 3] >> 24, a16[:, 3] >> 24)
+    _, _, tris, _ = refit_ref.gather(split_meshes(gen, M1), gen.materials_raw)
+    osc = oracle_of(sc, gen, tris)
+    cam = kgr.camera(gen.eye, gen.target, gen.fov, 1.0)
+    rays = np.concatenate([helpers.camera_rays(cam, 96, 96), helpers.random_rays(gen, 20000, 9)])
+    ref, _ = osc.trace_closest(rays)
+    got = gpu_closest(sc, rays, kgr.LAYOUT_CW8)
+    assert np.array_equal(got.view(np.uint32), ref["raw"].view(np.uint32))
+    short = rays.copy()
+    short[:, 7] = 0.7
+    occ, _ = osc.trace_any(short)
+    assert np.array_equal(gpu_any(sc, short, kgr.LAYOUT_CW8), occ)
+    # back to the creation transforms: the nodes come back bit for bit
+    sc.set_transforms([1, 2], [M0[1], M0[2]])
+    assert np.array_equal(sc.array(kgr.ARRAY_CW8_NODES), before)
+    sc.close()

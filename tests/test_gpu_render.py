@@ -45,7 +45,7 @@ def render_pt_gpu(g, sc, W, H, opts, frames=1, layout="fast", **kw):
     return cam, [b.cpu().numpy() for b in bufs], st
 
 
-@pytest.mark.parametrize("layout", ["fast", "threaded", "wide"])
+@pytest.mark.parametrize("layout", ["fast", "threaded", "wide", "cw8"])
 def test_path_tracer_matches_oracle(box4k, layout):
     g, sc, osc = box4k
     W, H = 96, 96
@@ -101,7 +101,7 @@ def restir_gpu(g, sc, W, H, frames, opts, max_depth=2):
 
 # the last case takes the most neighbours a pass allows (16): every neighbour
 # slot and the largest shadow-ray queues of the reuse kernels in use
-@pytest.mark.parametrize("passes,layout,neighbors", [(1, "fast", 5), (2, "threaded", 5), (1, "wide", 5),
+@pytest.mark.parametrize("passes,layout,neighbors", [(1, "fast", 5), (2, "threaded", 5), (1, "wide", 5), (1, "cw8", 5),
                                                      (2, "fast", 16)])
 def test_restir_di_matches_oracle(box4k, passes, layout, neighbors):
     g, sc, osc = box4k

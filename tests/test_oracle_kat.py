@@ -140,3 +140,32 @@ def test_transcendentals_against_float64():
     safe = np.abs(np.cos(x)) > 1e-2
     ref = np.tan(x[safe])
     assert np.all(np.abs(out[safe, 2] - ref) <= 1e-6 * np.maximum(np.abs(ref), 1.0) * 10)
+
+
+def test_atan2_and_asin_against_float64():
+    """The environment map's (u, v) use atan2 and asin built from the same
+    atan: within a few ulp of float64 over all quadrants and [-1, 1]."""
+    rng = np.random.default_rng(11)
+    d = rng.normal(size=(50000, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    y = np.concatenate([d[:, 0], [0, 0, 1, -1, 0.5, -0.5, 1e-30, -1e-30]]).astype(np.float32)
+    x = np.concatenate([d[:, 2], [1, -1, 0, 0, 0, -0.0, -1, -1]]).astype(np.float32)
+    s = np.concatenate([d[:, 1], [1, -1, 0, 0.999999, -0.999999, 0.5, 1e-8, -1e-8]]).astype(np.float32)
+    out = np.zeros((len(y), 2), np.float32)
+    pyoracle.lib().oracle_kat_atan2_asin(pyoracle.ptr(y), pyoracle.ptr(x), len(y), pyoracle.ptr(out))
+    ref = np.arctan2(y.astype(np.float64), x.astype(np.float64))
+    ok = np.abs(out[:, 0] - ref) <= 4e-7 * np.maximum(np.abs(ref), 1e-2)
+    # atan2(+-0, -1) may differ in sign from C's (+-pi); both mean the same azimuth
+    ok |= (np.abs(np.abs(out[:, 0]) - np.pi) < 1e-6) & (np.abs(np.abs(ref) - np.pi) < 1e-6)
+    assert ok.all()
+    sin_in = np.ascontiguousarray(s)
+    out2 = np.zeros((len(s), 2), np.float32)
+    pyoracle.lib().oracle_kat_atan2_asin(pyoracle.ptr(sin_in), pyoracle.ptr(np.ones_like(sin_in)), len(s),
+                                         pyoracle.ptr(out2))
+    ref = np.arcsin(s.astype(np.float64))
+    assert np.all(np.abs(out2[:, 1] - ref) <= 4e-7 * np.maximum(np.abs(ref), 1e-3) + 2e-7)
+    out3 = np.zeros((2, 2), np.float32)
+    bad = np.array([1.5, -2.0], np.float32)
+    pyoracle.lib().oracle_kat_atan2_asin(pyoracle.ptr(bad), pyoracle.ptr(np.ones(2, np.float32)), 2,
+                                         pyoracle.ptr(out3))
+    assert np.isnan(out3[:, 1]).all()

@@ -871,6 +871,17 @@ struct kgr_attachment {
 			return *b ? 1 : 0;
 		return def;
 	}
+	float opt_float(const char *k, float def) const
+	{
+		auto it = options.find(k);
+		if (it == options.end())
+			return def;
+		if (auto p = std::get_if<float>(&it->second))
+			return *p;
+		if (auto i = std::get_if<int>(&it->second))
+			return (float)*i;
+		return def;
+	}
 	std::string opt_str(const char *k, const std::string &def) const
 	{
 		auto it = options.find(k);
@@ -1477,6 +1488,9 @@ void render_restir_gi(kgr_attachment *att, const kgr_launch_info *info, const kg
 	fp.jitter = 1;
 	fp.gi_capture = 1;
 	fp.gi_mcap = att->opt_int("gi_mcap", 30);
+	fp.gi_jmax = att->opt_float("gi_jacobian_max", 4.0f);
+	KGR_REQUIRE(fp.gi_jmax >= 1.0f, KGR_ERR_INVALID_ARGUMENT, "gi_jacobian_max must be >= 1");
+	fp.gi_confidence_rule = att->opt_int("gi_neighbor_confidence", 1);
 	fp.gi_neighbors = att->opt_int("gi_neighbors", 8);
 	fp.gi_radius = att->opt_int("gi_radius", 30);
 	KGR_REQUIRE(fp.gi_neighbors >= 0 && fp.gi_neighbors <= KGR_GI_MAX_NEIGHBORS, KGR_ERR_INVALID_ARGUMENT,
@@ -1718,7 +1732,7 @@ static const std::map<std::string, OptionValue> &option_defaults()
 		{"spatial_passes", 2}, {"spatial_neighbors", 5}, {"spatial_radius", 30},
 		{"profile", false}, {"count_visits", false},
 		{"gi_temporal", true}, {"gi_mcap", 30}, {"gi_spatial_iterations", 3}, {"gi_neighbors", 8},
-		{"gi_radius", 30},
+		{"gi_radius", 30}, {"gi_jacobian_max", 4.0f}, {"gi_neighbor_confidence", true},
 		{"cache", false}, {"cache_train", true}, {"cache_train_paths", 16384}, {"cache_lr", 1e-3f},
 		{"cache_dtype", std::string("bf16")}, {"cache_infer", std::string("tcgen05")}, {"reset_history", false},
 		{"trace_shadow", std::string("")}, {"trace_block", 0}, {"trace_occupancy", -1}, {"trace_stack", -1},

@@ -34,7 +34,9 @@
  *               D = sum_i M_i p^<-i(y),  p^<-i(y) = p^_i(y) |J_q->i| v_i(y)
  *             over the centre, and the history or the neighbours; v_i is
  *             a visibility ray from receiver i (taken as 1 for the
- *             history).  The uniform 1/Z weight it replaces keeps W ~
+ *             history).  A spatial neighbour's confidence M_i is at most
+ *             the centre's M (gi_neighbor_confidence).  The uniform 1/Z
+ *             weight it replaces keeps W ~
  *             1/p^_q(y), which a neighbour with a much larger p^ for the
  *             same sample turns into an unbounded contribution; here the
  *             small p^_q(y) cancels in the neighbour's weight.  Normalised
@@ -71,14 +73,12 @@ namespace {
  * selection would no longer be independent of the candidates. */
 #define KGR_GI_REUSE_SALT 0x47495255u
 #define KGR_GI_COS_10DEG 0.984807753f
-/* A shift whose Jacobian leaves [1/10, 10] is invalid: reconnecting to a
- * secondary vertex much nearer one receiver than the other (a crease, a
- * contact) scales the sample's weight without bound.  The range is closed
- * under inversion, so the bias correction -- which shifts the selected
- * sample back to each neighbour -- sees the same domains. */
-#define KGR_GI_JACOBIAN_MIN 0.1f
-#define KGR_GI_JACOBIAN_MAX 10.0f
-
+/* A shift whose Jacobian leaves [1/jmax, jmax] (jmax: option
+ * gi_jacobian_max) is invalid: reconnecting to a secondary vertex much
+ * nearer one receiver than the other (a crease, a contact) scales the
+ * sample's weight without bound.  The range is closed under inversion, so
+ * the bias correction -- which shifts the selected sample back to each
+ * neighbour -- sees the same domains. */
 __device__ __forceinline__ f3 v3(const float *p) { return mk(p[0], p[1], p[2]); }
 
 struct GiSample {
@@ -164,14 +164,14 @@ __device__ __forceinline__ float gi_mis_weight(float w_sum, float num, float D, 
 
 /* Solid-angle Jacobian of moving a sample's receiver from xr to xq; 0 for
  * an invalid shift. */
-__device__ __forceinline__ float gi_jacobian(const f3 &xq, const f3 &xr, const GiSample &s)
+__device__ __forceinline__ float gi_jacobian(const f3 &xq, const f3 &xr, const GiSample &s, float jmax)
 {
 	f3 dq = xq - s.xs, dr = xr - s.xs;
 	float lq2 = dot(dq, dq), lr2 = dot(dr, dr);
 	float cq = fabsf(dot(s.ns, dq)) / ksqrt(lq2);
 	float cr = fabsf(dot(s.ns, dr)) / ksqrt(lr2);
 	float j = (cq / cr) * (lr2 / lq2);
-	return (j >= KGR_GI_JACOBIAN_MIN && j <= KGR_GI_JACOBIAN_MAX) ? j : 0.0f;
+	return (j >= 1.0f / jmax && j <= jmax) ? j : 0.0f;
 }
 
 __device__ __forceinline__ bool visible(const DeviceScene &s, int layout, const f3 &from, const f3 &to)
@@ -445,7 +445,7 @@ __global__ void __launch_bounds__(128) gi_temporal_kernel(DeviceScene s, FramePa
 	GiMerge r;
 	r.init(pixel_seed(pix, fp.frame, KGR_GI_REUSE_SALT));
 	r.update(C.s, gi_target(h, C.s) * C.W * C.M, -1);
-	float J = gi_jacobian(g.x, gp.x, P.s);
+	float J = gi_jacobian(g.x, gp.x, P.s, fp.gi_jmax);
 	float wp = gi_target(h, P.s) * J * P.W * pM;
 	r.update(P.s, wp, 0);
 	/* The history counts toward the normalisation whether or not its own
@@ -456,7 +456,7 @@ __global__ void __launch_bounds__(128) gi_temporal_kernel(DeviceScene s, FramePa
 	 * brightens pixels whose GI samples are often empty. */
 	int32_t M = C.M + pM;
 	float tq = gi_target(h, r.sel);
-	float jp = gi_jacobian(gp.x, g.x, r.sel);
+	float jp = gi_jacobian(gp.x, g.x, r.sel, fp.gi_jmax);
 	float tp = jp > 0.0f ? gi_target(receiver_prev(s, fp, gp), r.sel) * jp : 0.0f;
 	float D = (float)C.M * tq + (float)pM * tp;
 	float W = gi_mis_weight(r.w, r.src < 0 ? tq : tp, D, tq);
@@ -525,10 +525,18 @@ __global__ void __launch_bounds__(128) gi_spatial_gather_kernel(FrameParams fp, 
 		if (similar(g, depth, gn, length(gn.x - v3(fp.center)))) {
 			GiRes N = load_gi(gb.res[in], (uint32_t)index0);
 			if (N.M > 0) {
-				nb = make_int2(index0, N.M);
-				Msum += N.M;
-				float J = N.s.rc ? gi_jacobian(g.x, gn.x, N.s) : 0.0f;
-				wn = J > 0.0f ? gi_target(h, N.s) * J * N.W * N.M : 0.0f;
+				/* confidence of the neighbour's domain (option
+				 * gi_neighbor_confidence, on by default): at most the
+				 * centre's M.  Any positive confidences keep the balance
+				 * heuristic's weights summing to one; with a neighbour's M
+				 * far above the centre's, a sample the centre can barely
+				 * see would be shaded with the ratio M_n / M_c (up to 255
+				 * where a disocclusion meets reused neighbours) */
+				int32_t cn = fp.gi_confidence_rule && C.M < N.M ? C.M : N.M;
+				nb = make_int2(index0, cn);
+				Msum += cn;
+				float J = N.s.rc ? gi_jacobian(g.x, gn.x, N.s, fp.gi_jmax) : 0.0f;
+				wn = J > 0.0f ? gi_target(h, N.s) * J * N.W * cn : 0.0f;
 				rand_uniform(seed);
 			}
 		}
@@ -617,7 +625,7 @@ __global__ void __launch_bounds__(128) gi_spatial_resample_kernel(FrameParams fp
 			if (nb.x < 0)
 				continue;
 			GBuf gn = gbuf(gb.position, gb.normal, (uint32_t)nb.x);
-			float jn = gi_jacobian(gn.x, g.x, sel);
+			float jn = gi_jacobian(gn.x, g.x, sel, fp.gi_jmax);
 			float tn = jn > 0.0f ? gi_target(receiver(fp, gb, (uint32_t)nb.x, gn), sel) * jn : 0.0f;
 			gb.weights[slot] = tn;
 			queue_append(gb.vis_queue[1], gb.vis_count + 1, slot, tn > 0.0f);

@@ -128,6 +128,8 @@ struct FrameParams {
 	/* ReSTIR GI */
 	int32_t gi_capture; /* shade records the depth-1 vertex in aov_p/aov_n */
 	int32_t gi_mcap, gi_neighbors, gi_radius;
+	float gi_jmax;           /* shifts with a Jacobian outside [1 / jmax, jmax] are invalid */
+	int32_t gi_confidence_rule; /* a neighbour's confidence is at most the centre's M */
 	float prev_center[3];
 	TraceTune tune;
 };

@@ -145,6 +145,7 @@ typedef struct oracle_gi_state {
 	float *prev_normal;   /* float4 per pixel */
 	float prev_center[3];
 	int32_t gi_temporal, gi_mcap, gi_spatial_iterations, gi_neighbors, gi_radius;
+	int32_t gi_confidence_rule; /* a neighbour's confidence is at most the centre's M */
 } oracle_gi_state;
 
 /* One ReSTIR GI frame (DI candidates + GI reservoir reuse), see gi.cu's

@@ -73,17 +73,18 @@ class GiStateC(ctypes.Structure):
                 ("prev_normal", ctypes.c_void_p), ("prev_center", ctypes.c_float * 3),
                 ("gi_temporal", ctypes.c_int32), ("gi_mcap", ctypes.c_int32),
                 ("gi_spatial_iterations", ctypes.c_int32), ("gi_neighbors", ctypes.c_int32),
-                ("gi_radius", ctypes.c_int32)]
+                ("gi_radius", ctypes.c_int32), ("gi_confidence_rule", ctypes.c_int32)]
 
 
 class GiState:
     """Oracle-side ReSTIR GI state carried between frames."""
 
-    def __init__(self, n, temporal=True, mcap=30, iterations=3, neighbors=8, radius=30):
+    def __init__(self, n, temporal=True, mcap=30, iterations=3, neighbors=8, radius=30, confidence_rule=1):
         self.arrays = {k: np.zeros((n, 4), np.float32)
                        for k in ("res_a", "res_b", "prev_position", "prev_normal")}
         self.c = GiStateC(*[ptr(self.arrays[k]) for k in ("res_a", "res_b", "prev_position", "prev_normal")],
-                          (ctypes.c_float * 3)(0, 0, 0), int(temporal), mcap, iterations, neighbors, radius)
+                          (ctypes.c_float * 3)(0, 0, 0), int(temporal), mcap, iterations, neighbors, radius,
+                          int(confidence_rule))
         self.started = False
 
 

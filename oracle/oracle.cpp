@@ -6,8 +6,9 @@
  * with g++ -O2 -ffp-contract=off -fopenmp into oracle/liboracle.so.
  *
  * Floating-point expressions keep the reference's evaluation order; the
- * vector helpers and the transcendentals come from kgr_math.h, whose
- * definitions follow include/cuda/math.cuh and are identical on CPU and GPU.
+ * vector helpers, the RNG and the transcendentals are the oracle's own
+ * (ref_math.h), written apart from the kernels' so that a slip on either
+ * side fails the parity tests instead of passing on both.
  */
 #include "oracle.h"
 
@@ -24,9 +25,9 @@
 #include <omp.h>
 #endif
 
-#include "../artemis_gb300/csrc/kgr_math.h"
+#include "ref_math.h"
 
-using namespace kgr;
+using namespace oref;
 
 namespace {
 

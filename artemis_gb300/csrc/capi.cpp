@@ -25,6 +25,7 @@
 #include "kgr_internal.h"
 #include "kgr_cache.h"
 #include "kgr_gi.h"
+#include "kgr_mamba.h"
 #include "kgr_wavefront.h"
 
 namespace kgr {
@@ -748,7 +749,7 @@ kgr_status kgr_trace_counts(const kgr_scene *sc, const float *rays, uint32_t n, 
 
 namespace {
 
-enum Kind { KIND_PT = 0, KIND_RESTIR_DI = 1, KIND_RESTIR_GI = 2 };
+enum Kind { KIND_PT = 0, KIND_RESTIR_DI = 1, KIND_RESTIR_GI = 2, KIND_MAMBA = 3 };
 
 using OptionValue = std::variant<int, float, bool, std::string>;
 
@@ -790,6 +791,13 @@ struct kgr_attachment {
 	DevBuf<float> gi_weights;
 	DevBuf<uint32_t> gi_vis_queue[2], gi_vis_count;
 	int gi_prev = 0;
+
+	/* Mamba state: G-buffer, reservoirs, secondary rays, probe table; which
+	 * reservoir and previous sets are current; the next depth stamp */
+	MambaBuffers mamba;
+	bool mamba_loaded = false;
+	int mamba_res_in = 0, mamba_prev_in = 0;
+	uint64_t mamba_stamp = 0;
 
 	/* radiance cache: network, query rows, training paths, records, batch */
 	kgr_mlp *cache_mlp = nullptr;
@@ -1003,6 +1011,10 @@ struct kgr_attachment {
 			b->release();
 		b_count.release();
 		t_L.release();
+		if (mamba_loaded) {
+			mamba_free(mamba);
+			mamba_loaded = false;
+		}
 		capacity = 0;
 	}
 
@@ -1029,6 +1041,11 @@ struct kgr_attachment {
 				KGR_CUDA(cudaMemsetAsync(b->ptr, 0, npix * sizeof(float4), st));
 			KGR_CUDA(cudaMemsetAsync(pixel_materials.ptr, 0, npix * sizeof(kgr_material), st));
 			gi_prev = 0;
+		}
+		if (kind == KIND_MAMBA && mamba_loaded) {
+			mamba_reset(mamba, width, height, st);
+			mamba_res_in = mamba_prev_in = 0;
+			mamba_stamp = 0;
 		}
 		have_prev_camera = false;
 	}
@@ -1332,6 +1349,73 @@ void render_restir_di(kgr_attachment *att, const kgr_launch_info *info, const kg
 	att->last_paths = fp.paths;
 }
 
+/* The editor's Mamba frame (Mamba::render, editor/mamba.cu:1094-1300): see
+ * kgr_mamba.h.  Its options are the reference's Mamba switches:
+ * direct_lighting, indirect_lighting, irradiance, render_probes and
+ * render_probe_radiance (Mamba::options, editor/mamba.cuh:61-67),
+ * temporal_reuse and spatial_reuse (:57-58). */
+void render_mamba(kgr_attachment *att, const kgr_launch_info *info, const kgr_scene *sc, cudaStream_t st)
+{
+	KGR_REQUIRE(info->lights.quad_count == 0, KGR_ERR_UNSUPPORTED,
+		"the mamba attachment samples the scene's triangle lights and the environment only");
+	KGR_REQUIRE(att->mamba_loaded, KGR_ERR_NOT_LOADED, "load() was not called");
+	FrameParams fp = frame_params(att, info, sc);
+	MambaParams mp;
+	memset(&mp, 0, sizeof(mp));
+	mp.width = att->width;
+	mp.height = att->height;
+	mp.npix = att->width * att->height;
+	mp.sec_w = att->width / 4 + 1;
+	mp.sec_h = att->height / 4 + 1;
+	memcpy(mp.origin, info->camera.center, 12);
+	memcpy(mp.U, info->camera.ax_u, 12);
+	memcpy(mp.V, info->camera.ax_v, 12);
+	memcpy(mp.W, info->camera.ax_w, 12);
+	if (!att->have_prev_camera) {
+		memcpy(att->prev_projection, info->camera.projection, 64);
+		memcpy(att->prev_view, info->camera.view, 64);
+		att->have_prev_camera = true;
+	}
+	mat4_mul(att->prev_projection, att->prev_view, mp.prev_proj_view);
+	mp.time = info->time;
+	mp.samples = info->samples;
+	KGR_REQUIRE(mp.samples >= 0, KGR_ERR_INVALID_ARGUMENT, "samples must be >= 0");
+	mp.direct_lighting = att->opt_int("direct_lighting", 0);
+	mp.indirect_lighting = att->opt_int("indirect_lighting", 0);
+	mp.irradiance = att->opt_int("irradiance", 1);
+	mp.render_probes = att->opt_int("render_probes", 0);
+	mp.render_probe_radiance = att->opt_int("render_probe_radiance", 0);
+	mp.temporal = att->opt_int("temporal_reuse", 0);
+	mp.spatial = att->opt_int("spatial_reuse", 0);
+	mp.layout = fp.layout;
+	mp.res_in = att->mamba_res_in;
+	mp.prev_in = att->mamba_prev_in;
+	uint64_t records = 2ull * mp.sec_w * mp.sec_h;
+	if (att->mamba_stamp + records + 1 > 0xFFFFFFFFull) {
+		mamba_restamp(att->mamba.table, st);
+		att->mamba_stamp = 0;
+	}
+	mp.stamp_base = (uint32_t)att->mamba_stamp;
+	att->mamba_stamp += records;
+	mamba_bin_directions(mp.bin_dir);
+	att->ensure_paths(mp.npix);
+	PathBuffers pb = att->path_buffers();
+	prepare_visits(att, st);
+	DeviceScene s = scene_for_launch(sc, info);
+	att->mark(-1, st);
+	uint32_t launches = mamba_render(s, pb, mp, att->mamba, fp.tune, reinterpret_cast<float4 *>(info->buffers.color),
+		st, [&](int k) { att->mark(k, st); });
+	if (mp.direct_lighting && mp.spatial)
+		att->mamba_res_in = 1 - att->mamba_res_in;
+	if (mp.direct_lighting && (mp.temporal || mp.spatial))
+		att->mamba_prev_in = 1 - att->mamba_prev_in;
+	memcpy(att->prev_projection, info->camera.projection, 64);
+	memcpy(att->prev_view, info->camera.view, 64);
+	att->stats.kernel_launches = launches;
+	att->stats.camera_rays = mp.npix;
+	att->last_paths = mp.npix;
+}
+
 /* Path tracer with the radiance cache: render paths end at the first bounce
  * with a network query; training paths (plain, full depth) train it. */
 void render_pt_cached(kgr_attachment *att, const kgr_launch_info *info, const kgr_scene *sc, cudaStream_t st)
@@ -1604,6 +1688,9 @@ kgr_status kgr_create(const char *kind, kgr_attachment **out)
 		} else if (k == "restir_gi") {
 			kd = KIND_RESTIR_GI;
 			name = "ReSTIR GI";
+		} else if (k == "mamba") {
+			kd = KIND_MAMBA;
+			name = "Mamba";
 		} else {
 			throw Error(KGR_ERR_INVALID_ARGUMENT, "unknown attachment kind: " + k);
 		}
@@ -1686,6 +1773,14 @@ kgr_status kgr_load(kgr_attachment *att)
 				att->gi_prev = 0;
 				att->ensure_paths((uint32_t)npix);
 			}
+			if (att->kind == KIND_MAMBA) {
+				mamba_alloc(att->mamba, att->width, att->height, att->opt_int("max_probes", 1 << 20),
+					att->opt_int("max_luts", 1024));
+				att->mamba_loaded = true;
+				att->mamba_res_in = att->mamba_prev_in = 0;
+				att->mamba_stamp = 0;
+				att->ensure_paths((uint32_t)npix);
+			}
 			if (!att->ev_start) {
 				KGR_CUDA(cudaEventCreate(&att->ev_start));
 				KGR_CUDA(cudaEventCreate(&att->ev_stop));
@@ -1736,7 +1831,10 @@ static const std::map<std::string, OptionValue> &option_defaults()
 		{"cache", false}, {"cache_train", true}, {"cache_train_paths", 16384}, {"cache_lr", 1e-3f},
 		{"cache_dtype", std::string("bf16")}, {"cache_infer", std::string("tcgen05")}, {"reset_history", false},
 		{"trace_shadow", std::string("")}, {"trace_block", 0}, {"trace_occupancy", -1}, {"trace_stack", -1},
-		{"trace_overlap", true}};
+		{"trace_overlap", true},
+		{"direct_lighting", false}, {"indirect_lighting", false}, {"irradiance", true}, {"render_probes", false},
+		{"render_probe_radiance", false}, {"temporal_reuse", false}, {"spatial_reuse", false},
+		{"max_probes", 1 << 20}, {"max_luts", 1024}};
 	return d;
 }
 
@@ -1821,6 +1919,7 @@ void render_frame(kgr_attachment *att, const kgr_launch_info *info, const kgr_sc
 		break;
 	case KIND_RESTIR_DI: render_restir_di(att, info, sc, st); break;
 	case KIND_RESTIR_GI: render_restir_gi(att, info, sc, st); break;
+	case KIND_MAMBA: render_mamba(att, info, sc, st); break;
 	default: throw Error(KGR_ERR_UNSUPPORTED, "attachment kind not built");
 	}
 }
@@ -2017,6 +2116,11 @@ kgr_status kgr_debug_copy(const kgr_attachment *att, const char *what, void *hos
 		else if (w == "gi_reservoir_a") { src = att->gi_a[att->gi_prev].ptr; n = att->gi_a[att->gi_prev].bytes(); }
 		else if (w == "gi_reservoir_b") { src = att->gi_b[att->gi_prev].ptr; n = att->gi_b[att->gi_prev].bytes(); }
 		else if (w == "gi_direct") { src = att->g_direct.ptr; n = att->g_direct.bytes(); }
+		else if (w.compare(0, 6, "mamba_") == 0 && att->mamba_loaded) {
+			if (!mamba_buffer(att->mamba, att->mamba_res_in, att->mamba_prev_in, att->width, att->height,
+				    w.c_str() + 6, &src, &n))
+				throw Error(KGR_ERR_INVALID_ARGUMENT, "unknown buffer " + w);
+		}
 		else throw Error(KGR_ERR_INVALID_ARGUMENT, "unknown buffer " + w);
 		KGR_REQUIRE(src && bytes <= n, KGR_ERR_INVALID_ARGUMENT, "buffer missing or too small");
 		KGR_CUDA(cudaMemcpy(host, src, bytes, cudaMemcpyDeviceToHost));

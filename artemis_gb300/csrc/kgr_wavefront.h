@@ -66,7 +66,13 @@ enum StageKind {
 	 * only their resampling kernels (gather, resample/merge, finish) */
 	STAGE_RESTIR_TEMPORAL_VIS = 11,
 	STAGE_RESTIR_SPATIAL_VIS = 12,
-	STAGE_COUNT = 13
+	/* the "mamba" attachment: secondary rays, the probe splat, the probe
+	 * upkeep (Sobel, raster, collapse, allocation), the final gather */
+	STAGE_MAMBA_SECONDARY = 13,
+	STAGE_MAMBA_GATHER = 14,
+	STAGE_MAMBA_PROBES = 15,
+	STAGE_MAMBA_FINAL = 16,
+	STAGE_COUNT = 17
 };
 
 /* Called after each launch of a multi-kernel pass with the stage it belongs

@@ -41,32 +41,6 @@ __device__ __forceinline__ void make_ray(const FrameParams &fp, uint32_t ix, uin
 	camera_ray(fp.center, fp.U, fp.V, fp.W, fp.width, fp.height, fp.jitter, ix, iy, seed, origin, direction);
 }
 
-/* Queue position j of a sample's npix camera paths -> its pixel: bands of
- * four rows, each band cut into tiles eight pixels wide (the last band and
- * the last tile of a band may be smaller), a tile's pixels row by row.  A
- * warp's 32 consecutive positions are then an 8x4 tile of the image rather
- * than a 32-pixel strip of one row, so its camera rays, and the bounces the
- * shade kernel queues from them in the same order, stay closer together.
- * A bijection on [0, npix): every path is queued once. */
-__device__ __forceinline__ uint32_t tiled_pixel(uint32_t j, uint32_t width, uint32_t height)
-{
-	uint32_t band = j / (4u * width);
-	uint32_t jb = j - band * 4u * width;
-	uint32_t rows = height - 4u * band < 4u ? height - 4u * band : 4u;
-	uint32_t full = width / 8u;
-	uint32_t x, y;
-	if (jb < 8u * rows * full) {
-		uint32_t c = jb / (8u * rows), local = jb - c * 8u * rows;
-		x = 8u * c + local % 8u;
-		y = 4u * band + local / 8u;
-	} else {
-		uint32_t w = width - 8u * full, local = jb - 8u * rows * full;
-		x = 8u * full + local % w;
-		y = 4u * band + local / w;
-	}
-	return y * width + x;
-}
-
 __global__ void generate_kernel(PathBuffers pb, FrameParams fp)
 {
 	uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;

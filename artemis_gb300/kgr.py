@@ -655,7 +655,8 @@ class Attachment:
 
     STAGES = ("generate", "trace_closest", "shade", "shadow", "accumulate", "restir_primary",
               "restir_temporal", "restir_spatial", "restir_finalize", "cache_infer", "cache_train",
-              "restir_temporal_vis", "restir_spatial_vis")
+              "restir_temporal_vis", "restir_spatial_vis", "mamba_secondary", "mamba_gather",
+              "mamba_probes", "mamba_final")
 
     def stage_times(self):
         """{stage: (total ms, launches)} since the last call ("profile" option)."""

@@ -375,7 +375,10 @@ kgr_status kgr_environment_sample(const kgr_environment *env, const float *uv, u
 		void *stream);
 kgr_status kgr_environment_destroy(kgr_environment *env);
 
-/* kind: "path_tracer", "restir_di" or "restir_gi". */
+/* kind: "path_tracer", "restir_di", "restir_gi" or "mamba" (the editor's
+ * default GI mode, editor/mamba.cu:1094-1300: ReSTIR DI with 8 candidates,
+ * quarter-resolution secondary rays and irradiance probes; it lights with
+ * the scene's triangles and the environment map, and refuses quad lights). */
 kgr_status kgr_create(const char *kind, kgr_attachment **out);
 kgr_status kgr_attach(kgr_attachment *att, const kgr_context *ctx);
 kgr_status kgr_load(kgr_attachment *att);
@@ -420,7 +423,10 @@ kgr_status kgr_get_render_stats(const kgr_attachment *att, kgr_render_stats *sta
  * 5 ReSTIR RIS, 6 temporal resampling (gather and merge kernels),
  * 7 spatial resampling (gather, resample and finish kernels), 8 ReSTIR
  * finalise, 9 radiance-cache inference, 10 radiance-cache training,
- * 11 temporal-reuse visibility rays, 12 spatial-reuse visibility rays.
+ * 11 temporal-reuse visibility rays, 12 spatial-reuse visibility rays,
+ * and for the "mamba" attachment 13 secondary rays, 14 probe splat,
+ * 15 probe upkeep (Sobel, raster, collapse, allocation), 16 final gather
+ * (its G-buffer is charged to 0 and 1, its direct lighting to 5-7).
  * Synchronises on the last event, then resets the totals. */
 kgr_status kgr_get_stage_times(kgr_attachment *att, double *ms, uint32_t *launches, uint32_t count);
 

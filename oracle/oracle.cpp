@@ -19,6 +19,7 @@
 
 #include <algorithm>
 #include <memory>
+#include <string>
 #include <vector>
 
 #ifdef _OPENMP
@@ -612,7 +613,7 @@ inline void env_uv(const f3 &d, float &u, float &v)
  * bits.  Measured on a GB300 (a sweep of 65,536 coordinates over texels
  * holding their own index): the weights round half up, and the blend of
  * float32 texels is within 6e-8 relative of the exact blend. */
-f3 env_fetch(const oracle_scene *s, float u, float v)
+void env_fetch4(const oracle_scene *s, float u, float v, float out[4])
 {
 	const int W = (int)s->env_width, H = (int)s->env_height;
 	/* the wrapped coordinate in fixed point with 24 fractional bits
@@ -632,7 +633,9 @@ f3 env_fetch(const oracle_scene *s, float u, float v)
 	};
 	if (s->env_filter == KGR_FILTER_POINT) {
 		const float *t = texel((long)floor(x), (long)floor(y));
-		return mk(t[0], t[1], t[2]);
+		for (int k = 0; k < 4; k++)
+			out[k] = t[k];
+		return;
 	}
 	/* weights: the fraction below the texel centre, rounded half up to
 	 * 8 fractional bits; the blend is evaluated in double and rounded once */
@@ -642,10 +645,15 @@ f3 env_fetch(const oracle_scene *s, float u, float v)
 	double b = floor((yb - j0) * 256.0 + 0.5) / 256.0;
 	long i = (long)i0, j = (long)j0;
 	const float *t00 = texel(i, j), *t10 = texel(i + 1, j), *t01 = texel(i, j + 1), *t11 = texel(i + 1, j + 1);
-	float c[3];
-	for (int k = 0; k < 3; k++)
-		c[k] = (float)((1.0 - a) * (1.0 - b) * t00[k] + a * (1.0 - b) * t10[k] + (1.0 - a) * b * t01[k]
+	for (int k = 0; k < 4; k++)
+		out[k] = (float)((1.0 - a) * (1.0 - b) * t00[k] + a * (1.0 - b) * t10[k] + (1.0 - a) * b * t01[k]
 			+ a * b * t11[k]);
+}
+
+f3 env_fetch(const oracle_scene *s, float u, float v)
+{
+	float c[4];
+	env_fetch4(s, u, v, c);
 	return mk(c[0], c[1], c[2]);
 }
 
@@ -2272,3 +2280,1393 @@ extern "C" void oracle_tonemap(const float *hdr, uint32_t *ldr, uint32_t width, 
 				(255u << 24) | (quantize8(b) << 16) | (quantize8(g) << 8) | quantize8(r);
 		}
 }
+
+/* ================================================================ Mamba == */
+/*
+ * The editor's Mamba frame (Mamba::render, editor/mamba.cu:1094-1300) with
+ * the deterministic choices of the GPU build: traced G-buffer at pixel
+ * centres, probes allocated in 16x16-block order, bin radiance summed in
+ * 64-bit fixed point (2^-20), a bin's depth from the frame's last splat in
+ * splat order, every pass reading its inputs as they were when it began.
+ * The state is kept in the GPU build's layouts so that every buffer can be
+ * compared byte for byte.
+ */
+
+namespace {
+
+const int M_BINS = 25;        /* IrradianceProbe::size^2 (probe.cuh:11) */
+const int M_SIZE = 5;
+const int M_REFS = 32767;     /* MAX_REFS (probe.cuh:83) */
+const float M_PI_F = 3.14159265358979323846f;
+const double M_PI_DBL = 3.14159265358979323846;
+const float M_FIXED = 1048576.0f;
+const float M_UNFIXED = 9.5367431640625e-07f;
+
+struct MLut { /* IrradianceProbeLUT header (probe.cuh:85-106) */
+	float center[3];
+	float size;
+	float resolution;
+	int32_t level;
+	int32_t counter;
+	int32_t pad;
+};
+
+struct F4 {
+	float x, y, z, w;
+};
+inline F4 f4(const f3 &v, float w) { return F4{v.x, v.y, v.z, w}; }
+inline f3 f3of(const F4 &v) { return mk(v.x, v.y, v.z); }
+
+struct MRes4 {
+	std::vector<F4> r0, r1, r2, r3;
+	void resize(size_t n) { r0.assign(n, F4{0, 0, 0, 0}); r1 = r0; r2 = r0; r3 = r0; }
+};
+
+/* LightInfo (mamba_shader.cuh:19-25) */
+struct MLight {
+	f3 position, normal, emission;
+	bool sky;
+};
+
+inline MLight m_no_light() { return MLight{mk(0.0f), mk(0.0f), mk(0.0f), false}; }
+
+/* Reservoir<LightInfo> (editor/optix/common.cuh:53-104) */
+struct MRes {
+	MLight data;
+	float w, W;
+	int M;
+	f3 seed;
+	void update(const MLight &sample, float weight)
+	{
+		w += weight;
+		float eta = rand_uniform(seed);
+		if ((eta * w) < weight)
+			data = sample;
+		M++;
+	}
+	void resample(float target)
+	{
+		float d = target * (float)M;
+		W = (d > 0.0f) ? w / d : 0.0f;
+	}
+	void reset()
+	{
+		w = 0.0f;
+		M = 0;
+		W = 0.0f;
+	}
+};
+
+inline MRes m_fresh(const f3 &seed) { return MRes{m_no_light(), 0.0f, 0.0f, 0, seed}; }
+
+inline int32_t bits_of(float f) { return (int32_t)f2u(f); }
+inline float float_of(int32_t i) { return u2f((uint32_t)i); }
+
+inline MRes m_load(const MRes4 &R, size_t i)
+{
+	const F4 &a = R.r0[i], &b = R.r1[i], &c = R.r2[i], &d = R.r3[i];
+	MRes r;
+	r.data.position = mk(a.x, a.y, a.z);
+	r.data.normal = mk(b.x, b.y, b.z);
+	r.data.sky = b.w != 0.0f;
+	r.data.emission = mk(c.x, c.y, c.z);
+	r.M = bits_of(c.w);
+	r.w = d.x;
+	r.W = d.y;
+	r.seed = mk(d.z, d.w, a.w);
+	return r;
+}
+
+inline void m_store(MRes4 &R, size_t i, const MRes &r)
+{
+	R.r0[i] = F4{r.data.position.x, r.data.position.y, r.data.position.z, r.seed.z};
+	R.r1[i] = F4{r.data.normal.x, r.data.normal.y, r.data.normal.z, r.data.sky ? 1.0f : 0.0f};
+	R.r2[i] = F4{r.data.emission.x, r.data.emission.y, r.data.emission.z, float_of(r.M)};
+	R.r3[i] = F4{r.w, r.W, r.seed.x, r.seed.y};
+}
+
+/* ONB (brdf.cuh:77-105) */
+struct MOnb {
+	f3 u, v, w;
+	f3 local(const f3 &a) const { return a.x * u + a.y * v + a.z * w; }
+	f3 inv_local(const f3 &a) const { return mk(dot(a, u), dot(a, v), dot(a, w)); }
+};
+
+MOnb m_onb(const f3 &n)
+{
+	MOnb o;
+	o.w = normalize(n);
+	f3 a = ((double)fabsf(o.w.x) > 0.9) ? mk(0.0f, 1.0f, 0.0f) : mk(1.0f, 0.0f, 0.0f);
+	o.v = normalize(cross(o.w, a));
+	o.u = cross(o.w, o.v);
+	return o;
+}
+
+inline f3 m_cleanse(const f3 &v) { return anynan(v) ? mk(0.0f) : v; }
+inline float m_luminance(const f3 &v) { return v.x + v.y + v.z; }
+
+/* brdf / pdf (brdf.cuh:436-457) with sh.mat.type: Glass's lobes are zero */
+f3 m_brdf(const SurfaceHit &sh, const f3 &wi)
+{
+	if (sh.mat.type & KGR_SHADING_TRANSMISSION)
+		return sh.mat.diffuse / PI_F + mk(0.0f);
+	return brdf(sh, wi);
+}
+
+float m_pdf(const SurfaceHit &sh, const f3 &wi)
+{
+	if (sh.mat.type & KGR_SHADING_TRANSMISSION)
+		return 0.0f;
+	return ggx_pdf(sh.mat, sh.n, wi, sh.wo);
+}
+
+/* to_disk / to_index (probe.cuh:31-51); a NaN direction is bin 0 */
+void m_to_disk(const f3 &v, float &su, float &sv)
+{
+	float theta = katan2(v.y, v.x);
+	if (theta < 0.0f)
+		theta = (float)((double)theta + 2.0 * M_PI_DBL);
+	float rp = ksqrt(v.x * v.x + v.y * v.y);
+	su = (float)((double)theta / (2.0 * M_PI_DBL));
+	sv = rp;
+}
+
+int32_t m_bin(const f3 &v)
+{
+	if (kisnan(v.x) || kisnan(v.y))
+		return 0;
+	float su, sv;
+	m_to_disk(v, su, sv);
+	int32_t x = (int32_t)(su * (float)M_SIZE);
+	int32_t y = (int32_t)(sv * (float)M_SIZE);
+	int32_t i = y * M_SIZE + x;
+	return i < 0 ? 0 : (i > M_BINS - 1 ? M_BINS - 1 : i);
+}
+
+/* from_index + from_uv (probe.cuh:53-72) of every bin */
+void m_bin_dirs(f3 out[M_BINS])
+{
+	for (int index = 0; index < M_BINS; index++) {
+		int x = index % M_SIZE, y = index / M_SIZE;
+		float u = (float)x / (float)M_SIZE, v = (float)y / (float)M_SIZE;
+		u = u < 0.0f ? 0.0f : (u > 1.0f ? 1.0f : u);
+		v = v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v);
+		double theta = (double)(2.0f * u) * M_PI_DBL;
+		float dx = (float)((double)v * cos(theta));
+		float dy = (float)((double)v * sin(theta));
+		float dz = sqrtf(1.0f - dx * dx - dy * dy);
+		out[index] = mk(dx, dy, dz);
+	}
+}
+
+struct MambaState {
+	uint32_t width, height, npix, sec_w, sec_h, nsec;
+	int32_t max_probes, max_luts;
+	std::vector<F4> g_position, g_normal;
+	std::vector<int32_t> g_index;
+	MRes4 res[2], prev[2];
+	std::vector<F4> direct_le;
+	std::vector<F4> s_wi, s_le, s_ld, s_ld_wi, s_hit_x, s_hit_n, s_hit_wo;
+	std::vector<int32_t> s_hit_mat;
+	std::vector<float> sobel, raster;
+	std::vector<F4> raster_indicator, raster_radiance;
+	std::vector<int32_t> probe_ids;
+	std::vector<int32_t> group_probes; /* 4 per group */
+	std::vector<int32_t> group_sizes;
+	/* table */
+	std::vector<MLut> luts;
+	std::vector<int32_t> refs;
+	std::vector<uint32_t> hashes;
+	std::vector<F4> lut_positions;
+	std::vector<F4> probe_pos, probe_nrm;
+	std::vector<uint64_t> bin_le, bin_depth;
+	std::vector<uint32_t> bin_n;
+	int32_t counters[2];
+	int res_in = 0, prev_in = 0;
+	uint64_t stamp = 0;
+};
+
+void m_clear_table(MambaState &m)
+{
+	size_t slots = (size_t)m.max_luts * M_REFS, bins = (size_t)m.max_probes * M_BINS;
+	m.luts.assign((size_t)m.max_luts, MLut{{0, 0, 0}, 0, 0, 0, 0, 0});
+	m.refs.assign(slots, -1);
+	m.hashes.assign(slots, 0xFFFFFFFFu);
+	m.lut_positions.assign(slots, F4{0, 0, 0, 0});
+	m.probe_pos.assign((size_t)m.max_probes, F4{0, 0, 0, 0});
+	m.probe_nrm = m.probe_pos;
+	m.bin_le.assign(3 * bins, 0);
+	m.bin_n.assign(bins, 0);
+	m.bin_depth.assign(bins, 0);
+	/* IrradianceProbeLUT::alloc of the top table (probe.cuh:102-111) */
+	MLut &top = m.luts[0];
+	top.level = 2;
+	top.size = 250.0f;
+	top.resolution = 250.0f / 25.0f;
+	m.counters[0] = 0;
+	m.counters[1] = 1;
+}
+
+struct MambaFrame {
+	const oracle_scene *s;
+	const oracle_mamba_params *p;
+	MambaState *m;
+	std::vector<TriLight> lights;
+	f3 bin_dir[M_BINS];
+	f3 origin, U, V, W;
+	float prev_pv[16];
+	uint64_t shadow_rays = 0, closest_rays = 0;
+
+	bool has_env() const { return s->env != nullptr; }
+
+	/* sky_at (editor/optix/common.cuh:18-31) */
+	void sky_at(const f3 &d, float out[4]) const
+	{
+		if (!has_env()) {
+			out[0] = out[1] = out[2] = out[3] = 0.0f;
+			return;
+		}
+		float theta = kacos(d.y);
+		float phi = katan2(d.z, d.x);
+		float u = phi / (2.0f * M_PI_F);
+		float v = theta / M_PI_F;
+		env_fetch4(s, u, 1.0f - v, out);
+	}
+
+	/* load_surface_hit (mamba_shader.cu:167-216) */
+	bool surface(size_t pix, SurfaceHit &sh) const
+	{
+		int32_t idx = m->g_index[pix];
+		if (idx == -1)
+			return false;
+		f3 position = f3of(m->g_position[pix]);
+		f3 normal = f3of(m->g_normal[pix]);
+		f3 ray = position - origin;
+		if (dot(ray, normal) > 0.0f)
+			normal = -normal;
+		sh.x = position;
+		sh.wo = normalize(origin - position);
+		sh.n = normalize(normal);
+		sh.entering = true;
+		sh.mat = load_material(s->materials[idx]);
+		float sign = (sh.mat.type == KGR_SHADING_TRANSMISSION) ? -1.0f : 1.0f;
+		sh.x = sh.x + sign * sh.n * 1e-3f;
+		return true;
+	}
+
+	/* sample_light (mamba_shader.cu:103-164); an area light is one emissive
+	 * triangle with vertices a, a + ab, a + ac */
+	float sample_light(MLight &li, f3 &seed) const
+	{
+		unsigned int nl = (unsigned int)lights.size();
+		unsigned int total = nl + (has_env() ? 1u : 0u);
+		if (total == 0)
+			return -1.0f;
+		unsigned int light_index = (unsigned int)(rand_uniform(seed) * total);
+		float area;
+		if (light_index < nl) {
+			(void)rand_uniform(seed);
+			const TriLight &l = lights[light_index];
+			f3 v0 = l.a, v1 = l.a + l.ab, v2 = l.a + l.ac;
+			f3 c = cross(v1 - v0, v2 - v0);
+			f3 gnormal = normalize(c);
+			f3 bary = pcg3f(seed);
+			float u = bary.x, v = bary.y;
+			if (u + v > 1.0f) {
+				u = 1.0f - u;
+				v = 1.0f - v;
+			}
+			li.sky = false;
+			li.position = v0 * (1.0f - u - v) + v1 * u + v2 * v;
+			li.normal = gnormal;
+			li.emission = l.intensity;
+			area = length(c) * 0.5f;
+		} else {
+			float theta = (2.0f * M_PI_F) * rand_uniform(seed);
+			float phi = M_PI_F * rand_uniform(seed);
+			f3 dir = mk(ksin(phi) * kcos(theta), kcos(phi), ksin(phi) * ksin(theta));
+			float e[4];
+			sky_at(dir, e);
+			li.sky = true;
+			li.position = 1000.0f * dir;
+			li.normal = mk(0.0f);
+			li.emission = mk(e[0], e[1], e[2]);
+			area = 4.0f * M_PI_F;
+		}
+		return 1.0f / (area * (float)total);
+	}
+
+	/* direct_unoccluded (mamba_shader.cu:76-89) */
+	f3 direct_unoccluded(const SurfaceHit &sh, const MLight &li) const
+	{
+		f3 wi = normalize(li.position - sh.x);
+		float R = length(li.position - sh.x);
+		f3 rho = m_cleanse(m_brdf(sh, wi));
+		float ldotn = li.sky ? 1.0f : fabsf(dot(li.normal, wi));
+		float ndotwi = fabsf(dot(sh.n, wi));
+		float falloff = li.sky ? 1.0f : 1.0f / (R * R);
+		return rho * li.emission * ldotn * ndotwi * falloff;
+	}
+
+	bool blocked(const f3 &o, const f3 &d, float tmax, uint64_t &rays) const
+	{
+		uint64_t a = 0, b = 0;
+		rays++;
+		return trace_any(s, o, d, tmax, &a, &b);
+	}
+
+	/* occluded (mamba_shader.cu:36-64) */
+	bool occluded(const f3 &origin_, const f3 &target, uint64_t &rays) const
+	{
+		f3 dir = normalize(target - origin_);
+		return blocked(origin_, dir, length(target - origin_) - 1e-3f, rays);
+	}
+
+	float target(const SurfaceHit &sh, const MLight &li) const { return m_luminance(direct_unoccluded(sh, li)); }
+
+	float occluded_target(const SurfaceHit &sh, const MLight &li, uint64_t &rays) const
+	{
+		f3 Li = direct_unoccluded(sh, li);
+		return m_luminance(Li * (1.0f - (float)occluded(sh.x, li.position, rays)));
+	}
+
+	void accumulate_direct(size_t pix, const SurfaceHit &sh, const f3 &Ld, bool occl, float Wt) const
+	{
+		f3 new_direct = m_cleanse(Ld * (1.0f - (float)occl) * Wt);
+		f3 le = f3of(m->direct_le[pix]);
+		le = (le * (float)p->samples + sh.mat.emission + new_direct) / (float)(p->samples + 1);
+		m->direct_le[pix] = f4(le, 0.0f);
+	}
+
+	/* reproject (mamba_shader.cu:288-320) */
+	int reproject(int index, const f3 &x) const
+	{
+		if (p->samples > 0)
+			return index;
+		float q[4];
+		for (int i = 0; i < 4; i++)
+			q[i] = prev_pv[0 * 4 + i] * x.x + prev_pv[1 * 4 + i] * x.y + prev_pv[2 * 4 + i] * x.z
+				+ prev_pv[3 * 4 + i] * 1.0f;
+		float u = q[0] / q[3];
+		float v = q[1] / q[3];
+		if (!((u >= -1.0f && u <= 1.0f) && (v >= -1.0f && v <= 1.0f)))
+			return -1;
+		u = (u + 1.0f) * 0.5f;
+		v = (v + 1.0f) * 0.5f;
+		int ix = (int)((double)(u * (float)m->width) + 0.5);
+		int iy = (int)((double)(v * (float)m->height) + 0.5);
+		if (ix < 0 || iy < 0 || ix >= (int)m->width || iy >= (int)m->height)
+			return -1;
+		return iy * (int)m->width + ix;
+	}
+
+	/* sample_spatial_neighborhood (mamba_shader.cu:396-416) */
+	int spatial_neighbor(int index, f3 &seed) const
+	{
+		int width = (int)m->width, height = (int)m->height;
+		int x = index % width, y = index / width;
+		f3 offset = rand_uniform_3f(seed);
+		float theta = (float)(2.0 * M_PI_DBL * (double)offset.x);
+		float r = 20.0f * ksqrt(offset.y);
+		int x0 = (int)((float)x + r * kcos(theta));
+		int y0 = (int)((float)y + r * ksin(theta));
+		x0 = x0 < 0 ? 0 : (x0 > width - 1 ? width - 1 : x0);
+		y0 = y0 < 0 ? 0 : (y0 > height - 1 ? height - 1 : y0);
+		return x0 + y0 * width;
+	}
+
+	/* ---- probe tables (probe.cuh) ---- */
+
+	static bool contains(const MLut &L, const f3 &x, bool neighbor)
+	{
+		float e = L.size / 2.0f + (neighbor ? 1.0f : 0.0f) * L.resolution;
+		f3 c = mk(L.center[0], L.center[1], L.center[2]);
+		f3 mn = c - mk(e), mx = c + mk(e);
+		return (x.x >= mn.x && x.y >= mn.y && x.z >= mn.z) && (x.x <= mx.x && x.y <= mx.y && x.z <= mx.z);
+	}
+
+	/* hash (probe.cuh:138-158); the first shuffle shifts a signed value */
+	static uint32_t hash(const MLut &L, const f3 &x, int dx, int dy, int dz)
+	{
+		float cdx = x.x - L.center[0] + L.size / 2.0f;
+		float cdy = x.y - L.center[1] + L.size / 2.0f;
+		float cdz = x.z - L.center[2] + L.size / 2.0f;
+		int32_t ix = (int32_t)((cdx / L.resolution) + (float)dx);
+		int32_t iy = (int32_t)((cdy / L.resolution) + (float)dy);
+		int32_t iz = (int32_t)((cdz / L.resolution) + (float)dz);
+		uint32_t u = (uint32_t)(ix & 0x7FF) | ((uint32_t)(iy & 0x7FF) << 11) | ((uint32_t)(iz & 0x7FF) << 22);
+		int32_t h = (int32_t)u;
+		h ^= (h >> 11) ^ (h >> 22);
+		u = (uint32_t)h;
+		u ^= (u << 7) & 0x9D2C5680u;
+		u ^= (u << 15) & 0xEFC60000u;
+		return u;
+	}
+
+	static uint32_t neighbor_hash(const MLut &L, const f3 &x, int ni)
+	{
+		return hash(L, x, ni % 3 - 1, (ni / 3) % 3 - 1, ni / 9 - 1);
+	}
+
+	/* lookup (probe.cuh:209-241) */
+	int32_t lookup(int32_t l, const f3 &x, int ni) const
+	{
+		const MLut &L = m->luts[l];
+		if (!contains(L, x, ni != -1))
+			return -1;
+		uint32_t h = ni == -1 ? hash(L, x, 0, 0, 0) : neighbor_hash(L, x, ni);
+		size_t base = (size_t)l * M_REFS;
+		int32_t index = -1;
+		float closest = FLT_MAX;
+		for (int i = 0; i < 2; i++) {
+			int32_t j = (int32_t)((h + (uint32_t)(i * i)) % (uint32_t)M_REFS);
+			if (m->refs[base + j] == -1)
+				break;
+			if (m->hashes[base + j] == h) {
+				float dist = length(f3of(m->lut_positions[base + j]) - x);
+				if (dist < closest) {
+					closest = dist;
+					index = j;
+				}
+			}
+		}
+		return index;
+	}
+
+	/* full_lookup (probe.cuh:243-257) */
+	int32_t full_lookup(int32_t l, const f3 &x) const
+	{
+		int32_t r = lookup(l, x, -1);
+		for (int ni = 0; r == -1 && ni < 27; ni++)
+			r = lookup(l, x, ni);
+		return r;
+	}
+
+	/* lookup_L2 (probe.cuh:660-695) */
+	int32_t top_lookup(const f3 &x) const
+	{
+		const MLut &L = m->luts[0];
+		if (!contains(L, x, false))
+			return -1;
+		uint32_t h = hash(L, x, 0, 0, 0);
+		f3 half = mk(0.5f * L.resolution);
+		for (int i = 0; i < M_REFS; i++) {
+			uint32_t j = (h + (uint32_t)i) % (uint32_t)M_REFS;
+			if (m->refs[j] == -1)
+				return -1;
+			f3 c = f3of(m->lut_positions[j]);
+			f3 mn = c - half, mx = c + half;
+			if ((x.x <= mx.x && x.y <= mx.y && x.z <= mx.z) && (x.x >= mn.x && x.y >= mn.y && x.z >= mn.z))
+				return (int32_t)j;
+		}
+		return -1;
+	}
+
+	/* lookup_L2 and the guard against an index at or above the probe
+	 * counter (mamba.cu:274, :501) */
+	int32_t table_of(const f3 &x, int32_t probe_counter) const
+	{
+		int32_t r = top_lookup(x);
+		if (r == -1)
+			return -1;
+		int32_t l = m->refs[r];
+		if (l < 0 || l >= probe_counter)
+			return -1;
+		return l;
+	}
+
+	/* closest<2> (probe.cuh:259-325) */
+	void closest2(int32_t l, const f3 &x, int32_t idx[2], float dist[2]) const
+	{
+		const MLut &L = m->luts[l];
+		if (!contains(L, x, true))
+			return;
+		size_t base = (size_t)l * M_REFS;
+		for (int ni = -1; ni < 27; ni++) {
+			uint32_t h = ni == -1 ? hash(L, x, 0, 0, 0) : neighbor_hash(L, x, ni);
+			for (int i = 0; i < 2; i++) {
+				int32_t j = (int32_t)((h + (uint32_t)(i * i)) % (uint32_t)M_REFS);
+				if (m->refs[base + j] == -1)
+					break;
+				float d = length(f3of(m->lut_positions[base + j]) - x);
+				for (int k = 0; k < 2; k++) {
+					if (d < dist[k]) {
+						for (int q = 1; q > k; q--) {
+							dist[q] = dist[q - 1];
+							idx[q] = idx[q - 1];
+						}
+						dist[k] = d;
+						idx[k] = j;
+						break;
+					}
+				}
+			}
+		}
+	}
+
+	f3 bin_radiance(size_t b) const
+	{
+		return mk((float)(int64_t)m->bin_le[3 * b + 0] * M_UNFIXED, (float)(int64_t)m->bin_le[3 * b + 1] * M_UNFIXED,
+			(float)(int64_t)m->bin_le[3 * b + 2] * M_UNFIXED);
+	}
+
+	float bin_depth(size_t b) const { return u2f((uint32_t)(m->bin_depth[b] & 0xFFFFFFFFull)); }
+
+	/* ---- passes ---- */
+
+	void gbuffer()
+	{
+		const uint32_t width = m->width, height = m->height;
+		uint64_t rays = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : rays) num_threads(nthreads(p->threads))
+		for (long i = 0; i < (long)m->npix; i++) {
+			uint32_t x = (uint32_t)i % width, y = (uint32_t)i / width;
+			uint32_t yy = height - (y + 1);
+			float u = 2.0f * ((float)x + 0.5f) / (float)width - 1.0f;
+			float v = 2.0f * ((float)yy + 0.5f) / (float)height - 1.0f;
+			f3 d = normalize(u * U - v * V + W);
+			uint64_t a = 0, b = 0;
+			kgr_hit h = trace_closest(s, origin, d, 1e16f, &a, &b);
+			rays++;
+			if (h.prim < 0) {
+				m->g_position[i] = F4{0, 0, 0, 0};
+				m->g_normal[i] = F4{0, 0, 0, 0};
+				m->g_index[i] = -1;
+				continue;
+			}
+			const uint32_t *t = s->tris + 4 * (size_t)h.prim;
+			f3 pa = ld3(s->positions, t[0]), pb = ld3(s->positions, t[1]), pc = ld3(s->positions, t[2]);
+			f3 na = ld3(s->normals, t[0]), nb = ld3(s->normals, t[1]), nc = ld3(s->normals, t[2]);
+			float w0 = 1.0f - h.b1 - h.b2;
+			f3 xx = w0 * pa + h.b1 * pb + h.b2 * pc;
+			f3 n = normalize(w0 * na + h.b1 * nb + h.b2 * nc);
+			m->g_position[i] = f4(xx, 1.0f);
+			m->g_normal[i] = f4(n, 1.0f);
+			m->g_index[i] = (int32_t)t[3];
+		}
+		closest_rays += rays;
+	}
+
+	/* __raygen__direct_primary (mamba_shader.cu:221-269) */
+	void direct_primary()
+	{
+		MRes4 &R = m->res[m->res_in];
+		uint64_t rays = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : rays) num_threads(nthreads(p->threads))
+		for (long i = 0; i < (long)m->npix; i++) {
+			uint32_t x = (uint32_t)i % m->width, y = (uint32_t)i / m->width;
+			MRes r = m_load(R, i);
+			r.reset();
+			SurfaceHit sh;
+			if (!surface(i, sh)) {
+				m_store(R, i, r);
+				continue;
+			}
+			f3 seed = mk((float)x, (float)y, p->time);
+			for (int k = 0; k < 8; k++) {
+				MLight lighting = m_no_light();
+				float pdf = sample_light(lighting, seed);
+				f3 Ld = direct_unoccluded(sh, lighting);
+				float t = Ld.x + Ld.y + Ld.z;
+				r.update(lighting, t / pdf > 0.0f ? t / pdf : 0.0f);
+			}
+			f3 Ld_res = direct_unoccluded(sh, r.data);
+			bool occl = occluded(sh.x, r.data.position, rays);
+			r.resample(m_luminance(Ld_res * (1.0f - (float)occl)));
+			m_store(R, i, r);
+			if (!p->temporal_reuse && !p->spatial_reuse)
+				accumulate_direct(i, sh, Ld_res, occl, r.W);
+		}
+		shadow_rays += rays;
+	}
+
+	/* __raygen__temporal_reuse (mamba_shader.cu:322-393) */
+	void direct_temporal()
+	{
+		MRes4 &R = m->res[m->res_in];
+		const MRes4 &Pin = m->prev[m->prev_in];
+		MRes4 &Pout = m->prev[1 - m->prev_in];
+		bool end = !p->spatial_reuse;
+		uint64_t rays = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : rays) num_threads(nthreads(p->threads))
+		for (long i = 0; i < (long)m->npix; i++) {
+			uint32_t x = (uint32_t)i % m->width, y = (uint32_t)i / m->width;
+			SurfaceHit sh;
+			if (!surface(i, sh)) {
+				MRes q = m_load(Pin, i);
+				q.reset();
+				m_store(Pout, i, q);
+				continue;
+			}
+			int pindex = reproject((int)i, sh.x);
+			MRes cur = m_load(R, i);
+			if (cur.M <= 0) {
+				m_store(Pout, i, m_load(Pin, i));
+				continue;
+			}
+			MRes merged = m_fresh(2.0f * mk((float)x, (float)y, p->time));
+			float t_current = occluded_target(sh, cur.data, rays);
+			merged.update(cur.data, t_current * cur.W * (float)cur.M);
+			int N = cur.M;
+			if (pindex >= 0) {
+				MRes prev = m_load(Pin, (size_t)pindex);
+				if (prev.M > 0) {
+					prev.M = std::min(prev.M, 200);
+					float t_previous = occluded_target(sh, prev.data, rays);
+					merged.update(prev.data, t_previous * prev.W * (float)prev.M);
+					N += (t_previous > 0.0f) * prev.M;
+				}
+			}
+			merged.M = N;
+			merged.resample(target(sh, merged.data));
+			m_store(R, i, merged);
+			if (end) {
+				f3 Ld_res = direct_unoccluded(sh, merged.data);
+				bool occl = occluded(sh.x, merged.data.position, rays);
+				accumulate_direct(i, sh, Ld_res, occl, merged.W);
+				m_store(Pout, i, merged);
+			} else {
+				m_store(Pout, i, m_load(Pin, i));
+			}
+		}
+		shadow_rays += rays;
+	}
+
+	/* __raygen__spatial_reuse (mamba_shader.cu:418-510) */
+	void direct_spatial()
+	{
+		const MRes4 &Rin = m->res[m->res_in];
+		MRes4 &Rout = m->res[1 - m->res_in];
+		const MRes4 &Pin = m->prev[m->prev_in];
+		MRes4 &Pout = m->prev[1 - m->prev_in];
+		uint64_t rays = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : rays) num_threads(nthreads(p->threads))
+		for (long i = 0; i < (long)m->npix; i++) {
+			uint32_t x = (uint32_t)i % m->width, y = (uint32_t)i / m->width;
+			MRes cur = m_load(Rin, i);
+			SurfaceHit sh;
+			if (!surface(i, sh)) {
+				m_store(Rout, i, cur);
+				MRes q = m_load(Pin, i);
+				q.reset();
+				m_store(Pout, i, q);
+				continue;
+			}
+			if (cur.M <= 0) {
+				m->direct_le[i] = F4{0.0f, 0.0f, 1.0f, 0.0f};
+				m_store(Rout, i, cur);
+				MRes q = m_load(Pin, i);
+				q.reset();
+				m_store(Pout, i, q);
+				continue;
+			}
+			MRes merged = m_fresh(2.0f * mk((float)x, (float)y, p->time));
+			float t_current = target(sh, cur.data);
+			merged.update(cur.data, t_current * cur.W * (float)cur.M);
+			SurfaceHit hits[2];
+			int sizes[2];
+			bool valid[2];
+			int count = 0;
+			for (int k = 0; k < 2; k++) {
+				int index0 = spatial_neighbor((int)i, merged.seed);
+				MRes nb = m_load(Rin, (size_t)index0);
+				nb.M = std::min(nb.M, 200);
+				if (nb.M > 0) {
+					float t_neighbor = occluded_target(sh, nb.data, rays);
+					merged.update(nb.data, t_neighbor * nb.W * (float)nb.M);
+				}
+				hits[k].mat = sh.mat;
+				hits[k].x = hits[k].n = mk(0.0f);
+				surface((size_t)index0, hits[k]);
+				hits[k].wo = sh.wo;
+				valid[k] = nb.M > 0;
+				sizes[k] = nb.M;
+				count += nb.M;
+			}
+			merged.M = cur.M + count;
+			int Z = cur.M;
+			for (int k = 0; k < 2; k++) {
+				float t_neighbor = valid[k] ? occluded_target(hits[k], merged.data, rays) : 0.0f;
+				if (t_neighbor > 0.0f)
+					Z += sizes[k];
+			}
+			float t_merged = target(sh, merged.data);
+			float denominator = t_merged * (float)Z;
+			merged.W = (denominator > 0.0f) ? merged.w / denominator : 0.0f;
+			m_store(Rout, i, merged);
+			f3 Ld_res = direct_unoccluded(sh, merged.data);
+			bool occl = occluded(sh.x, merged.data.position, rays);
+			accumulate_direct(i, sh, Ld_res, occl, merged.W);
+			m_store(Pout, i, merged);
+		}
+		shadow_rays += rays;
+	}
+
+	/* Ld (mamba_shader.cu:512-560) */
+	f3 Ld(const SurfaceHit &sh, f3 &seed, f3 &Le, f3 &wi, float &R, uint64_t &rays) const
+	{
+		MLight li = m_no_light();
+		float light_pdf = sample_light(li, seed);
+		if (light_pdf < 0.0f)
+			return mk(0.0f);
+		f3 direction = normalize(li.position - sh.x);
+		f3 o = sh.x;
+		bool hit = blocked(o, direction, length(li.position - o) - 1e-3f, rays);
+		f3 out = sh.mat.emission;
+		if (!hit && length(out) < 1e-3f) {
+			wi = normalize(li.position - o);
+			R = length(li.position - o);
+			f3 f = m_cleanse(m_brdf(sh, wi));
+			float ldotn = li.sky ? 1.0f : fabsf(dot(li.normal, wi));
+			float ndotwi = fabsf(dot(sh.n, wi));
+			float falloff = li.sky ? 1.0f : (R * R) + 1e-3f;
+			out = f * li.emission * ldotn * ndotwi / (light_pdf * falloff);
+			Le = li.emission;
+		}
+		return out;
+	}
+
+	/* __raygen__secondary (mamba_shader.cu:562-679) with the closest-hit
+	 * program (:719-777) */
+	void secondary()
+	{
+		uint64_t rays = 0, crays = 0;
+		const int32_t cycle = p->samples % 16;
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : rays, crays) num_threads(nthreads(p->threads))
+		for (long li = 0; li < (long)m->nsec; li++) {
+			uint32_t sx = (uint32_t)li % m->sec_w, sy = (uint32_t)li / m->sec_w;
+			int32_t x = 4 * (int32_t)sx + (cycle % 4), y = 4 * (int32_t)sy + (cycle / 4);
+			if (x >= (int32_t)m->width || y >= (int32_t)m->height)
+				continue;
+			size_t pix = (size_t)y * m->width + (size_t)x;
+			SurfaceHit sh;
+			if (!surface(pix, sh)) {
+				m->s_wi[li] = F4{0, 0, 0, 0};
+				continue;
+			}
+			f3 wi;
+			float pdf;
+			f3 seed = mk((float)sx, (float)sy, p->time);
+			(void)eval(sh, wi, pdf, seed);
+			if (pdf <= 0.0f) {
+				m->s_wi[li] = m->s_hit_x[li] = m->s_hit_n[li] = m->s_hit_wo[li] = F4{0, 0, 0, 0};
+				continue;
+			}
+			uint64_t a = 0, b = 0;
+			kgr_hit h = trace_closest(s, sh.x, wi, 1e16f, &a, &b);
+			crays++;
+			if (h.prim < 0) {
+				float e[4];
+				sky_at(wi, e);
+				m->s_le[li] = f4(mk(e[0], e[1], e[2]) / pdf, 0.0f);
+				m->s_wi[li] = f4(wi, 0.0f);
+				m->s_hit_x[li] = f4(1000.0f * wi, 0.0f);
+				m->s_hit_n[li] = m->s_hit_wo[li] = F4{0, 0, 0, 0};
+				continue;
+			}
+			const uint32_t *t = s->tris + 4 * (size_t)h.prim;
+			f3 pa = ld3(s->positions, t[0]), pb = ld3(s->positions, t[1]), pc = ld3(s->positions, t[2]);
+			f3 na = ld3(s->normals, t[0]), nb = ld3(s->normals, t[1]), nc = ld3(s->normals, t[2]);
+			float bu = h.b1, bv = h.b2;
+			float bw = 1.0f - bu - bv;
+			f3 hx = bw * pa + bu * pb + bv * pc;
+			f3 ng = normalize(cross(pb - pa, pc - pa));
+			if (dot(wi, ng) > 0.0f)
+				ng = -ng;
+			f3 ns = bw * na + bu * nb + bv * nc;
+			if (dot(ng, ns) < 0.0f)
+				ns = -ns;
+			f3 hn = normalize(ns);
+			f3 Le = mk(0.0f), Le_wi = mk(0.0f);
+			float Le_depth = 0.0f;
+			f3 indirect = Ld(sh, seed, Le, Le_wi, Le_depth, rays);
+			m->s_wi[li] = f4(wi, 0.0f);
+			m->s_ld[li] = f4(Le, 0.0f);
+			m->s_ld_wi[li] = f4(Le_wi, Le_depth);
+			m->s_le[li] = f4(indirect, 0.0f);
+			m->s_hit_x[li] = f4(hx, 0.0f);
+			m->s_hit_n[li] = f4(hn, 0.0f);
+			m->s_hit_wo[li] = f4(-wi, 0.0f);
+			m->s_hit_mat[li] = (int32_t)t[3];
+		}
+		shadow_rays += rays;
+		closest_rays += crays;
+	}
+
+	/* secondary_gather (mamba.cu:436-616): the splats against the table as
+	 * it stood before the frame's splats, then added in splat order */
+	void gather()
+	{
+		const int32_t cycle = p->samples % 16;
+		const int32_t probe_counter = m->counters[0];
+		std::vector<int32_t> rec_bin(2 * (size_t)m->nsec, -1);
+		std::vector<F4> rec_val(2 * (size_t)m->nsec, F4{0, 0, 0, 0});
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads(p->threads))
+		for (long index = 0; index < (long)m->nsec; index++) {
+			uint32_t sx = (uint32_t)index % m->sec_w, sy = (uint32_t)index / m->sec_w;
+			int32_t tx = 4 * (int32_t)sx + (cycle % 4), ty = 4 * (int32_t)sy + (cycle / 4);
+			if (tx >= (int32_t)m->width || ty >= (int32_t)m->height)
+				continue;
+			f3 hx = f3of(m->s_hit_x[index]), hn = f3of(m->s_hit_n[index]), hwo = f3of(m->s_hit_wo[index]);
+			int32_t hmat = m->s_hit_mat[index];
+			f3 wi = f3of(m->s_wi[index]);
+			f3 Le = f3of(m->s_le[index]);
+			F4 ldw = m->s_ld_wi[index];
+			f3 Ld_wi = mk(ldw.x, ldw.y, ldw.z);
+			float Ld_depth = ldw.w;
+			f3 Ldv = f3of(m->s_ld[index]);
+			size_t pix = (size_t)ty * m->width + (size_t)tx;
+			if (m->g_index[pix] == -1) {
+				m->s_le[index] = F4{0, 0, 0, 0};
+				continue;
+			}
+			f3 position = f3of(m->g_position[pix]);
+			f3 normal = f3of(m->g_normal[pix]);
+			int32_t l = table_of(position, probe_counter);
+			if (l != -1) {
+				int32_t r2 = full_lookup(l, position);
+				if (r2 == -1) {
+					m->s_le[index] = F4{0, 0, 0, 0};
+				} else {
+					MOnb onb = m_onb(normal);
+					f3 local_wi = normalize(onb.inv_local(wi));
+					int32_t probe = m->refs[(size_t)l * M_REFS + r2];
+					int32_t bin = m_bin(local_wi);
+					if (!(length(hn) < 1e-6f)) {
+						int32_t l2 = table_of(hx, probe_counter);
+						int32_t r4 = l2 == -1 ? -1 : full_lookup(l2, hx);
+						if (r4 != -1) {
+							int32_t p2 = m->refs[(size_t)l2 * M_REFS + r4];
+							f3 ppos = f3of(m->probe_pos[p2]);
+							MOnb o2 = m_onb(f3of(m->probe_nrm[p2]));
+							SurfaceHit sec;
+							sec.mat = load_material(s->materials[hmat]);
+							sec.entering = true;
+							sec.n = hn;
+							sec.wo = hwo;
+							sec.x = hx;
+							f3 sum = mk(0.0f);
+							for (int j = 0; j < M_BINS; j++) {
+								f3 probe_wo = o2.local(bin_dir[j]);
+								size_t b = (size_t)p2 * M_BINS + j;
+								float d = bin_depth(b);
+								f3 wo = normalize((d * probe_wo + ppos) - hx);
+								if (dot(wo, hn) <= 0.0f)
+									continue;
+								float geometric = kmax(dot(wo, hn), 0.0f);
+								f3 f = m_cleanse(m_brdf(sec, wo));
+								f3 le = m_cleanse(bin_radiance(b));
+								float n = (float)m->bin_n[b];
+								sum = sum + (sec.mat.emission + (n > 0.0f ? (le / n) * f * geometric : mk(0.0f)));
+							}
+							Le = Le + sum / (float)M_BINS;
+						}
+					}
+					rec_bin[2 * index] = probe * M_BINS + bin;
+					rec_val[2 * index] = f4(Le, length(position - hx));
+				}
+			}
+			if (length(hn) > 1e-6f) {
+				int32_t lb = table_of(hx, probe_counter);
+				if (lb == -1)
+					continue;
+				int32_t r2 = full_lookup(lb, hx);
+				if (r2 == -1)
+					continue;
+				MOnb onb = m_onb(hn);
+				f3 local_wi = normalize(onb.inv_local(Ld_wi));
+				int32_t probe = m->refs[(size_t)lb * M_REFS + r2];
+				rec_bin[2 * index + 1] = probe * M_BINS + m_bin(local_wi);
+				rec_val[2 * index + 1] = f4(Ldv, Ld_depth);
+			}
+		}
+		for (size_t r = 0; r < rec_bin.size(); r++) {
+			int32_t bin = rec_bin[r];
+			if (bin < 0)
+				continue;
+			const F4 &v = rec_val[r];
+			float c[3] = {v.x, v.y, v.z};
+			for (int k = 0; k < 3; k++)
+				m->bin_le[3 * (size_t)bin + k] += (uint64_t)to_fixed(c[k]);
+			m->bin_n[bin] += 1;
+			m->bin_depth[bin] = ((uint64_t)(uint32_t)(m->stamp + r + 1) << 32) | f2u(v.w);
+		}
+	}
+
+	static int64_t to_fixed(float v)
+	{
+		float sc = v * M_FIXED;
+		if (kisnan(sc))
+			return 0;
+		if (sc >= 4611686018427387904.0f)
+			return 4611686018427387904ll;
+		if (sc <= -4611686018427387904.0f)
+			return -4611686018427387904ll;
+		return (int64_t)nearbyintf(sc);
+	}
+
+	/* sobel_normal (mamba.cu:169-200) */
+	void sobel()
+	{
+		int W = (int)m->width, H = (int)m->height;
+#pragma omp parallel for schedule(static) num_threads(nthreads(p->threads))
+		for (long i = 0; i < (long)m->npix; i++) {
+			int x = (int)(i % W), y = (int)(i / W);
+			int ys = H - (y + 1);
+			f3 n = f3of(m->g_normal[i]);
+			float acc = 0.0f;
+			for (int a = -1; a <= 1; a++)
+				for (int b = -1; b <= 1; b++) {
+					int x2 = x + a, y2s = ys + b;
+					if (x2 < 0 || x2 >= W || y2s < 0 || y2s >= H)
+						continue;
+					int y2 = H - (y2s + 1);
+					acc += length(n - f3of(m->g_normal[(size_t)y2 * W + x2]));
+				}
+			m->sobel[i] = acc;
+		}
+	}
+
+	/* raster_probes (mamba.cu:248-371) */
+	void raster()
+	{
+		static const float wheel[12][3] = {{0.910f, 0.490f, 0.490f}, {0.910f, 0.700f, 0.490f},
+			{0.910f, 0.910f, 0.490f}, {0.700f, 0.910f, 0.490f}, {0.490f, 0.910f, 0.490f},
+			{0.490f, 0.910f, 0.700f}, {0.490f, 0.910f, 0.910f}, {0.490f, 0.700f, 0.910f},
+			{0.490f, 0.490f, 0.910f}, {0.700f, 0.490f, 0.910f}, {0.910f, 0.490f, 0.910f},
+			{0.910f, 0.490f, 0.700f}};
+		const int32_t probe_counter = m->counters[0];
+#pragma omp parallel for schedule(dynamic, 256) num_threads(nthreads(p->threads))
+		for (long i = 0; i < (long)m->npix; i++) {
+			f3 position = f3of(m->g_position[i]);
+			int32_t l = table_of(position, probe_counter);
+			if (l == -1)
+				continue;
+			const MLut &L = m->luts[l];
+			size_t base = (size_t)l * M_REFS;
+			float closest = FLT_MAX;
+			int32_t closest_index = -1;
+			for (int ni = -1; ni < 27; ni++) {
+				int32_t r = lookup(l, position, ni);
+				if (r == -1)
+					continue;
+				int32_t q = m->refs[base + r];
+				float dist = length(position - f3of(m->probe_pos[q]));
+				if (dist < closest) {
+					closest = dist;
+					closest_index = q;
+				}
+			}
+			float v = 0.0f;
+			f3 indicator = mk((float)(l % 2)), radiance = mk((float)(l % 2));
+			int32_t probe_index = -1;
+			if (closest_index != -1) {
+				probe_index = closest_index;
+				f3 diff = position - f3of(m->probe_pos[probe_index]);
+				MOnb onb = m_onb(f3of(m->probe_nrm[probe_index]));
+				f3 local = onb.inv_local(diff) / L.resolution;
+				local.z = 0.0f;
+				if (length(local) < 1.0f) {
+					v = 1.0f;
+					if (p->render_probes || p->render_probe_radiance) {
+						f3 wi = normalize(mk(local.x, local.y, ksqrt(1.0f - local.x * local.x - local.y * local.y)));
+						int32_t idx = m_bin(wi);
+						if (p->render_probes) {
+							float su, sv;
+							m_to_disk(wi, su, sv);
+							int32_t ix = (int32_t)(su * (float)M_SIZE), iy = (int32_t)(sv * (float)M_SIZE);
+							int32_t mod = (ix + iy) % 2;
+							int32_t c = probe_index % 12;
+							indicator = mk(wheel[c][0], wheel[c][1], wheel[c][2]) * (0.5f + 0.5f * (float)mod);
+						} else {
+							size_t b = (size_t)probe_index * M_BINS + idx;
+							float n = (float)m->bin_n[b];
+							radiance = n > 0.0f ? bin_radiance(b) / n : mk(0.0f);
+						}
+					}
+				}
+			}
+			m->raster[i] = v;
+			m->raster_indicator[i] = f4(indicator, 0.0f);
+			m->raster_radiance[i] = f4(radiance, 0.0f);
+			m->probe_ids[i] = probe_index;
+		}
+	}
+
+	/* probe_collapse (mamba.cu:851-906) */
+	void collapse()
+	{
+		uint32_t gw = (m->width + 15) / 16, gh = (m->height + 15) / 16;
+		for (uint32_t i = 0; i < gw * gh; i++) {
+			uint32_t x16 = i % gw, y16 = i / gw;
+			int32_t dst[4] = {-1, -1, -1, -1};
+			int32_t size = 0;
+			for (uint32_t xo = 0; xo < 16; xo++)
+				for (uint32_t yo = 0; yo < 16; yo++) {
+					if (size >= 4)
+						break;
+					uint32_t x = x16 * 16 + xo, y = y16 * 16 + yo;
+					if (x >= m->width || y >= m->height)
+						continue;
+					int32_t id = m->probe_ids[(size_t)y * m->width + x];
+					bool dup = false;
+					for (int32_t j = 0; j < size; j++)
+						if (dst[j] == id)
+							dup = true;
+					if (!dup)
+						dst[size++] = id;
+				}
+			for (int k = 0; k < 4; k++)
+				m->group_probes[4 * (size_t)i + k] = dst[k];
+			m->group_sizes[i] = size;
+		}
+	}
+
+	/* probe_allocation (mamba_kernels.cu:5-182) with request_L2, the
+	 * second-level table's allocation and request_L1 (probe.cuh:531-657),
+	 * one 16x16 block after another */
+	void allocate()
+	{
+		int W = (int)m->width, H = (int)m->height;
+		int bw = W / 16, bh = H / 16;
+		for (int b = 0; b < bw * bh; b++) {
+			int x = b % bw, y = b / bw;
+			int x2 = x * 16, y2 = y * 16;
+			int misses = 0, best_distance = 0;
+			int x_best = x2 + 8, y_best = y2 + 8;
+			for (int i = 0; i < 16; i++)
+				for (int j = 0; j < 16; j++) {
+					int x3 = x2 + i, y3 = y2 + j;
+					if (m->raster[(size_t)y3 * W + x3] != 0.0f)
+						continue;
+					int distance = 0;
+					for (int k = -2; k <= 2; k++)
+						for (int l = -2; l <= 2; l++) {
+							int x4 = x3 + k, y4 = y3 + l;
+							if (x4 < 0 || x4 >= W || y4 < 0 || y4 >= H)
+								continue;
+							if (m->raster[(size_t)y4 * W + x4] == 0.0f)
+								continue;
+							distance = std::max(abs(k) + abs(l), distance);
+						}
+					if (distance > best_distance) {
+						best_distance = distance;
+						x_best = x3;
+						y_best = y3;
+					}
+					misses++;
+				}
+			if ((double)misses < 0.4 * 16 * 16)
+				continue;
+			if (misses == 16 * 16) {
+				x_best = x2 + 8;
+				y_best = y2 + 8;
+			}
+			size_t pix = (size_t)y_best * W + x_best;
+			if (m->g_index[pix] == -1)
+				continue;
+			f3 position = f3of(m->g_position[pix]);
+			f3 normal = f3of(m->g_normal[pix]);
+			MLut &top = m->luts[0];
+			if (!contains(top, position, false))
+				continue;
+			/* request_L2 */
+			uint32_t h = hash(top, position, 0, 0, 0);
+			int32_t idx = -1;
+			f3 half = mk(0.5f * top.resolution);
+			for (int i = 0; i < M_REFS; i++) {
+				uint32_t j = (h + (uint32_t)i) % (uint32_t)M_REFS;
+				if (m->refs[j] == -1) {
+					if (m->counters[1] >= m->max_luts)
+						break;
+					float cdx = position.x - top.center[0] + top.size / 2.0f;
+					float cdy = position.y - top.center[1] + top.size / 2.0f;
+					float cdz = position.z - top.center[2] + top.size / 2.0f;
+					int32_t ix = (int32_t)(cdx / top.resolution);
+					int32_t iy = (int32_t)(cdy / top.resolution);
+					int32_t iz = (int32_t)(cdz / top.resolution);
+					f3 c = mk(top.center[0] + ((float)ix + 0.5f) * top.resolution - top.size / 2.0f,
+						top.center[1] + ((float)iy + 0.5f) * top.resolution - top.size / 2.0f,
+						top.center[2] + ((float)iz + 0.5f) * top.resolution - top.size / 2.0f);
+					m->hashes[j] = h;
+					m->lut_positions[j] = f4(c, 0.0f);
+					top.counter++;
+					int32_t l = m->counters[1]++;
+					MLut &nl = m->luts[l];
+					nl.center[0] = c.x;
+					nl.center[1] = c.y;
+					nl.center[2] = c.z;
+					nl.size = 10.0f;
+					nl.resolution = 10.0f / 25.0f;
+					nl.level = 1;
+					nl.counter = 0;
+					nl.pad = 0;
+					m->refs[j] = l;
+					idx = (int32_t)j;
+					break;
+				}
+				f3 c = f3of(m->lut_positions[j]);
+				f3 mn = c - half, mx = c + half;
+				if ((position.x <= mx.x && position.y <= mx.y && position.z <= mx.z)
+					&& (position.x >= mn.x && position.y >= mn.y && position.z >= mn.z)) {
+					idx = (int32_t)j;
+					break;
+				}
+			}
+			if (idx == -1 || m->counters[0] >= m->max_probes)
+				continue;
+			/* request_L1 and the probe */
+			int32_t l = m->refs[idx];
+			MLut &L = m->luts[l];
+			uint32_t h1 = hash(L, position, 0, 0, 0);
+			size_t base = (size_t)l * M_REFS;
+			int32_t slot = -1;
+			for (int t = 0; t < 2; t++) {
+				uint32_t j = (h1 + (uint32_t)(t * t)) % (uint32_t)M_REFS;
+				if (m->refs[base + j] == -1) {
+					slot = (int32_t)j;
+					break;
+				}
+			}
+			if (slot == -1)
+				continue;
+			m->hashes[base + slot] = h1;
+			m->lut_positions[base + slot] = f4(position, 0.0f);
+			L.counter++;
+			int32_t q = m->counters[0]++;
+			m->probe_pos[q] = f4(position, 0.0f);
+			m->probe_nrm[q] = f4(normal, 0.0f);
+			m->refs[base + slot] = q;
+		}
+	}
+
+	/* final_gather (mamba.cu:698-841) */
+	void final_gather(float *color)
+	{
+		const uint32_t width = m->width;
+#pragma omp parallel for schedule(dynamic, 256) num_threads(nthreads(p->threads))
+		for (long i = 0; i < (long)m->npix; i++) {
+			uint32_t x = (uint32_t)i % width, y = (uint32_t)i / width;
+			SurfaceHit sh;
+			if (!surface(i, sh)) {
+				uint32_t yy = m->height - (y + 1);
+				float u = 2.0f * (float)x / (float)m->width - 1.0f;
+				float v = 2.0f * (float)yy / (float)m->height - 1.0f;
+				float e[4];
+				sky_at(normalize(u * U - v * V + W), e);
+				for (int k = 0; k < 4; k++)
+					color[4 * i + k] = e[k];
+				continue;
+			}
+			f3 c = sh.mat.emission + (float)(p->direct_lighting != 0) * f3of(m->direct_le[i]) + mk(0.0f);
+			f3 covered = mk(0.0f);
+			if (p->render_probes || p->render_probe_radiance)
+				covered = f3of(p->render_probes ? m->raster_indicator[i] : m->raster_radiance[i]);
+			uint32_t sidx = x / 4 + (y / 4) * m->sec_w;
+			f3 sec = mk(0.0f);
+			if (sidx < m->nsec && p->indirect_lighting) {
+				sec = f3of(m->s_le[sidx]);
+			} else if (p->irradiance) {
+				int32_t l = table_of(sh.x, m->counters[0]);
+				if (l != -1) {
+					int32_t closest[2] = {-1, -1};
+					float distance[2] = {FLT_MAX, FLT_MAX};
+					closest2(l, sh.x, closest, distance);
+					if (closest[0] != -1) {
+						f3 sum = mk(0.0f);
+						int32_t count = 0;
+						for (int k = 0; k < 2; k++) {
+							if (closest[k] == -1)
+								break;
+							int32_t q = m->refs[(size_t)l * M_REFS + closest[k]];
+							f3 ppos = f3of(m->probe_pos[q]), pn = f3of(m->probe_nrm[q]);
+							MOnb onb = m_onb(pn);
+							for (int j = 0; j < M_BINS; j++) {
+								f3 probe_wo = onb.local(bin_dir[j]);
+								/* scaled by the bin's index, as the reference does */
+								f3 wo = normalize(((float)j * probe_wo + ppos) - sh.x);
+								if (dot(wo, sh.n) <= 0.0f)
+									continue;
+								float geometric = kmax(dot(wo, sh.n), 0.0f);
+								f3 f = m_cleanse(m_brdf(sh, wo));
+								float pdf = m_pdf(sh, wo);
+								f = pdf > 0.0f ? f / pdf : mk(0.0f);
+								size_t b = (size_t)q * M_BINS + j;
+								f3 le = m_cleanse(bin_radiance(b));
+								float n = (float)m->bin_n[b];
+								sum = sum
+									+ (n > 0.0f ? (le / n) * f * fabsf(dot(wo, pn)) * geometric : mk(0.0f));
+							}
+							count++;
+						}
+						sec = sum / (float)(count * M_BINS);
+					}
+				}
+			}
+			f3 out = c + sec + covered;
+			color[4 * i + 0] = out.x;
+			color[4 * i + 1] = out.y;
+			color[4 * i + 2] = out.z;
+			color[4 * i + 3] = 1.0f;
+		}
+	}
+};
+
+} /* namespace */
+
+struct oracle_mamba {
+	MambaState st;
+};
+
+extern "C" {
+
+oracle_mamba *oracle_mamba_create(uint32_t width, uint32_t height, int32_t max_probes, int32_t max_luts)
+{
+	if (width == 0 || height == 0 || max_probes < 1 || max_luts < 2)
+		return nullptr;
+	oracle_mamba *o = new oracle_mamba();
+	MambaState &m = o->st;
+	m.width = width;
+	m.height = height;
+	m.npix = width * height;
+	m.sec_w = width / 4 + 1;
+	m.sec_h = height / 4 + 1;
+	m.nsec = m.sec_w * m.sec_h;
+	m.max_probes = max_probes;
+	m.max_luts = max_luts;
+	F4 z = {0, 0, 0, 0};
+	m.g_position.assign(m.npix, z);
+	m.g_normal.assign(m.npix, z);
+	m.g_index.assign(m.npix, 0);
+	for (int k = 0; k < 2; k++) {
+		m.res[k].resize(m.npix);
+		m.prev[k].resize(m.npix);
+	}
+	m.direct_le.assign(m.npix, z);
+	for (std::vector<F4> *v : {&m.s_wi, &m.s_le, &m.s_ld, &m.s_ld_wi, &m.s_hit_x, &m.s_hit_n, &m.s_hit_wo})
+		v->assign(m.nsec, z);
+	m.s_hit_mat.assign(m.nsec, 0);
+	m.sobel.assign(m.npix, 0.0f);
+	m.raster.assign(m.npix, 0.0f);
+	m.raster_indicator.assign(m.npix, z);
+	m.raster_radiance.assign(m.npix, z);
+	m.probe_ids.assign(m.npix, 0);
+	size_t groups = (size_t)((width + 15) / 16) * ((height + 15) / 16);
+	m.group_probes.assign(4 * groups, 0);
+	m.group_sizes.assign(groups, 0);
+	m_clear_table(m);
+	return o;
+}
+
+void oracle_mamba_destroy(oracle_mamba *o)
+{
+	delete o;
+}
+
+void oracle_mamba_frame(oracle_mamba *o, const oracle_scene *s, const oracle_mamba_params *p, float *color,
+		oracle_render_stats *stats)
+{
+	MambaState &m = o->st;
+	MambaFrame f;
+	f.s = s;
+	f.p = p;
+	f.m = &m;
+	f.lights = load_lights(s);
+	m_bin_dirs(f.bin_dir);
+	f.origin = mk(p->center[0], p->center[1], p->center[2]);
+	f.U = mk(p->ax_u[0], p->ax_u[1], p->ax_u[2]);
+	f.V = mk(p->ax_v[0], p->ax_v[1], p->ax_v[2]);
+	f.W = mk(p->ax_w[0], p->ax_w[1], p->ax_w[2]);
+	mat4_mul(p->prev_projection, p->prev_view, f.prev_pv);
+	uint64_t records = 2ull * m.nsec;
+	if (m.stamp + records + 1 > 0xFFFFFFFFull) {
+		for (uint64_t &k : m.bin_depth)
+			k &= 0xFFFFFFFFull;
+		m.stamp = 0;
+	}
+	f.gbuffer();
+	if (p->direct_lighting) {
+		f.direct_primary();
+		if (p->temporal_reuse)
+			f.direct_temporal();
+		if (p->spatial_reuse)
+			f.direct_spatial();
+	}
+	f.secondary();
+	f.gather();
+	f.sobel();
+	f.raster();
+	f.collapse();
+	f.allocate();
+	f.final_gather(color);
+	m.stamp += records;
+	if (p->direct_lighting && p->spatial_reuse)
+		m.res_in = 1 - m.res_in;
+	if (p->direct_lighting && (p->temporal_reuse || p->spatial_reuse))
+		m.prev_in = 1 - m.prev_in;
+	if (stats) {
+		stats->camera_rays = m.npix;
+		stats->bounce_rays = f.closest_rays - m.npix;
+		stats->shadow_rays = f.shadow_rays;
+	}
+}
+
+int64_t oracle_mamba_buffer(const oracle_mamba *o, const char *name, void *out, uint64_t bytes)
+{
+	const MambaState &m = o->st;
+	std::string n(name);
+	const MRes4 &R = m.res[m.res_in], &P = m.prev[m.prev_in];
+	const void *src = nullptr;
+	size_t size = 0;
+	auto pick = [&](const void *p, size_t b) {
+		src = p;
+		size = b;
+	};
+	if (n == "g_position") pick(m.g_position.data(), 16 * m.npix);
+	else if (n == "g_normal") pick(m.g_normal.data(), 16 * m.npix);
+	else if (n == "g_index") pick(m.g_index.data(), 4 * m.npix);
+	else if (n == "direct_le") pick(m.direct_le.data(), 16 * m.npix);
+	else if (n == "res_r0") pick(R.r0.data(), 16 * m.npix);
+	else if (n == "res_r1") pick(R.r1.data(), 16 * m.npix);
+	else if (n == "res_r2") pick(R.r2.data(), 16 * m.npix);
+	else if (n == "res_r3") pick(R.r3.data(), 16 * m.npix);
+	else if (n == "prev_r0") pick(P.r0.data(), 16 * m.npix);
+	else if (n == "prev_r1") pick(P.r1.data(), 16 * m.npix);
+	else if (n == "prev_r2") pick(P.r2.data(), 16 * m.npix);
+	else if (n == "prev_r3") pick(P.r3.data(), 16 * m.npix);
+	else if (n == "s_wi") pick(m.s_wi.data(), 16 * (size_t)m.nsec);
+	else if (n == "s_le") pick(m.s_le.data(), 16 * (size_t)m.nsec);
+	else if (n == "s_ld") pick(m.s_ld.data(), 16 * (size_t)m.nsec);
+	else if (n == "s_ld_wi") pick(m.s_ld_wi.data(), 16 * (size_t)m.nsec);
+	else if (n == "s_hit_x") pick(m.s_hit_x.data(), 16 * (size_t)m.nsec);
+	else if (n == "s_hit_n") pick(m.s_hit_n.data(), 16 * (size_t)m.nsec);
+	else if (n == "s_hit_wo") pick(m.s_hit_wo.data(), 16 * (size_t)m.nsec);
+	else if (n == "s_hit_mat") pick(m.s_hit_mat.data(), 4 * (size_t)m.nsec);
+	else if (n == "sobel") pick(m.sobel.data(), 4 * m.npix);
+	else if (n == "raster") pick(m.raster.data(), 4 * m.npix);
+	else if (n == "raster_indicator") pick(m.raster_indicator.data(), 16 * m.npix);
+	else if (n == "raster_radiance") pick(m.raster_radiance.data(), 16 * m.npix);
+	else if (n == "probe_ids") pick(m.probe_ids.data(), 4 * m.npix);
+	else if (n == "group_probes") pick(m.group_probes.data(), 4 * m.group_probes.size());
+	else if (n == "group_sizes") pick(m.group_sizes.data(), 4 * m.group_sizes.size());
+	else if (n == "counters") pick(m.counters, 8);
+	else if (n == "luts") pick(m.luts.data(), sizeof(MLut) * m.luts.size());
+	else if (n == "refs") pick(m.refs.data(), 4 * m.refs.size());
+	else if (n == "hashes") pick(m.hashes.data(), 4 * m.hashes.size());
+	else if (n == "lut_positions") pick(m.lut_positions.data(), 16 * m.lut_positions.size());
+	else if (n == "probe_pos") pick(m.probe_pos.data(), 16 * m.probe_pos.size());
+	else if (n == "probe_nrm") pick(m.probe_nrm.data(), 16 * m.probe_nrm.size());
+	else if (n == "bin_le") pick(m.bin_le.data(), 8 * m.bin_le.size());
+	else if (n == "bin_n") pick(m.bin_n.data(), 4 * m.bin_n.size());
+	else if (n == "bin_depth") pick(m.bin_depth.data(), 8 * m.bin_depth.size());
+	else
+		return -1;
+	if (out) {
+		if (bytes > size)
+			return -1;
+		memcpy(out, src, bytes);
+	}
+	return (int64_t)size;
+}
+
+} /* extern "C" */

@@ -155,6 +155,31 @@ typedef struct oracle_gi_state {
 void oracle_render_gi(const oracle_scene *s, const oracle_render_params *p, oracle_gi_state *st,
 		float *color, float *direct, oracle_render_stats *stats);
 
+/* The editor's Mamba frame (editor/mamba.cu:1094-1300), in the GPU build's
+ * deterministic form: a G-buffer traced at pixel centres, ReSTIR DI with 8
+ * candidates (when direct_lighting), quarter-resolution secondary rays,
+ * irradiance probes (splat, Sobel, raster, collapse, allocation in block
+ * order) and the final gather.  The state lives in the oracle_mamba, in the
+ * GPU build's layouts; oracle_mamba_buffer copies a named buffer (the names
+ * of the product's "mamba_" debug buffers without the prefix) and returns
+ * its size in bytes, or -1 for an unknown name or a short out. */
+typedef struct oracle_mamba oracle_mamba;
+typedef struct oracle_mamba_params {
+	uint32_t width, height;
+	float center[3], ax_u[3], ax_v[3], ax_w[3];
+	float prev_projection[16], prev_view[16];
+	float time;
+	int32_t samples;
+	int32_t direct_lighting, indirect_lighting, irradiance, render_probes, render_probe_radiance;
+	int32_t temporal_reuse, spatial_reuse;
+	int32_t threads;
+} oracle_mamba_params;
+oracle_mamba *oracle_mamba_create(uint32_t width, uint32_t height, int32_t max_probes, int32_t max_luts);
+void oracle_mamba_destroy(oracle_mamba *m);
+void oracle_mamba_frame(oracle_mamba *m, const oracle_scene *s, const oracle_mamba_params *p, float *color,
+		oracle_render_stats *stats);
+int64_t oracle_mamba_buffer(const oracle_mamba *m, const char *name, void *out, uint64_t bytes);
+
 /* The environment map's texture read (normalised coordinates, wrap
  * addressing) at n (u, v) pairs: rgb gets 3 floats per pair. */
 void oracle_env_lookup(const float *texels, uint32_t width, uint32_t height, int filter, const float *uv,

@@ -102,6 +102,91 @@ def render_gi(scene, params, state, color=None):
     return color, direct, st
 
 
+class MambaParams(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("center", ctypes.c_float * 3), ("ax_u", ctypes.c_float * 3),
+                ("ax_v", ctypes.c_float * 3), ("ax_w", ctypes.c_float * 3),
+                ("prev_projection", ctypes.c_float * 16), ("prev_view", ctypes.c_float * 16),
+                ("time", ctypes.c_float), ("samples", ctypes.c_int32),
+                ("direct_lighting", ctypes.c_int32), ("indirect_lighting", ctypes.c_int32),
+                ("irradiance", ctypes.c_int32), ("render_probes", ctypes.c_int32),
+                ("render_probe_radiance", ctypes.c_int32), ("temporal_reuse", ctypes.c_int32),
+                ("spatial_reuse", ctypes.c_int32), ("threads", ctypes.c_int32)]
+
+
+# dtype and row width of each Mamba buffer (the GPU build's layouts)
+MAMBA_BUFFERS = {
+    "g_position": (np.float32, 4), "g_normal": (np.float32, 4), "g_index": (np.int32, 1),
+    "direct_le": (np.float32, 4), "res_r0": (np.float32, 4), "res_r1": (np.float32, 4),
+    "res_r2": (np.float32, 4), "res_r3": (np.float32, 4), "prev_r0": (np.float32, 4),
+    "prev_r1": (np.float32, 4), "prev_r2": (np.float32, 4), "prev_r3": (np.float32, 4),
+    "s_wi": (np.float32, 4), "s_le": (np.float32, 4), "s_ld": (np.float32, 4), "s_ld_wi": (np.float32, 4),
+    "s_hit_x": (np.float32, 4), "s_hit_n": (np.float32, 4), "s_hit_wo": (np.float32, 4),
+    "s_hit_mat": (np.int32, 1), "sobel": (np.float32, 1), "raster": (np.float32, 1),
+    "raster_indicator": (np.float32, 4), "raster_radiance": (np.float32, 4), "probe_ids": (np.int32, 1),
+    "group_probes": (np.int32, 4), "group_sizes": (np.int32, 1), "counters": (np.int32, 2),
+    "luts": (np.float32, 8), "refs": (np.int32, 1), "hashes": (np.uint32, 1), "lut_positions": (np.float32, 4),
+    "probe_pos": (np.float32, 4), "probe_nrm": (np.float32, 4), "bin_le": (np.uint64, 3),
+    "bin_n": (np.uint32, 1), "bin_depth": (np.uint64, 1),
+}
+
+
+class Mamba:
+    """Oracle Mamba state (oracle_mamba_*): frame() renders one frame into a
+    (W*H, 4) float32 colour array; buffer(name) copies a state buffer."""
+
+    def __init__(self, width, height, max_probes=1 << 20, max_luts=1024):
+        self.width, self.height = width, height
+        self.h = lib().oracle_mamba_create(width, height, max_probes, max_luts)
+        assert self.h
+
+    def frame(self, scene, params, color=None):
+        if color is None:
+            color = np.zeros((self.width * self.height, 4), np.float32)
+        st = RenderStats()
+        lib().oracle_mamba_frame(self.h, ctypes.byref(scene.c), ctypes.byref(params), ptr(color), ctypes.byref(st))
+        return color, st
+
+    def buffer(self, name):
+        dt, w = MAMBA_BUFFERS[name]
+        n = lib().oracle_mamba_buffer(self.h, name.encode(), None, 0)
+        assert n >= 0, name
+        out = np.zeros(n // np.dtype(dt).itemsize, dt)
+        lib().oracle_mamba_buffer(self.h, name.encode(), ptr(out), n)
+        return out.reshape(-1, w) if w > 1 else out
+
+    def close(self):
+        if self.h:
+            lib().oracle_mamba_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def mamba_params(width, height, cam, prev=None, time=0.0, samples=0, threads=0, **flags):
+    """cam/prev: camera dicts {center, ax_u, ax_v, ax_w, projection, view};
+    flags: direct_lighting, indirect_lighting, irradiance, render_probes,
+    render_probe_radiance, temporal_reuse, spatial_reuse."""
+    prev = prev or cam
+    p = MambaParams()
+    p.width, p.height = width, height
+    for k in ("center", "ax_u", "ax_v", "ax_w"):
+        getattr(p, k)[:] = [float(v) for v in cam[k]]
+    p.prev_projection[:] = [float(v) for v in np.asarray(prev["projection"], np.float32).ravel()]
+    p.prev_view[:] = [float(v) for v in np.asarray(prev["view"], np.float32).ravel()]
+    p.time = time
+    p.samples = samples
+    p.irradiance = 1
+    for k, v in flags.items():
+        setattr(p, k, int(v))
+    p.threads = threads
+    return p
+
+
 def build():
     """Compile liboracle.so with the committed Makefile (g++, -ffp-contract=off)."""
     subprocess.check_call(["make", "-s", "-C", HERE, "liboracle.so"])
@@ -150,6 +235,13 @@ def lib():
         L.oracle_kat_brdf.argtypes = [vp] * 5
         L.oracle_kat_math.argtypes = [vp, ctypes.c_int, vp]
         L.oracle_kat_atan2_asin.argtypes = [vp, vp, ctypes.c_int, vp]
+        L.oracle_mamba_create.restype = vp
+        L.oracle_mamba_create.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int32, ctypes.c_int32]
+        L.oracle_mamba_destroy.argtypes = [vp]
+        L.oracle_mamba_frame.argtypes = [vp, ctypes.POINTER(OracleScene), ctypes.POINTER(MambaParams), vp,
+                                         ctypes.POINTER(RenderStats)]
+        L.oracle_mamba_buffer.restype = ctypes.c_int64
+        L.oracle_mamba_buffer.argtypes = [vp, ctypes.c_char_p, vp, ctypes.c_uint64]
         _LIB = L
     return _LIB
 

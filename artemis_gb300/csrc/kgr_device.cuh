@@ -822,6 +822,36 @@ __device__ __forceinline__ f3 ggx_sample(const Material &mat, f3 n, const f3 &wo
 	return rotate(v, n);
 }
 
+/* ggx_brdf and ggx_pdf of one direction pair together: the flipped normal,
+ * the half vector and D are the same in both, so they are computed once
+ * (the results are those of the two separate calls). */
+__device__ __forceinline__ void ggx_brdf_pdf(const Material &mat, f3 n, const f3 &wi, const f3 &wo, f3 &brdf_out,
+		float &pdf_out)
+{
+	if (dot(wo, n) <= 0.0f)
+		n = -n;
+	f3 h = normalize(wi + wo);
+	float d = ggx_D(n, h, mat);
+	float k = kpow5(1 - dot(wi, h));
+	f3 f = mat.specular + (1.0f - mat.specular) * k;
+	float g = G1(n, wo, mat) * G1(n, wi, mat);
+	f3 num = f * g * d;
+	float denom = 4 * dot(wi, n) * dot(wo, n);
+	brdf_out = num / (denom + 1e-6f);
+	if (dot(wi, n) <= 0.0f) {
+		pdf_out = 0.0f;
+		return;
+	}
+	float avg_Kd = (mat.diffuse.x + mat.diffuse.y + mat.diffuse.z) / 3.0f;
+	float avg_Ks = (mat.specular.x + mat.specular.y + mat.specular.z) / 3.0f;
+	float t = 1.0f;
+	if (avg_Kd + avg_Ks > 0.0f)
+		t = kmax(avg_Ks / (avg_Kd + avg_Ks), 0.25f);
+	float term1 = dot(n, wi) / KGR_PI_DEV;
+	float term2 = d * dot(n, h) / (4.0f * dot(wi, h));
+	pdf_out = (1 - t) * term1 + t * term2;
+}
+
 /* brdf() (brdf.cuh:437-449), out = eDiffuse */
 __device__ __forceinline__ f3 brdf(const SurfaceHit &sh, const f3 &wi)
 {

@@ -99,6 +99,14 @@ struct MambaBuffers {
 	 * (in, out), accumulated direct radiance */
 	MambaReservoirs res[2], prev[2];
 	float4 *direct_Le;
+	/* the direct passes' shadow rays in slots k * npix + pixel (k < 3):
+	 * {origin}, {direction, tmax}, blocked flag; the queue of the slots to
+	 * walk and its counters (CNT_SHADOW, CNT_FETCH_SHADOW of a path
+	 * tracer's counter array); the spatial pass's neighbours and their M
+	 * ({index0, index1, M0, M1}) */
+	float4 *vis_o, *vis_d;
+	uint32_t *vis_flag, *vis_queue, *vis_counters;
+	int4 *spatial_aux;
 	/* secondary rays at (W/4 + 1) x (H/4 + 1) */
 	float4 *s_wi, *s_Le, *s_Ld, *s_Ld_wi; /* s_Ld_wi.w = Ld_depth */
 	float4 *s_hit_x, *s_hit_n, *s_hit_wo;

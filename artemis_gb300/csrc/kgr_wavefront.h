@@ -47,6 +47,10 @@ struct PathBuffers {
 	 * any-hit stage; NULL unless visit counting is on */
 	unsigned long long *visits;
 	uint32_t capacity;
+	/* when set, the any-hit walks store each shadow ray's blocked flag
+	 * (1 or 0) at its path id instead of resolving the path's pending
+	 * light (visibility rays of other passes) */
+	uint32_t *shadow_flags = nullptr;
 };
 
 /* Stage kinds for the per-launch CUDA-event timing of an attachment. */

@@ -92,6 +92,19 @@ __device__ __forceinline__ float m_pdf(const SurfaceHit &sh, const f3 &wi)
 	return ggx_pdf(sh.mat, sh.n, wi, sh.wo);
 }
 
+/* m_brdf and m_pdf of one direction, sharing the GGX lobe's terms */
+__device__ __forceinline__ void m_brdf_pdf(const SurfaceHit &sh, const f3 &wi, f3 &f, float &pdf)
+{
+	if (sh.mat.type & KGR_SHADING_TRANSMISSION) {
+		f = sh.mat.diffuse / KGR_PI_DEV + mk(0.0f);
+		pdf = 0.0f;
+		return;
+	}
+	f3 spec;
+	ggx_brdf_pdf(sh.mat, sh.n, wi, sh.wo, spec, pdf);
+	f = sh.mat.diffuse / KGR_PI_DEV + spec;
+}
+
 /* sky_at (editor/optix/common.cuh:18-31) */
 __device__ __forceinline__ float4 sky_at(const DeviceScene &s, const f3 &d)
 {
@@ -184,25 +197,11 @@ __device__ __forceinline__ f3 m_direct_unoccluded(const SurfaceHit &sh, const Li
 	return rho * li.emission * ldotn * ndotwi * falloff;
 }
 
-/* occluded (mamba_shader.cu:36-64): any hit on (0, |target - origin| - 1e-3) */
-__device__ __forceinline__ bool m_occluded(const DeviceScene &s, int layout, const f3 &origin, const f3 &target)
-{
-	f3 dir = normalize(target - origin);
-	kgr_hit h;
-	return trace<true>(s, layout, origin, dir, length(target - origin) - MAMBA_OCCLUSION_EPS, h);
-}
-
-/* target / occluded_target (mamba_shader.cu:271-286) */
+/* target (mamba_shader.cu:271-276); occluded_target (:278-286) is this
+ * times 1 - occluded, with the shadow ray walked by visibility_kernel */
 __device__ __forceinline__ float m_target(const SurfaceHit &sh, const LightInfo &li)
 {
 	return luminance(m_direct_unoccluded(sh, li));
-}
-
-__device__ __forceinline__ float m_occluded_target(const DeviceScene &s, int layout, const SurfaceHit &sh,
-		const LightInfo &li)
-{
-	f3 Li = m_direct_unoccluded(sh, li);
-	return luminance(Li * (1.0f - (float)m_occluded(s, layout, sh.x, li.position)));
 }
 
 /* ---------------------------------------------------------- reservoirs -- */
@@ -584,8 +583,33 @@ __global__ void gbuffer_store_kernel(DeviceScene s, PathBuffers pb, MambaParams 
 	mb.g_index[pix] = (int32_t)t.w;
 }
 
-/* __raygen__direct_primary (mamba_shader.cu:221-269) */
-__global__ void __launch_bounds__(128) direct_primary_kernel(DeviceScene s, MambaParams mp, MambaBuffers mb)
+/* ------------------------------------------------ direct lighting rays -- */
+
+/* The direct-lighting passes run as wavefronts: a resampling kernel queues
+ * its shadow rays -- occluded(origin, target) of mamba_shader.cu:36-64, in
+ * slot k * npix + pixel -- the path tracer's any-hit walk (tuned launch
+ * shape) takes them all with full warps and stores a blocked flag per slot,
+ * and the next kernel reads the flags.  Each kernel redoes the arithmetic
+ * and the draws of the one before it, so the results are those of the
+ * per-pixel programs. */
+__device__ __forceinline__ void queue_ray(const MambaBuffers &mb, uint32_t slot, const f3 &o, const f3 &target,
+		bool pred)
+{
+	if (pred) {
+		mb.vis_o[slot] = f4_of(o, 0.0f);
+		mb.vis_d[slot] = f4_of(normalize(target - o), length(target - o) - MAMBA_OCCLUSION_EPS);
+	}
+	queue_append(mb.vis_queue, mb.vis_counters + CNT_SHADOW, slot, pred);
+}
+
+__device__ __forceinline__ bool blocked(const MambaBuffers &mb, uint32_t slot)
+{
+	return mb.vis_flag[slot] != 0u;
+}
+
+/* __raygen__direct_primary (mamba_shader.cu:221-269): the eight candidates
+ * and the selected sample's shadow ray */
+__global__ void __launch_bounds__(128) primary_ris_kernel(DeviceScene s, MambaParams mp, MambaBuffers mb)
 {
 	uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
 	if (pix >= mp.npix)
@@ -595,37 +619,52 @@ __global__ void __launch_bounds__(128) direct_primary_kernel(DeviceScene s, Mamb
 	MRes r = load_res(R, pix);
 	r.reset();
 	SurfaceHit sh;
-	if (!load_surface(mp, mb, s.materials, pix, sh)) {
-		store_res(R, pix, r);
-		return;
+	bool hit = load_surface(mp, mb, s.materials, pix, sh);
+	if (hit) {
+		f3 seed = mk((float)x, (float)y, mp.time);
+		for (int i = 0; i < MAMBA_CANDIDATES; i++) {
+			LightInfo lighting = no_light();
+			float pdf = m_sample_light(s, lighting, seed);
+			f3 Ld = m_direct_unoccluded(sh, lighting);
+			float target = Ld.x + Ld.y + Ld.z;
+			r.update(lighting, target / pdf > 0.0f ? target / pdf : 0.0f);
+		}
 	}
-	f3 seed = mk((float)x, (float)y, mp.time);
-	for (int i = 0; i < MAMBA_CANDIDATES; i++) {
-		LightInfo lighting = no_light();
-		float pdf = m_sample_light(s, lighting, seed);
-		f3 Ld = m_direct_unoccluded(sh, lighting);
-		float target = Ld.x + Ld.y + Ld.z;
-		r.update(lighting, target / pdf > 0.0f ? target / pdf : 0.0f);
-	}
-	f3 Ld_res = m_direct_unoccluded(sh, r.data);
-	bool occl = m_occluded(s, mp.layout, sh.x, r.data.position);
-	r.resample(luminance(Ld_res * (1.0f - (float)occl)));
 	store_res(R, pix, r);
+	queue_ray(mb, pix, hit ? sh.x : mk(0.0f), r.data.position, hit);
+}
+
+/* ... its resample(luminance(Ld * (1 - occluded))) and, when it is the
+ * last pass, the accumulated direct light */
+__global__ void __launch_bounds__(128) primary_finish_kernel(DeviceScene s, MambaParams mp, MambaBuffers mb)
+{
+	uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+	if (pix >= mp.npix)
+		return;
+	SurfaceHit sh;
+	if (!load_surface(mp, mb, s.materials, pix, sh))
+		return;
+	const MambaReservoirs R = mb.res[mp.res_in];
+	MRes r = load_res(R, pix);
+	f3 Ld_res = m_direct_unoccluded(sh, r.data);
+	bool occl = blocked(mb, pix);
+	r.resample(luminance(Ld_res * (1.0f - (float)occl)));
+	R.r3[pix].y = r.W;
 	if (!mp.temporal && !mp.spatial)
 		accumulate_direct(mp, mb, pix, sh, Ld_res, occl, r.W);
 }
 
 /* __raygen__temporal_reuse (mamba_shader.cu:322-393).  The previous
  * reservoirs are read from prev[prev_in] as the last frame left them and
- * written to prev[1 - prev_in] (every pixel writes its entry). */
-__global__ void __launch_bounds__(128) direct_temporal_kernel(DeviceScene s, MambaParams mp, MambaBuffers mb)
+ * written to prev[1 - prev_in] (every pixel writes its entry).  First
+ * launch: the shadow rays of the current and the reprojected previous
+ * sample (occluded_target). */
+__global__ void __launch_bounds__(128) temporal_gather_kernel(DeviceScene s, MambaParams mp, MambaBuffers mb)
 {
 	uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
 	if (pix >= mp.npix)
 		return;
-	uint32_t x = pix % mp.width, y = pix / mp.width;
 	const MambaReservoirs R = mb.res[mp.res_in], Pin = mb.prev[mp.prev_in], Pout = mb.prev[1 - mp.prev_in];
-	bool end = !mp.spatial;
 	SurfaceHit sh;
 	if (!load_surface(mp, mb, s.materials, pix, sh)) {
 		MRes p = load_res(Pin, pix);
@@ -633,21 +672,50 @@ __global__ void __launch_bounds__(128) direct_temporal_kernel(DeviceScene s, Mam
 		store_res(Pout, pix, p);
 		return;
 	}
-	int pindex = m_reproject(mp, (int)pix, sh.x);
 	MRes cur = load_res(R, pix);
 	if (cur.M <= 0) {
 		store_res(Pout, pix, load_res(Pin, pix));
 		return;
 	}
+	int pindex = m_reproject(mp, (int)pix, sh.x);
+	bool has_prev = false;
+	f3 prev_point = mk(0.0f);
+	if (pindex >= 0) {
+		MRes prev = load_res(Pin, (uint32_t)pindex);
+		has_prev = prev.M > 0;
+		prev_point = prev.data.position;
+	}
+	queue_ray(mb, pix, sh.x, cur.data.position, true);
+	queue_ray(mb, mp.npix + pix, sh.x, prev_point, has_prev);
+}
+
+/* ... the merge with the occluded targets, and the lighting ray when the
+ * temporal pass is the last */
+__global__ void __launch_bounds__(128) temporal_merge_kernel(DeviceScene s, MambaParams mp, MambaBuffers mb)
+{
+	uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+	if (pix >= mp.npix)
+		return;
+	uint32_t x = pix % mp.width, y = pix / mp.width;
+	const MambaReservoirs R = mb.res[mp.res_in], Pin = mb.prev[mp.prev_in], Pout = mb.prev[1 - mp.prev_in];
+	SurfaceHit sh;
+	if (!load_surface(mp, mb, s.materials, pix, sh))
+		return;
+	MRes cur = load_res(R, pix);
+	if (cur.M <= 0)
+		return;
+	int pindex = m_reproject(mp, (int)pix, sh.x);
 	MRes merged = fresh_res(2.0f * mk((float)x, (float)y, mp.time));
-	float t_current = m_occluded_target(s, mp.layout, sh, cur.data);
+	f3 Li = m_direct_unoccluded(sh, cur.data);
+	float t_current = luminance(Li * (1.0f - (float)blocked(mb, pix)));
 	merged.update(cur.data, t_current * cur.W * (float)cur.M);
 	int N = cur.M;
 	if (pindex >= 0) {
 		MRes prev = load_res(Pin, (uint32_t)pindex);
 		if (prev.M > 0) {
 			prev.M = min(prev.M, MAMBA_MCAP);
-			float t_previous = m_occluded_target(s, mp.layout, sh, prev.data);
+			f3 Lp = m_direct_unoccluded(sh, prev.data);
+			float t_previous = luminance(Lp * (1.0f - (float)blocked(mb, mp.npix + pix)));
 			merged.update(prev.data, t_previous * prev.W * (float)prev.M);
 			N += (t_previous > 0.0f) * prev.M;
 		}
@@ -655,19 +723,49 @@ __global__ void __launch_bounds__(128) direct_temporal_kernel(DeviceScene s, Mam
 	merged.M = N;
 	merged.resample(m_target(sh, merged.data));
 	store_res(R, pix, merged);
-	if (end) {
-		f3 Ld_res = m_direct_unoccluded(sh, merged.data);
-		bool occl = m_occluded(s, mp.layout, sh.x, merged.data.position);
-		accumulate_direct(mp, mb, pix, sh, Ld_res, occl, merged.W);
-		store_res(Pout, pix, merged);
-	} else {
+	if (mp.spatial)
 		store_res(Pout, pix, load_res(Pin, pix));
-	}
+	queue_ray(mb, pix, sh.x, merged.data.position, !mp.spatial);
+}
+
+/* ... the direct light of the merged sample and the previous reservoir of
+ * the next frame (when the temporal pass is the last) */
+__global__ void __launch_bounds__(128) temporal_finish_kernel(DeviceScene s, MambaParams mp, MambaBuffers mb)
+{
+	uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+	if (pix >= mp.npix)
+		return;
+	SurfaceHit sh;
+	if (!load_surface(mp, mb, s.materials, pix, sh))
+		return;
+	const MambaReservoirs R = mb.res[mp.res_in], Pout = mb.prev[1 - mp.prev_in];
+	MRes merged = load_res(R, pix);
+	if (merged.M <= 0)
+		return; /* skipped by the merge (no current sample) */
+	f3 Ld_res = m_direct_unoccluded(sh, merged.data);
+	accumulate_direct(mp, mb, pix, sh, Ld_res, blocked(mb, pix), merged.W);
+	store_res(Pout, pix, merged);
+}
+
+/* A spatial neighbour's surface as __raygen__spatial_reuse holds it:
+ * its G-buffer point and normal (zero for a miss) and the centre's wo. */
+__device__ __forceinline__ SurfaceHit neighbour_hit(const MambaParams &mp, const MambaBuffers &mb,
+		const kgr_material *mats, uint32_t index0, const SurfaceHit &sh)
+{
+	SurfaceHit h;
+	h.mat = sh.mat;
+	h.entering = true;
+	h.x = h.n = mk(0.0f);
+	load_surface(mp, mb, mats, index0, h);
+	h.wo = sh.wo;
+	return h;
 }
 
 /* __raygen__spatial_reuse (mamba_shader.cu:418-510): neighbours are read
- * from res[res_in], the result written to res[1 - res_in]. */
-__global__ void __launch_bounds__(128) direct_spatial_kernel(DeviceScene s, MambaParams mp, MambaBuffers mb)
+ * from res[res_in], the result written to res[1 - res_in].  First launch:
+ * the two neighbours (their draws replayed) and the shadow rays of their
+ * samples seen from the centre. */
+__global__ void __launch_bounds__(128) spatial_gather_kernel(DeviceScene s, MambaParams mp, MambaBuffers mb)
 {
 	uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
 	if (pix >= mp.npix)
@@ -677,58 +775,101 @@ __global__ void __launch_bounds__(128) direct_spatial_kernel(DeviceScene s, Mamb
 	const MambaReservoirs Pin = mb.prev[mp.prev_in], Pout = mb.prev[1 - mp.prev_in];
 	MRes cur = load_res(Rin, pix);
 	SurfaceHit sh;
-	if (!load_surface(mp, mb, s.materials, pix, sh)) {
+	bool hit = load_surface(mp, mb, s.materials, pix, sh);
+	if (!hit || cur.M <= 0) {
+		if (hit)
+			mb.direct_Le[pix] = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
 		store_res(Rout, pix, cur);
 		MRes p = load_res(Pin, pix);
 		p.reset();
 		store_res(Pout, pix, p);
 		return;
 	}
-	if (cur.M <= 0) {
-		mb.direct_Le[pix] = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
-		store_res(Rout, pix, cur);
-		MRes p = load_res(Pin, pix);
-		p.reset();
-		store_res(Pout, pix, p);
+	f3 seed = 2.0f * mk((float)x, (float)y, mp.time);
+	(void)rand_uniform(seed); /* the centre's update */
+	int i0 = m_spatial_neighbor(mp, (int)pix, seed, MAMBA_RADIUS);
+	MRes nb0 = load_res(Rin, (uint32_t)i0);
+	if (nb0.M > 0)
+		(void)rand_uniform(seed); /* the first neighbour's update */
+	int i1 = m_spatial_neighbor(mp, (int)pix, seed, MAMBA_RADIUS);
+	MRes nb1 = load_res(Rin, (uint32_t)i1);
+	queue_ray(mb, pix, sh.x, nb0.data.position, nb0.M > 0);
+	queue_ray(mb, mp.npix + pix, sh.x, nb1.data.position, nb1.M > 0);
+}
+
+/* ... the merge over the centre and the neighbours' occluded targets, then
+ * the bias correction's shadow rays (the merged sample seen from each
+ * neighbour with a sample) and the lighting ray */
+__global__ void __launch_bounds__(128) spatial_resample_kernel(DeviceScene s, MambaParams mp, MambaBuffers mb)
+{
+	uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+	if (pix >= mp.npix)
 		return;
-	}
+	uint32_t x = pix % mp.width, y = pix / mp.width;
+	const MambaReservoirs Rin = mb.res[mp.res_in], Rout = mb.res[1 - mp.res_in];
+	MRes cur = load_res(Rin, pix);
+	SurfaceHit sh;
+	if (!load_surface(mp, mb, s.materials, pix, sh) || cur.M <= 0)
+		return;
 	MRes merged = fresh_res(2.0f * mk((float)x, (float)y, mp.time));
 	float t_current = m_target(sh, cur.data);
 	merged.update(cur.data, t_current * cur.W * (float)cur.M);
-	SurfaceHit hits[MAMBA_NEIGHBORS];
-	int sizes[MAMBA_NEIGHBORS];
-	bool valid[MAMBA_NEIGHBORS];
+	int index[MAMBA_NEIGHBORS], sizes[MAMBA_NEIGHBORS];
 	int count = 0;
 	for (int i = 0; i < MAMBA_NEIGHBORS; i++) {
-		int index0 = m_spatial_neighbor(mp, (int)pix, merged.seed, MAMBA_RADIUS);
-		MRes nb = load_res(Rin, (uint32_t)index0);
+		index[i] = m_spatial_neighbor(mp, (int)pix, merged.seed, MAMBA_RADIUS);
+		MRes nb = load_res(Rin, (uint32_t)index[i]);
 		nb.M = min(nb.M, MAMBA_MCAP);
 		if (nb.M > 0) {
-			float t_neighbor = m_occluded_target(s, mp.layout, sh, nb.data);
+			f3 Li = m_direct_unoccluded(sh, nb.data);
+			float t_neighbor = luminance(Li * (1.0f - (float)blocked(mb, (uint32_t)i * mp.npix + pix)));
 			merged.update(nb.data, t_neighbor * nb.W * (float)nb.M);
 		}
-		hits[i].mat = sh.mat;
-		hits[i].x = hits[i].n = mk(0.0f);
-		load_surface(mp, mb, s.materials, (uint32_t)index0, hits[i]);
-		hits[i].wo = sh.wo;
-		valid[i] = nb.M > 0;
 		sizes[i] = nb.M;
 		count += nb.M;
 	}
 	merged.M = cur.M + count;
+	store_res(Rout, pix, merged);
+	mb.spatial_aux[pix] = make_int4(index[0], index[1], sizes[0], sizes[1]);
+	for (int i = 0; i < MAMBA_NEIGHBORS; i++) {
+		SurfaceHit h = neighbour_hit(mp, mb, s.materials, (uint32_t)index[i], sh);
+		queue_ray(mb, (uint32_t)i * mp.npix + pix, h.x, merged.data.position, sizes[i] > 0);
+	}
+	queue_ray(mb, 2 * mp.npix + pix, sh.x, merged.data.position, true);
+}
+
+/* ... Z over the neighbours whose surface sees the merged sample, W, the
+ * direct light, and the previous reservoir of the next frame */
+__global__ void __launch_bounds__(128) spatial_finish_kernel(DeviceScene s, MambaParams mp, MambaBuffers mb)
+{
+	uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+	if (pix >= mp.npix)
+		return;
+	const MambaReservoirs Rin = mb.res[mp.res_in], Rout = mb.res[1 - mp.res_in];
+	const MambaReservoirs Pout = mb.prev[1 - mp.prev_in];
+	MRes cur = load_res(Rin, pix);
+	SurfaceHit sh;
+	if (!load_surface(mp, mb, s.materials, pix, sh) || cur.M <= 0)
+		return;
+	MRes merged = load_res(Rout, pix);
+	int4 aux = mb.spatial_aux[pix];
+	int index[MAMBA_NEIGHBORS] = {aux.x, aux.y}, sizes[MAMBA_NEIGHBORS] = {aux.z, aux.w};
 	int Z = cur.M;
 	for (int i = 0; i < MAMBA_NEIGHBORS; i++) {
-		float t_neighbor = valid[i] ? m_occluded_target(s, mp.layout, hits[i], merged.data) : 0.0f;
+		if (sizes[i] <= 0)
+			continue;
+		SurfaceHit h = neighbour_hit(mp, mb, s.materials, (uint32_t)index[i], sh);
+		f3 Li = m_direct_unoccluded(h, merged.data);
+		float t_neighbor = luminance(Li * (1.0f - (float)blocked(mb, (uint32_t)i * mp.npix + pix)));
 		if (t_neighbor > 0.0f)
 			Z += sizes[i];
 	}
 	float t_merged = m_target(sh, merged.data);
 	float denominator = t_merged * (float)Z;
 	merged.W = (denominator > 0.0f) ? merged.w / denominator : 0.0f;
-	store_res(Rout, pix, merged);
+	Rout.r3[pix].y = merged.W;
 	f3 Ld_res = m_direct_unoccluded(sh, merged.data);
-	bool occl = m_occluded(s, mp.layout, sh.x, merged.data.position);
-	accumulate_direct(mp, mb, pix, sh, Ld_res, occl, merged.W);
+	accumulate_direct(mp, mb, pix, sh, Ld_res, blocked(mb, 2 * mp.npix + pix), merged.W);
 	store_res(Pout, pix, merged);
 }
 
@@ -906,11 +1047,16 @@ __global__ void __launch_bounds__(128) gather_splat_kernel(DeviceScene s, MambaP
 						f3 wo = normalize((d * probe_wo + ppos) - hx);
 						if (dot(wo, hn) <= 0.0f)
 							continue;
+						uint32_t nb = T.bin_n[b];
+						if (nb == 0) {
+							sum = sum + (sec.mat.emission + mk(0.0f));
+							continue;
+						}
 						float geometric = kmax(dot(wo, hn), 0.0f);
 						f3 f = cleanse(m_brdf(sec, wo));
 						f3 le = cleanse(bin_radiance(T, b));
-						float n = (float)T.bin_n[b];
-						sum = sum + (sec.mat.emission + (n > 0.0f ? (le / n) * f * geometric : mk(0.0f)));
+						float n = (float)nb;
+						sum = sum + (sec.mat.emission + (le / n) * f * geometric);
 					}
 					Le = Le + sum / (float)KGR_PROBE_BINS;
 				}
@@ -1317,14 +1463,19 @@ __global__ void __launch_bounds__(128) final_gather_kernel(DeviceScene s, MambaP
 						f3 wo = normalize(((float)j * probe_wo + ppos) - sh.x);
 						if (dot(wo, sh.n) <= 0.0f)
 							continue;
-						float geometric = kmax(dot(wo, sh.n), 0.0f);
-						f3 f = cleanse(m_brdf(sh, wo));
-						float pdf = m_pdf(sh, wo);
-						f = pdf > 0.0f ? f / pdf : mk(0.0f);
 						size_t b = (size_t)p * KGR_PROBE_BINS + j;
+						uint32_t nb = T.bin_n[b];
+						if (nb == 0)
+							continue; /* adds an exact zero to a non-negative sum */
+						float geometric = kmax(dot(wo, sh.n), 0.0f);
+						f3 f;
+						float pdf;
+						m_brdf_pdf(sh, wo, f, pdf);
+						f = cleanse(f);
+						f = pdf > 0.0f ? f / pdf : mk(0.0f);
 						f3 le = cleanse(bin_radiance(T, b));
-						float n = (float)T.bin_n[b];
-						sum = sum + (n > 0.0f ? (le / n) * f * fabsf(dot(wo, pn)) * geometric : mk(0.0f));
+						float n = (float)nb;
+						sum = sum + (le / n) * f * fabsf(dot(wo, pn)) * geometric;
 					}
 					count++;
 				}
@@ -1420,6 +1571,12 @@ void for_each_frame_buffer(MambaBuffers &mb, const BufferSizes &z, F f)
 		}
 	}
 	f((void **)&mb.direct_Le, sizeof(float4) * z.npix);
+	f((void **)&mb.vis_o, sizeof(float4) * 3 * z.npix);
+	f((void **)&mb.vis_d, sizeof(float4) * 3 * z.npix);
+	f((void **)&mb.vis_flag, sizeof(uint32_t) * 3 * z.npix);
+	f((void **)&mb.vis_queue, sizeof(uint32_t) * 3 * z.npix);
+	f((void **)&mb.vis_counters, sizeof(uint32_t) * CNT_COUNT);
+	f((void **)&mb.spatial_aux, sizeof(int4) * z.npix);
 	for (float4 **b : {&mb.s_wi, &mb.s_Le, &mb.s_Ld, &mb.s_Ld_wi, &mb.s_hit_x, &mb.s_hit_n, &mb.s_hit_wo})
 		f((void **)b, sizeof(float4) * z.nsec);
 	f((void **)&mb.s_hit_mat, sizeof(int32_t) * z.nsec);
@@ -1587,18 +1744,55 @@ uint32_t mamba_render(const DeviceScene &s, const PathBuffers &pb, const MambaPa
 	done(STAGE_GENERATE);
 	launches += 3;
 	if (mp.direct_lighting) {
-		direct_primary_kernel<<<blocks_for(npix, 128), 128, 0, st>>>(s, mp, mb);
-		done(STAGE_RESTIR_PRIMARY);
-		launches++;
-		if (mp.temporal) {
-			direct_temporal_kernel<<<blocks_for(npix, 128), 128, 0, st>>>(s, mp, mb);
-			done(STAGE_RESTIR_TEMPORAL);
+		const unsigned grid = blocks_for(npix, 128);
+		PathBuffers vb = pb;
+		vb.sh_o = mb.vis_o;
+		vb.sh_d = mb.vis_d;
+		vb.shadow_queue = mb.vis_queue;
+		vb.counters = mb.vis_counters;
+		vb.shadow_flags = mb.vis_flag;
+		vb.capacity = 3 * npix;
+		auto rays = [&](int stage) {
+			pt_shadow_resolve(s, vb, mp.layout, tune, st);
+			done(stage);
 			launches++;
+		};
+		auto clear_queue = [&]() { KGR_CUDA(cudaMemsetAsync(mb.vis_counters, 0, CNT_COUNT * sizeof(uint32_t), st)); };
+		clear_queue();
+		primary_ris_kernel<<<grid, 128, 0, st>>>(s, mp, mb);
+		done(STAGE_RESTIR_PRIMARY);
+		rays(STAGE_RESTIR_PRIMARY);
+		primary_finish_kernel<<<grid, 128, 0, st>>>(s, mp, mb);
+		done(STAGE_RESTIR_PRIMARY);
+		launches += 2;
+		if (mp.temporal) {
+			clear_queue();
+			temporal_gather_kernel<<<grid, 128, 0, st>>>(s, mp, mb);
+			done(STAGE_RESTIR_TEMPORAL);
+			rays(STAGE_RESTIR_TEMPORAL_VIS);
+			clear_queue();
+			temporal_merge_kernel<<<grid, 128, 0, st>>>(s, mp, mb);
+			done(STAGE_RESTIR_TEMPORAL);
+			launches += 2;
+			if (!mp.spatial) {
+				rays(STAGE_RESTIR_TEMPORAL_VIS);
+				temporal_finish_kernel<<<grid, 128, 0, st>>>(s, mp, mb);
+				done(STAGE_RESTIR_TEMPORAL);
+				launches++;
+			}
 		}
 		if (mp.spatial) {
-			direct_spatial_kernel<<<blocks_for(npix, 128), 128, 0, st>>>(s, mp, mb);
+			clear_queue();
+			spatial_gather_kernel<<<grid, 128, 0, st>>>(s, mp, mb);
 			done(STAGE_RESTIR_SPATIAL);
-			launches++;
+			rays(STAGE_RESTIR_SPATIAL_VIS);
+			clear_queue();
+			spatial_resample_kernel<<<grid, 128, 0, st>>>(s, mp, mb);
+			done(STAGE_RESTIR_SPATIAL);
+			rays(STAGE_RESTIR_SPATIAL_VIS);
+			spatial_finish_kernel<<<grid, 128, 0, st>>>(s, mp, mb);
+			done(STAGE_RESTIR_SPATIAL);
+			launches += 3;
 		}
 	}
 	secondary_kernel<<<blocks_for(nsec, 128), 128, 0, st>>>(s, mp, mb);

@@ -238,6 +238,10 @@ __global__ void __launch_bounds__(BLOCK, KGR_MIN_BLOCKS(BLOCK, OCC)) shadow_reso
 		else
 			occ = trace_fast_stack<true, COUNT, LAYOUT>(s, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), b.w, h, stack,
 				&cnt);
+		if (pb.shadow_flags) {
+			pb.shadow_flags[p] = occ ? 1u : 0u;
+			continue;
+		}
 		float4 c = pb.pend_c[p], e = pb.pend_e[p], be = pb.pend_b[p];
 		f3 contr = occ ? mk(0.0f) : mk(c.x, c.y, c.z);
 		f3 direct = mk(e.x, e.y, e.z) + contr / c.w;
@@ -252,6 +256,10 @@ __global__ void __launch_bounds__(BLOCK, KGR_MIN_BLOCKS(BLOCK, OCC)) shadow_reso
  * L += beta * (Le + Ld) in the order of the recursion. */
 __device__ __forceinline__ void resolve_shadow(const PathBuffers &pb, uint32_t p, bool occ)
 {
+	if (pb.shadow_flags) {
+		pb.shadow_flags[p] = occ ? 1u : 0u;
+		return;
+	}
 	pb.L[p] = nee_add(pb.L[p], pb.pend_c[p], pb.pend_e[p], pb.pend_b[p], occ);
 }
 

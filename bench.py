@@ -90,6 +90,7 @@ def parse(argv=None):
     ap.add_argument("--no-serve", action="store_true", help="skip the serving run")
     ap.add_argument("--no-restir", action="store_true", help="skip the ReSTIR DI (256^2) and GI (1080p) runs")
     ap.add_argument("--serve-seconds", type=float, default=1.0, help="arrival window of the 200 req/s phase")
+    ap.add_argument("--no-mamba", action="store_true", help="skip the Mamba (editor GI mode) run")
     return ap.parse_args(argv)
 
 
@@ -630,6 +631,80 @@ def restir_runs(args):
     return out
 
 
+def mamba_run(args, g, sc, W, H):
+    """The "mamba" attachment (the editor's default GI mode, editor/mamba.cu:
+    1094-1300) on the benchmark's scene and resolution with direct lighting,
+    temporal and spatial reuse: 3 warm-up frames, then `MAMBA_FRAMES` frames
+    timed one by one with CUDA events on the render stream (median), the
+    first frame's time (it allocates most probes), the per-stage split of
+    the timed frames, and one oracle frame of the same configuration on all
+    host cores (oracle_mamba_frame; its third frame, state carried)."""
+    import torch
+
+    from artemis_gb300 import kgr
+
+    stream = torch.cuda.current_stream()
+    sptr = ctypes.c_void_p(stream.cuda_stream)
+    bufs = [torch.zeros((W * H, 4), dtype=torch.float32, device="cuda") for _ in range(4)]
+    ptrs = [b.data_ptr() for b in bufs]
+    cam = kgr.camera(g.eye, g.target, g.fov, W / H)
+    flags = {"direct_lighting": True, "temporal_reuse": True, "spatial_reuse": True}
+    att = kgr.Attachment("mamba")
+    att.attach(W, H)
+    for k, v in {**flags, "profile": True}.items():
+        att.set_option(k, v)
+    att.load()
+
+    def frame(f):
+        info = kgr.launch_info(cam, W, H, ptrs, samples=f)
+        info.time = 0.1 * f
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        att.render(info, sc, sptr)
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1)
+
+    first = frame(0)
+    for f in range(1, 3):
+        frame(f)
+    att.stage_times()
+    ms = [frame(f) for f in range(3, 3 + MAMBA_FRAMES)]
+    st = att.stage_times()
+    counters = np.zeros(2, np.int32)
+    att.debug_copy("mamba_counters", counters)
+    launches = att.stats().kernel_launches
+    att.close()
+    out = {"scene": args.scene, "triangles": sc.info().triangle_count, "resolution": [W, H],
+           "options": sorted(flags), "frames_timed": MAMBA_FRAMES,
+           "ms_per_frame_median": round(float(np.median(ms)), 3), "ms_first_frame": round(first, 3),
+           "stage_ms_per_frame": {k: round(v[0] / MAMBA_FRAMES, 3) for k, v in st.items()
+                                  if v[1] and k in MAMBA_STAGES},
+           "probes": int(counters[0]), "lookup_tables": int(counters[1]), "kernel_launches_per_frame": launches}
+    if not args.no_cpu_baseline:
+        try:
+            from oracle import pyoracle
+            osc = pyoracle.Scene(g.positions, g.normals, g.tris4(), g.materials_raw, sc.lights(), sc.bvh())
+            om = pyoracle.Mamba(W, H, 1 << 16, 64)  # the probe count stays far below either capacity
+            d = kgr.camera_dict(cam)
+            for f in range(3):
+                t0 = time.time()
+                om.frame(osc, pyoracle.mamba_params(W, H, d, time=0.1 * f, samples=f,
+                                                    **{k: int(v) for k, v in flags.items()}))
+                dt = time.time() - t0
+            om.close()
+            out["cpu_oracle"] = {"ms_per_frame": round(dt * 1e3, 1), "cores": os.cpu_count(),
+                                 "sample": "third frame, state carried from two before"}
+        except Exception as exc:  # reported, not required
+            out["cpu_oracle"] = {"ms_per_frame": None, "sample": f"failed: {exc}"}
+    return out
+
+
+MAMBA_FRAMES = 20
+MAMBA_STAGES = ("generate", "trace_closest", "restir_primary", "restir_temporal", "restir_spatial",
+                "restir_temporal_vis", "restir_spatial_vis", "mamba_secondary", "mamba_gather", "mamba_probes",
+                "mamba_final")
+
 SERVE_RES = [(320, 240), (640, 480), (1280, 720), (1920, 1080), (3840, 2160)]
 SERVE_SCENES = ("terrain_s", "terrain_m", "terrain_l")  # 0.26M, 1.0M, 4.1M triangles
 
@@ -923,6 +998,9 @@ def bench_ours(args):
     restir = None
     if rank == 0 and not args.no_restir:
         restir = restir_runs(args)
+    mamba = None
+    if rank == 0 and not args.no_mamba:
+        mamba = mamba_run(args, g, sc, W, H)
 
     cpu_base = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -957,6 +1035,7 @@ def bench_ours(args):
                 "equal_relmse_terrain": quality_terrain,
                 "serve": serve,
                 "restir": restir,
+                "mamba": mamba,
                 "cpu_baseline": cpu_base,
                 "e2e": {"value": round(e2e_value, 2), "unit": "Mrays/s",
                         "h2d_bytes_per_step": ctypes.sizeof(kgr.LaunchInfo),

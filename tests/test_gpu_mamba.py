@@ -57,9 +57,12 @@ def first_difference(a, b):
     return len(rows), rows[:5].tolist()
 
 
-def run(name, layout, flags, sky=None, frames=FRAMES, compare_every_frame=True):
+def run(name, layout, flags, sky=None, frames=FRAMES, compare_every_frame=True, size=(W, H),
+        tables=(MAX_PROBES, MAX_LUTS)):
     """Renders `frames` frames on the GPU and the oracle; returns the two
     attachments' final buffers and the per-frame colour agreement."""
+    W, H = size
+    max_probes, max_luts = tables
     g, sc, osc = helpers.both(name, 1)
     env = None
     if sky is not None:
@@ -68,10 +71,10 @@ def run(name, layout, flags, sky=None, frames=FRAMES, compare_every_frame=True):
                              env_filter=kgr.FILTER_POINT)
     att = kgr.Attachment("mamba")
     att.attach(W, H)
-    for k, v in {**flags, "layout": layout, "max_probes": MAX_PROBES, "max_luts": MAX_LUTS}.items():
+    for k, v in {**flags, "layout": layout, "max_probes": max_probes, "max_luts": max_luts}.items():
         att.set_option(k, v)
     att.load()
-    om = pyoracle.Mamba(W, H, MAX_PROBES, MAX_LUTS)
+    om = pyoracle.Mamba(W, H, max_probes, max_luts)
     bufs = helpers.device_buffers(torch, W * H)
     oflags = {k: int(v) for k, v in flags.items()}
     prev = None
@@ -135,6 +138,17 @@ def test_mamba_box_scene_matches_oracle(flags):
     counters = check(out, colors, f"box4k {sorted(flags)}")
     assert counters[0] > 10 and counters[1] >= 2
     assert colors[-1][0][:, :3].mean() > 0.01
+
+
+def test_mamba_1080p_terrain_matches_oracle():
+    """The benchmark's configuration as configured: 1920x1080 on the
+    1.16M-triangle terrain (half GGX), direct lighting with temporal and
+    spatial reuse, three frames with the state carried; every buffer bit
+    for bit."""
+    out, colors = run("terrain", "fast", DIRECT, frames=3, compare_every_frame=False, size=(1920, 1080),
+                      tables=(1 << 16, 64))
+    counters = check(out, colors, "terrain 1080p")
+    assert counters[0] > 100
 
 
 @pytest.mark.parametrize("layout", ["fast", "cw8", "threaded"])
@@ -201,9 +215,12 @@ def test_mamba_stage_times_and_launches():
     for f in range(3):
         att.render(helpers.launch(cam, W, H, bufs, samples=f), sc)
     t = att.stage_times()
-    for k in ("generate", "trace_closest", "restir_primary", "restir_temporal", "restir_spatial", "mamba_secondary",
-              "mamba_gather", "mamba_probes", "mamba_final"):
+    for k in ("generate", "trace_closest", "restir_primary", "restir_temporal", "restir_spatial",
+              "restir_temporal_vis", "restir_spatial_vis", "mamba_secondary", "mamba_gather", "mamba_probes",
+              "mamba_final"):
         assert t[k][1] > 0 and t[k][0] > 0.0, k
-    assert att.stats().kernel_launches == 15
+    # G-buffer 3, primary 3, temporal 3 (2 rays + merge; spatial follows), spatial 5,
+    # secondary 1, splat 2, Sobel + raster + collapse + allocation 5, final gather 1
+    assert att.stats().kernel_launches == 23
     att.close()
     sc.close()

@@ -1349,10 +1349,10 @@ void render_restir_di(kgr_attachment *att, const kgr_launch_info *info, const kg
 	att->last_paths = fp.paths;
 }
 
-/* The editor's Mamba frame (Mamba::render, editor/mamba.cu:1094-1300): see
+/* The editor's Mamba frame (Mamba::render, editor/mamba.cu:941-1312): see
  * kgr_mamba.h.  Its options are the reference's Mamba switches:
  * direct_lighting, indirect_lighting, irradiance, render_probes and
- * render_probe_radiance (Mamba::options, editor/mamba.cuh:61-67),
+ * render_probe_radiance (Mamba::options, editor/mamba.cuh:60-67),
  * temporal_reuse and spatial_reuse (:57-58). */
 void render_mamba(kgr_attachment *att, const kgr_launch_info *info, const kgr_scene *sc, cudaStream_t st)
 {

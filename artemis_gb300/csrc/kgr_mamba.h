@@ -1,6 +1,6 @@
 /*
  * kgr_mamba.h -- state and launcher of the "mamba" attachment: the editor's
- * default global-illumination mode (Mamba::render, editor/mamba.cu:1094-1300).
+ * default global-illumination mode (Mamba::render, editor/mamba.cu:941-1312).
  *
  * A frame is, in the reference's order:
  *   G-buffer       primary hits of every pixel centre (the reference rasters
@@ -10,16 +10,16 @@
  *                  when "direct_lighting" is set
  *   secondary      one BSDF-sampled ray per 4x4 block of pixels, cycling
  *                  through the block over 16 frames, and a light sample at
- *                  the primary vertex (mamba_shader.cu:511-679)
+ *                  the primary vertex (mamba_shader.cu:512-680)
  *   gather         the secondary radiance splatted into irradiance probes
- *                  (secondary_gather, mamba.cu:436-616)
+ *                  (secondary_gather, mamba.cu:401-576)
  *   sobel, raster, collapse, allocation
  *                  normal edges, the probe that covers each pixel, up to
  *                  four probes per 16x16 group, and new probes where a
- *                  16x16 block is less than 60% covered (mamba.cu:169-371,
- *                  843-906, mamba_kernels.cu:5-183)
+ *                  16x16 block is less than 60% covered (mamba.cu:169-369,
+ *                  889-938, mamba_kernels.cu:5-183)
  *   final gather   emission + direct + the two nearest probes' irradiance
- *                  (mamba.cu:618-841)
+ *                  (mamba.cu:686-878)
  *
  * The probe table is the reference's two-level hash (editor/optix/probe.cuh):
  * a top lookup table of 10-unit cells over a 250-unit cube at the origin,
@@ -48,13 +48,13 @@ namespace kgr {
 
 /* IrradianceProbe::size^2 (probe.cuh:11) */
 #define KGR_PROBE_BINS 25
-/* IrradianceProbeLUT MAX_REFS (probe.cuh:83) */
+/* IrradianceProbeLUT MAX_REFS (probe.cuh:78) */
 #define KGR_LUT_REFS 32767
 /* fixed-point scale of a bin's radiance sum: 2^20 */
 #define KGR_MAMBA_FIXED 1048576.0f
 #define KGR_MAMBA_UNFIXED 9.5367431640625e-07f
 
-/* One lookup table's header (IrradianceProbeLUT, probe.cuh:85-106): the
+/* One lookup table's header (IrradianceProbeLUT, probe.cuh:80-104): the
  * top table is level 2 with 10-unit cells, a second-level table level 1
  * with 0.4-unit cells. */
 struct MambaLut {
@@ -66,7 +66,7 @@ struct MambaLut {
 	int32_t pad;
 };
 
-/* IrradianceProbeTable (probe.cuh:365-530) in structure-of-arrays form. */
+/* IrradianceProbeTable (probe.cuh:365-520) in structure-of-arrays form. */
 struct MambaTable {
 	MambaLut *luts;       /* max_luts */
 	int32_t *refs;        /* max_luts * KGR_LUT_REFS: -1 empty, else the LUT (top) or probe index */
@@ -141,7 +141,7 @@ struct MambaParams {
 	int32_t layout;
 	int32_t res_in, prev_in; /* which of the two reservoir and previous sets are current */
 	uint32_t stamp_base;     /* this frame's depth stamps are stamp_base + record + 1 */
-	/* IrradianceProbe::from_index (probe.cuh:53-72) of each bin: a local
+	/* IrradianceProbe::from_index (probe.cuh:56-73) of each bin: a local
 	 * direction, computed on the host */
 	float bin_dir[KGR_PROBE_BINS][3];
 };
@@ -169,7 +169,7 @@ bool mamba_buffer(const MambaBuffers &mb, int res_in, int prev_in, uint32_t widt
 void mamba_bin_directions(float out[KGR_PROBE_BINS][3]);
 
 /* Empty table: every ref -1, hashes all ones, the top table's header
- * (probe.cuh:102-111), counters {0, 1}, bins zero. */
+ * (probe.cuh:106-118), counters {0, 1}, bins zero. */
 void mamba_table_clear(const MambaTable &t, cudaStream_t st);
 
 /* Resets the depth stamps to 0 keeping the depths (when stamp_base would

@@ -2,7 +2,7 @@
  * mamba.cu -- the "mamba" attachment's kernels: G-buffer, ReSTIR DI with 8
  * candidates, the quarter-resolution secondary rays, the irradiance-probe
  * splat, Sobel filter, probe raster, collapse and allocation, and the final
- * gather (Mamba::render, editor/mamba.cu:1094-1300).  The state and the
+ * gather (Mamba::render, editor/mamba.cu:941-1312).  The state and the
  * choices that make the frame deterministic are described in kgr_mamba.h.
  */
 #include "kgr_mamba.h"
@@ -22,10 +22,10 @@ namespace {
 #define MAMBA_PI 3.14159265358979323846f  /* brdf.cuh PI, a float */
 #define MAMBA_PI_D 3.14159265358979323846 /* M_PI, a double */
 #define MAMBA_CANDIDATES 8                /* __raygen__direct_primary, mamba_shader.cu:249 */
-#define MAMBA_MCAP 200                    /* mamba_shader.cu:366, :459 */
-#define MAMBA_NEIGHBORS 2                 /* mamba_shader.cu:448 */
-#define MAMBA_RADIUS 20                   /* mamba_shader.cu:452 */
-#define MAMBA_ENV_DISTANCE 1000.0f        /* ENVIRONMENT_DISTANCE, mamba_shader.cu:101 */
+#define MAMBA_MCAP 200                    /* mamba_shader.cu:371, :468 */
+#define MAMBA_NEIGHBORS 2                 /* mamba_shader.cu:457 */
+#define MAMBA_RADIUS 20                   /* mamba_shader.cu:464 */
+#define MAMBA_ENV_DISTANCE 1000.0f        /* ENVIRONMENT_DISTANCE, mamba_shader.cu:99 */
 #define MAMBA_OCCLUSION_EPS 1e-3f         /* occluded(), mamba_shader.cu:41 */
 #define MAMBA_SIZE 5                      /* IrradianceProbe::size */
 #define MAMBA_TOP_SIZE 250.0f             /* IrradianceProbeLUT::L2 = L1 * 25 */
@@ -33,7 +33,7 @@ namespace {
 #define MAMBA_DIVISION 25.0f              /* RESOLUTION_DIVISION */
 #define MAMBA_FIXED_LIMIT 4611686018427387904.0f /* 2^62: a splat is clamped to +-2^62 */
 
-/* COLOR_WHEEL (mamba.cu:233-246): the probe indicator's colours. */
+/* COLOR_WHEEL (mamba.cu:227-241): the probe indicator's colours. */
 __constant__ float c_color_wheel[12][3] = {{0.910f, 0.490f, 0.490f}, {0.910f, 0.700f, 0.490f},
 	{0.910f, 0.910f, 0.490f}, {0.700f, 0.910f, 0.490f}, {0.490f, 0.910f, 0.490f}, {0.490f, 0.910f, 0.700f},
 	{0.490f, 0.910f, 0.910f}, {0.490f, 0.700f, 0.910f}, {0.490f, 0.490f, 0.910f}, {0.700f, 0.490f, 0.910f},
@@ -41,7 +41,7 @@ __constant__ float c_color_wheel[12][3] = {{0.910f, 0.490f, 0.490f}, {0.910f, 0.
 
 /* ------------------------------------------------------------ surfaces -- */
 
-/* load_surface_hit (mamba_shader.cu:167-216) over the traced G-buffer: the
+/* load_surface_hit (mamba_shader.cu:166-219) over the traced G-buffer: the
  * normal turned toward the camera, the point pushed 1e-3 along it (against
  * it for transmissive materials). */
 __device__ __forceinline__ bool load_surface(const MambaParams &mp, const MambaBuffers &mb,
@@ -117,7 +117,7 @@ __device__ __forceinline__ float4 sky_at(const DeviceScene &s, const f3 &d)
 	return tex2D<float4>((cudaTextureObject_t)s.env, u, 1.0f - v);
 }
 
-/* ray_at (mamba_shader.cu:91-98): the direction of a pixel's corner */
+/* ray_at (mamba_shader.cu:89-97): the direction of a pixel's corner */
 __device__ __forceinline__ f3 ray_at(const MambaParams &mp, uint32_t x, uint32_t y)
 {
 	uint32_t yy = mp.height - (y + 1);
@@ -143,7 +143,7 @@ __device__ __forceinline__ LightInfo no_light()
 	return l;
 }
 
-/* sample_light (mamba_shader.cu:103-164): a uniform pick over the area
+/* sample_light (mamba_shader.cu:101-164): a uniform pick over the area
  * lights and the sky, then a point.  An area light here is one emissive
  * triangle with vertices a, a + ab, a + ac.  Returns the point's pdf, or
  * -1 with nothing to sample. */
@@ -185,7 +185,7 @@ __device__ __forceinline__ float m_sample_light(const DeviceScene &s, LightInfo 
 	return 1.0f / (area * (float)total);
 }
 
-/* direct_unoccluded (mamba_shader.cu:76-89) */
+/* direct_unoccluded (mamba_shader.cu:74-87) */
 __device__ __forceinline__ f3 m_direct_unoccluded(const SurfaceHit &sh, const LightInfo &li)
 {
 	f3 wi = normalize(li.position - sh.x);
@@ -197,7 +197,7 @@ __device__ __forceinline__ f3 m_direct_unoccluded(const SurfaceHit &sh, const Li
 	return rho * li.emission * ldotn * ndotwi * falloff;
 }
 
-/* target (mamba_shader.cu:271-276); occluded_target (:278-286) is this
+/* target (mamba_shader.cu:274-279); occluded_target (:281-287) is this
  * times 1 - occluded, with the shadow ray walked by visibility_kernel */
 __device__ __forceinline__ float m_target(const SurfaceHit &sh, const LightInfo &li)
 {
@@ -279,7 +279,7 @@ __device__ __forceinline__ void accumulate_direct(const MambaParams &mp, const M
 	mb.direct_Le[pix] = f4_of(le, 0.0f);
 }
 
-/* reproject (mamba_shader.cu:288-320): the pixel itself unless the camera
+/* reproject (mamba_shader.cu:289-321): the pixel itself unless the camera
  * moved (samples = 0); indices outside the image are rejected */
 __device__ __forceinline__ int m_reproject(const MambaParams &mp, int index, const f3 &x)
 {
@@ -302,7 +302,7 @@ __device__ __forceinline__ int m_reproject(const MambaParams &mp, int index, con
 	return iy * (int)mp.width + ix;
 }
 
-/* sample_spatial_neighborhood (mamba_shader.cu:396-416) */
+/* sample_spatial_neighborhood (mamba_shader.cu:395-417) */
 __device__ __forceinline__ int m_spatial_neighbor(const MambaParams &mp, int index, f3 &seed, int radius)
 {
 	int width = (int)mp.width, height = (int)mp.height;
@@ -331,13 +331,16 @@ __device__ __forceinline__ Onb onb_from_normal(const f3 &n)
 {
 	Onb o;
 	o.w = normalize(n);
-	f3 a = ((double)fabsf(o.w.x) > 0.9) ? mk(0.0f, 1.0f, 0.0f) : mk(1.0f, 0.0f, 0.0f);
+	/* fabs(w.x) > 0.9 compares in double; for a float, x > 0.9f is the same
+	 * test (0.9f is just below 0.9, and the next float is above it) without
+	 * the FP64 pipe */
+	f3 a = (fabsf(o.w.x) > 0.9f) ? mk(0.0f, 1.0f, 0.0f) : mk(1.0f, 0.0f, 0.0f);
 	o.v = normalize(cross(o.w, a));
 	o.u = cross(o.w, o.v);
 	return o;
 }
 
-/* to_disk + to_index (probe.cuh:31-51): the disk bin of a local
+/* to_disk + to_index (probe.cuh:36-54): the disk bin of a local
  * direction.  A direction with a NaN component falls in bin 0, as the
  * reference's float-to-int conversion of NaN gives 0. */
 __device__ __forceinline__ void to_disk(const f3 &v, float &su, float &sv)
@@ -370,7 +373,7 @@ __device__ __forceinline__ bool lut_contains(const MambaLut &L, const f3 &x, boo
 	return (x.x >= mn.x && x.y >= mn.y && x.z >= mn.z) && (x.x <= mx.x && x.y <= mx.y && x.z <= mx.z);
 }
 
-/* hash (probe.cuh:138-158): cell coordinates in 11 bits each, shuffled;
+/* hash (probe.cuh:168-187): cell coordinates in 11 bits each, shuffled;
  * the first shuffle shifts a signed value (arithmetic shift) */
 __device__ __forceinline__ uint32_t lut_hash(const MambaLut &L, const f3 &x, int dx, int dy, int dz)
 {
@@ -399,7 +402,7 @@ __device__ __forceinline__ MambaLut load_lut(const MambaTable &T, int32_t l)
 	return T.luts[l];
 }
 
-/* lookup (probe.cuh:209-241): of the two slots of x's cell (or of a
+/* lookup (probe.cuh:256-285): of the two slots of x's cell (or of a
  * neighbouring cell ni), the one with the same hash nearest to x */
 __device__ __forceinline__ int32_t lut_lookup(const MambaTable &T, int32_t l, const MambaLut &L, const f3 &x,
 		int ni)
@@ -425,7 +428,7 @@ __device__ __forceinline__ int32_t lut_lookup(const MambaTable &T, int32_t l, co
 	return index;
 }
 
-/* full_lookup (probe.cuh:243-257) */
+/* full_lookup (probe.cuh:287-301) */
 __device__ __forceinline__ int32_t lut_full_lookup(const MambaTable &T, int32_t l, const f3 &x)
 {
 	MambaLut L = load_lut(T, l);
@@ -440,7 +443,7 @@ __device__ __forceinline__ int32_t lut_full_lookup(const MambaTable &T, int32_t 
 	return r;
 }
 
-/* lookup_L2 (probe.cuh:660-695): linear probing over the top table from
+/* lookup_L2 (probe.cuh:678-712): linear probing over the top table from
  * the cell's hash to the first empty slot or the slot whose cell holds x */
 __device__ __forceinline__ int32_t top_lookup(const MambaTable &T, const f3 &x)
 {
@@ -462,7 +465,7 @@ __device__ __forceinline__ int32_t top_lookup(const MambaTable &T, const f3 &x)
 }
 
 /* The second-level table of x, or -1: lookup_L2 and the reference's guard
- * against an index at or above the probe counter (mamba.cu:274, :501) */
+ * against an index at or above the probe counter (mamba.cu:278, 456, 490, 550, 793) */
 __device__ __forceinline__ int32_t table_of(const MambaTable &T, const f3 &x, int32_t probe_counter)
 {
 	int32_t r = top_lookup(T, x);
@@ -474,7 +477,7 @@ __device__ __forceinline__ int32_t table_of(const MambaTable &T, const f3 &x, in
 	return l;
 }
 
-/* closest<2> (probe.cuh:259-325): the two nearest occupied slots among the
+/* closest<2> (probe.cuh:305-363): the two nearest occupied slots among the
  * two tries of x's cell and of its 27 neighbours (no hash check) */
 __device__ __forceinline__ void lut_closest2(const MambaTable &T, int32_t l, const f3 &x, int32_t idx[2],
 		float dist[2])
@@ -586,7 +589,7 @@ __global__ void gbuffer_store_kernel(DeviceScene s, PathBuffers pb, MambaParams 
 /* ------------------------------------------------ direct lighting rays -- */
 
 /* The direct-lighting passes run as wavefronts: a resampling kernel queues
- * its shadow rays -- occluded(origin, target) of mamba_shader.cu:36-64, in
+ * its shadow rays -- occluded(origin, target) of mamba_shader.cu:38-64, in
  * slot k * npix + pixel -- the path tracer's any-hit walk (tuned launch
  * shape) takes them all with full warps and stores a blocked flag per slot,
  * and the next kernel reads the flags.  Each kernel redoes the arithmetic
@@ -607,7 +610,7 @@ __device__ __forceinline__ bool blocked(const MambaBuffers &mb, uint32_t slot)
 	return mb.vis_flag[slot] != 0u;
 }
 
-/* __raygen__direct_primary (mamba_shader.cu:221-269): the eight candidates
+/* __raygen__direct_primary (mamba_shader.cu:221-272): the eight candidates
  * and the selected sample's shadow ray */
 __global__ void __launch_bounds__(128) primary_ris_kernel(DeviceScene s, MambaParams mp, MambaBuffers mb)
 {
@@ -654,7 +657,7 @@ __global__ void __launch_bounds__(128) primary_finish_kernel(DeviceScene s, Mamb
 		accumulate_direct(mp, mb, pix, sh, Ld_res, occl, r.W);
 }
 
-/* __raygen__temporal_reuse (mamba_shader.cu:322-393).  The previous
+/* __raygen__temporal_reuse (mamba_shader.cu:323-393).  The previous
  * reservoirs are read from prev[prev_in] as the last frame left them and
  * written to prev[1 - prev_in] (every pixel writes its entry).  First
  * launch: the shadow rays of the current and the reprojected previous
@@ -761,7 +764,7 @@ __device__ __forceinline__ SurfaceHit neighbour_hit(const MambaParams &mp, const
 	return h;
 }
 
-/* __raygen__spatial_reuse (mamba_shader.cu:418-510): neighbours are read
+/* __raygen__spatial_reuse (mamba_shader.cu:419-510): neighbours are read
  * from res[res_in], the result written to res[1 - res_in].  First launch:
  * the two neighbours (their draws replayed) and the shadow rays of their
  * samples seen from the centre. */
@@ -873,7 +876,7 @@ __global__ void __launch_bounds__(128) spatial_finish_kernel(DeviceScene s, Mamb
 	store_res(Pout, pix, merged);
 }
 
-/* The closest-hit program of the secondary rays (mamba_shader.cu:719-777):
+/* The closest-hit program of the secondary rays (mamba_shader.cu:707-777):
  * interpolated position, geometric normal against the ray, shading normal
  * on its side. */
 __device__ __forceinline__ void m_closest_surface(const DeviceScene &s, const kgr_hit &h, const f3 &dir, f3 &x,
@@ -895,7 +898,7 @@ __device__ __forceinline__ void m_closest_surface(const DeviceScene &s, const kg
 	mat = (int32_t)t.w;
 }
 
-/* Ld (mamba_shader.cu:512-560): a light sample seen from the primary
+/* Ld (mamba_shader.cu:512-561): a light sample seen from the primary
  * vertex; Le, wi and R are set when it is unblocked and the vertex is not
  * emissive. */
 __device__ __forceinline__ f3 m_Ld(const DeviceScene &s, int layout, const SurfaceHit &sh, f3 &seed, f3 &Le, f3 &wi,
@@ -923,7 +926,7 @@ __device__ __forceinline__ f3 m_Ld(const DeviceScene &s, int layout, const Surfa
 	return out;
 }
 
-/* __raygen__secondary (mamba_shader.cu:562-679): pixel (4 sx + c % 4,
+/* __raygen__secondary (mamba_shader.cu:563-680): pixel (4 sx + c % 4,
  * 4 sy + c / 4) with c = samples % 16 of each 4x4 block */
 __global__ void __launch_bounds__(128) secondary_kernel(DeviceScene s, MambaParams mp, MambaBuffers mb)
 {
@@ -980,7 +983,7 @@ __global__ void __launch_bounds__(128) secondary_kernel(DeviceScene s, MambaPara
 	mb.s_hit_mat[li] = hmat;
 }
 
-/* secondary_gather (mamba.cu:436-616), first half: each secondary pixel's
+/* secondary_gather (mamba.cu:401-576), first half: each secondary pixel's
  * two splats -- its radiance (plus what the probe at its hit point sends
  * back) into the probe at the primary vertex, and the light sample's
  * emission into the probe at the hit point -- computed against the table
@@ -1102,7 +1105,7 @@ __global__ void gather_apply_kernel(MambaParams mp, MambaBuffers mb)
 	atomicMax(&T.bin_depth[bin], key);
 }
 
-/* sobel_normal (mamba.cu:169-200): the sum of |n - n'| over the 3x3
+/* sobel_normal (mamba.cu:169-201): the sum of |n - n'| over the 3x3
  * neighbourhood, in the reference's loop order (its rows run bottom up) */
 __global__ void sobel_kernel(MambaParams mp, MambaBuffers mb)
 {
@@ -1126,7 +1129,7 @@ __global__ void sobel_kernel(MambaParams mp, MambaBuffers mb)
 	mb.sobel[pix] = acc;
 }
 
-/* raster_probes (mamba.cu:248-371): the probe nearest each pixel's
+/* raster_probes (mamba.cu:244-369): the probe nearest each pixel's
  * position and whether the pixel lies within its disk; pixels outside the
  * table keep their values. */
 __global__ void __launch_bounds__(128) raster_kernel(MambaParams mp, MambaBuffers mb)
@@ -1191,7 +1194,7 @@ __global__ void __launch_bounds__(128) raster_kernel(MambaParams mp, MambaBuffer
 	mb.probe_ids[pix] = probe_index;
 }
 
-/* probe_collapse (mamba.cu:851-906): up to four distinct probe ids per
+/* probe_collapse (mamba.cu:889-938): up to four distinct probe ids per
  * 16x16 group, in column-major scan order */
 __global__ void collapse_kernel(MambaParams mp, MambaBuffers mb)
 {
@@ -1295,7 +1298,7 @@ __global__ void alloc_candidates_kernel(MambaParams mp, MambaBuffers mb)
 }
 
 /* request_L2 + lookup-table allocation + request_L1 + probe allocation of
- * one candidate (probe.cuh:589-657, :531-567; mamba_kernels.cu:100-182). */
+ * one candidate (probe.cuh:560-676, :522-558; mamba_kernels.cu:100-182). */
 __device__ void allocate_probe(const MambaParams &mp, const MambaBuffers &mb, int2 px)
 {
 	const MambaTable &T = mb.table;
@@ -1420,7 +1423,7 @@ __global__ void __launch_bounds__(1024) alloc_serial_kernel(MambaParams mp, Mamb
 		allocate_probe(mp, mb, mb.cand_pixel[mb.cand_list[c]]);
 }
 
-/* final_gather (mamba.cu:698-841) */
+/* final_gather (mamba.cu:686-878) */
 __global__ void __launch_bounds__(128) final_gather_kernel(DeviceScene s, MambaParams mp, MambaBuffers mb,
 		float4 *color)
 {

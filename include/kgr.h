@@ -376,7 +376,7 @@ kgr_status kgr_environment_sample(const kgr_environment *env, const float *uv, u
 kgr_status kgr_environment_destroy(kgr_environment *env);
 
 /* kind: "path_tracer", "restir_di", "restir_gi" or "mamba" (the editor's
- * default GI mode, editor/mamba.cu:1094-1300: ReSTIR DI with 8 candidates,
+ * default GI mode, editor/mamba.cu:941-1312: ReSTIR DI with 8 candidates,
  * quarter-resolution secondary rays and irradiance probes; it lights with
  * the scene's triangles and the environment map, and refuses quad lights). */
 kgr_status kgr_create(const char *kind, kgr_attachment **out);

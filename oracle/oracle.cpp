@@ -2283,7 +2283,7 @@ extern "C" void oracle_tonemap(const float *hdr, uint32_t *ldr, uint32_t width, 
 
 /* ================================================================ Mamba == */
 /*
- * The editor's Mamba frame (Mamba::render, editor/mamba.cu:1094-1300) with
+ * The editor's Mamba frame (Mamba::render, editor/mamba.cu:941-1312) with
  * the deterministic choices of the GPU build: traced G-buffer at pixel
  * centres, probes allocated in 16x16-block order, bin radiance summed in
  * 64-bit fixed point (2^-20), a bin's depth from the frame's last splat in
@@ -2296,13 +2296,13 @@ namespace {
 
 const int M_BINS = 25;        /* IrradianceProbe::size^2 (probe.cuh:11) */
 const int M_SIZE = 5;
-const int M_REFS = 32767;     /* MAX_REFS (probe.cuh:83) */
+const int M_REFS = 32767;     /* MAX_REFS (probe.cuh:78) */
 const float M_PI_F = 3.14159265358979323846f;
 const double M_PI_DBL = 3.14159265358979323846;
 const float M_FIXED = 1048576.0f;
 const float M_UNFIXED = 9.5367431640625e-07f;
 
-struct MLut { /* IrradianceProbeLUT header (probe.cuh:85-106) */
+struct MLut { /* IrradianceProbeLUT header (probe.cuh:80-104) */
 	float center[3];
 	float size;
 	float resolution;
@@ -2420,7 +2420,7 @@ float m_pdf(const SurfaceHit &sh, const f3 &wi)
 	return ggx_pdf(sh.mat, sh.n, wi, sh.wo);
 }
 
-/* to_disk / to_index (probe.cuh:31-51); a NaN direction is bin 0 */
+/* to_disk / to_index (probe.cuh:36-54); a NaN direction is bin 0 */
 void m_to_disk(const f3 &v, float &su, float &sv)
 {
 	float theta = katan2(v.y, v.x);
@@ -2443,7 +2443,7 @@ int32_t m_bin(const f3 &v)
 	return i < 0 ? 0 : (i > M_BINS - 1 ? M_BINS - 1 : i);
 }
 
-/* from_index + from_uv (probe.cuh:53-72) of every bin */
+/* from_index + from_uv (probe.cuh:56-73) of every bin */
 void m_bin_dirs(f3 out[M_BINS])
 {
 	for (int index = 0; index < M_BINS; index++) {
@@ -2498,7 +2498,7 @@ void m_clear_table(MambaState &m)
 	m.bin_le.assign(3 * bins, 0);
 	m.bin_n.assign(bins, 0);
 	m.bin_depth.assign(bins, 0);
-	/* IrradianceProbeLUT::alloc of the top table (probe.cuh:102-111) */
+	/* IrradianceProbeLUT::alloc of the top table (probe.cuh:106-118) */
 	MLut &top = m.luts[0];
 	top.level = 2;
 	top.size = 250.0f;
@@ -2533,7 +2533,7 @@ struct MambaFrame {
 		env_fetch4(s, u, 1.0f - v, out);
 	}
 
-	/* load_surface_hit (mamba_shader.cu:167-216) */
+	/* load_surface_hit (mamba_shader.cu:166-219) */
 	bool surface(size_t pix, SurfaceHit &sh) const
 	{
 		int32_t idx = m->g_index[pix];
@@ -2554,7 +2554,7 @@ struct MambaFrame {
 		return true;
 	}
 
-	/* sample_light (mamba_shader.cu:103-164); an area light is one emissive
+	/* sample_light (mamba_shader.cu:101-164); an area light is one emissive
 	 * triangle with vertices a, a + ab, a + ac */
 	float sample_light(MLight &li, f3 &seed) const
 	{
@@ -2596,7 +2596,7 @@ struct MambaFrame {
 		return 1.0f / (area * (float)total);
 	}
 
-	/* direct_unoccluded (mamba_shader.cu:76-89) */
+	/* direct_unoccluded (mamba_shader.cu:74-87) */
 	f3 direct_unoccluded(const SurfaceHit &sh, const MLight &li) const
 	{
 		f3 wi = normalize(li.position - sh.x);
@@ -2615,7 +2615,7 @@ struct MambaFrame {
 		return trace_any(s, o, d, tmax, &a, &b);
 	}
 
-	/* occluded (mamba_shader.cu:36-64) */
+	/* occluded (mamba_shader.cu:38-64) */
 	bool occluded(const f3 &origin_, const f3 &target, uint64_t &rays) const
 	{
 		f3 dir = normalize(target - origin_);
@@ -2638,7 +2638,7 @@ struct MambaFrame {
 		m->direct_le[pix] = f4(le, 0.0f);
 	}
 
-	/* reproject (mamba_shader.cu:288-320) */
+	/* reproject (mamba_shader.cu:289-321) */
 	int reproject(int index, const f3 &x) const
 	{
 		if (p->samples > 0)
@@ -2660,7 +2660,7 @@ struct MambaFrame {
 		return iy * (int)m->width + ix;
 	}
 
-	/* sample_spatial_neighborhood (mamba_shader.cu:396-416) */
+	/* sample_spatial_neighborhood (mamba_shader.cu:395-417) */
 	int spatial_neighbor(int index, f3 &seed) const
 	{
 		int width = (int)m->width, height = (int)m->height;
@@ -2685,7 +2685,7 @@ struct MambaFrame {
 		return (x.x >= mn.x && x.y >= mn.y && x.z >= mn.z) && (x.x <= mx.x && x.y <= mx.y && x.z <= mx.z);
 	}
 
-	/* hash (probe.cuh:138-158); the first shuffle shifts a signed value */
+	/* hash (probe.cuh:168-187); the first shuffle shifts a signed value */
 	static uint32_t hash(const MLut &L, const f3 &x, int dx, int dy, int dz)
 	{
 		float cdx = x.x - L.center[0] + L.size / 2.0f;
@@ -2708,7 +2708,7 @@ struct MambaFrame {
 		return hash(L, x, ni % 3 - 1, (ni / 3) % 3 - 1, ni / 9 - 1);
 	}
 
-	/* lookup (probe.cuh:209-241) */
+	/* lookup (probe.cuh:256-285) */
 	int32_t lookup(int32_t l, const f3 &x, int ni) const
 	{
 		const MLut &L = m->luts[l];
@@ -2733,7 +2733,7 @@ struct MambaFrame {
 		return index;
 	}
 
-	/* full_lookup (probe.cuh:243-257) */
+	/* full_lookup (probe.cuh:287-301) */
 	int32_t full_lookup(int32_t l, const f3 &x) const
 	{
 		int32_t r = lookup(l, x, -1);
@@ -2742,7 +2742,7 @@ struct MambaFrame {
 		return r;
 	}
 
-	/* lookup_L2 (probe.cuh:660-695) */
+	/* lookup_L2 (probe.cuh:678-712) */
 	int32_t top_lookup(const f3 &x) const
 	{
 		const MLut &L = m->luts[0];
@@ -2763,7 +2763,7 @@ struct MambaFrame {
 	}
 
 	/* lookup_L2 and the guard against an index at or above the probe
-	 * counter (mamba.cu:274, :501) */
+	 * counter (mamba.cu:278, 456, 490, 550, 793) */
 	int32_t table_of(const f3 &x, int32_t probe_counter) const
 	{
 		int32_t r = top_lookup(x);
@@ -2775,7 +2775,7 @@ struct MambaFrame {
 		return l;
 	}
 
-	/* closest<2> (probe.cuh:259-325) */
+	/* closest<2> (probe.cuh:305-363) */
 	void closest2(int32_t l, const f3 &x, int32_t idx[2], float dist[2]) const
 	{
 		const MLut &L = m->luts[l];
@@ -2847,7 +2847,7 @@ struct MambaFrame {
 		closest_rays += rays;
 	}
 
-	/* __raygen__direct_primary (mamba_shader.cu:221-269) */
+	/* __raygen__direct_primary (mamba_shader.cu:221-272) */
 	void direct_primary()
 	{
 		MRes4 &R = m->res[m->res_in];
@@ -2880,7 +2880,7 @@ struct MambaFrame {
 		shadow_rays += rays;
 	}
 
-	/* __raygen__temporal_reuse (mamba_shader.cu:322-393) */
+	/* __raygen__temporal_reuse (mamba_shader.cu:323-393) */
 	void direct_temporal()
 	{
 		MRes4 &R = m->res[m->res_in];
@@ -2932,7 +2932,7 @@ struct MambaFrame {
 		shadow_rays += rays;
 	}
 
-	/* __raygen__spatial_reuse (mamba_shader.cu:418-510) */
+	/* __raygen__spatial_reuse (mamba_shader.cu:419-510) */
 	void direct_spatial()
 	{
 		const MRes4 &Rin = m->res[m->res_in];
@@ -3002,7 +3002,7 @@ struct MambaFrame {
 		shadow_rays += rays;
 	}
 
-	/* Ld (mamba_shader.cu:512-560) */
+	/* Ld (mamba_shader.cu:512-561) */
 	f3 Ld(const SurfaceHit &sh, f3 &seed, f3 &Le, f3 &wi, float &R, uint64_t &rays) const
 	{
 		MLight li = m_no_light();
@@ -3026,8 +3026,8 @@ struct MambaFrame {
 		return out;
 	}
 
-	/* __raygen__secondary (mamba_shader.cu:562-679) with the closest-hit
-	 * program (:719-777) */
+	/* __raygen__secondary (mamba_shader.cu:563-680) with the closest-hit
+	 * program (:707-777) */
 	void secondary()
 	{
 		uint64_t rays = 0, crays = 0;
@@ -3093,7 +3093,7 @@ struct MambaFrame {
 		closest_rays += crays;
 	}
 
-	/* secondary_gather (mamba.cu:436-616): the splats against the table as
+	/* secondary_gather (mamba.cu:401-576): the splats against the table as
 	 * it stood before the frame's splats, then added in splat order */
 	void gather()
 	{
@@ -3205,7 +3205,7 @@ struct MambaFrame {
 		return (int64_t)nearbyintf(sc);
 	}
 
-	/* sobel_normal (mamba.cu:169-200) */
+	/* sobel_normal (mamba.cu:169-201) */
 	void sobel()
 	{
 		int W = (int)m->width, H = (int)m->height;
@@ -3227,7 +3227,7 @@ struct MambaFrame {
 		}
 	}
 
-	/* raster_probes (mamba.cu:248-371) */
+	/* raster_probes (mamba.cu:244-369) */
 	void raster()
 	{
 		static const float wheel[12][3] = {{0.910f, 0.490f, 0.490f}, {0.910f, 0.700f, 0.490f},
@@ -3293,7 +3293,7 @@ struct MambaFrame {
 		}
 	}
 
-	/* probe_collapse (mamba.cu:851-906) */
+	/* probe_collapse (mamba.cu:889-938) */
 	void collapse()
 	{
 		uint32_t gw = (m->width + 15) / 16, gh = (m->height + 15) / 16;
@@ -3323,7 +3323,7 @@ struct MambaFrame {
 	}
 
 	/* probe_allocation (mamba_kernels.cu:5-182) with request_L2, the
-	 * second-level table's allocation and request_L1 (probe.cuh:531-657),
+	 * second-level table's allocation and request_L1 (probe.cuh:522-676),
 	 * one 16x16 block after another */
 	void allocate()
 	{
@@ -3440,7 +3440,7 @@ struct MambaFrame {
 		}
 	}
 
-	/* final_gather (mamba.cu:698-841) */
+	/* final_gather (mamba.cu:686-878) */
 	void final_gather(float *color)
 	{
 		const uint32_t width = m->width;

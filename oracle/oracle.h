@@ -155,7 +155,7 @@ typedef struct oracle_gi_state {
 void oracle_render_gi(const oracle_scene *s, const oracle_render_params *p, oracle_gi_state *st,
 		float *color, float *direct, oracle_render_stats *stats);
 
-/* The editor's Mamba frame (editor/mamba.cu:1094-1300), in the GPU build's
+/* The editor's Mamba frame (editor/mamba.cu:941-1312), in the GPU build's
  * deterministic form: a G-buffer traced at pixel centres, ReSTIR DI with 8
  * candidates (when direct_lighting), quarter-resolution secondary rays,
  * irradiance probes (splat, Sobel, raster, collapse, allocation in block

@@ -1,5 +1,5 @@
 """Parity of the "mamba" attachment -- the editor's default GI mode
-(Mamba::render, editor/mamba.cu:1094-1300; editor/optix/mamba_shader.cu;
+(Mamba::render, editor/mamba.cu:941-1312; editor/optix/mamba_shader.cu;
 editor/optix/probe.cuh; editor/mamba_kernels.cu) -- with the oracle's
 restatement (oracle_mamba_*, oracle/oracle.cpp).
 
@@ -178,7 +178,7 @@ def test_mamba_environment_matches_oracle():
 
 @pytest.mark.parametrize("view", ["indirect_lighting", "render_probes", "render_probe_radiance"])
 def test_mamba_debug_views_match_oracle(view):
-    """The other switches of Mamba::options (editor/mamba.cuh:61-67): the
+    """The other switches of Mamba::options (editor/mamba.cuh:60-67): the
     secondary radiance instead of the probes, and the probe indicator and
     probe radiance overlays of raster_probes."""
     out, colors = run("box4k", "fast", {"direct_lighting": True, view: True}, frames=4)
@@ -223,4 +223,48 @@ def test_mamba_stage_times_and_launches():
     # secondary 1, splat 2, Sobel + raster + collapse + allocation 5, final gather 1
     assert att.stats().kernel_launches == 23
     att.close()
+    sc.close()
+
+
+def test_mamba_reset_history_restarts_the_state():
+    """reset_history clears the reservoirs, the direct light, the secondary
+    records and the probe table: three frames after a reset equal three
+    frames of a fresh attachment, buffers included."""
+    g, sc, _ = helpers.both("box4k", 1)
+    cam = kgr.camera(g.eye, g.target, g.fov, W / H)
+
+    def frames(att, bufs, n):
+        for f in range(n):
+            info = helpers.launch(cam, W, H, bufs, samples=f)
+            info.time = 0.25 * f
+            att.render(info, sc)
+        torch.cuda.synchronize()
+        return bufs[0].cpu().numpy()
+
+    def make():
+        att = kgr.Attachment("mamba")
+        att.attach(W, H)
+        for k, v in {**DIRECT, "max_probes": MAX_PROBES, "max_luts": MAX_LUTS}.items():
+            att.set_option(k, v)
+        att.load()
+        return att
+
+    a, b = make(), make()
+    ba, bb = helpers.device_buffers(torch, W * H), helpers.device_buffers(torch, W * H)
+    frames(a, ba, 3)
+    a.set_option("reset_history", True)
+    ca = frames(a, ba, 3)
+    cb = frames(b, bb, 3)
+    assert same(ca, cb)
+    for name in ("bin_le", "bin_n", "refs", "probe_pos", "res_r3", "prev_r3", "direct_le", "s_le", "raster"):
+        dt, w = pyoracle.MAMBA_BUFFERS[name]
+        n = pyoracle.Mamba(W, H, MAX_PROBES, MAX_LUTS)
+        ref = n.buffer(name)
+        n.close()
+        xa, xb = np.zeros_like(ref), np.zeros_like(ref)
+        a.debug_copy("mamba_" + name, xa)
+        b.debug_copy("mamba_" + name, xb)
+        assert same(xa, xb), name
+    a.close()
+    b.close()
     sc.close()

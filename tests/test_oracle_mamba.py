@@ -1,13 +1,13 @@
 """The oracle's Mamba probe table (oracle_mamba_*) against an independent
 NumPy reading of editor/optix/probe.cuh, on the CPU.
 
-- hash (probe.cuh:138-158): cell coordinates in 11 bits each, shuffled with
+- hash (probe.cuh:168-187): cell coordinates in 11 bits each, shuffled with
   an arithmetic right shift of a signed value, then two masked left
   shifts -- restated here with Python integers;
-- the top table (request_L2 / lookup_L2, probe.cuh:589-695) probes
+- the top table (request_L2 / lookup_L2, probe.cuh:560-712) probes
   linearly: every occupied slot's cell hashes to a slot at or before it,
   with no empty slot between;
-- a second-level table (request_L1, probe.cuh:531-567) tries the hash's
+- a second-level table (request_L1, probe.cuh:522-558) tries the hash's
   slot and the next: each probe sits in one of its two slots, under the
   hash of its own position, inside its table's 10-unit cell;
 - probes are allocated one 16x16 block at a time in block order;

@@ -21,7 +21,8 @@ struct MlpParams {
 	float *partial;     /* per-block gradient slices [partial_blocks][6][64][64] */
 	int partial_blocks;
 	int infer;          /* KGR_MLP_INFER_MMA or KGR_MLP_INFER_TCGEN05 */
-	uint32_t *tc_err;   /* error word of the tcgen05 inference (bit 0: a wait ran out) */
+	uint32_t *tc_err;   /* error word of the tcgen05 kernels (bit 0: a wait ran out) */
+	int train;          /* KGR_MLP_TRAIN_MMA or KGR_MLP_TRAIN_TCGEN05 */
 };
 
 /* out[i] = {r, g, b, 0} for the n rows of x ([n][64] half precision); with
@@ -34,6 +35,11 @@ void mlp_infer(const MlpParams &mp, const void *x, uint32_t n, float4 *out, cuda
  * issued, so its wait runs out; no output row is written). */
 void mlp_infer_tc(const MlpParams &mp, const void *x, uint32_t n, float4 *out, uint32_t *err, cudaStream_t st,
 		const uint32_t *n_dev = nullptr, bool withhold_first = false);
+/* The gradient pass of mlp_gradients on the tensor cores (mlp_tc.cu):
+ * grid blocks write their slices of mp.partial (tiles of 128 rows) and add
+ * their loss into *loss; sets bit 0 of *mp.tc_err if a wait ran out. */
+void mlp_train_tc(const MlpParams &mp, const void *x, const float4 *target, uint32_t n, int grid, float *loss,
+		cudaStream_t st, const uint32_t *n_dev);
 /* grad (FP32, [6][64][64]) = d loss / d W over n rows; loss = sum of the
  * relative L2 terms (not divided by n).  Uses mp.partial as scratch; the
  * result does not depend on block scheduling.  max_blocks > 0 caps the grid
@@ -55,13 +61,14 @@ struct kgr_mlp {
 	int step = 0;
 	int partial_blocks = 0;
 	int infer = KGR_MLP_INFER_TCGEN05;
+	int train = KGR_MLP_TRAIN_TCGEN05;
 	kgr::DevBuf<float> master, m, v, grad, loss, partial;
 	kgr::DevBuf<uint16_t> wn, wt;
 	kgr::DevBuf<uint32_t> tc_err;
 	kgr::MlpParams params()
 	{
 		return kgr::MlpParams{dtype, master.ptr, m.ptr, v.ptr, wn.ptr, wt.ptr, partial.ptr, partial_blocks, infer,
-			tc_err.ptr};
+			tc_err.ptr, train};
 	}
 };
 

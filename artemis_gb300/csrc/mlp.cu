@@ -564,11 +564,14 @@ void mlp_gradients(const MlpParams &mp, const void *x, const float4 *target, uin
 	int grid = mp.partial_blocks;
 	if (max_blocks > 0 && max_blocks < grid)
 		grid = max_blocks;
-	long long tiles = ((long long)n + TRAIN_ROWS - 1) / TRAIN_ROWS;
+	const long long rows_per_tile = mp.train == KGR_MLP_TRAIN_TCGEN05 ? 128 : TRAIN_ROWS;
+	long long tiles = ((long long)n + rows_per_tile - 1) / rows_per_tile;
 	if (tiles < grid)
 		grid = (int)tiles;
 	KGR_REQUIRE(grid >= 1 && mp.partial, KGR_ERR_INTERNAL, "MLP gradient scratch missing");
-	if (mp.dtype == KGR_MLP_BF16) {
+	if (mp.train == KGR_MLP_TRAIN_TCGEN05) {
+		mlp_train_tc(mp, x, target, n, grid, loss, st, n_dev);
+	} else if (mp.dtype == KGR_MLP_BF16) {
 		static bool once = (set_smem(mlp_train_kernel<__nv_bfloat16>, sm), true);
 		(void)once;
 		mlp_train_kernel<__nv_bfloat16><<<grid, 128, sm, st>>>(static_cast<const __nv_bfloat16 *>(mp.wt),

@@ -166,6 +166,16 @@ kgr_status kgr_mlp_set_inference(kgr_mlp *m, int32_t kernel)
 	});
 }
 
+kgr_status kgr_mlp_set_training(kgr_mlp *m, int32_t kernel)
+{
+	return guard([&] {
+		KGR_REQUIRE(m, KGR_ERR_INVALID_ARGUMENT, "NULL network");
+		KGR_REQUIRE(kernel == KGR_MLP_TRAIN_MMA || kernel == KGR_MLP_TRAIN_TCGEN05, KGR_ERR_INVALID_ARGUMENT,
+			"unknown training kernel");
+		m->train = kernel;
+	});
+}
+
 kgr_status kgr_mlp_test_wait_timeout(kgr_mlp *m, const void *x, uint32_t n, float *out, void *stream)
 {
 	return guard([&] {

@@ -335,6 +335,344 @@ __global__ void __launch_bounds__(128) mlp_infer_tc_kernel(const T *__restrict__
 			: "memory");
 }
 
+/* ------------------------------------------------------------ training -- */
+
+/* Training (forward, loss, backward) on the fifth-generation tensor cores.
+ * One CTA of 128 threads per SM (225 KB of shared memory, 512 TMEM
+ * columns) walks tiles of 128 rows; every operand sits in shared memory in
+ * the canonical K-major layout without swizzle (8 x 8 core matrices of 128
+ * contiguous bytes, K neighbours 128 bytes apart, 8-row groups K/8 x 128
+ * bytes apart):
+ *   WT   the six layers' weights as [out][in] (forward B operands, 42 KB)
+ *   WN   layers 1..5 as [in][out] (the delta's B operands, 34 KB)
+ *   X    the tile's input of the current layer [128][64] (forward A operand)
+ *   AT   every layer's input transposed, [64][128] (A operands of dW)
+ *   D    the delta of the current layer's output [128][cols] (A operand)
+ *   DT   the same transposed, [cols][128] (B operand of dW)
+ * Per tile: six forward MMAs (M = 128) whose epilogue applies ReLU, rounds
+ * to half precision and writes X and AT; the loss and the output delta;
+ * then for each layer from the last, dW += AT^T-shaped MMA (M = 64: the
+ * layer's 64 inputs, N = its outputs, K = the 128 rows), accumulated in
+ * TMEM over every tile of the block, and the delta of the layer input
+ * (M = 128, N = 64, K = outputs) masked by ReLU'.  With M = 64 the
+ * accumulator's rows 16q..16q+15 are TMEM lanes 32q..32q+15.  At the end
+ * the block writes its dW to its slice of `partial`, which the host sums in
+ * block order; the rounding points are those of mlp_train_kernel. */
+#define TT_ROWS 128
+#define TT_SBO16 256u
+#define TT_SBO64 1024u
+#define TT_SBO128 2048u
+#define TT_WN_OFF TC_W_BYTES                      /* 43,008 */
+#define TT_WN_BYTES (4u * TC_LAYER_BYTES + 2048u) /* layers 1..4, then layer 5 (K = 16) */
+#define TT_X_OFF (TT_WN_OFF + TT_WN_BYTES)        /* 77,824 */
+#define TT_TILE_BYTES (TT_ROWS * TC_W * 2u)       /* 16 KB */
+#define TT_AT_OFF (TT_X_OFF + TT_TILE_BYTES)
+#define TT_D_OFF (TT_AT_OFF + 6u * TT_TILE_BYTES)
+#define TT_DT_OFF (TT_D_OFF + TT_TILE_BYTES)
+#define TT_BAR_OFF (TT_DT_OFF + TT_TILE_BYTES)    /* 225,280 */
+#define TT_SLOT_OFF (TT_BAR_OFF + 8u)
+#define TT_SMEM (TT_SLOT_OFF + 8u)
+#define TT_TMEM_COLS 512u
+#define TT_DW_COL(l) (64u + 64u * (uint32_t)(l))   /* dW of layer l (layer 5: 16 columns) */
+
+__device__ __forceinline__ uint32_t kmaj_off(uint32_t r, uint32_t k, uint32_t sbo)
+{
+	return (r >> 3) * sbo + (k >> 3) * 128u + (r & 7u) * 16u + (k & 7u) * 2u;
+}
+
+__device__ __forceinline__ uint32_t wn_off(int l)
+{
+	return TT_WN_OFF + (l < TC_LAYERS - 1 ? (uint32_t)(l - 1) * TC_LAYER_BYTES : 4u * TC_LAYER_BYTES);
+}
+
+template <class T>
+__device__ __forceinline__ T half_bits(uint16_t b)
+{
+	T h;
+	*reinterpret_cast<uint16_t *>(&h) = b;
+	return h;
+}
+
+template <class T>
+__device__ __forceinline__ uint16_t bits_of(T h)
+{
+	return *reinterpret_cast<uint16_t *>(&h);
+}
+
+template <class T>
+__device__ __forceinline__ float half_to_float(T h);
+template <>
+__device__ __forceinline__ float half_to_float<__nv_bfloat16>(__nv_bfloat16 h) { return __bfloat162float(h); }
+template <>
+__device__ __forceinline__ float half_to_float<__half>(__half h) { return __half2float(h); }
+
+template <class T>
+__device__ __forceinline__ T float_to_half(float f);
+template <>
+__device__ __forceinline__ __nv_bfloat16 float_to_half<__nv_bfloat16>(float f) { return __float2bfloat16_rn(f); }
+template <>
+__device__ __forceinline__ __half float_to_half<__half>(float f) { return __float2half_rn(f); }
+
+/* A row of 8 halves (one 16-byte chunk) from 8 values. */
+template <class T>
+__device__ __forceinline__ uint4 pack8(const uint16_t (&h)[8])
+{
+	uint4 p;
+	p.x = (uint32_t)h[0] | ((uint32_t)h[1] << 16);
+	p.y = (uint32_t)h[2] | ((uint32_t)h[3] << 16);
+	p.z = (uint32_t)h[4] | ((uint32_t)h[5] << 16);
+	p.w = (uint32_t)h[6] | ((uint32_t)h[7] << 16);
+	return p;
+}
+
+template <class T>
+__global__ void __launch_bounds__(128, 1) mlp_train_tc_kernel(const T *__restrict__ wt_g, const T *__restrict__ wn_g,
+		const T *__restrict__ x, const float4 *__restrict__ target, uint32_t n, float *__restrict__ partial,
+		float *__restrict__ loss_sum, const uint32_t *__restrict__ n_dev, uint32_t *__restrict__ err)
+{
+	if (n_dev) {
+		uint32_t c = *n_dev;
+		n = c < n ? c : n;
+	}
+	extern __shared__ __align__(1024) unsigned char sm[];
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	const bool bf16 = std::is_same<T, __nv_bfloat16>::value;
+	const uint32_t bar = smem_addr(sm + TT_BAR_OFF);
+	uint32_t *slot = reinterpret_cast<uint32_t *>(sm + TT_SLOT_OFF);
+	const uint32_t tiles = (n + TT_ROWS - 1) / TT_ROWS;
+
+	/* weights: forward [out][in], then layers 1..5 as [in][out] */
+	for (int l = 0; l < TC_LAYERS; l++) {
+		int rows = l == TC_LAYERS - 1 ? TC_OUT : TC_W;
+		const uint4 *src = reinterpret_cast<const uint4 *>(wt_g + (size_t)l * TC_W * TC_W);
+		unsigned char *dst = sm + l * TC_LAYER_BYTES;
+		for (int c = tid; c < rows * 8; c += 128) {
+			uint32_t r = (uint32_t)c >> 3, kb = (uint32_t)c & 7u;
+			*reinterpret_cast<uint4 *>(dst + kmaj_off(r, kb * 8u, TT_SBO64)) = __ldg(src + c);
+		}
+	}
+	for (int l = 1; l < TC_LAYERS; l++) {
+		uint32_t cols = l == TC_LAYERS - 1 ? TC_OUT : TC_W, chunks = cols / 8u, sbo = chunks * 128u;
+		const uint4 *src = reinterpret_cast<const uint4 *>(wn_g + (size_t)l * TC_W * TC_W);
+		unsigned char *dst = sm + wn_off(l);
+		for (uint32_t c = (uint32_t)tid; c < TC_W * chunks; c += 128u) {
+			uint32_t r = c / chunks, kb = c % chunks;
+			*reinterpret_cast<uint4 *>(dst + kmaj_off(r, kb * 8u, sbo)) = __ldg(src + c);
+		}
+	}
+	if (tid == 0) {
+		asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(bar), "r"(1u) : "memory");
+		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+	}
+	if (warp == 0) {
+		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+			:: "r"(smem_addr(slot)), "r"(TT_TMEM_COLS) : "memory");
+		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+	}
+	fence_async_smem();
+	tc_before();
+	__syncthreads();
+	tc_after();
+	const uint32_t tmem = *slot;
+	const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+	const uint32_t base = smem_addr(sm);
+	const uint32_t id_hidden = instr_desc(bf16, TC_W, TT_ROWS), id_out = instr_desc(bf16, TC_OUT, TT_ROWS);
+	const uint32_t id_dw = instr_desc(bf16, TC_W, 64), id_dw_out = instr_desc(bf16, TC_OUT, 64);
+	const uint32_t r = (uint32_t)tid; /* this thread's row of the tile, and its TMEM lane */
+	unsigned char *xs = sm + TT_X_OFF, *ds = sm + TT_D_OFF, *dts = sm + TT_DT_OFF;
+	uint32_t parity = 0;
+	bool ok = true, first = true;
+	float lsum = 0.0f;
+
+	/* wait for the committed MMAs, then make the epilogue's view current */
+	auto mma_wait = [&]() -> bool {
+		bool got = bar_wait(bar, parity, TC_WAIT_LIMIT);
+		parity ^= 1u;
+		bool all = __syncthreads_and(got) != 0;
+		tc_after();
+		return all;
+	};
+	/* make this thread's shared-memory writes visible to the MMAs */
+	auto publish = [&]() {
+		fence_async_smem();
+		tc_before();
+		__syncthreads();
+		tc_after();
+	};
+
+	for (uint32_t t = blockIdx.x; ok && t < tiles; t += gridDim.x) {
+		const size_t gr = (size_t)t * TT_ROWS + r;
+		/* ---- the tile's input: X (row r) and AT[0] (column r) ---- */
+		{
+			uint4 c[8];
+			const uint4 *src = reinterpret_cast<const uint4 *>(x + gr * TC_W);
+#pragma unroll
+			for (int kb = 0; kb < 8; kb++)
+				c[kb] = gr < n ? __ldg(src + kb) : make_uint4(0u, 0u, 0u, 0u);
+			unsigned char *at = sm + TT_AT_OFF;
+#pragma unroll
+			for (int kb = 0; kb < 8; kb++) {
+				*reinterpret_cast<uint4 *>(xs + kmaj_off(r, kb * 8u, TT_SBO64)) = c[kb];
+				const uint32_t w4[4] = {c[kb].x, c[kb].y, c[kb].z, c[kb].w};
+#pragma unroll
+				for (int e = 0; e < 8; e++) {
+					uint16_t h = (uint16_t)(w4[e >> 1] >> (16 * (e & 1)));
+					*reinterpret_cast<uint16_t *>(at + kmaj_off((uint32_t)(kb * 8 + e), r, TT_SBO128)) = h;
+				}
+			}
+		}
+		publish();
+		/* ---- forward ---- */
+		for (int l = 0; l < TC_LAYERS && ok; l++) {
+			const bool last = l == TC_LAYERS - 1;
+			if (tid == 0) {
+				for (uint32_t kc = 0; kc < 4; kc++)
+					tc_mma(tmem, smem_desc(base + TT_X_OFF + kc * 256u, TC_LBO, TT_SBO64, 0u),
+						smem_desc(base + l * TC_LAYER_BYTES + kc * 256u, TC_LBO, TT_SBO64, 0u),
+						last ? id_out : id_hidden, kc > 0 ? 1u : 0u);
+				tc_commit(bar);
+			}
+			ok = mma_wait();
+			if (!ok)
+				break;
+			if (!last) {
+				uint32_t v[64];
+				tmem_ld64(lane_addr, v);
+				tmem_wait_ld();
+				unsigned char *at = sm + TT_AT_OFF + (uint32_t)(l + 1) * TT_TILE_BYTES;
+#pragma unroll
+				for (uint32_t kb = 0; kb < 8; kb++) {
+					uint16_t h[8];
+#pragma unroll
+					for (int e = 0; e < 8; e++) {
+						h[e] = bits_of<T>(float_to_half<T>(fmaxf(__uint_as_float(v[8 * kb + e]), 0.0f)));
+						*reinterpret_cast<uint16_t *>(at + kmaj_off(8u * kb + (uint32_t)e, r, TT_SBO128)) = h[e];
+					}
+					*reinterpret_cast<uint4 *>(xs + kmaj_off(r, kb * 8u, TT_SBO64)) = pack8<T>(h);
+				}
+			} else {
+				/* the loss and the output delta (columns 0..15, 0..2 non-zero) */
+				uint32_t v[16];
+				tmem_ld16(lane_addr, v);
+				tmem_wait_ld();
+				float4 tg = gr < n ? target[gr] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+				const float tv[3] = {tg.x, tg.y, tg.z};
+				uint16_t h[16];
+#pragma unroll
+				for (int col = 0; col < 16; col++) {
+					float d = 0.0f;
+					if (col < 3 && gr < n) {
+						float y = __uint_as_float(v[col]);
+						float diff = y - tv[col];
+						float den = y * y + 0.01f;
+						lsum += diff * diff / den;
+						d = 2.0f * diff / den / (float)n;
+					}
+					h[col] = bits_of<T>(float_to_half<T>(d));
+					*reinterpret_cast<uint16_t *>(dts + kmaj_off((uint32_t)col, r, TT_SBO128)) = h[col];
+				}
+				uint16_t lo[8], hi[8];
+#pragma unroll
+				for (int e = 0; e < 8; e++) {
+					lo[e] = h[e];
+					hi[e] = h[8 + e];
+				}
+				*reinterpret_cast<uint4 *>(ds + kmaj_off(r, 0u, TT_SBO16)) = pack8<T>(lo);
+				*reinterpret_cast<uint4 *>(ds + kmaj_off(r, 8u, TT_SBO16)) = pack8<T>(hi);
+			}
+			publish();
+		}
+		/* ---- backward ---- */
+		for (int l = TC_LAYERS - 1; l >= 0 && ok; l--) {
+			const uint32_t cols = l == TC_LAYERS - 1 ? TC_OUT : TC_W;
+			const uint32_t sbo_d = cols / 8u * 128u;
+			if (tid == 0) {
+				/* dW[l] (+)= AT[l] x DT: M = 64 inputs, N = cols outputs, K = 128 rows */
+				for (uint32_t kc = 0; kc < 8; kc++)
+					tc_mma(tmem + TT_DW_COL(l),
+						smem_desc(base + TT_AT_OFF + (uint32_t)l * TT_TILE_BYTES + kc * 256u, TC_LBO, TT_SBO128, 0u),
+						smem_desc(base + TT_DT_OFF + kc * 256u, TC_LBO, TT_SBO128, 0u),
+						l == TC_LAYERS - 1 ? id_dw_out : id_dw, (!first || kc > 0) ? 1u : 0u);
+				/* the delta of the layer input: D x WN[l], M = 128, N = 64, K = cols */
+				if (l > 0)
+					for (uint32_t kc = 0; kc < cols / 16u; kc++)
+						tc_mma(tmem, smem_desc(base + TT_D_OFF + kc * 256u, TC_LBO, sbo_d, 0u),
+							smem_desc(base + wn_off(l) + kc * 256u, TC_LBO, sbo_d, 0u), id_hidden,
+							kc > 0 ? 1u : 0u);
+				tc_commit(bar);
+			}
+			ok = mma_wait();
+			if (!ok || l == 0)
+				break;
+			uint32_t v[64];
+			tmem_ld64(lane_addr, v);
+			tmem_wait_ld();
+			const unsigned char *at = sm + TT_AT_OFF + (uint32_t)l * TT_TILE_BYTES;
+#pragma unroll
+			for (uint32_t kb = 0; kb < 8; kb++) {
+				uint16_t h[8];
+#pragma unroll
+				for (int e = 0; e < 8; e++) {
+					uint32_t i = 8u * kb + (uint32_t)e;
+					float av = half_to_float<T>(half_bits<T>(*reinterpret_cast<const uint16_t *>(
+						at + kmaj_off(i, r, TT_SBO128))));
+					float d = av > 0.0f ? __uint_as_float(v[i]) : 0.0f;
+					h[e] = bits_of<T>(float_to_half<T>(d));
+					*reinterpret_cast<uint16_t *>(dts + kmaj_off(i, r, TT_SBO128)) = h[e];
+				}
+				*reinterpret_cast<uint4 *>(ds + kmaj_off(r, kb * 8u, TT_SBO64)) = pack8<T>(h);
+			}
+			publish();
+		}
+		first = false;
+	}
+	if (!ok && tid == 0)
+		atomicOr(err, 1u);
+	tc_before();
+	__syncthreads();
+	tc_after();
+	/* this block's dW: lanes 32w..32w+15 hold rows 16w..16w+15 */
+	float *dst = partial + (size_t)blockIdx.x * TC_LAYERS * TC_W * TC_W;
+	for (int l = 0; l < TC_LAYERS; l++) {
+		const uint32_t cols = l == TC_LAYERS - 1 ? TC_OUT : TC_W;
+		const uint32_t i = 16u * (uint32_t)warp + (uint32_t)lane;
+		uint32_t v[64];
+		if (cols == TC_W) {
+			tmem_ld64(lane_addr + TT_DW_COL(l), v);
+		} else {
+			uint32_t w16[16];
+			tmem_ld16(lane_addr + TT_DW_COL(l), w16);
+#pragma unroll
+			for (int j = 0; j < 16; j++)
+				v[j] = w16[j];
+#pragma unroll
+			for (int j = 16; j < 64; j++)
+				v[j] = 0u;
+		}
+		tmem_wait_ld();
+		if (lane < 16) {
+			float *row = dst + (size_t)l * TC_W * TC_W + (size_t)i * TC_W;
+			const bool valid = ok && !first;
+#pragma unroll
+			for (int j = 0; j < 64; j += 4)
+				*reinterpret_cast<float4 *>(row + j) = valid
+					? make_float4(__uint_as_float(v[j]), __uint_as_float(v[j + 1]), __uint_as_float(v[j + 2]),
+						__uint_as_float(v[j + 3]))
+					: make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+		}
+	}
+	for (int off = 16; off > 0; off >>= 1)
+		lsum += __shfl_down_sync(0xffffffffu, lsum, off);
+	if (lane == 0)
+		atomicAdd(loss_sum, lsum);
+	tc_before();
+	__syncthreads();
+	tc_after();
+	if (warp == 0)
+		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(TT_TMEM_COLS)
+			: "memory");
+}
+
 template <class K>
 void set_tc_smem(K kernel)
 {
@@ -363,7 +701,33 @@ EncodeTiledFn encode_tiled()
 	return fn;
 }
 
+template <class K>
+void set_train_smem(K kernel)
+{
+	KGR_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TT_SMEM));
+}
+
 } /* namespace */
+
+void mlp_train_tc(const MlpParams &mp, const void *x, const float4 *target, uint32_t n, int grid, float *loss,
+		cudaStream_t st, const uint32_t *n_dev)
+{
+	KGR_REQUIRE(((uintptr_t)x & 15u) == 0, KGR_ERR_INVALID_ARGUMENT, "inputs must be 16-byte aligned");
+	if (mp.dtype == KGR_MLP_BF16) {
+		static bool once = (set_train_smem(mlp_train_tc_kernel<__nv_bfloat16>), true);
+		(void)once;
+		mlp_train_tc_kernel<__nv_bfloat16><<<grid, 128, TT_SMEM, st>>>(static_cast<const __nv_bfloat16 *>(mp.wt),
+			static_cast<const __nv_bfloat16 *>(mp.wn), static_cast<const __nv_bfloat16 *>(x), target, n, mp.partial,
+			loss, n_dev, mp.tc_err);
+	} else {
+		static bool once = (set_train_smem(mlp_train_tc_kernel<__half>), true);
+		(void)once;
+		mlp_train_tc_kernel<__half><<<grid, 128, TT_SMEM, st>>>(static_cast<const __half *>(mp.wt),
+			static_cast<const __half *>(mp.wn), static_cast<const __half *>(x), target, n, mp.partial, loss, n_dev,
+			mp.tc_err);
+	}
+	KGR_CUDA(cudaGetLastError());
+}
 
 void mlp_infer_tc(const MlpParams &mp, const void *x, uint32_t n, float4 *out, uint32_t *err, cudaStream_t st,
 		const uint32_t *n_dev, bool withhold_first)

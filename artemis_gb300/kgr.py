@@ -165,6 +165,7 @@ def lib():
             "kgr_mlp_train_step": (c_i32, [vp, vp, vp, c_u32, c_f, vp]),
             "kgr_mlp_destroy": (c_i32, [vp]),
             "kgr_mlp_set_inference": (c_i32, [vp, c_i32]),
+            "kgr_mlp_set_training": (c_i32, [vp, c_i32]),
             "kgr_tonemap": (c_i32, [vp, vp, c_u32, c_u32, c_i32, vp]),
             "kgr_denoiser_create": (c_i32, [c_u32, c_u32, c_i32, c_i32, vp]),
             "kgr_denoise": (c_i32, [vp, vp, vp, vp]),
@@ -567,8 +568,12 @@ class Mlp:
         """"mma" (warp-level mma.sync) or "tcgen05" (tensor memory accumulators)."""
         check(lib().kgr_mlp_set_inference(self.handle, {"mma": 0, "tcgen05": 1}[kernel]))
 
+    def set_training(self, kernel):
+        """Gradient kernel: "mma" (warp-level mma.sync) or "tcgen05" (tensor memory accumulators)."""
+        check(lib().kgr_mlp_set_training(self.handle, {"mma": 0, "tcgen05": 1}[kernel]))
+
     def check(self):
-        """Raise if a tcgen05 inference gave up on an mbarrier wait."""
+        """Raise if a tcgen05 kernel gave up on an mbarrier wait."""
         check(lib().kgr_mlp_check(self.handle))
 
     def test_wait_timeout(self, x_ptr, n, out_ptr, stream=None):

@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define KGR_ABI_VERSION 4
+#define KGR_ABI_VERSION 5
 
 typedef enum kgr_status {
 	KGR_OK = 0,
@@ -534,6 +534,16 @@ kgr_status kgr_mlp_destroy(kgr_mlp *mlp);
  * reference, whose only network is an unused FP32 forward pass. */
 enum { KGR_MLP_INFER_MMA = 0, KGR_MLP_INFER_TCGEN05 = 1 };
 kgr_status kgr_mlp_set_inference(kgr_mlp *mlp, int32_t kernel);
+/* Gradient kernel of kgr_mlp_gradients, kgr_mlp_train_step and the
+ * radiance cache's training: KGR_MLP_TRAIN_TCGEN05 (the default:
+ * tcgen05.mma on 128-row tiles, forward and the input deltas at M = 128,
+ * the weight gradient at M = 64 accumulated in tensor memory over a block's
+ * tiles) or KGR_MLP_TRAIN_MMA (warp-level mma.sync, 64-row tiles, the
+ * weight gradient summed in shared memory).  Same network and rounding points;
+ * the gradients differ only in FP32 summation order.  A tcgen05 wait that
+ * runs out is reported by kgr_mlp_check. */
+enum { KGR_MLP_TRAIN_MMA = 0, KGR_MLP_TRAIN_TCGEN05 = 1 };
+kgr_status kgr_mlp_set_training(kgr_mlp *mlp, int32_t kernel);
 /* Synchronise the device and report a tcgen05 inference whose mbarrier wait
  * ran out (KGR_ERR_CUDA; the flag is then cleared).  KGR_OK otherwise. */
 kgr_status kgr_mlp_check(kgr_mlp *mlp);

@@ -26,7 +26,7 @@ def test_library_exports_every_declared_symbol():
     assert len(names) >= 45
     missing = [n for n in names if not hasattr(L, n)]
     assert not missing, missing
-    assert L.kgr_abi_version() == 4
+    assert L.kgr_abi_version() == 5
 
 
 def test_status_strings():

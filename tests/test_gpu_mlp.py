@@ -41,6 +41,7 @@ def test_forward_matches_oracle(dtype, tol):
 @pytest.mark.parametrize("dtype", ["bf16", "fp16"])
 def test_gradients_match_oracle(dtype):
     net = kgr.Mlp(dtype, seed=5)
+    net.set_training("mma")  # the tcgen05 kernel is tested in test_gpu_mlp_tc.py
     W = net.weights()
     rng = np.random.default_rng(1)
     n = 4096 + 77
@@ -62,6 +63,7 @@ def test_gradients_match_oracle(dtype):
 
 def test_training_lowers_loss():
     net = kgr.Mlp("bf16", seed=7)
+    net.set_training("mma")
     rng = np.random.default_rng(2)
     n = 1 << 14
     x = mlp_ref.encode_inputs(rng, n, "bf16")

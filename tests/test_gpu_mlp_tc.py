@@ -90,3 +90,81 @@ def test_tcgen05_wait_timeout_is_reported_and_the_network_recovers():
     net.check()
     ref, _ = mlp_ref.forward(W, x, "bf16")
     assert np.abs(out.cpu().numpy()[:, :3] - ref).max() <= 2e-2 * np.abs(ref).max() + 1e-6
+
+
+def gradients(net, kernel, xd, td, n):
+    net.set_training(kernel)
+    loss, g = net.gradients(xd.data_ptr(), td.data_ptr(), n)
+    net.check()
+    return loss, g
+
+
+@pytest.mark.parametrize("dtype", ["bf16", "fp16"])
+def test_tcgen05_gradients_match_oracle_and_mma(dtype):
+    """Training on tcgen05 (forward and input deltas at M = 128, weight
+    gradients at M = 64 accumulated in tensor memory) against the NumPy
+    oracle -- within 5e-2 of each layer's gradient norm, the tolerance of the
+    mma.sync kernel's test -- and against the mma.sync kernel within 1e-2
+    (same rounding points, different FP32 summation order).  Row counts:
+    ragged, whole 128-row tiles, less than one tile."""
+    net = kgr.Mlp(dtype, seed=5)
+    W = net.weights()
+    rng = np.random.default_rng(1)
+    for n in (4096 + 77, 2 * 128, 51):
+        x = mlp_ref.encode_inputs(rng, n, dtype)
+        t = np.zeros((n, 4), np.float32)
+        t[:, :3] = rng.uniform(0, 2, (n, 3))
+        xd, td = half_tensor(x, dtype), torch.from_numpy(t).cuda()
+        loss_tc, g_tc = gradients(net, "tcgen05", xd, td, n)
+        loss_mma, g_mma = gradients(net, "mma", xd, td, n)
+        rl, rg = mlp_ref.loss_and_grad(W, x, t, dtype)
+        assert abs(loss_tc - rl) <= 2e-2 * abs(rl)
+        assert abs(loss_tc - loss_mma) <= 1e-3 * abs(loss_mma)
+        for l in range(6):
+            cols = 3 if l == 5 else 64
+            a, b, c = g_tc[l][:, :cols], rg[l][:, :cols], g_mma[l][:, :cols]
+            print(f"{dtype} n={n} layer {l}: |tc - oracle| / |oracle| = "
+                  f"{np.linalg.norm(a - b) / (np.linalg.norm(b) + 1e-30):.2e}, "
+                  f"|tc - mma| / |mma| = {np.linalg.norm(a - c) / (np.linalg.norm(c) + 1e-30):.2e}")
+            assert np.linalg.norm(a - b) <= 5e-2 * np.linalg.norm(b) + 1e-9, l
+            assert np.linalg.norm(a - c) <= 1e-2 * np.linalg.norm(c) + 1e-9, l
+        assert np.all(g_tc[5][:, 3:] == 0)
+
+
+def test_tcgen05_training_lowers_loss_and_times_both_kernels():
+    """300 Adam steps with the tcgen05 gradients lower the loss as the
+    mma.sync ones do; the gradient pass of each kernel over 2^16 rows is
+    timed (CUDA events, 20 passes after 3)."""
+    n = 1 << 16
+    rng = np.random.default_rng(2)
+    x = mlp_ref.encode_inputs(rng, n, "bf16")
+    t = np.zeros((n, 4), np.float32)
+    t[:, 0] = 0.5 + 0.4 * np.sin(3 * x[:, 0])
+    t[:, 1] = 0.5 + 0.4 * x[:, 1] * x[:, 2]
+    t[:, 2] = np.abs(x[:, 3])
+    xd, td = half_tensor(x, "bf16"), torch.from_numpy(t).cuda()
+    net = kgr.Mlp("bf16", seed=7)
+    net.set_training("tcgen05")
+    first, _ = net.gradients(xd.data_ptr(), td.data_ptr(), n)
+    for _ in range(300):
+        net.train_step(xd.data_ptr(), td.data_ptr(), n, lr=1e-3)
+    last, _ = net.gradients(xd.data_ptr(), td.data_ptr(), n)
+    net.check()
+    print(f"tcgen05 training: relative L2 loss {first / n:.4f} -> {last / n:.4f}")
+    assert last < 0.2 * first
+    times = {}
+    for kernel in ("mma", "tcgen05"):
+        net.set_training(kernel)
+        for _ in range(3):
+            net.train_step(xd.data_ptr(), td.data_ptr(), n, lr=0.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(20):
+            net.train_step(xd.data_ptr(), td.data_ptr(), n, lr=0.0)
+        e1.record()
+        torch.cuda.synchronize()
+        times[kernel] = e0.elapsed_time(e1) / 20
+    net.check()
+    print(f"gradient pass + Adam over 2^16 rows: mma.sync {times['mma'] * 1e3:.1f} us, "
+          f"tcgen05 {times['tcgen05'] * 1e3:.1f} us")

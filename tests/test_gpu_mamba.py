@@ -268,3 +268,12 @@ def test_mamba_reset_history_restarts_the_state():
     a.close()
     b.close()
     sc.close()
+
+
+def test_mamba_full_tables_match_oracle():
+    """A table of 16 probes fills in the first frame: the later allocations
+    find no probe left (a second-level slot is then not claimed), and the
+    frames stay bit-exact with the oracle's."""
+    out, colors = run("box4k", "fast", DIRECT, frames=4, tables=(16, 2))
+    counters = check(out, colors, "box4k 16 probes")
+    assert counters[0] == 16 and counters[1] == 2

@@ -1,10 +1,14 @@
-"""Regenerate tests/golden/reference_kat.json from the reference's own headers.
+"""Regenerate tests/golden/reference_kat.json and reference_traversal.json
+from the reference's own headers and shaders.
 
 Builds oracle/_ref/ref_kat and oracle/_ref/ref_color_kat (oracle/Makefile,
 target `ref`), which compile include/cuda/random.cuh, include/cuda/math.cuh,
 include/cuda/brdf.cuh, include/cuda/color.cuh and include/optix/lighting.cuh
 of the reference checkout unmodified on the host, runs them and stores their
-JSON output.  Needs the reference checkout, named by --reference or the
+JSON output.  Builds oracle/_ref/ref_glsl, the traversal shaders
+(shaders/rt/modules/{ray,primitives,bbox,intersect,bvh}.glsl) compiled as
+C++, runs trace() on two procedural scenes with the oracle's BVHs and stores
+each ray's closest object and distance.  Needs the reference checkout, named by --reference or the
 REFERENCE environment variable; the committed JSON is what the tests read, so
 this script only runs when the vectors are regenerated.
 
@@ -37,6 +41,90 @@ def main():
     with open(os.path.join(HERE, "reference_kat.json"), "w") as f:
         json.dump(data, f, indent=0)
     print("wrote", os.path.join(HERE, "reference_kat.json"), file=sys.stderr)
+    traversal = {"scenes": [traversal_case(*c) for c in TRAVERSAL_CASES],
+                 "_generated_by": "tests/golden/gen_golden.py: trace() of the reference's "
+                                  "shaders/rt/modules/bvh.glsl (with bbox.glsl, intersect.glsl, ray.glsl, "
+                                  "primitives.glsl) compiled as C++ by oracle/ref_glsl.cpp"}
+    with open(os.path.join(HERE, "reference_traversal.json"), "w") as f:
+        json.dump(traversal, f, separators=(",", ":"))
+    print("wrote", os.path.join(HERE, "reference_traversal.json"), file=sys.stderr)
+
+
+# (scene, generator seed, builder, max leaf size, camera rays per side, random rays)
+TRAVERSAL_CASES = [("box4k", 1, "sah", 4, 24, 512), ("box64", 3, "kobra", 1, 24, 512),
+                   ("terrain_s", 1, "sah", 4, 24, 512)]
+
+
+def traversal_rays(g, side, n_random, seed):
+    """Camera rays through a side x side grid, seeded random rays between
+    random points and triangle centroids, and edge cases: directions with
+    zero components, axis-aligned rays, origins inside the scene box."""
+    import numpy as np
+    from artemis_gb300 import kgr
+    rays = []
+    cam = kgr.camera_dict(kgr.camera(g.eye, g.target, g.fov, 1.0))
+    U, V, W, C = (np.asarray(cam[k], np.float32) for k in ("ax_u", "ax_v", "ax_w", "center"))
+    for iy in range(side):
+        for ix in range(side):
+            u = np.float32(2.0 * (ix + 0.5) / side - 1.0)
+            v = np.float32(2.0 * (iy + 0.5) / side - 1.0)
+            d = u * U + v * V + W
+            d = d / np.float32(np.sqrt(np.float32(d @ d)))
+            rays.append(np.concatenate([C, d]))
+    rng = np.random.default_rng(seed)
+    lo, hi = g.positions.min(axis=0), g.positions.max(axis=0)
+    cent = g.positions[g.indices].mean(axis=1)
+    for _ in range(n_random):
+        o = rng.uniform(lo, hi).astype(np.float32)
+        t = cent[rng.integers(0, len(cent))]
+        d = (t - o).astype(np.float32)
+        d = d / np.float32(np.linalg.norm(d))
+        rays.append(np.concatenate([o, d]))
+    mid = ((lo + hi) * 0.5).astype(np.float32)
+    for axis in range(3):
+        for sign in (1.0, -1.0):
+            d = np.zeros(3, np.float32)
+            d[axis] = sign
+            rays.append(np.concatenate([mid, d]))
+            rays.append(np.concatenate([C, d]))
+    for d in ([1, 1, 0], [0, 1, 1], [1, 0, -1], [0.3, -1, 0], [0, 0, -1]):
+        d = np.asarray(d, np.float32)
+        d = d / np.float32(np.linalg.norm(d))
+        rays.append(np.concatenate([C, d]))
+        rays.append(np.concatenate([mid, d]))
+    return np.asarray(rays, np.float32)
+
+
+def traversal_case(name, seed, builder, max_leaf, side, n_random):
+    import hashlib
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    from oracle import pyoracle
+    g = pyoracle.GeneratedScene(name, seed)
+    bvh = build_bvh(g, builder, max_leaf)
+    rays = traversal_rays(g, side, n_random, seed)
+    tris = np.ascontiguousarray(g.tris4(), np.uint32)
+    blob = (np.asarray([len(g.positions), len(tris), len(bvh), len(rays)], np.uint32).tobytes()
+            + np.ascontiguousarray(g.positions, np.float32).tobytes() + tris.tobytes()
+            + np.ascontiguousarray(bvh, np.float32).tobytes() + rays.tobytes())
+    out = subprocess.run([os.path.join(ROOT, "oracle", "_ref", "ref_glsl")], input=blob, capture_output=True,
+                         check=True).stdout.decode().split("\n")
+    hits = [[int(o), int(t, 16)] for o, t in (line.split() for line in out if line.strip())]
+    assert len(hits) == len(rays)
+    return {"scene": name, "seed": seed, "builder": builder, "max_leaf": max_leaf,
+            "bvh_sha256": hashlib.sha256(np.ascontiguousarray(bvh, np.float32).tobytes()).hexdigest(),
+            "rays": rays.view(np.uint32).tolist(), "hits": hits}
+
+
+def build_bvh(g, builder, max_leaf):
+    """The oracle's BVH of a generated scene in the threaded layout: its SAH
+    builder, or its restatement of the reference's bvh.cpp builder."""
+    from oracle import pyoracle
+    if builder == "sah":
+        return g.sah_bvh(max_leaf)
+    osc = pyoracle.Scene(g.positions, g.normals, g.tris4(), g.materials_raw, g.lights(),
+                         __import__("numpy").zeros((0, 4), "float32"))
+    return pyoracle.build_kobra_bvh(osc.triangle_boxes())
 
 
 if __name__ == "__main__":

@@ -13,9 +13,12 @@
  * known-answer vectors produced by compiling the reference's own headers
  * (include/cuda/random.cuh, include/cuda/math.cuh, include/cuda/brdf.cuh,
  * include/optix/lighting.cuh) on the host (oracle/_ref, tests/golden/).  The
- * BVH builder, the GLSL traversal and the OptiX programs cannot be compiled
- * here (glm, OptiX runtime and Vulkan are absent), so those restatements are
- * unpinned beyond structural invariants.
+ * BVH builder is pinned against source/bvh.cpp compiled on the host with a
+ * glm stand-in (oracle/ref_bvh.cpp), and the threaded walk against the
+ * traversal shaders (shaders/rt/modules/bvh.glsl and the modules it uses)
+ * compiled as C++ (oracle/ref_glsl.cpp).  The OptiX programs cannot be
+ * compiled here (the OptiX runtime is absent); the kernels that restate them
+ * are pinned through the helpers above and the walk.
  */
 #ifndef KGR_ORACLE_H_
 #define KGR_ORACLE_H_

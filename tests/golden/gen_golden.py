@@ -1,5 +1,5 @@
-"""Regenerate tests/golden/reference_kat.json and reference_traversal.json
-from the reference's own headers and shaders.
+"""Regenerate tests/golden/reference_kat.json, reference_traversal.json and
+reference_bvh.json from the reference's own headers, shaders and builder.
 
 Builds oracle/_ref/ref_kat and oracle/_ref/ref_color_kat (oracle/Makefile,
 target `ref`), which compile include/cuda/random.cuh, include/cuda/math.cuh,
@@ -8,7 +8,10 @@ of the reference checkout unmodified on the host, runs them and stores their
 JSON output.  Builds oracle/_ref/ref_glsl, the traversal shaders
 (shaders/rt/modules/{ray,primitives,bbox,intersect,bvh}.glsl) compiled as
 C++, runs trace() on two procedural scenes with the oracle's BVHs and stores
-each ray's closest object and distance.  Needs the reference checkout, named by --reference or the
+each ray's closest object and distance.  Builds oracle/_ref/ref_bvh, the
+reference's source/bvh.cpp (partition, serialize) compiled on the host, and
+stores the buffer it builds from the triangle boxes of three procedural
+scenes (as a SHA-256) and from small hand-made box sets (in full).  Needs the reference checkout, named by --reference or the
 REFERENCE environment variable; the committed JSON is what the tests read, so
 this script only runs when the vectors are regenerated.
 
@@ -48,6 +51,12 @@ def main():
     with open(os.path.join(HERE, "reference_traversal.json"), "w") as f:
         json.dump(traversal, f, separators=(",", ":"))
     print("wrote", os.path.join(HERE, "reference_traversal.json"), file=sys.stderr)
+    bvh = {"scenes": [bvh_scene_case(*c) for c in BVH_SCENES], "box_sets": bvh_box_sets(),
+           "_generated_by": "tests/golden/gen_golden.py: serialize(partition(boxes)) of the reference's "
+                            "source/bvh.cpp compiled on the host by oracle/ref_bvh.cpp"}
+    with open(os.path.join(HERE, "reference_bvh.json"), "w") as f:
+        json.dump(bvh, f, separators=(",", ":"))
+    print("wrote", os.path.join(HERE, "reference_bvh.json"), file=sys.stderr)
 
 
 # (scene, generator seed, builder, max leaf size, camera rays per side, random rays)
@@ -125,6 +134,58 @@ def build_bvh(g, builder, max_leaf):
     osc = pyoracle.Scene(g.positions, g.normals, g.tris4(), g.materials_raw, g.lights(),
                          __import__("numpy").zeros((0, 4), "float32"))
     return pyoracle.build_kobra_bvh(osc.triangle_boxes())
+
+
+BVH_SCENES = [("box64", 3), ("box4k", 1), ("terrain_s", 1)]
+
+
+def reference_bvh(boxes):
+    """serialize(partition(boxes)) of the reference's builder, as float32
+    rows of 4 (3 per node)."""
+    import numpy as np
+    boxes = np.ascontiguousarray(boxes, np.float32)
+    blob = np.asarray([len(boxes)], np.uint32).tobytes() + boxes.tobytes()
+    out = subprocess.run([os.path.join(ROOT, "oracle", "_ref", "ref_bvh")], input=blob, capture_output=True,
+                         check=True).stdout
+    return np.frombuffer(out, np.float32).reshape(-1, 4)
+
+
+def bvh_scene_case(name, seed):
+    import hashlib
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    from oracle import pyoracle
+    g = pyoracle.GeneratedScene(name, seed)
+    osc = pyoracle.Scene(g.positions, g.normals, g.tris4(), g.materials_raw, g.lights(), np.zeros((0, 4), np.float32))
+    boxes = np.ascontiguousarray(osc.triangle_boxes(), np.float32)
+    ref = reference_bvh(boxes)
+    return {"scene": name, "seed": seed, "boxes": len(boxes),
+            "boxes_sha256": hashlib.sha256(boxes.tobytes()).hexdigest(), "rows": len(ref),
+            "bvh_sha256": hashlib.sha256(ref.tobytes()).hexdigest()}
+
+
+def bvh_box_sets():
+    """Seeded box sets at the builder's edges: one, two and three boxes,
+    seven identical boxes, boxes flat in y, point boxes, a row of boxes
+    along x, and a thousand random boxes."""
+    import numpy as np
+    rng = np.random.default_rng(5)
+
+    def rnd(n):
+        lo = rng.uniform(-5, 5, (n, 3))
+        return np.hstack([lo, lo + rng.uniform(0, 1, (n, 3))]).astype(np.float32)
+    sets = {"one": rnd(1), "two": rnd(2), "three": rnd(3), "identical": np.tile(rnd(1), (7, 1))}
+    flat = rnd(40)
+    flat[:, 4] = flat[:, 1]
+    pts = rnd(33)
+    pts[:, 3:] = pts[:, :3]
+    row = np.zeros((50, 6), np.float32)
+    row[:, 0] = np.arange(50)
+    row[:, 3] = np.arange(50) + 0.5
+    row[:, 4:] = 1
+    sets.update({"flat": flat, "points": pts, "row": row, "random1000": rnd(1000)})
+    return [{"name": k, "boxes": v.view(np.uint32).tolist(), "bvh": reference_bvh(v).view(np.uint32).tolist()}
+            for k, v in sets.items()]
 
 
 if __name__ == "__main__":

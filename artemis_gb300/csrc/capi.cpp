@@ -786,6 +786,9 @@ struct kgr_attachment {
 	DevBuf<int2> di_neighbours;
 	DevBuf<float> di_targets;
 	DevBuf<uint32_t> di_vis_queue[2], di_vis_count;
+	/* the visibility rounds' rays, blocked flags and walk counters */
+	DevBuf<float4> di_vis_o, di_vis_d;
+	DevBuf<uint32_t> di_vis_flag;
 	DevBuf<float4> gi_selection;
 	DevBuf<int2> gi_neighbours;
 	DevBuf<float> gi_weights;
@@ -999,6 +1002,9 @@ struct kgr_attachment {
 		di_vis_queue[0].release();
 		di_vis_queue[1].release();
 		di_vis_count.release();
+		di_vis_o.release();
+		di_vis_d.release();
+		di_vis_flag.release();
 		gi_selection.release();
 		gi_neighbours.release();
 		gi_weights.release();
@@ -1297,6 +1303,11 @@ void render_restir_di(kgr_attachment *att, const kgr_launch_info *info, const kg
 	rb.vis_queue[0] = att->di_vis_queue[0].ptr;
 	rb.vis_queue[1] = att->di_vis_queue[1].ptr;
 	rb.vis_count = att->di_vis_count.ptr;
+	rb.vis_o = att->di_vis_o.ptr;
+	rb.vis_d = att->di_vis_d.ptr;
+	rb.vis_flag = att->di_vis_flag.ptr;
+	rb.vis_capacity = (uint32_t)att->di_vis_o.count;
+	KGR_REQUIRE(fp.paths <= rb.vis_capacity, KGR_ERR_INTERNAL, "ReSTIR visibility buffers below the path count");
 	int prev = att->prev_index, cur = 1 - prev;
 	uint32_t launches = 0;
 
@@ -1310,7 +1321,7 @@ void render_restir_di(kgr_attachment *att, const kgr_launch_info *info, const kg
 	att->mark(STAGE_TRACE_CLOSEST, st);
 	restir_primary(s, pb, fp, rb, cur, st);
 	att->mark(STAGE_RESTIR_PRIMARY, st);
-	launches += 4; /* generate, closest hit, primary vertex, its shadow rays */
+	launches += 2 + KGR_RESTIR_PRIMARY_LAUNCHES; /* generate, closest hit, primary vertex, its shadow rays */
 	/* with an environment map one more bounce is traced for its misses */
 	for (int d = 1; d <= fp.max_depth + (s.has_env ? 1 : 0); d++) {
 		int q = d & 1;
@@ -1330,7 +1341,7 @@ void render_restir_di(kgr_attachment *att, const kgr_launch_info *info, const kg
 	/* temporal pass */
 	if (fp.temporal) {
 		restir_temporal(s, fp, rb, out, cur, prev, st, [&](int k) { att->mark(k, st); });
-		launches += 3;
+		launches += KGR_RESTIR_TEMPORAL_LAUNCHES;
 	}
 	/* spatial passes with the ping-pong of restir.cuh:280-300 */
 	int passes = att->opt_int("spatial_passes", 2);
@@ -1746,7 +1757,11 @@ kgr_status kgr_load(kgr_attachment *att)
 				att->di_targets.alloc(npix * (KGR_MAX_NEIGHBORS + 1));
 				att->di_vis_queue[0].alloc(npix * KGR_MAX_NEIGHBORS);
 				att->di_vis_queue[1].alloc(npix * (KGR_MAX_NEIGHBORS + 1));
-				att->di_vis_count.alloc(4); /* two queue counts, two fetch counters */
+				att->di_vis_count.alloc(2 * CNT_COUNT); /* a counter array per visibility round */
+				att->di_vis_o.alloc(npix * (KGR_MAX_NEIGHBORS + 1));
+				att->di_vis_d.alloc(npix * (KGR_MAX_NEIGHBORS + 1));
+				att->di_vis_flag.alloc(npix * (KGR_MAX_NEIGHBORS + 1));
+				KGR_CUDA(cudaMemset(att->di_vis_flag.ptr, 0, npix * (KGR_MAX_NEIGHBORS + 1) * sizeof(uint32_t)));
 				att->prev_index = 1;
 				att->ensure_paths((uint32_t)npix);
 			}

@@ -49,7 +49,9 @@ struct PathBuffers {
 	uint32_t capacity;
 	/* when set, the any-hit walks store each shadow ray's blocked flag
 	 * (1 or 0) at its path id instead of resolving the path's pending
-	 * light (visibility rays of other passes) */
+	 * light (visibility rays of other passes); with shadow_queue NULL the
+	 * walks take rays 0 .. counters[CNT_SHADOW]-1 in order (the id of a
+	 * ray is its position) */
 	uint32_t *shadow_flags = nullptr;
 };
 
@@ -165,13 +167,29 @@ struct RestirFrameBuffers {
 	int2 *neighbours;
 	float *targets;
 	uint32_t *vis_queue[2];
+	/* two counter arrays of CNT_COUNT entries, one per round: the queue
+	 * count at CNT_SHADOW, the any-hit walk's fetch counter at
+	 * CNT_FETCH_SHADOW */
 	uint32_t *vis_count;
+	/* per slot of the target array: the queued shadow ray ({origin},
+	 * {direction, tmax}) and the walk's blocked flag (per path for the
+	 * primary pass's rays); vis_capacity slots, (KGR_MAX_NEIGHBORS + 1) *
+	 * npix */
+	float4 *vis_o, *vis_d;
+	uint32_t *vis_flag;
+	uint32_t vis_capacity;
 };
 
 /* Most neighbours a ReSTIR DI spatial pass takes (spatial_neighbors). */
 #define KGR_MAX_NEIGHBORS 16
-/* Kernels one ReSTIR DI spatial pass launches. */
+/* Kernels one ReSTIR DI spatial pass launches: gather, the any-hit walk of
+ * the neighbours' rays, resample, the walk of the selection's rays,
+ * finish. */
 #define KGR_RESTIR_SPATIAL_LAUNCHES 5
+/* Kernels the temporal pass launches (gather, walk, merge) and the primary
+ * pass (selection, walk, blocked weights). */
+#define KGR_RESTIR_TEMPORAL_LAUNCHES 3
+#define KGR_RESTIR_PRIMARY_LAUNCHES 3
 
 struct OutputBuffers {
 	float4 *color, *normal, *albedo, *position;

@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(BLOCK, KGR_MIN_BLOCKS(BLOCK, OCC)) shadow_reso
 	uint32_t stride = gridDim.x * blockDim.x;
 	TraceCounters cnt = {0, 0};
 	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-		uint32_t p = pb.shadow_queue[i];
+		uint32_t p = pb.shadow_queue ? pb.shadow_queue[i] : i;
 		float4 a = pb.sh_o[p], b = pb.sh_d[p];
 		kgr_hit h;
 		bool occ;
@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(BLOCK, KGR_MIN_BLOCKS(BLOCK, OCC)) fast_persis
 			if (need) {
 				uint32_t i = base + __popc(m & ((1u << lane) - 1u));
 				if (i < n) {
-					p = queue[i];
+					p = (ANY && !queue) ? i : queue[i];
 					float4 a = ANY ? pb.sh_o[p] : pb.ray_o[p];
 					float4 b = ANY ? pb.sh_d[p] : pb.ray_d[p];
 					r = fast_ray(mk(a.x, a.y, a.z), mk(b.x, b.y, b.z));
@@ -368,7 +368,7 @@ __global__ void __launch_bounds__(BLOCK, KGR_MIN_BLOCKS(BLOCK, OCC)) cw_persiste
 			if (need) {
 				uint32_t i = base + __popc(m & ((1u << lane) - 1u));
 				if (i < n) {
-					p = queue[i];
+					p = (ANY && !queue) ? i : queue[i];
 					float4 a = ANY ? pb.sh_o[p] : pb.ray_o[p];
 					float4 b = ANY ? pb.sh_d[p] : pb.ray_d[p];
 					cw_begin(w, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), stack);

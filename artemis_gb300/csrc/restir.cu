@@ -105,11 +105,6 @@ __device__ __forceinline__ void store_res(const ReservoirBuffers &rb, uint32_t i
 	rb.b[i] = make_float4(w, W, __int_as_float(M), smp.env_v);
 }
 
-__device__ __forceinline__ bool occluded(const DeviceScene &s, int layout, const f3 &o, const f3 &d, float R)
-{
-	kgr_hit h;
-	return trace<true>(s, layout, o, d, R - KGR_SHADOW_EPS, h);
-}
 
 /* target (amadeus_restir.cu:147-161) */
 __device__ __forceinline__ float target(const DeviceScene &s, const Sample &smp, const SurfaceHit &hit)
@@ -126,9 +121,10 @@ __device__ __forceinline__ float target(const DeviceScene &s, const Sample &smp,
 
 /* occluded_target (amadeus_restir.cu:163-178, via direct_occluded of
  * amadeus_common.cuh:399-421) is target() when the shadow ray from the
- * surface to the sample, occluded() over D / |D| and |D|, is unblocked, and
- * 0 when it is blocked.  The reuse kernels compute target() and queue that
- * ray; the visibility kernels set the target to 0 when the ray is blocked. */
+ * surface to the sample -- the any-hit walk over D / |D| up to |D| - eps --
+ * is unblocked, and 0 when it is blocked.  The reuse kernels compute
+ * target() and queue that ray (vis_ray); the path tracer's tuned any-hit
+ * walk flags it, and the next kernel reads the target through vis_target. */
 
 __device__ __forceinline__ f3 v3(const float *p) { return mk(p[0], p[1], p[2]); }
 
@@ -148,6 +144,36 @@ __device__ __forceinline__ SurfaceHit gbuffer_hit(const FrameParams &fp, const R
 	h.wo = normalize(v3(fp.center) - x);
 	h.x = x;
 	return h;
+}
+
+/* The reuse passes' shadow rays.  The kernel that queues an entry (a slot
+ * of the target array) also writes the entry's ray there, {origin} and
+ * {D / |D|, |D| - eps} -- the ray of occluded_target from `from` towards
+ * `to` (amadeus_common.cuh:399-421); the path tracer's tuned any-hit walk
+ * takes the queue and stores a blocked flag per entry; the next kernel
+ * reads an entry's target as 0 when its flag is set.  The queue count of
+ * round q sits in a counter array of its own (vis_count + q * CNT_COUNT),
+ * where the walk looks for it. */
+__device__ __forceinline__ uint32_t *vis_n(const RestirFrameBuffers &rb, int q)
+{
+	return rb.vis_count + q * CNT_COUNT + CNT_SHADOW;
+}
+
+__device__ __forceinline__ void vis_ray(const RestirFrameBuffers &rb, uint32_t e, const f3 &from, const f3 &to)
+{
+	f3 D = to - from;
+	float d = length(D);
+	f3 Dn = D / d;
+	rb.vis_o[e] = f4_of(from, 0.0f);
+	rb.vis_d[e] = f4_of(Dn, d - KGR_SHADOW_EPS);
+}
+
+/* An entry's target after its walk.  An entry that was not queued holds
+ * +0, or a target its reader ignores (not above 0), so a flag left from an
+ * earlier round does not change what is read. */
+__device__ __forceinline__ float vis_target(const RestirFrameBuffers &rb, uint32_t e)
+{
+	return rb.vis_flag[e] ? 0.0f : rb.targets[e];
 }
 
 /* RIS at the primary vertex, then the continuation ray. */
@@ -216,7 +242,7 @@ __global__ void __launch_bounds__(128) primary_kernel(DeviceScene s, PathBuffers
 				 * answer).  The reservoir is stored as if the selection were
 				 * visible and its shadow ray queued: a blocked ray makes the
 				 * target 0, so resample and the visibility factor give W = +0,
-				 * which primary_visibility_kernel writes. */
+				 * which primary_blocked_kernel writes. */
 				float tgt = 0.0f;
 				if (has_light(res.data)) {
 					f3 Le, ln;
@@ -265,23 +291,22 @@ __global__ void __launch_bounds__(128) primary_kernel(DeviceScene s, PathBuffers
 			}
 		}
 		queue_append(pb.queue[1], out_counter, p, cont, pb.counters + CNT_BOUNCE_TOTAL);
-		queue_append(rb.vis_queue[0], rb.vis_count + 0, p, shadow);
+		queue_append(rb.vis_queue[0], vis_n(rb, 0), p, shadow);
 	}
 }
 
 /* The selections' shadow rays queued by primary_kernel (in the shadow-ray
- * arrays, free until the first bounce is shaded): a blocked one sets the
- * reservoir's W to +0. */
-__global__ void __launch_bounds__(128) primary_visibility_kernel(DeviceScene s, PathBuffers pb, FrameParams fp,
-		RestirFrameBuffers rb, int cur)
+ * arrays, free until the first bounce is shaded) are walked by the tuned
+ * any-hit walk, which flags each blocked one at its path; a blocked
+ * selection's reservoir gets W = +0. */
+__global__ void primary_blocked_kernel(RestirFrameBuffers rb, int cur)
 {
-	for_each_queued(rb.vis_count[0], rb.vis_count + 2, [&](uint32_t i) {
+	const uint32_t n = *vis_n(rb, 0);
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
 		uint32_t p = rb.vis_queue[0][i];
-		float4 a = pb.sh_o[p], b = pb.sh_d[p];
-		kgr_hit h;
-		if (trace<true>(s, fp.layout, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), b.w, h))
+		if (rb.vis_flag[p])
 			rb.res[cur].b[p].y = 0.0f;
-	});
+	}
 }
 
 __device__ __forceinline__ void accumulate4(float4 *buf, uint32_t i, float4 v, bool acc, float count)
@@ -346,9 +371,9 @@ __device__ __forceinline__ int reproject(const FrameParams &fp, int index, const
 /* Temporal reuse (amadeus_restir.cu:316-365) in three launches: the two
  * occluded targets -- the current reservoir's and the reprojected previous
  * one's -- are computed unoccluded with their shadow rays queued
- * (temporal_gather_kernel), the rays walked (temporal_visibility_kernel: a
- * blocked ray sets its target to 0, occluded_target's result), then the
- * merge (temporal_merge_kernel).  Targets sit in rows 0 (current) and 1
+ * (temporal_gather_kernel), the rays walked (a blocked ray makes its
+ * target 0, occluded_target's result), then the merge
+ * (temporal_merge_kernel).  Targets sit in rows 0 (current) and 1
  * (previous) of the spatial pass's target array, the reprojected pixel and
  * its M in the neighbour array: both are free until spatial reuse starts. */
 __global__ void __launch_bounds__(128) temporal_gather_kernel(DeviceScene s, FrameParams fp, RestirFrameBuffers rb,
@@ -369,7 +394,11 @@ __global__ void __launch_bounds__(128) temporal_gather_kernel(DeviceScene s, Fra
 	float t_current = target(s, cs, hit);
 	rb.targets[pix] = t_current;
 	/* +0 stays +0 whatever the ray; anything else is traced */
-	queue_append(rb.vis_queue[0], rb.vis_count + 0, pix, __float_as_uint(t_current) != 0u);
+	bool ray = __float_as_uint(t_current) != 0u;
+	f3 from = f3_of(out.position[pix]);
+	if (ray)
+		vis_ray(rb, pix, from, cs.point);
+	queue_append(rb.vis_queue[0], vis_n(rb, 0), pix, ray);
 	int32_t pM = 0;
 	if (pindex >= 0) {
 		Sample ps;
@@ -378,27 +407,13 @@ __global__ void __launch_bounds__(128) temporal_gather_kernel(DeviceScene s, Fra
 		if (pM > 0) {
 			float t_previous = target(s, ps, hit);
 			rb.targets[fp.npix + pix] = t_previous;
-			queue_append(rb.vis_queue[0], rb.vis_count + 0, fp.npix + pix, __float_as_uint(t_previous) != 0u);
+			bool pray = __float_as_uint(t_previous) != 0u;
+			if (pray)
+				vis_ray(rb, fp.npix + pix, from, ps.point);
+			queue_append(rb.vis_queue[0], vis_n(rb, 0), fp.npix + pix, pray);
 		}
 	}
 	rb.neighbours[pix] = make_int2(pindex, pM);
-}
-
-__global__ void __launch_bounds__(128) temporal_visibility_kernel(DeviceScene s, FrameParams fp,
-		RestirFrameBuffers rb, OutputBuffers out, int cur, int prev)
-{
-	for_each_queued(rb.vis_count[0], rb.vis_count + 2, [&](uint32_t i) {
-		uint32_t e = rb.vis_queue[0][i];
-		bool previous = e >= fp.npix;
-		uint32_t pix = previous ? e - fp.npix : e;
-		f3 from = f3_of(out.position[pix]);
-		f3 to = previous ? f3_of(rb.res[prev].a[rb.neighbours[pix].x]) : f3_of(rb.res[cur].a[pix]);
-		f3 D = to - from;
-		float d = length(D);
-		f3 Dn = D / d;
-		if (occluded(s, fp.layout, from, Dn, d))
-			rb.targets[e] = 0.0f;
-	});
 }
 
 __global__ void __launch_bounds__(128) temporal_merge_kernel(DeviceScene s, FrameParams fp, RestirFrameBuffers rb,
@@ -419,7 +434,7 @@ __global__ void __launch_bounds__(128) temporal_merge_kernel(DeviceScene s, Fram
 	float4 av = rb.auxiliary[pix];
 	Reservoir merged;
 	merged.init(mk(av.x, av.y, av.z));
-	float t_current = rb.targets[pix];
+	float t_current = vis_target(rb, pix);
 	merged.update(cs, t_current * cW * cM);
 	int32_t N = cM;
 	if (pr.x >= 0) {
@@ -429,7 +444,7 @@ __global__ void __launch_bounds__(128) temporal_merge_kernel(DeviceScene s, Fram
 		load_res(P, (uint32_t)pr.x, ps, pw, pW, pM);
 		if (pM > 0) {
 			pM = pM < fp.temporal_mcap ? pM : fp.temporal_mcap;
-			float t_previous = rb.targets[fp.npix + pix];
+			float t_previous = vis_target(rb, fp.npix + pix);
 			merged.update(ps, t_previous * pW * pM);
 			N += (t_previous > 0) * pM;
 		}
@@ -463,11 +478,11 @@ __device__ __forceinline__ int spatial_neighbor(const FrameParams &fp, int index
  * per pass.  Its shadow rays -- one per neighbour reservoir (occluded_target
  * at this pixel), one per neighbour for the bias correction (the selected
  * sample seen from the neighbour's surface) and the final lighting ray --
- * are queued and walked by restir_visibility_kernel, one ray per thread,
- * instead of inside the per-pixel loops.  Between the launches: per
+ * are queued with their rays and walked by the path tracer's tuned any-hit
+ * walk, instead of inside the per-pixel loops.  Between the launches: per
  * neighbour slot (k-major, slot = i * npix + pixel) {neighbour pixel, M}
- * and a target value that a blocked ray sets to 0 (occluded_target's
- * result); row KGR_MAX_NEIGHBORS of the target array holds the lighting
+ * and a target value that reads as 0 once its ray is found blocked
+ * (occluded_target's result); row KGR_MAX_NEIGHBORS of the target array holds the lighting
  * ray's 1 (visible) or 0; the merged reservoir sits in the output buffer
  * between resample and finish.  Every value is computed by the reference's
  * expressions in its order, and each pixel's random stream is replayed
@@ -492,6 +507,7 @@ __global__ void __launch_bounds__(128) restir_gather_kernel(DeviceScene s, Frame
 	if (cM <= 0)
 		return;
 	SurfaceHit hit = gbuffer_hit(fp, rb, out, pix);
+	f3 from = f3_of(out.position[pix]);
 	float4 av = rb.auxiliary[pix];
 	f3 seed = mk(av.x, av.y, av.z);
 	rand_uniform(seed);
@@ -514,38 +530,10 @@ __global__ void __launch_bounds__(128) restir_gather_kernel(DeviceScene s, Frame
 		}
 		rb.neighbours[slot] = make_int2(index0, nM);
 		rb.targets[slot] = t;
-		queue_append(rb.vis_queue[0], rb.vis_count + 0, slot, ray);
+		if (ray)
+			vis_ray(rb, slot, from, ns.point);
+		queue_append(rb.vis_queue[0], vis_n(rb, 0), slot, ray);
 	}
-}
-
-/* Shadow rays of the queued entries; a blocked ray sets its target to 0.
- * Round 0: this pixel's surface to a neighbour reservoir's light sample.
- * Round 1: a neighbour's surface to this pixel's selected sample (entries
- * below KGR_MAX_NEIGHBORS * npix), or this pixel's surface to it (the
- * lighting ray, entries above). */
-__global__ void __launch_bounds__(128) restir_visibility_kernel(DeviceScene s, FrameParams fp,
-		RestirFrameBuffers rb, OutputBuffers out, int inb, int outb, int round)
-{
-	const uint32_t *queue = rb.vis_queue[round];
-	const uint32_t lighting = (uint32_t)KGR_MAX_NEIGHBORS * fp.npix;
-	for_each_queued(rb.vis_count[round], rb.vis_count + 2 + round, [&](uint32_t i) {
-		uint32_t e = queue[i];
-		uint32_t pix = e < lighting ? e % fp.npix : e - lighting;
-		f3 from, to;
-		if (round == 0) {
-			from = f3_of(out.position[pix]);
-			to = f3_of(rb.res[inb].a[rb.neighbours[e].x]);
-		} else {
-			uint32_t at = e < lighting ? (uint32_t)rb.neighbours[e].x : pix;
-			from = f3_of(out.position[at]);
-			to = f3_of(rb.res[outb].a[pix]);
-		}
-		f3 D = to - from;
-		float d = length(D);
-		f3 Dn = D / d;
-		if (occluded(s, fp.layout, from, Dn, d))
-			rb.targets[e] = 0.0f;
-	});
 }
 
 /* resample: the merged reservoir over the centre and the neighbours with
@@ -582,7 +570,7 @@ __global__ void __launch_bounds__(128) restir_resample_kernel(DeviceScene s, Fra
 			float nw, nW;
 			int32_t nM;
 			load_res(IN, (uint32_t)nb.x, ns, nw, nW, nM);
-			merged.update(ns, rb.targets[slot] * nW * nM);
+			merged.update(ns, vis_target(rb, slot) * nW * nM);
 		}
 		count += nb.y;
 	}
@@ -600,11 +588,15 @@ __global__ void __launch_bounds__(128) restir_resample_kernel(DeviceScene s, Fra
 			t = target(s, merged.data, h0);
 		}
 		rb.targets[slot] = t;
-		queue_append(rb.vis_queue[1], rb.vis_count + 1, slot, t > 0.0f);
+		if (t > 0.0f)
+			vis_ray(rb, slot, f3_of(out.position[nb.x]), merged.data.point);
+		queue_append(rb.vis_queue[1], vis_n(rb, 1), slot, t > 0.0f);
 	}
 	uint32_t lit = (uint32_t)KGR_MAX_NEIGHBORS * fp.npix + pix;
 	rb.targets[lit] = has_light(merged.data) ? 1.0f : 0.0f;
-	queue_append(rb.vis_queue[1], rb.vis_count + 1, lit, has_light(merged.data));
+	if (has_light(merged.data))
+		vis_ray(rb, lit, f3_of(out.position[pix]), merged.data.point);
+	queue_append(rb.vis_queue[1], vis_n(rb, 1), lit, has_light(merged.data));
 	store_res(OUT, pix, merged.data, merged.w, 0.0f, merged.M);
 }
 
@@ -632,14 +624,14 @@ __global__ void __launch_bounds__(128) restir_finish_kernel(DeviceScene s, Frame
 			int32_t size = rb.neighbours[slot].y;
 			if (size <= 0)
 				continue;
-			if (rb.targets[slot] > 0.0f)
+			if (vis_target(rb, slot) > 0.0f)
 				Z += size;
 		}
 		float t_merged = target(s, data, hit);
 		float denominator = t_merged * Z;
 		float W = (denominator > 0.0f) ? w / denominator : 0.0f;
 		f3 lighting = mk(0.0f);
-		if (has_light(data) && rb.targets[(uint32_t)KGR_MAX_NEIGHBORS * fp.npix + pix] > 0.0f) {
+		if (has_light(data) && vis_target(rb, (uint32_t)KGR_MAX_NEIGHBORS * fp.npix + pix) > 0.0f) {
 			f3 Le, ln;
 			int type = emitter(s, data, Le, ln);
 			f3 D = data.point - hit.x;
@@ -663,6 +655,29 @@ __global__ void __launch_bounds__(128) restir_finish_kernel(DeviceScene s, Frame
 	accumulate4(out.color, pix, f4_of(c, cwt), fp.accumulate != 0, (float)fp.samples);
 }
 
+/* The tuned any-hit walk over the queued entries of round q: their rays
+ * (the slots' rays, or the paths' shadow rays for the primary pass), a
+ * blocked flag per entry, the round's counter array. */
+void vis_walk(const DeviceScene &s, const FrameParams &fp, const RestirFrameBuffers &rb, float4 *o, float4 *d,
+		int q, cudaStream_t st)
+{
+	PathBuffers vb{};
+	vb.sh_o = o;
+	vb.sh_d = d;
+	vb.shadow_queue = rb.vis_queue[q];
+	vb.counters = rb.vis_count + q * CNT_COUNT;
+	vb.shadow_flags = rb.vis_flag;
+	vb.visits = nullptr;
+	vb.capacity = rb.vis_capacity;
+	pt_shadow_resolve(s, vb, fp.layout, fp.tune, st);
+}
+
+/* both rounds' counter arrays to zero */
+void vis_clear(const RestirFrameBuffers &rb, cudaStream_t st)
+{
+	KGR_CUDA(cudaMemsetAsync(rb.vis_count, 0, 2 * CNT_COUNT * sizeof(uint32_t), st));
+}
+
 } /* namespace */
 
 void restir_primary(const DeviceScene &s, const PathBuffers &pb, const FrameParams &fp,
@@ -670,9 +685,10 @@ void restir_primary(const DeviceScene &s, const PathBuffers &pb, const FramePara
 {
 	int grid = (int)((pb.capacity + 127) / 128);
 	int cap = device_sm_count() * 16;
-	KGR_CUDA(cudaMemsetAsync(rb.vis_count, 0, 4 * sizeof(uint32_t), st));
+	vis_clear(rb, st);
 	primary_kernel<<<grid < cap ? grid : cap, 128, 0, st>>>(s, pb, fp, rb, cur);
-	primary_visibility_kernel<<<device_sm_count() * 8, 128, 0, st>>>(s, pb, fp, rb, cur);
+	vis_walk(s, fp, rb, pb.sh_o, pb.sh_d, 0, st);
+	primary_blocked_kernel<<<device_sm_count() * 8, 128, 0, st>>>(rb, cur);
 	KGR_CUDA(cudaGetLastError());
 }
 
@@ -691,10 +707,10 @@ void restir_temporal(const DeviceScene &s, const FrameParams &fp, const RestirFr
 		if (mark)
 			mark(stage);
 	};
-	KGR_CUDA(cudaMemsetAsync(rb.vis_count, 0, 4 * sizeof(uint32_t), st));
+	vis_clear(rb, st);
 	temporal_gather_kernel<<<grid, 128, 0, st>>>(s, fp, rb, out, cur, prev);
 	done(STAGE_RESTIR_TEMPORAL);
-	temporal_visibility_kernel<<<device_sm_count() * 8, 128, 0, st>>>(s, fp, rb, out, cur, prev);
+	vis_walk(s, fp, rb, rb.vis_o, rb.vis_d, 0, st);
 	done(STAGE_RESTIR_TEMPORAL_VIS);
 	temporal_merge_kernel<<<grid, 128, 0, st>>>(s, fp, rb, out, cur, prev);
 	done(STAGE_RESTIR_TEMPORAL);
@@ -705,19 +721,18 @@ void restir_spatial(const DeviceScene &s, const FrameParams &fp, const RestirFra
 		const OutputBuffers &out, int in, int outbuf, cudaStream_t st, const StageMark &mark)
 {
 	unsigned grid = (fp.npix + 127) / 128;
-	int vis_grid = device_sm_count() * 8;
 	auto done = [&](int stage) {
 		if (mark)
 			mark(stage);
 	};
-	KGR_CUDA(cudaMemsetAsync(rb.vis_count, 0, 4 * sizeof(uint32_t), st));
+	vis_clear(rb, st);
 	restir_gather_kernel<<<grid, 128, 0, st>>>(s, fp, rb, out, in);
 	done(STAGE_RESTIR_SPATIAL);
-	restir_visibility_kernel<<<vis_grid, 128, 0, st>>>(s, fp, rb, out, in, outbuf, 0);
+	vis_walk(s, fp, rb, rb.vis_o, rb.vis_d, 0, st);
 	done(STAGE_RESTIR_SPATIAL_VIS);
 	restir_resample_kernel<<<grid, 128, 0, st>>>(s, fp, rb, out, in, outbuf);
 	done(STAGE_RESTIR_SPATIAL);
-	restir_visibility_kernel<<<vis_grid, 128, 0, st>>>(s, fp, rb, out, in, outbuf, 1);
+	vis_walk(s, fp, rb, rb.vis_o, rb.vis_d, 1, st);
 	done(STAGE_RESTIR_SPATIAL_VIS);
 	restir_finish_kernel<<<grid, 128, 0, st>>>(s, fp, rb, out, in, outbuf);
 	done(STAGE_RESTIR_SPATIAL);

@@ -109,8 +109,9 @@ uint64_t request_bytes(const kgr_request &q)
 	 * auxiliary terms, and the reuse passes' scratch for up to 16
 	 * neighbours: {pixel, M} and a target per neighbour slot, a row of
 	 * lighting targets, the two shadow-ray queues (16 * 8 + 17 * 4 +
-	 * 16 * 4 + 17 * 4 = 328 bytes) */
-	return q.kind == KGR_REQUEST_RESTIR_DI ? npix * (64 + 64 + 64 + 32 + 328) : npix * 16;
+	 * 16 * 4 + 17 * 4 = 328 bytes), and per target slot a shadow ray and
+	 * its blocked flag (17 * 36 = 612 bytes) */
+	return q.kind == KGR_REQUEST_RESTIR_DI ? npix * (64 + 64 + 64 + 32 + 328 + 612) : npix * 16;
 }
 
 } /* namespace */

@@ -793,6 +793,8 @@ struct kgr_attachment {
 	DevBuf<int2> gi_neighbours;
 	DevBuf<float> gi_weights;
 	DevBuf<uint32_t> gi_vis_queue[2], gi_vis_count;
+	DevBuf<float4> gi_vis_o, gi_vis_d;
+	DevBuf<uint32_t> gi_vis_flag;
 	int gi_prev = 0;
 
 	/* Mamba state: G-buffer, reservoirs, secondary rays, probe table; which
@@ -1011,6 +1013,9 @@ struct kgr_attachment {
 		gi_vis_queue[0].release();
 		gi_vis_queue[1].release();
 		gi_vis_count.release();
+		gi_vis_o.release();
+		gi_vis_d.release();
+		gi_vis_flag.release();
 		for (DevBuf<uint16_t> *b : {&q_feat, &r_feat, &b_x})
 			b->release();
 		for (DevBuf<float4> *b : {&q_le, &q_out, &r_beta, &r_lb, &r_le, &b_t})
@@ -1625,6 +1630,11 @@ void render_restir_gi(kgr_attachment *att, const kgr_launch_info *info, const kg
 	gb.vis_queue[0] = att->gi_vis_queue[0].ptr;
 	gb.vis_queue[1] = att->gi_vis_queue[1].ptr;
 	gb.vis_count = att->gi_vis_count.ptr;
+	gb.vis_o = att->gi_vis_o.ptr;
+	gb.vis_d = att->gi_vis_d.ptr;
+	gb.vis_flag = att->gi_vis_flag.ptr;
+	gb.vis_capacity = (uint32_t)att->gi_vis_o.count;
+	KGR_REQUIRE(fp.paths <= gb.vis_capacity, KGR_ERR_INTERNAL, "GI visibility buffers below the path count");
 	int prev = att->gi_prev, cur = (prev + 1) % 3, tmp = (prev + 2) % 3;
 	uint32_t launches = 0;
 
@@ -1636,7 +1646,7 @@ void render_restir_gi(kgr_attachment *att, const kgr_launch_info *info, const kg
 	att->mark(STAGE_TRACE_CLOSEST, st);
 	gi_primary(s, pb, fp, gb, st);
 	att->mark(STAGE_RESTIR_PRIMARY, st);
-	launches += 4; /* generate, closest hit, primary vertex, its shadow rays */
+	launches += 2 + KGR_GI_PRIMARY_LAUNCHES; /* generate, closest hit, primary vertex, its shadow rays */
 	for (int d = 1; d <= fp.max_depth; d++) {
 		int q = d & 1;
 		reset_counters(pb, (1 << (q ^ 1)) | (1 << CNT_SHADOW), st);
@@ -1668,7 +1678,7 @@ void render_restir_gi(kgr_attachment *att, const kgr_launch_info *info, const kg
 	}
 	gi_final(s, fp, gb, out, in, st);
 	att->mark(STAGE_ACCUMULATE, st);
-	launches++;
+	launches += KGR_GI_FINAL_LAUNCHES;
 	att->gi_prev = in;
 	memcpy(att->prev_projection, info->camera.projection, 64);
 	memcpy(att->prev_view, info->camera.view, 64);
@@ -1784,7 +1794,11 @@ kgr_status kgr_load(kgr_attachment *att)
 				att->gi_weights.alloc(npix * KGR_GI_MAX_NEIGHBORS);
 				att->gi_vis_queue[0].alloc(npix * KGR_GI_MAX_NEIGHBORS);
 				att->gi_vis_queue[1].alloc(npix * KGR_GI_MAX_NEIGHBORS);
-				att->gi_vis_count.alloc(4); /* two queue counts, two fetch counters */
+				att->gi_vis_count.alloc(2 * CNT_COUNT); /* a counter array per visibility round */
+				att->gi_vis_o.alloc(npix);
+				att->gi_vis_d.alloc(npix);
+				att->gi_vis_flag.alloc(npix);
+				KGR_CUDA(cudaMemset(att->gi_vis_flag.ptr, 0, npix * sizeof(uint32_t)));
 				att->gi_prev = 0;
 				att->ensure_paths((uint32_t)npix);
 			}

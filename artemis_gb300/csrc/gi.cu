@@ -174,12 +174,31 @@ __device__ __forceinline__ float gi_jacobian(const f3 &xq, const f3 &xr, const G
 	return (j >= 1.0f / jmax && j <= jmax) ? j : 0.0f;
 }
 
+/* The any-hit test of the visibility ray from `from` to `to`. */
 __device__ __forceinline__ bool visible(const DeviceScene &s, int layout, const f3 &from, const f3 &to)
 {
 	f3 D = to - from;
 	float d = length(D);
 	kgr_hit h;
 	return !trace<true>(s, layout, from, D / d, d - KGR_SHADOW_EPS, h);
+}
+
+/* Round q's queue count sits in its own counter array (vis_count +
+ * q * CNT_COUNT), where the tuned any-hit walk looks for it; the fetch
+ * counter of a one-ray-per-thread round sits in the same array. */
+__device__ __forceinline__ uint32_t *gi_vis_n(const GiFrameBuffers &gb, int q)
+{
+	return gb.vis_count + q * CNT_COUNT + CNT_SHADOW;
+}
+
+/* A ray for the tuned any-hit walk at slot e: {from}, {D / |D|, |D| - eps}
+ * with D = to - from, the ray visible() walks. */
+__device__ __forceinline__ void gi_vis_ray(const GiFrameBuffers &gb, uint32_t e, const f3 &from, const f3 &to)
+{
+	f3 D = to - from;
+	float d = length(D);
+	gb.vis_o[e] = f4_of(from, 0.0f);
+	gb.vis_d[e] = f4_of(D / d, d - KGR_SHADOW_EPS);
 }
 
 struct GBuf {
@@ -315,8 +334,8 @@ __global__ void __launch_bounds__(128) gi_primary_kernel(DeviceScene s, PathBuff
 					M++;
 				}
 				/* the selected light's contribution, with its shadow ray
-				 * queued for gi_direct_visibility_kernel, which zeroes the
-				 * contribution when the ray is blocked */
+				 * queued for the any-hit walk; gi_direct_blocked_kernel
+				 * zeroes the contribution when the ray is blocked */
 				f3 direct = mk(0.0f);
 				if (sel >= 0) {
 					TriLight l = load_light(s.lights, (uint32_t)sel);
@@ -349,23 +368,22 @@ __global__ void __launch_bounds__(128) gi_primary_kernel(DeviceScene s, PathBuff
 			}
 		}
 		queue_append(pb.queue[1], out_counter, p, cont, pb.counters + CNT_BOUNCE_TOTAL);
-		queue_append(gb.vis_queue[0], gb.vis_count + 0, p, shadow);
+		queue_append(gb.vis_queue[0], gi_vis_n(gb, 0), p, shadow);
 	}
 }
 
 /* The primary vertices' ReSTIR DI shadow rays (queued by gi_primary_kernel
- * in the shadow-ray arrays, free until the first bounce is shaded): a
- * blocked ray zeroes the pixel's direct light. */
-__global__ void __launch_bounds__(128) gi_direct_visibility_kernel(DeviceScene s, PathBuffers pb, FrameParams fp,
-		GiFrameBuffers gb)
+ * in the shadow-ray arrays, free until the first bounce is shaded) are
+ * walked by the tuned any-hit walk, which flags a blocked one at its path:
+ * a blocked ray zeroes the pixel's direct light. */
+__global__ void gi_direct_blocked_kernel(GiFrameBuffers gb)
 {
-	for_each_queued(gb.vis_count[0], gb.vis_count + 2, [&](uint32_t i) {
+	const uint32_t n = *gi_vis_n(gb, 0);
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
 		uint32_t p = gb.vis_queue[0][i];
-		float4 a = pb.sh_o[p], b = pb.sh_d[p];
-		kgr_hit hh;
-		if (trace<true>(s, fp.layout, mk(a.x, a.y, a.z), mk(b.x, b.y, b.z), b.w, hh))
+		if (gb.vis_flag[p])
 			gb.direct[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-	});
+	}
 }
 
 /* Initial reservoir from the finished path: one candidate, W in FP64. */
@@ -542,7 +560,7 @@ __global__ void __launch_bounds__(128) gi_spatial_gather_kernel(FrameParams fp, 
 		}
 		gb.neighbours[slot] = nb;
 		gb.weights[slot] = wn;
-		queue_append(gb.vis_queue[0], gb.vis_count + 0, slot, wn > 0.0f);
+		queue_append(gb.vis_queue[0], gi_vis_n(gb, 0), slot, wn > 0.0f);
 	}
 	gb.selection[pix] = make_float4(wC, 0.0f, __int_as_float(Msum), 0.0f);
 }
@@ -555,14 +573,17 @@ __device__ __forceinline__ uint32_t selected_from(const GiFrameBuffers &gb, uint
 	return domain < 0 ? pix : (uint32_t)gb.neighbours[(size_t)domain * npix + pix].x;
 }
 
-/* visibility of queued slots; a blocked ray's weight becomes 0.  Round 0:
- * from the pixel's receiver to the neighbour's sample.  Round 1: from the
- * neighbour's receiver to the pixel's selected sample. */
+/* visibility of queued slots, one ray per thread; a blocked ray's weight
+ * becomes 0.  Round 0: from the pixel's receiver to the neighbour's
+ * sample.  Round 1: from the neighbour's receiver to the pixel's selected
+ * sample.  (These rays are short and two per neighbour: writing them out
+ * for the tuned walk cost more than the walk saved.) */
 __global__ void __launch_bounds__(128) gi_visibility_kernel(DeviceScene s, FrameParams fp, GiFrameBuffers gb, int in,
 		int round)
 {
 	const uint32_t *queue = gb.vis_queue[round];
-	for_each_queued(gb.vis_count[round], gb.vis_count + 2 + round, [&](uint32_t i) {
+	uint32_t *n = gi_vis_n(gb, round);
+	for_each_queued(*n, n + (CNT_FETCH_SHADOW - CNT_SHADOW), [&](uint32_t i) {
 		uint32_t slot = queue[i];
 		uint32_t pix = slot % fp.npix;
 		uint32_t idx = (uint32_t)gb.neighbours[slot].x;
@@ -628,7 +649,7 @@ __global__ void __launch_bounds__(128) gi_spatial_resample_kernel(FrameParams fp
 			float jn = gi_jacobian(gn.x, g.x, sel, fp.gi_jmax);
 			float tn = jn > 0.0f ? gi_target(receiver(fp, gb, (uint32_t)nb.x, gn), sel) * jn : 0.0f;
 			gb.weights[slot] = tn;
-			queue_append(gb.vis_queue[1], gb.vis_count + 1, slot, tn > 0.0f);
+			queue_append(gb.vis_queue[1], gi_vis_n(gb, 1), slot, tn > 0.0f);
 		}
 	}
 	gb.selection[pix] = make_float4(r.w, __int_as_float(domain), st.z, target);
@@ -688,8 +709,27 @@ __device__ __forceinline__ void accumulate4(float4 *buf, uint32_t i, float4 v, b
 	}
 }
 
-/* Final shading: emission + direct + f L_o |n.w| W through a visibility ray;
- * the G-buffer becomes the history of the next frame. */
+/* The final shading's visibility rays, from the primary vertex to the
+ * selected sample of each pixel with W > 0 (slot = pixel). */
+__global__ void __launch_bounds__(128) gi_final_rays_kernel(FrameParams fp, GiFrameBuffers gb, int fin)
+{
+	uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+	if (pix >= fp.npix)
+		return;
+	GBuf g = gbuf(gb.position, gb.normal, pix);
+	bool ray = false;
+	if (g.hit) {
+		GiRes R = load_gi(gb.res[fin], pix);
+		if (R.W > 0.0f) {
+			gi_vis_ray(gb, pix, g.x, R.s.xs);
+			ray = true;
+		}
+	}
+	queue_append(gb.vis_queue[0], gi_vis_n(gb, 0), pix, ray);
+}
+
+/* Final shading: emission + direct + f L_o |n.w| W when the visibility ray
+ * is unblocked; the G-buffer becomes the history of the next frame. */
 __global__ void __launch_bounds__(128) gi_final_kernel(DeviceScene s, FrameParams fp, GiFrameBuffers gb,
 		OutputBuffers out, int fin)
 {
@@ -707,8 +747,7 @@ __global__ void __launch_bounds__(128) gi_final_kernel(DeviceScene s, FrameParam
 			f3 D = R.s.xs - g.x;
 			float d = length(D);
 			f3 w = D / d;
-			kgr_hit hh;
-			if (!trace<true>(s, fp.layout, g.x, w, d - KGR_SHADOW_EPS, hh))
+			if (!gb.vis_flag[pix])
 				gi = brdf(h, w) * R.s.Lo * (fabsf(dot(h.n, w)) * R.W);
 		}
 		c = h.mat.emission + mk(dv.x, dv.y, dv.z) + gi;
@@ -727,14 +766,40 @@ __global__ void __launch_bounds__(128) gi_final_kernel(DeviceScene s, FrameParam
 
 } /* namespace */
 
+namespace {
+
+/* The tuned any-hit walk over round q's queue (the slots' rays, or the
+ * paths' shadow rays of the primary vertices), flags per entry. */
+void gi_walk(const DeviceScene &s, const FrameParams &fp, const GiFrameBuffers &gb, float4 *o, float4 *d, int q,
+		cudaStream_t st)
+{
+	PathBuffers vb{};
+	vb.sh_o = o;
+	vb.sh_d = d;
+	vb.shadow_queue = gb.vis_queue[q];
+	vb.counters = gb.vis_count + q * CNT_COUNT;
+	vb.shadow_flags = gb.vis_flag;
+	vb.visits = nullptr;
+	vb.capacity = gb.vis_capacity;
+	pt_shadow_resolve(s, vb, fp.layout, fp.tune, st);
+}
+
+void gi_vis_clear(const GiFrameBuffers &gb, cudaStream_t st)
+{
+	KGR_CUDA(cudaMemsetAsync(gb.vis_count, 0, 2 * CNT_COUNT * sizeof(uint32_t), st));
+}
+
+} /* namespace */
+
 void gi_primary(const DeviceScene &s, const PathBuffers &pb, const FrameParams &fp, const GiFrameBuffers &gb,
 		cudaStream_t st)
 {
 	int grid = (int)((pb.capacity + 127) / 128);
 	int cap = device_sm_count() * 16;
-	KGR_CUDA(cudaMemsetAsync(gb.vis_count, 0, 4 * sizeof(uint32_t), st));
+	gi_vis_clear(gb, st);
 	gi_primary_kernel<<<grid < cap ? grid : cap, 128, 0, st>>>(s, pb, fp, gb);
-	gi_direct_visibility_kernel<<<device_sm_count() * 8, 128, 0, st>>>(s, pb, fp, gb);
+	gi_walk(s, fp, gb, pb.sh_o, pb.sh_d, 0, st);
+	gi_direct_blocked_kernel<<<device_sm_count() * 8, 128, 0, st>>>(gb);
 	KGR_CUDA(cudaGetLastError());
 }
 
@@ -755,8 +820,8 @@ void gi_spatial(const DeviceScene &s, const FrameParams &fp, const GiFrameBuffer
 		int iteration, cudaStream_t st)
 {
 	unsigned grid = (fp.npix + 127) / 128;
+	gi_vis_clear(gb, st);
 	int vis_grid = device_sm_count() * 8;
-	KGR_CUDA(cudaMemsetAsync(gb.vis_count, 0, 4 * sizeof(uint32_t), st));
 	gi_spatial_gather_kernel<<<grid, 128, 0, st>>>(fp, gb, in, out, iteration);
 	gi_visibility_kernel<<<vis_grid, 128, 0, st>>>(s, fp, gb, in, 0);
 	gi_spatial_resample_kernel<<<grid, 128, 0, st>>>(fp, gb, in, iteration);
@@ -768,7 +833,11 @@ void gi_spatial(const DeviceScene &s, const FrameParams &fp, const GiFrameBuffer
 void gi_final(const DeviceScene &s, const FrameParams &fp, const GiFrameBuffers &gb, const OutputBuffers &out,
 		int fin, cudaStream_t st)
 {
-	gi_final_kernel<<<(fp.npix + 127) / 128, 128, 0, st>>>(s, fp, gb, out, fin);
+	unsigned grid = (fp.npix + 127) / 128;
+	gi_vis_clear(gb, st);
+	gi_final_rays_kernel<<<grid, 128, 0, st>>>(fp, gb, fin);
+	gi_walk(s, fp, gb, gb.vis_o, gb.vis_d, 0, st);
+	gi_final_kernel<<<grid, 128, 0, st>>>(s, fp, gb, out, fin);
 	KGR_CUDA(cudaGetLastError());
 }
 

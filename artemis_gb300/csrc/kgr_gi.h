@@ -29,20 +29,32 @@ struct GiFrameBuffers {
 	/* between the launches of a spatial iteration: per pixel {w_sum,
 	 * bits(domain), bits(M sum), target}; per neighbour slot (k-major,
 	 * k * npix + pixel) {neighbour pixel or -1, its M} and its weight; the
-	 * queues of visibility rays (slots) of the two rounds, their counts and
-	 * (entries 2, 3) the visibility kernels' fetch counters */
+	 * queues of visibility rays (slots) of the two rounds and a counter
+	 * array of CNT_COUNT entries per round (the queue count at CNT_SHADOW,
+	 * the any-hit walk's fetch counter at CNT_FETCH_SHADOW) */
 	float4 *selection;
 	int2 *neighbours;
 	float *weights;
 	uint32_t *vis_queue[2];
 	uint32_t *vis_count;
+	/* rays for the tuned any-hit walk ({origin}, {direction, tmax}) of the
+	 * final shading (slot = pixel), and the walk's blocked flag per slot
+	 * (per path for the primary vertices' DI rays); the spatial rounds walk
+	 * one ray per thread and zero a blocked slot's weight instead; vis_capacity slots */
+	float4 *vis_o, *vis_d;
+	uint32_t *vis_flag;
+	uint32_t vis_capacity;
 };
 
 /* Most neighbours a spatial iteration takes (the gi_neighbors option). */
 #define KGR_GI_MAX_NEIGHBORS 16
 /* Kernels one spatial iteration launches (gather, visibility, resample,
- * visibility, finish). */
+ * visibility, finish), the primary vertex (its kernel, the walk of its DI
+ * shadow rays, the blocked direct light) and the final shading (its rays,
+ * the walk, the shading). */
 #define KGR_GI_SPATIAL_LAUNCHES 5
+#define KGR_GI_PRIMARY_LAUNCHES 3
+#define KGR_GI_FINAL_LAUNCHES 3
 
 void gi_primary(const DeviceScene &s, const PathBuffers &pb, const FrameParams &fp, const GiFrameBuffers &gb,
 		cudaStream_t st);

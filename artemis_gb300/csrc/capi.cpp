@@ -1312,6 +1312,7 @@ void render_restir_di(kgr_attachment *att, const kgr_launch_info *info, const kg
 	rb.vis_d = att->di_vis_d.ptr;
 	rb.vis_flag = att->di_vis_flag.ptr;
 	rb.vis_capacity = (uint32_t)att->di_vis_o.count;
+	rb.ray_total = pb.counters + CNT_SHADOW_TOTAL;
 	KGR_REQUIRE(fp.paths <= rb.vis_capacity, KGR_ERR_INTERNAL, "ReSTIR visibility buffers below the path count");
 	int prev = att->prev_index, cur = 1 - prev;
 	uint32_t launches = 0;
@@ -1634,6 +1635,7 @@ void render_restir_gi(kgr_attachment *att, const kgr_launch_info *info, const kg
 	gb.vis_d = att->gi_vis_d.ptr;
 	gb.vis_flag = att->gi_vis_flag.ptr;
 	gb.vis_capacity = (uint32_t)att->gi_vis_o.count;
+	gb.ray_total = pb.counters + CNT_SHADOW_TOTAL;
 	KGR_REQUIRE(fp.paths <= gb.vis_capacity, KGR_ERR_INTERNAL, "GI visibility buffers below the path count");
 	int prev = att->gi_prev, cur = (prev + 1) % 3, tmp = (prev + 2) % 3;
 	uint32_t launches = 0;
@@ -1689,6 +1691,18 @@ void render_restir_gi(kgr_attachment *att, const kgr_launch_info *info, const kg
 }
 
 } /* namespace */
+
+namespace kgr {
+
+void attachment_ray_totals_async(const kgr_attachment *att, uint32_t *dst, cudaStream_t st)
+{
+	static_assert(CNT_SHADOW_TOTAL == CNT_BOUNCE_TOTAL + 1, "the two totals are adjacent");
+	KGR_REQUIRE(att->loaded && att->counters.ptr, KGR_ERR_NOT_LOADED, "attachment is not loaded");
+	KGR_CUDA(cudaMemcpyAsync(dst, att->counters.ptr + CNT_BOUNCE_TOTAL, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+		st));
+}
+
+} /* namespace kgr */
 
 extern "C" {
 

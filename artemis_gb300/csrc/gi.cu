@@ -368,7 +368,7 @@ __global__ void __launch_bounds__(128) gi_primary_kernel(DeviceScene s, PathBuff
 			}
 		}
 		queue_append(pb.queue[1], out_counter, p, cont, pb.counters + CNT_BOUNCE_TOTAL);
-		queue_append(gb.vis_queue[0], gi_vis_n(gb, 0), p, shadow);
+		queue_append(gb.vis_queue[0], gi_vis_n(gb, 0), p, shadow, gb.ray_total);
 	}
 }
 
@@ -560,7 +560,7 @@ __global__ void __launch_bounds__(128) gi_spatial_gather_kernel(FrameParams fp, 
 		}
 		gb.neighbours[slot] = nb;
 		gb.weights[slot] = wn;
-		queue_append(gb.vis_queue[0], gi_vis_n(gb, 0), slot, wn > 0.0f);
+		queue_append(gb.vis_queue[0], gi_vis_n(gb, 0), slot, wn > 0.0f, gb.ray_total);
 	}
 	gb.selection[pix] = make_float4(wC, 0.0f, __int_as_float(Msum), 0.0f);
 }
@@ -649,7 +649,7 @@ __global__ void __launch_bounds__(128) gi_spatial_resample_kernel(FrameParams fp
 			float jn = gi_jacobian(gn.x, g.x, sel, fp.gi_jmax);
 			float tn = jn > 0.0f ? gi_target(receiver(fp, gb, (uint32_t)nb.x, gn), sel) * jn : 0.0f;
 			gb.weights[slot] = tn;
-			queue_append(gb.vis_queue[1], gi_vis_n(gb, 1), slot, tn > 0.0f);
+			queue_append(gb.vis_queue[1], gi_vis_n(gb, 1), slot, tn > 0.0f, gb.ray_total);
 		}
 	}
 	gb.selection[pix] = make_float4(r.w, __int_as_float(domain), st.z, target);
@@ -725,7 +725,7 @@ __global__ void __launch_bounds__(128) gi_final_rays_kernel(FrameParams fp, GiFr
 			ray = true;
 		}
 	}
-	queue_append(gb.vis_queue[0], gi_vis_n(gb, 0), pix, ray);
+	queue_append(gb.vis_queue[0], gi_vis_n(gb, 0), pix, ray, gb.ray_total);
 }
 
 /* Final shading: emission + direct + f L_o |n.w| W when the visibility ray

@@ -44,6 +44,9 @@ struct GiFrameBuffers {
 	float4 *vis_o, *vis_d;
 	uint32_t *vis_flag;
 	uint32_t vis_capacity;
+	/* every queued visibility ray also counts here (the frame's shadow-ray
+	 * total, CNT_SHADOW_TOTAL of the path counters) */
+	uint32_t *ray_total;
 };
 
 /* Most neighbours a spatial iteration takes (the gi_neighbors option). */

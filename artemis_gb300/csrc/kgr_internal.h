@@ -412,6 +412,12 @@ void launch_trace_any(const DeviceScene &s, const float4 *rays, uint32_t n,
 void launch_trace_stats(const DeviceScene &s, const float4 *rays, uint32_t n, int any,
 		unsigned long long *counters, cudaStream_t stream);
 
+/* Enqueue on st a copy of a loaded attachment's ray totals of its last
+ * frame -- bounce rays, then shadow and visibility rays -- into dst (two
+ * uint32 of pinned host memory), as kgr_get_render_stats reads them but
+ * without waiting. */
+void attachment_ray_totals_async(const kgr_attachment *att, uint32_t *dst, cudaStream_t st);
+
 } /* namespace kgr */
 
 #endif

@@ -178,6 +178,9 @@ struct RestirFrameBuffers {
 	float4 *vis_o, *vis_d;
 	uint32_t *vis_flag;
 	uint32_t vis_capacity;
+	/* every queued visibility ray also counts here (the frame's shadow-ray
+	 * total, CNT_SHADOW_TOTAL of the path counters) */
+	uint32_t *ray_total;
 };
 
 /* Most neighbours a ReSTIR DI spatial pass takes (spatial_neighbors). */

@@ -291,7 +291,7 @@ __global__ void __launch_bounds__(128) primary_kernel(DeviceScene s, PathBuffers
 			}
 		}
 		queue_append(pb.queue[1], out_counter, p, cont, pb.counters + CNT_BOUNCE_TOTAL);
-		queue_append(rb.vis_queue[0], vis_n(rb, 0), p, shadow);
+		queue_append(rb.vis_queue[0], vis_n(rb, 0), p, shadow, rb.ray_total);
 	}
 }
 
@@ -398,7 +398,7 @@ __global__ void __launch_bounds__(128) temporal_gather_kernel(DeviceScene s, Fra
 	f3 from = f3_of(out.position[pix]);
 	if (ray)
 		vis_ray(rb, pix, from, cs.point);
-	queue_append(rb.vis_queue[0], vis_n(rb, 0), pix, ray);
+	queue_append(rb.vis_queue[0], vis_n(rb, 0), pix, ray, rb.ray_total);
 	int32_t pM = 0;
 	if (pindex >= 0) {
 		Sample ps;
@@ -410,7 +410,7 @@ __global__ void __launch_bounds__(128) temporal_gather_kernel(DeviceScene s, Fra
 			bool pray = __float_as_uint(t_previous) != 0u;
 			if (pray)
 				vis_ray(rb, fp.npix + pix, from, ps.point);
-			queue_append(rb.vis_queue[0], vis_n(rb, 0), fp.npix + pix, pray);
+			queue_append(rb.vis_queue[0], vis_n(rb, 0), fp.npix + pix, pray, rb.ray_total);
 		}
 	}
 	rb.neighbours[pix] = make_int2(pindex, pM);
@@ -532,7 +532,7 @@ __global__ void __launch_bounds__(128) restir_gather_kernel(DeviceScene s, Frame
 		rb.targets[slot] = t;
 		if (ray)
 			vis_ray(rb, slot, from, ns.point);
-		queue_append(rb.vis_queue[0], vis_n(rb, 0), slot, ray);
+		queue_append(rb.vis_queue[0], vis_n(rb, 0), slot, ray, rb.ray_total);
 	}
 }
 
@@ -590,13 +590,13 @@ __global__ void __launch_bounds__(128) restir_resample_kernel(DeviceScene s, Fra
 		rb.targets[slot] = t;
 		if (t > 0.0f)
 			vis_ray(rb, slot, f3_of(out.position[nb.x]), merged.data.point);
-		queue_append(rb.vis_queue[1], vis_n(rb, 1), slot, t > 0.0f);
+		queue_append(rb.vis_queue[1], vis_n(rb, 1), slot, t > 0.0f, rb.ray_total);
 	}
 	uint32_t lit = (uint32_t)KGR_MAX_NEIGHBORS * fp.npix + pix;
 	rb.targets[lit] = has_light(merged.data) ? 1.0f : 0.0f;
 	if (has_light(merged.data))
 		vis_ray(rb, lit, f3_of(out.position[pix]), merged.data.point);
-	queue_append(rb.vis_queue[1], vis_n(rb, 1), lit, has_light(merged.data));
+	queue_append(rb.vis_queue[1], vis_n(rb, 1), lit, has_light(merged.data), rb.ray_total);
 	store_res(OUT, pix, merged.data, merged.w, 0.0f, merged.M);
 }
 

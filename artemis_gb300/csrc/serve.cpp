@@ -13,13 +13,25 @@
  *               and path settings, then every admitted path-tracer request
  *               with the same ones, oldest first, adds a slice of its
  *               samples (spp_per_tick, or as many as fit the path
- *               capacity).  Two ticks are in flight: the host composes the
- *               next while the GPU runs the current, and requests that
- *               arrive meanwhile join the next tick -- continuous batching.
+ *               capacity).  Up to two ticks are in flight: the host
+ *               composes the next while the GPU runs the current, and
+ *               requests that arrive meanwhile join the next tick --
+ *               continuous batching; behind a tick expected to run longer
+ *               than KGR_SHORT_TICK_MS the next is composed only when it
+ *               ends, so that a request arriving meanwhile can take it.
  *   ReSTIR DI   requests render their frames (temporal and spatial reuse
  *               inside the request, history reset at its start) through a
  *               resident "restir_di" attachment of their resolution, as a
- *               tick of their own on the same stream.
+ *               tick of their own on the same stream; under FAIR a tick
+ *               holds as many frames as cost about a full path-tracer tick,
+ *               by the scene's measured costs.
+ *   costs       every tick is timed by CUDA events on the stream; the ms per
+ *               path-traced path and per ReSTIR DI pixel-frame of each scene
+ *               are kept as exponential averages.
+ *   rays        a tick's rays are counted on the device: camera, bounce and
+ *               shadow rays of the path tracer, and for ReSTIR DI also the
+ *               reuse passes' visibility rays (read after each frame into
+ *               pinned memory).
  *   completion  when a request's last tick is done its image is copied to
  *               the caller's host buffer on a copy stream (directly when the
  *               buffer is pinned, through a pinned staging buffer when it is
@@ -88,9 +100,29 @@ struct TickJob {
 struct Tick {
 	std::vector<TickJob> jobs;
 	int batch_slot = -1; /* the batcher's ring slot, or -1 for a ReSTIR tick */
-	cudaEvent_t ev = nullptr;
+	cudaEvent_t start = nullptr, ev = nullptr; /* timing events before and after the tick's work */
 	kgr_attachment *restir = nullptr;
+	uint32_t scene = 0;
+	uint64_t work = 0;             /* paths (path tracer) or pixel-frames (ReSTIR DI) */
+	double est_ms = 0.0;           /* expected device time by the scene's costs (0: not known yet) */
+	uint32_t *frame_rays = nullptr; /* ReSTIR DI: pinned, bounce and shadow rays of each frame */
+	size_t frame_rays_bytes = 0;
 };
+
+/* What a tick costs on a scene, from the ticks timed so far (exponential
+ * average, 0 until the first): ms per path-traced path and per ReSTIR DI
+ * pixel-frame. */
+struct SceneCost {
+	double pt = 0.0, restir = 0.0;
+};
+
+/* The cost of a ReSTIR DI pixel-frame against a path-traced path assumed
+ * until a scene has had a tick of each kind (about what depth 8 measures). */
+#define KGR_RESTIR_COST_RATIO 4.0
+/* A second tick is composed while one runs only when the running one is
+ * expected to take at most this long: a request that arrives during a long
+ * tick then waits for that tick alone, not for the next one as well. */
+#define KGR_SHORT_TICK_MS 4.0
 
 /* A resident "restir_di" attachment of one resolution; `owner` is the
  * request whose frames it renders (its temporal history is that request's),
@@ -128,6 +160,7 @@ struct kgr_server {
 		kgr_trace_tune tune = {KGR_LAYOUT_FAST, KGR_TRACE_PERSISTENT, 128, 0, 0};
 	};
 	std::vector<SceneTune> scene_tune;
+	std::vector<SceneCost> scene_cost;
 
 	std::mutex mu; /* guards everything callers touch */
 	std::condition_variable cv_done, cv_work;
@@ -144,7 +177,7 @@ struct kgr_server {
 	/* owned by the loop thread */
 	std::vector<Request *> active, copying;
 	std::deque<Tick> inflight;
-	std::vector<cudaEvent_t> event_pool;
+	std::vector<cudaEvent_t> event_pool, timing_pool;
 	std::vector<RestirEntry> restir;
 	std::multimap<size_t, unsigned char *> pinned_pool;
 	std::thread loop;
@@ -159,6 +192,32 @@ struct kgr_server {
 		cudaEvent_t e;
 		KGR_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
 		return e;
+	}
+
+	cudaEvent_t take_timing_event()
+	{
+		if (!timing_pool.empty()) {
+			cudaEvent_t e = timing_pool.back();
+			timing_pool.pop_back();
+			return e;
+		}
+		cudaEvent_t e;
+		KGR_CUDA(cudaEventCreate(&e));
+		return e;
+	}
+
+	/* a tick's events and pinned buffer back to their pools */
+	void release_tick(Tick &t)
+	{
+		if (t.start)
+			timing_pool.push_back(t.start);
+		if (t.ev)
+			timing_pool.push_back(t.ev);
+		t.start = t.ev = nullptr;
+		if (t.frame_rays) {
+			pinned_pool.emplace(t.frame_rays_bytes, reinterpret_cast<unsigned char *>(t.frame_rays));
+			t.frame_rays = nullptr;
+		}
 	}
 
 	unsigned char *take_pinned(size_t bytes, size_t &got)
@@ -230,9 +289,22 @@ struct kgr_server {
 		uint64_t total_paths = 0;
 		for (auto &j : t.jobs)
 			total_paths += (uint64_t)j.r->req.width * j.r->req.height * j.k;
-		/* ReSTIR ticks add no rays: the reuse passes' shadow rays are not
-		 * counted on the device */
 		uint64_t tick_rays = counts[0] + counts[1] + counts[2];
+		if (t.restir && t.frame_rays) {
+			/* camera rays, then the bounce and the shadow and visibility
+			 * rays the attachment counted, frame by frame */
+			uint64_t npix = (uint64_t)t.jobs[0].r->req.width * t.jobs[0].r->req.height;
+			for (uint32_t f = 0; f < t.jobs[0].k; f++)
+				tick_rays += npix + t.frame_rays[2 * f] + t.frame_rays[2 * f + 1];
+		}
+		float ms = 0.0f;
+		if (t.start && t.work && cudaEventElapsedTime(&ms, t.start, t.ev) == cudaSuccess && ms > 0.0f) {
+			SceneCost &c = scene_cost[t.scene];
+			double x = (double)ms / (double)t.work;
+			double &v = t.restir ? c.restir : c.pt;
+			v = v > 0.0 ? 0.7 * v + 0.3 * x : x;
+		}
+		cudaGetLastError();
 		for (auto &j : t.jobs) {
 			Request *r = j.r;
 			/* rays shared out by paths */
@@ -270,7 +342,7 @@ struct kgr_server {
 				finish(r, e.status);
 			}
 		}
-		event_pool.push_back(t.ev);
+		release_tick(t);
 	}
 
 	/* the attachment rendering request r: its own, or a free one of its
@@ -314,8 +386,12 @@ struct kgr_server {
 		uint32_t first = r->scheduled;
 		uint32_t count = q.spp - first;
 		if (cfg.policy == KGR_SCHEDULE_FAIR) {
-			uint64_t fit = cfg.path_capacity / ((uint64_t)q.width * q.height);
-			count = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(count, fit));
+			/* as many frames as cost about what a full path-tracer tick
+			 * costs on this scene, by the ticks timed so far */
+			const SceneCost &c = scene_cost[q.scene];
+			double ratio = (c.pt > 0.0 && c.restir > 0.0) ? c.restir / c.pt : KGR_RESTIR_COST_RATIO;
+			double fit = (double)cfg.path_capacity / ((double)q.width * q.height * ratio);
+			count = (uint32_t)std::max<double>(1.0, std::min<double>((double)count, std::floor(fit)));
 		}
 		if (first == 0)
 			set_opt_int(att, "reset_history", 1, KGR_VALUE_BOOL);
@@ -328,18 +404,35 @@ struct kgr_server {
 		info.buffers.albedo = reinterpret_cast<float *>(r->aov + npix);
 		info.buffers.position = reinterpret_cast<float *>(r->aov + 2 * npix);
 		info.max_depth = (int32_t)q.max_depth;
-		for (uint32_t i = first; i < first + count; i++) {
-			info.frame = q.frame + i;
-			info.accumulate = i > 0;
-			info.samples = (int32_t)i;
-			KGR_REQUIRE(kgr_render(att, &info, scenes[q.scene], stream) == KGR_OK, KGR_ERR_CUDA, kgr_last_error());
+		t.restir = att;
+		t.scene = q.scene;
+		t.work = (uint64_t)npix * count;
+		t.est_ms = (double)t.work * scene_cost[q.scene].restir;
+		try {
+			t.frame_rays =
+				reinterpret_cast<uint32_t *>(take_pinned(2 * sizeof(uint32_t) * count, t.frame_rays_bytes));
+			t.start = take_timing_event();
+			t.ev = take_timing_event();
+			KGR_CUDA(cudaEventRecord(t.start, stream));
+			for (uint32_t i = first; i < first + count; i++) {
+				info.frame = q.frame + i;
+				info.accumulate = i > 0;
+				info.samples = (int32_t)i;
+				KGR_REQUIRE(kgr_render(att, &info, scenes[q.scene], stream) == KGR_OK, KGR_ERR_CUDA,
+					kgr_last_error());
+				attachment_ray_totals_async(att, t.frame_rays + 2 * (i - first), stream);
+			}
+			KGR_CUDA(cudaEventRecord(t.ev, stream));
+		} catch (const Error &) {
+			/* copies into the pinned buffer may still be queued */
+			cudaStreamSynchronize(stream);
+			cudaGetLastError();
+			release_tick(t);
+			throw;
 		}
 		r->scheduled = first + count;
 		r->last_tick = ticks + 1;
 		t.jobs.push_back(TickJob{r, count});
-		t.restir = att;
-		t.ev = take_event();
-		KGR_CUDA(cudaEventRecord(t.ev, stream));
 		note_launch(t);
 		inflight.push_back(std::move(t));
 	}
@@ -555,12 +648,18 @@ struct kgr_server {
 			return true;
 		}
 		try {
+			t.scene = h.scene;
+			t.work = paths;
+			t.est_ms = (double)paths * scene_cost[h.scene].pt;
+			t.start = take_timing_event();
+			t.ev = take_timing_event();
+			KGR_CUDA(cudaEventRecord(t.start, stream));
 			batcher->render(scenes[h.scene], jobs.data(), (uint32_t)jobs.size(), opt, stream);
 			t.batch_slot = batcher->last;
-			t.ev = take_event();
 			KGR_CUDA(cudaEventRecord(t.ev, stream));
 		} catch (const Error &e) {
 			set_last_error(e.what());
+			release_tick(t);
 			for (auto &j : t.jobs)
 				fail_active(j.r, e.status);
 			return true;
@@ -629,7 +728,8 @@ struct kgr_server {
 				}
 				cudaGetLastError(); /* cudaErrorNotReady of the queries */
 				admit();
-				if (inflight.size() < 2 && launch_tick())
+				bool room = inflight.empty() || (inflight.size() == 1 && inflight.back().est_ms <= KGR_SHORT_TICK_MS);
+				if (room && launch_tick())
 					worked = true;
 			} catch (const Error &e) {
 				/* a failed CUDA call in the loop: every request in flight
@@ -639,7 +739,7 @@ struct kgr_server {
 				cudaStreamSynchronize(copy_stream);
 				cudaGetLastError();
 				for (auto &t : inflight)
-					event_pool.push_back(t.ev);
+					release_tick(t);
 				inflight.clear();
 				std::vector<Request *> left = active;
 				left.insert(left.end(), copying.begin(), copying.end());
@@ -665,7 +765,7 @@ struct kgr_server {
 		cudaStreamSynchronize(copy_stream);
 		cudaGetLastError();
 		while (!inflight.empty()) {
-			event_pool.push_back(inflight.front().ev);
+			release_tick(inflight.front());
 			inflight.pop_front();
 		}
 		for (Request *r : copying)
@@ -692,6 +792,8 @@ struct kgr_server {
 		if (batcher)
 			kgr_batcher_destroy(batcher);
 		for (cudaEvent_t e : event_pool)
+			cudaEventDestroy(e);
+		for (cudaEvent_t e : timing_pool)
 			cudaEventDestroy(e);
 		for (auto &p : pinned_pool)
 			cudaFreeHost(p.second);
@@ -748,6 +850,7 @@ kgr_status kgr_server_add_scene(kgr_server *s, const kgr_scene *scene, uint32_t 
 		KGR_REQUIRE(s->scenes.size() < KGR_SERVER_MAX_SCENES, KGR_ERR_INVALID_ARGUMENT, "too many scenes");
 		s->scenes.push_back(scene);
 		s->scene_tune.emplace_back();
+		s->scene_cost.emplace_back();
 		*id = (uint32_t)(s->scenes.size() - 1);
 	});
 }

@@ -717,13 +717,16 @@ def serve_run(args):
     admission by a 120 GB budget.  Phase 1 offers 200 req/s for
     --serve-seconds; phase 2 offers half the request rate phase 1 completed,
     for 10 s.  `mpaths_per_s` counts pixels x spp of every completed request;
-    `mrays_per_s_pt` the camera, bounce and shadow rays of the path-tracer
-    ticks (ReSTIR's reuse passes do not count their shadow rays).  Latency = submission to image in host memory;
+    `mrays_per_s` the camera, bounce and shadow rays of every tick, counted
+    on the device (ReSTIR DI's reuse-pass visibility rays included).  Latency
+    = submission to image in host memory;
     `latency_per_mpath` divides it by the request's paths (pixels x spp),
     which removes the 1700x spread of request sizes; `by_resolution` gives
-    p50/p99 per resolution class.  The server schedules with processor
+    p50/p99 per resolution class; `slowdown` replays every request of the
+    sustainable phase alone on the idle server and divides its latency in
+    the stream by its latency alone.  The server schedules with processor
     sharing (KGR_SCHEDULE_FAIR) and tunes each scene's traversal launch shape
-    before its first tick (the warm-up requests trigger it)."""
+    before its first tick (the warm-up requests of every scene trigger it)."""
     from artemis_gb300 import kgr
 
     t_build = time.perf_counter()
@@ -740,8 +743,10 @@ def serve_run(args):
         return srv.submit(sids[i], w, h, spp, g.eye, g.target, g.fov, out, kind=kind, max_depth=8, frame=frame,
                           russian_roulette=True, rr_start_depth=3)
 
-    # warm-up: every resolution and kind once (ReSTIR attachments, graphs)
-    warm = [submit(0, w, h, 1, k, 0) for (w, h) in SERVE_RES for k in (kgr.REQUEST_PATH_TRACER, kgr.REQUEST_RESTIR_DI)]
+    # warm-up: every scene, resolution and kind once (each scene's launch-shape
+    # tuning, ReSTIR attachments, graphs), so that none of it runs in a phase
+    warm = [submit(i, w, h, 1, k, 0) for i in range(len(gens)) for (w, h) in SERVE_RES
+            for k in (kgr.REQUEST_PATH_TRACER, kgr.REQUEST_RESTIR_DI)]
     for r in warm:
         srv.wait(r, 600000.0)
 
@@ -777,11 +782,12 @@ def serve_run(args):
             a = np.array([x for x, wh in zip(lat, res_of) if wh == (w, h)])
             if len(a):
                 by_res[f"{w}x{h}"] = {"n": len(a), "p50": q(a, 50), "p99": q(a, 99)}
+        phase.last = (arrivals, res)
         return {"offered_rps": rate, "window_s": seconds, "requests": len(arrivals), "completed": len(ok),
                 "failed": len(res) - len(ok), "wall_s": round(wall, 2),
                 "completed_rps": round(len(ok) / wall, 2),
                 "mpaths_per_s": round(float(mpaths.sum()) / wall, 1),
-                "mrays_per_s_pt": round((s1.rays - s0.rays) / wall / 1e6, 1),
+                "mrays_per_s": round((s1.rays - s0.rays) / wall / 1e6, 1),
                 "latency_ms": {"p50": q(lat, 50), "p90": q(lat, 90), "p99": q(lat, 99), "max": q(lat, 100)},
                 "latency_per_mpath_ms": {"p50": q(norm, 50), "p99": q(norm, 99)},
                 "by_resolution": by_res,
@@ -790,6 +796,26 @@ def serve_run(args):
 
     p1 = phase(200.0, args.serve_seconds, 1)
     p2 = phase(max(0.5, 0.5 * p1["completed_rps"]), 10.0, 2)
+    # each request of the sustainable phase again, alone on the idle server:
+    # its latency without other requests, and the slowdown (latency in the
+    # stream / latency alone) that processor sharing keeps even across sizes
+    arrivals, res = phase.last
+    alone, slow, slow_res = [], [], []
+    for k, ((_, sc, w, h, spp, kind), r) in enumerate(zip(arrivals, res)):
+        if r.status != 0:
+            continue
+        a = srv.wait(submit(sc, w, h, spp, kind, k), 1200000.0)
+        if a.status == 0:
+            alone.append(a.latency_ms)
+            slow.append(r.latency_ms / a.latency_ms)
+            slow_res.append((w, h))
+    slow = np.array(slow)
+    qs = lambda a, p: round(float(np.percentile(a, p)), 2) if len(a) else None
+    p2["slowdown"] = {"p50": qs(slow, 50), "p90": qs(slow, 90), "p99": qs(slow, 99), "max": qs(slow, 100),
+                      "alone_latency_ms": {"p50": qs(np.array(alone), 50), "p99": qs(np.array(alone), 99)},
+                      "by_resolution": {f"{w}x{h}": {"p50": qs(a, 50), "p99": qs(a, 99)} for (w, h) in SERVE_RES
+                                        for a in [np.array([x for x, wh in zip(slow, slow_res) if wh == (w, h)])]
+                                        if len(a)}}
     st = srv.stats()
     out = {"scenes": {n: sc.info().triangle_count for n, sc in zip(SERVE_SCENES, scenes)},
            "scene_build_s": round(build_s, 1),

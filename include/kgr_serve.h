@@ -97,8 +97,10 @@ enum { KGR_REQUEST_PATH_TRACER = 0, KGR_REQUEST_RESTIR_DI = 1 };
  * scene of the request served longest ago, its requests share the path
  * capacity equally (a request too large for its share banks the share until
  * a whole sample fits), and capacity left over goes to the requests closest
- * to their next sample; latency then grows with a request's size instead of
- * with the size of the requests queued before it. */
+ * to their next sample; a ReSTIR DI request's tick holds as many frames as
+ * cost about a full path-tracer tick on its scene (by the ticks timed so
+ * far, at least one frame); latency then grows with a request's size
+ * instead of with the size of the requests queued before it. */
 enum { KGR_SCHEDULE_FCFS = 0, KGR_SCHEDULE_FAIR = 1 };
 
 typedef struct kgr_server_config {
@@ -142,7 +144,8 @@ typedef struct kgr_request_result {
 
 typedef struct kgr_server_stats {
 	uint64_t submitted, completed, failed;
-	uint64_t rays;            /* camera + bounce + shadow rays of the path-tracer ticks */
+	uint64_t rays;            /* camera + bounce + shadow rays of every tick, the ReSTIR DI reuse
+	                           * passes' visibility rays included */
 	uint64_t ticks;
 	double busy_ms;           /* wall time from the first submission to the last completion */
 	double latency_p50_ms, latency_p90_ms, latency_p99_ms, latency_max_ms;

@@ -23,9 +23,9 @@ using namespace kgr;
 kgr::PathBuffers kgr_batcher::path_buffers()
 {
 	PathBuffers pb;
-	float4 **fields[14] = {&pb.ray_o, &pb.ray_d, &pb.beta, &pb.L, &pb.seed, &pb.hit, &pb.sh_o, &pb.sh_d,
-		&pb.pend_c, &pb.pend_e, &pb.pend_b, &pb.aov_n, &pb.aov_a, &pb.aov_p};
-	for (int k = 0; k < 14; k++)
+	float4 **fields[KGR_PATH_ARRAYS];
+	path_array_slots(pb, fields);
+	for (int k = 0; k < KGR_PATH_ARRAYS; k++)
 		*fields[k] = f4[k].ptr;
 	pb.queue[0] = queues[0].ptr;
 	pb.queue[1] = queues[1].ptr;

@@ -769,7 +769,7 @@ struct kgr_attachment {
 	std::string option_string; /* storage for get_option strings */
 
 	/* path state */
-	DevBuf<float4> f4[14];
+	DevBuf<float4> f4[KGR_PATH_ARRAYS];
 	DevBuf<uint32_t> queues[3];
 	DevBuf<uint32_t> counters;
 	uint32_t capacity = 0;
@@ -949,9 +949,9 @@ struct kgr_attachment {
 	PathBuffers path_buffers()
 	{
 		PathBuffers pb;
-		float4 **fields[14] = {&pb.ray_o, &pb.ray_d, &pb.beta, &pb.L, &pb.seed, &pb.hit, &pb.sh_o, &pb.sh_d,
-			&pb.pend_c, &pb.pend_e, &pb.pend_b, &pb.aov_n, &pb.aov_a, &pb.aov_p};
-		for (int k = 0; k < 14; k++)
+		float4 **fields[KGR_PATH_ARRAYS];
+		path_array_slots(pb, fields);
+		for (int k = 0; k < KGR_PATH_ARRAYS; k++)
 			*fields[k] = f4[k].ptr;
 		pb.queue[0] = queues[0].ptr;
 		pb.queue[1] = queues[1].ptr;

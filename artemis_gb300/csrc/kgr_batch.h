@@ -59,7 +59,7 @@ struct kgr_batcher {
 	static const int RING = 4;
 	int device = 0;
 	uint32_t capacity = 0, max_jobs = 0;
-	kgr::DevBuf<float4> f4[14];
+	kgr::DevBuf<float4> f4[KGR_PATH_ARRAYS];
 	kgr::DevBuf<uint32_t> queues[3], counters;
 	kgr::DevBuf<unsigned char> table;
 	unsigned char *staging[RING] = {};

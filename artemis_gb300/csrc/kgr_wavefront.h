@@ -36,9 +36,10 @@ struct PathBuffers {
 	float4 *hit;    /* prim bits, t, b1, b2 */
 	float4 *sh_o;   /* shadow ray origin */
 	float4 *sh_d;   /* shadow ray direction, tmax */
-	float4 *pend_c; /* unoccluded NEE contribution xyz, pdf */
-	float4 *pend_e; /* emission xyz */
-	float4 *pend_b; /* throughput before the bounce */
+	/* the path radiance with this vertex's NEE term added as if its shadow
+	 * ray were unblocked; L already holds it added as if blocked (shade
+	 * computes both, the resolve keeps this one when the ray is unblocked) */
+	float4 *pend_c;
 	float4 *aov_n, *aov_a, *aov_p;
 	uint32_t *queue[2];
 	uint32_t *shadow_queue;
@@ -54,6 +55,17 @@ struct PathBuffers {
 	 * ray is its position) */
 	uint32_t *shadow_flags = nullptr;
 };
+
+/* The float4 arrays of the path state, in the order their allocators lay
+ * them out. */
+#define KGR_PATH_ARRAYS 12
+inline void path_array_slots(PathBuffers &pb, float4 **slots[KGR_PATH_ARRAYS])
+{
+	float4 **f[KGR_PATH_ARRAYS] = {&pb.ray_o, &pb.ray_d, &pb.beta, &pb.L, &pb.seed, &pb.hit, &pb.sh_o, &pb.sh_d,
+		&pb.pend_c, &pb.aov_n, &pb.aov_a, &pb.aov_p};
+	for (int k = 0; k < KGR_PATH_ARRAYS; k++)
+		slots[k] = f[k];
+}
 
 /* Stage kinds for the per-launch CUDA-event timing of an attachment. */
 enum StageKind {

@@ -15,7 +15,7 @@
  *  - at most KGR_NOALLOC_MAX_PATHS (65536) paths per call, i.e.
  *    width * height * spp <= 65536 (256x256 at 1 spp, 128x128 at 4 spp);
  *    larger requests fail with KGR_ERR_INVALID_ARGUMENT before any launch;
- *  - the array (about 14.8 MiB) is part of the library image: every GPU the
+ *  - the array (about 12.8 MiB) is part of the library image: every GPU the
  *    library is loaded on holds it until the process exits;
  *  - every call on a device uses the same array, and it keeps the previous
  *    call's contents.  The kernels overwrite every path slot they read and
@@ -39,8 +39,8 @@
 #define KGR_NOALLOC_MAX_PATHS 65536u
 #define KGR_NOALLOC_SLOT_BYTES ((size_t)KGR_NOALLOC_MAX_PATHS * 16u)
 #define KGR_NOALLOC_QUEUE_BYTES ((size_t)KGR_NOALLOC_MAX_PATHS * 4u)
-/* 14 float4 path arrays + 3 uint32 queues + 256 bytes of counters */
-#define KGR_NOALLOC_BYTES (14u * KGR_NOALLOC_SLOT_BYTES + 3u * KGR_NOALLOC_QUEUE_BYTES + 256u)
+/* KGR_PATH_ARRAYS float4 path arrays + 3 uint32 queues + 256 bytes of counters */
+#define KGR_NOALLOC_BYTES ((size_t)KGR_PATH_ARRAYS * KGR_NOALLOC_SLOT_BYTES + 3u * KGR_NOALLOC_QUEUE_BYTES + 256u)
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[KGR_NOALLOC_BYTES];
 
@@ -71,11 +71,11 @@ unsigned char *noalloc_scratch(int device)
 PathBuffers noalloc_buffers(unsigned char *base)
 {
 	PathBuffers pb;
-	float4 **fields[14] = {&pb.ray_o, &pb.ray_d, &pb.beta, &pb.L, &pb.seed, &pb.hit, &pb.sh_o, &pb.sh_d,
-		&pb.pend_c, &pb.pend_e, &pb.pend_b, &pb.aov_n, &pb.aov_a, &pb.aov_p};
-	for (int k = 0; k < 14; k++)
+	float4 **fields[KGR_PATH_ARRAYS];
+	path_array_slots(pb, fields);
+	for (int k = 0; k < KGR_PATH_ARRAYS; k++)
 		*fields[k] = reinterpret_cast<float4 *>(base + (size_t)k * KGR_NOALLOC_SLOT_BYTES);
-	unsigned char *q = base + 14u * KGR_NOALLOC_SLOT_BYTES;
+	unsigned char *q = base + (size_t)KGR_PATH_ARRAYS * KGR_NOALLOC_SLOT_BYTES;
 	pb.queue[0] = reinterpret_cast<uint32_t *>(q);
 	pb.queue[1] = reinterpret_cast<uint32_t *>(q + KGR_NOALLOC_QUEUE_BYTES);
 	pb.shadow_queue = reinterpret_cast<uint32_t *>(q + 2u * KGR_NOALLOC_QUEUE_BYTES);

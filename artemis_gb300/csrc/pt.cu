@@ -131,11 +131,15 @@ struct WavefrontSink {
 		float4 Lv = pb.L[p];
 		pb.L[p] = f4_of(mk(Lv.x, Lv.y, Lv.z) + add, 0.0f);
 	}
+	/* L += beta * (Le + Ld) waits for the shadow ray; nothing else changes
+	 * L before the ray is resolved, so both outcomes are computed here: L
+	 * takes the blocked one, pend_c the unblocked one, and the resolve
+	 * copies pend_c into L when the ray is unblocked. */
 	__device__ __forceinline__ void nee(float4 c, float4 e, float4 b, float4 o, float4 d)
 	{
-		pb.pend_c[p] = c;
-		pb.pend_e[p] = e;
-		pb.pend_b[p] = b;
+		float4 L = pb.L[p];
+		pb.L[p] = nee_add(L, c, e, b, true);
+		pb.pend_c[p] = nee_add(L, c, e, b, false);
 		pb.sh_o[p] = o;
 		pb.sh_d[p] = d;
 		shadow = true;
@@ -242,25 +246,24 @@ __global__ void __launch_bounds__(BLOCK, KGR_MIN_BLOCKS(BLOCK, OCC)) shadow_reso
 			pb.shadow_flags[p] = occ ? 1u : 0u;
 			continue;
 		}
-		float4 c = pb.pend_c[p], e = pb.pend_e[p], be = pb.pend_b[p];
-		f3 contr = occ ? mk(0.0f) : mk(c.x, c.y, c.z);
-		f3 direct = mk(e.x, e.y, e.z) + contr / c.w;
-		float4 Lv = pb.L[p];
-		pb.L[p] = f4_of(mk(Lv.x, Lv.y, Lv.z) + mk(be.x, be.y, be.z) * direct, 0.0f);
+		if (!occ)
+			pb.L[p] = pb.pend_c[p];
 	}
 	if (COUNT)
 		add_visits(pb.visits + 2, cnt);
 }
 
-/* Shadow-ray resolve: Ld = contr / pdf (zero contribution when occluded),
- * L += beta * (Le + Ld) in the order of the recursion. */
+/* Shadow-ray resolve: L holds L + beta * (Le + 0) already (the blocked
+ * outcome, computed at shade); an unblocked ray replaces it with
+ * L + beta * (Le + contr / pdf), computed at shade into pend_c. */
 __device__ __forceinline__ void resolve_shadow(const PathBuffers &pb, uint32_t p, bool occ)
 {
 	if (pb.shadow_flags) {
 		pb.shadow_flags[p] = occ ? 1u : 0u;
 		return;
 	}
-	pb.L[p] = nee_add(pb.L[p], pb.pend_c[p], pb.pend_e[p], pb.pend_b[p], occ);
+	if (!occ)
+		pb.L[p] = pb.pend_c[p];
 }
 
 /* Persistent traversal of the fast or wide layout: each lane takes a new ray

@@ -396,7 +396,7 @@ kgr_status kgr_destroy(kgr_attachment *att);
  * accounting or fail.  The same kernels
  * as the "path_tracer" attachment (fast layout) write one frame into the
  * caller's buffers of info->buffers; the per-path scratch is a fixed array of
- * about 14.8 MiB inside the library, so width * height * spp must be at most
+ * about 12.8 MiB inside the library, so width * height * spp must be at most
  * 65536, and each resolution component a whole number in [1, 65536]
  * (KGR_ERR_INVALID_ARGUMENT otherwise, before anything runs).  All calls on a device share
  * that array: calls that overlap on the GPU race, so order them on one

@@ -6,31 +6,41 @@
  * BF16 or FP16 weights and activations, FP32 accumulation); this kernel is
  * an alternative to its mma.sync inference and computes the same function.
  *
- * One CTA of 128 threads works on tiles of 128 rows (the MMA's M):
+ * A CTA of four warpgroups (512 threads) holds the weights once and runs
+ * four independent chains, one a warpgroup, each walking tiles of 128 rows
+ * (the MMA's M) with its own buffer, barriers and accumulator; two CTAs fit
+ * an SM, so eight tiles move through the network on an SM at once and the
+ * 512 TMEM columns are all in use:
  *   weights        the six layers (B operands, N x K) in shared memory in
  *                  the canonical K-major layout without swizzle: 8 x 8 core
  *                  matrices of 128 contiguous bytes, K neighbours 128 bytes
  *                  apart (leading byte offset), 8-row groups 1024 bytes apart
  *                  (stride byte offset);
- *   activations    two 128 x 64 tiles (A operands) in the K-major layout
- *                  with the 128-byte swizzle: row r at r x 128 bytes, its
- *                  16-byte chunk c at chunk c ^ (r mod 8).  A tile arrives by
- *                  one TMA load (cp.async.bulk.tensor.2d, the tensor map's
- *                  128-byte swizzle writes exactly this layout; rows past the
- *                  end read as zero), and the next tile's load runs while the
- *                  current one goes through the network;
- *   TMEM           a 128-lane x 64-column FP32 accumulator, row i in lane i;
- *   per layer      one thread issues four tcgen05.mma (K = 16 each; the A
- *                  start address advances 32 bytes inside the swizzled row)
- *                  and a tcgen05.commit to an mbarrier; after it every warp
- *                  reads its 32 lanes with tcgen05.ld (32x32b), applies ReLU,
- *                  rounds to half precision and writes the row back into the
- *                  tile, swizzled, as the next layer's A operand.
+ *   activations    one 128 x 64 tile (A operand) a chain in the K-major
+ *                  layout with the 128-byte swizzle: row r at r x 128 bytes,
+ *                  its 16-byte chunk c at chunk c ^ (r mod 8).  A tile
+ *                  arrives by one TMA load (cp.async.bulk.tensor.2d, the
+ *                  tensor map's 128-byte swizzle writes exactly this layout;
+ *                  rows past the end read as zero); the chain's next tile is
+ *                  loaded into the same buffer as soon as the last layer's
+ *                  MMA has read it, while the outputs are read back;
+ *   TMEM           a 128-lane x 64-column FP32 accumulator a chain (columns
+ *                  64 c .. 64 c + 63), row i in lane i; a warp reads lanes
+ *                  32 (warp mod 4) .. +31;
+ *   per layer      one thread of the chain issues four tcgen05.mma (K = 16
+ *                  each; the A start address advances 32 bytes inside the
+ *                  swizzled row) and a tcgen05.commit to the chain's
+ *                  mbarrier; after it every warp of the chain reads its 32
+ *                  lanes with tcgen05.ld (32x32b, two halves of 32 columns),
+ *                  applies ReLU, rounds to half precision and writes the row
+ *                  back into the tile, swizzled, as the next layer's A
+ *                  operand; the chain's 128 threads meet at a named barrier
+ *                  (1 + chain).
  *
  * Every wait on an mbarrier is bounded.  A wait that runs out sets bit 0 of
- * the error word; the block stops at the next layer boundary (the decision
+ * the error word; the chain stops at the next layer boundary (the decision
  * is taken by all its threads together), waits (bounded) for its TMA load in
- * flight, frees its TMEM and returns; the host reads the word with
+ * flight, and the block frees its TMEM and returns; the host reads the word with
  * kgr_mlp_check.  kgr_mlp_test_wait_timeout exercises that path: its launch
  * withholds each block's first load, so the wait on it runs out (after
  * TC_WAIT_TEST_LIMIT polls) before any MMA was issued.
@@ -57,12 +67,14 @@ namespace {
 #define TC_SBO 1024u                /* bytes between 8-row groups (64-wide K) */
 #define TC_LAYER_BYTES 8192u        /* 64 x 64 half-precision weights */
 #define TC_W_BYTES (5u * TC_LAYER_BYTES + 2048u)
+#define TC_CHAINS 4                 /* warpgroups a CTA, each walking tiles of its own */
+#define TC_THREADS (128 * TC_CHAINS)
 #define TC_X_OFF 43008u             /* = TC_W_BYTES, a multiple of 1024 (swizzle atom) */
 #define TC_X_BYTES (TC_ROWS * TC_W * 2u)
-#define TC_BAR_OFF (TC_X_OFF + 2u * TC_X_BYTES)  /* MMA barrier, then one TMA barrier per tile */
-#define TC_SLOT_OFF (TC_BAR_OFF + 24u)
-#define TC_SMEM (TC_SLOT_OFF + 8u)              /* 75,808 bytes: three CTAs fit an SM */
-#define TC_TMEM_COLS 64u
+#define TC_BAR_OFF (TC_X_OFF + TC_CHAINS * TC_X_BYTES)  /* per chain: MMA barrier, TMA barrier */
+#define TC_SLOT_OFF (TC_BAR_OFF + TC_CHAINS * 16u)
+#define TC_SMEM (TC_SLOT_OFF + 8u)  /* 108,616 bytes: two CTAs fit an SM */
+#define TC_TMEM_COLS 256u           /* 64 columns a chain, rounded up to a power of two */
 #define TC_WAIT_LIMIT (1u << 24)    /* mbarrier polls before a wait gives up */
 #define TC_WAIT_TEST_LIMIT (1u << 16) /* the same, in a launch that tests the give-up path */
 
@@ -120,6 +132,26 @@ __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.a
 __device__ __forceinline__ void tc_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
+/* Barrier of one chain's 128 threads (named barrier 1 + chain; 0 is the
+ * CTA's), and the same with an AND over a flag of every thread. */
+__device__ __forceinline__ void chain_sync(int chain)
+{
+	asm volatile("bar.sync %0, 128;" :: "r"(chain + 1) : "memory");
+}
+
+__device__ __forceinline__ bool chain_and(int chain, bool v)
+{
+	uint32_t r;
+	asm volatile(
+		"{\n\t.reg .pred p, q;\n\t"
+		"setp.ne.u32 q, %1, 0;\n\t"
+		"bar.red.and.pred p, %2, 128, q;\n\t"
+		"selp.u32 %0, 1, 0, p;\n\t"
+		"}"
+		: "=r"(r) : "r"((uint32_t)v), "r"(chain + 1) : "memory");
+	return r != 0;
+}
+
 __device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
 {
 	asm volatile(
@@ -169,6 +201,15 @@ __device__ __forceinline__ void tmem_ld64(uint32_t taddr, uint32_t (&v)[64])
 		: "r"(taddr) : "memory");
 }
 
+/* 32 consecutive FP32 columns of this thread's TMEM lane. */
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32])
+{
+	asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+		"{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+		"%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+		: TC_R8(0), TC_R8(8), TC_R8(16), TC_R8(24) : "r"(taddr) : "memory");
+}
+
 /* 16 consecutive FP32 columns of this thread's TMEM lane. */
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16])
 {
@@ -197,7 +238,7 @@ __device__ __forceinline__ uint32_t pack_relu<__half>(uint32_t lo, uint32_t hi)
 }
 
 template <class T>
-__global__ void __launch_bounds__(128) mlp_infer_tc_kernel(const T *__restrict__ wt_g,
+__global__ void __launch_bounds__(TC_THREADS, 2) mlp_infer_tc_kernel(const T *__restrict__ wt_g,
 		const __grid_constant__ CUtensorMap xmap, uint32_t n, float4 *__restrict__ out,
 		const uint32_t *__restrict__ n_dev, uint32_t *__restrict__ err, uint32_t withhold_first)
 {
@@ -208,6 +249,8 @@ __global__ void __launch_bounds__(128) mlp_infer_tc_kernel(const T *__restrict__
 	}
 	extern __shared__ __align__(1024) unsigned char sm[];
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	/* chain = warpgroup; a warp reads the TMEM lanes 32 (warp mod 4) .. +31 */
+	const int chain = warp >> 2, ctid = tid & 127, cwarp = warp & 3;
 	/* the 128-byte swizzle repeats every 1024 bytes; the kernel has no static
 	 * shared memory, so its dynamic block starts on such a boundary.  If it
 	 * did not, report it (bit 1) and do nothing. */
@@ -217,8 +260,7 @@ __global__ void __launch_bounds__(128) mlp_infer_tc_kernel(const T *__restrict__
 		return;
 	}
 	const bool bf16 = std::is_same<T, __nv_bfloat16>::value;
-	const uint32_t bar = smem_addr(sm + TC_BAR_OFF);
-	const uint32_t tbar[2] = {bar + 8u, bar + 16u};
+	const uint32_t mbar = smem_addr(sm + TC_BAR_OFF + 16u * (uint32_t)chain), tbar = mbar + 8u;
 	uint32_t *slot = reinterpret_cast<uint32_t *>(sm + TC_SLOT_OFF);
 	const uint32_t tiles = (n + TC_ROWS - 1) / TC_ROWS;
 
@@ -227,14 +269,15 @@ __global__ void __launch_bounds__(128) mlp_infer_tc_kernel(const T *__restrict__
 		int rows = l == TC_LAYERS - 1 ? TC_OUT : TC_W;
 		const uint4 *src = reinterpret_cast<const uint4 *>(wt_g + (size_t)l * TC_W * TC_W);
 		unsigned char *dst = sm + l * TC_LAYER_BYTES;
-		for (int c = tid; c < rows * 8; c += 128) {
+		for (int c = tid; c < rows * 8; c += TC_THREADS) {
 			uint32_t r = (uint32_t)c >> 3, kb = (uint32_t)c & 7u;
 			*reinterpret_cast<uint4 *>(dst + core_off(r, kb * 8u)) = __ldg(src + c);
 		}
 	}
 	if (tid == 0) {
-		for (int i = 0; i < 3; i++)
-			asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(bar + 8u * i), "r"(1u) : "memory");
+		for (int i = 0; i < 2 * TC_CHAINS; i++)
+			asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_addr(sm + TC_BAR_OFF) + 8u * i),
+				"r"(1u) : "memory");
 		asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 	}
 	if (warp == 0) {
@@ -246,67 +289,73 @@ __global__ void __launch_bounds__(128) mlp_infer_tc_kernel(const T *__restrict__
 	tc_before();
 	__syncthreads();
 	tc_after();
-	const uint32_t tmem = *slot;
-	const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
-	const uint32_t wbase = smem_addr(sm), xbase0 = smem_addr(sm + TC_X_OFF);
+	const uint32_t tmem_base = *slot;
+	const uint32_t tmem = tmem_base + 64u * (uint32_t)chain;
+	const uint32_t lane_addr = tmem + ((uint32_t)(cwarp * 32) << 16);
+	const uint32_t wbase = smem_addr(sm), xbase = smem_addr(sm + TC_X_OFF + (uint32_t)chain * TC_X_BYTES);
+	unsigned char *xs = sm + TC_X_OFF + (uint32_t)chain * TC_X_BYTES;
 	const uint32_t id_hidden = instr_desc(bf16, TC_W, TC_ROWS), id_out = instr_desc(bf16, TC_OUT, TC_ROWS);
 	uint32_t parity = 0;
 	bool ok = true;
-	/* the TMA load issued but not yet waited for: its barrier and parity */
+	/* a TMA load issued and not yet waited for, and its parity */
 	bool pending = false;
-	uint32_t pend_bar = 0, pend_parity = 0;
+	uint32_t pend_parity = 0;
 
-	uint32_t t = blockIdx.x;
-	if (tid == 0 && t < tiles && !withhold_first)
-		tma_tile(&xmap, xbase0, tbar[0], (int)(t * TC_ROWS));
-	for (uint32_t i = 0; ok && t < tiles; i++, t += gridDim.x) {
-		const uint32_t buf = i & 1u;
-		const uint32_t xbase = xbase0 + buf * TC_X_BYTES;
-		unsigned char *xs = sm + TC_X_OFF + buf * TC_X_BYTES;
-		/* start the next tile's load into the other buffer, whose last tile
-		 * is finished (and fenced) */
-		uint32_t tn = t + gridDim.x;
-		if (tid == 0 && tn < tiles)
-			tma_tile(&xmap, xbase0 + (buf ^ 1u) * TC_X_BYTES, tbar[buf ^ 1u], (int)(tn * TC_ROWS));
-		pending = tn < tiles;
-		pend_bar = tbar[buf ^ 1u];
-		pend_parity = ((i + 1u) >> 1) & 1u;
-		bool got = bar_wait(tbar[buf], (i >> 1) & 1u, limit);
-		ok = __syncthreads_and(got) != 0;
+	const uint32_t stride = gridDim.x * TC_CHAINS;
+	uint32_t t = blockIdx.x * TC_CHAINS + (uint32_t)chain;
+	if (ctid == 0 && t < tiles && !withhold_first)
+		tma_tile(&xmap, xbase, tbar, (int)(t * TC_ROWS));
+	pending = t < tiles && !withhold_first;
+	for (uint32_t i = 0; ok && t < tiles; i++, t += stride) {
+		pend_parity = i & 1u;
+		bool got = bar_wait(tbar, i & 1u, limit);
+		ok = chain_and(chain, got);
 		if (!ok)
 			break;
+		pending = false;
 		const uint64_t lo_sw = 2u; /* layout type: 128-byte swizzle */
 		for (int l = 0; l < TC_LAYERS; l++) {
 			const bool last = l == TC_LAYERS - 1;
-			if (tid == 0) {
+			if (ctid == 0) {
 				for (uint32_t kc = 0; kc < 4; kc++)
 					tc_mma(tmem, smem_desc(xbase + kc * 32u, 16u, 1024u, (uint32_t)lo_sw),
 						smem_desc(wbase + l * TC_LAYER_BYTES + kc * 256u, TC_LBO, TC_SBO, 0u),
 						last ? id_out : id_hidden, kc > 0 ? 1u : 0u);
-				tc_commit(bar);
+				tc_commit(mbar);
 			}
-			got = bar_wait(bar, parity, limit);
+			got = bar_wait(mbar, parity, limit);
 			parity ^= 1u;
-			ok = __syncthreads_and(got) != 0;
+			ok = chain_and(chain, got);
 			tc_after();
 			if (!ok)
 				break;
-			uint32_t r = (uint32_t)(warp * 32 + lane);
+			uint32_t r = (uint32_t)(cwarp * 32 + lane);
 			if (!last) {
-				uint32_t v[64];
-				tmem_ld64(lane_addr, v);
-				tmem_wait_ld();
+				/* two halves of 32 columns: two CTAs of 512 threads leave
+				 * 64 registers a thread */
 #pragma unroll
-				for (uint32_t kb = 0; kb < 8; kb++) {
-					uint4 p;
-					p.x = pack_relu<T>(v[8 * kb + 0], v[8 * kb + 1]);
-					p.y = pack_relu<T>(v[8 * kb + 2], v[8 * kb + 3]);
-					p.z = pack_relu<T>(v[8 * kb + 4], v[8 * kb + 5]);
-					p.w = pack_relu<T>(v[8 * kb + 6], v[8 * kb + 7]);
-					*reinterpret_cast<uint4 *>(xs + sw128_off(r, kb)) = p;
+				for (uint32_t h = 0; h < 2; h++) {
+					uint32_t v[32];
+					tmem_ld32(lane_addr + 32u * h, v);
+					tmem_wait_ld();
+#pragma unroll
+					for (uint32_t kb = 0; kb < 4; kb++) {
+						uint4 p;
+						p.x = pack_relu<T>(v[8 * kb + 0], v[8 * kb + 1]);
+						p.y = pack_relu<T>(v[8 * kb + 2], v[8 * kb + 3]);
+						p.z = pack_relu<T>(v[8 * kb + 4], v[8 * kb + 5]);
+						p.w = pack_relu<T>(v[8 * kb + 6], v[8 * kb + 7]);
+						*reinterpret_cast<uint4 *>(xs + sw128_off(r, 4u * h + kb)) = p;
+					}
 				}
 				fence_async_smem();
 			} else {
+				/* the last MMA has read the tile: the next tile's load into
+				 * the same buffer runs while the outputs are read */
+				uint32_t tn = t + stride;
+				if (ctid == 0 && tn < tiles)
+					tma_tile(&xmap, xbase, tbar, (int)(tn * TC_ROWS));
+				pending = tn < tiles;
 				uint32_t v[16];
 				tmem_ld16(lane_addr, v);
 				tmem_wait_ld();
@@ -315,23 +364,23 @@ __global__ void __launch_bounds__(128) mlp_infer_tc_kernel(const T *__restrict__
 					out[row] = make_float4(__uint_as_float(v[0]), __uint_as_float(v[1]), __uint_as_float(v[2]), 0.0f);
 			}
 			tc_before();
-			__syncthreads();
+			chain_sync(chain);
 			tc_after();
 		}
 	}
 	if (!ok) {
-		if (tid == 0)
+		if (ctid == 0)
 			atomicOr(err, 1u);
-		/* the next tile's load may still be in flight: give it its
-		 * (bounded) time before the block exits */
+		/* a load may still be in flight: give it its (bounded) time before
+		 * the block frees its memory */
 		if (pending)
-			bar_wait(pend_bar, pend_parity, limit);
+			bar_wait(tbar, pend_parity, limit);
 	}
 	tc_before();
 	__syncthreads();
 	tc_after();
 	if (warp == 0)
-		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"(TC_TMEM_COLS)
+		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem_base), "r"(TC_TMEM_COLS)
 			: "memory");
 }
 
@@ -747,19 +796,21 @@ void mlp_infer_tc(const MlpParams &mp, const void *x, uint32_t n, float4 *out, u
 		const_cast<void *>(x), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
 		CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
 	KGR_REQUIRE(r == CUDA_SUCCESS, KGR_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
-	/* three CTAs fit an SM (75.8 KB of shared memory, 64 TMEM columns each) */
+	/* two CTAs fit an SM (106 KB of shared memory, 256 TMEM columns and 512
+	 * threads at 64 registers each); a CTA walks TC_CHAINS tiles at a time */
 	long long tiles = ((long long)n + TC_ROWS - 1) / TC_ROWS;
-	long long cap = (long long)device_sm_count() * 3;
-	int grid = (int)(tiles < cap ? tiles : cap);
+	long long blocks = (tiles + TC_CHAINS - 1) / TC_CHAINS;
+	long long cap = (long long)device_sm_count() * 2;
+	int grid = (int)(blocks < cap ? blocks : cap);
 	if (mp.dtype == KGR_MLP_BF16) {
 		static bool once = (set_tc_smem(mlp_infer_tc_kernel<__nv_bfloat16>), true);
 		(void)once;
-		mlp_infer_tc_kernel<__nv_bfloat16><<<grid, 128, TC_SMEM, st>>>(
+		mlp_infer_tc_kernel<__nv_bfloat16><<<grid, TC_THREADS, TC_SMEM, st>>>(
 			static_cast<const __nv_bfloat16 *>(mp.wt), map, n, out, n_dev, err, withhold_first ? 1u : 0u);
 	} else {
 		static bool once = (set_tc_smem(mlp_infer_tc_kernel<__half>), true);
 		(void)once;
-		mlp_infer_tc_kernel<__half><<<grid, 128, TC_SMEM, st>>>(static_cast<const __half *>(mp.wt), map, n, out,
+		mlp_infer_tc_kernel<__half><<<grid, TC_THREADS, TC_SMEM, st>>>(static_cast<const __half *>(mp.wt), map, n, out,
 			n_dev, err, withhold_first ? 1u : 0u);
 	}
 	KGR_CUDA(cudaGetLastError());

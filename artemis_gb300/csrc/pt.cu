@@ -163,13 +163,23 @@ __global__ void __launch_bounds__(128) shade_kernel(DeviceScene s, PathBuffers p
 	const uint32_t *queue = pb.queue[q];
 	uint32_t stride = gridDim.x * blockDim.x;
 	uint32_t iters = (n + stride - 1) / stride;
+	/* the next item's queue entry and hit record are loaded while the
+	 * current one is shaded: two links fewer in its chain of dependent
+	 * loads (queue, hit, triangle, vertices, material, light) */
+	const uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x;
+	uint32_t p_next = i0 < n ? queue[i0] : 0;
+	float4 hv_next = i0 < n ? pb.hit[p_next] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 	for (uint32_t it = 0; it < iters; it++) {
-		uint32_t i = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
+		uint32_t i = it * stride + i0;
 		bool active = i < n;
-		uint32_t p = active ? queue[i] : 0;
+		uint32_t p = p_next;
+		float4 hv = hv_next;
+		if (i + stride < n) {
+			p_next = queue[i + stride];
+			hv_next = pb.hit[p_next];
+		}
 		bool shadow = false, cont = false;
 		if (active) {
-			float4 hv = pb.hit[p];
 			kgr_hit h;
 			h.prim = __float_as_int(hv.x);
 			h.t = hv.y;

@@ -1206,9 +1206,9 @@ void render_pt(kgr_attachment *att, const kgr_launch_info *info, const kgr_scene
 	OutputBuffers out = {reinterpret_cast<float4 *>(info->buffers.color),
 		reinterpret_cast<float4 *>(info->buffers.normal), reinterpret_cast<float4 *>(info->buffers.albedo),
 		reinterpret_cast<float4 *>(info->buffers.position)};
-	/* with an environment map one more bounce is traced: its misses see the
-	 * map, its hits add nothing */
-	const int last = fp.max_depth + (s.has_env ? 1 : 0);
+	/* bounces 0 .. max_depth; a ray past the last vertex would add nothing,
+	 * hit or miss (LOAD_RAYPACKET, amadeus_common.cuh:480-488) */
+	const int last = fp.max_depth;
 	uint32_t launches = 0;
 	prepare_visits(att, st);
 	int m = att->mark(-1, st);
@@ -1329,7 +1329,7 @@ void render_restir_di(kgr_attachment *att, const kgr_launch_info *info, const kg
 	att->mark(STAGE_RESTIR_PRIMARY, st);
 	launches += 2 + KGR_RESTIR_PRIMARY_LAUNCHES; /* generate, closest hit, primary vertex, its shadow rays */
 	/* with an environment map one more bounce is traced for its misses */
-	for (int d = 1; d <= fp.max_depth + (s.has_env ? 1 : 0); d++) {
+	for (int d = 1; d <= fp.max_depth; d++) {
 		int q = d & 1;
 		reset_counters(pb, (1 << (q ^ 1)) | (1 << CNT_SHADOW), st);
 		att->mark(-1, st);

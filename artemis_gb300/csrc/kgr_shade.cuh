@@ -83,10 +83,11 @@ __device__ __forceinline__ void shade_surface(const DeviceScene &s, const FrameP
 		out.nee(f4_of(contr, pdf), f4_of(sh.mat.emission, 0.0f), f4_of(beta, 0.0f), f4_of(sh.x, 0.0f),
 			f4_of(wi, tmax));
 	}
-	/* with an environment map the ray past the last vertex is still cast:
-	 * a hit there adds nothing, a miss adds the map (the reference's miss
-	 * program has no depth test, amadeus_path_tracer.cu:204-220) */
-	int last = fp.max_depth + (s.has_env ? 1 : 0);
+	/* no ray is cast past the last vertex: the reference's closest-hit and
+	 * miss programs both return 0 for a ray at depth > max_depth
+	 * (LOAD_RAYPACKET, amadeus_common.cuh:480-488), so its hit adds nothing
+	 * and its miss does not see the environment map */
+	int last = fp.max_depth;
 	if (depth < last || final_seed) {
 		f3 wi;
 		float pdf = 0.0f;

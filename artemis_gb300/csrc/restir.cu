@@ -280,7 +280,7 @@ __global__ void __launch_bounds__(128) primary_kernel(DeviceScene s, PathBuffers
 						else
 							beta = beta / (1.0f - qq);
 					}
-					if (alive && 0 < fp.max_depth + (s.has_env ? 1 : 0)) {
+					if (alive && 0 < fp.max_depth) {
 						pb.ray_o[p] = f4_of(sh.x, 0.0f);
 						pb.ray_d[p] = f4_of(wi, 1e16f);
 						pb.beta[p] = f4_of(beta, 0.0f);

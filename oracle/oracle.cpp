@@ -920,10 +920,10 @@ PathResult trace_path(Ctx &ctx, const oracle_render_params *p, f3 o, f3 d, f3 &s
 	r.normal = r.albedo = r.position = mk(0.0f);
 	r.hit = false;
 	f3 beta = mk(1.0f);
-	/* with an environment map the ray past the last vertex is cast too: the
-	 * miss program has no depth test, so its miss sees the map, while its
-	 * hit adds nothing */
-	const int last = p->max_depth + (ctx.has_env() ? 1 : 0);
+	/* no ray past the last vertex: the closest-hit and miss programs both
+	 * return 0 for a ray at depth > max_depth (LOAD_RAYPACKET,
+	 * amadeus_common.cuh:480-488), so such a ray adds nothing, hit or miss */
+	const int last = p->max_depth;
 	for (int depth = 0;; depth++) {
 		if (depth > last)
 			break;

@@ -16,9 +16,12 @@
  * BVH builder is pinned against source/bvh.cpp compiled on the host with a
  * glm stand-in (oracle/ref_bvh.cpp), and the threaded walk against the
  * traversal shaders (shaders/rt/modules/bvh.glsl and the modules it uses)
- * compiled as C++ (oracle/ref_glsl.cpp).  The OptiX programs cannot be
- * compiled here (the OptiX runtime is absent); the kernels that restate them
- * are pinned through the helpers above and the walk.
+ * compiled as C++ (oracle/ref_glsl.cpp).  The path tracer is pinned
+ * against the reference's own path-tracer programs
+ * (source/optix/amadeus_path_tracer.cu, amadeus_common.cuh) compiled on the
+ * host with the OptiX device calls stood in for (oracle/ref_pt.cpp).  The
+ * ReSTIR programs are pinned through the helpers above, the walk and the
+ * path tracer they share.
  */
 #ifndef KGR_ORACLE_H_
 #define KGR_ORACLE_H_

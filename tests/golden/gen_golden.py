@@ -1,5 +1,6 @@
-"""Regenerate tests/golden/reference_kat.json, reference_traversal.json and
-reference_bvh.json from the reference's own headers, shaders and builder.
+"""Regenerate tests/golden/reference_kat.json, reference_traversal.json,
+reference_bvh.json and reference_pt.json from the reference's own headers,
+shaders, builder and path-tracer programs.
 
 Builds oracle/_ref/ref_kat and oracle/_ref/ref_color_kat (oracle/Makefile,
 target `ref`), which compile include/cuda/random.cuh, include/cuda/math.cuh,
@@ -11,7 +12,12 @@ C++, runs trace() on two procedural scenes with the oracle's BVHs and stores
 each ray's closest object and distance.  Builds oracle/_ref/ref_bvh, the
 reference's source/bvh.cpp (partition, serialize) compiled on the host, and
 stores the buffer it builds from the triangle boxes of three procedural
-scenes (as a SHA-256) and from small hand-made box sets (in full).  Needs the reference checkout, named by --reference or the
+scenes (as a SHA-256) and from small hand-made box sets (in full).  Builds
+oracle/_ref/ref_pt, the reference's path-tracer programs
+(source/optix/amadeus_path_tracer.cu with amadeus_common.cuh) compiled on
+the host over the oracle's scene and walk, and stores one sample of each
+pixel of small images of two procedural scenes, with and without an
+environment map.  Needs the reference checkout, named by --reference or the
 REFERENCE environment variable; the committed JSON is what the tests read, so
 this script only runs when the vectors are regenerated.
 
@@ -57,6 +63,13 @@ def main():
     with open(os.path.join(HERE, "reference_bvh.json"), "w") as f:
         json.dump(bvh, f, separators=(",", ":"))
     print("wrote", os.path.join(HERE, "reference_bvh.json"), file=sys.stderr)
+    pt = {"cases": [pt_case(*c) for c in PT_CASES],
+          "_generated_by": "tests/golden/gen_golden.py: the reference's __closesthit__ / __miss__ programs "
+                           "(source/optix/amadeus_path_tracer.cu, amadeus_common.cuh) compiled on the host by "
+                           "oracle/ref_pt.cpp"}
+    with open(os.path.join(HERE, "reference_pt.json"), "w") as f:
+        json.dump(pt, f, separators=(",", ":"))
+    print("wrote", os.path.join(HERE, "reference_pt.json"), file=sys.stderr)
 
 
 # (scene, generator seed, builder, max leaf size, camera rays per side, random rays)
@@ -186,6 +199,48 @@ def bvh_box_sets():
     sets.update({"flat": flat, "points": pts, "row": row, "random1000": rnd(1000)})
     return [{"name": k, "boxes": v.view(np.uint32).tolist(), "bvh": reference_bvh(v).view(np.uint32).tolist()}
             for k, v in sets.items()]
+
+
+# (scene, generator seed, width, height, max depth, frame, environment filter or None)
+PT_CASES = [("box4k", 1, 24, 24, 1, 0, None), ("box4k", 1, 24, 24, 3, 1, None), ("box4k", 1, 24, 24, 6, 2, None),
+            ("terrain_s", 1, 24, 24, 0, 0, None), ("terrain_s", 1, 24, 24, 3, 1, None),
+            ("terrain_s", 1, 24, 24, 2, 0, 0), ("terrain_s", 1, 24, 24, 1, 3, 1)]
+
+
+def pt_environment():
+    """A seeded 32 x 16 RGBA environment map (alpha 1), stored in the
+    fixture so that the test does not depend on the generator."""
+    import numpy as np
+    rng = np.random.default_rng(7)
+    env = rng.uniform(0.0, 2.0, (16, 32, 4)).astype(np.float32)
+    env[..., 3] = 1.0
+    return env
+
+
+def pt_case(name, seed, w, h, depth, frame, env_filter):
+    import tempfile
+    import numpy as np
+    cmd = [os.path.join(ROOT, "oracle", "_ref", "ref_pt"), name, str(seed), str(w), str(h), str(depth), str(frame)]
+    case = {"scene": name, "seed": seed, "width": w, "height": h, "max_depth": depth, "frame": frame}
+    path = None
+    if env_filter is not None:
+        env = pt_environment()
+        with tempfile.NamedTemporaryFile(delete=False) as f:
+            f.write(np.array([env.shape[1], env.shape[0]], np.uint32).tobytes() + env.tobytes())
+            path = f.name
+        cmd += [path, str(env_filter)]
+        case["env"] = env.view(np.uint32).ravel().tolist()
+        case["env_shape"] = list(env.shape)
+        case["env_filter"] = env_filter
+    try:
+        out = subprocess.run(cmd, capture_output=True, check=True).stdout
+    finally:
+        if path:
+            os.unlink(path)
+    img = np.frombuffer(out, np.float32)
+    assert len(img) == 3 * w * h
+    case["radiance"] = img.view(np.uint32).tolist()
+    return case
 
 
 if __name__ == "__main__":

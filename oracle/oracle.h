@@ -19,9 +19,9 @@
  * compiled as C++ (oracle/ref_glsl.cpp).  The path tracer is pinned
  * against the reference's own path-tracer programs
  * (source/optix/amadeus_path_tracer.cu, amadeus_common.cuh) compiled on the
- * host with the OptiX device calls stood in for (oracle/ref_pt.cpp).  The
- * ReSTIR programs are pinned through the helpers above, the walk and the
- * path tracer they share.
+ * host with the OptiX device calls stood in for (oracle/ref_pt.cpp), and
+ * ReSTIR DI against source/optix/amadeus_restir.cu compiled the same way
+ * (oracle/ref_restir.cpp).
  */
 #ifndef KGR_ORACLE_H_
 #define KGR_ORACLE_H_

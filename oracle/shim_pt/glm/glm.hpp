@@ -3,7 +3,8 @@
  * host (TEST INFRASTRUCTURE; glm is an empty submodule in the reference
  * checkout).  It restates what glm publishes for the operations those
  * programs and their headers evaluate, in glm's order of operations:
- *   vector +, -, * and / componentwise, with a scalar on either side;
+ *   vector +, -, +=, * and / componentwise, with a scalar on either side;
+ *   isnan and any componentwise;
  *   dot(a, b) = (a.x * b.x + a.y * b.y) + a.z * b.z (the product vector
  *     summed left to right; two components for vec2);
  *   cross(x, y) = (x.y y.z - y.y x.z, x.z y.x - y.z x.x, x.x y.y - y.x x.y);
@@ -60,7 +61,21 @@ struct vec4 {
 	vec4(const vec3 &v, float d) : x(v.x), y(v.y), z(v.z), w(d) {}
 	float &operator[](int i) { return i == 0 ? x : (i == 1 ? y : (i == 2 ? z : w)); }
 	float operator[](int i) const { return i == 0 ? x : (i == 1 ? y : (i == 2 ? z : w)); }
+	vec4 &operator+=(const vec4 &o)
+	{
+		x += o.x;
+		y += o.y;
+		z += o.z;
+		w += o.w;
+		return *this;
+	}
 };
+
+struct bvec4 {
+	bool x, y, z, w;
+};
+inline bvec4 isnan(const vec4 &v) { return bvec4{std::isnan(v.x), std::isnan(v.y), std::isnan(v.z), std::isnan(v.w)}; }
+inline bool any(const bvec4 &b) { return b.x || b.y || b.z || b.w; }
 
 inline vec3::vec3(const vec4 &v) : x(v.x), y(v.y), z(v.z) {}
 

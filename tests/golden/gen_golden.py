@@ -1,6 +1,7 @@
 """Regenerate tests/golden/reference_kat.json, reference_traversal.json,
-reference_bvh.json and reference_pt.json from the reference's own headers,
-shaders, builder and path-tracer programs.
+reference_bvh.json, reference_pt.json and reference_restir.json from the
+reference's own headers, shaders, builder, path-tracer and ReSTIR DI
+programs.
 
 Builds oracle/_ref/ref_kat and oracle/_ref/ref_color_kat (oracle/Makefile,
 target `ref`), which compile include/cuda/random.cuh, include/cuda/math.cuh,
@@ -17,7 +18,10 @@ oracle/_ref/ref_pt, the reference's path-tracer programs
 (source/optix/amadeus_path_tracer.cu with amadeus_common.cuh) compiled on
 the host over the oracle's scene and walk, and stores one sample of each
 pixel of small images of two procedural scenes, with and without an
-environment map.  Needs the reference checkout, named by --reference or the
+environment map.  Builds oracle/_ref/ref_restir, the reference's ReSTIR DI
+programs (source/optix/amadeus_restir.cu) compiled the same way, and stores
+the colour after a few frames of a still camera and the reservoirs the
+next frame would reuse.  Needs the reference checkout, named by --reference or the
 REFERENCE environment variable; the committed JSON is what the tests read, so
 this script only runs when the vectors are regenerated.
 
@@ -70,6 +74,12 @@ def main():
     with open(os.path.join(HERE, "reference_pt.json"), "w") as f:
         json.dump(pt, f, separators=(",", ":"))
     print("wrote", os.path.join(HERE, "reference_pt.json"), file=sys.stderr)
+    restir = {"cases": [restir_case(*c) for c in RESTIR_CASES],
+              "_generated_by": "tests/golden/gen_golden.py: the reference's ReSTIR DI programs "
+                               "(source/optix/amadeus_restir.cu) compiled on the host by oracle/ref_restir.cpp"}
+    with open(os.path.join(HERE, "reference_restir.json"), "w") as f:
+        json.dump(restir, f, separators=(",", ":"))
+    print("wrote", os.path.join(HERE, "reference_restir.json"), file=sys.stderr)
 
 
 # (scene, generator seed, builder, max leaf size, camera rays per side, random rays)
@@ -240,6 +250,41 @@ def pt_case(name, seed, w, h, depth, frame, env_filter):
     img = np.frombuffer(out, np.float32)
     assert len(img) == 3 * w * h
     case["radiance"] = img.view(np.uint32).tolist()
+    return case
+
+
+# (scene, generator seed, width, height, max depth, frames, environment filter or None)
+RESTIR_CASES = [("box4k", 1, 24, 24, 0, 3, None), ("box4k", 1, 24, 24, 2, 3, None),
+                ("terrain_s", 1, 24, 24, 2, 3, None), ("terrain_s", 1, 24, 24, 0, 2, 0),
+                ("terrain_s", 1, 24, 24, 1, 2, 1)]
+
+
+def restir_case(name, seed, w, h, depth, frames, env_filter):
+    import tempfile
+    import numpy as np
+    cmd = [os.path.join(ROOT, "oracle", "_ref", "ref_restir"), name, str(seed), str(w), str(h), str(depth),
+           str(frames)]
+    case = {"scene": name, "seed": seed, "width": w, "height": h, "max_depth": depth, "frames": frames}
+    path = None
+    if env_filter is not None:
+        env = pt_environment()
+        with tempfile.NamedTemporaryFile(delete=False) as f:
+            f.write(np.array([env.shape[1], env.shape[0]], np.uint32).tobytes() + env.tobytes())
+            path = f.name
+        cmd += [path, str(env_filter)]
+        case["env"] = env.view(np.uint32).ravel().tolist()
+        case["env_shape"] = list(env.shape)
+        case["env_filter"] = env_filter
+    try:
+        out = subprocess.run(cmd, capture_output=True, check=True).stdout
+    finally:
+        if path:
+            os.unlink(path)
+    a = np.frombuffer(out, np.float32)
+    n = w * h
+    assert len(a) == frames * n * 4 + n * 6
+    case["color"] = a[(frames - 1) * n * 4:frames * n * 4].view(np.uint32).tolist()
+    case["reservoirs"] = a[frames * n * 4:].view(np.uint32).tolist()
     return case
 
 

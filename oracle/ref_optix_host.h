@@ -238,6 +238,54 @@ inline bool host_load_environment(const char *path, int filter)
 	return ok;
 }
 
+/* quad lights, in the oracle's form and the reference's */
+static std::vector<kgr_quad_light> g_quads;
+static std::vector<kobra::optix::QuadLight> g_quad_lights;
+
+/* Read a quad-light file: uint32 count, then count x 12 float32 {a, ab, ac,
+ * intensity}. */
+inline bool host_load_quads(const char *path)
+{
+	FILE *f = fopen(path, "rb");
+	uint32_t n;
+	if (!f || fread(&n, 4, 1, f) != 1)
+		return false;
+	g_quads.resize(n);
+	bool ok = fread(g_quads.data(), sizeof(kgr_quad_light), n, f) == n;
+	fclose(f);
+	g_quad_lights.resize(n);
+	for (uint32_t i = 0; i < n; i++) {
+		const kgr_quad_light &q = g_quads[i];
+		g_quad_lights[i].a = make_float3(q.a[0], q.a[1], q.a[2]);
+		g_quad_lights[i].ab = make_float3(q.ab[0], q.ab[1], q.ab[2]);
+		g_quad_lights[i].ac = make_float3(q.ac[0], q.ac[1], q.ac[2]);
+		g_quad_lights[i].intensity = make_float3(q.intensity[0], q.intensity[1], q.intensity[2]);
+	}
+	return ok;
+}
+
+/* Options after the positional arguments: --env <file> <filter> (uint32
+ * width, height, then width * height RGBA float32 texels, row 0 first;
+ * filter 0 linear, 1 point) and --quads <file>.  Returns false on a bad
+ * option or file. */
+inline bool host_options(int argc, char **argv, int first)
+{
+	for (int i = first; i < argc; i++) {
+		if (!strcmp(argv[i], "--env") && i + 2 < argc) {
+			if (!host_load_environment(argv[i + 1], atoi(argv[i + 2])))
+				return false;
+			i += 2;
+		} else if (!strcmp(argv[i], "--quads") && i + 1 < argc) {
+			if (!host_load_quads(argv[i + 1]))
+				return false;
+			i += 1;
+		} else {
+			return false;
+		}
+	}
+	return true;
+}
+
 inline bool host_scene_build(HostScene &hs, const char *name, uint64_t seed, uint32_t W, uint32_t H)
 {
 	if (oracle_generate_scene(name, seed, &hs.gen) != 0)
@@ -274,6 +322,10 @@ inline bool host_scene_build(HostScene &hs, const char *name, uint64_t seed, uin
 		g_scene.env_width = g_env_w;
 		g_scene.env_height = g_env_h;
 		g_scene.env_filter = g_env_filter;
+	}
+	if (!g_quads.empty()) {
+		g_scene.quads = g_quads.data();
+		g_scene.quad_count = (uint32_t)g_quads.size();
 	}
 
 	hs.vertices.resize(a.vertex_count);

@@ -24,9 +24,8 @@
  * seed is the reference's code.
  *
  * Usage: ref_pt <scene> <seed> <width> <height> <max_depth> <frame>
- *               [<environment file> <filter>]
- * The environment file holds uint32 width, height, then width * height
- * RGBA float32 texels, row 0 first; filter 0 is linear, 1 point.
+ *               [--env <file> <filter>] [--quads <file>]
+ * (oracle/ref_optix_host.h gives the file formats).
  * Output on stdout: width * height * 3 float32 (the radiance of one sample
  * of each pixel, row 0 first).
  */
@@ -113,13 +112,12 @@ static float3 raygen(uint32_t ix, uint32_t iy, uint32_t frame)
 
 int main(int argc, char **argv)
 {
-	if (argc != 7 && argc != 9) {
-		fprintf(stderr, "usage: ref_pt <scene> <seed> <width> <height> <max_depth> <frame> [<env> <filter>]\n");
+	if (argc < 7 || !host_options(argc, argv, 7)) {
+		fprintf(stderr, "usage: ref_pt <scene> <seed> <width> <height> <max_depth> <frame> [--env <file> <filter>] "
+			"[--quads <file>]\n");
 		return 2;
 	}
 	uint32_t W = (uint32_t)atoi(argv[3]), H = (uint32_t)atoi(argv[4]), frame = (uint32_t)atoi(argv[6]);
-	if (argc == 9 && !host_load_environment(argv[7], atoi(argv[8])))
-		return 1;
 	HostScene hs;
 	if (!host_scene_build(hs, argv[1], strtoull(argv[2], nullptr, 10), W, H))
 		return 1;
@@ -129,9 +127,9 @@ int main(int argc, char **argv)
 	parameters.camera.ax_u = glm::vec3(hs.ax_u[0], hs.ax_u[1], hs.ax_u[2]);
 	parameters.camera.ax_v = glm::vec3(hs.ax_v[0], hs.ax_v[1], hs.ax_v[2]);
 	parameters.camera.ax_w = glm::vec3(hs.ax_w[0], hs.ax_w[1], hs.ax_w[2]);
-	parameters.lights.quad_lights = nullptr;
+	parameters.lights.quad_lights = g_quad_lights.data();
 	parameters.lights.tri_lights = hs.tri_lights.data();
-	parameters.lights.quad_count = 0;
+	parameters.lights.quad_count = (int)g_quad_lights.size();
 	parameters.lights.tri_count = (int)hs.tri_lights.size();
 	parameters.materials = hs.materials.data();
 	parameters.has_environment_map = g_env_w != 0;

@@ -34,7 +34,8 @@
  *     oracle's per-frame seed pixel_seed(pixel, frame, 0x9E3779B9).
  *
  * Usage: ref_restir <scene> <seed> <width> <height> <max_depth> <frames>
- *                   [<environment file> <filter>]
+ *                   [--env <file> <filter>] [--quads <file>]
+ * (oracle/ref_optix_host.h gives the file formats).
  * Output on stdout: for each frame the colour buffer after it (width *
  * height RGBA float32, accumulated over the frames, row 0 first); then the
  * reservoirs the next frame would reuse, six float32 a pixel: the selected
@@ -156,13 +157,12 @@ static void each_pixel(uint32_t W, uint32_t H, F f)
 
 int main(int argc, char **argv)
 {
-	if (argc != 7 && argc != 9) {
-		fprintf(stderr, "usage: ref_restir <scene> <seed> <width> <height> <max_depth> <frames> [<env> <filter>]\n");
+	if (argc < 7 || !host_options(argc, argv, 7)) {
+		fprintf(stderr, "usage: ref_restir <scene> <seed> <width> <height> <max_depth> <frames> "
+			"[--env <file> <filter>] [--quads <file>]\n");
 		return 2;
 	}
 	uint32_t W = (uint32_t)atoi(argv[3]), H = (uint32_t)atoi(argv[4]), frames = (uint32_t)atoi(argv[6]);
-	if (argc == 9 && !host_load_environment(argv[7], atoi(argv[8])))
-		return 1;
 	HostScene hs;
 	if (!host_scene_build(hs, argv[1], strtoull(argv[2], nullptr, 10), W, H))
 		return 1;
@@ -180,9 +180,9 @@ int main(int argc, char **argv)
 	parameters.camera.ax_u = glm::vec3(hs.ax_u[0], hs.ax_u[1], hs.ax_u[2]);
 	parameters.camera.ax_v = glm::vec3(hs.ax_v[0], hs.ax_v[1], hs.ax_v[2]);
 	parameters.camera.ax_w = glm::vec3(hs.ax_w[0], hs.ax_w[1], hs.ax_w[2]);
-	parameters.lights.quad_lights = nullptr;
+	parameters.lights.quad_lights = g_quad_lights.data();
 	parameters.lights.tri_lights = hs.tri_lights.data();
-	parameters.lights.quad_count = 0;
+	parameters.lights.quad_count = (int)g_quad_lights.size();
 	parameters.lights.tri_count = (int)hs.tri_lights.size();
 	parameters.buffers.color = color.data();
 	parameters.buffers.normal = normal.data();

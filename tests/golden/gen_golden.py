@@ -211,10 +211,46 @@ def bvh_box_sets():
             for k, v in sets.items()]
 
 
-# (scene, generator seed, width, height, max depth, frame, environment filter or None)
-PT_CASES = [("box4k", 1, 24, 24, 1, 0, None), ("box4k", 1, 24, 24, 3, 1, None), ("box4k", 1, 24, 24, 6, 2, None),
-            ("terrain_s", 1, 24, 24, 0, 0, None), ("terrain_s", 1, 24, 24, 3, 1, None),
-            ("terrain_s", 1, 24, 24, 2, 0, 0), ("terrain_s", 1, 24, 24, 1, 3, 1)]
+# (scene, generator seed, width, height, max depth, frame, environment filter or None, quad lights)
+PT_CASES = [("box4k", 1, 24, 24, 1, 0, None, False), ("box4k", 1, 24, 24, 3, 1, None, False),
+            ("box4k", 1, 24, 24, 6, 2, None, False), ("terrain_s", 1, 24, 24, 0, 0, None, False),
+            ("terrain_s", 1, 24, 24, 3, 1, None, False), ("terrain_s", 1, 24, 24, 2, 0, 0, False),
+            ("terrain_s", 1, 24, 24, 1, 3, 1, False), ("terrain_s", 1, 24, 24, 1, 0, None, True),
+            ("terrain_s", 1, 24, 24, 2, 1, 0, True)]
+
+
+def pt_quads():
+    """Three quad lights {a, ab, ac, intensity} above and beside the
+    terrain."""
+    import numpy as np
+    return np.array([[-1.0, 1.6, -1.0, 0.5, 0, 0, 0, 0, 0.5, 4.0, 3.5, 3.0],
+                     [0.4, 1.5, 0.2, 0.4, 0, 0, 0, 0, 0.6, 2.0, 2.5, 3.0],
+                     [1.5, 0.3, -1.0, 0, 0.3, 0, 0, 0, 0.5, 6.0, 6.0, 6.0]], np.float32)
+
+
+def light_options(case, env_filter, quads, files):
+    """The harness options for an environment map and quad lights, their
+    temporary files, and the fixture entries that describe them."""
+    import tempfile
+    import numpy as np
+    opts = []
+    if env_filter is not None:
+        env = pt_environment()
+        with tempfile.NamedTemporaryFile(delete=False) as f:
+            f.write(np.array([env.shape[1], env.shape[0]], np.uint32).tobytes() + env.tobytes())
+            files.append(f.name)
+        opts += ["--env", f.name, str(env_filter)]
+        case["env"] = env.view(np.uint32).ravel().tolist()
+        case["env_shape"] = list(env.shape)
+        case["env_filter"] = env_filter
+    if quads:
+        q = pt_quads()
+        with tempfile.NamedTemporaryFile(delete=False) as f:
+            f.write(np.array([len(q)], np.uint32).tobytes() + q.tobytes())
+            files.append(f.name)
+        opts += ["--quads", f.name]
+        case["quads"] = q.view(np.uint32).ravel().tolist()
+    return opts
 
 
 def pt_environment():
@@ -227,25 +263,16 @@ def pt_environment():
     return env
 
 
-def pt_case(name, seed, w, h, depth, frame, env_filter):
-    import tempfile
+def pt_case(name, seed, w, h, depth, frame, env_filter, quads):
     import numpy as np
     cmd = [os.path.join(ROOT, "oracle", "_ref", "ref_pt"), name, str(seed), str(w), str(h), str(depth), str(frame)]
     case = {"scene": name, "seed": seed, "width": w, "height": h, "max_depth": depth, "frame": frame}
-    path = None
-    if env_filter is not None:
-        env = pt_environment()
-        with tempfile.NamedTemporaryFile(delete=False) as f:
-            f.write(np.array([env.shape[1], env.shape[0]], np.uint32).tobytes() + env.tobytes())
-            path = f.name
-        cmd += [path, str(env_filter)]
-        case["env"] = env.view(np.uint32).ravel().tolist()
-        case["env_shape"] = list(env.shape)
-        case["env_filter"] = env_filter
+    files = []
+    cmd += light_options(case, env_filter, quads, files)
     try:
         out = subprocess.run(cmd, capture_output=True, check=True).stdout
     finally:
-        if path:
+        for path in files:
             os.unlink(path)
     img = np.frombuffer(out, np.float32)
     assert len(img) == 3 * w * h
@@ -253,32 +280,24 @@ def pt_case(name, seed, w, h, depth, frame, env_filter):
     return case
 
 
-# (scene, generator seed, width, height, max depth, frames, environment filter or None)
-RESTIR_CASES = [("box4k", 1, 24, 24, 0, 3, None), ("box4k", 1, 24, 24, 2, 3, None),
-                ("terrain_s", 1, 24, 24, 2, 3, None), ("terrain_s", 1, 24, 24, 0, 2, 0),
-                ("terrain_s", 1, 24, 24, 1, 2, 1)]
+# (scene, generator seed, width, height, max depth, frames, environment filter or None, quad lights)
+RESTIR_CASES = [("box4k", 1, 24, 24, 0, 3, None, False), ("box4k", 1, 24, 24, 2, 3, None, False),
+                ("terrain_s", 1, 24, 24, 2, 3, None, False), ("terrain_s", 1, 24, 24, 0, 2, 0, False),
+                ("terrain_s", 1, 24, 24, 1, 2, 1, False), ("terrain_s", 1, 24, 24, 0, 2, None, True),
+                ("terrain_s", 1, 24, 24, 1, 2, 0, True)]
 
 
-def restir_case(name, seed, w, h, depth, frames, env_filter):
-    import tempfile
+def restir_case(name, seed, w, h, depth, frames, env_filter, quads):
     import numpy as np
     cmd = [os.path.join(ROOT, "oracle", "_ref", "ref_restir"), name, str(seed), str(w), str(h), str(depth),
            str(frames)]
     case = {"scene": name, "seed": seed, "width": w, "height": h, "max_depth": depth, "frames": frames}
-    path = None
-    if env_filter is not None:
-        env = pt_environment()
-        with tempfile.NamedTemporaryFile(delete=False) as f:
-            f.write(np.array([env.shape[1], env.shape[0]], np.uint32).tobytes() + env.tobytes())
-            path = f.name
-        cmd += [path, str(env_filter)]
-        case["env"] = env.view(np.uint32).ravel().tolist()
-        case["env_shape"] = list(env.shape)
-        case["env_filter"] = env_filter
+    files = []
+    cmd += light_options(case, env_filter, quads, files)
     try:
         out = subprocess.run(cmd, capture_output=True, check=True).stdout
     finally:
-        if path:
+        for path in files:
             os.unlink(path)
     a = np.frombuffer(out, np.float32)
     n = w * h

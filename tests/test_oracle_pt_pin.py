@@ -7,11 +7,11 @@ images rendered by the reference's __closesthit__ and __miss__ programs
 include/cuda/brdf.cuh and include/optix/lighting.cuh), compiled unmodified
 on the host by oracle/ref_pt.cpp: the Lambertian box scene and the
 50%-GGX terrain, depths 0 to 6, with and without an environment map
-(linear and point filtering).  The harness finds hits with the oracle's
+(linear and point filtering) and quad lights.  The harness finds hits with the oracle's
 walk and takes each pixel's PCG seed from the pixel index and frame, as the
 benchmark configurations do; everything else -- make_ray, the shading
 normal and position, the material, next-event estimation over the
-triangle lights and the map, the BSDF sample, the recursion with its depth
+triangle and quad lights and the map, the BSDF sample, the recursion with its depth
 test and the miss program -- is the reference's code.
 
 The oracle (oracle_render_pt, Russian roulette off: the reference's
@@ -42,8 +42,11 @@ def oracle_image(case):
     env = None
     if "env" in case:
         env = np.asarray(case["env"], np.uint32).view(np.float32).reshape(case["env_shape"])
-    osc = pyoracle.Scene(g.positions, g.normals, g.tris4(), g.materials_raw, g.lights(), g.sah_bvh(4), env=env,
-                         env_filter=case.get("env_filter", 0))
+    quads = None
+    if "quads" in case:
+        quads = np.asarray(case["quads"], np.uint32).view(np.float32).reshape(-1, 12)
+    osc = pyoracle.Scene(g.positions, g.normals, g.tris4(), g.materials_raw, g.lights(), g.sah_bvh(4), quads=quads,
+                         env=env, env_filter=case.get("env_filter", 0))
     W, H = case["width"], case["height"]
     cam = pyoracle.camera(g.eye, g.target, g.fov, W / H)
     p = pyoracle.render_params(W, H, cam, max_depth=case["max_depth"], spp=1, frame=case["frame"],
@@ -53,7 +56,7 @@ def oracle_image(case):
 
 
 def case_id(c):
-    env = f"-env{c['env_filter']}" if "env" in c else ""
+    env = (f"-env{c['env_filter']}" if "env" in c else "") + ("-quads" if "quads" in c else "")
     return f"{c['scene']}-d{c['max_depth']}-f{c['frame']}{env}"
 
 

@@ -9,7 +9,8 @@ reservoir swaps of include/amadeus/restir.cuh:254-303) compute when
 compiled unmodified on the host by oracle/ref_restir.cpp: the colour after
 two or three frames of a still camera, and the reservoirs the next frame
 would reuse (selected point, w, W, M), on the box scene and the 50%-GGX
-terrain, depths 0 to 2, with and without an environment map.  The harness
+terrain, depths 0 to 2, with and without an environment map and quad
+lights.  The harness
 finds hits with the oracle's walk and takes the pixel's PCG seeds from the
 pixel index and frame (the RIS reservoir's seed, which the reference draws
 from std::random_device at allocation, with the oracle's salt); the rest is
@@ -37,7 +38,7 @@ REL_TOL = 1e-6  # the path part's recursive against running sums
 
 
 def case_id(c):
-    env = f"-env{c['env_filter']}" if "env" in c else ""
+    env = (f"-env{c['env_filter']}" if "env" in c else "") + ("-quads" if "quads" in c else "")
     return f"{c['scene']}-d{c['max_depth']}-{c['frames']}frames{env}"
 
 
@@ -46,8 +47,11 @@ def oracle_run(case):
     env = None
     if "env" in case:
         env = np.asarray(case["env"], np.uint32).view(np.float32).reshape(case["env_shape"])
-    osc = pyoracle.Scene(g.positions, g.normals, g.tris4(), g.materials_raw, g.lights(), g.sah_bvh(4), env=env,
-                         env_filter=case.get("env_filter", 0))
+    quads = None
+    if "quads" in case:
+        quads = np.asarray(case["quads"], np.uint32).view(np.float32).reshape(-1, 12)
+    osc = pyoracle.Scene(g.positions, g.normals, g.tris4(), g.materials_raw, g.lights(), g.sah_bvh(4), quads=quads,
+                         env=env, env_filter=case.get("env_filter", 0))
     W, H = case["width"], case["height"]
     cam = pyoracle.camera(g.eye, g.target, g.fov, W / H)
     n = W * H

@@ -153,63 +153,108 @@ struct WavefrontSink {
 	}
 };
 
-/* One vertex of amadeus_path_tracer.cu:133-201 for every queued path. */
-__global__ void __launch_bounds__(128) shade_kernel(DeviceScene s, PathBuffers pb, FrameParams fp,
+/* One vertex of amadeus_path_tracer.cu:133-201 for path p, whose ray hit
+ * `hv`: the surface, the shading (NEE sample and continuation), then the
+ * appends to the next bounce's queue and the shadow queue.  Every active
+ * lane of the warp calls it (the appends vote over the active lanes). */
+__device__ __forceinline__ void shade_hit(const DeviceScene &s, const PathBuffers &pb, const FrameParams &fp,
+		int depth, int final_seed, uint32_t *next_queue, uint32_t *out_counter, uint32_t p, float4 hv)
+{
+	bool shadow = false, cont = false;
+	kgr_hit h;
+	h.prim = __float_as_int(hv.x);
+	h.t = hv.y;
+	h.b1 = hv.z;
+	h.b2 = hv.w;
+	float4 dv = pb.ray_d[p];
+	SurfaceHit sh;
+	if (surface(s, h, mk(dv.x, dv.y, dv.z), sh)) {
+		WavefrontSink out{pb, p, depth, fp.gi_capture, sh.mat.diffuse};
+		float4 sv = pb.seed[p];
+		f3 seed = mk(sv.x, sv.y, sv.z);
+		float4 bv = pb.beta[p];
+		shade_surface(s, fp, depth, final_seed, sh, mk(bv.x, bv.y, bv.z), seed, out);
+		shadow = out.shadow;
+		cont = out.cont;
+		pb.seed[p] = f4_of(seed, 0.0f);
+	}
+	queue_append(next_queue, out_counter, p, cont, pb.counters + CNT_BOUNCE_TOTAL);
+	queue_append(pb.shadow_queue, pb.counters + CNT_SHADOW, p, shadow, pb.counters + CNT_SHADOW_TOTAL);
+}
+
+/* One vertex for every queued path.  A missed ray ends its path: it only
+ * adds the environment map (__miss__, amadeus_path_tracer.cu:204-220) and
+ * takes no further work, which at the bounces of a scene open to the sky is
+ * about half of the queue.  So each block reads SHADE_BLOCK queue entries at
+ * a time, handles the misses in place and gathers the hits in shared
+ * memory; whenever SHADE_BLOCK hits have gathered, they are shaded one per
+ * thread, so the shading runs in full warps.  The order in which paths are
+ * shaded changes nothing but the order of the next queues: every path's
+ * state is its own. */
+#define SHADE_BLOCK 128
+__global__ void __launch_bounds__(SHADE_BLOCK) shade_kernel(DeviceScene s, PathBuffers pb, FrameParams fp,
 		int depth, int q, int final_seed)
 {
+	__shared__ uint32_t held_p[2 * SHADE_BLOCK];
+	__shared__ float4 held_hit[2 * SHADE_BLOCK];
+	__shared__ uint32_t held;
 	const int qn = q ^ 1;
 	const uint32_t n = pb.counters[q == 0 ? CNT_Q0 : CNT_Q1];
 	uint32_t *out_counter = pb.counters + (qn == 0 ? CNT_Q0 : CNT_Q1);
+	uint32_t *next_queue = pb.queue[qn];
 	const uint32_t *queue = pb.queue[q];
-	uint32_t stride = gridDim.x * blockDim.x;
-	uint32_t iters = (n + stride - 1) / stride;
-	/* the next item's queue entry and hit record are loaded while the
-	 * current one is shaded: two links fewer in its chain of dependent
-	 * loads (queue, hit, triangle, vertices, material, light) */
-	const uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x;
-	uint32_t p_next = i0 < n ? queue[i0] : 0;
-	float4 hv_next = i0 < n ? pb.hit[p_next] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-	for (uint32_t it = 0; it < iters; it++) {
-		uint32_t i = it * stride + i0;
-		bool active = i < n;
-		uint32_t p = p_next;
-		float4 hv = hv_next;
-		if (i + stride < n) {
-			p_next = queue[i + stride];
-			hv_next = pb.hit[p_next];
-		}
-		bool shadow = false, cont = false;
-		if (active) {
-			kgr_hit h;
-			h.prim = __float_as_int(hv.x);
-			h.t = hv.y;
-			h.b1 = hv.z;
-			h.b2 = hv.w;
-			float4 dv = pb.ray_d[p];
-			f3 dir = mk(dv.x, dv.y, dv.z);
-			SurfaceHit sh;
-			if (h.prim < 0) {
-				/* __miss__ (amadeus_path_tracer.cu:204-220): the environment
-				 * map along the ray, weighted by the path throughput */
-				if (s.has_env) {
-					float4 bv = pb.beta[p], Lv = pb.L[p];
-					f3 add = mk(bv.x, bv.y, bv.z) * env_miss(s, dir);
-					pb.L[p] = f4_of(mk(Lv.x, Lv.y, Lv.z) + add, 0.0f);
-				}
-			} else if (depth <= fp.max_depth && surface(s, h, dir, sh)) {
-				WavefrontSink out{pb, p, depth, fp.gi_capture, sh.mat.diffuse};
-				float4 sv = pb.seed[p];
-				f3 seed = mk(sv.x, sv.y, sv.z);
-				float4 bv = pb.beta[p];
-				shade_surface(s, fp, depth, final_seed, sh, mk(bv.x, bv.y, bv.z), seed, out);
-				shadow = out.shadow;
-				cont = out.cont;
-				pb.seed[p] = f4_of(seed, 0.0f);
+	const uint32_t stride = gridDim.x * SHADE_BLOCK;
+	const int lane = threadIdx.x & 31;
+	if (threadIdx.x == 0)
+		held = 0;
+	__syncthreads();
+	/* `base` is the same for every thread of the block, so all of them take
+	 * the same number of iterations and reach every barrier */
+	for (uint32_t base = blockIdx.x * SHADE_BLOCK; base < n; base += stride) {
+		uint32_t i = base + threadIdx.x;
+		bool hit = false;
+		uint32_t p = 0;
+		float4 hv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+		if (i < n) {
+			p = queue[i];
+			hv = pb.hit[p];
+			if (__float_as_int(hv.x) >= 0) {
+				hit = depth <= fp.max_depth;
+			} else if (s.has_env) {
+				/* the environment map along the ray, weighted by the path
+				 * throughput */
+				float4 dv = pb.ray_d[p], bv = pb.beta[p], Lv = pb.L[p];
+				f3 add = mk(bv.x, bv.y, bv.z) * env_miss(s, mk(dv.x, dv.y, dv.z));
+				pb.L[p] = f4_of(mk(Lv.x, Lv.y, Lv.z) + add, 0.0f);
 			}
 		}
-		queue_append(pb.queue[qn], out_counter, p, cont, pb.counters + CNT_BOUNCE_TOTAL);
-		queue_append(pb.shadow_queue, pb.counters + CNT_SHADOW, p, shadow, pb.counters + CNT_SHADOW_TOTAL);
+		/* gather the hits: one shared-memory atomic a warp; `held` stays
+		 * below SHADE_BLOCK between iterations, so the slots fit */
+		unsigned ballot = __ballot_sync(0xffffffffu, hit);
+		uint32_t slot = 0;
+		if (lane == 0 && ballot)
+			slot = atomicAdd(&held, (uint32_t)__popc(ballot));
+		slot = __shfl_sync(0xffffffffu, slot, 0) + __popc(ballot & ((1u << lane) - 1u));
+		if (hit) {
+			held_p[slot] = p;
+			held_hit[slot] = hv;
+		}
+		__syncthreads();
+		const uint32_t c = held;
+		__syncthreads();
+		if (c >= SHADE_BLOCK) {
+			const uint32_t k = c - SHADE_BLOCK + threadIdx.x;
+			shade_hit(s, pb, fp, depth, final_seed, next_queue, out_counter, held_p[k], held_hit[k]);
+			if (threadIdx.x == 0)
+				held = c - SHADE_BLOCK;
+			__syncthreads();
+		}
 	}
+	/* the hits left over: fewer than SHADE_BLOCK */
+	const uint32_t c = held;
+	if (threadIdx.x < c)
+		shade_hit(s, pb, fp, depth, final_seed, next_queue, out_counter, held_p[threadIdx.x],
+			held_hit[threadIdx.x]);
 }
 
 /* is_occluded for every queued shadow ray, then Ld = contr / pdf and
@@ -596,16 +641,16 @@ void pt_trace_closest(const DeviceScene &s, const PathBuffers &pb, int q, int la
 void pt_shade(const DeviceScene &s, const PathBuffers &pb, const FrameParams &fp, int depth, int q,
 		cudaStream_t st)
 {
-	int grid = grid_for(pb.capacity, 128);
-	shade_kernel<<<grid, 128, 0, st>>>(s, pb, fp, depth, q, 0);
+	int grid = grid_for(pb.capacity, SHADE_BLOCK);
+	shade_kernel<<<grid, SHADE_BLOCK, 0, st>>>(s, pb, fp, depth, q, 0);
 	KGR_CUDA(cudaGetLastError());
 }
 
 void pt_shade_final_seed(const DeviceScene &s, const PathBuffers &pb, const FrameParams &fp, int depth,
 		int q, cudaStream_t st)
 {
-	int grid = grid_for(pb.capacity, 128);
-	shade_kernel<<<grid, 128, 0, st>>>(s, pb, fp, depth, q, 1);
+	int grid = grid_for(pb.capacity, SHADE_BLOCK);
+	shade_kernel<<<grid, SHADE_BLOCK, 0, st>>>(s, pb, fp, depth, q, 1);
 	KGR_CUDA(cudaGetLastError());
 }
 

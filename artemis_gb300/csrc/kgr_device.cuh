@@ -1195,6 +1195,65 @@ __device__ __forceinline__ void for_each_queued(uint32_t n, uint32_t *fetch, F f
 	}
 }
 
+/* Visit entries 0..n-1 of a ray queue, grid-stride, and run the heavy work
+ * of the entries whose ray hit in full warps.  A missed ray ends its path
+ * and needs at most an environment lookup, and on a scene open to the sky a
+ * third of the camera rays and about half of each bounce's rays miss, so
+ * one path a thread leaves that share of a warp's lanes idle through the
+ * shading.  Here each block reads BLOCK entries at a time: look(i, hv)
+ * returns entry i's path (hv: its hit record), does what a miss needs in
+ * place and sets `heavy` for an entry that needs work(p, hv).  Those are
+ * gathered in shared memory (one shared atomic a warp) and, whenever BLOCK
+ * of them have gathered, run one per thread; the last fewer than BLOCK run
+ * at the end.  Every thread of a block of BLOCK threads calls it with the
+ * same n.  Entries reach `work` in another order than the queue's, which
+ * changes only the order of the queues that work appends to. */
+template <int BLOCK, class Look, class Work>
+__device__ __forceinline__ void for_each_hit(uint32_t n, Look look, Work work)
+{
+	__shared__ uint32_t held_p[2 * BLOCK];
+	__shared__ float4 held_hit[2 * BLOCK];
+	__shared__ uint32_t held;
+	const uint32_t stride = gridDim.x * BLOCK;
+	const int lane = threadIdx.x & 31;
+	if (threadIdx.x == 0)
+		held = 0;
+	__syncthreads();
+	/* `base` is the same for every thread of the block, so all of them take
+	 * the same number of iterations and reach every barrier */
+	for (uint32_t base = blockIdx.x * BLOCK; base < n; base += stride) {
+		uint32_t i = base + threadIdx.x;
+		bool heavy = false;
+		uint32_t p = 0;
+		float4 hv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+		if (i < n)
+			p = look(i, hv, heavy);
+		/* `held` is below BLOCK between iterations, so the slots fit */
+		unsigned ballot = __ballot_sync(0xffffffffu, heavy);
+		uint32_t slot = 0;
+		if (lane == 0 && ballot)
+			slot = atomicAdd(&held, (uint32_t)__popc(ballot));
+		slot = __shfl_sync(0xffffffffu, slot, 0) + __popc(ballot & ((1u << lane) - 1u));
+		if (heavy) {
+			held_p[slot] = p;
+			held_hit[slot] = hv;
+		}
+		__syncthreads();
+		const uint32_t c = held;
+		__syncthreads();
+		if (c >= BLOCK) {
+			const uint32_t k = c - BLOCK + threadIdx.x;
+			work(held_p[k], held_hit[k]);
+			if (threadIdx.x == 0)
+				held = c - BLOCK;
+			__syncthreads();
+		}
+	}
+	const uint32_t c = held;
+	if (threadIdx.x < c)
+		work(held_p[threadIdx.x], held_hit[threadIdx.x]);
+}
+
 } /* namespace kgr */
 
 #endif

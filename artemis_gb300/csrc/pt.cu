@@ -182,44 +182,25 @@ __device__ __forceinline__ void shade_hit(const DeviceScene &s, const PathBuffer
 	queue_append(pb.shadow_queue, pb.counters + CNT_SHADOW, p, shadow, pb.counters + CNT_SHADOW_TOTAL);
 }
 
-/* One vertex for every queued path.  A missed ray ends its path: it only
- * adds the environment map (__miss__, amadeus_path_tracer.cu:204-220) and
- * takes no further work, which at the bounces of a scene open to the sky is
- * about half of the queue.  So each block reads SHADE_BLOCK queue entries at
- * a time, handles the misses in place and gathers the hits in shared
- * memory; whenever SHADE_BLOCK hits have gathered, they are shaded one per
- * thread, so the shading runs in full warps.  The order in which paths are
- * shaded changes nothing but the order of the next queues: every path's
- * state is its own. */
+/* One vertex of amadeus_path_tracer.cu:133-201 for every queued path: a
+ * miss adds the environment map along the ray (__miss__,
+ * amadeus_path_tracer.cu:204-220) in place; the hits are shaded in full
+ * warps (for_each_hit). */
 #define SHADE_BLOCK 128
 __global__ void __launch_bounds__(SHADE_BLOCK) shade_kernel(DeviceScene s, PathBuffers pb, FrameParams fp,
 		int depth, int q, int final_seed)
 {
-	__shared__ uint32_t held_p[2 * SHADE_BLOCK];
-	__shared__ float4 held_hit[2 * SHADE_BLOCK];
-	__shared__ uint32_t held;
 	const int qn = q ^ 1;
 	const uint32_t n = pb.counters[q == 0 ? CNT_Q0 : CNT_Q1];
 	uint32_t *out_counter = pb.counters + (qn == 0 ? CNT_Q0 : CNT_Q1);
 	uint32_t *next_queue = pb.queue[qn];
 	const uint32_t *queue = pb.queue[q];
-	const uint32_t stride = gridDim.x * SHADE_BLOCK;
-	const int lane = threadIdx.x & 31;
-	if (threadIdx.x == 0)
-		held = 0;
-	__syncthreads();
-	/* `base` is the same for every thread of the block, so all of them take
-	 * the same number of iterations and reach every barrier */
-	for (uint32_t base = blockIdx.x * SHADE_BLOCK; base < n; base += stride) {
-		uint32_t i = base + threadIdx.x;
-		bool hit = false;
-		uint32_t p = 0;
-		float4 hv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-		if (i < n) {
-			p = queue[i];
+	for_each_hit<SHADE_BLOCK>(n,
+		[&](uint32_t i, float4 &hv, bool &heavy) {
+			uint32_t p = queue[i];
 			hv = pb.hit[p];
 			if (__float_as_int(hv.x) >= 0) {
-				hit = depth <= fp.max_depth;
+				heavy = depth <= fp.max_depth;
 			} else if (s.has_env) {
 				/* the environment map along the ray, weighted by the path
 				 * throughput */
@@ -227,34 +208,9 @@ __global__ void __launch_bounds__(SHADE_BLOCK) shade_kernel(DeviceScene s, PathB
 				f3 add = mk(bv.x, bv.y, bv.z) * env_miss(s, mk(dv.x, dv.y, dv.z));
 				pb.L[p] = f4_of(mk(Lv.x, Lv.y, Lv.z) + add, 0.0f);
 			}
-		}
-		/* gather the hits: one shared-memory atomic a warp; `held` stays
-		 * below SHADE_BLOCK between iterations, so the slots fit */
-		unsigned ballot = __ballot_sync(0xffffffffu, hit);
-		uint32_t slot = 0;
-		if (lane == 0 && ballot)
-			slot = atomicAdd(&held, (uint32_t)__popc(ballot));
-		slot = __shfl_sync(0xffffffffu, slot, 0) + __popc(ballot & ((1u << lane) - 1u));
-		if (hit) {
-			held_p[slot] = p;
-			held_hit[slot] = hv;
-		}
-		__syncthreads();
-		const uint32_t c = held;
-		__syncthreads();
-		if (c >= SHADE_BLOCK) {
-			const uint32_t k = c - SHADE_BLOCK + threadIdx.x;
-			shade_hit(s, pb, fp, depth, final_seed, next_queue, out_counter, held_p[k], held_hit[k]);
-			if (threadIdx.x == 0)
-				held = c - SHADE_BLOCK;
-			__syncthreads();
-		}
-	}
-	/* the hits left over: fewer than SHADE_BLOCK */
-	const uint32_t c = held;
-	if (threadIdx.x < c)
-		shade_hit(s, pb, fp, depth, final_seed, next_queue, out_counter, held_p[threadIdx.x],
-			held_hit[threadIdx.x]);
+			return p;
+		},
+		[&](uint32_t p, float4 hv) { shade_hit(s, pb, fp, depth, final_seed, next_queue, out_counter, p, hv); });
 }
 
 /* is_occluded for every queued shadow ray, then Ld = contr / pdf and

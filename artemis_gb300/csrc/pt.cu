@@ -186,7 +186,7 @@ __device__ __forceinline__ void shade_hit(const DeviceScene &s, const PathBuffer
  * miss adds the environment map along the ray (__miss__,
  * amadeus_path_tracer.cu:204-220) in place; the hits are shaded in full
  * warps (for_each_hit). */
-#define SHADE_BLOCK 128
+#define SHADE_BLOCK 256
 __global__ void __launch_bounds__(SHADE_BLOCK) shade_kernel(DeviceScene s, PathBuffers pb, FrameParams fp,
 		int depth, int q, int final_seed)
 {

@@ -132,3 +132,24 @@ def test_restir_di_matches_oracle(box4k, passes, layout, neighbors):
     print(f"ReSTIR colour within 1e-4: {close:.6f}")
     assert close >= 0.999
     assert st.shadow_rays > 0
+
+
+@pytest.mark.parametrize("W,H,spp", [(7, 5, 1), (16, 16, 1), (33, 9, 3)])
+def test_path_tracer_small_and_ragged_queues(W, H, spp):
+    """Queues shorter than one block of the shade kernel (35 paths), exactly
+    one block (256) and ragged ones (891 paths), on the terrain, where a
+    third of the camera rays and about half of each bounce's rays miss: the
+    kernel ends the misses in place and gathers the hits in shared memory,
+    so these sizes take its leftover and partial-chunk paths.  The colour
+    bit for bit against the oracle, the AOVs as in the test above."""
+    g, sc, osc = helpers.both("terrain_s", 1)
+    opts = {"spp": spp, "russian_roulette": True, "rr_start_depth": 2}
+    cam, out, st = render_pt_gpu(g, sc, W, H, opts, frames=1, max_depth=4)
+    ref = [np.zeros((W * H, 4), np.float32) for _ in range(4)]
+    p = helpers.oracle_params(cam, W, H, max_depth=4, spp=spp, frame=0, russian_roulette=1, rr_start_depth=2)
+    pyoracle.render_pt(osc, p, ref)
+    np.testing.assert_array_equal(out[0].view(np.uint32), ref[0].view(np.uint32))
+    for k in (1, 2, 3):
+        assert np.all(rel_ok(out[k], ref[k]), axis=1).mean() >= 0.999
+    assert st.camera_rays == W * H * spp
+    sc.close()
